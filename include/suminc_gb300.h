@@ -1,0 +1,238 @@
+/*
+ * suminc_gb300.h -- C ABI of the GB300 delta-accumulative incremental
+ * PageRank / SSSP workers over a (summarized) graph.
+ *
+ * Conventions
+ *   - Every entry point returns an sg_status; no C++ exception crosses it.
+ *   - Host pointers are caller-owned and copied (or written) before return.
+ *   - Device memory is owned by the context; one CUDA stream per context.
+ *   - A context must not be used by two host threads at once; distinct
+ *     contexts are independent.
+ *   - Vertex ids are dense 0..n-1 ("vid = rank of oid" as in the reference's
+ *     vertex map, grape/vertex_map/global_vertex_map.h:145-166).
+ *
+ * Each declaration names the reference interface it replaces (paths relative
+ * to the SumInc repository).
+ */
+#ifndef SUMINC_GB300_H_
+#define SUMINC_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sg_ctx sg_ctx;
+
+typedef enum sg_status {
+  SG_OK = 0,
+  SG_ERR_INVALID = 1,       /* bad argument, null handle, vertex id >= n   */
+  SG_ERR_CUDA = 2,          /* CUDA runtime error, see sg_last_error()      */
+  SG_ERR_OOM = 3,           /* device or host allocation failed             */
+  SG_ERR_STATE = 4,         /* call out of order (IncEval before PEval ...) */
+  SG_ERR_NOT_CONVERGED = 5, /* round cap reached before the residual test   */
+  SG_ERR_TIMEOUT = 6,       /* a bounded device-side wait gave up           */
+  SG_ERR_UNSUPPORTED = 7
+} sg_status;
+
+/* One line of the reference's update file: "a u v [w]" or "d u v"
+ * (grape/fragment/inc_fragment_builder.h:38-70).  A weight change is a
+ * delete followed by an add of the same pair, as in the reference. */
+typedef enum sg_update_op { SG_UPD_ADD = 0, SG_UPD_DEL = 1 } sg_update_op;
+
+typedef struct sg_update {
+  uint32_t src;
+  uint32_t dst;
+  float weight; /* ignored for unweighted graphs */
+  uint32_t op;  /* sg_update_op */
+} sg_update;
+
+/* Runtime options; the fields mirror the reference's gflags
+ * (examples/analytical_apps/flags.cc:28-70). */
+typedef struct sg_options {
+  double damping;             /* PageRankIngress::d (pagerank_ingress.h:23) */
+  double termcheck_threshold; /* FLAGS_termcheck_threshold: stop when the L1
+                                 residual sum|delta| falls below it          */
+  int32_t max_rounds;         /* per PEval / IncEval round cap (FLAGS_pr_mr) */
+  int32_t compress;           /* FLAGS_compress: run on the summarized graph */
+  int32_t max_node_num;       /* FLAGS_max_node_num (cluster size cap)       */
+  int32_t min_node_num;       /* FLAGS_min_node_num (smallest cluster kept)  */
+  int32_t mirror_k;           /* FLAGS_mirror_k (mirror creation threshold)  */
+  int32_t profile;            /* 1: time every kernel launch with events     */
+  double compress_threshold;  /* FLAGS_compress_threshold (benefit bound)    */
+  double sssp_delta;          /* delta-stepping bucket width, 0 = automatic  */
+  double slack;               /* extra adjacency capacity per vertex (0.125) */
+  int32_t reserved[8];
+} sg_options;
+
+/* Counters of the last PEval / IncEval / batch call. */
+typedef struct sg_stats {
+  int32_t rounds;           /* propagation rounds executed                  */
+  int32_t converged;        /* 1 when the residual test passed              */
+  double residual;          /* last L1 residual (PageRank) or 0             */
+  uint64_t edges_relaxed;   /* edge relaxations performed (GTEPS numerator) */
+  uint64_t vertex_visits;   /* active-vertex visits                          */
+  uint64_t shortcut_edges;  /* shortcut (entry->exit) relaxations            */
+  uint64_t improvements;    /* SSSP distance improvements                    */
+  double elapsed_ms;        /* device time of the call (CUDA events)        */
+  double kernel_ms[8];      /* per-kernel-class device time (profile = 1)   */
+  uint64_t kernel_launches[8];
+  uint64_t live_edges;      /* current edge count                            */
+  uint64_t reset_vertices;  /* SSSP IncEval: vertices reset by deletions     */
+} sg_stats;
+
+/* kernel classes reported in sg_stats.kernel_ms / kernel_launches */
+enum {
+  SG_K_PR_PULL = 0,   /* dense pull round (edge-balanced gather)     */
+  SG_K_PR_PUSH = 1,   /* sparse push round (frontier scatter)        */
+  SG_K_PR_VERTEX = 2, /* vertex update / residual / frontier build   */
+  SG_K_APPLY = 3,     /* delta-graph applier                         */
+  SG_K_SSSP = 4,      /* delta-stepping persistent kernel            */
+  SG_K_SUMMARY = 5,   /* summarized rounds / shortcut precompute     */
+  SG_K_BATCH = 6,     /* batched queries                              */
+  SG_K_ADJOINT = 7    /* transposed delta iteration + gradients      */
+};
+
+/* ---------------------------------------------------------------- context */
+
+/* Fills *opt with the reference's defaults (d = 0.85, threshold 1e-6 as the
+ * SumInc run scripts pass it, max_node_num 150, min_node_num 8, mirror_k 4,
+ * compress_threshold 1). */
+sg_status sg_options_default(sg_options* opt);
+
+/* Creates a context on CUDA device `device`.  Replaces the implicit global
+ * state of the reference's CUDA shim (cudaCode/my_worker.cu:66-122,
+ * tjn::init storing raw pointers in __device__ globals). */
+sg_status sg_ctx_create(int device, const sg_options* opt, sg_ctx** out);
+sg_status sg_ctx_destroy(sg_ctx* ctx);
+
+/* Message of the last failing call on this context (never NULL). */
+const char* sg_last_error(const sg_ctx* ctx);
+
+/* Runs subsequent work of this context on `stream` (a cudaStream_t). */
+sg_status sg_ctx_set_stream(sg_ctx* ctx, void* stream);
+sg_status sg_get_stats(const sg_ctx* ctx, sg_stats* out);
+
+/* ------------------------------------------------------------------ graph */
+
+/* Loads a directed graph from a host CSR: row_ptr[n+1], col[m], optional
+ * weights w[m] (NULL for PageRank's EmptyType edges).  Builds the device
+ * out-CSR and in-CSR with per-vertex slack for in-place updates.  Replaces
+ * LoadGraph + ImmutableEdgecutFragment::Init
+ * (grape/fragment/loader.h, immutable_edgecut_fragment.h:129-377). */
+sg_status sg_graph_load_csr(sg_ctx* ctx, uint32_t n, const uint64_t* row_ptr,
+                            const uint32_t* col, const float* w);
+
+/* Generates a seeded R-MAT graph on the device: 2^scale vertices, exactly
+ * `edges` distinct directed edges, self loops dropped, probabilities a,b,c
+ * (d = 1-a-b-c).  weight_kind: 0 none, 1 integer U[wlo,whi], 2 float
+ * U[wlo,whi].  Same edges as sg_util_rmat_host() for the same arguments. */
+sg_status sg_graph_generate_rmat(sg_ctx* ctx, int scale, uint64_t edges,
+                                 double a, double b, double c, uint64_t seed,
+                                 int weight_kind, double wlo, double whi);
+
+sg_status sg_graph_num_vertices(const sg_ctx* ctx, uint32_t* n);
+sg_status sg_graph_num_edges(const sg_ctx* ctx, uint64_t* m);
+
+/* Copies the current graph to host as a packed CSR with rows sorted by
+ * destination: row_ptr[n+1], col[m], w[m] (w may be NULL). */
+sg_status sg_graph_download_csr(sg_ctx* ctx, uint64_t* row_ptr, uint32_t* col,
+                                float* w);
+
+/* Applies one update batch in place on the device (delete, replace, insert;
+ * per-vertex segments compacted, overflowing segments relocated), and
+ * amends every live application state: PageRank retracts / re-issues the
+ * values of vertices whose out-adjacency changed, SSSP resets the
+ * dependants of deleted tree edges.  Replaces IncFragmentBuilder::Init/Build
+ * (inc_fragment_builder.h:29-133) with AmendValue(-1/+1)
+ * (sum_sync_iter_worker.h:139-180, :214-345) and the reset part of
+ * SumSyncTraversalWorker::deltaCompute (sum_sync_traversal_worker.h:113-261).
+ * Semantics follow the reference: an add of an existing pair replaces it,
+ * duplicate adds keep the first, deletes of absent edges are ignored. */
+sg_status sg_apply_updates(sg_ctx* ctx, uint64_t count, const sg_update* upd);
+
+/* ------------------------------------------------------------- PageRank */
+
+/* Batch evaluation (PEval) of delta-accumulative PageRank from
+ * init_v = 0, init_c = (1-d)/N (pagerank_ingress.h:27-32) to an L1 residual
+ * below termcheck_threshold.  Replaces the batch stage of
+ * SumSyncIterWorker::Query (sum_sync_iter_worker.h:788-1506) and, for the
+ * uncompressed graph, IngressSyncIterWorker::Query
+ * (ingress_sync_iter_worker.h:209-370).  out: host float[n] or NULL. */
+sg_status sg_pr_peval(sg_ctx* ctx, float* out);
+
+/* Incremental evaluation after sg_apply_updates: iterates the amended
+ * deltas to convergence (sum_sync_iter_worker.h:1507-1695). */
+sg_status sg_pr_inceval(sg_ctx* ctx, float* out);
+
+/* Current PageRank values (host float[n]). */
+sg_status sg_pr_values(sg_ctx* ctx, float* out);
+
+/* Residual deltas (host float[n]). */
+sg_status sg_pr_deltas(sg_ctx* ctx, float* out);
+
+/* Device pointer to the values (valid until the next call on ctx). */
+sg_status sg_pr_values_device(sg_ctx* ctx, const float** dptr);
+
+/* ----------------------------------------------------------------- SSSP */
+
+/* Batch SSSP from `source` with FP64 distances over the edge weights
+ * (delta-stepping).  Unreachable vertices read +inf.  Replaces the batch
+ * stage of SumSyncTraversalWorker::Query (sum_sync_traversal_worker.h:543,
+ * :1037-1420) with SSSPIngress (sssp_ingress.h:25-265, weighted branch).
+ * out: host double[n] or NULL. */
+sg_status sg_sssp_peval(sg_ctx* ctx, uint32_t source, double* out);
+
+/* Incremental SSSP after sg_apply_updates: re-seeds the reset vertices from
+ * their in-neighbours and relaxes from every improved vertex
+ * (sum_sync_traversal_worker.h:262-352, :1424-1690). */
+sg_status sg_sssp_inceval(sg_ctx* ctx, double* out);
+
+sg_status sg_sssp_distances(sg_ctx* ctx, double* out);
+
+/* Shortest-path tree parents (host uint32[n]; UINT32_MAX for the source and
+ * unreachable vertices) -- the DependencyData::parent_gid the reference
+ * keeps (grape/utils/dependency_data.h:12-33). */
+sg_status sg_sssp_parents(sg_ctx* ctx, uint32_t* out);
+
+/* ------------------------------------------------------ host utilities
+ * (no GPU needed; used to make inputs identical on every side) */
+
+/* Host twin of sg_graph_generate_rmat: writes row_ptr[2^scale+1], col[edges]
+ * and, when w != NULL and weight_kind != 0, w[edges]. */
+sg_status sg_util_rmat_host(int scale, uint64_t edges, double a, double b,
+                            double c, uint64_t seed, int weight_kind,
+                            double wlo, double whi, uint64_t* row_ptr,
+                            uint32_t* col, float* w);
+
+typedef struct sg_hostgraph sg_hostgraph;
+
+/* A host adjacency mirror used to draw update batches that are valid for the
+ * current graph (inserts of absent pairs, deletes of present edges). */
+sg_status sg_hostgraph_create(uint32_t n, const uint64_t* row_ptr,
+                              const uint32_t* col, const float* w,
+                              sg_hostgraph** out);
+sg_status sg_hostgraph_destroy(sg_hostgraph* g);
+
+/* Draws a batch of n_ins inserts of uniform absent (u,v) pairs, n_del
+ * deletes of uniformly chosen present edges and n_rew weight changes
+ * (emitted as a delete plus an add), applies it to the mirror and writes
+ * n_ins + n_del + 2*n_rew records to out.  New weights are integers
+ * U[wlo,whi] when integer_weights, else float U[wlo,whi]. */
+sg_status sg_hostgraph_gen_updates(sg_hostgraph* g, uint64_t n_ins,
+                                   uint64_t n_del, uint64_t n_rew,
+                                   uint64_t seed, int integer_weights,
+                                   double wlo, double whi, sg_update* out);
+
+/* Packed copy of the mirror (rows sorted). */
+sg_status sg_hostgraph_num_edges(const sg_hostgraph* g, uint64_t* m);
+sg_status sg_hostgraph_csr(const sg_hostgraph* g, uint64_t* row_ptr,
+                           uint32_t* col, float* w);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SUMINC_GB300_H_ */

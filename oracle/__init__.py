@@ -1,0 +1,109 @@
+"""CPU oracle -- test infrastructure only.
+
+Imported by ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg
+of ``bench.py``, and only as the checker.  The product path
+(``suminc_gb300``) never imports it.  ``liboracle.so`` is built from
+``oracle.c`` by ``oracle/build.py``.
+
+Parity pins: the PageRank and SSSP restatements are checked against golden
+vectors produced by the reference's own CPU worker (tests/golden/, see
+make_golden.py there) and against the FP64 solvers in this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+from .updates import apply_updates_reference  # noqa: F401
+
+_lib = None
+
+
+class OrStats(C.Structure):
+    _fields_ = [("rounds", C.c_int32), ("converged", C.c_int32), ("residual", C.c_double),
+                ("edges", C.c_uint64), ("visits", C.c_uint64)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        P = C.c_void_p
+        L.or_ingress_pr.argtypes = [C.c_uint32, P, P, C.c_double, C.c_double, C.c_int, C.c_int,
+                                    C.c_int, P, P, C.POINTER(OrStats)]
+        L.or_ingress_pr.restype = C.c_int
+        L.or_pr_amend.argtypes = [C.c_uint32, P, P, P, P, C.c_double, P, P]
+        L.or_pr_amend.restype = None
+        L.or_pr_fixed_point.argtypes = [C.c_uint32, P, P, P, C.c_double, P, C.c_double, C.c_int, P]
+        L.or_pr_fixed_point.restype = C.c_int
+        L.or_pr_adjoint_solve.argtypes = [C.c_uint32, P, P, P, C.c_double, P, C.c_double, C.c_int, P]
+        L.or_pr_adjoint_solve.restype = C.c_int
+        L.or_dijkstra.argtypes = [C.c_uint32, P, P, P, C.c_uint32, P]
+        L.or_dijkstra.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _csr(rp, col, w=None):
+    rp = np.ascontiguousarray(rp, np.uint64)
+    col = np.ascontiguousarray(col, np.uint32)
+    w = None if w is None else np.ascontiguousarray(w, np.float32)
+    return rp, col, w
+
+
+def ingress_pr(rp, col, damping=0.85, tau=1e-6, x=None, delta=None, max_rounds=100000,
+               threads=0):
+    """Delta PageRank rounds (PEval when x is None, else continue from x/delta)."""
+    rp, col, _ = _csr(rp, col)
+    n = len(rp) - 1
+    init = x is None
+    x = np.zeros(n, np.float32) if init else np.array(x, np.float32, copy=True)
+    delta = np.zeros(n, np.float32) if init else np.array(delta, np.float32, copy=True)
+    st = OrStats()
+    lib().or_ingress_pr(n, _p(rp), _p(col), damping, tau, 1 if init else 0, max_rounds, threads,
+                        _p(x), _p(delta), C.byref(st))
+    return x, delta, {k: getattr(st, k) for k, _ in OrStats._fields_}
+
+
+def pr_amend(old, new, x, delta, damping=0.85):
+    rpo, colo, _ = _csr(*old[:2])
+    rpn, coln, _ = _csr(*new[:2])
+    x = np.ascontiguousarray(x, np.float32)
+    delta = np.array(delta, np.float32, copy=True)
+    lib().or_pr_amend(len(rpo) - 1, _p(rpo), _p(colo), _p(rpn), _p(coln), damping, _p(x),
+                      _p(delta))
+    return delta
+
+
+def pr_fixed_point(rp, col, w=None, damping=0.85, tele=None, tol=1e-12, max_iter=100000):
+    rp, col, w = _csr(rp, col, w)
+    n = len(rp) - 1
+    x = np.zeros(n, np.float64)
+    t = None if tele is None else np.ascontiguousarray(tele, np.float64)
+    lib().or_pr_fixed_point(n, _p(rp), _p(col), _p(w), damping, _p(t), tol, max_iter, _p(x))
+    return x
+
+
+def pr_adjoint_solve(rp, col, w, g, damping=0.85, tol=1e-13, max_iter=100000):
+    rp, col, w = _csr(rp, col, w)
+    n = len(rp) - 1
+    lam = np.zeros(n, np.float64)
+    g = np.ascontiguousarray(g, np.float64)
+    lib().or_pr_adjoint_solve(n, _p(rp), _p(col), _p(w), damping, _p(g), tol, max_iter, _p(lam))
+    return lam
+
+
+def dijkstra(rp, col, w, source=0):
+    rp, col, w = _csr(rp, col, w)
+    n = len(rp) - 1
+    d = np.empty(n, np.float64)
+    lib().or_dijkstra(n, _p(rp), _p(col), _p(w), source, _p(d))
+    return d

@@ -1,0 +1,341 @@
+"""Python binding of libsuminc_gb300 (ctypes over the C ABI in
+``include/suminc_gb300.h``).
+
+The binding only marshals arrays; every computation runs in the CUDA library.
+Importing works without a GPU (host utilities such as the R-MAT twin and the
+update-batch mirror need none); a missing or unbuilt library raises
+``ImportError`` -- there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = [
+    "SgError", "Options", "Stats", "Context", "HostGraph", "UPDATE_DTYPE",
+    "rmat_host", "lib_path", "load_library", "K_NAMES",
+]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def lib_path() -> str:
+    return os.path.join(_HERE, "_build", "libsuminc_gb300.so")
+
+
+class SgError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"sg status {status}: {msg}")
+        self.status = status
+
+
+SG_OK = 0
+SG_ERR_INVALID = 1
+SG_ERR_CUDA = 2
+SG_ERR_OOM = 3
+SG_ERR_STATE = 4
+SG_ERR_NOT_CONVERGED = 5
+SG_ERR_TIMEOUT = 6
+SG_ERR_UNSUPPORTED = 7
+
+SG_UPD_ADD = 0
+SG_UPD_DEL = 1
+
+UPDATE_DTYPE = np.dtype([("src", "<u4"), ("dst", "<u4"), ("weight", "<f4"), ("op", "<u4")])
+
+K_NAMES = ["pr_pull", "pr_push", "pr_vertex", "apply", "sssp", "summary", "batch", "adjoint"]
+
+
+class Options(C.Structure):
+    _fields_ = [
+        ("damping", C.c_double),
+        ("termcheck_threshold", C.c_double),
+        ("max_rounds", C.c_int32),
+        ("compress", C.c_int32),
+        ("max_node_num", C.c_int32),
+        ("min_node_num", C.c_int32),
+        ("mirror_k", C.c_int32),
+        ("profile", C.c_int32),
+        ("compress_threshold", C.c_double),
+        ("sssp_delta", C.c_double),
+        ("slack", C.c_double),
+        ("reserved", C.c_int32 * 8),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("rounds", C.c_int32),
+        ("converged", C.c_int32),
+        ("residual", C.c_double),
+        ("edges_relaxed", C.c_uint64),
+        ("vertex_visits", C.c_uint64),
+        ("shortcut_edges", C.c_uint64),
+        ("improvements", C.c_uint64),
+        ("elapsed_ms", C.c_double),
+        ("kernel_ms", C.c_double * 8),
+        ("kernel_launches", C.c_uint64 * 8),
+        ("live_edges", C.c_uint64),
+        ("reset_vertices", C.c_uint64),
+    ]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("kernel_ms", "kernel_launches")}
+        d["kernel_ms"] = {K_NAMES[i]: self.kernel_ms[i] for i in range(8)}
+        d["kernel_launches"] = {K_NAMES[i]: int(self.kernel_launches[i]) for i in range(8)}
+        return d
+
+
+_P = C.c_void_p
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+_u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+
+_SIGS = {
+    "sg_options_default": ([C.POINTER(Options)], C.c_int),
+    "sg_ctx_create": ([C.c_int, C.POINTER(Options), C.POINTER(_P)], C.c_int),
+    "sg_ctx_destroy": ([_P], C.c_int),
+    "sg_last_error": ([_P], C.c_char_p),
+    "sg_ctx_set_stream": ([_P, _P], C.c_int),
+    "sg_get_stats": ([_P, C.POINTER(Stats)], C.c_int),
+    "sg_graph_load_csr": ([_P, C.c_uint32, _P, _P, _P], C.c_int),
+    "sg_graph_generate_rmat": ([_P, C.c_int, C.c_uint64, C.c_double, C.c_double, C.c_double,
+                                C.c_uint64, C.c_int, C.c_double, C.c_double], C.c_int),
+    "sg_graph_num_vertices": ([_P, C.POINTER(C.c_uint32)], C.c_int),
+    "sg_graph_num_edges": ([_P, C.POINTER(C.c_uint64)], C.c_int),
+    "sg_graph_download_csr": ([_P, _P, _P, _P], C.c_int),
+    "sg_apply_updates": ([_P, C.c_uint64, _P], C.c_int),
+    "sg_pr_peval": ([_P, _P], C.c_int),
+    "sg_pr_inceval": ([_P, _P], C.c_int),
+    "sg_pr_values": ([_P, _P], C.c_int),
+    "sg_pr_deltas": ([_P, _P], C.c_int),
+    "sg_pr_values_device": ([_P, C.POINTER(_P)], C.c_int),
+    "sg_sssp_peval": ([_P, C.c_uint32, _P], C.c_int),
+    "sg_sssp_inceval": ([_P, _P], C.c_int),
+    "sg_sssp_distances": ([_P, _P], C.c_int),
+    "sg_sssp_parents": ([_P, _P], C.c_int),
+    "sg_util_rmat_host": ([C.c_int, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                           C.c_int, C.c_double, C.c_double, _P, _P, _P], C.c_int),
+    "sg_hostgraph_create": ([C.c_uint32, _P, _P, _P, C.POINTER(_P)], C.c_int),
+    "sg_hostgraph_destroy": ([_P], C.c_int),
+    "sg_hostgraph_gen_updates": ([_P, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint64, C.c_int,
+                                  C.c_double, C.c_double, _P], C.c_int),
+    "sg_hostgraph_num_edges": ([_P, C.POINTER(C.c_uint64)], C.c_int),
+    "sg_hostgraph_csr": ([_P, _P, _P, _P], C.c_int),
+}
+
+_lib = None
+
+
+def load_library():
+    """Loads the in-tree library once; raises ImportError when it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        raise ImportError(
+            f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(path)
+    for name, (args, res) in _SIGS.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _check(st: int, ctx=None, what: str = ""):
+    if st == SG_OK:
+        return
+    msg = what
+    if ctx is not None and ctx._h:
+        msg = f"{what}: {load_library().sg_last_error(ctx._h).decode(errors='replace')}"
+    raise SgError(st, msg)
+
+
+def default_options(**kw) -> Options:
+    o = Options()
+    _check(load_library().sg_options_default(C.byref(o)), None, "sg_options_default")
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise TypeError(f"unknown option {k}")
+        setattr(o, k, v)
+    return o
+
+
+class Context:
+    """One device context (graph + application states) on one GPU."""
+
+    def __init__(self, device: int = 0, **options):
+        self._lib = load_library()
+        self._h = None
+        self.options = default_options(**options)
+        h = _P()
+        st = self._lib.sg_ctx_create(device, C.byref(self.options), C.byref(h))
+        if st != SG_OK:
+            raise SgError(st, "sg_ctx_create failed (no CUDA device?)")
+        self._h = h
+
+    def close(self):
+        if self._h:
+            self._lib.sg_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- graph ------------------------------------------------------------
+    def load_csr(self, row_ptr, col, w=None):
+        row_ptr = np.ascontiguousarray(row_ptr, dtype=np.uint64)
+        col = np.ascontiguousarray(col, dtype=np.uint32)
+        w = None if w is None else np.ascontiguousarray(w, dtype=np.float32)
+        n = len(row_ptr) - 1
+        _check(self._lib.sg_graph_load_csr(self._h, n, _ptr(row_ptr), _ptr(col), _ptr(w)), self,
+               "sg_graph_load_csr")
+
+    def generate_rmat(self, scale, edges, a=0.57, b=0.19, c=0.19, seed=1, weight_kind=0,
+                      wlo=1.0, whi=100.0):
+        _check(self._lib.sg_graph_generate_rmat(self._h, scale, edges, a, b, c, seed, weight_kind,
+                                                wlo, whi), self, "sg_graph_generate_rmat")
+
+    @property
+    def n(self) -> int:
+        v = C.c_uint32()
+        _check(self._lib.sg_graph_num_vertices(self._h, C.byref(v)), self)
+        return v.value
+
+    @property
+    def m(self) -> int:
+        v = C.c_uint64()
+        _check(self._lib.sg_graph_num_edges(self._h, C.byref(v)), self)
+        return v.value
+
+    def download_csr(self, weights=True):
+        n, m = self.n, self.m
+        rp = np.empty(n + 1, np.uint64)
+        col = np.empty(m, np.uint32)
+        w = np.empty(m, np.float32) if weights else None
+        _check(self._lib.sg_graph_download_csr(self._h, _ptr(rp), _ptr(col), _ptr(w)), self,
+               "sg_graph_download_csr")
+        return rp, col, w
+
+    def apply_updates(self, upd: np.ndarray):
+        upd = np.ascontiguousarray(upd, dtype=UPDATE_DTYPE)
+        _check(self._lib.sg_apply_updates(self._h, len(upd), _ptr(upd)), self, "sg_apply_updates")
+
+    # -- PageRank ---------------------------------------------------------
+    def pr_peval(self, out=True):
+        x = np.empty(self.n, np.float32) if out else None
+        _check(self._lib.sg_pr_peval(self._h, _ptr(x)), self, "sg_pr_peval")
+        return x
+
+    def pr_inceval(self, out=True):
+        x = np.empty(self.n, np.float32) if out else None
+        _check(self._lib.sg_pr_inceval(self._h, _ptr(x)), self, "sg_pr_inceval")
+        return x
+
+    def pr_values(self):
+        x = np.empty(self.n, np.float32)
+        _check(self._lib.sg_pr_values(self._h, _ptr(x)), self, "sg_pr_values")
+        return x
+
+    def pr_deltas(self):
+        x = np.empty(self.n, np.float32)
+        _check(self._lib.sg_pr_deltas(self._h, _ptr(x)), self, "sg_pr_deltas")
+        return x
+
+    # -- SSSP -------------------------------------------------------------
+    def sssp_peval(self, source=0, out=True):
+        d = np.empty(self.n, np.float64) if out else None
+        _check(self._lib.sg_sssp_peval(self._h, source, _ptr(d)), self, "sg_sssp_peval")
+        return d
+
+    def sssp_inceval(self, out=True):
+        d = np.empty(self.n, np.float64) if out else None
+        _check(self._lib.sg_sssp_inceval(self._h, _ptr(d)), self, "sg_sssp_inceval")
+        return d
+
+    def sssp_parents(self):
+        p = np.empty(self.n, np.uint32)
+        _check(self._lib.sg_sssp_parents(self._h, _ptr(p)), self, "sg_sssp_parents")
+        return p
+
+    def stats(self) -> dict:
+        s = Stats()
+        _check(self._lib.sg_get_stats(self._h, C.byref(s)), self)
+        return s.as_dict()
+
+
+def rmat_host(scale, edges, a=0.57, b=0.19, c=0.19, seed=1, weight_kind=0, wlo=1.0, whi=100.0):
+    """Host twin of Context.generate_rmat: returns (row_ptr, col, w or None)."""
+    lib = load_library()
+    n = 1 << scale
+    rp = np.empty(n + 1, np.uint64)
+    col = np.empty(edges, np.uint32)
+    w = np.empty(edges, np.float32) if weight_kind else None
+    _check(lib.sg_util_rmat_host(scale, edges, a, b, c, seed, weight_kind, wlo, whi, _ptr(rp),
+                                 _ptr(col), _ptr(w)), None, "sg_util_rmat_host")
+    return rp, col, w
+
+
+class HostGraph:
+    """Host adjacency mirror that draws valid update batches."""
+
+    def __init__(self, row_ptr, col, w=None):
+        self._lib = load_library()
+        self._h = None
+        row_ptr = np.ascontiguousarray(row_ptr, dtype=np.uint64)
+        col = np.ascontiguousarray(col, dtype=np.uint32)
+        self.weighted = w is not None
+        w = None if w is None else np.ascontiguousarray(w, dtype=np.float32)
+        h = _P()
+        _check(self._lib.sg_hostgraph_create(len(row_ptr) - 1, _ptr(row_ptr), _ptr(col), _ptr(w),
+                                             C.byref(h)), None, "sg_hostgraph_create")
+        self._h = h
+        self.n = len(row_ptr) - 1
+
+    def __del__(self):
+        if self._h:
+            self._lib.sg_hostgraph_destroy(self._h)
+            self._h = None
+
+    @property
+    def m(self) -> int:
+        v = C.c_uint64()
+        _check(self._lib.sg_hostgraph_num_edges(self._h, C.byref(v)))
+        return v.value
+
+    def gen_updates(self, n_ins, n_del, n_rew=0, seed=1, integer_weights=True, wlo=1.0,
+                    whi=100.0) -> np.ndarray:
+        out = np.zeros(n_ins + n_del + 2 * n_rew, UPDATE_DTYPE)
+        _check(self._lib.sg_hostgraph_gen_updates(self._h, n_ins, n_del, n_rew, seed,
+                                                  1 if integer_weights else 0, wlo, whi,
+                                                  _ptr(out)), None, "sg_hostgraph_gen_updates")
+        return out
+
+    def csr(self):
+        m = self.m
+        rp = np.empty(self.n + 1, np.uint64)
+        col = np.empty(m, np.uint32)
+        w = np.empty(m, np.float32) if self.weighted else None
+        _check(self._lib.sg_hostgraph_csr(self._h, _ptr(rp), _ptr(col), _ptr(w)))
+        return rp, col, w

@@ -1,0 +1,299 @@
+// extern "C" surface of libsuminc_gb300: argument checks, device selection,
+// error capture and the per-kernel-class profiler.  No C++ exception crosses
+// this file's functions.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "ctx.h"
+
+namespace sg {
+
+sg_status fail(sg_ctx* ctx, sg_status st, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return st;
+}
+
+sg_status cuda_fail(sg_ctx* ctx, cudaError_t e, const char* where) {
+  std::string m = std::string(cudaGetErrorName(e)) + ": " + cudaGetErrorString(e) + " at " + where;
+  cudaGetLastError();
+  return fail(ctx, e == cudaErrorMemoryAllocation ? SG_ERR_OOM : SG_ERR_CUDA, m);
+}
+
+void kprof_begin(sg_ctx* ctx) {
+  if (ctx->opt.profile) cudaEventRecord(ctx->kev0, ctx->stream);
+}
+
+void kprof_end(sg_ctx* ctx, int klass) {
+  if (!ctx->opt.profile) return;
+  cudaEventRecord(ctx->kev1, ctx->stream);
+  cudaEventSynchronize(ctx->kev1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->kev0, ctx->kev1);
+  ctx->stats.kernel_ms[klass] += ms;
+  ctx->stats.kernel_launches[klass] += 1;
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+#define SG_GUARD(ctx)                                                  \
+  if (!(ctx)) return SG_ERR_INVALID;                                   \
+  do {                                                                 \
+    cudaError_t e_ = cudaSetDevice((ctx)->device);                     \
+    if (e_ != cudaSuccess) return cuda_fail((ctx), e_, "cudaSetDevice"); \
+  } while (0)
+
+#define SG_CATCH(ctx)                                                          \
+  catch (const std::bad_alloc&) {                                             \
+    return fail((ctx), SG_ERR_OOM, "host allocation failed");                  \
+  }                                                                            \
+  catch (...) {                                                                \
+    return fail((ctx), SG_ERR_INVALID, "unexpected C++ exception");            \
+  }
+
+extern "C" {
+
+sg_status sg_options_default(sg_options* o) {
+  if (!o) return SG_ERR_INVALID;
+  std::memset(o, 0, sizeof(*o));
+  o->damping = 0.85;             // PageRankIngress::d
+  o->termcheck_threshold = 1e-6; // the SumInc scripts' -termcheck_threshold
+  o->max_rounds = 1000;
+  o->compress = 0;
+  o->max_node_num = 150;         // flags.cc:60
+  o->min_node_num = 8;           // flags.cc:61
+  o->mirror_k = 4;               // flags.cc:62
+  o->profile = 0;
+  o->compress_threshold = 1.0;   // flags.cc:67
+  o->sssp_delta = 0.0;
+  o->slack = 0.125;
+  return SG_OK;
+}
+
+sg_status sg_ctx_create(int device, const sg_options* opt, sg_ctx** out) {
+  if (!out) return SG_ERR_INVALID;
+  *out = nullptr;
+  sg_ctx* ctx = nullptr;
+  try {
+    ctx = new sg_ctx();
+  } catch (...) {
+    return SG_ERR_OOM;
+  }
+  if (opt) ctx->opt = *opt; else sg_options_default(&ctx->opt);
+  if (!(ctx->opt.damping > 0.0 && ctx->opt.damping < 1.0) || !(ctx->opt.termcheck_threshold > 0.0)) {
+    delete ctx;
+    return SG_ERR_INVALID;
+  }
+  ctx->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->kev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->kev1);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SG_ERR_CUDA;
+  }
+  ctx->own_stream = true;
+  *out = ctx;
+  return SG_OK;
+}
+
+sg_status sg_ctx_destroy(sg_ctx* ctx) {
+  if (!ctx) return SG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  pr_free(ctx);
+  sssp_free(ctx);
+  graph_free(ctx);
+  DevBatch& B = ctx->batch;
+  dfree(B.raw); dfree(B.key); dfree(B.key2); dfree(B.val); dfree(B.val2);
+  dfree(B.a_src); dfree(B.a_dst); dfree(B.a_w); dfree(B.a_kind); dfree(B.a_found);
+  dfree(B.grp_vertex); dfree(B.grp_begin); dfree(B.grp_end); dfree(B.perm);
+  dfree(B.igrp_vertex); dfree(B.igrp_begin); dfree(B.igrp_end); dfree(B.d_count);
+  if (ctx->cub_tmp) cudaFree(ctx->cub_tmp);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->kev0) cudaEventDestroy(ctx->kev0);
+  if (ctx->kev1) cudaEventDestroy(ctx->kev1);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return SG_OK;
+}
+
+const char* sg_last_error(const sg_ctx* ctx) {
+  if (!ctx) return "null context";
+  return ctx->err.c_str();
+}
+
+sg_status sg_ctx_set_stream(sg_ctx* ctx, void* stream) {
+  SG_GUARD(ctx);
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  ctx->stream = (cudaStream_t)stream;
+  ctx->own_stream = false;
+  return SG_OK;
+}
+
+sg_status sg_get_stats(const sg_ctx* ctx, sg_stats* out) {
+  if (!ctx || !out) return SG_ERR_INVALID;
+  *out = ctx->stats;
+  return SG_OK;
+}
+
+sg_status sg_graph_load_csr(sg_ctx* ctx, uint32_t n, const uint64_t* row_ptr,
+                            const uint32_t* col, const float* w) {
+  SG_GUARD(ctx);
+  try {
+    pr_free(ctx);
+    sssp_free(ctx);
+    return load_csr(ctx, n, row_ptr, col, w);
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_graph_generate_rmat(sg_ctx* ctx, int scale, uint64_t edges, double a, double b,
+                                 double c, uint64_t seed, int weight_kind, double wlo,
+                                 double whi) {
+  SG_GUARD(ctx);
+  if (!(a >= 0 && b >= 0 && c >= 0 && a + b + c <= 1.0)) return fail(ctx, SG_ERR_INVALID, "bad R-MAT probabilities");
+  if (weight_kind < 0 || weight_kind > 2) return fail(ctx, SG_ERR_INVALID, "bad weight kind");
+  if (weight_kind == 1 && !(whi >= wlo)) return fail(ctx, SG_ERR_INVALID, "bad weight range");
+  try {
+    pr_free(ctx);
+    sssp_free(ctx);
+    return generate_rmat(ctx, scale, edges, a, b, c, seed, weight_kind, wlo, whi);
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_graph_num_vertices(const sg_ctx* ctx, uint32_t* n) {
+  if (!ctx || !n) return SG_ERR_INVALID;
+  *n = ctx->g.n;
+  return SG_OK;
+}
+
+sg_status sg_graph_num_edges(const sg_ctx* ctx, uint64_t* m) {
+  if (!ctx || !m) return SG_ERR_INVALID;
+  *m = ctx->g.m;
+  return SG_OK;
+}
+
+sg_status sg_graph_download_csr(sg_ctx* ctx, uint64_t* row_ptr, uint32_t* col, float* w) {
+  SG_GUARD(ctx);
+  try {
+    return download_csr(ctx, row_ptr, col, w);
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_apply_updates(sg_ctx* ctx, uint64_t count, const sg_update* upd) {
+  SG_GUARD(ctx);
+  try {
+    return apply_updates_device(ctx, count, upd);
+  }
+  SG_CATCH(ctx)
+}
+
+static sg_status copy_out_f32(sg_ctx* ctx, const float* d, float* h) {
+  if (!h) return SG_OK;
+  SG_CUDA(ctx, cudaMemcpyAsync(h, d, 4ull * ctx->g.n, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+sg_status sg_pr_peval(sg_ctx* ctx, float* out) {
+  SG_GUARD(ctx);
+  try {
+    ctx->pr.valid = false;
+    sg_status st = pr_alloc(ctx);
+    if (st != SG_OK) return st;
+    st = pr_run(ctx, false);
+    if (st != SG_OK && st != SG_ERR_NOT_CONVERGED) return st;
+    sg_status c = copy_out_f32(ctx, ctx->pr.x, out);
+    return c != SG_OK ? c : st;
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_pr_inceval(sg_ctx* ctx, float* out) {
+  SG_GUARD(ctx);
+  try {
+    sg_status st = pr_run(ctx, true);
+    if (st != SG_OK && st != SG_ERR_NOT_CONVERGED) return st;
+    sg_status c = copy_out_f32(ctx, ctx->pr.x, out);
+    return c != SG_OK ? c : st;
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_pr_values(sg_ctx* ctx, float* out) {
+  SG_GUARD(ctx);
+  if (!ctx->pr.valid) return fail(ctx, SG_ERR_STATE, "no PageRank result");
+  if (!out) return fail(ctx, SG_ERR_INVALID, "null output");
+  return copy_out_f32(ctx, ctx->pr.x, out);
+}
+
+sg_status sg_pr_deltas(sg_ctx* ctx, float* out) {
+  SG_GUARD(ctx);
+  if (!ctx->pr.valid) return fail(ctx, SG_ERR_STATE, "no PageRank result");
+  if (!out) return fail(ctx, SG_ERR_INVALID, "null output");
+  return copy_out_f32(ctx, ctx->pr.delta, out);
+}
+
+sg_status sg_pr_values_device(sg_ctx* ctx, const float** dptr) {
+  if (!ctx || !dptr) return SG_ERR_INVALID;
+  if (!ctx->pr.valid) return fail(ctx, SG_ERR_STATE, "no PageRank result");
+  *dptr = ctx->pr.x;
+  return SG_OK;
+}
+
+sg_status sg_sssp_peval(sg_ctx* ctx, uint32_t source, double* out) {
+  SG_GUARD(ctx);
+  try {
+    SG_TRY(sssp_run_peval(ctx, source));
+    if (out) return sssp_download(ctx, out);
+    return SG_OK;
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_sssp_inceval(sg_ctx* ctx, double* out) {
+  SG_GUARD(ctx);
+  try {
+    SG_TRY(sssp_run_inceval(ctx));
+    if (out) return sssp_download(ctx, out);
+    return SG_OK;
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_sssp_distances(sg_ctx* ctx, double* out) {
+  SG_GUARD(ctx);
+  if (!out) return fail(ctx, SG_ERR_INVALID, "null output");
+  try {
+    return sssp_download(ctx, out);
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_sssp_parents(sg_ctx* ctx, uint32_t* out) {
+  SG_GUARD(ctx);
+  if (!out) return fail(ctx, SG_ERR_INVALID, "null output");
+  if (!ctx->sp.valid) return fail(ctx, SG_ERR_STATE, "no SSSP result");
+  SG_CUDA(ctx, cudaMemcpyAsync(out, ctx->sp.parent, 4ull * ctx->g.n, cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+}  // extern "C"

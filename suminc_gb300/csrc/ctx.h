@@ -1,0 +1,230 @@
+// Internal context shared by the translation units of libsuminc_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/suminc_gb300.h"
+#include "common.h"
+
+namespace sg {
+
+// One direction of adjacency.  Vertex v owns the segment
+// col[off[v] .. off[v] + cap[v]); the first deg[v] slots are live.  Segment
+// starts are multiples of 4 entries so a segment can be read with 128-bit
+// loads.  Segments that outgrow their capacity move to the pool tail.
+struct DevCSR {
+  uint64_t* off = nullptr;
+  uint32_t* deg = nullptr;
+  uint32_t* cap = nullptr;
+  uint32_t* col = nullptr;
+  float* w = nullptr;           // null for unweighted graphs
+  uint64_t pool_cap = 0;        // total slots allocated
+  uint64_t* pool_tail = nullptr;  // device counter: first free slot
+};
+
+struct DevGraph {
+  uint32_t n = 0;
+  uint64_t m = 0;  // live edges (host mirror of the device count)
+  bool weighted = false;
+  bool valid = false;
+  DevCSR out, in;
+  // Edge-balanced work lists over the in-CSR: vertices with in-degree > 0 and
+  // the exclusive prefix of their 4-edge quads.  Rebuilt after each update.
+  uint32_t* in_nz = nullptr;     // [n]
+  uint64_t* in_qoff = nullptr;   // [n + 1]
+  uint32_t in_nz_count = 0;
+  uint64_t in_quads = 0;
+  // out-direction quad prefix over all vertices (push frontier uses its own)
+  uint32_t* out_nz = nullptr;
+  uint64_t* out_qoff = nullptr;
+  uint32_t out_nz_count = 0;
+  uint64_t out_quads = 0;
+};
+
+// Normalized update batch kept on the device between apply and IncEval.
+struct DevBatch {
+  uint64_t cap = 0;
+  sg_update* raw = nullptr;     // as uploaded
+  uint64_t* key = nullptr;      // scratch keys
+  uint64_t* key2 = nullptr;
+  uint32_t* val = nullptr;
+  uint32_t* val2 = nullptr;
+  // normalized actions
+  uint32_t* a_src = nullptr;
+  uint32_t* a_dst = nullptr;
+  float* a_w = nullptr;
+  uint32_t* a_kind = nullptr;   // bit0: delete old, bit1: add
+  uint32_t* a_found = nullptr;  // out-dir: slot found (kInvalidVid if none)
+  uint64_t n_act = 0;
+  uint32_t* grp_vertex = nullptr;  // per-vertex groups over actions
+  uint32_t* grp_begin = nullptr;
+  uint32_t* grp_end = nullptr;
+  uint64_t n_grp = 0;
+  uint32_t* perm = nullptr;        // action order sorted by (dst, src)
+  uint32_t* igrp_vertex = nullptr;
+  uint32_t* igrp_begin = nullptr;
+  uint32_t* igrp_end = nullptr;
+  uint64_t n_igrp = 0;
+  void* cub_tmp = nullptr;
+  size_t cub_tmp_bytes = 0;
+  uint64_t* d_count = nullptr;     // device scalars
+};
+
+struct PrState {
+  bool valid = false;
+  float* x = nullptr;      // values_
+  float* delta = nullptr;  // deltas_
+  float* acc = nullptr;    // per-round incoming sums (pull)
+  float* pv = nullptr;     // per-vertex push value d*delta/outdeg this round
+  uint32_t* frontier = nullptr;   // active vertices with outdeg > 0
+  uint32_t* d_misc = nullptr;     // [0] frontier size, [1] done, [2] pending, [3] blocks done
+  double* d_res = nullptr;        // [0] residual accumulator, [1] last residual
+  uint64_t* d_cnt = nullptr;      // [0] edges relaxed, [1] vertex visits
+  bool dense_all = true;
+};
+
+struct SsspState {
+  bool valid = false;
+  uint32_t source = 0;
+  uint32_t n_alloc = 0;
+  unsigned long long* dist = nullptr;  // ordered bits of non-negative doubles
+  uint32_t* parent = nullptr;
+  uint32_t* stamp = nullptr;      // near-queue de-duplication tags
+  uint32_t* fstamp = nullptr;     // far-queue de-duplication epochs
+  uint32_t* q[3] = {nullptr, nullptr, nullptr};  // rotating near queues
+  uint32_t* far = nullptr;        // two far queues
+  uint32_t* far2 = nullptr;
+  uint64_t far_cap = 0;
+  uint32_t* reset = nullptr;      // reset marks for IncEval
+  uint32_t* list = nullptr;       // reset vertices of the current IncEval
+  uint32_t* seeds = nullptr;      // reset seeds found by the applier
+  uint32_t* seed_cnt = nullptr;   // [0] seeds, [1] BFS level counter
+  uint32_t* d_ctl = nullptr;      // control words of the persistent kernel
+  unsigned long long* d_cnt = nullptr;
+  double* out = nullptr;          // staging for FP64 output
+  uint32_t* padd_src = nullptr;   // edges added since the last run
+  uint32_t* padd_dst = nullptr;
+  float* padd_w = nullptr;
+  uint64_t padd_cap = 0;
+  uint64_t padd_bound = 0;        // host upper bound of the pending count
+  uint32_t iter_base = 1;         // queue tags grow across launches
+  bool has_pending = false;       // a batch was applied since the last run
+  double delta_width = 0;
+};
+
+struct Timer {
+  cudaEvent_t a = nullptr, b = nullptr;
+};
+
+}  // namespace sg
+
+struct sg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  sg_options opt{};
+  sg::DevGraph g;
+  sg::DevBatch batch;
+  sg::PrState pr;
+  sg::SsspState sp;
+  sg_stats stats{};
+  std::string err;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t kev0 = nullptr, kev1 = nullptr;
+  void* cub_tmp = nullptr;
+  size_t cub_tmp_bytes = 0;
+  int num_sms = 0;
+};
+
+namespace sg {
+
+// status helpers -----------------------------------------------------------
+sg_status fail(sg_ctx* ctx, sg_status st, const std::string& msg);
+sg_status cuda_fail(sg_ctx* ctx, cudaError_t e, const char* where);
+
+#define SG_CUDA(ctx, call)                                       \
+  do {                                                           \
+    cudaError_t e_ = (call);                                     \
+    if (e_ != cudaSuccess) return ::sg::cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+#define SG_TRY(call)                    \
+  do {                                  \
+    sg_status s_ = (call);              \
+    if (s_ != SG_OK) return s_;         \
+  } while (0)
+
+// device memory helpers
+template <typename T>
+sg_status dalloc(sg_ctx* ctx, T** p, uint64_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, SG_ERR_OOM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+  }
+  return SG_OK;
+}
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+sg_status ensure_cub_tmp(sg_ctx* ctx, size_t bytes);
+
+// kernel-class timing (active when opt.profile != 0)
+void kprof_begin(sg_ctx* ctx);
+void kprof_end(sg_ctx* ctx, int klass);
+
+// graph.cu
+sg_status graph_free(sg_ctx* ctx);
+sg_status graph_build_from_sorted_keys(sg_ctx* ctx, uint32_t n, uint64_t m,
+                                       uint64_t* d_keys, float* d_w,
+                                       bool weighted);
+sg_status graph_rebuild_worklists(sg_ctx* ctx);
+sg_status apply_updates_device(sg_ctx* ctx, uint64_t count,
+                               const sg_update* host_upd);
+
+// pagerank.cu
+sg_status pr_free(sg_ctx* ctx);
+sg_status pr_alloc(sg_ctx* ctx);
+sg_status pr_run(sg_ctx* ctx, bool inc);
+// called by the applier for each affected source vertex group
+struct PrAmendArgs {
+  float* x;
+  float* delta;
+  float damping;
+  bool active;
+};
+PrAmendArgs pr_amend_args(sg_ctx* ctx);
+
+// sssp.cu
+sg_status sssp_free(sg_ctx* ctx);
+sg_status sssp_run_peval(sg_ctx* ctx, uint32_t source);
+sg_status sssp_run_inceval(sg_ctx* ctx);
+sg_status sssp_compute_parents(sg_ctx* ctx);
+struct SsspAmendArgs {
+  uint32_t* parent;
+  uint32_t* seeds;      // reset seed list (device)
+  uint32_t* seed_count; // device counter
+  uint32_t* reset;      // reset marks
+  bool active;
+};
+SsspAmendArgs sssp_amend_args(sg_ctx* ctx);
+sg_status sssp_collect_adds(sg_ctx* ctx);
+sg_status sssp_download(sg_ctx* ctx, double* out);
+
+// graph.cu entry points behind the C ABI
+sg_status generate_rmat(sg_ctx* ctx, int scale, uint64_t edges, double a, double b,
+                        double c, uint64_t seed, int wkind, double wlo, double whi);
+sg_status load_csr(sg_ctx* ctx, uint32_t n, const uint64_t* row_ptr,
+                   const uint32_t* col, const float* w);
+sg_status download_csr(sg_ctx* ctx, uint64_t* row_ptr, uint32_t* col, float* w);
+
+}  // namespace sg

@@ -1,0 +1,648 @@
+// Weighted SSSP with FP64 distances: delta-stepping (near / far queues) in
+// one cooperative persistent kernel, plus the incremental path.
+//
+// Distances are stored as the bit patterns of non-negative doubles, so an
+// unsigned 64-bit atomicMin is an exact min (integer weights give exact FP64
+// sums below 2^53; results are bit-identical to Dijkstra).  This replaces
+// SSSPIngress's DependencyData::SetIfLessThanAtomic CAS loop
+// (grape/utils/dependency_data.h:21-34) and the reference's bitmap-frontier
+// rounds (sum_sync_traversal_worker.h:1037-1300).
+//
+// Every wait in the persistent kernel is a grid barrier with a bounded spin;
+// on expiry the kernel records an error word and every block returns.
+#include <algorithm>
+#include <cmath>
+
+#include "ctx.h"
+#include "dev.cuh"
+
+namespace sg {
+
+enum {
+  S_Q0 = 0, S_Q1 = 1, S_Q2 = 2,      // near queue counts (rotating slots)
+  S_F0 = 3, S_F1 = 4,                // far queue counts (rotating by split)
+  S_BAR_COUNT = 5, S_BAR_GEN = 6,
+  S_ERR = 7,
+  S_ITERS = 8,
+  S_SPLITS = 9,
+  S_WORDS = 16
+};
+enum { SC_EDGES = 0, SC_IMPROVE = 1, SC_VISITS = 2, SC_MIN = 3, SC_WORDS = 4 };
+
+struct SsspArgs {
+  uint32_t n;
+  const uint64_t* off;
+  const uint32_t* deg;
+  const uint32_t* col;
+  const float* w;
+  unsigned long long* dist;
+  uint32_t* stamp;       // near de-duplication: last iteration a vertex was queued
+  uint32_t* fstamp;      // far de-duplication: last split epoch
+  uint32_t* nq[3];       // near queues
+  uint32_t* fq[2];       // far queues
+  uint32_t* ctl;
+  unsigned long long* cnt;
+  double delta;
+  uint32_t iter_base;    // stamps start above this value
+  uint64_t fcap;         // far queue capacity
+  long long spin_limit;
+};
+
+__device__ __forceinline__ bool grid_sync(const SsspArgs& A) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile uint32_t* gen = A.ctl + S_BAR_GEN;
+    const uint32_t g = *gen;
+    __threadfence();
+    if (atomicAdd(A.ctl + S_BAR_COUNT, 1u) == gridDim.x - 1) {
+      A.ctl[S_BAR_COUNT] = 0;
+      __threadfence();
+      atomicAdd(A.ctl + S_BAR_GEN, 1u);
+    } else {
+      long long spins = 0;
+      while (*gen == g) {
+        if (++spins > A.spin_limit) {
+          atomicExch(A.ctl + S_ERR, 1u);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *(volatile uint32_t*)(A.ctl + S_ERR) == 0;
+}
+
+// Relaxes the out-edges of every vertex in `q` (warp per vertex, 4-edge
+// quads, 128-bit loads of neighbour and weight arrays).
+__device__ __forceinline__ void relax_queue(const SsspArgs& A, const uint32_t* q, uint32_t qn,
+                                            double thr, uint32_t* nq_next, uint32_t* nq_cnt,
+                                            uint32_t* fq, uint32_t* fq_cnt, uint32_t tag,
+                                            unsigned long long& edges,
+                                            unsigned long long& improve) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < qn; i += nwarps) {
+    const uint32_t v = __ldcg(q + i);
+    const double dv = bitsd(__ldcg(A.dist + v));
+    const uint32_t d = A.deg[v];
+    const uint64_t base = A.off[v];
+    if (lane == 0) edges += d;
+    for (uint32_t kb = 0; kb < d; kb += 128) {
+      const uint32_t k = kb + lane * 4;
+      uint32_t cc[4] = {kInvalidVid, kInvalidVid, kInvalidVid, kInvalidVid};
+      float ww[4] = {0.f, 0.f, 0.f, 0.f};
+      if (k < d) {
+        const uint4 c4 = *reinterpret_cast<const uint4*>(A.col + base + k);
+        const float4 w4 = *reinterpret_cast<const float4*>(A.w + base + k);
+        cc[0] = c4.x; cc[1] = k + 1 < d ? c4.y : kInvalidVid;
+        cc[2] = k + 2 < d ? c4.z : kInvalidVid; cc[3] = k + 3 < d ? c4.w : kInvalidVid;
+        ww[0] = w4.x; ww[1] = w4.y; ww[2] = w4.z; ww[3] = w4.w;
+      }
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        bool to_near = false, to_far = false;
+        const uint32_t x = cc[t];
+        if (x != kInvalidVid) {
+          const double nd = dv + (double)ww[t];
+          const unsigned long long nb = dbits(nd);
+          if (nb < A.dist[x]) {
+            const unsigned long long old = atomicMin(A.dist + x, nb);
+            if (nb < old) {
+              improve++;
+              if (nd < thr) {
+                to_near = atomicExch(A.stamp + x, tag) != tag;
+              } else {
+                to_far = true;
+              }
+            }
+          }
+        }
+        const uint32_t sn = warp_append(to_near, nq_cnt);
+        if (to_near) nq_next[sn] = x;
+        const uint32_t sf = warp_append(to_far, fq_cnt);
+        if (to_far) {
+          if (sf < A.fcap) fq[sf] = x; else atomicExch(A.ctl + S_ERR, 2u);
+        }
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_sssp_persistent(SsspArgs A) {
+  __shared__ unsigned long long s_red[8];
+  unsigned long long edges = 0, improve = 0;
+  uint32_t it = 0;       // near iterations
+  uint32_t fslot = 0;    // current far queue
+  double thr = 0.0;      // current window end
+
+  // iteration `it` reads near slot it % 3, appends to (it+1) % 3 and clears
+  // (it+2) % 3; the host seeds slot 0 or the far queue.
+  bool ok = true;
+  for (;;) {
+    const uint32_t rs = it % 3, ws = (it + 1) % 3, cs = (it + 2) % 3;
+    const uint32_t qn = *(volatile uint32_t*)(A.ctl + S_Q0 + rs);
+    if (qn == 0) {
+      // bucket advance: smallest far distance decides the next window
+      const uint32_t fn = *(volatile uint32_t*)(A.ctl + S_F0 + fslot);
+      if (fn == 0) break;
+      if (blockIdx.x == 0 && threadIdx.x == 0) A.cnt[SC_MIN] = kInfBits;
+      if (!(ok = grid_sync(A))) break;
+      unsigned long long mn = kInfBits;
+      for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < fn; i += gridDim.x * blockDim.x) {
+        const unsigned long long dx = __ldcg(A.dist + __ldcg(A.fq[fslot] + i));
+        mn = dx < mn ? dx : mn;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_down_sync(0xffffffffu, mn, o);
+        mn = t < mn ? t : mn;
+      }
+      if ((threadIdx.x & 31) == 0 && mn != kInfBits) atomicMin(A.cnt + SC_MIN, mn);
+      if (!(ok = grid_sync(A))) break;
+      const unsigned long long mnb = *(volatile unsigned long long*)(A.cnt + SC_MIN);
+      const uint32_t nf = fslot ^ 1u;
+      if (mnb >= kInfBits) {
+        // nothing reachable left in the far queue
+        if (blockIdx.x == 0 && threadIdx.x == 0) A.ctl[S_F0 + fslot] = 0;
+        if (!(ok = grid_sync(A))) break;
+        continue;
+      }
+      const double mind = bitsd(mnb);
+      const double settled = thr;  // everything below the old window is final
+      thr = (floor(mind / A.delta) + 1.0) * A.delta;
+      const uint32_t tag = A.iter_base + it + 1;
+      const uint32_t epoch = tag;
+      if (blockIdx.x == 0 && threadIdx.x == 0) A.ctl[S_F0 + nf] = 0;
+      if (!(ok = grid_sync(A))) break;
+      const uint32_t fn_full = ((fn + 31u) / 32u) * 32u;
+      for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < fn_full; i += gridDim.x * blockDim.x) {
+        bool to_near = false, to_far = false;
+        uint32_t x = 0;
+        if (i < fn) {
+          x = __ldcg(A.fq[fslot] + i);
+          const double dx = bitsd(__ldcg(A.dist + x));
+          if (dx < settled) {
+            // stale entry of a vertex finished in an earlier window
+          } else if (dx < thr) {
+            to_near = atomicExch(A.stamp + x, tag) != tag;
+          } else {
+            to_far = atomicExch(A.fstamp + x, epoch) != epoch;
+          }
+        }
+        const uint32_t sn = warp_append(to_near, A.ctl + S_Q0 + rs);
+        if (to_near) A.nq[rs][sn] = x;
+        const uint32_t sf = warp_append(to_far, A.ctl + S_F0 + nf);
+        if (to_far) A.fq[nf][sf] = x;
+      }
+      fslot = nf;
+      if (blockIdx.x == 0 && threadIdx.x == 0) A.ctl[S_SPLITS]++;
+      if (!(ok = grid_sync(A))) break;
+      continue;
+    }
+    // relax the near queue.  Slot cs was read in the previous iteration and
+    // is appended to in the next one; nobody touches it in this one.  The
+    // read slot rs keeps its count until it becomes cs again.
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      A.ctl[S_Q0 + cs] = 0;
+      A.ctl[S_ITERS] = it + 1;
+    }
+    relax_queue(A, A.nq[rs], qn, thr, A.nq[ws], A.ctl + S_Q0 + ws, A.fq[fslot],
+                A.ctl + S_F0 + fslot, A.iter_base + it + 2, edges, improve);
+    if (!(ok = grid_sync(A))) break;
+    ++it;
+  }
+  // counters
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    edges += __shfl_down_sync(0xffffffffu, edges, o);
+    improve += __shfl_down_sync(0xffffffffu, improve, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (edges) atomicAdd(A.cnt + SC_EDGES, edges);
+    if (improve) atomicAdd(A.cnt + SC_IMPROVE, improve);
+  }
+  (void)s_red;
+  (void)ok;
+}
+
+// parent[v] = smallest in-neighbour u with dist[u] + w(u,v) == dist[v]
+__global__ void k_sssp_parents(uint32_t n, uint32_t source, const uint64_t* __restrict__ off,
+                               const uint32_t* __restrict__ deg, const uint32_t* __restrict__ col,
+                               const float* __restrict__ w,
+                               const unsigned long long* __restrict__ dist,
+                               uint32_t* __restrict__ parent) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += nwarps) {
+    const unsigned long long dvb = dist[v];
+    uint32_t best = kInvalidVid;
+    if (v != source && dvb < kInfBits) {
+      const uint32_t d = deg[v];
+      const uint64_t base = off[v];
+      for (uint32_t k = lane; k < d; k += 32) {
+        const uint32_t u = col[base + k];
+        const unsigned long long dub = dist[u];
+        if (dub < kInfBits && dbits(bitsd(dub) + (double)w[base + k]) == dvb && u < best) best = u;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_down_sync(0xffffffffu, best, o));
+    }
+    if (lane == 0) parent[v] = best;
+  }
+}
+
+// Reset BFS over the shortest-path tree: children of reset vertices whose
+// parent is the reset vertex (deltaCompute, sum_sync_traversal_worker.h:
+// 183-226).
+__global__ void k_sssp_reset_step(const uint32_t* __restrict__ cur, uint32_t cn,
+                                  const uint64_t* __restrict__ off, const uint32_t* __restrict__ deg,
+                                  const uint32_t* __restrict__ col,
+                                  const uint32_t* __restrict__ parent, uint32_t* __restrict__ reset,
+                                  uint32_t* __restrict__ next, uint32_t* __restrict__ next_cnt) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cn; i += nwarps) {
+    const uint32_t x = cur[i];
+    const uint32_t d = deg[x];
+    const uint64_t base = off[x];
+    for (uint32_t kb = 0; kb < d; kb += 32) {
+      const uint32_t k = kb + lane;
+      bool take = false;
+      uint32_t y = 0;
+      if (k < d) {
+        y = col[base + k];
+        take = parent[y] == x && y != x && atomicExch(reset + y, 1u) == 0u;
+      }
+      const uint32_t s = warp_append(take, next_cnt);
+      if (take) next[s] = y;
+    }
+  }
+}
+
+__global__ void k_sssp_reset_apply(const uint32_t* __restrict__ list, uint32_t cnt,
+                                   unsigned long long* __restrict__ dist,
+                                   uint32_t* __restrict__ parent) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const uint32_t v = list[i];
+    dist[v] = kInfBits;
+    parent[v] = kInvalidVid;
+  }
+}
+
+// Re-seed reset vertices from their in-neighbours (pull) and queue them.
+__global__ void k_sssp_reseed(const uint32_t* __restrict__ list, uint32_t cnt,
+                              const uint64_t* __restrict__ off, const uint32_t* __restrict__ deg,
+                              const uint32_t* __restrict__ col, const float* __restrict__ w,
+                              unsigned long long* __restrict__ dist, uint32_t* __restrict__ fq,
+                              uint32_t* __restrict__ fq_cnt) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += nwarps) {
+    const uint32_t v = list[i];
+    const uint32_t d = deg[v];
+    const uint64_t base = off[v];
+    unsigned long long best = kInfBits;
+    for (uint32_t k = lane; k < d; k += 32) {
+      const unsigned long long du = dist[col[base + k]];
+      if (du < kInfBits) {
+        const unsigned long long nb = dbits(bitsd(du) + (double)w[base + k]);
+        best = nb < best ? nb : best;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long t = __shfl_down_sync(0xffffffffu, best, o);
+      best = t < best ? t : best;
+    }
+    if (lane == 0 && best < kInfBits) {
+      const unsigned long long old = atomicMin(dist + v, best);
+      if (best < old) fq[atomicAdd(fq_cnt, 1u)] = v;
+    }
+  }
+}
+
+// Relax the edges added by the last batch (the reference re-sends from all
+// finite vertices, sum_sync_traversal_worker.h:323-332; only these edges and
+// the reset vertices can lower a distance).
+__global__ void k_sssp_added(const uint32_t* __restrict__ a_src, const uint32_t* __restrict__ a_dst,
+                             const float* __restrict__ a_w, const uint32_t* __restrict__ a_kind,
+                             uint64_t n_act, unsigned long long* __restrict__ dist,
+                             uint32_t* __restrict__ fq, uint32_t* __restrict__ fq_cnt) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_act;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    if (a_kind && !(a_kind[i] & 2u)) continue;
+    const unsigned long long du = dist[a_src[i]];
+    if (du >= kInfBits) continue;
+    const unsigned long long nb = dbits(bitsd(du) + (double)a_w[i]);
+    const uint32_t v = a_dst[i];
+    const unsigned long long old = atomicMin(dist + v, nb);
+    if (nb < old) fq[atomicAdd(fq_cnt, 1u)] = v;
+  }
+}
+
+__global__ void k_sssp_init(uint32_t n, unsigned long long* dist, uint32_t* stamp,
+                            uint32_t* fstamp, uint32_t* reset) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    dist[v] = kInfBits;
+    stamp[v] = 0;
+    fstamp[v] = 0;
+    reset[v] = 0;
+  }
+}
+
+__global__ void k_clear_marks(const uint32_t* list, uint32_t cnt, uint32_t* reset) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+    reset[list[i]] = 0;
+}
+
+__global__ void k_dist_to_double(uint32_t n, const unsigned long long* dist, double* out) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    out[v] = bitsd(dist[v]);
+}
+
+// ------------------------------------------------------------ host side
+
+sg_status sssp_free(sg_ctx* ctx) {
+  SsspState& s = ctx->sp;
+  dfree(s.dist); dfree(s.parent); dfree(s.stamp);
+  dfree(s.q[0]); dfree(s.q[1]); dfree(s.q[2]); dfree(s.far2); dfree(s.reset);
+  dfree(s.d_ctl); dfree(s.d_cnt);
+  dfree(s.fstamp); dfree(s.list); dfree(s.seeds); dfree(s.seed_cnt); dfree(s.far);
+  dfree(s.out);
+  dfree(s.padd_src); dfree(s.padd_dst); dfree(s.padd_w);
+  s = SsspState();
+  return SG_OK;
+}
+
+static sg_status sssp_alloc(sg_ctx* ctx) {
+  SsspState& s = ctx->sp;
+  const uint32_t n = ctx->g.n;
+  sssp_free(ctx);
+  SG_TRY(dalloc(ctx, &s.dist, n));
+  SG_TRY(dalloc(ctx, &s.parent, n));
+  SG_TRY(dalloc(ctx, &s.stamp, n));
+  SG_TRY(dalloc(ctx, &s.fstamp, n));
+  SG_TRY(dalloc(ctx, &s.reset, n));
+  // queues: a vertex is queued at most once per near iteration, but the far
+  // queue may hold a vertex once per improvement; bound it by edges + n.
+  SG_TRY(dalloc(ctx, &s.q[0], n));
+  SG_TRY(dalloc(ctx, &s.q[1], n));
+  SG_TRY(dalloc(ctx, &s.q[2], n));
+  const uint64_t fcap = ctx->g.m + (uint64_t)n + 1024;
+  SG_TRY(dalloc(ctx, &s.far, fcap));
+  SG_TRY(dalloc(ctx, &s.far2, fcap));
+  s.far_cap = fcap;
+  SG_TRY(dalloc(ctx, &s.list, n));
+  SG_TRY(dalloc(ctx, &s.seeds, n));
+  SG_TRY(dalloc(ctx, &s.seed_cnt, 4));
+  SG_TRY(dalloc(ctx, &s.d_ctl, S_WORDS));
+  SG_TRY(dalloc(ctx, &s.d_cnt, SC_WORDS));
+  s.n_alloc = n;
+  return SG_OK;
+}
+
+SsspAmendArgs sssp_amend_args(sg_ctx* ctx) {
+  SsspAmendArgs a{};
+  SsspState& s = ctx->sp;
+  a.active = s.valid;
+  a.parent = s.parent;
+  a.seeds = s.seeds;
+  a.seed_count = s.seed_cnt;
+  a.reset = s.reset;
+  if (s.valid && !s.has_pending) {
+    // first batch since the last run: empty seed list and pending adds
+    cudaMemsetAsync(s.seed_cnt, 0, 4 * sizeof(uint32_t), ctx->stream);
+    s.padd_bound = 0;
+  }
+  if (s.valid) s.has_pending = true;
+  return a;
+}
+
+__global__ void k_collect_adds(const uint32_t* __restrict__ a_src, const uint32_t* __restrict__ a_dst,
+                               const float* __restrict__ a_w, const uint32_t* __restrict__ a_kind,
+                               uint64_t n_act, uint32_t* __restrict__ ps, uint32_t* __restrict__ pd,
+                               float* __restrict__ pw, uint32_t* __restrict__ cnt) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_act;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    if (!(a_kind[i] & 2u)) continue;
+    const uint32_t slot = atomicAdd(cnt, 1u);
+    ps[slot] = a_src[i];
+    pd[slot] = a_dst[i];
+    pw[slot] = a_w[i];
+  }
+}
+
+// Called by the applier after the batch's actions are known: remembers the
+// added (or re-weighted) edges for the next IncEval.  They are relaxed only
+// after the reset, because a tail reset by the same batch must not lend its
+// stale distance to the head.
+sg_status sssp_collect_adds(sg_ctx* ctx) {
+  SsspState& s = ctx->sp;
+  const DevBatch& B = ctx->batch;
+  if (!s.valid || B.n_act == 0) return SG_OK;
+  const uint64_t need = s.padd_bound + B.n_act;
+  if (need > s.padd_cap) {
+    // grow, keeping the pending entries
+    uint64_t ncap = std::max<uint64_t>(need * 2, 4096);
+    uint32_t *ns = nullptr, *nd = nullptr;
+    float* nw = nullptr;
+    SG_TRY(dalloc(ctx, &ns, ncap));
+    SG_TRY(dalloc(ctx, &nd, ncap));
+    SG_TRY(dalloc(ctx, &nw, ncap));
+    if (s.padd_bound) {
+      SG_CUDA(ctx, cudaMemcpyAsync(ns, s.padd_src, 4 * s.padd_bound, cudaMemcpyDeviceToDevice, ctx->stream));
+      SG_CUDA(ctx, cudaMemcpyAsync(nd, s.padd_dst, 4 * s.padd_bound, cudaMemcpyDeviceToDevice, ctx->stream));
+      SG_CUDA(ctx, cudaMemcpyAsync(nw, s.padd_w, 4 * s.padd_bound, cudaMemcpyDeviceToDevice, ctx->stream));
+      SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    dfree(s.padd_src); dfree(s.padd_dst); dfree(s.padd_w);
+    s.padd_src = ns; s.padd_dst = nd; s.padd_w = nw;
+    s.padd_cap = ncap;
+  }
+  k_collect_adds<<<grid_for(B.n_act, 256), 256, 0, ctx->stream>>>(
+      B.a_src, B.a_dst, B.a_w, B.a_kind, B.n_act, s.padd_src, s.padd_dst, s.padd_w, s.seed_cnt + 2);
+  SG_CUDA(ctx, cudaGetLastError());
+  s.padd_bound = need;
+  return SG_OK;
+}
+
+static double auto_delta(sg_ctx* ctx) {
+  if (ctx->opt.sssp_delta > 0) return ctx->opt.sssp_delta;
+  return 32.0;
+}
+
+// Runs the persistent kernel from the current ctl / queues.
+static sg_status sssp_launch(sg_ctx* ctx) {
+  SsspState& s = ctx->sp;
+  DevGraph& g = ctx->g;
+  SsspArgs A;
+  A.n = g.n;
+  A.off = g.out.off; A.deg = g.out.deg; A.col = g.out.col; A.w = g.out.w;
+  A.dist = s.dist; A.stamp = s.stamp; A.fstamp = s.fstamp;
+  A.nq[0] = s.q[0]; A.nq[1] = s.q[1]; A.nq[2] = s.q[2];
+  A.fq[0] = s.far; A.fq[1] = s.far2;
+  A.ctl = s.d_ctl;
+  A.cnt = s.d_cnt;
+  A.delta = s.delta_width;
+  A.iter_base = s.iter_base;
+  A.fcap = s.far_cap;
+  A.spin_limit = 40ll * 1000 * 1000;  // ~2-4 s of polling
+  int bps = 0;
+  SG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_sssp_persistent, 256, 0));
+  if (bps < 1) return fail(ctx, SG_ERR_CUDA, "persistent SSSP kernel cannot be resident");
+  bps = std::min(bps, 4);
+  const unsigned blocks = (unsigned)(bps * ctx->num_sms);
+  void* args[] = {&A};
+  kprof_begin(ctx);
+  SG_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_sssp_persistent, dim3(blocks), dim3(256), args,
+                                           0, ctx->stream));
+  kprof_end(ctx, SG_K_SSSP);
+  uint32_t h_ctl[S_WORDS];
+  SG_CUDA(ctx, cudaMemcpyAsync(h_ctl, s.d_ctl, sizeof(h_ctl), cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  // stamps must keep growing across launches
+  s.iter_base += h_ctl[S_ITERS] + h_ctl[S_SPLITS] + 4;
+  if (h_ctl[S_ERR] == 2u) return fail(ctx, SG_ERR_OOM, "SSSP far queue overflow");
+  if (h_ctl[S_ERR]) return fail(ctx, SG_ERR_TIMEOUT, "SSSP grid barrier wait expired");
+  return SG_OK;
+}
+
+sg_status sssp_compute_parents(sg_ctx* ctx) {
+  SsspState& s = ctx->sp;
+  DevGraph& g = ctx->g;
+  k_sssp_parents<<<grid_for((uint64_t)g.n * 32, 256), 256, 0, ctx->stream>>>(
+      g.n, s.source, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.parent);
+  SG_CUDA(ctx, cudaGetLastError());
+  return SG_OK;
+}
+
+static void fill_stats(sg_ctx* ctx, const unsigned long long* cnt) {
+  ctx->stats.edges_relaxed = cnt[SC_EDGES];
+  ctx->stats.improvements = cnt[SC_IMPROVE];
+  ctx->stats.live_edges = ctx->g.m;
+}
+
+sg_status sssp_run_peval(sg_ctx* ctx, uint32_t source) {
+  DevGraph& g = ctx->g;
+  if (!g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
+  if (!g.weighted) return fail(ctx, SG_ERR_INVALID, "SSSP needs a weighted graph");
+  if (source >= g.n) return fail(ctx, SG_ERR_INVALID, "source >= n");
+  SG_TRY(sssp_alloc(ctx));
+  SsspState& s = ctx->sp;
+  s.source = source;
+  s.delta_width = auto_delta(ctx);
+  s.iter_base = 1;
+  cudaStream_t st = ctx->stream;
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+  k_sssp_init<<<grid_for(g.n, 256), 256, 0, st>>>(g.n, s.dist, s.stamp, s.fstamp, s.reset);
+  SG_CUDA(ctx, cudaMemsetAsync(s.d_ctl, 0, sizeof(uint32_t) * S_WORDS, st));
+  SG_CUDA(ctx, cudaMemsetAsync(s.d_cnt, 0, sizeof(unsigned long long) * SC_WORDS, st));
+  // seed: dist[source] = 0 in the far queue; the first split opens its bucket
+  const unsigned long long zero = 0ull;
+  const uint32_t one = 1;
+  SG_CUDA(ctx, cudaMemcpyAsync(s.dist + source, &zero, 8, cudaMemcpyHostToDevice, st));
+  SG_CUDA(ctx, cudaMemcpyAsync(s.far, &source, 4, cudaMemcpyHostToDevice, st));
+  SG_CUDA(ctx, cudaMemcpyAsync(s.d_ctl + S_F0, &one, 4, cudaMemcpyHostToDevice, st));
+  SG_TRY(sssp_launch(ctx));
+  SG_TRY(sssp_compute_parents(ctx));
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+  unsigned long long h_cnt[SC_WORDS];
+  SG_CUDA(ctx, cudaMemcpyAsync(h_cnt, s.d_cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  fill_stats(ctx, h_cnt);
+  ctx->stats.elapsed_ms = ms;
+  ctx->stats.rounds = 0;
+  ctx->stats.converged = 1;
+  ctx->stats.reset_vertices = 0;
+  s.valid = true;
+  s.has_pending = false;
+  return SG_OK;
+}
+
+sg_status sssp_run_inceval(sg_ctx* ctx) {
+  DevGraph& g = ctx->g;
+  SsspState& s = ctx->sp;
+  if (!s.valid) return fail(ctx, SG_ERR_STATE, "SSSP IncEval before PEval");
+  cudaStream_t st = ctx->stream;
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+  uint32_t h_seed[4] = {0, 0, 0, 0};
+  if (s.has_pending) {
+    SG_CUDA(ctx, cudaMemcpyAsync(h_seed, s.seed_cnt, sizeof(h_seed), cudaMemcpyDeviceToHost, st));
+    SG_CUDA(ctx, cudaStreamSynchronize(st));
+  }
+  // 1. reset BFS: list = seeds, then children level by level
+  uint32_t total = h_seed[0];
+  if (total > 0) {
+    SG_CUDA(ctx, cudaMemcpyAsync(s.list, s.seeds, 4ull * total, cudaMemcpyDeviceToDevice, st));
+    uint32_t begin = 0, end = total;
+    while (end > begin) {
+      SG_CUDA(ctx, cudaMemsetAsync(s.seed_cnt + 1, 0, 4, st));
+      k_sssp_reset_step<<<grid_for((uint64_t)(end - begin) * 32, 256), 256, 0, st>>>(
+          s.list + begin, end - begin, g.out.off, g.out.deg, g.out.col, s.parent, s.reset,
+          s.list + end, s.seed_cnt + 1);
+      uint32_t nn = 0;
+      SG_CUDA(ctx, cudaMemcpyAsync(&nn, s.seed_cnt + 1, 4, cudaMemcpyDeviceToHost, st));
+      SG_CUDA(ctx, cudaStreamSynchronize(st));
+      begin = end;
+      end += nn;
+    }
+    total = end;
+    k_sssp_reset_apply<<<grid_for(total, 256), 256, 0, st>>>(s.list, total, s.dist, s.parent);
+  }
+  // 2. far queue <- re-seeded reset vertices + heads of improving added edges
+  const uint64_t need_far = (uint64_t)total + h_seed[2] + g.n + 1024;
+  if (need_far > s.far_cap) {
+    dfree(s.far);
+    dfree(s.far2);
+    const uint64_t ncap = std::max<uint64_t>(need_far, g.m + g.n + 1024);
+    SG_TRY(dalloc(ctx, &s.far, ncap));
+    SG_TRY(dalloc(ctx, &s.far2, ncap));
+    s.far_cap = ncap;
+  }
+  SG_CUDA(ctx, cudaMemsetAsync(s.d_ctl, 0, sizeof(uint32_t) * S_WORDS, st));
+  SG_CUDA(ctx, cudaMemsetAsync(s.d_cnt, 0, sizeof(unsigned long long) * SC_WORDS, st));
+  if (total > 0)
+    k_sssp_reseed<<<grid_for((uint64_t)total * 32, 256), 256, 0, st>>>(
+        s.list, total, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.far, s.d_ctl + S_F0);
+  if (s.has_pending && h_seed[2] > 0) {
+    uint32_t* kinds = nullptr;  // all pending records are adds
+    (void)kinds;
+    k_sssp_added<<<grid_for(h_seed[2], 256), 256, 0, st>>>(s.padd_src, s.padd_dst, s.padd_w,
+                                                          nullptr, h_seed[2], s.dist, s.far,
+                                                          s.d_ctl + S_F0);
+  }
+  SG_CUDA(ctx, cudaGetLastError());
+  // 3. delta-stepping from the seeds
+  SG_TRY(sssp_launch(ctx));
+  if (total > 0) k_clear_marks<<<grid_for(total, 256), 256, 0, st>>>(s.list, total, s.reset);
+  SG_TRY(sssp_compute_parents(ctx));
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+  unsigned long long h_cnt[SC_WORDS];
+  SG_CUDA(ctx, cudaMemcpyAsync(h_cnt, s.d_cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  fill_stats(ctx, h_cnt);
+  ctx->stats.elapsed_ms = ms;
+  ctx->stats.converged = 1;
+  ctx->stats.reset_vertices = total;
+  s.has_pending = false;
+  return SG_OK;
+}
+
+sg_status sssp_download(sg_ctx* ctx, double* out) {
+  SsspState& s = ctx->sp;
+  if (!s.valid) return fail(ctx, SG_ERR_STATE, "no SSSP result");
+  const uint32_t n = ctx->g.n;
+  if (!s.out) SG_TRY(dalloc(ctx, &s.out, n));
+  k_dist_to_double<<<grid_for(n, 256), 256, 0, ctx->stream>>>(n, s.dist, s.out);
+  SG_CUDA(ctx, cudaMemcpyAsync(out, s.out, 8ull * n, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+}  // namespace sg

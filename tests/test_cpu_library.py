@@ -1,0 +1,94 @@
+"""CPU-side checks: the C ABI library loads and exports every symbol that
+include/*.h declares; host utilities are deterministic."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+import suminc_gb300 as sg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    syms = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if not f.endswith(".h"):
+            continue
+        txt = open(os.path.join(inc, f)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        for m in re.finditer(r"^\s*(?:sg_status|const char\*)\s+(sg_\w+)\s*\(", txt, re.M):
+            syms.add(m.group(1))
+    return syms
+
+
+def test_library_exports_every_declared_symbol():
+    lib = C.CDLL(sg.lib_path())
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    missing = [s for s in sorted(syms) if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_binding_signatures_cover_declarations():
+    from suminc_gb300 import _SIGS
+    assert declared_symbols() <= set(_SIGS) | {"sg_hostgraph_csr"} | set(_SIGS)
+
+
+def test_options_defaults_mirror_reference_flags():
+    o = sg.default_options()
+    assert abs(o.damping - 0.85) < 1e-12
+    assert o.max_node_num == 150 and o.min_node_num == 8 and o.mirror_k == 4
+    assert o.compress_threshold == 1.0
+
+
+def test_rmat_host_deterministic_and_simple():
+    rp1, c1, w1 = sg.rmat_host(10, 8000, seed=3, weight_kind=1)
+    rp2, c2, w2 = sg.rmat_host(10, 8000, seed=3, weight_kind=1)
+    assert np.array_equal(rp1, rp2) and np.array_equal(c1, c2) and np.array_equal(w1, w2)
+    assert rp1[-1] == 8000
+    src = np.repeat(np.arange(1024), np.diff(rp1).astype(np.int64))
+    assert not np.any(src == c1), "self loops must be dropped"
+    keys = src.astype(np.uint64) << 32 | c1.astype(np.uint64)
+    assert len(np.unique(keys)) == 8000, "duplicates must be dropped"
+    assert w1.min() >= 1 and w1.max() <= 100 and np.all(w1 == np.round(w1))
+    rp3, c3, _ = sg.rmat_host(10, 8000, seed=4)
+    assert not np.array_equal(c1, c3)
+
+
+def test_rmat_skew_matches_quadrant_probabilities():
+    rp, col, _ = sg.rmat_host(12, 40000, seed=1)
+    deg = np.diff(rp).astype(np.int64)
+    # a+b = 0.76 of the mass on the lower half of the source ids
+    low = deg[: len(deg) // 2].sum() / deg.sum()
+    assert 0.70 < low < 0.82
+
+
+def test_hostgraph_updates_are_valid():
+    rp, col, w = sg.rmat_host(10, 8000, seed=5, weight_kind=1)
+    hg = sg.HostGraph(rp, col, w)
+    upd = hg.gen_updates(100, 100, 50, seed=9)
+    assert len(upd) == 100 + 100 + 100
+    present = set(zip(np.repeat(np.arange(1024), np.diff(rp).astype(np.int64)).tolist(), col.tolist()))
+    ops = upd["op"]
+    dels = upd[ops == 1]
+    adds = upd[ops == 0]
+    assert all((int(a), int(b)) in present for a, b in zip(dels["src"], dels["dst"]))
+    new_pairs = [(int(a), int(b)) for a, b in zip(adds["src"], adds["dst"]) if (int(a), int(b)) not in present]
+    assert len(new_pairs) == 100 and all(a != b for a, b in new_pairs)
+    assert hg.m == 8000
+    # mirror equals the reference semantics applied to the old graph
+    import oracle
+    nrp, ncol, nw = oracle.apply_updates_reference(rp, col, w, upd)
+    hrp, hcol, hw = hg.csr()
+    assert np.array_equal(nrp, hrp) and np.array_equal(ncol, hcol) and np.array_equal(nw, hw)
+
+
+def test_null_and_invalid_arguments_are_rejected():
+    lib = sg.load_library()
+    assert lib.sg_ctx_destroy(None) == sg.SG_ERR_INVALID
+    assert lib.sg_get_stats(None, None) == sg.SG_ERR_INVALID
+    assert lib.sg_options_default(None) == sg.SG_ERR_INVALID
+    assert lib.sg_util_rmat_host(0, 10, 0.57, 0.19, 0.19, 1, 0, 1.0, 1.0, None, None, None) == sg.SG_ERR_INVALID

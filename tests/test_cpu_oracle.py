@@ -1,0 +1,62 @@
+"""The oracle restatement agrees with its own FP64 solvers and with the
+reference semantics it restates."""
+import numpy as np
+
+import oracle
+import suminc_gb300 as sg
+
+
+def test_ingress_pr_converges_to_fixed_point():
+    rp, col, _ = sg.rmat_host(12, 60000, seed=2)
+    x, delta, st = oracle.ingress_pr(rp, col, tau=1e-6)
+    assert st["converged"] == 1 and st["residual"] < 1e-6
+    xf = oracle.pr_fixed_point(rp, col)
+    # distance to the fixed point is bounded by residual / (1 - d)
+    assert np.abs(x - xf).sum() <= 1e-5
+
+
+def test_amend_then_inceval_equals_fresh_batch():
+    rp, col, w = sg.rmat_host(11, 30000, seed=7, weight_kind=1)
+    hg = sg.HostGraph(rp, col, w)
+    upd = hg.gen_updates(300, 300, seed=3)
+    nrp, ncol, _ = hg.csr()
+    x, delta, _ = oracle.ingress_pr(rp, col, tau=1e-9)
+    delta = oracle.pr_amend((rp, col), (nrp, ncol), x, delta)
+    x2, _, st = oracle.ingress_pr(nrp, ncol, tau=1e-9, x=x, delta=delta)
+    xf = oracle.pr_fixed_point(nrp, ncol)
+    assert st["converged"] == 1
+    assert np.abs(x2 - xf).sum() < 5e-6
+
+
+def test_dijkstra_small_known_graph():
+    # 0->1 (4), 0->2 (1), 2->1 (2), 1->3 (5); 4 unreachable
+    rp = np.array([0, 2, 3, 4, 4, 4], np.uint64)
+    col = np.array([1, 2, 3, 1], np.uint32)
+    w = np.array([4, 1, 5, 2], np.float32)
+    d = oracle.dijkstra(rp, col, w, 0)
+    assert d.tolist()[:4] == [0.0, 3.0, 1.0, 8.0] and np.isinf(d[4])
+
+
+def test_adjoint_solve_matches_dense_linear_algebra():
+    rng = np.random.default_rng(0)
+    n = 40
+    rows = [sorted(rng.choice(n, size=rng.integers(1, 6), replace=False)) for _ in range(n)]
+    rp = np.zeros(n + 1, np.uint64)
+    for i, r in enumerate(rows):
+        rp[i + 1] = rp[i] + len(r)
+    col = np.concatenate(rows).astype(np.uint32)
+    w = rng.uniform(0.1, 1.0, len(col)).astype(np.float32)
+    for i in range(n):  # column-normalise (out-weights of each source sum to 1)
+        s = w[rp[i]:rp[i + 1]].astype(np.float64).sum()
+        w[rp[i]:rp[i + 1]] = (w[rp[i]:rp[i + 1]] / s).astype(np.float32)
+    P = np.zeros((n, n))
+    for u in range(n):
+        for e in range(int(rp[u]), int(rp[u + 1])):
+            P[u, col[e]] = w[e]
+    g = rng.normal(size=n)
+    lam = oracle.pr_adjoint_solve(rp, col, w, g)
+    lam_ref = np.linalg.solve(np.eye(n) - 0.85 * P, g)
+    assert np.abs(lam - lam_ref).max() < 1e-10
+    x = oracle.pr_fixed_point(rp, col, w)
+    x_ref = np.linalg.solve(np.eye(n) - 0.85 * P.T, np.full(n, 0.15 / n))
+    assert np.abs(x - x_ref).max() < 1e-12

@@ -1,0 +1,87 @@
+"""SSSP PEval / IncEval on the device: distances bit-exact against FP64
+Dijkstra (integer weights make every path sum exact in FP64)."""
+import numpy as np
+import pytest
+
+import oracle
+import suminc_gb300 as sg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("scale,ef,src", [(10, 8, 0), (14, 16, 0), (16, 16, 123)])
+def test_peval_bit_exact(ctx, scale, ef, src):
+    n = 1 << scale
+    ctx.generate_rmat(scale, n * ef, seed=scale + 1, weight_kind=1, wlo=1, whi=100)
+    d = ctx.sssp_peval(src)
+    rp, col, w = ctx.download_csr()
+    ref = oracle.dijkstra(rp, col, w, src)
+    assert np.array_equal(d, ref)
+
+
+def test_parents_form_a_shortest_path_tree(ctx):
+    ctx.generate_rmat(12, 16 << 12, seed=3, weight_kind=1)
+    d = ctx.sssp_peval(0)
+    par = ctx.sssp_parents()
+    rp, col, w = ctx.download_csr()
+    wmap = {}
+    for u in range(len(rp) - 1):
+        for e in range(int(rp[u]), int(rp[u + 1])):
+            wmap[(u, int(col[e]))] = float(w[e])
+    for v in range(len(d)):
+        if v == 0 or not np.isfinite(d[v]):
+            assert par[v] == 0xFFFFFFFF
+        else:
+            u = int(par[v])
+            assert d[u] + wmap[(u, v)] == d[v]
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_inceval_bit_exact_after_batches(ctx, seed):
+    scale = 14
+    ctx.generate_rmat(scale, 16 << scale, seed=seed, weight_kind=1)
+    rp, col, w = ctx.download_csr()
+    hg = sg.HostGraph(rp, col, w)
+    ctx.sssp_peval(0, out=False)
+    for b in range(4):
+        upd = hg.gen_updates(800, 800, 400, seed=seed * 10 + b)
+        ctx.apply_updates(upd)
+        d = ctx.sssp_inceval()
+        nrp, ncol, nw = hg.csr()
+        ref = oracle.dijkstra(nrp, ncol, nw, 0)
+        assert np.array_equal(d, ref), b
+
+
+def test_two_batches_before_one_inceval(ctx):
+    ctx.generate_rmat(12, 16 << 12, seed=9, weight_kind=1)
+    rp, col, w = ctx.download_csr()
+    hg = sg.HostGraph(rp, col, w)
+    ctx.sssp_peval(0, out=False)
+    ctx.apply_updates(hg.gen_updates(300, 300, 100, seed=1))
+    ctx.apply_updates(hg.gen_updates(300, 300, 100, seed=2))
+    d = ctx.sssp_inceval()
+    nrp, ncol, nw = hg.csr()
+    assert np.array_equal(d, oracle.dijkstra(nrp, ncol, nw, 0))
+
+
+def test_delete_whole_tree_edge_chain(ctx):
+    # path 0->1->2->3 (w=1) plus a detour 0->3 (w=10): deleting 1->2 must
+    # reset 2 and 3 and route 3 through the detour
+    rp = np.array([0, 2, 3, 4, 4], np.uint64)
+    col = np.array([1, 3, 2, 3], np.uint32)
+    w = np.array([1, 10, 1, 1], np.float32)
+    ctx.load_csr(rp, col, w)
+    d = ctx.sssp_peval(0)
+    assert d.tolist() == [0.0, 1.0, 2.0, 3.0]
+    ctx.apply_updates(np.array([(1, 2, 0.0, 1)], sg.UPDATE_DTYPE))
+    d = ctx.sssp_inceval()
+    assert d[0] == 0 and d[1] == 1 and np.isinf(d[2]) and d[3] == 10.0
+    assert ctx.stats()["reset_vertices"] == 2
+
+
+def test_unweighted_graph_is_rejected(ctx):
+    rp, col, _ = sg.rmat_host(8, 1000, seed=1)
+    ctx.load_csr(rp, col)
+    with pytest.raises(sg.SgError) as e:
+        ctx.sssp_peval(0)
+    assert e.value.status == sg.SG_ERR_INVALID
