@@ -1,0 +1,389 @@
+#!/usr/bin/env python
+"""Headline benchmark: incremental PageRank re-evaluation on one GB300.
+
+Workload (the reference's "plain incremental PageRank at scale" case):
+R-MAT scale 24 (16,777,216 vertices, 268,435,456 distinct directed edges,
+a/b/c/d = 0.57/0.19/0.19/0.05, self loops and duplicates removed, seeded),
+damping 0.85, FP32 values, L1 residual < 1e-6 (FP64 reduction).  After the
+batch evaluation (PEval, untimed), every step applies one update batch of
+0.1 % of the edges (50 % inserts of absent uniform pairs, 50 % deletes of
+uniformly chosen edges) and runs IncEval to convergence.
+
+Metric: GTEPS = edge relaxations performed during IncEval / IncEval time.
+  value  batches already resident in HBM (sg_apply_updates_device +
+         sg_pr_inceval without output copy), CUDA events on the library stream
+  e2e    the C-ABI call a user makes: batch in pinned host memory
+         (sg_apply_updates), result copied back to pinned host memory
+         (sg_pr_inceval with an output buffer), both inside the timed region
+The graph (>1 GB per direction) is larger than the 126 MB L2, so no flush is
+needed between steps.
+
+--impl reference times the CPU restatement of the reference worker
+(oracle/: AmendValue(-1/+1) + delta rounds, OpenMP over every host core) on
+the same workload, one bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_BYTES = 126 * 1024 * 1024
+BYTES_PER_RELAXED_EDGE = 12   # 4 B neighbour + 4 B delta read + 4 B delta write
+BYTES_PER_VERTEX_VISIT = 24   # 8 B row offset + 4 B delta read/reset + 8 B value RMW
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--scale", type=int, default=24)
+    p.add_argument("--edge-factor", type=int, default=16)
+    p.add_argument("--batch-frac", type=float, default=0.001)
+    p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-sample-rounds", type=int, default=3)
+    p.add_argument("--no-clocks", action="store_true")
+    return p.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max-over-ranks for replicas (gloo on CPU tensors)."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_info()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int, enabled: bool):
+        self.proc = None
+        self.path = None
+        if not enabled:
+            return
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append(parts)
+            except ValueError:
+                pass
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_batches(hg, count, size, seed0):
+    half = size // 2
+    return [hg.gen_updates(half, size - half, 0, seed=seed0 + i, integer_weights=True)
+            for i in range(count)]
+
+
+def cpu_sample(rp_old, col_old, rp_new, col_new, x, delta, rounds):
+    """One bounded sample of the reference's IncEval on the host cores:
+    AmendValue(-1) over the old graph + AmendValue(+1) over the new graph +
+    `rounds` delta rounds.  Returns (relaxations, seconds)."""
+    import oracle
+    t0 = time.perf_counter()
+    d2 = oracle.pr_amend((rp_old, col_old), (rp_new, col_new), x, delta)
+    _, _, st = oracle.ingress_pr(rp_new, col_new, x=x, delta=d2, max_rounds=rounds)
+    dt = time.perf_counter() - t0
+    relax = int(rp_old[-1]) + int(rp_new[-1]) + int(st["edges"])
+    return relax, dt
+
+
+def run_reference(args, D: Dist):
+    if D.rank != 0:
+        return
+    import oracle
+    import suminc_gb300 as sg
+    n = 1 << args.scale
+    E = n * args.edge_factor
+    bsz = int(round(E * args.batch_frac))
+    with sg.Context(D.local) as ctx:
+        ctx.generate_rmat(args.scale, E, seed=args.seed)
+        rp, col, _ = ctx.download_csr(weights=False)
+    hg = sg.HostGraph(rp, col)
+    # untimed: a few CPU rounds give a non-trivial starting state
+    x, delta, _ = oracle.ingress_pr(rp, col, max_rounds=args.cpu_sample_rounds)
+    cores = os.cpu_count() or 1
+    relax_t, time_t = 0, 0.0
+    cur = (rp, col)
+    for step in range(args.warmup + args.steps):
+        hg.gen_updates(bsz // 2, bsz - bsz // 2, 0, seed=1000 + step)
+        new = hg.csr()[:2]
+        relax, dt = cpu_sample(cur[0], cur[1], new[0], new[1], x, delta, args.cpu_sample_rounds)
+        cur = new
+        if step >= args.warmup:
+            relax_t += relax
+            time_t += dt
+    gteps = relax_t / time_t / 1e9
+    sample = (f"per step: AmendValue(-1/+1) over the full scale-{args.scale} graph "
+              f"({E} edges) + {args.cpu_sample_rounds} delta rounds, after one "
+              f"{bsz}-change batch; {args.steps} steps after {args.warmup} warm-up")
+    line = {
+        "metric": "GTEPS for PR incremental re-eval (IncEval)",
+        "value": round(gteps, 4), "unit": "GTEPS", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(time_t / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic R-MAT (seeded)", "impl": "reference",
+        "config": workload_config(args, n, E, bsz),
+        "cpu_baseline": {"value": round(gteps, 4), "unit": "GTEPS", "cores": cores,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(gteps, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, n, E, bsz):
+    return {"workload": f"incremental PageRank, R-MAT scale {args.scale}",
+            "vertices": n, "edges": E, "edge_factor": args.edge_factor,
+            "rmat_abcd": [0.57, 0.19, 0.19, 0.05], "damping": 0.85,
+            "termcheck_threshold": 1e-6, "batch_changes": bsz,
+            "batch_mix": "50% insert / 50% delete", "seed": args.seed,
+            "l2": "inputs larger than L2 (graph > 1 GB per direction), no flush",
+            "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU"}
+
+
+def run_ours(args, D: Dist):
+    import torch
+    import suminc_gb300 as sg
+
+    dev = D.local
+    n = 1 << args.scale
+    E = n * args.edge_factor
+    bsz = int(round(E * args.batch_frac))
+    ctx = sg.Context(dev)
+    ctx.generate_rmat(args.scale, E, seed=args.seed)
+    ctx.pr_peval(out=False)
+    peval_stats = ctx.stats()
+    rp0, col0, _ = ctx.download_csr(weights=False)
+    hg = sg.HostGraph(rp0, col0)
+    del rp0, col0
+    K, W = args.steps, args.warmup
+    P = 2  # profiled steps for the per-kernel roofline
+    batches = make_batches(hg, W + 2 * K + P, bsz, 100)
+    # device-resident copies for `value`, pinned host copies for `e2e`
+    dev_b = [torch.from_numpy(b.view(np.uint8)).to(f"cuda:{dev}") for b in batches[: W + K]]
+    pin_b = [torch.from_numpy(b.view(np.uint8)).pin_memory() for b in batches[W + K: W + 2 * K]]
+    out_pin = torch.empty(n, dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize(dev)
+
+    clocks = Clocks(dev, not args.no_clocks)
+    # warm-up
+    for i in range(W):
+        ctx.apply_updates_ptr(bsz, dev_b[i].data_ptr(), True)
+        ctx.pr_inceval_into(None)
+    # timed: device-resident batches
+    ctx.reset_stats()
+    D.barrier()
+    ctx.synchronize()
+    ctx.record_event(0)
+    relax = 0
+    rounds = []
+    for i in range(W, W + K):
+        ctx.apply_updates_ptr(bsz, dev_b[i].data_ptr(), True)
+        ctx.pr_inceval_into(None)
+        st = ctx.stats()
+        relax += st["edges_relaxed"]
+        rounds.append(st["rounds"])
+    ctx.record_event(1)
+    ctx.synchronize()
+    D.barrier()
+    t_ms = ctx.elapsed_ms(0, 1)
+    launches = ctx.stats()["launches_total"]
+    t_ms_max = D.max(t_ms)
+    relax_all = D.sum(relax)
+    value = relax_all / (t_ms_max * 1e-3) / 1e9
+
+    # timed: end to end through the C ABI with pinned host buffers
+    D.barrier()
+    ctx.synchronize()
+    ctx.record_event(2)
+    relax_e = 0
+    for i in range(K):
+        ctx.apply_updates_ptr(bsz, pin_b[i].data_ptr(), False)
+        ctx.pr_inceval_into(out_pin.data_ptr())
+        relax_e += ctx.stats()["edges_relaxed"]
+    ctx.record_event(3)
+    ctx.synchronize()
+    D.barrier()
+    te_ms = D.max(ctx.elapsed_ms(2, 3))
+    e2e = D.sum(relax_e) / (te_ms * 1e-3) / 1e9
+    clk = clocks.stop()
+
+    # profiled steps: the same work with CUDA events around every kernel of
+    # the PageRank classes; gives the per-launch duration of the dominant one
+    ctx.set_profile(0xFF)
+    ctx.reset_stats()
+    pe_pull = pe_push = 0
+    m_live = []
+    for i in range(W + 2 * K, W + 2 * K + P):
+        ctx.apply_updates(batches[i])
+        ctx.pr_inceval_into(None)
+        st = ctx.stats()
+        pe_pull += st["edges_pull"]
+        pe_push += st["edges_push"]
+        m_live.append(st["live_edges"])
+    st = ctx.stats()
+    ctx.set_profile(0)
+    kms, kl = st["kernel_ms"], st["kernel_launches"]
+    total_k = sum(kms.values()) or 1.0
+    kernels = {k: {"launches": kl[k], "ms": round(kms[k], 4), "share": round(kms[k] / total_k, 4)}
+               for k in kms if kl[k]}
+    dom = max(kernels, key=lambda k: kernels[k]["ms"])
+    avg_ms = kms[dom] / kl[dom]
+    if dom == "pr_pull":
+        bytes_per_launch = BYTES_PER_RELAXED_EDGE * pe_pull / kl[dom]
+    elif dom == "pr_push":
+        bytes_per_launch = BYTES_PER_RELAXED_EDGE * pe_push / kl[dom]
+    else:
+        bytes_per_launch = BYTES_PER_VERTEX_VISIT * n
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "traffic": None, "avg_launch_ms": round(avg_ms, 4),
+                "algorithmic_bytes_per_launch": int(bytes_per_launch),
+                "kernels": kernels}
+
+    cpu = None
+    if not args.no_cpu_baseline and D.rank == 0:
+        x = ctx.pr_values()
+        delta = ctx.pr_deltas()
+        old = hg.csr()[:2]
+        hg.gen_updates(bsz // 2, bsz - bsz // 2, 0, seed=99999)
+        new = hg.csr()[:2]
+        relax_c, dt = cpu_sample(old[0], old[1], new[0], new[1], x, delta, args.cpu_sample_rounds)
+        cpu = {"value": round(relax_c / dt / 1e9, 4), "unit": "GTEPS",
+               "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": (f"one IncEval sample on the host: AmendValue(-1/+1) over the full "
+                          f"scale-{args.scale} graph + {args.cpu_sample_rounds} delta rounds "
+                          f"after a {bsz}-change batch ({dt:.1f} s)")}
+    ctx.close()
+
+    result = {
+        "metric": "GTEPS for PR incremental re-eval (IncEval)",
+        "value": round(value, 4), "unit": "GTEPS", "n_gpus": D.ws,
+        "steps": K, "warmup": W, "ms_per_step": round(t_ms_max / K, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic R-MAT (seeded), random update batches",
+        "config": workload_config(args, n, E, bsz),
+        "e2e": {"value": round(e2e, 4), "unit": "GTEPS",
+                "h2d_bytes_per_step": int(bsz * 16), "d2h_bytes_per_step": int(n * 4),
+                "ms_per_step": round(te_ms / K, 4)},
+        "gpu_launches": int(launches),
+        "rounds_per_step": rounds,
+        "relaxations_per_step": int(relax / K),
+        "graph_gteps": round(E * K / (t_ms_max * 1e-3) / 1e9, 4),
+        "peval": {"rounds": peval_stats["rounds"], "ms": round(peval_stats["elapsed_ms"], 3)},
+        "roofline": roofline,
+    }
+    if cpu:
+        result["cpu_baseline"] = cpu
+    if clk:
+        result["clocks"] = clk
+    return result, hg, batches, None
+
+
+def main():
+    args = parse()
+    D = Dist()
+    if args.impl == "reference":
+        run_reference(args, D)
+        return
+    result, hg, batches, _ = run_ours(args, D)
+    if D.rank == 0:
+        print(json.dumps(result), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -60,7 +60,8 @@ typedef struct sg_options {
   int32_t max_node_num;       /* FLAGS_max_node_num (cluster size cap)       */
   int32_t min_node_num;       /* FLAGS_min_node_num (smallest cluster kept)  */
   int32_t mirror_k;           /* FLAGS_mirror_k (mirror creation threshold)  */
-  int32_t profile;            /* 1: time every kernel launch with events     */
+  int32_t profile;            /* bitmask of kernel classes to time with CUDA
+                                 events (0xFF = all); resolved per call      */
   double compress_threshold;  /* FLAGS_compress_threshold (benefit bound)    */
   double sssp_delta;          /* delta-stepping bucket width, 0 = automatic  */
   double slack;               /* extra adjacency capacity per vertex (0.125) */
@@ -81,6 +82,9 @@ typedef struct sg_stats {
   uint64_t kernel_launches[8];
   uint64_t live_edges;      /* current edge count                            */
   uint64_t reset_vertices;  /* SSSP IncEval: vertices reset by deletions     */
+  uint64_t launches_total;  /* kernels launched by the library since reset   */
+  uint64_t edges_pull;      /* relaxations done by dense pull rounds         */
+  uint64_t edges_push;      /* relaxations done by sparse push rounds        */
 } sg_stats;
 
 /* kernel classes reported in sg_stats.kernel_ms / kernel_launches */
@@ -114,6 +118,18 @@ const char* sg_last_error(const sg_ctx* ctx);
 /* Runs subsequent work of this context on `stream` (a cudaStream_t). */
 sg_status sg_ctx_set_stream(sg_ctx* ctx, void* stream);
 sg_status sg_get_stats(const sg_ctx* ctx, sg_stats* out);
+
+/* Clears the counters of sg_get_stats (kernel times, launches). */
+sg_status sg_reset_stats(sg_ctx* ctx);
+
+/* Device-side timing on the context's stream: record event `slot` (0..7),
+ * then read the milliseconds between two recorded slots. */
+sg_status sg_ctx_record_event(sg_ctx* ctx, int slot);
+sg_status sg_ctx_elapsed_ms(sg_ctx* ctx, int a, int b, double* ms);
+sg_status sg_ctx_synchronize(sg_ctx* ctx);
+
+/* Changes sg_options.profile (kernel classes timed with CUDA events). */
+sg_status sg_ctx_set_profile(sg_ctx* ctx, int32_t mask);
 
 /* ------------------------------------------------------------------ graph */
 
@@ -152,6 +168,9 @@ sg_status sg_graph_download_csr(sg_ctx* ctx, uint64_t* row_ptr, uint32_t* col,
  * Semantics follow the reference: an add of an existing pair replaces it,
  * duplicate adds keep the first, deletes of absent edges are ignored. */
 sg_status sg_apply_updates(sg_ctx* ctx, uint64_t count, const sg_update* upd);
+
+/* Same as sg_apply_updates with the batch already in device memory. */
+sg_status sg_apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* dptr);
 
 /* ------------------------------------------------------------- PageRank */
 

@@ -15,8 +15,8 @@
  *                      reference's cilk_for; the float accumulate is an
  *                      atomic add like grape/utils/atomic_ops.h:172-179.
  *   or_pr_amend        AmendValue(-1) on the old graph followed by
- *                      AmendValue(+1) on the new one
- *                      (sum_sync_iter_worker.h:139-180, :289, :341).
+ *                      AmendValue(+1) on the new one, every vertex, on all
+ *                      threads (sum_sync_iter_worker.h:139-180, :289, :341).
  *   or_pr_fixed_point  FP64 Jacobi solve of x = (1-d)/N + d * P^T x with
  *                      dangling rows dropped (the fixed point the delta
  *                      iteration converges to), iterated to a tolerance.
@@ -143,12 +143,14 @@ void or_pr_amend(uint32_t n, const uint64_t* rp_old, const uint32_t* col_old,
     const uint64_t* rp = pass == 0 ? rp_old : rp_new;
     const uint32_t* col = pass == 0 ? col_old : col_new;
     const float sign = pass == 0 ? -1.f : 1.f;
-    for (uint32_t u = 0; u < n; ++u) {
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t i = 0; i < (int64_t)n; ++i) {
+      const uint32_t u = (uint32_t)i;
       const float dl = sign * x[u];
       const uint64_t deg = rp[u + 1] - rp[u];
       if (dl == 0.f || deg == 0) continue;
       const float outv = dl * d / (float)deg;
-      for (uint64_t e = rp[u]; e < rp[u + 1]; ++e) delta[col[e]] += outv;
+      for (uint64_t e = rp[u]; e < rp[u + 1]; ++e) atomic_add_f32(&delta[col[e]], outv);
     }
   }
 }

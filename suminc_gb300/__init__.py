@@ -79,6 +79,9 @@ class Stats(C.Structure):
         ("kernel_launches", C.c_uint64 * 8),
         ("live_edges", C.c_uint64),
         ("reset_vertices", C.c_uint64),
+        ("launches_total", C.c_uint64),
+        ("edges_pull", C.c_uint64),
+        ("edges_push", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:
@@ -108,6 +111,12 @@ _SIGS = {
     "sg_graph_num_edges": ([_P, C.POINTER(C.c_uint64)], C.c_int),
     "sg_graph_download_csr": ([_P, _P, _P, _P], C.c_int),
     "sg_apply_updates": ([_P, C.c_uint64, _P], C.c_int),
+    "sg_apply_updates_device": ([_P, C.c_uint64, _P], C.c_int),
+    "sg_reset_stats": ([_P], C.c_int),
+    "sg_ctx_record_event": ([_P, C.c_int], C.c_int),
+    "sg_ctx_elapsed_ms": ([_P, C.c_int, C.c_int, C.POINTER(C.c_double)], C.c_int),
+    "sg_ctx_synchronize": ([_P], C.c_int),
+    "sg_ctx_set_profile": ([_P, C.c_int32], C.c_int),
     "sg_pr_peval": ([_P, _P], C.c_int),
     "sg_pr_inceval": ([_P, _P], C.c_int),
     "sg_pr_values": ([_P, _P], C.c_int),
@@ -241,6 +250,32 @@ class Context:
     def apply_updates(self, upd: np.ndarray):
         upd = np.ascontiguousarray(upd, dtype=UPDATE_DTYPE)
         _check(self._lib.sg_apply_updates(self._h, len(upd), _ptr(upd)), self, "sg_apply_updates")
+
+    def apply_updates_ptr(self, count: int, ptr: int, on_device: bool):
+        """Batch given as a raw pointer (pinned host or device memory)."""
+        fn = self._lib.sg_apply_updates_device if on_device else self._lib.sg_apply_updates
+        _check(fn(self._h, count, C.c_void_p(ptr)), self, "apply_updates_ptr")
+
+    def pr_inceval_into(self, out_ptr: int | None):
+        _check(self._lib.sg_pr_inceval(self._h, None if out_ptr is None else C.c_void_p(out_ptr)),
+               self, "sg_pr_inceval")
+
+    def record_event(self, slot: int):
+        _check(self._lib.sg_ctx_record_event(self._h, slot), self, "sg_ctx_record_event")
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        v = C.c_double()
+        _check(self._lib.sg_ctx_elapsed_ms(self._h, a, b, C.byref(v)), self, "sg_ctx_elapsed_ms")
+        return v.value
+
+    def set_profile(self, mask: int):
+        _check(self._lib.sg_ctx_set_profile(self._h, mask), self, "sg_ctx_set_profile")
+
+    def synchronize(self):
+        _check(self._lib.sg_ctx_synchronize(self._h), self, "sg_ctx_synchronize")
+
+    def reset_stats(self):
+        _check(self._lib.sg_reset_stats(self._h), self, "sg_reset_stats")
 
     # -- PageRank ---------------------------------------------------------
     def pr_peval(self, out=True):

@@ -23,18 +23,52 @@ sg_status cuda_fail(sg_ctx* ctx, cudaError_t e, const char* where) {
   return fail(ctx, e == cudaErrorMemoryAllocation ? SG_ERR_OOM : SG_ERR_CUDA, m);
 }
 
+// Profiling records an event pair around each launch of a kernel class and
+// resolves the pairs after the API call's final synchronisation, so the
+// launches stay asynchronous.  The bitmask opt.profile selects classes
+// (bit k = class k; any non-zero value below 256 enables the listed ones).
 void kprof_begin(sg_ctx* ctx) {
-  if (ctx->opt.profile) cudaEventRecord(ctx->kev0, ctx->stream);
+  count_launch(ctx);
+  if (!ctx->opt.profile) return;
+  if (ctx->kused + 2 > ctx->kpool.size()) {
+    if (ctx->kpool.size() >= 8192) {
+      cudaStreamSynchronize(ctx->stream);
+      kprof_flush(ctx);
+    } else {
+      const size_t old = ctx->kpool.size();
+      const size_t want = old ? old * 2 : 256;
+      ctx->kpool.resize(want, nullptr);
+      ctx->kclass.resize(want / 2, -1);
+      for (size_t i = old; i < want; ++i) cudaEventCreate(&ctx->kpool[i]);
+    }
+  }
+  cudaEventRecord(ctx->kpool[ctx->kused], ctx->stream);
+  ctx->kopen = (int)ctx->kused;
 }
 
 void kprof_end(sg_ctx* ctx, int klass) {
-  if (!ctx->opt.profile) return;
-  cudaEventRecord(ctx->kev1, ctx->stream);
-  cudaEventSynchronize(ctx->kev1);
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, ctx->kev0, ctx->kev1);
-  ctx->stats.kernel_ms[klass] += ms;
-  ctx->stats.kernel_launches[klass] += 1;
+  if (!ctx->opt.profile || ctx->kopen < 0) return;
+  if (!(ctx->opt.profile & (1 << klass)) && ctx->opt.profile != 0xFF) {
+    ctx->kopen = -1;  // class not selected: drop the begin event
+    return;
+  }
+  cudaEventRecord(ctx->kpool[ctx->kused + 1], ctx->stream);
+  ctx->kclass[ctx->kused / 2] = klass;
+  ctx->kused += 2;
+  ctx->kopen = -1;
+}
+
+void kprof_flush(sg_ctx* ctx) {
+  for (size_t i = 0; i + 1 < ctx->kused; i += 2) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx->kpool[i], ctx->kpool[i + 1]) == cudaSuccess) {
+      const int k = ctx->kclass[i / 2];
+      ctx->stats.kernel_ms[k] += ms;
+      ctx->stats.kernel_launches[k] += 1;
+    }
+  }
+  cudaGetLastError();
+  ctx->kused = 0;
 }
 
 }  // namespace sg
@@ -125,6 +159,10 @@ sg_status sg_ctx_destroy(sg_ctx* ctx) {
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->kev0) cudaEventDestroy(ctx->kev0);
   if (ctx->kev1) cudaEventDestroy(ctx->kev1);
+  for (auto e : ctx->kpool)
+    if (e) cudaEventDestroy(e);
+  for (auto e : ctx->user_ev)
+    if (e) cudaEventDestroy(e);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return SG_OK;
@@ -147,6 +185,50 @@ sg_status sg_ctx_set_stream(sg_ctx* ctx, void* stream) {
 sg_status sg_get_stats(const sg_ctx* ctx, sg_stats* out) {
   if (!ctx || !out) return SG_ERR_INVALID;
   *out = ctx->stats;
+  out->launches_total = ctx->launches;
+  return SG_OK;
+}
+
+sg_status sg_ctx_record_event(sg_ctx* ctx, int slot) {
+  SG_GUARD(ctx);
+  if (slot < 0 || slot >= 8) return fail(ctx, SG_ERR_INVALID, "event slot out of range");
+  if (!ctx->user_ev[slot]) SG_CUDA(ctx, cudaEventCreate(&ctx->user_ev[slot]));
+  SG_CUDA(ctx, cudaEventRecord(ctx->user_ev[slot], ctx->stream));
+  return SG_OK;
+}
+
+sg_status sg_ctx_elapsed_ms(sg_ctx* ctx, int a, int b, double* ms) {
+  SG_GUARD(ctx);
+  if (a < 0 || a >= 8 || b < 0 || b >= 8 || !ms || !ctx->user_ev[a] || !ctx->user_ev[b])
+    return fail(ctx, SG_ERR_INVALID, "bad event slots");
+  SG_CUDA(ctx, cudaEventSynchronize(ctx->user_ev[b]));
+  float f = 0.f;
+  SG_CUDA(ctx, cudaEventElapsedTime(&f, ctx->user_ev[a], ctx->user_ev[b]));
+  *ms = f;
+  return SG_OK;
+}
+
+sg_status sg_ctx_set_profile(sg_ctx* ctx, int32_t mask) {
+  SG_GUARD(ctx);
+  cudaStreamSynchronize(ctx->stream);
+  kprof_flush(ctx);
+  ctx->opt.profile = mask;
+  return SG_OK;
+}
+
+sg_status sg_ctx_synchronize(sg_ctx* ctx) {
+  SG_GUARD(ctx);
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+sg_status sg_reset_stats(sg_ctx* ctx) {
+  if (!ctx) return SG_ERR_INVALID;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  kprof_flush(ctx);
+  std::memset(&ctx->stats, 0, sizeof(ctx->stats));
+  ctx->launches = 0;
   return SG_OK;
 }
 
@@ -199,7 +281,19 @@ sg_status sg_graph_download_csr(sg_ctx* ctx, uint64_t* row_ptr, uint32_t* col, f
 sg_status sg_apply_updates(sg_ctx* ctx, uint64_t count, const sg_update* upd) {
   SG_GUARD(ctx);
   try {
-    return apply_updates_device(ctx, count, upd);
+    sg_status st = apply_updates_device(ctx, count, upd, false);
+    kprof_flush(ctx);
+    return st;
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* dptr) {
+  SG_GUARD(ctx);
+  try {
+    sg_status st = apply_updates_device(ctx, count, dptr, true);
+    kprof_flush(ctx);
+    return st;
   }
   SG_CATCH(ctx)
 }
@@ -218,6 +312,7 @@ sg_status sg_pr_peval(sg_ctx* ctx, float* out) {
     sg_status st = pr_alloc(ctx);
     if (st != SG_OK) return st;
     st = pr_run(ctx, false);
+    kprof_flush(ctx);
     if (st != SG_OK && st != SG_ERR_NOT_CONVERGED) return st;
     sg_status c = copy_out_f32(ctx, ctx->pr.x, out);
     return c != SG_OK ? c : st;
@@ -229,6 +324,7 @@ sg_status sg_pr_inceval(sg_ctx* ctx, float* out) {
   SG_GUARD(ctx);
   try {
     sg_status st = pr_run(ctx, true);
+    kprof_flush(ctx);
     if (st != SG_OK && st != SG_ERR_NOT_CONVERGED) return st;
     sg_status c = copy_out_f32(ctx, ctx->pr.x, out);
     return c != SG_OK ? c : st;
@@ -260,7 +356,9 @@ sg_status sg_pr_values_device(sg_ctx* ctx, const float** dptr) {
 sg_status sg_sssp_peval(sg_ctx* ctx, uint32_t source, double* out) {
   SG_GUARD(ctx);
   try {
-    SG_TRY(sssp_run_peval(ctx, source));
+    sg_status st = sssp_run_peval(ctx, source);
+    kprof_flush(ctx);
+    if (st != SG_OK) return st;
     if (out) return sssp_download(ctx, out);
     return SG_OK;
   }
@@ -270,7 +368,9 @@ sg_status sg_sssp_peval(sg_ctx* ctx, uint32_t source, double* out) {
 sg_status sg_sssp_inceval(sg_ctx* ctx, double* out) {
   SG_GUARD(ctx);
   try {
-    SG_TRY(sssp_run_inceval(ctx));
+    sg_status st = sssp_run_inceval(ctx);
+    kprof_flush(ctx);
+    if (st != SG_OK) return st;
     if (out) return sssp_download(ctx, out);
     return SG_OK;
   }

@@ -135,6 +135,13 @@ struct sg_ctx {
   std::string err;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t kev0 = nullptr, kev1 = nullptr;
+  cudaEvent_t user_ev[8] = {};  // caller-visible timing events on the stream
+  // kernel-class profiler: event pairs resolved after the call's final sync
+  std::vector<cudaEvent_t> kpool;
+  std::vector<int> kclass;
+  size_t kused = 0;
+  int kopen = -1;
+  uint64_t launches = 0;  // kernels launched by the library (all classes)
   void* cub_tmp = nullptr;
   size_t cub_tmp_bytes = 0;
   int num_sms = 0;
@@ -181,6 +188,8 @@ sg_status ensure_cub_tmp(sg_ctx* ctx, size_t bytes);
 // kernel-class timing (active when opt.profile != 0)
 void kprof_begin(sg_ctx* ctx);
 void kprof_end(sg_ctx* ctx, int klass);
+void kprof_flush(sg_ctx* ctx);  // after a stream sync: accumulate durations
+inline void count_launch(sg_ctx* ctx, uint64_t k = 1) { ctx->launches += k; }
 
 // graph.cu
 sg_status graph_free(sg_ctx* ctx);
@@ -189,7 +198,7 @@ sg_status graph_build_from_sorted_keys(sg_ctx* ctx, uint32_t n, uint64_t m,
                                        bool weighted);
 sg_status graph_rebuild_worklists(sg_ctx* ctx);
 sg_status apply_updates_device(sg_ctx* ctx, uint64_t count,
-                               const sg_update* host_upd);
+                               const sg_update* upd, bool on_device);
 
 // pagerank.cu
 sg_status pr_free(sg_ctx* ctx);

@@ -722,7 +722,7 @@ __global__ void __launch_bounds__(256) k_apply_dir(ApplyDirArgs A) {
       // PageRank: retract x_u over the old adjacency and re-issue it over the
       // new one (AmendValue(-1) / AmendValue(+1) restricted to u; for every
       // other vertex the two cancel).
-      if (A.pr_x && d0 != d1) {
+      if (A.pr_x && (ndel > 0 || nins > 0)) {
         const float xu = A.pr_x[u];
         if (xu != 0.f) {
           const float sub = d0 > 0 ? A.damping * xu / (float)d0 : 0.f;
@@ -872,20 +872,23 @@ static sg_status make_groups(sg_ctx* ctx, const uint32_t* vtx, const uint32_t* p
   return SG_OK;
 }
 
-sg_status apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* host_upd) {
+sg_status apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* upd,
+                               bool on_device) {
   DevGraph& g = ctx->g;
   DevBatch& B = ctx->batch;
   if (!g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
   if (count == 0) return SG_OK;
-  if (!host_upd) return fail(ctx, SG_ERR_INVALID, "null update array");
+  if (!upd) return fail(ctx, SG_ERR_INVALID, "null update array");
   if (count >= (1ull << 31)) return fail(ctx, SG_ERR_INVALID, "batch too large");
   SG_TRY(batch_reserve(ctx, count));
-  SG_CUDA(ctx, cudaMemcpyAsync(B.raw, host_upd, sizeof(sg_update) * count,
-                               cudaMemcpyHostToDevice, ctx->stream));
+  SG_CUDA(ctx, cudaMemcpyAsync(B.raw, upd, sizeof(sg_update) * count,
+                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               ctx->stream));
   uint32_t* d_err = (uint32_t*)B.d_count + 2;  // words 2..3 of the scalar block
   unsigned long long* d_dm = (unsigned long long*)B.d_count + 2;
   SG_CUDA(ctx, cudaMemsetAsync(B.d_count, 0, 32, ctx->stream));
   k_upd_keys<<<grid_for(count, 256), 256, 0, ctx->stream>>>(B.raw, count, g.n, B.key, B.val, d_err);
+  count_launch(ctx, 3);
   SG_TRY(sort_pairs(ctx, B.key, B.key2, B.val, B.val2, count));
   // run starts
   uint8_t* flags = (uint8_t*)B.key;  // key no longer needed
@@ -898,6 +901,7 @@ sg_status apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* hos
   SG_CUDA(ctx, cudaMemcpyAsync(&h_err, d_err, 4, cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (h_err) return fail(ctx, SG_ERR_INVALID, "update with vertex id >= n or bad op");
+  count_launch(ctx, 4);
   k_make_actions<<<grid_for(n_runs, 256), 256, 0, ctx->stream>>>(
       B.key2, B.val2, B.grp_begin, n_runs, count, B.raw, B.a_src, B.a_dst, B.a_w, B.a_kind,
       B.a_found);
@@ -936,6 +940,7 @@ sg_status apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* hos
   I.a_nbr = B.a_src;
   I.out_dir = false;
   I.pr_x = nullptr; I.pr_delta = nullptr; I.sp_parent = nullptr;
+  count_launch(ctx, 8);  // group and sort kernels above
   k_apply_dir<<<grid_for(B.n_igrp * 32, 256), 256, 0, ctx->stream>>>(I);
   kprof_end(ctx, SG_K_APPLY);
   SG_CUDA(ctx, cudaGetLastError());

@@ -32,7 +32,7 @@ enum {
   M_NOTCONV = 7,
   M_WORDS = 8
 };
-enum { C_EDGES = 0, C_VISITS = 1, C_FEDGES = 2, C_WORDS = 4 };
+enum { C_EDGES = 0, C_VISITS = 1, C_FEDGES = 2, C_PUSHED = 3, C_WORDS = 4 };
 
 struct PrRoundArgs {
   uint32_t n;
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(VT) k_pr_vertex(PrRoundArgs A, int round) {
     else mode = 0;
     A.misc[M_MODE] = mode;
     if (mode == 0) A.cnt[C_EDGES] += A.live_edges;
-    else if (mode == 1) A.cnt[C_EDGES] += fe;
+    else if (mode == 1) A.cnt[C_PUSHED] += fe;
     if (R < A.tau || fe == 0) A.misc[M_PENDING] = 1;
     if ((int)rounds >= A.max_rounds && !(R < A.tau)) {
       A.misc[M_PENDING] = 1;
@@ -378,7 +378,9 @@ sg_status pr_run(sg_ctx* ctx, bool inc) {
   ctx->stats.rounds = (int32_t)h_misc[M_ROUNDS];
   ctx->stats.converged = h_misc[M_NOTCONV] ? 0 : 1;
   ctx->stats.residual = h_res[0];
-  ctx->stats.edges_relaxed = h_cnt[C_EDGES];
+  ctx->stats.edges_relaxed = h_cnt[C_EDGES] + h_cnt[C_PUSHED];
+  ctx->stats.edges_pull = h_cnt[C_EDGES];
+  ctx->stats.edges_push = h_cnt[C_PUSHED];
   ctx->stats.vertex_visits = h_cnt[C_VISITS];
   ctx->stats.elapsed_ms = ms;
   ctx->stats.live_edges = g.m;
