@@ -195,6 +195,45 @@ sg_status sg_pr_deltas(sg_ctx* ctx, float* out);
 /* Device pointer to the values (valid until the next call on ctx). */
 sg_status sg_pr_values_device(sg_ctx* ctx, const float** dptr);
 
+/* ------------------------------------------------------ summarized graph */
+
+/* Counters of the summarized graph (the quantities the reference logs while
+ * building it: CompressorBase::statistic, compressor_base.h:431-519, and
+ * sketch2csr_mirror, :4636-4880). */
+typedef struct sg_summary_info {
+  uint64_t clusters;          /* kept clusters (supernode_ids)               */
+  uint64_t supernodes;        /* one per entry vertex and in-mirror          */
+  uint64_t cluster_members;   /* members incl. absorbed vertices             */
+  uint64_t sources;           /* entry vertices                               */
+  uint64_t bound_nodes;       /* exit vertices                                */
+  uint64_t bound_index;       /* shortcut weights entry -> exit / out-mirror */
+  uint64_t inner_index;       /* residual shortcuts (inner_delta)             */
+  uint64_t inner_value_index; /* value shortcuts (inner_value)                */
+  uint64_t all_rows;          /* vertices + mirror rows                       */
+  uint64_t absorbed;          /* unclustered mirror candidates absorbed       */
+  uint64_t in_mirrors;
+  uint64_t out_mirrors;
+  uint64_t sync_edges;        /* master <-> mirror edges                      */
+  uint64_t boundary_edges;    /* ib_e: exit -> outside, unclustered edges     */
+  uint64_t shortcut_edges;    /* is_e: entry -> exit shortcuts                */
+  uint64_t node_type_count[7];/* NodeType 0..6 (grape/types.h:70-78)          */
+} sg_summary_info;
+
+/* Builds the summarized graph from a clustering (the cluster file records
+ * of compress_by_cluster, compressor_base.h:3160-3250): cluster i =
+ * members[cluster_ptr[i] .. cluster_ptr[i+1]).  Applies the reference's
+ * benefit filter and mirror choice (get_init_supernode_by_clusters, :3253),
+ * absorbs unclustered mirror candidates (final_build_supernode, :3616),
+ * marks exits (judge_out_bound_node, :3924), builds cluster subgraphs
+ * (:3786), computes every supernode's shortcuts on the device
+ * (build_iter_index_mirror, iter_compressor.h:318-491), node types (:4144)
+ * and the sketch CSRs (:4636).  With options.compress = 1, PEval and IncEval
+ * then run the summarized rounds (sum_sync_iter_worker.h:949-1492) before
+ * the plain ones. */
+sg_status sg_summary_build(sg_ctx* ctx, uint32_t n_clusters, const uint32_t* cluster_ptr,
+                           const uint32_t* members);
+sg_status sg_summary_info_get(sg_ctx* ctx, sg_summary_info* out);
+
 /* ----------------------------------------------------------------- SSSP */
 
 /* Batch SSSP from `source` with FP64 distances over the edge weights
@@ -244,6 +283,20 @@ sg_status sg_hostgraph_gen_updates(sg_hostgraph* g, uint64_t n_ins,
                                    uint64_t n_del, uint64_t n_rew,
                                    uint64_t seed, int integer_weights,
                                    double wlo, double whi, sg_update* out);
+
+/* The in-repo greedy clustering used to produce the cluster file of the
+ * summarized graph: restates the reference's flag-default builder
+ * parallel_find_multi_source_supernode_2_sort_sample with one compress
+ * thread (grape/fragment/compressor_base.h:367-419, :1448-1875), drawing its
+ * candidate samples from a generator seeded by `seed` instead of
+ * std::random_device.  Output: cluster i = members[cluster_ptr[i] ..
+ * cluster_ptr[i+1]) (sorted); the caller provides cluster_ptr[n+1] and
+ * members[n]. */
+sg_status sg_util_greedy_clusters(uint32_t n, const uint64_t* row_ptr,
+                                  const uint32_t* col, int max_node_num,
+                                  int min_node_num, uint64_t seed,
+                                  uint32_t* cluster_ptr, uint32_t* members,
+                                  uint32_t* n_clusters);
 
 /* Packed copy of the mirror (rows sorted). */
 sg_status sg_hostgraph_num_edges(const sg_hostgraph* g, uint64_t* m);

@@ -65,6 +65,18 @@ class Options(C.Structure):
     ]
 
 
+class SummaryInfo(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in (
+        "clusters", "supernodes", "cluster_members", "sources", "bound_nodes", "bound_index",
+        "inner_index", "inner_value_index", "all_rows", "absorbed", "in_mirrors", "out_mirrors",
+        "sync_edges", "boundary_edges", "shortcut_edges")] + [("node_type_count", C.c_uint64 * 7)]
+
+    def as_dict(self) -> dict:
+        d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "node_type_count"}
+        d["node_type_count"] = [int(x) for x in self.node_type_count]
+        return d
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("rounds", C.c_int32),
@@ -134,6 +146,10 @@ _SIGS = {
                                   C.c_double, C.c_double, _P], C.c_int),
     "sg_hostgraph_num_edges": ([_P, C.POINTER(C.c_uint64)], C.c_int),
     "sg_hostgraph_csr": ([_P, _P, _P, _P], C.c_int),
+    "sg_summary_build": ([_P, C.c_uint32, _P, _P], C.c_int),
+    "sg_summary_info_get": ([_P, C.POINTER(SummaryInfo)], C.c_int),
+    "sg_util_greedy_clusters": ([C.c_uint32, _P, _P, C.c_int, C.c_int, C.c_uint64, _P, _P,
+                                 C.POINTER(C.c_uint32)], C.c_int),
 }
 
 _lib = None
@@ -298,6 +314,22 @@ class Context:
         _check(self._lib.sg_pr_deltas(self._h, _ptr(x)), self, "sg_pr_deltas")
         return x
 
+    # -- summarized graph -------------------------------------------------
+    def summary_build(self, clusters):
+        """clusters: list of member arrays (the cluster file's records)."""
+        cp = np.zeros(len(clusters) + 1, np.uint32)
+        for i, c in enumerate(clusters):
+            cp[i + 1] = cp[i] + len(c)
+        mem = (np.concatenate([np.asarray(c, np.uint32) for c in clusters])
+               if clusters else np.zeros(1, np.uint32))
+        _check(self._lib.sg_summary_build(self._h, len(clusters), _ptr(cp), _ptr(mem)), self,
+               "sg_summary_build")
+
+    def summary_info(self) -> dict:
+        info = SummaryInfo()
+        _check(self._lib.sg_summary_info_get(self._h, C.byref(info)), self, "sg_summary_info_get")
+        return info.as_dict()
+
     # -- SSSP -------------------------------------------------------------
     def sssp_peval(self, source=0, out=True):
         d = np.empty(self.n, np.float64) if out else None
@@ -330,6 +362,21 @@ def rmat_host(scale, edges, a=0.57, b=0.19, c=0.19, seed=1, weight_kind=0, wlo=1
     _check(lib.sg_util_rmat_host(scale, edges, a, b, c, seed, weight_kind, wlo, whi, _ptr(rp),
                                  _ptr(col), _ptr(w)), None, "sg_util_rmat_host")
     return rp, col, w
+
+
+def greedy_clusters(row_ptr, col, max_node_num=150, min_node_num=8, seed=1):
+    """In-repo greedy clustering; returns a list of sorted member arrays."""
+    lib = load_library()
+    row_ptr = np.ascontiguousarray(row_ptr, np.uint64)
+    col = np.ascontiguousarray(col, np.uint32)
+    n = len(row_ptr) - 1
+    cp = np.zeros(n + 1, np.uint32)
+    mem = np.zeros(max(n, 1), np.uint32)
+    k = C.c_uint32()
+    _check(lib.sg_util_greedy_clusters(n, _ptr(row_ptr), _ptr(col), max_node_num, min_node_num,
+                                       seed, _ptr(cp), _ptr(mem), C.byref(k)), None,
+           "sg_util_greedy_clusters")
+    return [mem[cp[i]:cp[i + 1]].copy() for i in range(k.value)]
 
 
 class HostGraph:

@@ -148,12 +148,15 @@ sg_status sg_ctx_destroy(sg_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   pr_free(ctx);
   sssp_free(ctx);
+  summary_free(ctx);
   graph_free(ctx);
   DevBatch& B = ctx->batch;
   dfree(B.raw); dfree(B.key); dfree(B.key2); dfree(B.val); dfree(B.val2);
   dfree(B.a_src); dfree(B.a_dst); dfree(B.a_w); dfree(B.a_kind); dfree(B.a_found);
   dfree(B.grp_vertex); dfree(B.grp_begin); dfree(B.grp_end); dfree(B.perm);
   dfree(B.igrp_vertex); dfree(B.igrp_begin); dfree(B.igrp_end); dfree(B.d_count);
+  dfree(B.a_pos_in); dfree(B.a_tmp); dfree(B.g_d0); dfree(B.g_ndel); dfree(B.g_nins);
+  dfree(B.chunk_off); dfree(B.nch);
   if (ctx->cub_tmp) cudaFree(ctx->cub_tmp);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -238,6 +241,7 @@ sg_status sg_graph_load_csr(sg_ctx* ctx, uint32_t n, const uint64_t* row_ptr,
   try {
     pr_free(ctx);
     sssp_free(ctx);
+    summary_free(ctx);
     return load_csr(ctx, n, row_ptr, col, w);
   }
   SG_CATCH(ctx)
@@ -253,6 +257,7 @@ sg_status sg_graph_generate_rmat(sg_ctx* ctx, int scale, uint64_t edges, double 
   try {
     pr_free(ctx);
     sssp_free(ctx);
+    summary_free(ctx);
     return generate_rmat(ctx, scale, edges, a, b, c, seed, weight_kind, wlo, whi);
   }
   SG_CATCH(ctx)
@@ -282,6 +287,7 @@ sg_status sg_apply_updates(sg_ctx* ctx, uint64_t count, const sg_update* upd) {
   SG_GUARD(ctx);
   try {
     sg_status st = apply_updates_device(ctx, count, upd, false);
+    if (st == SG_OK && ctx->opt.compress) st = summary_after_apply(ctx);
     kprof_flush(ctx);
     return st;
   }
@@ -292,6 +298,7 @@ sg_status sg_apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* 
   SG_GUARD(ctx);
   try {
     sg_status st = apply_updates_device(ctx, count, dptr, true);
+    if (st == SG_OK && ctx->opt.compress) st = summary_after_apply(ctx);
     kprof_flush(ctx);
     return st;
   }
@@ -311,7 +318,8 @@ sg_status sg_pr_peval(sg_ctx* ctx, float* out) {
     ctx->pr.valid = false;
     sg_status st = pr_alloc(ctx);
     if (st != SG_OK) return st;
-    st = pr_run(ctx, false);
+    if (ctx->opt.compress) st = pr_summarized(ctx, false);
+    else st = pr_run(ctx, false);
     kprof_flush(ctx);
     if (st != SG_OK && st != SG_ERR_NOT_CONVERGED) return st;
     sg_status c = copy_out_f32(ctx, ctx->pr.x, out);
@@ -323,7 +331,7 @@ sg_status sg_pr_peval(sg_ctx* ctx, float* out) {
 sg_status sg_pr_inceval(sg_ctx* ctx, float* out) {
   SG_GUARD(ctx);
   try {
-    sg_status st = pr_run(ctx, true);
+    sg_status st = ctx->opt.compress ? pr_summarized(ctx, true) : pr_run(ctx, true);
     kprof_flush(ctx);
     if (st != SG_OK && st != SG_ERR_NOT_CONVERGED) return st;
     sg_status c = copy_out_f32(ctx, ctx->pr.x, out);
@@ -351,6 +359,33 @@ sg_status sg_pr_values_device(sg_ctx* ctx, const float** dptr) {
   if (!ctx->pr.valid) return fail(ctx, SG_ERR_STATE, "no PageRank result");
   *dptr = ctx->pr.x;
   return SG_OK;
+}
+
+sg_status sg_summary_build(sg_ctx* ctx, uint32_t n_clusters, const uint32_t* cluster_ptr,
+                           const uint32_t* members) {
+  SG_GUARD(ctx);
+  if (n_clusters > 0 && (!cluster_ptr || !members))
+    return fail(ctx, SG_ERR_INVALID, "null cluster arrays");
+  try {
+    std::vector<std::vector<uint32_t>> cl(n_clusters);
+    for (uint32_t i = 0; i < n_clusters; ++i) {
+      if (cluster_ptr[i + 1] < cluster_ptr[i]) return fail(ctx, SG_ERR_INVALID, "cluster_ptr not monotone");
+      cl[i].assign(members + cluster_ptr[i], members + cluster_ptr[i + 1]);
+      for (uint32_t v : cl[i])
+        if (v >= ctx->g.n) return fail(ctx, SG_ERR_INVALID, "cluster member >= n");
+    }
+    pr_free(ctx);
+    sg_status st = summary_build(ctx, cl);
+    kprof_flush(ctx);
+    return st;
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_summary_info_get(sg_ctx* ctx, sg_summary_info* out) {
+  SG_GUARD(ctx);
+  if (!out) return fail(ctx, SG_ERR_INVALID, "null output");
+  return summary_info(ctx, out);
 }
 
 sg_status sg_sssp_peval(sg_ctx* ctx, uint32_t source, double* out) {

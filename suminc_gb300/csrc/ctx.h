@@ -38,11 +38,11 @@ struct DevGraph {
   uint64_t* in_qoff = nullptr;   // [n + 1]
   uint32_t in_nz_count = 0;
   uint64_t in_quads = 0;
-  // out-direction quad prefix over all vertices (push frontier uses its own)
-  uint32_t* out_nz = nullptr;
-  uint64_t* out_qoff = nullptr;
-  uint32_t out_nz_count = 0;
-  uint64_t out_quads = 0;
+  uint32_t* in_tile_v0 = nullptr;  // owner (index into in_nz) of each tile's first quad
+  uint64_t in_ntiles = 0;
+  uint64_t tile_cap = 0;
+  uint32_t* in_bnd = nullptr;      // vertices whose quads span tiles
+  uint32_t in_bnd_count = 0;
 };
 
 // Normalized update batch kept on the device between apply and IncEval.
@@ -69,8 +69,13 @@ struct DevBatch {
   uint32_t* igrp_begin = nullptr;
   uint32_t* igrp_end = nullptr;
   uint64_t n_igrp = 0;
-  void* cub_tmp = nullptr;
-  size_t cub_tmp_bytes = 0;
+  uint32_t* a_pos_in = nullptr;    // in-direction slot of each action's pair
+  uint32_t* a_tmp = nullptr;       // per-action scratch (hole lists)
+  uint32_t* g_d0 = nullptr;        // per group (out: [0,cap), in: [cap,2cap))
+  uint32_t* g_ndel = nullptr;
+  uint32_t* g_nins = nullptr;
+  uint32_t* chunk_off = nullptr;   // work-item prefix per direction
+  uint32_t* nch = nullptr;
   uint64_t* d_count = nullptr;     // device scalars
 };
 
@@ -106,9 +111,7 @@ struct SsspState {
   uint32_t* d_ctl = nullptr;      // control words of the persistent kernel
   unsigned long long* d_cnt = nullptr;
   double* out = nullptr;          // staging for FP64 output
-  uint32_t* padd_src = nullptr;   // edges added since the last run
-  uint32_t* padd_dst = nullptr;
-  float* padd_w = nullptr;
+  uint32_t* padd_dst = nullptr;   // heads of edges added since the last run
   uint64_t padd_cap = 0;
   uint64_t padd_bound = 0;        // host upper bound of the pending count
   uint32_t iter_base = 1;         // queue tags grow across launches
@@ -145,6 +148,7 @@ struct sg_ctx {
   void* cub_tmp = nullptr;
   size_t cub_tmp_bytes = 0;
   int num_sms = 0;
+  void* summary = nullptr;  // summary.cu: summarized graph (compress = 1)
 };
 
 namespace sg {
@@ -228,6 +232,14 @@ struct SsspAmendArgs {
 SsspAmendArgs sssp_amend_args(sg_ctx* ctx);
 sg_status sssp_collect_adds(sg_ctx* ctx);
 sg_status sssp_download(sg_ctx* ctx, double* out);
+
+// summary.cu
+sg_status summary_free(sg_ctx* ctx);
+sg_status summary_build(sg_ctx* ctx, const std::vector<std::vector<uint32_t>>& clusters);
+sg_status summary_after_apply(sg_ctx* ctx);
+sg_status pr_summarized(sg_ctx* ctx, bool inc);
+uint32_t summary_rows(sg_ctx* ctx);  // rows incl. mirrors, 0 without a summary
+sg_status summary_info(sg_ctx* ctx, sg_summary_info* out);
 
 // graph.cu entry points behind the C ABI
 sg_status generate_rmat(sg_ctx* ctx, int scale, uint64_t edges, double a, double b,

@@ -10,6 +10,9 @@
 
 namespace sg {
 
+// 4-edge quads per tile of the edge-balanced pull over the in-CSR
+constexpr uint32_t kPullTileQuads = 1024;
+
 // Blocks for a grid-stride loop over n items: at most 16 resident CTAs per
 // SM of the 152-SM part (the loop covers the rest).
 inline unsigned grid_for(uint64_t n, int threads, int max_blocks = 152 * 16) {

@@ -189,8 +189,8 @@ sg_status graph_free(sg_ctx* ctx) {
   csr_free(g.in);
   dfree(g.in_nz);
   dfree(g.in_qoff);
-  dfree(g.out_nz);
-  dfree(g.out_qoff);
+  dfree(g.in_tile_v0);
+  dfree(g.in_bnd);
   g = DevGraph();
   return SG_OK;
 }
@@ -260,8 +260,7 @@ sg_status graph_build_from_sorted_keys(sg_ctx* ctx, uint32_t n, uint64_t m,
   dfree(rw2);
   SG_TRY(dalloc(ctx, &g.in_nz, n));
   SG_TRY(dalloc(ctx, &g.in_qoff, (uint64_t)n + 1));
-  SG_TRY(dalloc(ctx, &g.out_nz, n));
-  SG_TRY(dalloc(ctx, &g.out_qoff, (uint64_t)n + 1));
+  SG_TRY(dalloc(ctx, &g.in_bnd, n));
   g.valid = true;
   return graph_rebuild_worklists(ctx);
 }
@@ -315,10 +314,48 @@ static sg_status worklist_dir(sg_ctx* ctx, const DevCSR& c, uint32_t* nz,
   return SG_OK;
 }
 
+__global__ void k_tile_v0(const uint64_t* __restrict__ qoff, uint32_t nz_count, uint64_t ntiles,
+                          uint32_t* __restrict__ tv0) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < ntiles;
+       t += (uint64_t)gridDim.x * blockDim.x)
+    tv0[t] = upper_owner(qoff, 0u, nz_count, t * (uint64_t)kPullTileQuads);
+}
+
+__global__ void k_bnd_flags(const uint64_t* __restrict__ qoff, uint32_t nz_count,
+                            uint8_t* __restrict__ f) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nz_count; i += gridDim.x * blockDim.x)
+    f[i] = (qoff[i] / kPullTileQuads) != ((qoff[i + 1] - 1) / kPullTileQuads);
+}
+
 sg_status graph_rebuild_worklists(sg_ctx* ctx) {
   DevGraph& g = ctx->g;
   SG_TRY(worklist_dir(ctx, g.in, g.in_nz, g.in_qoff, &g.in_nz_count, &g.in_quads));
-  SG_TRY(worklist_dir(ctx, g.out, g.out_nz, g.out_qoff, &g.out_nz_count, &g.out_quads));
+  g.in_ntiles = (g.in_quads + kPullTileQuads - 1) / kPullTileQuads;
+  if (g.in_ntiles + 1 > g.tile_cap) {
+    dfree(g.in_tile_v0);
+    g.tile_cap = g.in_ntiles + g.in_ntiles / 8 + 1024;
+    SG_TRY(dalloc(ctx, &g.in_tile_v0, g.tile_cap));
+  }
+  if (g.in_ntiles)
+    k_tile_v0<<<grid_for(g.in_ntiles, 256), 256, 0, ctx->stream>>>(g.in_qoff, g.in_nz_count,
+                                                                    g.in_ntiles, g.in_tile_v0);
+  // boundary vertices: in_nz entries whose quads cross a tile edge
+  uint8_t* flags = nullptr;
+  uint64_t* cnt = nullptr;
+  SG_TRY(dalloc(ctx, &flags, std::max<uint32_t>(g.in_nz_count, 1)));
+  SG_TRY(dalloc(ctx, &cnt, 1));
+  uint64_t h = 0;
+  if (g.in_nz_count) {
+    k_bnd_flags<<<grid_for(g.in_nz_count, 256), 256, 0, ctx->stream>>>(g.in_qoff, g.in_nz_count,
+                                                                        flags);
+    SG_TRY(select_flagged(ctx, g.in_nz, flags, g.in_bnd, cnt, g.in_nz_count));
+    SG_CUDA(ctx, cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  g.in_bnd_count = (uint32_t)h;
+  dfree(flags);
+  dfree(cnt);
+  count_launch(ctx, 8);
   return SG_OK;
 }
 
@@ -636,6 +673,8 @@ __global__ void k_inv_keys(const uint32_t* __restrict__ s, const uint32_t* __res
 }
 
 
+constexpr uint32_t kApplyChunk = 1024;  // segment entries per find / amend work item
+
 struct ApplyDirArgs {
   DevCSR c;
   const uint32_t* gv;     // group vertex
@@ -646,7 +685,14 @@ struct ApplyDirArgs {
   const uint32_t* a_nbr;  // neighbour id of each action in this direction
   const float* a_w;
   const uint32_t* a_kind;
-  uint32_t* a_found;      // out direction writes, in direction reads
+  const uint32_t* a_found;  // out-direction slot of the pair before the batch
+  uint32_t* a_pos;          // this direction's slot of the pair (written by find)
+  uint32_t* a_tmp;          // per-action scratch (hole list)
+  uint32_t* g_d0;           // degree before the batch
+  uint32_t* g_ndel;         // deletions of the group
+  uint32_t* g_nins;         // insertions of the group
+  const uint32_t* chunk_off;  // [n_grp + 1] work-item prefix
+  uint64_t n_chunks;
   bool out_dir;
   // PageRank amend (out direction; null when no PageRank state is live)
   float* pr_x;
@@ -678,35 +724,65 @@ __device__ __forceinline__ int find_action(const ApplyDirArgs& A, uint32_t b, ui
   return -1;
 }
 
-// One warp per vertex whose segment changes.  Action kinds: 1 = delete the
-// old edge, 2 = add, 3 = delete + add (weight change).  "found" = the pair
-// was present before the batch (decided by the out direction).
-__global__ void __launch_bounds__(256) k_apply_dir(ApplyDirArgs A) {
+// work items per group: ceil(d0 / chunk), at least one
+__global__ void k_apply_chunks(ApplyDirArgs A, uint32_t* nch) {
+  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g <= A.n_grp;
+       g += (uint64_t)gridDim.x * blockDim.x) {
+    if (g == A.n_grp) {
+      nch[g] = 0;
+      continue;
+    }
+    const uint32_t d0 = A.c.deg[A.gv[g]];
+    A.g_d0[g] = d0;
+    nch[g] = d0 == 0 ? 1u : (d0 + kApplyChunk - 1) / kApplyChunk;
+  }
+}
+
+__device__ __forceinline__ uint32_t group_of_chunk(const ApplyDirArgs& A, uint64_t c) {
+  uint32_t lo = 0, hi = (uint32_t)A.n_grp;  // largest g with chunk_off[g] <= c
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (A.chunk_off[mid] <= c) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// 1. locate every action's pair in its segment (one warp per 1024-entry
+//    chunk): record the slot, tombstone pure deletes, overwrite re-added
+//    weights.
+__global__ void __launch_bounds__(256) k_apply_find(ApplyDirArgs A) {
   const uint32_t lane = threadIdx.x & 31;
-  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t gi = warp; gi < A.n_grp; gi += nwarps) {
-    const uint32_t u = A.gv[gi];
-    const uint32_t b = A.gb[gi], e = A.ge[gi];
-    const uint32_t d0 = A.c.deg[u];
-    uint64_t base = A.c.off[u];
-    // phase 1: match segment entries against the group's actions
-    for (uint32_t k = lane; k < d0; k += 32) {
+  for (uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; c < A.n_chunks;
+       c += nwarps) {
+    const uint32_t g = group_of_chunk(A, c);
+    const uint32_t u = A.gv[g], b = A.gb[g], e = A.ge[g];
+    const uint32_t d0 = A.g_d0[g];
+    const uint64_t base = A.c.off[u];
+    const uint32_t k0 = (uint32_t)(c - A.chunk_off[g]) * kApplyChunk;
+    const uint32_t k1 = min(k0 + kApplyChunk, d0);
+    for (uint32_t k = k0 + lane; k < k1; k += 32) {
       const uint32_t t = A.c.col[base + k];
       const int j = find_action(A, b, e, t);
-      if (j >= 0) {
-        const uint32_t a = act_at(A, (uint32_t)j);
-        const uint32_t kind = A.a_kind[a];
-        if (A.out_dir) A.a_found[a] = k;
-        if (kind == 1u) {
-          A.c.col[base + k] = kInvalidVid;
-        } else if ((kind & 2u) && A.c.w) {
-          A.c.w[base + k] = A.a_w[a];
-        }
-      }
+      if (j < 0) continue;
+      const uint32_t a = act_at(A, (uint32_t)j);
+      const uint32_t kind = A.a_kind[a];
+      A.a_pos[a] = k;
+      if (kind == 1u) A.c.col[base + k] = kInvalidVid;
+      else if ((kind & 2u) && A.c.w) A.c.w[base + k] = A.a_w[a];
     }
-    __syncwarp();
-    // phase 2: deletions and insertions of this vertex
+  }
+}
+
+// 2. per vertex (warp per group, over its actions only): counts, the
+//    PageRank amend of deleted / inserted targets, SSSP reset seeds.
+__global__ void __launch_bounds__(256) k_apply_group(ApplyDirArgs A) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t g = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; g < A.n_grp;
+       g += nwarps) {
+    const uint32_t u = A.gv[g], b = A.gb[g], e = A.ge[g];
+    const uint32_t d0 = A.g_d0[g];
     uint32_t ndel = 0, nins = 0;
     for (uint32_t j = b + lane; j < e; j += 32) {
       const uint32_t a = act_at(A, j);
@@ -717,78 +793,139 @@ __global__ void __launch_bounds__(256) k_apply_dir(ApplyDirArgs A) {
     }
     ndel = __reduce_add_sync(0xffffffffu, ndel);
     nins = __reduce_add_sync(0xffffffffu, nins);
+    if (lane == 0) {
+      A.g_ndel[g] = ndel;
+      A.g_nins[g] = nins;
+    }
+    if (!A.out_dir) continue;
     const uint32_t d1 = d0 - ndel + nins;
-    if (A.out_dir) {
-      // PageRank: retract x_u over the old adjacency and re-issue it over the
-      // new one (AmendValue(-1) / AmendValue(+1) restricted to u; for every
-      // other vertex the two cancel).
-      if (A.pr_x && (ndel > 0 || nins > 0)) {
-        const float xu = A.pr_x[u];
-        if (xu != 0.f) {
-          const float sub = d0 > 0 ? A.damping * xu / (float)d0 : 0.f;
-          const float add = d1 > 0 ? A.damping * xu / (float)d1 : 0.f;
-          for (uint32_t j = b + lane; j < e; j += 32) {
-            const uint32_t a = act_at(A, j);
-            const uint32_t kind = A.a_kind[a];
-            const bool found = A.a_found[a] != kInvalidVid;
-            if (kind == 1u && found && sub != 0.f) atomicAdd(&A.pr_delta[A.a_nbr[a]], -sub);
-            if ((kind & 2u) && !found && add != 0.f) atomicAdd(&A.pr_delta[A.a_nbr[a]], add);
-          }
-          const float diff = add - sub;
-          if (diff != 0.f)
-            for (uint32_t k = lane; k < d0; k += 32) {
-              const uint32_t t = A.c.col[base + k];
-              if (t != kInvalidVid) atomicAdd(&A.pr_delta[t], diff);
-            }
-        }
-      }
-      // SSSP: a deleted (or re-weighted) edge that is the tree edge of its
-      // head resets the head (deltaCompute, sum_sync_traversal_worker.h:140-176)
-      if (A.sp_parent) {
+    // PageRank: AmendValue(-1) / AmendValue(+1) restricted to u (for every
+    // other vertex the two cancel); surviving edges are amended by
+    // k_apply_amend.
+    if (A.pr_x && (ndel > 0 || nins > 0)) {
+      const float xu = A.pr_x[u];
+      if (xu != 0.f) {
+        const float sub = d0 > 0 ? A.damping * xu / (float)d0 : 0.f;
+        const float add = d1 > 0 ? A.damping * xu / (float)d1 : 0.f;
         for (uint32_t j = b + lane; j < e; j += 32) {
           const uint32_t a = act_at(A, j);
-          if ((A.a_kind[a] & 1u) && A.a_found[a] != kInvalidVid) {
-            const uint32_t v = A.a_nbr[a];
-            if (A.sp_parent[v] == u && atomicExch(&A.sp_reset[v], 1u) == 0u)
-              A.sp_seeds[atomicAdd(A.sp_seed_count, 1u)] = v;
-          }
+          const uint32_t kind = A.a_kind[a];
+          const bool found = A.a_found[a] != kInvalidVid;
+          if (kind == 1u && found && sub != 0.f) atomicAdd(&A.pr_delta[A.a_nbr[a]], -sub);
+          if ((kind & 2u) && !found && add != 0.f) atomicAdd(&A.pr_delta[A.a_nbr[a]], add);
         }
       }
     }
-    __syncwarp();
-    // phase 3: compact the live entries to the segment head
-    uint32_t wp = 0;
-    for (uint32_t kb = 0; kb < d0; kb += 32) {
-      const uint32_t k = kb + lane;
-      uint32_t c = kInvalidVid;
-      float wv = 0.f;
-      if (k < d0) {
-        c = A.c.col[base + k];
-        if (A.c.w) wv = A.c.w[base + k];
+    // SSSP: a deleted (or re-weighted) edge that is the tree edge of its
+    // head resets the head (deltaCompute, sum_sync_traversal_worker.h:140-176)
+    if (A.sp_parent) {
+      for (uint32_t j = b + lane; j < e; j += 32) {
+        const uint32_t a = act_at(A, j);
+        if ((A.a_kind[a] & 1u) && A.a_found[a] != kInvalidVid) {
+          const uint32_t v = A.a_nbr[a];
+          if (A.sp_parent[v] == u && atomicExch(&A.sp_reset[v], 1u) == 0u)
+            A.sp_seeds[atomicAdd(A.sp_seed_count, 1u)] = v;
+        }
       }
-      const bool live = (k < d0) && c != kInvalidVid;
-      const uint32_t mask = __ballot_sync(0xffffffffu, live);
-      const uint32_t pos = wp + __popc(mask & lanemask_lt());
-      __syncwarp();
-      if (live) {
-        A.c.col[base + pos] = c;
-        if (A.c.w) A.c.w[base + pos] = wv;
+    }
+    if (lane == 0) atomicAdd(A.d_dm, (unsigned long long)((long long)nins - (long long)ndel));
+  }
+}
+
+// 3. PageRank amend of the surviving edges of a vertex whose out-degree
+//    changed (one warp per chunk).
+__global__ void __launch_bounds__(256) k_apply_amend(ApplyDirArgs A) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; c < A.n_chunks;
+       c += nwarps) {
+    const uint32_t g = group_of_chunk(A, c);
+    const uint32_t u = A.gv[g];
+    const uint32_t d0 = A.g_d0[g];
+    const uint32_t d1 = d0 - A.g_ndel[g] + A.g_nins[g];
+    if (d0 == d1) continue;
+    const float xu = A.pr_x[u];
+    if (xu == 0.f) continue;
+    const float sub = d0 > 0 ? A.damping * xu / (float)d0 : 0.f;
+    const float add = d1 > 0 ? A.damping * xu / (float)d1 : 0.f;
+    const float diff = add - sub;
+    if (diff == 0.f) continue;
+    const uint64_t base = A.c.off[u];
+    const uint32_t k0 = (uint32_t)(c - A.chunk_off[g]) * kApplyChunk;
+    const uint32_t k1 = min(k0 + kApplyChunk, d0);
+    for (uint32_t k = k0 + lane; k < k1; k += 32) {
+      const uint32_t t = A.c.col[base + k];
+      if (t != kInvalidVid) atomicAdd(&A.pr_delta[t], diff);
+    }
+  }
+}
+
+// 4. per vertex: fill the tombstones below the new live length with the
+//    live entries above it (O(deletions)), grow into the pool if needed,
+//    append insertions.
+__global__ void __launch_bounds__(256) k_apply_finish(ApplyDirArgs A) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t g = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; g < A.n_grp;
+       g += nwarps) {
+    const uint32_t u = A.gv[g], b = A.gb[g], e = A.ge[g];
+    const uint32_t d0 = A.g_d0[g], ndel = A.g_ndel[g];
+    uint64_t base = A.c.off[u];
+    const uint32_t newlen = d0 - ndel;
+    // tombstone slots below newlen, in action order
+    uint32_t nh = 0;
+    for (uint32_t jb = b; jb < e; jb += 32) {
+      const uint32_t j = jb + lane;
+      bool hole = false;
+      uint32_t pos = 0;
+      if (j < e) {
+        const uint32_t a = act_at(A, j);
+        if (A.a_kind[a] == 1u && A.a_found[a] != kInvalidVid) {
+          pos = A.a_pos[a];
+          hole = pos < newlen;
+        }
       }
-      wp += __popc(mask);
+      const uint32_t mask = __ballot_sync(0xffffffffu, hole);
+      if (hole) A.a_tmp[b + nh + __popc(mask & lanemask_lt())] = pos;
+      nh += __popc(mask);
     }
     __syncwarp();
-    // phase 4: grow into the pool when the segment is too small
-    uint32_t cap = A.c.cap[u];
+    // live entries at or above newlen move into those holes
+    uint32_t r = 0;
+    for (uint32_t kb = newlen; kb < d0; kb += 32) {
+      const uint32_t k = kb + lane;
+      uint32_t cval = kInvalidVid;
+      float wv = 0.f;
+      if (k < d0) {
+        cval = A.c.col[base + k];
+        if (A.c.w) wv = A.c.w[base + k];
+      }
+      const bool live = k < d0 && cval != kInvalidVid;
+      const uint32_t mask = __ballot_sync(0xffffffffu, live);
+      if (live) {
+        const uint32_t h = A.a_tmp[b + r + __popc(mask & lanemask_lt())];
+        A.c.col[base + h] = cval;
+        if (A.c.w) A.c.w[base + h] = wv;
+      }
+      r += __popc(mask);
+    }
+    if (r != nh && lane == 0) atomicExch(A.d_err, 3u);
+    __syncwarp();
+    const uint32_t d1 = newlen + A.g_nins[g];
+    const uint32_t cap = A.c.cap[u];
     if (d1 > cap) {
       const uint32_t ncap = (d1 + d1 / 8u + 4u + 3u) & ~3u;
       unsigned long long nb = 0;
       if (lane == 0) nb = atomicAdd((unsigned long long*)A.c.pool_tail, (unsigned long long)ncap);
       nb = __shfl_sync(0xffffffffu, nb, 0);
       if (nb + ncap > A.c.pool_cap) {
-        if (lane == 0) atomicExch(A.d_err, 1u);
-        continue;  // segment left as compacted; host reports SG_ERR_OOM
+        if (lane == 0) {
+          atomicExch(A.d_err, 1u);
+          A.c.deg[u] = newlen;
+        }
+        continue;  // insertions dropped; host reports SG_ERR_OOM
       }
-      for (uint32_t k = lane; k < wp; k += 32) {
+      for (uint32_t k = lane; k < newlen; k += 32) {
         A.c.col[nb + k] = A.c.col[base + k];
         if (A.c.w) A.c.w[nb + k] = A.c.w[base + k];
       }
@@ -799,7 +936,7 @@ __global__ void __launch_bounds__(256) k_apply_dir(ApplyDirArgs A) {
         A.c.cap[u] = ncap;
       }
     }
-    // phase 5: append insertions
+    uint32_t wp = newlen;
     for (uint32_t jb = b; jb < e; jb += 32) {
       const uint32_t j = jb + lane;
       bool ins = false;
@@ -816,10 +953,7 @@ __global__ void __launch_bounds__(256) k_apply_dir(ApplyDirArgs A) {
       }
       wp += __popc(mask);
     }
-    if (lane == 0) {
-      A.c.deg[u] = wp;
-      if (A.out_dir) atomicAdd(A.d_dm, (unsigned long long)((long long)nins - (long long)ndel));
-    }
+    if (lane == 0) A.c.deg[u] = wp;
   }
 }
 
@@ -830,6 +964,8 @@ static sg_status batch_reserve(sg_ctx* ctx, uint64_t count) {
   dfree(B.a_src); dfree(B.a_dst); dfree(B.a_w); dfree(B.a_kind); dfree(B.a_found);
   dfree(B.grp_vertex); dfree(B.grp_begin); dfree(B.grp_end); dfree(B.perm);
   dfree(B.igrp_vertex); dfree(B.igrp_begin); dfree(B.igrp_end); dfree(B.d_count);
+  dfree(B.a_pos_in); dfree(B.a_tmp); dfree(B.g_d0); dfree(B.g_ndel); dfree(B.g_nins);
+  dfree(B.chunk_off); dfree(B.nch);
   uint64_t c = std::max<uint64_t>(count, 1024);
   SG_TRY(dalloc(ctx, &B.raw, c));
   SG_TRY(dalloc(ctx, &B.key, c));
@@ -849,6 +985,13 @@ static sg_status batch_reserve(sg_ctx* ctx, uint64_t count) {
   SG_TRY(dalloc(ctx, &B.igrp_begin, c));
   SG_TRY(dalloc(ctx, &B.igrp_end, c));
   SG_TRY(dalloc(ctx, &B.d_count, 4));
+  SG_TRY(dalloc(ctx, &B.a_pos_in, c));
+  SG_TRY(dalloc(ctx, &B.a_tmp, c));
+  SG_TRY(dalloc(ctx, &B.g_d0, 2 * c));
+  SG_TRY(dalloc(ctx, &B.g_ndel, 2 * c));
+  SG_TRY(dalloc(ctx, &B.g_nins, 2 * c));
+  SG_TRY(dalloc(ctx, &B.chunk_off, 2 * (c + 1)));
+  SG_TRY(dalloc(ctx, &B.nch, c + 1));
   B.cap = c;
   return SG_OK;
 }
@@ -921,7 +1064,10 @@ sg_status apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* upd
   A.c = g.out;
   A.gv = B.grp_vertex; A.gb = B.grp_begin; A.ge = B.grp_end; A.n_grp = B.n_grp;
   A.perm = nullptr;
-  A.a_nbr = B.a_dst; A.a_w = B.a_w; A.a_kind = B.a_kind; A.a_found = B.a_found;
+  A.a_nbr = B.a_dst; A.a_w = B.a_w; A.a_kind = B.a_kind;
+  A.a_found = B.a_found; A.a_pos = B.a_found; A.a_tmp = B.a_tmp;
+  A.g_d0 = B.g_d0; A.g_ndel = B.g_ndel; A.g_nins = B.g_nins;
+  A.chunk_off = B.chunk_off;
   A.out_dir = true;
   const PrAmendArgs pa = pr_amend_args(ctx);
   if (pa.active) { A.pr_x = pa.x; A.pr_delta = pa.delta; A.damping = pa.damping; }
@@ -931,18 +1077,39 @@ sg_status apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* upd
   }
   A.d_dm = d_dm;
   A.d_err = d_err;
-  kprof_begin(ctx);
-  k_apply_dir<<<grid_for(B.n_grp * 32, 256), 256, 0, ctx->stream>>>(A);
   ApplyDirArgs I = A;
   I.c = g.in;
   I.gv = B.igrp_vertex; I.gb = B.igrp_begin; I.ge = B.igrp_end; I.n_grp = B.n_igrp;
   I.perm = B.perm;
   I.a_nbr = B.a_src;
+  I.a_pos = B.a_pos_in;
+  I.g_d0 = B.g_d0 + B.cap; I.g_ndel = B.g_ndel + B.cap; I.g_nins = B.g_nins + B.cap;
+  I.chunk_off = B.chunk_off + (B.cap + 1);
   I.out_dir = false;
   I.pr_x = nullptr; I.pr_delta = nullptr; I.sp_parent = nullptr;
-  count_launch(ctx, 8);  // group and sort kernels above
-  k_apply_dir<<<grid_for(B.n_igrp * 32, 256), 256, 0, ctx->stream>>>(I);
+  // work items: ceil(degree / chunk) per group and direction
+  k_apply_chunks<<<grid_for(A.n_grp + 1, 256), 256, 0, ctx->stream>>>(A, B.nch);
+  SG_TRY(exclusive_sum(ctx, B.nch, B.chunk_off, A.n_grp + 1));
+  k_apply_chunks<<<grid_for(I.n_grp + 1, 256), 256, 0, ctx->stream>>>(I, B.nch);
+  SG_TRY(exclusive_sum(ctx, B.nch, B.chunk_off + (B.cap + 1), I.n_grp + 1));
+  uint32_t nck[2] = {0, 0};
+  SG_CUDA(ctx, cudaMemcpyAsync(&nck[0], B.chunk_off + A.n_grp, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaMemcpyAsync(&nck[1], B.chunk_off + (B.cap + 1) + I.n_grp, 4,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  A.n_chunks = nck[0];
+  I.n_chunks = nck[1];
+  count_launch(ctx, 12);  // group, sort and scan kernels above
+  kprof_begin(ctx);
+  k_apply_find<<<grid_for(A.n_chunks * 32, 256), 256, 0, ctx->stream>>>(A);
+  k_apply_find<<<grid_for(I.n_chunks * 32, 256), 256, 0, ctx->stream>>>(I);
+  k_apply_group<<<grid_for(A.n_grp * 32, 256), 256, 0, ctx->stream>>>(A);
+  k_apply_group<<<grid_for(I.n_grp * 32, 256), 256, 0, ctx->stream>>>(I);
+  if (A.pr_x) k_apply_amend<<<grid_for(A.n_chunks * 32, 256), 256, 0, ctx->stream>>>(A);
+  k_apply_finish<<<grid_for(A.n_grp * 32, 256), 256, 0, ctx->stream>>>(A);
+  k_apply_finish<<<grid_for(I.n_grp * 32, 256), 256, 0, ctx->stream>>>(I);
   kprof_end(ctx, SG_K_APPLY);
+  count_launch(ctx, 6);
   SG_CUDA(ctx, cudaGetLastError());
   long long dm = 0;
   SG_CUDA(ctx, cudaMemcpyAsync(&dm, d_dm, 8, cudaMemcpyDeviceToHost, ctx->stream));
@@ -950,6 +1117,7 @@ sg_status apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* upd
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (h_err) {
     g.valid = false;
+    if (h_err == 3u) return fail(ctx, SG_ERR_INVALID, "applier found an inconsistent segment");
     return fail(ctx, SG_ERR_OOM, "adjacency pool exhausted while applying updates");
   }
   g.m = (uint64_t)((long long)g.m + dm);

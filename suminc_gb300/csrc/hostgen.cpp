@@ -253,3 +253,74 @@ sg_status sg_hostgraph_gen_updates(sg_hostgraph* g, uint64_t n_ins, uint64_t n_d
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------ greedy clustering
+#include "summary.h"
+
+namespace sg {
+// in-adjacency with rows sorted by source id
+void host_transpose(const HostAdj& out, HostAdj& in) {
+  in.n = out.n;
+  in.rp.assign((size_t)out.n + 1, 0);
+  for (uint64_t e = 0; e < out.rp[out.n]; ++e) in.rp[out.col[e] + 1]++;
+  for (uint32_t v = 0; v < out.n; ++v) in.rp[v + 1] += in.rp[v];
+  in.col.resize(out.rp[out.n]);
+  if (!out.w.empty()) in.w.resize(out.rp[out.n]);
+  std::vector<uint64_t> pos(in.rp.begin(), in.rp.end() - 1);
+  for (uint32_t u = 0; u < out.n; ++u)
+    for (uint64_t e = out.rp[u]; e < out.rp[u + 1]; ++e) {
+      const uint64_t p = pos[out.col[e]]++;
+      in.col[p] = u;
+      if (!out.w.empty()) in.w[p] = out.w[e];
+    }
+}
+
+void host_adj_from_csr(uint32_t n, const uint64_t* rp, const uint32_t* col, const float* w,
+                       HostAdj& out) {
+  out.n = n;
+  out.rp.assign(rp, rp + n + 1);
+  out.col.assign(col, col + rp[n]);
+  if (w) out.w.assign(w, w + rp[n]);
+  // rows sorted by destination, as the reference fragment keeps them
+  for (uint32_t v = 0; v < n; ++v) {
+    const uint64_t b = out.rp[v], e = out.rp[v + 1];
+    bool sorted = true;
+    for (uint64_t k = b + 1; k < e; ++k)
+      if (out.col[k - 1] > out.col[k]) { sorted = false; break; }
+    if (sorted) continue;
+    std::vector<std::pair<uint32_t, float>> row;
+    for (uint64_t k = b; k < e; ++k) row.push_back({out.col[k], w ? out.w[k] : 0.f});
+    std::sort(row.begin(), row.end());
+    for (uint64_t k = b; k < e; ++k) {
+      out.col[k] = row[k - b].first;
+      if (w) out.w[k] = row[k - b].second;
+    }
+  }
+}
+}  // namespace sg
+
+extern "C" sg_status sg_util_greedy_clusters(uint32_t n, const uint64_t* row_ptr,
+                                             const uint32_t* col, int max_node_num,
+                                             int min_node_num, uint64_t seed,
+                                             uint32_t* cluster_ptr, uint32_t* members,
+                                             uint32_t* n_clusters) {
+  if (!row_ptr || !col || !cluster_ptr || !members || !n_clusters || n == 0 ||
+      max_node_num < 1 || min_node_num < 1)
+    return SG_ERR_INVALID;
+  try {
+    HostAdj out, in;
+    host_adj_from_csr(n, row_ptr, col, nullptr, out);
+    host_transpose(out, in);
+    auto cl = greedy_clusters(out, in, max_node_num, min_node_num, seed);
+    uint32_t k = 0;
+    cluster_ptr[0] = 0;
+    for (size_t i = 0; i < cl.size(); ++i) {
+      for (uint32_t v : cl[i]) members[k++] = v;
+      cluster_ptr[i + 1] = k;
+    }
+    *n_clusters = (uint32_t)cl.size();
+    return SG_OK;
+  } catch (const std::bad_alloc&) {
+    return SG_ERR_OOM;
+  }
+}

@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(256) k_sssp_persistent(SsspArgs A) {
   __shared__ unsigned long long s_red[8];
   unsigned long long edges = 0, improve = 0;
   uint32_t it = 0;       // near iterations
+  uint32_t seq = 0;      // phases so far: every phase gets a fresh queue tag
   uint32_t fslot = 0;    // current far queue
   double thr = 0.0;      // current window end
 
@@ -149,10 +150,13 @@ __global__ void __launch_bounds__(256) k_sssp_persistent(SsspArgs A) {
       if (fn == 0) break;
       if (blockIdx.x == 0 && threadIdx.x == 0) A.cnt[SC_MIN] = kInfBits;
       if (!(ok = grid_sync(A))) break;
+      // smallest distance among far entries not already settled: entries of
+      // vertices finished in an earlier window are stale and ignored
+      const unsigned long long settled_b = dbits(thr);
       unsigned long long mn = kInfBits;
       for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < fn; i += gridDim.x * blockDim.x) {
         const unsigned long long dx = __ldcg(A.dist + __ldcg(A.fq[fslot] + i));
-        mn = dx < mn ? dx : mn;
+        if (dx >= settled_b && dx < mn) mn = dx;
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -172,7 +176,7 @@ __global__ void __launch_bounds__(256) k_sssp_persistent(SsspArgs A) {
       const double mind = bitsd(mnb);
       const double settled = thr;  // everything below the old window is final
       thr = (floor(mind / A.delta) + 1.0) * A.delta;
-      const uint32_t tag = A.iter_base + it + 1;
+      const uint32_t tag = A.iter_base + (++seq);
       const uint32_t epoch = tag;
       if (blockIdx.x == 0 && threadIdx.x == 0) A.ctl[S_F0 + nf] = 0;
       if (!(ok = grid_sync(A))) break;
@@ -197,7 +201,7 @@ __global__ void __launch_bounds__(256) k_sssp_persistent(SsspArgs A) {
         if (to_far) A.fq[nf][sf] = x;
       }
       fslot = nf;
-      if (blockIdx.x == 0 && threadIdx.x == 0) A.ctl[S_SPLITS]++;
+      if (blockIdx.x == 0 && threadIdx.x == 0) A.ctl[S_SPLITS] = seq;
       if (!(ok = grid_sync(A))) break;
       continue;
     }
@@ -207,9 +211,10 @@ __global__ void __launch_bounds__(256) k_sssp_persistent(SsspArgs A) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       A.ctl[S_Q0 + cs] = 0;
       A.ctl[S_ITERS] = it + 1;
+      A.ctl[S_SPLITS] = seq + 1;
     }
     relax_queue(A, A.nq[rs], qn, thr, A.nq[ws], A.ctl + S_Q0 + ws, A.fq[fslot],
-                A.ctl + S_F0 + fslot, A.iter_base + it + 2, edges, improve);
+                A.ctl + S_F0 + fslot, A.iter_base + (++seq), edges, improve);
     if (!(ok = grid_sync(A))) break;
     ++it;
   }
@@ -323,25 +328,6 @@ __global__ void k_sssp_reseed(const uint32_t* __restrict__ list, uint32_t cnt,
   }
 }
 
-// Relax the edges added by the last batch (the reference re-sends from all
-// finite vertices, sum_sync_traversal_worker.h:323-332; only these edges and
-// the reset vertices can lower a distance).
-__global__ void k_sssp_added(const uint32_t* __restrict__ a_src, const uint32_t* __restrict__ a_dst,
-                             const float* __restrict__ a_w, const uint32_t* __restrict__ a_kind,
-                             uint64_t n_act, unsigned long long* __restrict__ dist,
-                             uint32_t* __restrict__ fq, uint32_t* __restrict__ fq_cnt) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_act;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    if (a_kind && !(a_kind[i] & 2u)) continue;
-    const unsigned long long du = dist[a_src[i]];
-    if (du >= kInfBits) continue;
-    const unsigned long long nb = dbits(bitsd(du) + (double)a_w[i]);
-    const uint32_t v = a_dst[i];
-    const unsigned long long old = atomicMin(dist + v, nb);
-    if (nb < old) fq[atomicAdd(fq_cnt, 1u)] = v;
-  }
-}
-
 __global__ void k_sssp_init(uint32_t n, unsigned long long* dist, uint32_t* stamp,
                             uint32_t* fstamp, uint32_t* reset) {
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
@@ -371,7 +357,7 @@ sg_status sssp_free(sg_ctx* ctx) {
   dfree(s.d_ctl); dfree(s.d_cnt);
   dfree(s.fstamp); dfree(s.list); dfree(s.seeds); dfree(s.seed_cnt); dfree(s.far);
   dfree(s.out);
-  dfree(s.padd_src); dfree(s.padd_dst); dfree(s.padd_w);
+  dfree(s.padd_dst);
   s = SsspState();
   return SG_OK;
 }
@@ -420,24 +406,24 @@ SsspAmendArgs sssp_amend_args(sg_ctx* ctx) {
   return a;
 }
 
-__global__ void k_collect_adds(const uint32_t* __restrict__ a_src, const uint32_t* __restrict__ a_dst,
-                               const float* __restrict__ a_w, const uint32_t* __restrict__ a_kind,
-                               uint64_t n_act, uint32_t* __restrict__ ps, uint32_t* __restrict__ pd,
-                               float* __restrict__ pw, uint32_t* __restrict__ cnt) {
+__global__ void k_collect_adds(const uint32_t* __restrict__ a_dst, const uint32_t* __restrict__ a_kind,
+                               uint64_t n_act, uint32_t* __restrict__ pd, uint32_t* __restrict__ cnt) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_act;
        i += (uint64_t)gridDim.x * blockDim.x) {
     if (!(a_kind[i] & 2u)) continue;
-    const uint32_t slot = atomicAdd(cnt, 1u);
-    ps[slot] = a_src[i];
-    pd[slot] = a_dst[i];
-    pw[slot] = a_w[i];
+    pd[atomicAdd(cnt, 1u)] = a_dst[i];
   }
 }
 
 // Called by the applier after the batch's actions are known: remembers the
-// added (or re-weighted) edges for the next IncEval.  They are relaxed only
-// after the reset, because a tail reset by the same batch must not lend its
-// stale distance to the head.
+// heads of added (or re-weighted) edges for the next IncEval.  The
+// reference re-sends from every finite vertex after the reset
+// (sum_sync_traversal_worker.h:323-332); only these heads and the reset
+// vertices can get a shorter distance, so IncEval re-seeds them by a pull
+// over their in-edges in the graph as it is then.  Pulling (rather than
+// relaxing the recorded edges) stays exact when a later batch deletes or
+// re-weights an edge before the IncEval, and runs after the reset, so a
+// tail reset by the same batch lends no stale distance to its head.
 sg_status sssp_collect_adds(sg_ctx* ctx) {
   SsspState& s = ctx->sp;
   const DevBatch& B = ctx->batch;
@@ -445,24 +431,19 @@ sg_status sssp_collect_adds(sg_ctx* ctx) {
   const uint64_t need = s.padd_bound + B.n_act;
   if (need > s.padd_cap) {
     // grow, keeping the pending entries
-    uint64_t ncap = std::max<uint64_t>(need * 2, 4096);
-    uint32_t *ns = nullptr, *nd = nullptr;
-    float* nw = nullptr;
-    SG_TRY(dalloc(ctx, &ns, ncap));
+    const uint64_t ncap = std::max<uint64_t>(need * 2, 4096);
+    uint32_t* nd = nullptr;
     SG_TRY(dalloc(ctx, &nd, ncap));
-    SG_TRY(dalloc(ctx, &nw, ncap));
     if (s.padd_bound) {
-      SG_CUDA(ctx, cudaMemcpyAsync(ns, s.padd_src, 4 * s.padd_bound, cudaMemcpyDeviceToDevice, ctx->stream));
       SG_CUDA(ctx, cudaMemcpyAsync(nd, s.padd_dst, 4 * s.padd_bound, cudaMemcpyDeviceToDevice, ctx->stream));
-      SG_CUDA(ctx, cudaMemcpyAsync(nw, s.padd_w, 4 * s.padd_bound, cudaMemcpyDeviceToDevice, ctx->stream));
       SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
-    dfree(s.padd_src); dfree(s.padd_dst); dfree(s.padd_w);
-    s.padd_src = ns; s.padd_dst = nd; s.padd_w = nw;
+    dfree(s.padd_dst);
+    s.padd_dst = nd;
     s.padd_cap = ncap;
   }
-  k_collect_adds<<<grid_for(B.n_act, 256), 256, 0, ctx->stream>>>(
-      B.a_src, B.a_dst, B.a_w, B.a_kind, B.n_act, s.padd_src, s.padd_dst, s.padd_w, s.seed_cnt + 2);
+  k_collect_adds<<<grid_for(B.n_act, 256), 256, 0, ctx->stream>>>(B.a_dst, B.a_kind, B.n_act,
+                                                                 s.padd_dst, s.seed_cnt + 2);
   SG_CUDA(ctx, cudaGetLastError());
   s.padd_bound = need;
   return SG_OK;
@@ -593,7 +574,7 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
     total = end;
     k_sssp_reset_apply<<<grid_for(total, 256), 256, 0, st>>>(s.list, total, s.dist, s.parent);
   }
-  // 2. far queue <- re-seeded reset vertices + heads of improving added edges
+  // 2. far queue <- re-seeded reset vertices and heads of added edges
   const uint64_t need_far = (uint64_t)total + h_seed[2] + g.n + 1024;
   if (need_far > s.far_cap) {
     dfree(s.far);
@@ -608,13 +589,9 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
   if (total > 0)
     k_sssp_reseed<<<grid_for((uint64_t)total * 32, 256), 256, 0, st>>>(
         s.list, total, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.far, s.d_ctl + S_F0);
-  if (s.has_pending && h_seed[2] > 0) {
-    uint32_t* kinds = nullptr;  // all pending records are adds
-    (void)kinds;
-    k_sssp_added<<<grid_for(h_seed[2], 256), 256, 0, st>>>(s.padd_src, s.padd_dst, s.padd_w,
-                                                          nullptr, h_seed[2], s.dist, s.far,
-                                                          s.d_ctl + S_F0);
-  }
+  if (s.has_pending && h_seed[2] > 0)
+    k_sssp_reseed<<<grid_for((uint64_t)h_seed[2] * 32, 256), 256, 0, st>>>(
+        s.padd_dst, h_seed[2], g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.far, s.d_ctl + S_F0);
   SG_CUDA(ctx, cudaGetLastError());
   // 3. delta-stepping from the seeds
   SG_TRY(sssp_launch(ctx));

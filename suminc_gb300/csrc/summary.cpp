@@ -1,0 +1,759 @@
+// Host construction of the summarized graph.  Each function restates one
+// step of the reference's CompressorBase (grape/fragment/compressor_base.h)
+// and keeps its observable rules, including the container types whose
+// iteration order feeds into the result (mirror sets are unordered sets of
+// vertex ids with the identity hash, built from sorted ranges).
+#include "summary.h"
+
+#include <algorithm>
+#include <cmath>
+#include <set>
+#include <unordered_map>
+
+#include "common.h"
+
+namespace sg {
+
+// ---------------------------------------------------------------- greedy
+//
+// compressor_base.h:367-419 (dispatch, one compress thread) and :1448-1875
+// (parallel_find_multi_source_supernode_2_sort_sample).  The reference draws
+// its candidate samples from std::random_device; this restatement draws them
+// from a seeded counter-based generator so the clustering is reproducible.
+
+namespace {
+
+struct CandidateQueue {  // grape/utils/Queue.h: vector queue with swap-erase
+  std::vector<uint32_t> data;
+  uint32_t head = 0, tail = 0;
+  void push(uint32_t v) {
+    if (tail >= data.size()) data.resize(std::max<size_t>(16, data.size() * 2));
+    data[tail++] = v;
+  }
+  void erase(uint32_t id) {
+    if (id != tail - 1) std::swap(data[id], data[tail - 1]);
+    tail--;
+  }
+  uint32_t size() const { return tail - head; }
+  bool empty() const { return size() == 0; }
+};
+
+struct Rng {
+  uint64_t key, ctr = 0;
+  explicit Rng(uint64_t seed) : key(mix64(seed ^ 0x94D049BB133111EBull)) {}
+  uint64_t next() { return mix64(key + (ctr++)); }
+};
+
+bool contains(const std::set<uint32_t>& s, uint32_t v) { return s.find(v) != s.end(); }
+
+struct Greedy {
+  const HostAdj& out;
+  const HostAdj& in;
+  int max_node_num;
+  std::vector<int32_t> Fc;
+  std::vector<std::vector<uint32_t>> clusters;
+  Rng rng;
+
+  Greedy(const HostAdj& o, const HostAdj& i, int mx, uint64_t seed)
+      : out(o), in(i), max_node_num(mx), Fc(o.n, Summary::kFcDefault), rng(seed) {}
+
+  float check_score(uint32_t d, const std::set<uint32_t>& S, const std::set<uint32_t>& P,
+                    const std::set<uint32_t>& B, uint32_t inner, bool& is_s, bool& is_b,
+                    uint32_t& temp_inner, std::vector<uint32_t>& tS, std::vector<uint32_t>& tB) {
+    is_s = false;
+    is_b = false;
+    temp_inner = inner;
+    tS.clear();
+    tB.clear();
+    std::set<uint32_t> setS, setB;
+    uint32_t now_s = (uint32_t)S.size(), now_b = (uint32_t)B.size();
+    for (uint64_t e = out.rp[d]; e < out.rp[d + 1]; ++e) {
+      const uint32_t o = out.col[e];
+      if (contains(S, o)) {
+        bool flag = true;
+        for (uint64_t f = in.rp[o]; f < in.rp[o + 1]; ++f) {
+          const uint32_t x = in.col[f];
+          if (!contains(P, x) && x != d) {
+            flag = false;
+            break;
+          }
+        }
+        if (flag) setS.insert(o);
+      }
+      if (!contains(P, o) && o != d) is_b = true;
+      else temp_inner += 1;
+    }
+    for (uint64_t e = in.rp[d]; e < in.rp[d + 1]; ++e) {
+      const uint32_t i = in.col[e];
+      if (contains(B, i)) {
+        bool flag = true;
+        for (uint64_t f = out.rp[i]; f < out.rp[i + 1]; ++f) {
+          const uint32_t x = out.col[f];
+          if (!contains(P, x) && x != d) {
+            flag = false;
+            break;
+          }
+        }
+        if (flag) setB.insert(i);
+      }
+      if (contains(P, i)) temp_inner++;
+      else is_s = true;
+    }
+    now_s -= (uint32_t)setS.size();
+    now_b -= (uint32_t)setB.size();
+    if (is_s) now_s++;
+    if (is_b) now_b++;
+    tS.assign(setS.begin(), setS.end());
+    tB.assign(setB.begin(), setB.end());
+    return (float)(temp_inner * 1.0 - (double)(uint32_t)(now_s * now_b));
+  }
+
+  void sample(const CandidateQueue& D, uint32_t want, std::vector<uint32_t>& out_idx) {
+    out_idx.clear();
+    if (want >= D.size()) {
+      for (uint32_t i = D.head; i < D.tail; ++i) out_idx.push_back(i);
+      return;
+    }
+    std::set<uint32_t> taken;
+    while (out_idx.size() < want) {
+      const uint32_t pos = D.head + (uint32_t)(rng.next() % D.size());
+      if (taken.insert(pos).second) out_idx.push_back(pos);
+    }
+  }
+
+  void find(uint32_t source, int now_min) {
+    const uint64_t try_max_node = (uint64_t)max_node_num * 1000;
+    const int try_max_step = max_node_num * 1000;
+    const uint32_t sample_size = 32;
+    const int try_sample_cnt = 3;
+    std::set<uint32_t> S, P, B, visited;
+    CandidateQueue D;
+    if (Fc[source] == Summary::kFcDefault) {
+      P.insert(source);
+      visited.insert(source);
+      if (out.deg(source) < try_max_node)
+        for (uint64_t e = out.rp[source]; e < out.rp[source + 1]; ++e) {
+          const uint32_t v = out.col[e];
+          if (Fc[v] == Summary::kFcDefault && !contains(P, v) && !contains(visited, v)) {
+            D.push(v);
+            visited.insert(v);
+          }
+        }
+    }
+    uint32_t inner_edge_num = 0;
+    for (uint32_t u : P) {
+      bool f = true;
+      for (uint64_t e = out.rp[u]; e < out.rp[u + 1]; ++e) {
+        if (!contains(P, out.col[e])) {
+          if (f) {
+            B.insert(u);
+            f = false;
+          }
+        } else {
+          inner_edge_num++;
+        }
+      }
+      for (uint64_t e = in.rp[u]; e < in.rp[u + 1]; ++e)
+        if (!contains(P, in.col[e])) {
+          S.insert(u);
+          break;
+        }
+    }
+    float pre_score = 0;
+    int step = 0;
+    std::vector<float> scores(sample_size);
+    std::vector<char> is_s_vec(sample_size), is_b_vec(sample_size);
+    std::vector<uint32_t> inner_vec(sample_size);
+    std::vector<std::vector<uint32_t>> tS_vec(sample_size), tB_vec(sample_size);
+    std::vector<uint32_t> smp;
+    while (!D.empty() && P.size() <= (size_t)max_node_num) {
+      step++;
+      if (step > try_max_step) break;
+      int max_id = -1;
+      float max_score = 0;
+      bool found = false;
+      uint32_t d = 0;
+      int cnt = 0;
+      while (cnt < try_sample_cnt) {
+        sample(D, sample_size, smp);
+        const int real = (int)smp.size();
+        for (int i = 0; i < real; ++i) {
+          bool is_s, is_b;
+          uint32_t ti;
+          scores[i] = check_score(D.data[smp[i]], S, P, B, inner_edge_num, is_s, is_b, ti,
+                                  tS_vec[i], tB_vec[i]);
+          is_s_vec[i] = is_s;
+          is_b_vec[i] = is_b;
+          inner_vec[i] = ti;
+        }
+        max_score = -1e10f;
+        for (int i = 0; i < real; ++i)
+          if (max_score < scores[i]) {
+            max_score = scores[i];
+            max_id = i;
+          }
+        if ((max_score >= 0 && max_score >= pre_score) || (P.size() < (size_t)(now_min - 1))) {
+          pre_score = max_score;
+          d = D.data[smp[max_id]];
+          D.erase(smp[max_id]);
+          found = true;
+          break;
+        }
+        if (sample_size >= D.size()) break;
+        cnt++;
+      }
+      if (!found) break;
+      if (is_b_vec[max_id]) B.insert(d);
+      for (uint32_t v : tB_vec[max_id]) B.erase(v);
+      if (is_s_vec[max_id]) S.insert(d);
+      for (uint32_t v : tS_vec[max_id]) S.erase(v);
+      inner_edge_num = inner_vec[max_id];
+      P.insert(d);
+      if (out.deg(d) < try_max_node)
+        for (uint64_t e = out.rp[d]; e < out.rp[d + 1]; ++e) {
+          const uint32_t v = out.col[e];
+          if (Fc[v] == Summary::kFcDefault && !contains(P, v) && !contains(visited, v)) {
+            D.push(v);
+            visited.insert(v);
+          }
+        }
+    }
+    if (P.size() >= (size_t)now_min) {
+      if (S.empty()) S.insert(source);
+      const int32_t ids = (int32_t)clusters.size();
+      clusters.emplace_back(P.begin(), P.end());
+      for (uint32_t u : P) Fc[u] = -(ids + 1);
+      for (uint32_t s : S) Fc[s] = ids;
+    }
+  }
+};
+
+}  // namespace
+
+std::vector<std::vector<uint32_t>> greedy_clusters(const HostAdj& out, const HostAdj& in,
+                                                   int max_node_num, int min_node_num,
+                                                   uint64_t seed) {
+  Greedy G(out, in, max_node_num, seed);
+  std::vector<std::pair<uint32_t, uint32_t>> order(out.n);
+  for (uint32_t u = 0; u < out.n; ++u) order[u] = {u, (uint32_t)out.deg(u)};
+  // big to small by out-degree, ties by id (cmp_pair_b2s, compressor_base.h:2789)
+  std::sort(order.begin(), order.end(), [](const auto& a, const auto& b) {
+    if (a.second != b.second) return a.second > b.second;
+    return a.first < b.first;
+  });
+  for (int i = 1; i <= 3; ++i) {
+    const int b = min_node_num * i;
+    for (auto& pr : order) {
+      if (G.Fc[pr.first] != Summary::kFcDefault) continue;
+      G.find(pr.first, b);
+    }
+  }
+  return G.clusters;
+}
+
+// ------------------------------------------------------- supernode build
+//
+// compress_by_cluster (compressor_base.h:3160-3250), the benefit filter and
+// mirror selection of get_init_supernode_by_clusters (:3253-3611) and
+// final_build_supernode (:3616-3783).
+
+void summary_from_clusters(Summary& S, const HostAdj& out, const HostAdj& in,
+                           const std::vector<std::vector<uint32_t>>& clusters_in,
+                           int min_node_num, int mirror_k, double compress_threshold) {
+  const uint32_t n = out.n;
+  S = Summary();
+  S.old_n = n;
+  S.Fc.assign(n, Summary::kFcDefault);
+  S.id2spids.assign(n, Summary::kIdDefault);
+  S.out_bound.assign(n, 0);
+  // cluster file records: a record smaller than min_node_num is dropped, but
+  // its vertices keep the cluster number assigned while reading, which the
+  // next kept cluster then takes (compressor_base.h:3211-3233).
+  std::vector<uint32_t> id2clusterid(n, Summary::kIdDefault);
+  std::vector<std::vector<uint32_t>> clusters;
+  uint32_t cluster_num = 0;
+  for (const auto& rec : clusters_in) {
+    std::set<uint32_t> P;
+    for (uint32_t v : rec) {
+      if (v >= n) continue;
+      P.insert(v);
+      id2clusterid[v] = cluster_num;
+    }
+    if (P.size() >= (size_t)min_node_num) {
+      clusters.emplace_back(P.begin(), P.end());
+      cluster_num++;
+    }
+  }
+  typedef long long count_t;
+  const count_t k = mirror_k;
+  const float obj = (float)compress_threshold;
+  const bool use_mirror = mirror_k != 100000000;
+  count_t mirror_node_num = 0;
+  for (uint32_t j = 0; j < clusters.size(); ++j) {
+    const auto& node_set = clusters[j];
+    std::unordered_map<uint32_t, uint32_t> in_freq, out_freq;
+    std::set<uint32_t> old_entry, old_exit;
+    count_t inner_edges = 0;
+    for (uint32_t u : node_set) {
+      for (uint64_t e = in.rp[u]; e < in.rp[u + 1]; ++e) {
+        const uint32_t x = in.col[e];
+        if (id2clusterid[x] != j) {
+          if (use_mirror) {
+            const uint32_t newids = S.id2spids[x];
+            if (newids != Summary::kIdDefault) {
+              if (S.supernode_out_mirror[newids].count(u) == 0) in_freq[x] += 1;
+            } else {
+              in_freq[x] += 1;
+            }
+          }
+          old_entry.insert(u);
+        } else {
+          inner_edges++;
+        }
+      }
+      for (uint64_t e = out.rp[u]; e < out.rp[u + 1]; ++e) {
+        const uint32_t x = out.col[e];
+        if (id2clusterid[x] != j) {
+          if (use_mirror) {
+            const uint32_t newids = S.id2spids[x];
+            if (newids != Summary::kIdDefault) {
+              if (S.supernode_in_mirror[newids].count(u) == 0) out_freq[x] += 1;
+            } else {
+              out_freq[x] += 1;
+            }
+          }
+          old_exit.insert(u);
+        }
+      }
+    }
+    count_t in_edge_num = 0, out_edge_num = 0, in_mirror_num = 0, out_mirror_num = 0;
+    const count_t old_exit_num = (count_t)old_exit.size(), old_entry_num = (count_t)old_entry.size();
+    std::set<uint32_t> in_P(node_set.begin(), node_set.end()), out_P(node_set.begin(), node_set.end());
+    std::set<uint32_t> in_mirror, out_mirror;
+    if (use_mirror) {
+      for (const auto& f : in_freq)
+        if ((count_t)f.second > k) {
+          in_edge_num += f.second;
+          in_mirror_num++;
+          in_P.insert(f.first);
+          in_mirror.insert(f.first);
+        }
+      for (const auto& f : out_freq)
+        if ((count_t)f.second > k) {
+          out_edge_num += f.second;
+          out_mirror_num++;
+          out_P.insert(f.first);
+          out_mirror.insert(f.first);
+        }
+    }
+    std::set<uint32_t> B, Sset;
+    for (uint32_t v : node_set)
+      for (uint64_t e = out.rp[v]; e < out.rp[v + 1]; ++e)
+        if (out_P.count(out.col[e]) == 0) {
+          B.insert(v);
+          break;
+        }
+    for (uint32_t v : node_set)
+      for (uint64_t e = in.rp[v]; e < in.rp[v + 1]; ++e)
+        if (in_P.count(in.col[e]) == 0) {
+          Sset.insert(v);
+          break;
+        }
+    const count_t new_exit = (count_t)B.size() + out_mirror_num;
+    const count_t new_entry = (count_t)Sset.size() + in_mirror_num;
+    const count_t idx_old = old_exit_num * old_entry_num;
+    const count_t idx_entry = old_exit_num * new_entry;
+    const count_t idx_exit = new_exit * old_entry_num;
+    const count_t idx_new = new_exit * new_entry;
+    float benefit[4];
+    benefit[0] = (float)(inner_edges * 1.0 - (double)idx_old);
+    benefit[1] = (float)((inner_edges + in_edge_num) * 1.0 - (double)(idx_entry + in_mirror_num));
+    benefit[2] = (float)((inner_edges + out_edge_num) * 1.0 - (double)(idx_exit + out_mirror_num));
+    benefit[3] = (float)((inner_edges + in_edge_num + out_edge_num) * 1.0 -
+                         (double)(idx_new + in_mirror_num + out_mirror_num));
+    int max_i = 0;
+    for (int i = 0; i < 4; ++i)
+      if (benefit[max_i] < benefit[i]) max_i = i;
+    if (!(benefit[max_i] > obj)) continue;
+    std::set<uint32_t> src = Sset;
+    if (max_i == 0) {
+      src = old_entry;
+      in_mirror.clear();
+      out_mirror.clear();
+    } else if (max_i == 1) {
+      out_mirror.clear();
+    } else if (max_i == 2) {
+      src = old_entry;
+      in_mirror.clear();
+    }
+    const uint32_t ids = (uint32_t)S.supernode_ids.size();
+    S.supernode_ids.emplace_back(node_set.begin(), node_set.end());
+    S.cluster_ids.emplace_back(node_set.begin(), node_set.end());
+    S.supernode_source.emplace_back(src.begin(), src.end());
+    S.supernode_in_mirror.emplace_back(in_mirror.begin(), in_mirror.end());
+    S.supernode_out_mirror.emplace_back(out_mirror.begin(), out_mirror.end());
+    mirror_node_num += (count_t)(in_mirror.size() + out_mirror.size());
+    for (uint32_t u : node_set) {
+      S.Fc[u] = -(int32_t)(ids + 1);
+      S.id2spids[u] = ids;
+    }
+  }
+
+  // final_build_supernode
+  S.all_n = n;
+  const uint64_t cap_all = (uint64_t)n + (uint64_t)mirror_node_num;
+  S.Fc_map.assign(cap_all, Summary::kIdDefault);
+  S.vid2in_mirror_mids.assign(n, {});
+  const uint32_t n_clusters = (uint32_t)S.supernode_ids.size();
+  std::vector<uint32_t> mirror_cluster;  // cluster of each mirror id (index m - n)
+  for (uint32_t i = 0; i < n_clusters; ++i) {
+    auto& old_P = S.supernode_ids[i];
+    auto& src = S.supernode_source[i];
+    auto& in_mirror = S.supernode_in_mirror[i];
+    auto& out_mirror = S.supernode_out_mirror[i];
+    std::vector<uint32_t> del_v;
+    // an unclustered vertex chosen as a mirror joins the cluster instead
+    for (uint32_t v : in_mirror) {
+      if (S.Fc[v] != Summary::kFcDefault) continue;
+      S.mirror_node_cnt++;
+      old_P.push_back(v);
+      S.cluster_ids[i].push_back(v);
+      del_v.push_back(v);
+      for (uint64_t e = in.rp[v]; e < in.rp[v + 1]; ++e) {
+        const uint32_t x = in.col[e];
+        if (S.id2spids[x] != i && in_mirror.count(x) == 0) {
+          src.push_back(v);
+          S.inmirror2source_cnt++;
+          break;
+        }
+      }
+      S.Fc[v] = -(int32_t)(i + 1);
+      S.id2spids[v] = i;
+    }
+    for (uint32_t v : del_v) {
+      in_mirror.erase(v);
+      out_mirror.erase(v);
+    }
+    del_v.clear();
+    for (uint32_t v : out_mirror) {
+      if (S.Fc[v] != Summary::kFcDefault) continue;
+      S.mirror_node_cnt++;
+      old_P.push_back(v);
+      S.cluster_ids[i].push_back(v);
+      del_v.push_back(v);
+      for (uint64_t e = in.rp[v]; e < in.rp[v + 1]; ++e) {
+        const uint32_t x = in.col[e];
+        if (S.id2spids[x] != i && in_mirror.count(x) == 0) {
+          src.push_back(v);
+          S.outmirror2source_cnt++;
+          break;
+        }
+      }
+      S.Fc[v] = -(int32_t)(i + 1);
+      S.id2spids[v] = i;
+    }
+    for (uint32_t v : del_v) {
+      out_mirror.erase(v);
+      in_mirror.erase(v);
+    }
+    S.cluster_in_mirror_ids.emplace_back();
+    S.cluster_out_mirror_ids.emplace_back();
+    for (uint32_t v : in_mirror) {
+      const uint32_t m = S.all_n++;
+      S.mirrorid2vid.push_back(v);
+      mirror_cluster.push_back(i);
+      S.cluster_ids[i].push_back(m);
+      S.cluster_in_mirror_ids[i].push_back(m);
+    }
+    for (uint32_t v : out_mirror) {
+      const uint32_t m = S.all_n++;
+      S.mirrorid2vid.push_back(v);
+      mirror_cluster.push_back(i);
+      S.cluster_ids[i].push_back(m);
+      S.cluster_out_mirror_ids[i].push_back(m);
+    }
+    for (uint32_t s : src) {
+      S.Fc[s] = (int32_t)i;
+      const uint32_t spid = (uint32_t)S.supernodes.size();
+      S.Fc_map[s] = spid;
+      Supernode sp;
+      sp.id = s;
+      sp.ids = i;
+      S.supernodes.push_back(sp);
+    }
+    for (uint32_t m : S.cluster_in_mirror_ids[i]) {
+      const uint32_t spid = (uint32_t)S.supernodes.size();
+      S.vid2in_mirror_mids[S.mirror_master(m)].push_back(m);
+      S.Fc_map[m] = spid;
+      Supernode sp;
+      sp.id = m;
+      sp.ids = i;
+      S.supernodes.push_back(sp);
+    }
+  }
+  S.Fc_map.resize(S.all_n);
+  S.id2spids.resize(S.all_n, Summary::kIdDefault);
+  for (uint32_t m = n; m < S.all_n; ++m) S.id2spids[m] = mirror_cluster[m - n];
+  S.all_out_mirror.clear();
+  for (uint32_t j = 0; j < n_clusters; ++j)
+    for (uint32_t m : S.cluster_out_mirror_ids[j]) S.all_out_mirror.push_back(m);
+}
+
+// judge_out_bound_node (compressor_base.h:3924-3956, detail :3993-4007).
+// Exit marks are only ever set; `only` restricts the pass to some clusters.
+void summary_judge_out_bound(Summary& S, const HostAdj& out, const std::vector<uint32_t>* only) {
+  const uint32_t nc = (uint32_t)S.supernode_ids.size();
+  auto judge = [&](uint32_t j) {
+    const auto& om = S.supernode_out_mirror[j];
+    for (uint32_t v : S.supernode_ids[j])
+      for (uint64_t e = out.rp[v]; e < out.rp[v + 1]; ++e) {
+        const uint32_t x = out.col[e];
+        if (S.id2spids[x] != j && om.count(x) == 0) {
+          S.out_bound[v] = 1;
+          break;
+        }
+      }
+  };
+  if (only) {
+    for (uint32_t j : *only) judge(j);
+    for (uint32_t j : *only)
+      for (uint32_t v : S.supernode_in_mirror[j]) S.out_bound[v] = 1;
+  } else {
+    for (uint32_t j = 0; j < nc; ++j) judge(j);
+    for (uint32_t j = 0; j < nc; ++j)
+      for (uint32_t v : S.supernode_in_mirror[j]) S.out_bound[v] = 1;
+  }
+}
+
+// build_subgraph_mirror (compressor_base.h:3786-3856) and its incremental
+// form (:3859-3922): inner edges of each cluster, the in-mirror's edges into
+// its cluster and member edges redirected to out-mirrors.
+void summary_build_subgraph(Summary& S, const HostAdj& out, const HostAdj& in,
+                            const std::vector<uint32_t>* only) {
+  const bool weighted = !out.w.empty();
+  if (S.subgraph.size() != S.all_n) {
+    S.subgraph.assign(S.all_n, {});
+    if (weighted) S.subgraph_w.assign(S.all_n, {});
+  }
+  auto build = [&](uint32_t i) {
+    for (uint32_t v : S.supernode_ids[i]) {
+      S.subgraph[v].clear();
+      if (weighted) S.subgraph_w[v].clear();
+      for (uint64_t e = out.rp[v]; e < out.rp[v + 1]; ++e)
+        if (S.id2spids[out.col[e]] == i) {
+          S.subgraph[v].push_back(out.col[e]);
+          if (weighted) S.subgraph_w[v].push_back(out.w[e]);
+        }
+    }
+    for (uint32_t m : S.cluster_in_mirror_ids[i]) {
+      S.subgraph[m].clear();
+      if (weighted) S.subgraph_w[m].clear();
+      const uint32_t v = S.mirror_master(m);
+      for (uint64_t e = out.rp[v]; e < out.rp[v + 1]; ++e)
+        if (S.id2spids[out.col[e]] == i) {
+          S.subgraph[m].push_back(out.col[e]);
+          if (weighted) S.subgraph_w[m].push_back(out.w[e]);
+        }
+    }
+    for (uint32_t m : S.cluster_out_mirror_ids[i]) {
+      const uint32_t v = S.mirror_master(m);
+      const auto& v_in_mirror = S.supernode_in_mirror[S.id2spids[v]];
+      for (uint64_t e = in.rp[v]; e < in.rp[v + 1]; ++e) {
+        const uint32_t x = in.col[e];
+        if (S.id2spids[x] == i && v_in_mirror.count(x) == 0) {
+          S.subgraph[x].push_back(m);
+          if (weighted) S.subgraph_w[x].push_back(in.w[e]);
+        }
+      }
+    }
+  };
+  if (only) {
+    for (uint32_t i : *only) build(i);
+  } else {
+    for (uint32_t i = 0; i < S.supernode_ids.size(); ++i) build(i);
+  }
+}
+
+// get_nodetype_mirror (compressor_base.h:4144-4182).
+void summary_node_types(Summary& S) {
+  const uint32_t n = S.old_n;
+  S.node_type.assign(n, 127);
+  for (uint32_t i = 0; i < n; ++i) {
+    const int32_t fc = S.Fc[i];
+    if (fc == Summary::kFcDefault) S.node_type[i] = kSingle;
+    else if (fc >= 0) S.node_type[i] = kOnlyIn;
+    else if (!S.out_bound[i]) S.node_type[i] = kInner;
+    if (S.out_bound[i]) {
+      S.node_type[i] = kOnlyOut;
+      if (fc >= 0) S.node_type[i] = kBothOutIn;
+    }
+  }
+  for (size_t j = 0; j < S.supernode_in_mirror.size(); ++j)
+    for (uint32_t v : S.supernode_in_mirror[j]) {
+      if (S.node_type[v] == kOnlyOut) S.node_type[v] = kOutMaster;
+      else if (S.node_type[v] == kBothOutIn) S.node_type[v] = kBothOutInMaster;
+    }
+}
+
+// sketch2csr_mirror (compressor_base.h:4636-4880): is_e (entry / in-mirror ->
+// exit shortcuts, from bound_delta), ib_e (exit -> outside edges, and every
+// edge of unclustered vertices) and sync_e (master -> in-mirror,
+// out-mirror -> master).
+void summary_sketch_csr(Summary& S, const HostAdj& out) {
+  const uint32_t all = S.all_n, n = S.old_n;
+  const bool weighted = !out.w.empty();
+  // sync edges
+  std::vector<std::vector<uint32_t>> syncE(all);
+  for (size_t i = 0; i < S.cluster_in_mirror_ids.size(); ++i) {
+    for (uint32_t m : S.cluster_in_mirror_ids[i]) syncE[S.mirror_master(m)].push_back(m);
+    for (uint32_t m : S.cluster_out_mirror_ids[i]) syncE[m].push_back(S.mirror_master(m));
+  }
+  S.sync_off.assign(all + 1, 0);
+  for (uint32_t i = 0; i < all; ++i) S.sync_off[i + 1] = S.sync_off[i] + syncE[i].size();
+  S.sync_nbr.clear();
+  S.sync_nbr.reserve(S.sync_off[all]);
+  for (uint32_t i = 0; i < all; ++i)
+    for (uint32_t m : syncE[i]) S.sync_nbr.push_back(m);
+  // shortcut and boundary edges
+  auto is_row = [&](uint32_t i) -> const Supernode* {
+    if (i >= n) {
+      const uint32_t sp = S.Fc_map[i];
+      return sp != Summary::kIdDefault ? &S.supernodes[sp] : nullptr;
+    }
+    const char t = S.node_type[i];
+    if (t == kOnlyIn || t == kBothOutIn || t == kBothOutInMaster) return &S.supernodes[S.Fc_map[i]];
+    return nullptr;
+  };
+  auto ib_take = [&](uint32_t u, uint32_t x) {
+    const uint32_t ids = S.id2spids[u];
+    const uint32_t out_ids = S.id2spids[x];
+    const auto& om = S.supernode_out_mirror[ids];
+    if (out_ids != Summary::kIdDefault) {
+      const auto& im = S.supernode_in_mirror[out_ids];
+      return ids != out_ids && om.count(x) == 0 && im.count(u) == 0;
+    }
+    return ids != out_ids && om.count(x) == 0;
+  };
+  S.is_off.assign(all + 1, 0);
+  S.ib_off.assign(all + 1, 0);
+  S.is_nbr.clear();
+  S.is_w.clear();
+  S.ib_nbr.clear();
+  S.ib_w.clear();
+  for (uint32_t i = 0; i < all; ++i) {
+    if (const Supernode* sp = is_row(i)) {
+      std::vector<std::pair<uint32_t, double>> row = sp->bound_delta;
+      std::stable_sort(row.begin(), row.end(),
+                       [](const auto& a, const auto& b) { return a.first < b.first; });
+      for (auto& e : row) {
+        S.is_nbr.push_back(e.first);
+        S.is_w.push_back((float)e.second);
+      }
+    }
+    S.is_off[i + 1] = S.is_nbr.size();
+    if (i < n) {
+      const char t = S.node_type[i];
+      if (t == kOnlyOut || t == kBothOutIn || t == kBothOutInMaster || t == kOutMaster) {
+        for (uint64_t e = out.rp[i]; e < out.rp[i + 1]; ++e)
+          if (ib_take(i, out.col[e])) {
+            S.ib_nbr.push_back(out.col[e]);
+            if (weighted) S.ib_w.push_back(out.w[e]);
+          }
+      } else if (t == kSingle) {
+        for (uint64_t e = out.rp[i]; e < out.rp[i + 1]; ++e) {
+          S.ib_nbr.push_back(out.col[e]);
+          if (weighted) S.ib_w.push_back(out.w[e]);
+        }
+      }
+    }
+    S.ib_off[i + 1] = S.ib_nbr.size();
+  }
+}
+
+// inc_compress_mirror (compressor_base.h:5634-5803): cluster membership and
+// mirrors stay; a deleted edge can retire an entry that has no other outside
+// in-neighbour, an added edge from outside creates an entry; the clusters
+// and supernodes touched by the batch are recorded for shortcut repair.
+void summary_inc_entries(Summary& S, const HostAdj& new_out, const HostAdj& new_in,
+                         const std::vector<std::pair<uint32_t, uint32_t>>& deleted,
+                         const std::vector<std::pair<uint32_t, uint32_t>>& added) {
+  (void)new_out;
+  std::unordered_set<uint32_t> upd_c, upd_s;
+  std::vector<uint32_t> delete_spid;
+  auto touch_source = [&](uint32_t u) {
+    const uint32_t src_id = S.id2spids[u];
+    upd_c.insert(src_id);
+    for (uint32_t s : S.supernode_source[src_id]) upd_s.insert(s);
+    for (uint32_t m : S.cluster_in_mirror_ids[src_id]) upd_s.insert(m);
+    for (uint32_t m : S.vid2in_mirror_mids[u]) {
+      upd_s.insert(m);
+      upd_c.insert(S.id2spids[m]);
+    }
+  };
+  for (const auto& pr : deleted) {
+    const uint32_t u = pr.first, v = pr.second;
+    if (S.Fc[u] != Summary::kFcDefault) touch_source(u);
+    if (S.Fc[v] != Summary::kFcDefault && S.Fc[v] >= 0) {
+      const uint32_t ids = S.id2spids[v];
+      upd_c.insert(ids);
+      if (ids != S.id2spids[u]) {
+        const auto& im = S.supernode_in_mirror[ids];
+        bool outside = false;
+        for (uint64_t e = new_in.rp[v]; e < new_in.rp[v + 1]; ++e) {
+          const uint32_t x = new_in.col[e];
+          if (x != u && ids != S.id2spids[x] && im.count(x) == 0) {
+            outside = true;
+            break;
+          }
+        }
+        if (!outside) {
+          auto& srcs = S.supernode_source[ids];
+          auto it = std::find(srcs.begin(), srcs.end(), v);
+          if (it != srcs.end()) srcs.erase(it);
+          const uint32_t sp = S.Fc_map[v];
+          S.supernodes[sp].clear();
+          delete_spid.push_back(sp);
+          S.Fc[v] = -(int32_t)(ids + 1);
+          S.Fc_map[v] = Summary::kIdDefault;
+        }
+      }
+    }
+  }
+  int del_index = (int)delete_spid.size() - 1;
+  for (const auto& pr : added) {
+    const uint32_t u = pr.first, v = pr.second;
+    if (S.Fc[u] != Summary::kFcDefault) touch_source(u);
+    if (S.Fc[v] != Summary::kFcDefault) {
+      const uint32_t ids = S.id2spids[v];
+      upd_c.insert(ids);
+      const auto& im = S.supernode_in_mirror[ids];
+      if (S.Fc[v] < 0 && ids != S.id2spids[u] && im.count(u) == 0) {
+        S.Fc[v] = (int32_t)ids;
+        S.supernode_source[ids].push_back(v);
+        uint32_t spid;
+        if (del_index >= 0) {
+          spid = delete_spid[del_index--];
+        } else {
+          spid = (uint32_t)S.supernodes.size();
+          S.supernodes.emplace_back();
+        }
+        S.Fc_map[v] = spid;
+        S.supernodes[spid].id = v;
+        S.supernodes[spid].ids = ids;
+        S.supernodes[spid].status = false;
+        upd_s.insert(v);
+      }
+    }
+  }
+  // retired supernode ids that were not reused stay empty (id = kIdDefault)
+  for (int i = 0; i <= del_index; ++i) {
+    S.supernodes[delete_spid[i]].clear();
+    S.supernodes[delete_spid[i]].id = Summary::kIdDefault;
+  }
+  S.update_cluster_ids.assign(upd_c.begin(), upd_c.end());
+  std::sort(S.update_cluster_ids.begin(), S.update_cluster_ids.end());
+  S.update_source_id.assign(upd_s.begin(), upd_s.end());
+  std::sort(S.update_source_id.begin(), S.update_source_id.end());
+}
+
+}  // namespace sg

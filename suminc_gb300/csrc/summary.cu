@@ -1,0 +1,872 @@
+// Summarized-graph PageRank on the device (the reference's SumInc PR path).
+//
+//   shortcut precompute   one CTA per supernode runs the cluster-local
+//                         delta iteration from its entry (delta = 1 at the
+//                         entry) in shared memory with FP64 accumulation and
+//                         returns the converged values / residual deltas
+//                         (build_iter_index_mirror, iter_compressor.h:318-491)
+//   cluster precompute    one CTA per cluster converges the current deltas
+//                         inside the cluster; exits then push the mass that
+//                         passed through them out of the cluster
+//                         (first_step + precompute_spnode_one/two,
+//                         sum_sync_iter_worker.h:348-438,
+//                         iter_compressor.h:534-785)
+//   summarized rounds     entries push deltas along shortcuts into exit
+//                         buffers, exits push along boundary edges (and
+//                         masters through their in-mirrors' shortcuts),
+//                         unclustered vertices push along all their edges,
+//                         out-mirrors hand their buffer to the master
+//                         (sum_sync_iter_worker.h:949-1127)
+//   correction            accumulated entry mass flows to the inner vertices
+//                         through inner_delta / inner_value
+//                         (sum_sync_iter_worker.h:1385-1492)
+// after which the plain rounds of pagerank.cu finish the residual.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <unordered_map>
+
+#include "ctx.h"
+#include "dev.cuh"
+#include "summary.h"
+
+namespace sg {
+
+void host_transpose(const HostAdj& out, HostAdj& in);
+void host_adj_from_csr(uint32_t n, const uint64_t* rp, const uint32_t* col, const float* w,
+                       HostAdj& out);
+
+struct SummaryDev {
+  bool valid = false;
+  uint32_t old_n = 0, all_n = 0;
+  Summary S;
+  HostAdj out, in;  // host copy of the graph the summary was built on
+  // device sketch
+  uint64_t *is_off = nullptr, *ib_off = nullptr, *sync_off = nullptr;
+  uint32_t *is_nbr = nullptr, *ib_nbr = nullptr, *sync_nbr = nullptr;
+  float* is_w = nullptr;
+  uint32_t* out_deg_all = nullptr;       // out-degree of each row (mirrors: master's)
+  uint32_t *l_entry = nullptr, *l_exit = nullptr, *l_single = nullptr, *l_omirror = nullptr;
+  uint32_t n_entry = 0, n_exit = 0, n_single = 0, n_omirror = 0;
+  uint32_t* omirror_master = nullptr;
+  uint8_t* ntype = nullptr;
+  // correction: per row -> supernode, cluster size; supernode CSRs
+  uint32_t *corr_sp = nullptr, *corr_c = nullptr;
+  uint64_t *id_off = nullptr, *iv_off = nullptr;
+  uint32_t *id_nbr = nullptr, *iv_nbr = nullptr;
+  float *id_w = nullptr, *iv_w = nullptr;
+  // cluster precompute: members and subgraph CSR
+  uint64_t *cm_off = nullptr, *sub_off = nullptr;
+  uint32_t *cm_v = nullptr, *sub_nbr = nullptr;
+  uint32_t *bound_list = nullptr;  // exit members per cluster (cm layout)
+  uint64_t* bl_off = nullptr;
+  // state
+  float *bound = nullptr, *spnode = nullptr, *old_x = nullptr;
+  double* d_res = nullptr;
+  std::vector<uint32_t> pending_clusters;  // touched since the last IncEval
+};
+
+static SummaryDev* sdev(sg_ctx* ctx) { return (SummaryDev*)ctx->summary; }
+
+static void sfree(SummaryDev& D) {
+  dfree(D.is_off); dfree(D.ib_off); dfree(D.sync_off);
+  dfree(D.is_nbr); dfree(D.ib_nbr); dfree(D.sync_nbr); dfree(D.is_w);
+  dfree(D.out_deg_all);
+  dfree(D.l_entry); dfree(D.l_exit); dfree(D.l_single); dfree(D.l_omirror);
+  dfree(D.omirror_master); dfree(D.ntype);
+  dfree(D.corr_sp); dfree(D.corr_c);
+  dfree(D.id_off); dfree(D.iv_off); dfree(D.id_nbr); dfree(D.iv_nbr); dfree(D.id_w); dfree(D.iv_w);
+  dfree(D.cm_off); dfree(D.sub_off); dfree(D.cm_v); dfree(D.sub_nbr);
+  dfree(D.bound_list); dfree(D.bl_off);
+  dfree(D.bound); dfree(D.spnode); dfree(D.old_x); dfree(D.d_res);
+}
+
+sg_status summary_free(sg_ctx* ctx) {
+  SummaryDev* D = sdev(ctx);
+  if (!D) return SG_OK;
+  sfree(*D);
+  delete D;
+  ctx->summary = nullptr;
+  return SG_OK;
+}
+
+template <typename T>
+static sg_status upload(sg_ctx* ctx, T** d, const std::vector<T>& h) {
+  dfree(*d);
+  SG_TRY(dalloc(ctx, d, std::max<size_t>(h.size(), 1)));
+  if (!h.empty())
+    SG_CUDA(ctx, cudaMemcpyAsync(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+  return SG_OK;
+}
+
+// ------------------------------------------------------ shortcut kernel
+
+struct ShortcutArgs {
+  uint32_t n_sp;
+  const uint32_t* sp_cluster;   // cluster of each supernode job
+  const uint32_t* sp_src;       // local index of the entry
+  const uint64_t* cl_off;       // local node range of each cluster [cl_off[c], cl_off[c+1])
+  const uint32_t* cl_inner;     // number of members (iterated nodes) of each cluster
+  const uint64_t* adj_off;      // per local node (global local index) edge range
+  const uint32_t* adj_nbr;      // local target index (relative to the cluster)
+  const float* div;             // out-degree divisor per local node
+  const uint64_t* out_off;      // per job output offset
+  double* out_value;
+  double* out_delta;
+  float damping;
+  double thr_per_node;          // threshold / N
+};
+
+__global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A) {
+  extern __shared__ double sm[];
+  const uint32_t s = blockIdx.x;
+  if (s >= A.n_sp) return;
+  const uint32_t c = A.sp_cluster[s];
+  const uint64_t l0 = A.cl_off[c];
+  const uint32_t L = (uint32_t)(A.cl_off[c + 1] - l0);
+  const uint32_t inner = A.cl_inner[c];
+  const uint32_t src = A.sp_src[s];
+  double* value = sm;
+  double* delta = sm + L;
+  double* next = sm + 2 * L;
+  __shared__ double s_diff;
+  for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) {
+    value[i] = 0.0;
+    delta[i] = (i == src) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  // an in-mirror entry first sends its unit along its edges into the cluster
+  if (src >= inner) {
+    const uint64_t e0 = A.adj_off[l0 + src], e1 = A.adj_off[l0 + src + 1];
+    const double outv = (double)A.damping / (double)A.div[l0 + src];
+    for (uint64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) atomicAdd(&delta[A.adj_nbr[e]], outv);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      value[src] += 1.0;
+      delta[src] = 0.0;
+    }
+    __syncthreads();
+  }
+  const double thr = A.thr_per_node * (double)inner;
+  for (int step = 1;; ++step) {
+    if (threadIdx.x == 0) s_diff = 0.0;
+    for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) next[i] = i < inner ? 0.0 : delta[i];
+    __syncthreads();
+    double diff = 0.0;
+    for (uint32_t i = threadIdx.x; i < inner; i += blockDim.x) {
+      const double ts = delta[i];
+      if (ts == 0.0) continue;
+      value[i] += ts;
+      diff += fabs(ts);
+      const double outv = ts * (double)A.damping / (double)A.div[l0 + i];
+      for (uint64_t e = A.adj_off[l0 + i]; e < A.adj_off[l0 + i + 1]; ++e)
+        atomicAdd(&next[A.adj_nbr[e]], outv);
+    }
+    if (diff != 0.0) atomicAdd(&s_diff, diff);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) delta[i] = next[i];
+    __syncthreads();
+    const double d_all = s_diff;
+    __syncthreads();
+    if (d_all <= thr || step > 100) break;
+  }
+  const uint64_t o = A.out_off[s];
+  for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) {
+    A.out_value[o + i] = value[i];
+    A.out_delta[o + i] = delta[i];
+  }
+}
+
+// Builds the local problems of the given supernodes, runs the kernel and
+// writes inner_value / inner_delta / bound_delta back into the summary.
+static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector<uint32_t>& spids) {
+  Summary& S = D.S;
+  if (spids.empty()) return SG_OK;
+  // clusters involved
+  std::unordered_map<uint32_t, uint32_t> cl_index;
+  std::vector<uint32_t> cls;
+  for (uint32_t sp : spids) {
+    const uint32_t c = S.supernodes[sp].ids;
+    if (cl_index.emplace(c, (uint32_t)cls.size()).second) cls.push_back(c);
+  }
+  std::vector<uint64_t> cl_off(cls.size() + 1, 0), adj_off(1, 0);
+  std::vector<uint32_t> cl_inner(cls.size()), adj_nbr;
+  std::vector<float> div;
+  std::vector<uint32_t> local_of(S.all_n, 0xFFFFFFFFu);
+  size_t maxL = 1;
+  for (size_t k = 0; k < cls.size(); ++k) {
+    const uint32_t c = cls[k];
+    const auto& nodes = S.cluster_ids[c];  // members first, then mirror ids
+    const uint32_t inner = (uint32_t)S.supernode_ids[c].size();
+    cl_inner[k] = inner;
+    for (uint32_t i = 0; i < nodes.size(); ++i) local_of[nodes[i]] = i;
+    for (uint32_t i = 0; i < nodes.size(); ++i) {
+      const uint32_t v = nodes[i];
+      const uint32_t master = v < S.old_n ? v : S.mirror_master(v);
+      div.push_back((float)std::max<uint64_t>(D.out.deg(master), 1));
+      for (uint32_t t : S.subgraph[v]) adj_nbr.push_back(local_of[t]);
+      adj_off.push_back(adj_nbr.size());
+    }
+    cl_off[k + 1] = cl_off[k] + nodes.size();
+    maxL = std::max(maxL, nodes.size());
+    for (uint32_t v : nodes) local_of[v] = 0xFFFFFFFFu;
+  }
+  std::vector<uint32_t> sp_cluster(spids.size()), sp_src(spids.size());
+  std::vector<uint64_t> out_off(spids.size() + 1, 0);
+  for (size_t j = 0; j < spids.size(); ++j) {
+    const Supernode& sp = S.supernodes[spids[j]];
+    const uint32_t k = cl_index[sp.ids];
+    sp_cluster[j] = k;
+    const auto& nodes = S.cluster_ids[sp.ids];
+    uint32_t src = 0;
+    for (uint32_t i = 0; i < nodes.size(); ++i)
+      if (nodes[i] == sp.id) src = i;
+    sp_src[j] = src;
+    out_off[j + 1] = out_off[j] + (cl_off[k + 1] - cl_off[k]);
+  }
+  const size_t smem = 3 * maxL * sizeof(double);
+  if (smem > 200 * 1024) return fail(ctx, SG_ERR_UNSUPPORTED, "cluster too large for the shortcut kernel");
+  uint32_t *d_spc = nullptr, *d_src = nullptr, *d_inner = nullptr, *d_adj = nullptr;
+  uint64_t *d_cloff = nullptr, *d_adjoff = nullptr, *d_outoff = nullptr;
+  float* d_div = nullptr;
+  double *d_val = nullptr, *d_del = nullptr;
+  SG_TRY(upload(ctx, &d_spc, sp_cluster));
+  SG_TRY(upload(ctx, &d_src, sp_src));
+  SG_TRY(upload(ctx, &d_inner, cl_inner));
+  SG_TRY(upload(ctx, &d_adj, adj_nbr));
+  SG_TRY(upload(ctx, &d_cloff, cl_off));
+  SG_TRY(upload(ctx, &d_adjoff, adj_off));
+  SG_TRY(upload(ctx, &d_outoff, out_off));
+  SG_TRY(upload(ctx, &d_div, div));
+  SG_TRY(dalloc(ctx, &d_val, std::max<uint64_t>(out_off.back(), 1)));
+  SG_TRY(dalloc(ctx, &d_del, std::max<uint64_t>(out_off.back(), 1)));
+  ShortcutArgs A;
+  A.n_sp = (uint32_t)spids.size();
+  A.sp_cluster = d_spc;
+  A.sp_src = d_src;
+  A.cl_off = d_cloff;
+  A.cl_inner = d_inner;
+  A.adj_off = d_adjoff;
+  A.adj_nbr = d_adj;
+  A.div = d_div;
+  A.out_off = d_outoff;
+  A.out_value = d_val;
+  A.out_delta = d_del;
+  A.damping = (float)ctx->opt.damping;
+  A.thr_per_node = ctx->opt.termcheck_threshold / (double)S.old_n;
+  if (smem > 48 * 1024)
+    SG_CUDA(ctx, cudaFuncSetAttribute(k_shortcuts, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  kprof_begin(ctx);
+  k_shortcuts<<<A.n_sp, 128, smem, ctx->stream>>>(A);
+  kprof_end(ctx, SG_K_SUMMARY);
+  SG_CUDA(ctx, cudaGetLastError());
+  std::vector<double> val(out_off.back()), del(out_off.back());
+  SG_CUDA(ctx, cudaMemcpyAsync(val.data(), d_val, 8 * val.size(), cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaMemcpyAsync(del.data(), d_del, 8 * del.size(), cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  dfree(d_spc); dfree(d_src); dfree(d_inner); dfree(d_adj); dfree(d_cloff); dfree(d_adjoff);
+  dfree(d_outoff); dfree(d_div); dfree(d_val); dfree(d_del);
+  // fianl_build_iter_index_for_mirror (iter_compressor.h:433-491)
+  for (size_t j = 0; j < spids.size(); ++j) {
+    Supernode& sp = S.supernodes[spids[j]];
+    const uint32_t c = sp.ids;
+    const auto& nodes = S.cluster_ids[c];
+    const uint32_t inner = (uint32_t)S.supernode_ids[c].size();
+    const uint64_t o = out_off[j];
+    sp.inner_value.clear();
+    sp.inner_delta.clear();
+    sp.bound_delta.clear();
+    sp.status = true;
+    for (uint32_t i = 0; i < inner; ++i) {
+      const uint32_t v = nodes[i];
+      if (val[o + i] != 0.0) {
+        if (S.out_bound[v]) sp.bound_delta.push_back({v, val[o + i]});
+        else sp.inner_value.push_back({v, val[o + i]});
+      }
+      if (del[o + i] != 0.0) sp.inner_delta.push_back({v, del[o + i]});
+    }
+    const auto& om = S.cluster_out_mirror_ids[c];
+    for (uint32_t m : om) {
+      uint32_t i = 0;
+      while (nodes[i] != m) ++i;
+      const double v = val[o + i] + del[o + i];
+      if (v != 0.0) sp.bound_delta.push_back({m, v});
+    }
+  }
+  return SG_OK;
+}
+
+// ------------------------------------------------------ device sketch upload
+
+static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
+  Summary& S = D.S;
+  const uint32_t all = S.all_n, n = S.old_n;
+  SG_TRY(upload(ctx, &D.is_off, S.is_off));
+  SG_TRY(upload(ctx, &D.is_nbr, S.is_nbr));
+  SG_TRY(upload(ctx, &D.is_w, S.is_w));
+  SG_TRY(upload(ctx, &D.ib_off, S.ib_off));
+  SG_TRY(upload(ctx, &D.ib_nbr, S.ib_nbr));
+  SG_TRY(upload(ctx, &D.sync_off, S.sync_off));
+  SG_TRY(upload(ctx, &D.sync_nbr, S.sync_nbr));
+  std::vector<uint32_t> odeg(all);
+  for (uint32_t v = 0; v < all; ++v)
+    odeg[v] = (uint32_t)D.out.deg(v < n ? v : S.mirror_master(v));
+  SG_TRY(upload(ctx, &D.out_deg_all, odeg));
+  std::vector<uint32_t> le, lx, ls;
+  std::vector<uint8_t> nt(n);
+  for (uint32_t v = 0; v < n; ++v) {
+    const char t = S.node_type[v];
+    nt[v] = (uint8_t)t;
+    if (t == kOnlyIn || t == kBothOutIn || t == kBothOutInMaster) le.push_back(v);
+    if (t == kOnlyOut || t == kBothOutIn || t == kOutMaster || t == kBothOutInMaster) lx.push_back(v);
+    if (t == kSingle) ls.push_back(v);
+  }
+  SG_TRY(upload(ctx, &D.ntype, nt));
+  SG_TRY(upload(ctx, &D.l_entry, le));
+  SG_TRY(upload(ctx, &D.l_exit, lx));
+  SG_TRY(upload(ctx, &D.l_single, ls));
+  D.n_entry = (uint32_t)le.size();
+  D.n_exit = (uint32_t)lx.size();
+  D.n_single = (uint32_t)ls.size();
+  std::vector<uint32_t> om, omm;
+  for (uint32_t m : S.all_out_mirror) {
+    om.push_back(m);
+    omm.push_back(S.mirror_master(m));
+  }
+  SG_TRY(upload(ctx, &D.l_omirror, om));
+  SG_TRY(upload(ctx, &D.omirror_master, omm));
+  D.n_omirror = (uint32_t)om.size();
+  // correction tables
+  std::vector<uint32_t> csp(all, 0xFFFFFFFFu), cc(all, 0);
+  std::vector<uint64_t> ido(1, 0), ivo(1, 0);
+  std::vector<uint32_t> idn, ivn;
+  std::vector<float> idw, ivw;
+  for (uint32_t sp = 0; sp < S.supernodes.size(); ++sp) {
+    const Supernode& s = S.supernodes[sp];
+    for (auto& e : s.inner_delta) {
+      idn.push_back(e.first);
+      idw.push_back((float)e.second);
+    }
+    for (auto& e : s.inner_value) {
+      ivn.push_back(e.first);
+      ivw.push_back((float)e.second);
+    }
+    ido.push_back(idn.size());
+    ivo.push_back(ivn.size());
+  }
+  for (uint32_t u = 0; u < all; ++u) {
+    const uint32_t sp = S.Fc_map[u];
+    if (sp == Summary::kIdDefault || sp >= S.supernodes.size()) continue;
+    if (S.supernodes[sp].id != u) continue;
+    csp[u] = sp;
+    cc[u] = (uint32_t)S.supernode_ids[S.id2spids[u]].size();
+  }
+  SG_TRY(upload(ctx, &D.corr_sp, csp));
+  SG_TRY(upload(ctx, &D.corr_c, cc));
+  SG_TRY(upload(ctx, &D.id_off, ido));
+  SG_TRY(upload(ctx, &D.iv_off, ivo));
+  SG_TRY(upload(ctx, &D.id_nbr, idn));
+  SG_TRY(upload(ctx, &D.iv_nbr, ivn));
+  SG_TRY(upload(ctx, &D.id_w, idw));
+  SG_TRY(upload(ctx, &D.iv_w, ivw));
+  // cluster members and subgraph CSR (over all rows)
+  std::vector<uint64_t> cmo(1, 0), subo(1, 0), blo(1, 0);
+  std::vector<uint32_t> cmv, subn, bl;
+  for (size_t c = 0; c < S.supernode_ids.size(); ++c) {
+    for (uint32_t v : S.supernode_ids[c]) {
+      cmv.push_back(v);
+      if (S.out_bound[v]) bl.push_back(v);
+    }
+    cmo.push_back(cmv.size());
+    blo.push_back(bl.size());
+  }
+  for (uint32_t v = 0; v < all; ++v) {
+    for (uint32_t t : S.subgraph[v]) subn.push_back(t);
+    subo.push_back(subn.size());
+  }
+  SG_TRY(upload(ctx, &D.cm_off, cmo));
+  SG_TRY(upload(ctx, &D.cm_v, cmv));
+  SG_TRY(upload(ctx, &D.sub_off, subo));
+  SG_TRY(upload(ctx, &D.sub_nbr, subn));
+  SG_TRY(upload(ctx, &D.bl_off, blo));
+  SG_TRY(upload(ctx, &D.bound_list, bl));
+  if (!D.bound) {
+    SG_TRY(dalloc(ctx, &D.bound, all));
+    SG_TRY(dalloc(ctx, &D.spnode, all));
+    SG_TRY(dalloc(ctx, &D.old_x, n));
+    SG_TRY(dalloc(ctx, &D.d_res, 2));
+  }
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+// ------------------------------------------------------ build entry point
+
+sg_status summary_build(sg_ctx* ctx, const std::vector<std::vector<uint32_t>>& clusters) {
+  if (!ctx->g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
+  summary_free(ctx);
+  SummaryDev* D = new SummaryDev();
+  ctx->summary = D;
+  // host copy of the graph (rows sorted, as the reference fragment keeps them)
+  const uint32_t n = ctx->g.n;
+  const uint64_t m = ctx->g.m;
+  std::vector<uint64_t> rp(n + 1);
+  std::vector<uint32_t> col(m);
+  std::vector<float> w(ctx->g.weighted ? m : 0);
+  SG_TRY(download_csr(ctx, rp.data(), col.data(), ctx->g.weighted ? w.data() : nullptr));
+  host_adj_from_csr(n, rp.data(), col.data(), ctx->g.weighted ? w.data() : nullptr, D->out);
+  host_transpose(D->out, D->in);
+  Summary& S = D->S;
+  summary_from_clusters(S, D->out, D->in, clusters, ctx->opt.min_node_num, ctx->opt.mirror_k,
+                        ctx->opt.compress_threshold);
+  summary_judge_out_bound(S, D->out, nullptr);
+  summary_build_subgraph(S, D->out, D->in, nullptr);
+  std::vector<uint32_t> all_sp(S.supernodes.size());
+  for (uint32_t i = 0; i < all_sp.size(); ++i) all_sp[i] = i;
+  SG_TRY(compute_shortcuts(ctx, *D, all_sp));
+  summary_node_types(S);
+  summary_sketch_csr(S, D->out);
+  D->old_n = S.old_n;
+  D->all_n = S.all_n;
+  SG_TRY(upload_sketch(ctx, *D));
+  D->valid = true;
+  return SG_OK;
+}
+
+// ------------------------------------------------------ PageRank kernels
+
+struct SumArgs {
+  float damping;
+  float thr_v;
+  uint32_t old_n;
+  float* x;
+  float* delta;
+  float* bound;
+  float* spnode;
+  const uint64_t *is_off, *ib_off, *sync_off;
+  const uint32_t *is_nbr, *ib_nbr, *sync_nbr;
+  const float* is_w;
+  const uint32_t* out_deg_all;
+  const uint8_t* ntype;
+  unsigned long long* cnt;  // [0] edges, [1] shortcut edges
+};
+
+// mass a (mirror) entry receives goes along its shortcuts into exit buffers
+__device__ __forceinline__ void entry_push(const SumArgs& A, uint32_t u, float d, uint32_t lane,
+                                           unsigned long long& sc) {
+  for (uint64_t e = A.is_off[u] + lane; e < A.is_off[u + 1]; e += 32)
+    atomicAdd(&A.bound[A.is_nbr[e]], A.is_w[e] * d);
+  if (lane == 0) {
+    atomicAdd(&A.spnode[u], d);
+    sc += A.is_off[u + 1] - A.is_off[u];
+  }
+}
+
+__global__ void __launch_bounds__(256) k_sum_entries(SumArgs A, const uint32_t* list, uint32_t cnt) {
+  const uint32_t lane = threadIdx.x & 31;
+  unsigned long long sc = 0;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt;
+       i += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t u = list[i];
+    float d = 0.f;
+    if (lane == 0) {
+      d = A.delta[u];
+      d = fabsf(d) > A.thr_v ? atomicExch(&A.delta[u], 0.f) : 0.f;
+    }
+    d = __shfl_sync(0xffffffffu, d, 0);
+    if (d != 0.f) entry_push(A, u, d, lane, sc);
+  }
+  if (lane == 0 && sc) atomicAdd(&A.cnt[1], sc);
+}
+
+__global__ void __launch_bounds__(256) k_sum_exits(SumArgs A, const uint32_t* list, uint32_t cnt) {
+  const uint32_t lane = threadIdx.x & 31;
+  unsigned long long ed = 0, sc = 0;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt;
+       i += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t u = list[i];
+    float b = 0.f;
+    if (lane == 0) {
+      b = A.bound[u];
+      b = fabsf(b) > A.thr_v ? atomicExch(&A.bound[u], 0.f) : 0.f;
+      if (b != 0.f) A.x[u] += b;
+    }
+    b = __shfl_sync(0xffffffffu, b, 0);
+    if (b == 0.f) continue;
+    // boundary edges with the original out-degree (g_function, pagerank_ingress.h:75-99)
+    const float outv = b * A.damping / (float)A.out_deg_all[u];
+    for (uint64_t e = A.ib_off[u] + lane; e < A.ib_off[u + 1]; e += 32)
+      atomicAdd(&A.delta[A.ib_nbr[e]], outv);
+    if (lane == 0) ed += A.ib_off[u + 1] - A.ib_off[u];
+    // a master forwards to its in-mirrors, which push at once
+    const uint8_t t = A.ntype[u];
+    if (t == kOutMaster || t == kBothOutInMaster) {
+      for (uint64_t s = A.sync_off[u]; s < A.sync_off[u + 1]; ++s) {
+        const uint32_t mm = A.sync_nbr[s];
+        float dm = 0.f;
+        if (lane == 0) {
+          atomicAdd(&A.delta[mm], b);
+          dm = atomicExch(&A.delta[mm], 0.f);
+        }
+        dm = __shfl_sync(0xffffffffu, dm, 0);
+        if (dm != 0.f) entry_push(A, mm, dm, lane, sc);
+      }
+    }
+  }
+  if (lane == 0) {
+    if (ed) atomicAdd(&A.cnt[0], ed);
+    if (sc) atomicAdd(&A.cnt[1], sc);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_sum_singles(SumArgs A, const uint32_t* list, uint32_t cnt) {
+  const uint32_t lane = threadIdx.x & 31;
+  unsigned long long ed = 0;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt;
+       i += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t u = list[i];
+    float d = 0.f;
+    if (lane == 0) {
+      d = A.delta[u];
+      d = fabsf(d) > A.thr_v ? atomicExch(&A.delta[u], 0.f) : 0.f;
+      if (d != 0.f) A.x[u] += d;
+    }
+    d = __shfl_sync(0xffffffffu, d, 0);
+    if (d == 0.f) continue;
+    const uint64_t e0 = A.ib_off[u], e1 = A.ib_off[u + 1];
+    if (e1 == e0) continue;
+    const float outv = d * A.damping / (float)(e1 - e0);
+    for (uint64_t e = e0 + lane; e < e1; e += 32) atomicAdd(&A.delta[A.ib_nbr[e]], outv);
+    if (lane == 0) ed += e1 - e0;
+  }
+  if (lane == 0 && ed) atomicAdd(&A.cnt[0], ed);
+}
+
+__global__ void k_sum_omirror(SumArgs A, const uint32_t* list, const uint32_t* master, uint32_t cnt) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const uint32_t m = list[i];
+    if (fabsf(A.bound[m]) > A.thr_v) atomicAdd(&A.delta[master[i]], atomicExch(&A.bound[m], 0.f));
+  }
+}
+
+__global__ void __launch_bounds__(256) k_sum_residual(uint32_t n, const float* delta, double* res) {
+  __shared__ double s_red[8];
+  double r = 0.0;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    r += fabs((double)delta[v]);
+  const double b = block_sum<256>(r, s_red);
+  if (threadIdx.x == 0) atomicAdd(res, b);
+}
+
+// correction through inner_delta / inner_value (warp per row)
+__global__ void __launch_bounds__(256) k_sum_correct(SumArgs A, uint32_t all_n, const uint32_t* corr_sp,
+                                                     const uint32_t* corr_c, const uint64_t* id_off,
+                                                     const uint32_t* id_nbr, const float* id_w,
+                                                     const uint64_t* iv_off, const uint32_t* iv_nbr,
+                                                     const float* iv_w) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < all_n;
+       u += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t sp = corr_sp[u];
+    if (sp == 0xFFFFFFFFu) continue;
+    const float d = A.spnode[u];
+    if (!(fabsf(d) * (float)corr_c[u] > A.thr_v)) continue;
+    for (uint64_t e = id_off[sp] + lane; e < id_off[sp + 1]; e += 32)
+      atomicAdd(&A.delta[id_nbr[e]], d * id_w[e]);
+    for (uint64_t e = iv_off[sp] + lane; e < iv_off[sp + 1]; e += 32)
+      atomicAdd(&A.x[iv_nbr[e]], d * iv_w[e]);
+    __syncwarp();
+    if (lane == 0) A.spnode[u] = 0.f;
+  }
+}
+
+// cluster-local convergence of the current deltas (CTA per cluster)
+__global__ void __launch_bounds__(256) k_sum_precompute(SumArgs A, const uint32_t* clusters,
+                                                        uint32_t n_cl, const uint64_t* cm_off,
+                                                        const uint32_t* cm_v,
+                                                        const uint64_t* sub_off,
+                                                        const uint32_t* sub_nbr, double thr_v) {
+  __shared__ double s_diff;
+  for (uint32_t k = blockIdx.x; k < n_cl; k += gridDim.x) {
+    const uint32_t c = clusters[k];
+    const uint64_t b = cm_off[c], e = cm_off[c + 1];
+    const double thr = thr_v * (double)(e - b);
+    for (int step = 1;; ++step) {
+      if (threadIdx.x == 0) s_diff = 0.0;
+      __syncthreads();
+      double diff = 0.0;
+      for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        const uint32_t v = cm_v[i];
+        const float ts = atomicExch(&A.delta[v], 0.f);
+        if (ts == 0.f) continue;
+        A.x[v] += ts;
+        diff += fabs((double)ts);
+        const float outv = ts * A.damping / (float)A.out_deg_all[v];
+        for (uint64_t f = sub_off[v]; f < sub_off[v + 1]; ++f) atomicAdd(&A.delta[sub_nbr[f]], outv);
+      }
+      if (diff != 0.0) atomicAdd(&s_diff, diff);
+      __syncthreads();
+      const double d = s_diff;
+      __syncthreads();
+      if (d <= thr || step > 100) break;
+    }
+  }
+}
+
+// exits of the precomputed clusters push the mass that passed through them
+__global__ void __launch_bounds__(256) k_sum_bound_push(SumArgs A, const uint32_t* clusters, uint32_t n_cl,
+                                                        const uint64_t* bl_off, const uint32_t* bl) {
+  const uint32_t lane = threadIdx.x & 31;
+  unsigned long long sc = 0;
+  for (uint32_t k = blockIdx.x; k < n_cl; k += gridDim.x) {
+    const uint32_t c = clusters[k];
+    for (uint64_t i = bl_off[c] + (threadIdx.x >> 5); i < bl_off[c + 1]; i += blockDim.x >> 5) {
+      const uint32_t u = bl[i];
+      const float val = A.x[u];
+      if (val == 0.f) continue;
+      const float outv = val * A.damping / (float)A.out_deg_all[u];
+      for (uint64_t e = A.ib_off[u] + lane; e < A.ib_off[u + 1]; e += 32)
+        atomicAdd(&A.delta[A.ib_nbr[e]], outv);
+      for (uint64_t s = A.sync_off[u]; s < A.sync_off[u + 1]; ++s) {
+        const uint32_t mm = A.sync_nbr[s];
+        float dm = 0.f;
+        if (lane == 0) {
+          atomicAdd(&A.delta[mm], val);
+          dm = atomicExch(&A.delta[mm], 0.f);
+        }
+        dm = __shfl_sync(0xffffffffu, dm, 0);
+        if (dm != 0.f) entry_push(A, mm, dm, lane, sc);
+      }
+    }
+  }
+}
+
+__global__ void k_sum_mirror_to_master(float* delta, const uint32_t* om, const uint32_t* master,
+                                       uint32_t cnt) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const float d = atomicExch(&delta[om[i]], 0.f);
+    if (d != 0.f) atomicAdd(&delta[master[i]], d);
+  }
+}
+
+__global__ void k_stash_x(uint32_t n, float* x, float* old_x, int restore) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    if (restore) {
+      x[v] += old_x[v];
+    } else {
+      old_x[v] = x[v];
+      x[v] = 0.f;
+    }
+  }
+}
+
+static SumArgs sum_args(sg_ctx* ctx, SummaryDev& D, unsigned long long* cnt) {
+  SumArgs A;
+  A.damping = (float)ctx->opt.damping;
+  A.thr_v = (float)(ctx->opt.termcheck_threshold / (double)D.old_n);
+  A.old_n = D.old_n;
+  A.x = ctx->pr.x;
+  A.delta = ctx->pr.delta;
+  A.bound = D.bound;
+  A.spnode = D.spnode;
+  A.is_off = D.is_off; A.ib_off = D.ib_off; A.sync_off = D.sync_off;
+  A.is_nbr = D.is_nbr; A.ib_nbr = D.ib_nbr; A.sync_nbr = D.sync_nbr;
+  A.is_w = D.is_w;
+  A.out_deg_all = D.out_deg_all;
+  A.ntype = D.ntype;
+  A.cnt = cnt;
+  return A;
+}
+
+// first_step: precompute the given clusters (all for PEval), push exits,
+// hand out-mirror deltas to their masters
+static sg_status first_step(sg_ctx* ctx, SummaryDev& D, const std::vector<uint32_t>& cls,
+                            unsigned long long* cnt) {
+  cudaStream_t st = ctx->stream;
+  SumArgs A = sum_args(ctx, D, cnt);
+  SG_CUDA(ctx, cudaMemsetAsync(D.bound, 0, 4ull * D.all_n, st));
+  SG_CUDA(ctx, cudaMemsetAsync(D.spnode, 0, 4ull * D.all_n, st));
+  if (cls.empty()) return SG_OK;
+  uint32_t* d_cls = nullptr;
+  SG_TRY(upload(ctx, &d_cls, cls));
+  k_stash_x<<<grid_for(D.old_n, 256), 256, 0, st>>>(D.old_n, ctx->pr.x, D.old_x, 0);
+  k_sum_precompute<<<std::min<uint32_t>((uint32_t)cls.size(), ctx->num_sms * 8), 256, 0, st>>>(
+      A, d_cls, (uint32_t)cls.size(), D.cm_off, D.cm_v, D.sub_off, D.sub_nbr,
+      ctx->opt.termcheck_threshold / (double)D.old_n);
+  k_sum_bound_push<<<std::min<uint32_t>((uint32_t)cls.size(), ctx->num_sms * 8), 256, 0, st>>>(
+      A, d_cls, (uint32_t)cls.size(), D.bl_off, D.bound_list);
+  if (D.n_omirror)
+    k_sum_mirror_to_master<<<grid_for(D.n_omirror, 256), 256, 0, st>>>(ctx->pr.delta, D.l_omirror,
+                                                                      D.omirror_master, D.n_omirror);
+  k_stash_x<<<grid_for(D.old_n, 256), 256, 0, st>>>(D.old_n, ctx->pr.x, D.old_x, 1);
+  count_launch(ctx, 5);
+  SG_CUDA(ctx, cudaGetLastError());
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  dfree(d_cls);
+  return SG_OK;
+}
+
+// summarized rounds until the residual test passes, then the correction
+static sg_status summarized_rounds(sg_ctx* ctx, SummaryDev& D, unsigned long long* cnt,
+                                   int* rounds_out) {
+  cudaStream_t st = ctx->stream;
+  SumArgs A = sum_args(ctx, D, cnt);
+  const double tau = ctx->opt.termcheck_threshold;
+  const int cap = ctx->opt.max_rounds > 0 ? ctx->opt.max_rounds : 1000;
+  int r = 0;
+  for (; r < cap; ++r) {
+    kprof_begin(ctx);
+    if (D.n_entry) k_sum_entries<<<grid_for((uint64_t)D.n_entry * 32, 256), 256, 0, st>>>(A, D.l_entry, D.n_entry);
+    if (D.n_exit) k_sum_exits<<<grid_for((uint64_t)D.n_exit * 32, 256), 256, 0, st>>>(A, D.l_exit, D.n_exit);
+    if (D.n_single) k_sum_singles<<<grid_for((uint64_t)D.n_single * 32, 256), 256, 0, st>>>(A, D.l_single, D.n_single);
+    if (D.n_omirror) k_sum_omirror<<<grid_for(D.n_omirror, 256), 256, 0, st>>>(A, D.l_omirror, D.omirror_master, D.n_omirror);
+    SG_CUDA(ctx, cudaMemsetAsync(D.d_res, 0, 8, st));
+    k_sum_residual<<<grid_for(D.old_n, 256), 256, 0, st>>>(D.old_n, ctx->pr.delta, D.d_res);
+    kprof_end(ctx, SG_K_SUMMARY);
+    count_launch(ctx, 4);
+    double R = 0;
+    SG_CUDA(ctx, cudaMemcpyAsync(&R, D.d_res, 8, cudaMemcpyDeviceToHost, st));
+    SG_CUDA(ctx, cudaStreamSynchronize(st));
+    if (R < tau) {
+      ++r;
+      break;
+    }
+  }
+  k_sum_correct<<<grid_for((uint64_t)D.all_n * 32, 256), 256, 0, st>>>(
+      A, D.all_n, D.corr_sp, D.corr_c, D.id_off, D.id_nbr, D.id_w, D.iv_off, D.iv_nbr, D.iv_w);
+  count_launch(ctx);
+  SG_CUDA(ctx, cudaGetLastError());
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  *rounds_out = r;
+  return SG_OK;
+}
+
+sg_status pr_summarized(sg_ctx* ctx, bool inc) {
+  SummaryDev* D = sdev(ctx);
+  if (!D || !D->valid) return fail(ctx, SG_ERR_STATE, "compress=1 needs sg_summary_build first");
+  PrState& s = ctx->pr;
+  cudaStream_t st = ctx->stream;
+  unsigned long long* cnt = nullptr;
+  SG_TRY(dalloc(ctx, &cnt, 2));
+  SG_CUDA(ctx, cudaMemsetAsync(cnt, 0, 16, st));
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+  std::vector<uint32_t> cls;
+  if (!inc) {
+    const float init_c = (float)((1.0 - ctx->opt.damping) / (double)ctx->g.n);
+    std::vector<float> z(D->all_n, 0.f), dl(D->all_n, 0.f);
+    for (uint32_t v = 0; v < D->old_n; ++v) dl[v] = init_c;
+    SG_CUDA(ctx, cudaMemcpyAsync(s.x, z.data(), 4ull * D->all_n, cudaMemcpyHostToDevice, st));
+    SG_CUDA(ctx, cudaMemcpyAsync(s.delta, dl.data(), 4ull * D->all_n, cudaMemcpyHostToDevice, st));
+    SG_CUDA(ctx, cudaStreamSynchronize(st));
+    for (uint32_t c = 0; c < D->S.supernode_ids.size(); ++c) cls.push_back(c);
+  } else {
+    cls = D->pending_clusters;
+    D->pending_clusters.clear();
+  }
+  SG_TRY(first_step(ctx, *D, cls, cnt));
+  int srounds = 0;
+  SG_TRY(summarized_rounds(ctx, *D, cnt, &srounds));
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+  unsigned long long hc[2];
+  SG_CUDA(ctx, cudaMemcpyAsync(hc, cnt, 16, cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  float ms_sum = 0.f;
+  cudaEventElapsedTime(&ms_sum, ctx->ev0, ctx->ev1);
+  dfree(cnt);
+  // the plain rounds finish the residual on the original graph
+  s.valid = true;
+  sg_status stt = pr_run(ctx, true);
+  ctx->stats.rounds += srounds;
+  ctx->stats.edges_relaxed += hc[0] + hc[1];
+  ctx->stats.shortcut_edges = hc[1];
+  ctx->stats.elapsed_ms += ms_sum;
+  return stt;
+}
+
+// After sg_apply_updates on a summarized graph: entry changes, exits,
+// subgraphs and shortcuts of the touched clusters, node types and sketch.
+sg_status summary_after_apply(sg_ctx* ctx) {
+  SummaryDev* D = sdev(ctx);
+  if (!D || !D->valid) return SG_OK;
+  const DevBatch& B = ctx->batch;
+  // deleted / added pairs of the batch (actions are small; copy to host)
+  const uint64_t na = B.n_act;
+  std::vector<uint32_t> as(na), ad(na), ak(na), af(na);
+  SG_CUDA(ctx, cudaMemcpyAsync(as.data(), B.a_src, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaMemcpyAsync(ad.data(), B.a_dst, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaMemcpyAsync(ak.data(), B.a_kind, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaMemcpyAsync(af.data(), B.a_found, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  std::vector<std::pair<uint32_t, uint32_t>> deleted, added;
+  for (uint64_t i = 0; i < na; ++i) {
+    if ((ak[i] & 1u) && af[i] != kInvalidVid) deleted.push_back({as[i], ad[i]});
+    if (ak[i] & 2u) added.push_back({as[i], ad[i]});
+  }
+  // new graph on the host
+  const uint32_t n = ctx->g.n;
+  const uint64_t m = ctx->g.m;
+  std::vector<uint64_t> rp(n + 1);
+  std::vector<uint32_t> col(m);
+  std::vector<float> w(ctx->g.weighted ? m : 0);
+  SG_TRY(download_csr(ctx, rp.data(), col.data(), ctx->g.weighted ? w.data() : nullptr));
+  host_adj_from_csr(n, rp.data(), col.data(), ctx->g.weighted ? w.data() : nullptr, D->out);
+  host_transpose(D->out, D->in);
+  Summary& S = D->S;
+  summary_inc_entries(S, D->out, D->in, deleted, added);
+  {
+    std::vector<uint32_t> u = D->pending_clusters;
+    u.insert(u.end(), S.update_cluster_ids.begin(), S.update_cluster_ids.end());
+    std::sort(u.begin(), u.end());
+    u.erase(std::unique(u.begin(), u.end()), u.end());
+    D->pending_clusters = u;
+  }
+  summary_judge_out_bound(S, D->out, &S.update_cluster_ids);
+  summary_build_subgraph(S, D->out, D->in, &S.update_cluster_ids);
+  std::vector<uint32_t> sps;
+  for (uint32_t v : S.update_source_id) {
+    const uint32_t sp = S.Fc_map[v];
+    if (sp != Summary::kIdDefault && sp < S.supernodes.size()) sps.push_back(sp);
+  }
+  SG_TRY(compute_shortcuts(ctx, *D, sps));
+  summary_node_types(S);
+  summary_sketch_csr(S, D->out);
+  SG_TRY(upload_sketch(ctx, *D));
+  return SG_OK;
+}
+
+uint32_t summary_rows(sg_ctx* ctx) {
+  SummaryDev* D = sdev(ctx);
+  return (D && D->valid) ? D->all_n : 0;
+}
+
+sg_status summary_info(sg_ctx* ctx, sg_summary_info* o) {
+  SummaryDev* D = sdev(ctx);
+  if (!D || !D->valid) return fail(ctx, SG_ERR_STATE, "no summary built");
+  const Summary& S = D->S;
+  std::memset(o, 0, sizeof(*o));
+  o->clusters = S.supernode_ids.size();
+  for (const auto& sp : S.supernodes)
+    if (sp.id != Summary::kIdDefault) {
+      o->supernodes++;
+      o->bound_index = o->bound_index + sp.bound_delta.size();
+      o->inner_index = o->inner_index + sp.inner_delta.size();
+      o->inner_value_index = o->inner_value_index + sp.inner_value.size();
+    }
+  for (const auto& c : S.supernode_ids) o->cluster_members += c.size();
+  for (const auto& c : S.supernode_source) o->sources += c.size();
+  for (uint32_t v = 0; v < S.old_n; ++v) o->bound_nodes += S.out_bound[v] ? 1 : 0;
+  o->all_rows = S.all_n;
+  o->absorbed = S.mirror_node_cnt;
+  for (const auto& c : S.cluster_in_mirror_ids) o->in_mirrors += c.size();
+  for (const auto& c : S.cluster_out_mirror_ids) o->out_mirrors += c.size();
+  o->sync_edges = S.sync_off.empty() ? 0 : S.sync_off.back();
+  o->boundary_edges = S.ib_off.empty() ? 0 : S.ib_off.back();
+  o->shortcut_edges = S.is_off.empty() ? 0 : S.is_off.back();
+  for (uint32_t v = 0; v < S.old_n; ++v)
+    if (S.node_type[v] >= 0 && S.node_type[v] < 7) o->node_type_count[(int)S.node_type[v]]++;
+  return SG_OK;
+}
+
+}  // namespace sg

@@ -1,0 +1,222 @@
+#!/usr/bin/env python
+"""Generates the golden fixtures in this directory by running the
+reference's own CPU workers (built by oracle/ref_harness/build_ref.py from
+the reference checkout) on seeded inputs.
+
+Run here, where the reference checkout exists:
+    python tests/golden/make_golden.py
+Each case writes <case>.npz with:
+  params        json: generator parameters and reference flags
+  input_sha256  hash of the (row_ptr, col, weights) the case was run on
+  clusters_*    the cluster file both sides consume (in-repo greedy builder)
+  updates       the update batch (sg_update records)
+  ref_*         per-vertex results of the reference (float64):
+                  pr_sum_peval / pr_sum_inc   SumSyncIterWorker (compress=1)
+                  pr_plain_inc                IngressSyncIterWorker (compress=0)
+                  sssp_sum_peval / sssp_sum_inc  SumSyncTraversalWorker
+                  sssp_plain_inc              IngressSyncTraversalWorker (compress=0)
+  stats         json: counters the reference logged while building its
+                summary (node types, supernodes, mirrors, sketch edges)
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import suminc_gb300 as sg  # noqa: E402
+
+REF_FLAGS_PR = dict(application="pagerank", cilk="true", compress="1", compress_type="2", portion="1",
+                    termcheck_threshold="1e-6", message_type="push", gpu_start="0",
+                    max_node_num="150", min_node_num="8", mirror_k="4",
+                    compress_threshold="1", app_concurrency="4", directed="true")
+REF_FLAGS_SSSP = dict(REF_FLAGS_PR, application="sssp", cilk="false", sssp_source="0")
+
+
+def input_hash(rp, col, w):
+    h = hashlib.sha256()
+    for a in (rp, col) + ((w,) if w is not None else ()):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def planted_graph(n_clusters=60, size=40, p_in=0.2, n_free=200, seed=7):
+    """Directed graph with planted communities (seeded).  Each community has
+    three entry and three exit vertices; free vertices carry random edges and
+    some of them send / receive more than mirror_k edges to / from one
+    community, which makes them in- and out-mirror candidates."""
+    rng = np.random.default_rng(seed)
+    n = n_clusters * size + n_free
+    edges = set()
+    for c in range(n_clusters):
+        base = c * size
+        m = rng.random((size, size)) < p_in
+        np.fill_diagonal(m, False)
+        for a, b in zip(*np.nonzero(m)):
+            edges.add((base + int(a), base + int(b)))
+        for x in range(size - 3, size):  # exits -> entries of other communities
+            for _ in range(4):
+                oc = int(rng.integers(n_clusters))
+                if oc != c:
+                    edges.add((base + x, oc * size + int(rng.integers(3))))
+    free0 = n_clusters * size
+    for f in range(free0, n):
+        for _ in range(3):
+            v = int(rng.integers(n))
+            if v != f:
+                edges.add((f, v))
+        if (f - free0) % 10 == 0:  # mirror candidates
+            c = int(rng.integers(n_clusters))
+            for mbr in rng.choice(size, 6, replace=False):
+                edges.add((f, c * size + int(mbr)))
+            for mbr in rng.choice(size, 6, replace=False):
+                edges.add((c * size + int(mbr), f))
+    edges = sorted(edges)
+    rp = np.zeros(n + 1, np.uint64)
+    for u, _ in edges:
+        rp[u + 1] += 1
+    rp = np.cumsum(rp).astype(np.uint64)
+    col = np.array([v for _, v in edges], np.uint32)
+    w = np.array([1 + (u * 2654435761 + v * 40503) % 100 for u, v in edges], np.float32)
+    return rp, col, w
+
+
+def write_graph(d, rp, col, w):
+    n = len(rp) - 1
+    src = np.repeat(np.arange(n), np.diff(rp).astype(np.int64))
+    with open(os.path.join(d, "g.e"), "w") as f:
+        for u, v in zip(src.tolist(), col.tolist()):
+            f.write(f"{u} {v}\n")
+    with open(os.path.join(d, "g_w.e"), "w") as f:
+        for u, v, x in zip(src.tolist(), col.tolist(), w.astype(np.int64).tolist()):
+            f.write(f"{u} {v} {x}\n")
+    with open(os.path.join(d, "g.v"), "w") as f:
+        for v in range(n):
+            f.write(f"{v}\n")
+
+
+def write_updates(path, upd, weighted):
+    with open(path, "w") as f:
+        for r in upd:
+            if int(r["op"]) == 0:
+                f.write(f"a {r['src']} {r['dst']}" + (f" {int(r['weight'])}\n" if weighted else "\n"))
+            else:
+                f.write(f"d {r['src']} {r['dst']}\n")
+
+
+def parse_stats(log):
+    st = {}
+    for key, pat in [("spn_num", r"#global_spn_num: (\d+)"), ("ids_num", r"#global_ids_num: (\d+)"),
+                     ("spn_com_num", r"#global_spn_com_num: (\d+)"),
+                     ("bound_node_num", r"#global_bound_node_num: (\d+)"),
+                     ("source_node_num", r"#global_source_node_num: (\d+)"),
+                     ("bound_index_num", r"#global_bound_index_num: (\d+)"),
+                     ("all_node_num", r" all_node_num=(\d+)"),
+                     ("mirror_node_cnt", r"mirror_node_cnt=(\d+)"),
+                     ("sync_e_num", r" sync_e_num=(\d+)"), ("bound_e_num", r" bound_e_num=(\d+)"),
+                     ("source_e_num", r" source_e_num=(\d+)")]:
+        m = re.findall(pat, log)
+        if m:
+            st[key] = [int(x) for x in m]
+    types = re.findall(r"  type(\d)=(\d+) rate", log)
+    if types:
+        st["node_types"] = [[int(a), int(b)] for a, b in types]
+    for key, pat in [("batch_time", r"#?Batch time: ([0-9.e-]+)"),
+                     ("inc_time", r"#?Inc time: ([0-9.e-]+)")]:
+        m = re.findall(pat, log)
+        if m:
+            st[key] = [float(x) for x in m]
+    return st
+
+
+def run_ref(exe, d, app, flags, update=None):
+    out = os.path.join(d, f"{app}.bin")
+    args = [exe, app, out] + [f"{k}={v}" for k, v in flags.items()]
+    efile = "g_w.e" if app.startswith("sssp") else "g.e"
+    args += [f"efile={os.path.join(d, efile)}", f"vfile={os.path.join(d, 'g.v')}"]
+    if update:
+        args.append(f"efile_update={update}")
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="", OMP_NUM_THREADS="4")
+    p = subprocess.run(args, capture_output=True, text=True, env=env, timeout=3600)
+    if p.returncode != 0:
+        sys.stderr.write(p.stderr[-4000:])
+        raise RuntimeError(f"reference run failed: {app}")
+    return np.fromfile(out, dtype=np.float64), p.stderr
+
+
+def make_case(name, rp, col, w, exe, seed, clusters=None):
+    n = len(rp) - 1
+    if clusters is None:
+        clusters = sg.greedy_clusters(rp, col, 150, 8, seed=seed)
+    hg = sg.HostGraph(rp, col, w)
+    m = int(rp[-1])
+    n_upd = max(100, m // 100)
+    upd_pr = hg.gen_updates(n_upd // 2, n_upd // 2, 0, seed=seed + 1)
+    hg2 = sg.HostGraph(rp, col, w)
+    upd_ss = hg2.gen_updates(int(n_upd * 0.4), int(n_upd * 0.4), int(n_upd * 0.2), seed=seed + 2)
+    res = {}
+    stats = {}
+    with tempfile.TemporaryDirectory() as d:
+        write_graph(d, rp, col, w)
+        with open(os.path.join(d, "g.e.c_150"), "w") as f:
+            for c in clusters:
+                f.write(" ".join([str(len(c))] + [str(int(v)) for v in c]) + "\n")
+        upd_pr_path = os.path.join(d, "pr.update")
+        write_updates(upd_pr_path, upd_pr, False)
+        upd_ss_path = os.path.join(d, "sssp.update")
+        write_updates(upd_ss_path, upd_ss, True)
+        res["pr_sum_peval"], log = run_ref(exe, d, "pagerank", REF_FLAGS_PR)
+        stats["pr_peval"] = parse_stats(log)
+        res["pr_sum_inc"], log = run_ref(exe, d, "pagerank", REF_FLAGS_PR, upd_pr_path)
+        stats["pr_inc"] = parse_stats(log)
+        res["pr_plain_inc"], log = run_ref(exe, d, "pagerank_plain", dict(REF_FLAGS_PR, compress="0"),
+                                           upd_pr_path)
+        stats["pr_plain"] = parse_stats(log)
+        res["sssp_sum_peval"], log = run_ref(exe, d, "sssp", REF_FLAGS_SSSP)
+        stats["sssp_peval"] = parse_stats(log)
+        res["sssp_sum_inc"], log = run_ref(exe, d, "sssp", REF_FLAGS_SSSP, upd_ss_path)
+        stats["sssp_inc"] = parse_stats(log)
+        res["sssp_plain_inc"], log = run_ref(exe, d, "sssp_plain", dict(REF_FLAGS_SSSP, compress="0"),
+                                             upd_ss_path)
+    cp = np.zeros(len(clusters) + 1, np.uint32)
+    for i, c in enumerate(clusters):
+        cp[i + 1] = cp[i] + len(c)
+    mem = np.concatenate(clusters).astype(np.uint32) if clusters else np.zeros(0, np.uint32)
+    params = {"name": name, "n": n, "m": m, "cluster_seed": seed, "flags_pr": REF_FLAGS_PR,
+              "flags_sssp": REF_FLAGS_SSSP, "n_updates": n_upd}
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), params=json.dumps(params),
+                        input_sha256=input_hash(rp, col, w), row_ptr=rp, col=col, w=w,
+                        clusters_ptr=cp, clusters_members=mem, updates_pr=upd_pr,
+                        updates_sssp=upd_ss, stats=json.dumps(stats),
+                        **{f"ref_{k}": v for k, v in res.items()})
+    print(name, {k: (len(v), float(np.nansum(np.where(np.isfinite(v), v, 0)))) for k, v in res.items()},
+          "clusters", len(clusters))
+
+
+def main():
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "ref_harness"))
+    import build_ref
+    exe = build_ref.build()
+    if exe is None:
+        raise SystemExit("reference checkout or harness build unavailable")
+    rp, col, w = sg.rmat_host(12, 16 << 12, seed=1, weight_kind=1, wlo=1, whi=100)
+    make_case("rmat12", rp, col, w, exe, seed=1)
+    rp, col, w = planted_graph()
+    # the planted communities are the cluster file (the role of the external
+    # community-detection output the reference reads)
+    planted = [np.arange(c * 40, (c + 1) * 40, dtype=np.uint32) for c in range(60)]
+    make_case("planted2600", rp, col, w, exe, seed=3, clusters=planted)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,85 @@
+"""The golden fixtures (outputs of the reference's own CPU workers, made by
+tests/golden/make_golden.py) pin the oracle: the FP64 solvers and the C
+restatement agree with the reference on the same inputs."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import suminc_gb300 as sg
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = ["rmat12", "planted2600"]
+
+
+def load(name):
+    d = np.load(os.path.join(HERE, f"{name}.npz"))
+    return {k: d[k] for k in d.files}
+
+
+def after(fx, key):
+    return oracle.apply_updates_reference(fx["row_ptr"], fx["col"], fx["w"], fx[key])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fixture_inputs_regenerate(name):
+    fx = load(name)
+    if name == "rmat12":
+        rp, col, w = sg.rmat_host(12, 16 << 12, seed=1, weight_kind=1, wlo=1, whi=100)
+        assert np.array_equal(rp, fx["row_ptr"]) and np.array_equal(col, fx["col"])
+        assert np.array_equal(w, fx["w"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_reference_pagerank_against_fp64(name):
+    fx = load(name)
+    x_star = oracle.pr_fixed_point(fx["row_ptr"], fx["col"])
+    # reference stops at sum|delta| < 1e-6: distance <= 1e-6 / (1 - d) + rounding
+    assert np.abs(fx["ref_pr_sum_peval"] - x_star).sum() < 1e-5
+    nrp, ncol, _ = after(fx, "updates_pr")
+    x_new = oracle.pr_fixed_point(nrp, ncol)
+    assert np.abs(fx["ref_pr_sum_inc"] - x_new).sum() < 1e-5
+    assert np.abs(fx["ref_pr_plain_inc"] - x_new).sum() < 1e-5
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_restatement_matches_reference(name):
+    fx = load(name)
+    rp, col = fx["row_ptr"], fx["col"]
+    x, delta, _ = oracle.ingress_pr(rp, col, tau=1e-6)
+    assert np.abs(x - fx["ref_pr_sum_peval"]).sum() < 1.5e-5
+    nrp, ncol, _ = after(fx, "updates_pr")
+    d2 = oracle.pr_amend((rp, col), (nrp, ncol), x, delta)
+    x2, _, _ = oracle.ingress_pr(nrp, ncol, x=x, delta=d2, tau=1e-6)
+    assert np.abs(x2 - fx["ref_pr_plain_inc"]).sum() < 1.5e-5
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_reference_sssp_equals_dijkstra(name):
+    fx = load(name)
+    d0 = oracle.dijkstra(fx["row_ptr"], fx["col"], fx["w"], 0)
+    assert np.array_equal(fx["ref_sssp_sum_peval"], d0)
+    nrp, ncol, nw = after(fx, "updates_sssp")
+    d1 = oracle.dijkstra(nrp, ncol, nw, 0)
+    assert np.array_equal(fx["ref_sssp_plain_inc"], d1)
+    bad = np.nonzero(fx["ref_sssp_sum_inc"] != d1)[0]
+    if name == "planted2600":
+        # The reference's summarized traversal worker leaves 61 distances too
+        # long after the batch deletes the intra-community edge 370->380 of
+        # community 9 (vertices 360..399; the excess flows on to vertices
+        # reached through it): a known deviation of its IncEval, pinned here
+        # so that a change of the fixture shows up.
+        assert len(bad) == 61 and bad.min() == 361
+        assert np.all(fx["ref_sssp_sum_inc"][bad] > d1[bad])
+    else:
+        assert len(bad) == 0
+
+
+def test_greedy_clusters_regenerate():
+    fx = load("rmat12")
+    cl = sg.greedy_clusters(fx["row_ptr"], fx["col"], 150, 8, seed=1)
+    cp, mem = fx["clusters_ptr"], fx["clusters_members"]
+    ref = [mem[cp[i]:cp[i + 1]] for i in range(len(cp) - 1)]
+    assert len(cl) == len(ref) and all(np.array_equal(a, b) for a, b in zip(cl, ref))
