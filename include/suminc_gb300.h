@@ -34,7 +34,8 @@ typedef enum sg_status {
   SG_ERR_STATE = 4,         /* call out of order (IncEval before PEval ...) */
   SG_ERR_NOT_CONVERGED = 5, /* round cap reached before the residual test   */
   SG_ERR_TIMEOUT = 6,       /* a bounded device-side wait gave up           */
-  SG_ERR_UNSUPPORTED = 7
+  SG_ERR_UNSUPPORTED = 7,
+  SG_ERR_TOO_LARGE = 8      /* input exceeds a fixed capacity (see below)   */
 } sg_status;
 
 /* One line of the reference's update file: "a u v [w]" or "d u v"
@@ -254,6 +255,33 @@ sg_status sg_sssp_distances(sg_ctx* ctx, double* out);
  * unreachable vertices) -- the DependencyData::parent_gid the reference
  * keeps (grape/utils/dependency_data.h:12-33). */
 sg_status sg_sssp_parents(sg_ctx* ctx, uint32_t* out);
+
+/* ------------------------------------------------- allocation-free PEval */
+
+/* Largest vertex count sg_pr_peval_noalloc accepts. */
+#define SG_PR_NOALLOC_MAX_VERTICES (1u << 22)
+
+/* PageRank PEval that allocates nothing -- no counterpart in the reference.
+ * For callers that cannot call cudaMalloc: a process whose device memory is
+ * owned by another framework's pool, code running while a stream is being
+ * captured, or latency-bound loops that must not hit cudaMalloc's implicit
+ * synchronisation.  The caller passes a packed CSR (d_row_ptr[n+1],
+ * d_col[m]) and the outputs (d_values[n], d_deltas[n]) in device memory of
+ * the current device, and a stream (NULL = default stream); the result is
+ * the delta-accumulative PageRank of sg_pr_peval (L1 residual below
+ * `threshold`).  Scratch (one float per vertex and a few control words) is a
+ * fixed file-scope device array of SG_PR_NOALLOC_MAX_VERTICES entries that
+ * every GPU loading the library keeps until the process exits; n above that
+ * returns SG_ERR_TOO_LARGE.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress) with that device current,
+ * so make that first call before any stream capture.  Every call shares the
+ * array: calls whose work overlaps on the GPU race and must be serialised
+ * by the caller.  Returns SG_ERR_NOT_CONVERGED when max_rounds is reached. */
+sg_status sg_pr_peval_noalloc(uint32_t n, uint64_t m, const uint64_t* d_row_ptr,
+                              const uint32_t* d_col, double damping,
+                              double threshold, int32_t max_rounds, void* stream,
+                              float* d_values, float* d_deltas,
+                              int32_t* rounds_out, double* residual_out);
 
 /* ------------------------------------------------------ host utilities
  * (no GPU needed; used to make inputs identical on every side) */

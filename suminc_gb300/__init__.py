@@ -39,6 +39,8 @@ SG_ERR_STATE = 4
 SG_ERR_NOT_CONVERGED = 5
 SG_ERR_TIMEOUT = 6
 SG_ERR_UNSUPPORTED = 7
+SG_ERR_TOO_LARGE = 8
+PR_NOALLOC_MAX_VERTICES = 1 << 22
 
 SG_UPD_ADD = 0
 SG_UPD_DEL = 1
@@ -146,6 +148,8 @@ _SIGS = {
                                   C.c_double, C.c_double, _P], C.c_int),
     "sg_hostgraph_num_edges": ([_P, C.POINTER(C.c_uint64)], C.c_int),
     "sg_hostgraph_csr": ([_P, _P, _P, _P], C.c_int),
+    "sg_pr_peval_noalloc": ([C.c_uint32, C.c_uint64, _P, _P, C.c_double, C.c_double, C.c_int32,
+                             _P, _P, _P, C.POINTER(C.c_int32), C.POINTER(C.c_double)], C.c_int),
     "sg_summary_build": ([_P, C.c_uint32, _P, _P], C.c_int),
     "sg_summary_info_get": ([_P, C.POINTER(SummaryInfo)], C.c_int),
     "sg_util_greedy_clusters": ([C.c_uint32, _P, _P, C.c_int, C.c_int, C.c_uint64, _P, _P,
