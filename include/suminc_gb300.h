@@ -66,6 +66,7 @@ typedef struct sg_options {
   double compress_threshold;  /* FLAGS_compress_threshold (benefit bound)    */
   double sssp_delta;          /* delta-stepping bucket width, 0 = automatic  */
   double slack;               /* extra adjacency capacity per vertex (0.125) */
+  double adjoint_rel_tol;     /* adjoint stop: residual < tol * sum|dL/dx|   */
   int32_t reserved[8];
 } sg_options;
 
@@ -255,6 +256,98 @@ sg_status sg_sssp_distances(sg_ctx* ctx, double* out);
  * unreachable vertices) -- the DependencyData::parent_gid the reference
  * keeps (grape/utils/dependency_data.h:12-33). */
 sg_status sg_sssp_parents(sg_ctx* ctx, uint32_t* out);
+
+/* ------------------------------------------- personalized PageRank, batches */
+
+/* Personalized PageRank of one query on the plain graph: teleport mass
+ * (1-d) spread uniformly over the seeds (the PPR app's seed set,
+ * examples/analytical_apps/ppr/ppr.h:24-31), x = 0 at start, the Ingress
+ * delta rounds of sg_pr_peval to the same residual test.  out: host
+ * float[n] or NULL.  Seeds should be distinct (a repeated seed gets its
+ * share once per occurrence).  Leaves no IncEval state behind. */
+sg_status sg_ppr(sg_ctx* ctx, uint32_t n_seeds, const uint32_t* seeds, float* out);
+
+/* A batch of independent queries evaluated by one persistent kernel (no
+ * counterpart in the reference, which answers one query per run):
+ *   PPR  query q teleports to seeds[seed_ptr[q] .. seed_ptr[q+1]), each
+ *        query as sg_ppr; at most 256 queries;
+ *   SSSP one distance vector per source, as sg_sssp_peval; at most 64
+ *        sources; needs a weighted graph. */
+typedef struct {
+  uint32_t ppr_queries;
+  const uint32_t* ppr_seed_ptr;  /* [ppr_queries + 1], seed_ptr[0] = 0   */
+  const uint32_t* ppr_seeds;     /* vertex ids                           */
+  uint32_t sssp_sources;
+  const uint32_t* sources;       /* [sssp_sources] vertex ids            */
+} sg_batch_spec;
+
+typedef struct {
+  uint32_t ppr_queries, sssp_sources;
+  uint32_t chunk_quads;      /* schedule: quads per PPR work chunk        */
+  uint32_t blocks_per_sm;    /* schedule: persistent CTAs per SM          */
+  double sssp_bucket;        /* schedule: delta-stepping bucket width     */
+  int32_t graph_launch;      /* 1 when the run replayed a CUDA graph      */
+  double tune_ms;            /* host time of the last autotune            */
+  uint32_t iterations;       /* persistent-kernel iterations              */
+  uint32_t ppr_pulls, sssp_steps, sssp_scans;
+  uint32_t ppr_not_converged;/* queries that hit the round cap            */
+  uint64_t ppr_edge_visits;  /* sum over pulls of edges x queries pulled  */
+  uint64_t sssp_relaxations; /* (edge, source) pairs relaxed              */
+  uint64_t sssp_improvements;
+  double elapsed_ms;         /* device time of the launch sequence        */
+} sg_batch_info;
+
+/* Runs the batch.  The first batch of a given shape on a graph picks the
+ * schedule by timing candidates (chunk size x CTAs per SM for PPR, bucket
+ * width for SSSP) and captures the launch sequence in a CUDA graph; later
+ * batches of that shape replay it.  Outputs (host, or NULL to keep them on
+ * the device): ppr_out float[ppr_queries][n], sssp_out double[sources][n]
+ * (+inf for unreachable). */
+sg_status sg_batch_run(sg_ctx* ctx, const sg_batch_spec* spec, float* ppr_out,
+                       double* sssp_out);
+/* As sg_batch_run, re-running the autotuner first. */
+sg_status sg_batch_tune_run(sg_ctx* ctx, const sg_batch_spec* spec,
+                            float* ppr_out, double* sssp_out);
+sg_status sg_batch_info_get(sg_ctx* ctx, sg_batch_info* out);
+/* Per PPR query of the last batch: rounds (counted as sg_pr_peval counts
+ * them) and final residual; arrays of ppr_queries entries, either NULL. */
+sg_status sg_batch_query_stats(sg_ctx* ctx, int32_t* rounds, double* residual);
+/* Device pointers to the last batch's outputs (layouts as above); valid
+ * until the next batch or sg_ctx_destroy. */
+sg_status sg_batch_outputs_device(sg_ctx* ctx, const float** ppr,
+                                  const double** sssp);
+
+/* ------------------------------------------ weighted PageRank and adjoint */
+
+/* PageRank with edge weights (no counterpart in the reference, whose
+ * PageRank divides by the out-degree): x = (1-d) t + d M x with
+ * M[v][u] = w_uv as loaded (column-normalised weights make M column-
+ * stochastic), teleport t (host float[n], or NULL for uniform 1/n); the
+ * Ingress delta rounds of sg_pr_peval with the weights applied in the
+ * gather, to the same residual test.  x_out: host float[n] or NULL. */
+sg_status sg_pr_weighted(sg_ctx* ctx, const float* tele, float* x_out);
+
+/* Adjoint of the last sg_pr_weighted on the current graph: given
+ * dl_dx = dL/dx (host float[n]) solves lambda = dl_dx + d M^T lambda by the
+ * transposed delta iteration (pulls along out-edges) to a residual below
+ * opt.adjoint_rel_tol * sum|dl_dx|, then
+ *   dl_dw[e]  = d * lambda[v] * x[u] for the e-th edge (u, v) in the order
+ *               of sg_graph_download_csr (host float[m] or NULL),
+ *   dl_dtele  = (1-d) * lambda (host float[n] or NULL). */
+sg_status sg_pr_adjoint(sg_ctx* ctx, const float* dl_dx, float* dl_dw, float* dl_dtele);
+/* As sg_pr_adjoint with dl_dx already in device memory. */
+sg_status sg_pr_adjoint_device(sg_ctx* ctx, const float* d_dl_dx, float* dl_dw,
+                               float* dl_dtele);
+
+typedef struct {
+  int32_t forward_rounds, adjoint_rounds;
+  double forward_ms, adjoint_ms;      /* device time; adjoint incl. gradients */
+  double forward_residual, adjoint_residual;
+  uint64_t forward_edges, adjoint_edges, gradient_edges;
+} sg_adjoint_info;
+sg_status sg_adjoint_info_get(sg_ctx* ctx, sg_adjoint_info* out);
+/* The forward values x and the adjoint lambda (each host float[n] or NULL). */
+sg_status sg_adjoint_values(sg_ctx* ctx, float* x, float* lambda);
 
 /* ------------------------------------------------- allocation-free PEval */
 

@@ -63,6 +63,7 @@ class Options(C.Structure):
         ("compress_threshold", C.c_double),
         ("sssp_delta", C.c_double),
         ("slack", C.c_double),
+        ("adjoint_rel_tol", C.c_double),
         ("reserved", C.c_int32 * 8),
     ]
 
@@ -77,6 +78,40 @@ class SummaryInfo(C.Structure):
         d = {k: int(getattr(self, k)) for k, _ in self._fields_ if k != "node_type_count"}
         d["node_type_count"] = [int(x) for x in self.node_type_count]
         return d
+
+
+class BatchSpec(C.Structure):
+    _fields_ = [
+        ("ppr_queries", C.c_uint32),
+        ("ppr_seed_ptr", C.c_void_p),
+        ("ppr_seeds", C.c_void_p),
+        ("sssp_sources", C.c_uint32),
+        ("sources", C.c_void_p),
+    ]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [
+        ("ppr_queries", C.c_uint32),
+        ("sssp_sources", C.c_uint32),
+        ("chunk_quads", C.c_uint32),
+        ("blocks_per_sm", C.c_uint32),
+        ("sssp_bucket", C.c_double),
+        ("graph_launch", C.c_int32),
+        ("tune_ms", C.c_double),
+        ("iterations", C.c_uint32),
+        ("ppr_pulls", C.c_uint32),
+        ("sssp_steps", C.c_uint32),
+        ("sssp_scans", C.c_uint32),
+        ("ppr_not_converged", C.c_uint32),
+        ("ppr_edge_visits", C.c_uint64),
+        ("sssp_relaxations", C.c_uint64),
+        ("sssp_improvements", C.c_uint64),
+        ("elapsed_ms", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Stats(C.Structure):
@@ -151,6 +186,12 @@ _SIGS = {
     "sg_pr_peval_noalloc": ([C.c_uint32, C.c_uint64, _P, _P, C.c_double, C.c_double, C.c_int32,
                              _P, _P, _P, C.POINTER(C.c_int32), C.POINTER(C.c_double)], C.c_int),
     "sg_summary_build": ([_P, C.c_uint32, _P, _P], C.c_int),
+    "sg_ppr": ([_P, C.c_uint32, _P, _P], C.c_int),
+    "sg_batch_run": ([_P, C.POINTER(BatchSpec), _P, _P], C.c_int),
+    "sg_batch_tune_run": ([_P, C.POINTER(BatchSpec), _P, _P], C.c_int),
+    "sg_batch_info_get": ([_P, C.POINTER(BatchInfo)], C.c_int),
+    "sg_batch_query_stats": ([_P, _P, _P], C.c_int),
+    "sg_batch_outputs_device": ([_P, C.POINTER(_P), C.POINTER(_P)], C.c_int),
     "sg_summary_info_get": ([_P, C.POINTER(SummaryInfo)], C.c_int),
     "sg_util_greedy_clusters": ([C.c_uint32, _P, _P, C.c_int, C.c_int, C.c_uint64, _P, _P,
                                  C.POINTER(C.c_uint32)], C.c_int),
@@ -333,6 +374,42 @@ class Context:
         info = SummaryInfo()
         _check(self._lib.sg_summary_info_get(self._h, C.byref(info)), self, "sg_summary_info_get")
         return info.as_dict()
+
+    # -- personalized PageRank and batches -------------------------------
+    def ppr(self, seeds, out=True):
+        seeds = np.ascontiguousarray(seeds, np.uint32)
+        x = np.empty(self.n, np.float32) if out else None
+        _check(self._lib.sg_ppr(self._h, len(seeds), _ptr(seeds), _ptr(x)), self, "sg_ppr")
+        return x
+
+    def batch_run(self, ppr_seeds=(), sources=(), out=True, retune=False):
+        """ppr_seeds: list of seed arrays (one PPR query each); sources: SSSP
+        sources.  Returns (ppr float32[Q, n], sssp float64[S, n]) or Nones."""
+        q = len(ppr_seeds)
+        sp = np.zeros(q + 1, np.uint32)
+        for i, sd in enumerate(ppr_seeds):
+            sp[i + 1] = sp[i] + len(sd)
+        seeds = (np.concatenate([np.asarray(x, np.uint32) for x in ppr_seeds])
+                 if q else np.zeros(1, np.uint32))
+        src = np.ascontiguousarray(sources, np.uint32) if len(sources) else np.zeros(1, np.uint32)
+        spec = BatchSpec(q, sp.ctypes.data, seeds.ctypes.data, len(sources), src.ctypes.data)
+        po = np.empty((q, self.n), np.float32) if (out and q) else None
+        so = np.empty((len(sources), self.n), np.float64) if (out and len(sources)) else None
+        fn = self._lib.sg_batch_tune_run if retune else self._lib.sg_batch_run
+        _check(fn(self._h, C.byref(spec), _ptr(po), _ptr(so)), self, "sg_batch_run")
+        return po, so
+
+    def batch_info(self) -> dict:
+        info = BatchInfo()
+        _check(self._lib.sg_batch_info_get(self._h, C.byref(info)), self, "sg_batch_info_get")
+        return info.as_dict()
+
+    def batch_query_stats(self, nq):
+        r = np.empty(nq, np.int32)
+        res = np.empty(nq, np.float64)
+        _check(self._lib.sg_batch_query_stats(self._h, _ptr(r), _ptr(res)), self,
+               "sg_batch_query_stats")
+        return r, res
 
     # -- SSSP -------------------------------------------------------------
     def sssp_peval(self, source=0, out=True):

@@ -1,0 +1,1256 @@
+// Batched queries: many personalized-PageRank queries and many SSSP sources
+// advanced together by one cooperative persistent kernel.
+//
+// PPR (ppr/ppr.h's teleport to a seed set, the Ingress delta rounds of
+// pagerank_ingress.h:50-72 per query).  Per-vertex state is laid out
+// vertex-major with the queries of a vertex contiguous ([n][qw] floats), so
+// one in-edge costs a single contiguous, coalesced read of the source's push
+// values for every query, and the neighbour list is read once per round for
+// the whole batch.  Work is edge-balanced: the in-CSR's 4-edge quads are cut
+// into chunks of `cq` quads; a group of lanes (32 for qw >= 128, fewer for
+// narrow batches) walks one chunk, summing push-value rows in registers and
+// finishing every vertex whose quads lie inside the chunk; vertices spanning
+// chunks collect partial sums by atomicAdd and are finished after a grid
+// barrier.  Each query has its own state (active -> drain -> done), its own
+// FP64 residual and round count, so queries of uneven convergence retire
+// independently; a per-vertex activity byte lets a round skip rows whose
+// push values are all zero (the sparse first rounds of a seeded query).
+//
+// SSSP (sssp_ingress.h:25-265 per source).  Distances are [n][ns] ordered
+// bits of non-negative doubles (exact atomicMin; integer weights give
+// bit-exact FP64 sums).  Each vertex carries two source masks, near and far,
+// and sits in the near / far list when its mask turns non-zero: the per-query
+// frontiers.  A near step relaxes the out-edges of every near-list vertex
+// for the sources in its mask; an improvement below the bucket limit goes to
+// the near mask, one above it to the far mask.  When no near work is left,
+// the limit moves one bucket above the smallest pending far distance and a
+// scan step moves the far pairs below it to the near masks (delta-stepping
+// with one bucket window shared by all sources).
+//
+// One launch runs both: every iteration does a PPR round and an SSSP step
+// side by side, separated by bounded grid barriers; block 0 takes the
+// per-query decisions between them.  The launch sequence (state reset, seed
+// scatter, persistent kernel, result transposes) is captured once into a
+// CUDA graph per schedule and replayed.  The schedule -- chunk size, blocks
+// per SM and the SSSP bucket width -- is picked by timing candidates on the
+// caller's batch (batch_tune).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ctx.h"
+#include "dev.cuh"
+
+namespace sg {
+
+namespace {
+
+constexpr int BT = 256;           // threads per block
+constexpr uint32_t kMaxQW = 256;  // PPR query width (max queries per launch)
+constexpr uint32_t kMaxNS = 64;   // SSSP sources per launch (one 64-bit mask)
+
+enum QState : uint32_t { Q_ACTIVE = 0, Q_PENDING = 1, Q_DONE = 2 };
+
+enum {
+  B_BAR_COUNT = 0, B_BAR_GEN = 1, B_ERR = 2, B_ITER = 3,
+  B_PPR_LIVE = 4,     // queries not done
+  B_PULL = 5,         // PPR pull index (0 = first pull)
+  B_SMODE = 6,        // 0 near step, 1 far scan
+  B_NSEL = 7,         // near list being read
+  B_FSEL = 8,         // far list being appended (a scan reads it)
+  B_NCNT0 = 9, B_NCNT1 = 10,  // near list counts
+  B_FCNT0 = 11, B_FCNT1 = 12, // far list counts
+  B_SSSP_LIVE = 13,
+  B_NOTCONV = 14,
+  B_ITERS_PPR = 15, B_ITERS_SSSP = 16, B_SCANS = 17,
+  B_WORDS = 32
+};
+enum {
+  BC_PPR_EDGES = 0, BC_SSSP_RELAX = 1, BC_SSSP_IMPROVE = 2,
+  BC_MINFAR = 3,      // smallest pending far distance (ordered bits)
+  BC_LIMIT = 4,       // current bucket limit (ordered bits of a double)
+  BC_WORDS = 8
+};
+
+struct BatchArgs {
+  uint32_t n;
+  uint64_t live_edges;
+  // in-CSR (pull)
+  const uint64_t* in_off;
+  const uint32_t* in_col;
+  const uint32_t* in_deg;
+  const uint32_t* out_deg;
+  const uint32_t* nz;
+  const uint64_t* qoff;
+  uint32_t nz_count;
+  uint64_t quads;
+  // chunking of the quads
+  uint32_t cq;
+  uint64_t nchunks;
+  const uint32_t* chunk_v0;
+  const uint32_t* bnd;
+  uint32_t nbnd;
+  // PPR
+  uint32_t qw, nq;
+  float* X;
+  float* D;
+  float* PV0;
+  float* PV[2];
+  float* ACC;
+  uint8_t* act0;
+  uint8_t* act[2];
+  uint32_t* qstate;
+  uint32_t* qrounds;
+  double* qres;
+  double* qres0;
+  double* qlast;
+  float damping, thr_v;
+  double tau;
+  uint32_t max_rounds;
+  // SSSP
+  uint32_t ns;
+  const uint64_t* out_off;
+  const uint32_t* out_col;
+  const float* out_w;
+  unsigned long long* dist;
+  unsigned long long* fm_near;
+  unsigned long long* fm_far;
+  uint32_t* nl[2];
+  uint32_t* fl[2];
+  uint64_t lcap;
+  double sdelta;
+  // control
+  uint32_t* ctl;
+  unsigned long long* cnt;
+  long long spin_limit;
+  uint32_t max_iters;
+};
+
+__device__ __forceinline__ bool bgrid_sync(const BatchArgs& A) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile uint32_t* gen = A.ctl + B_BAR_GEN;
+    const uint32_t g = *gen;
+    __threadfence();
+    if (atomicAdd(A.ctl + B_BAR_COUNT, 1u) == gridDim.x - 1) {
+      A.ctl[B_BAR_COUNT] = 0;
+      __threadfence();
+      atomicAdd(A.ctl + B_BAR_GEN, 1u);
+    } else {
+      long long spins = 0;
+      while (*gen == g) {
+        if (++spins > A.spin_limit) {
+          atomicExch(A.ctl + B_ERR, 1u);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *(volatile uint32_t*)(A.ctl + B_ERR) == 0;
+}
+
+struct Smem {
+  uint32_t qstate[kMaxQW];
+  double qres[kMaxQW];
+  double dv[BT / 32][kMaxNS];
+};
+
+// ---------------------------------------------------------------- PPR
+
+// One query's delta update at vertex v (query column j of a float4).
+__device__ __forceinline__ void ppr_update(uint32_t st, float& d, float& x, float& pvn, float s,
+                                           float scale, float thr, double& res) {
+  if (st == Q_DONE) {
+    pvn = 0.f;
+    return;
+  }
+  const float dl = d + s;
+  res += fabs((double)dl);
+  if (st == Q_PENDING) {  // drain round: collect, activate nothing
+    d = dl;
+    pvn = 0.f;
+    return;
+  }
+  if (fabsf(dl) > thr) {
+    x += dl;
+    d = 0.f;
+    pvn = scale * dl;
+  } else {
+    d = dl;
+    pvn = 0.f;
+  }
+}
+
+// Finishes vertex v for the lane's query columns: delta += s, activation,
+// next push value; returns whether any of the lane's push values is non-zero.
+template <int F>
+__device__ __forceinline__ bool ppr_finish(const BatchArgs& A, const Smem& S, uint32_t v,
+                                           const float (&s)[F * 4], float* pv_next,
+                                           uint32_t li, uint32_t L, double (&res)[F * 4]) {
+  const uint32_t od = A.out_deg[v];
+  const float scale = od > 0 ? A.damping / (float)od : 0.f;
+  bool any = false;
+#pragma unroll
+  for (int f = 0; f < F; ++f) {
+    const uint32_t qb = (li + f * L) * 4;
+    if (qb >= A.qw) continue;
+    const uint64_t o = (uint64_t)v * A.qw + qb;
+    float4 d4 = __ldcg(reinterpret_cast<const float4*>(A.D + o));
+    float4 x4 = __ldcg(reinterpret_cast<const float4*>(A.X + o));
+    float4 p4;
+    ppr_update(S.qstate[qb + 0], d4.x, x4.x, p4.x, s[f * 4 + 0], scale, A.thr_v, res[f * 4 + 0]);
+    ppr_update(S.qstate[qb + 1], d4.y, x4.y, p4.y, s[f * 4 + 1], scale, A.thr_v, res[f * 4 + 1]);
+    ppr_update(S.qstate[qb + 2], d4.z, x4.z, p4.z, s[f * 4 + 2], scale, A.thr_v, res[f * 4 + 2]);
+    ppr_update(S.qstate[qb + 3], d4.w, x4.w, p4.w, s[f * 4 + 3], scale, A.thr_v, res[f * 4 + 3]);
+    *reinterpret_cast<float4*>(A.D + o) = d4;
+    *reinterpret_cast<float4*>(A.X + o) = x4;
+    *reinterpret_cast<float4*>(pv_next + o) = p4;
+    any |= (p4.x != 0.f) | (p4.y != 0.f) | (p4.z != 0.f) | (p4.w != 0.f);
+  }
+  return any;
+}
+
+// First activation of every vertex (before the first pull).
+template <int F>
+__device__ void ppr_activate_all(const BatchArgs& A, Smem& S) {
+  const uint32_t L = min(32u, A.qw / 4);
+  const uint32_t G = 32 / L;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t li = lane % L;
+  const uint64_t gid = ((uint64_t)blockIdx.x * BT + threadIdx.x) / 32 * G + lane / L;
+  const uint64_t ng = (uint64_t)gridDim.x * BT / 32 * G;
+  const unsigned gmask = L == 32 ? 0xffffffffu : (((1u << L) - 1) << ((lane / L) * L));
+  const float zero[F * 4] = {};
+  for (uint64_t v = gid; v < A.n; v += ng) {
+    double r[F * 4];
+#pragma unroll
+    for (int j = 0; j < F * 4; ++j) r[j] = 0.0;
+    const bool any = ppr_finish<F>(A, S, (uint32_t)v, zero, A.PV0, li, L, r);
+    const unsigned a = __reduce_or_sync(gmask, any ? 1u : 0u);
+    if (li == 0) A.act0[v] = (uint8_t)a;
+    const bool zero_in = A.in_deg[v] == 0;
+#pragma unroll
+    for (int f = 0; f < F; ++f) {
+      const uint32_t qb = (li + f * L) * 4;
+      if (qb >= A.qw) continue;
+      const uint64_t o = (uint64_t)v * A.qw + qb;
+      const float4 d4 = __ldcg(reinterpret_cast<const float4*>(A.D + o));
+      const float dd[4] = {d4.x, d4.y, d4.z, d4.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        // vertices without in-edges never change again: their leftover delta
+        // is a constant part of the query's residual
+        if (zero_in && dd[j] != 0.f && S.qstate[qb + j] != Q_DONE)
+          atomicAdd(&A.qres0[qb + j], fabs((double)dd[j]));
+      }
+    }
+  }
+}
+
+// Pull number p: sums push values over the in-edges of every chunk.
+template <int F>
+__device__ void ppr_pull(const BatchArgs& A, Smem& S, uint32_t p, double (&res)[F * 4]) {
+  const uint32_t L = min(32u, A.qw / 4);
+  const uint32_t G = 32 / L;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t li = lane % L;
+  const uint64_t gid = ((uint64_t)blockIdx.x * BT + threadIdx.x) / 32 * G + lane / L;
+  const uint64_t ng = (uint64_t)gridDim.x * BT / 32 * G;
+  const unsigned gmask = L == 32 ? 0xffffffffu : (((1u << L) - 1) << ((lane / L) * L));
+  const float* __restrict__ pv = p == 0 ? A.PV0 : A.PV[p & 1];
+  const uint8_t* __restrict__ act = p == 0 ? A.act0 : A.act[p & 1];
+  float* pv_next = A.PV[(p + 1) & 1];
+  uint8_t* act_next = A.act[(p + 1) & 1];
+  for (uint64_t ch = gid; ch < A.nchunks; ch += ng) {
+    const uint64_t q0 = ch * A.cq;
+    const uint64_t q1 = min(q0 + A.cq, A.quads);
+    uint32_t i = A.chunk_v0[ch];
+    uint32_t v = A.nz[i];
+    uint64_t qbeg = A.qoff[i], qend = A.qoff[i + 1];
+    uint64_t base = A.in_off[v];
+    uint32_t deg = A.in_deg[v];
+    float acc[F * 4];
+#pragma unroll
+    for (int j = 0; j < F * 4; ++j) acc[j] = 0.f;
+    for (uint64_t q = q0;; ++q) {
+      if (q >= qend || q >= q1) {
+        // owner i is complete within this chunk, or the chunk ends
+        const bool interior = qbeg >= q0 && qend <= q1;
+        if (interior) {
+          const bool any = ppr_finish<F>(A, S, v, acc, pv_next, li, L, res);
+          const unsigned a = __reduce_or_sync(gmask, any ? 1u : 0u);
+          if (li == 0) act_next[v] = (uint8_t)a;
+        } else {
+#pragma unroll
+          for (int f = 0; f < F; ++f) {
+            const uint32_t qb = (li + f * L) * 4;
+            if (qb >= A.qw) continue;
+            float* dst = A.ACC + (uint64_t)v * A.qw + qb;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              if (acc[f * 4 + j] != 0.f) atomicAdd(dst + j, acc[f * 4 + j]);
+          }
+        }
+        if (q >= q1) break;
+#pragma unroll
+        for (int j = 0; j < F * 4; ++j) acc[j] = 0.f;
+        ++i;
+        v = A.nz[i];
+        qbeg = A.qoff[i];
+        qend = A.qoff[i + 1];
+        base = A.in_off[v];
+        deg = A.in_deg[v];
+      }
+      const uint32_t k = (uint32_t)(q - qbeg) * 4;
+      const uint4 c4 = *reinterpret_cast<const uint4*>(A.in_col + base + k);
+      const uint32_t cc[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        if (k + t >= deg) break;
+        const uint32_t u = cc[t];
+        if (!__ldcg(act + u)) continue;
+#pragma unroll
+        for (int f = 0; f < F; ++f) {
+          const uint32_t qb = (li + f * L) * 4;
+          if (qb >= A.qw) continue;
+          const float4 r = __ldcg(reinterpret_cast<const float4*>(pv + (uint64_t)u * A.qw + qb));
+          acc[f * 4 + 0] += r.x;
+          acc[f * 4 + 1] += r.y;
+          acc[f * 4 + 2] += r.z;
+          acc[f * 4 + 3] += r.w;
+        }
+      }
+    }
+  }
+}
+
+// Vertices spanning chunks: their sums arrived in ACC.
+template <int F>
+__device__ void ppr_fixup(const BatchArgs& A, Smem& S, uint32_t p, double (&res)[F * 4]) {
+  const uint32_t L = min(32u, A.qw / 4);
+  const uint32_t G = 32 / L;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t li = lane % L;
+  const uint64_t gid = ((uint64_t)blockIdx.x * BT + threadIdx.x) / 32 * G + lane / L;
+  const uint64_t ng = (uint64_t)gridDim.x * BT / 32 * G;
+  const unsigned gmask = L == 32 ? 0xffffffffu : (((1u << L) - 1) << ((lane / L) * L));
+  float* pv_next = A.PV[(p + 1) & 1];
+  uint8_t* act_next = A.act[(p + 1) & 1];
+  for (uint64_t b = gid; b < A.nbnd; b += ng) {
+    const uint32_t v = A.bnd[b];
+    float s[F * 4];
+#pragma unroll
+    for (int f = 0; f < F; ++f) {
+      const uint32_t qb = (li + f * L) * 4;
+      if (qb >= A.qw) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) s[f * 4 + j] = 0.f;
+        continue;
+      }
+      float4* src = reinterpret_cast<float4*>(A.ACC + (uint64_t)v * A.qw + qb);
+      const float4 a = __ldcg(src);
+      s[f * 4 + 0] = a.x; s[f * 4 + 1] = a.y; s[f * 4 + 2] = a.z; s[f * 4 + 3] = a.w;
+      *src = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const bool any = ppr_finish<F>(A, S, v, s, pv_next, li, L, res);
+    const unsigned a = __reduce_or_sync(gmask, any ? 1u : 0u);
+    if (li == 0) act_next[v] = (uint8_t)a;
+  }
+}
+
+// Lane-held residuals -> block sums -> one global atomic per query.
+template <int F>
+__device__ void ppr_flush_res(const BatchArgs& A, Smem& S, double (&res)[F * 4]) {
+  const uint32_t L = min(32u, A.qw / 4);
+  const uint32_t li = (threadIdx.x & 31) % L;
+#pragma unroll
+  for (int f = 0; f < F; ++f) {
+    const uint32_t qb = (li + f * L) * 4;
+    if (qb >= A.qw) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (res[f * 4 + j] != 0.0) atomicAdd(&S.qres[qb + j], res[f * 4 + j]);
+      res[f * 4 + j] = 0.0;
+    }
+  }
+  __syncthreads();
+  for (uint32_t q = threadIdx.x; q < A.qw; q += BT) {
+    if (S.qres[q] != 0.0) atomicAdd(&A.qres[q], S.qres[q]);
+    S.qres[q] = 0.0;
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- SSSP
+
+__device__ __forceinline__ void list_push(const BatchArgs& A, uint32_t* list, uint32_t* cnt,
+                                          uint32_t v) {
+  const uint32_t s = atomicAdd(cnt, 1u);
+  if (s < A.lcap) list[s] = v;
+  else atomicExch(A.ctl + B_ERR, 2u);
+}
+
+// Near step: relax the out-edges of each near-list vertex for the sources
+// in its near mask (warp per vertex, lanes over 4-edge quads, 128-bit loads
+// of neighbours and weights).
+__device__ void sssp_near(const BatchArgs& A, Smem& S, unsigned long long& relax,
+                          unsigned long long& improve) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t w = threadIdx.x >> 5;
+  const uint32_t nsel = __ldcg(A.ctl + B_NSEL);
+  const uint32_t fsel = __ldcg(A.ctl + B_FSEL);
+  const uint32_t cnt = (uint32_t)min((uint64_t)__ldcg(A.ctl + B_NCNT0 + nsel), A.lcap);
+  const uint32_t* list = A.nl[nsel];
+  uint32_t* nnext = A.nl[nsel ^ 1];
+  uint32_t* nnext_cnt = A.ctl + B_NCNT0 + (nsel ^ 1);
+  uint32_t* far = A.fl[fsel];
+  uint32_t* far_cnt = A.ctl + B_FCNT0 + fsel;
+  const double lim = bitsd(__ldcg(A.cnt + BC_LIMIT));
+  const uint32_t ns = A.ns;
+  const uint32_t nwarps = gridDim.x * (BT / 32);
+  for (uint32_t i = blockIdx.x * (BT / 32) + w; i < cnt; i += nwarps) {
+    const uint32_t v = __ldcg(list + i);
+    unsigned long long m = 0;
+    if (lane == 0) m = atomicExch(A.fm_near + v, 0ull);
+    m = __shfl_sync(0xffffffffu, m, 0);
+    if (m == 0) continue;
+    // the source distances of v, read after the mask was taken: a later
+    // improvement sets the bit again and v comes back
+    for (uint32_t s = lane; s < ns; s += 32)
+      if ((m >> s) & 1ull) S.dv[w][s] = bitsd(__ldcg(A.dist + (uint64_t)v * ns + s));
+    __syncwarp();
+    const uint32_t d = A.out_deg[v];
+    const uint64_t base = A.out_off[v];
+    if (lane == 0) relax += (unsigned long long)d * __popcll(m);
+    unsigned long long minfar = kInfBits;
+    for (uint32_t kb = 0; kb < d; kb += 128) {
+      const uint32_t k = kb + lane * 4;
+      uint32_t cc[4] = {kInvalidVid, kInvalidVid, kInvalidVid, kInvalidVid};
+      float ww[4] = {0.f, 0.f, 0.f, 0.f};
+      if (k < d) {
+        const uint4 c4 = *reinterpret_cast<const uint4*>(A.out_col + base + k);
+        const float4 w4 = *reinterpret_cast<const float4*>(A.out_w + base + k);
+        cc[0] = c4.x; cc[1] = k + 1 < d ? c4.y : kInvalidVid;
+        cc[2] = k + 2 < d ? c4.z : kInvalidVid; cc[3] = k + 3 < d ? c4.w : kInvalidVid;
+        ww[0] = w4.x; ww[1] = w4.y; ww[2] = w4.z; ww[3] = w4.w;
+      }
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const uint32_t u = cc[t];
+        unsigned long long nb = 0, fb = 0;
+        if (u != kInvalidVid) {
+          unsigned long long* du = A.dist + (uint64_t)u * ns;
+          for (unsigned long long mm = m; mm; mm &= mm - 1) {
+            const uint32_t s = __ffsll((long long)mm) - 1;
+            const double cand = S.dv[w][s] + (double)ww[t];
+            const unsigned long long cb = dbits(cand);
+            if (cb < __ldcg(du + s)) {
+              const unsigned long long old = atomicMin(du + s, cb);
+              if (cb < old) {
+                improve++;
+                if (cand < lim) {
+                  nb |= 1ull << s;
+                } else {
+                  fb |= 1ull << s;
+                  minfar = cb < minfar ? cb : minfar;
+                }
+              }
+            }
+          }
+        }
+        bool push_near = false, push_far = false;
+        if (nb) push_near = atomicOr(A.fm_near + u, nb) == 0ull;
+        if (fb) push_far = atomicOr(A.fm_far + u, fb) == 0ull;
+        const uint32_t sn = warp_append(push_near, nnext_cnt);
+        if (push_near) {
+          if (sn < A.lcap) nnext[sn] = u; else atomicExch(A.ctl + B_ERR, 2u);
+        }
+        const uint32_t sf = warp_append(push_far, far_cnt);
+        if (push_far) {
+          if (sf < A.lcap) far[sf] = u; else atomicExch(A.ctl + B_ERR, 2u);
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long t = __shfl_down_sync(0xffffffffu, minfar, o);
+      minfar = t < minfar ? t : minfar;
+    }
+    if (lane == 0 && minfar < kInfBits) atomicMin(A.cnt + BC_MINFAR, minfar);
+    __syncwarp();
+  }
+}
+
+// Far scan: after the bucket limit moved, every far pair below it goes to
+// the near mask; the rest stays far (into the other far list).
+__device__ void sssp_scan(const BatchArgs& A) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t w = threadIdx.x >> 5;
+  const uint32_t nsel = __ldcg(A.ctl + B_NSEL);
+  const uint32_t fsel = __ldcg(A.ctl + B_FSEL);
+  const uint32_t cnt = (uint32_t)min((uint64_t)__ldcg(A.ctl + B_FCNT0 + fsel), A.lcap);
+  const uint32_t* list = A.fl[fsel];
+  uint32_t* nnext = A.nl[nsel ^ 1];
+  uint32_t* nnext_cnt = A.ctl + B_NCNT0 + (nsel ^ 1);
+  uint32_t* fnext = A.fl[fsel ^ 1];
+  uint32_t* fnext_cnt = A.ctl + B_FCNT0 + (fsel ^ 1);
+  const unsigned long long lim = __ldcg(A.cnt + BC_LIMIT);
+  const uint32_t ns = A.ns;
+  const uint32_t nwarps = gridDim.x * (BT / 32);
+  // lanes over list entries; sources of one vertex in a loop
+  for (uint32_t i0 = (blockIdx.x * (BT / 32) + w) * 32; i0 < cnt; i0 += nwarps * 32) {
+    const uint32_t i = i0 + lane;
+    bool push_near = false, push_far = false;
+    uint32_t v = 0;
+    unsigned long long minfar = kInfBits;
+    if (i < cnt) {
+      v = __ldcg(list + i);
+      const unsigned long long m = atomicExch(A.fm_far + v, 0ull);
+      unsigned long long nb = 0, fb = 0;
+      for (unsigned long long mm = m; mm; mm &= mm - 1) {
+        const uint32_t s = __ffsll((long long)mm) - 1;
+        const unsigned long long d = __ldcg(A.dist + (uint64_t)v * ns + s);
+        if (d < lim) {
+          nb |= 1ull << s;
+        } else {
+          fb |= 1ull << s;
+          minfar = d < minfar ? d : minfar;
+        }
+      }
+      if (nb) push_near = atomicOr(A.fm_near + v, nb) == 0ull;
+      if (fb) push_far = atomicOr(A.fm_far + v, fb) == 0ull;
+    }
+    const uint32_t sn = warp_append(push_near, nnext_cnt);
+    if (push_near) {
+      if (sn < A.lcap) nnext[sn] = v; else atomicExch(A.ctl + B_ERR, 2u);
+    }
+    const uint32_t sf = warp_append(push_far, fnext_cnt);
+    if (push_far) {
+      if (sf < A.lcap) fnext[sf] = v; else atomicExch(A.ctl + B_ERR, 2u);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long t = __shfl_down_sync(0xffffffffu, minfar, o);
+      minfar = t < minfar ? t : minfar;
+    }
+    if (lane == 0 && minfar < kInfBits) atomicMin(A.cnt + BC_MINFAR, minfar);
+  }
+}
+
+// Block 0, between the barriers: per-query PPR decisions and the SSSP list
+// rotation / bucket advance.  Everything it reads was written by other
+// blocks before the barrier, so it reads through L2 (__ldcg).
+__device__ void decide(const BatchArgs& A) {
+  __shared__ uint32_t s_part, s_live;
+  if (threadIdx.x == 0) {
+    s_part = 0;
+    s_live = 0;
+  }
+  __syncthreads();
+  const bool ppr_on = A.qw > 0 && __ldcg(A.ctl + B_PPR_LIVE) != 0;
+  if (ppr_on) {
+    for (uint32_t q = threadIdx.x; q < A.nq; q += BT) {
+      const uint32_t st = __ldcg(A.qstate + q);
+      if (st == Q_DONE) continue;
+      atomicAdd(&s_part, 1u);
+      const double R = __ldcg(A.qres + q) + __ldcg(A.qres0 + q);
+      A.qres[q] = 0.0;
+      A.qlast[q] = R;
+      if (st == Q_ACTIVE) {
+        const uint32_t r = __ldcg(A.qrounds + q) + 1;
+        A.qrounds[q] = r;
+        if (R < A.tau) {
+          A.qstate[q] = Q_PENDING;
+        } else if (r >= A.max_rounds) {
+          A.qstate[q] = Q_PENDING;
+          atomicAdd(A.ctl + B_NOTCONV, 1u);
+        }
+        atomicAdd(&s_live, 1u);
+      } else {  // the drain round ran: the query is finished
+        A.qstate[q] = Q_DONE;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (ppr_on) {
+      A.ctl[B_PPR_LIVE] = s_live;
+      A.ctl[B_PULL] = __ldcg(A.ctl + B_PULL) + 1;
+      A.ctl[B_ITERS_PPR] = __ldcg(A.ctl + B_ITERS_PPR) + 1;
+      A.cnt[BC_PPR_EDGES] = __ldcg(A.cnt + BC_PPR_EDGES) + A.live_edges * (unsigned long long)s_part;
+    }
+    if (A.ns > 0 && __ldcg(A.ctl + B_SSSP_LIVE)) {
+      A.ctl[B_ITERS_SSSP] = __ldcg(A.ctl + B_ITERS_SSSP) + 1;
+      const uint32_t nsel = __ldcg(A.ctl + B_NSEL);
+      uint32_t fsel = __ldcg(A.ctl + B_FSEL);
+      if (__ldcg(A.ctl + B_SMODE) == 1) {  // the scan consumed far list fsel
+        A.ctl[B_FCNT0 + fsel] = 0;
+        fsel ^= 1;
+        A.ctl[B_FSEL] = fsel;
+      }
+      // the near list just read is consumed; the one filled becomes current
+      A.ctl[B_NCNT0 + nsel] = 0;
+      A.ctl[B_NSEL] = nsel ^ 1;
+      const uint32_t ncur = __ldcg(A.ctl + B_NCNT0 + (nsel ^ 1));
+      const uint32_t fcur = __ldcg(A.ctl + B_FCNT0 + fsel);
+      if (ncur > 0) {
+        A.ctl[B_SMODE] = 0;
+      } else if (fcur > 0) {
+        // next bucket: the one holding the smallest pending far distance
+        const double mf = bitsd(__ldcg(A.cnt + BC_MINFAR));
+        const double lim = (floor(mf / A.sdelta) + 1.0) * A.sdelta;
+        A.cnt[BC_LIMIT] = dbits(lim);
+        A.cnt[BC_MINFAR] = kInfBits;
+        A.ctl[B_SMODE] = 1;
+        A.ctl[B_SCANS] = __ldcg(A.ctl + B_SCANS) + 1;
+      } else {
+        A.ctl[B_SSSP_LIVE] = 0;
+      }
+    }
+    A.ctl[B_ITER] = __ldcg(A.ctl + B_ITER) + 1;
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+template <int F>
+__global__ void __launch_bounds__(BT) k_batch(BatchArgs A) {
+  __shared__ Smem S;
+  for (uint32_t q = threadIdx.x; q < kMaxQW; q += BT) {
+    S.qres[q] = 0.0;
+    S.qstate[q] = q < A.nq ? A.qstate[q] : Q_DONE;
+  }
+  __syncthreads();
+  double res[F * 4];
+#pragma unroll
+  for (int j = 0; j < F * 4; ++j) res[j] = 0.0;
+  unsigned long long relax = 0, improve = 0;
+  if (A.qw > 0 && __ldcg(A.ctl + B_PULL) == 0 && __ldcg(A.ctl + B_ITER) == 0) {
+    // the first activation's residual is not tested (the first pull's is)
+    ppr_activate_all<F>(A, S);
+    if (!bgrid_sync(A)) return;
+  }
+  for (uint32_t it = 0; it < A.max_iters; ++it) {
+    const bool ppr_on = A.qw > 0 && *(volatile uint32_t*)(A.ctl + B_PPR_LIVE) != 0;
+    const bool sssp_on = A.ns > 0 && *(volatile uint32_t*)(A.ctl + B_SSSP_LIVE) != 0;
+    if (!ppr_on && !sssp_on) break;
+    const uint32_t p = *(volatile uint32_t*)(A.ctl + B_PULL);
+    if (ppr_on) {
+      for (uint32_t q = threadIdx.x; q < kMaxQW; q += BT)
+        S.qstate[q] = q < A.nq ? __ldcg(A.qstate + q) : Q_DONE;
+      __syncthreads();
+      ppr_pull<F>(A, S, p, res);
+    }
+    if (sssp_on) {
+      if (*(volatile uint32_t*)(A.ctl + B_SMODE) == 0) sssp_near(A, S, relax, improve);
+      else sssp_scan(A);
+    }
+    if (!bgrid_sync(A)) return;
+    if (ppr_on) {
+      ppr_fixup<F>(A, S, p, res);
+      ppr_flush_res<F>(A, S, res);
+    }
+    if (!bgrid_sync(A)) return;
+    if (blockIdx.x == 0) decide(A);
+    if (!bgrid_sync(A)) return;
+  }
+  // counters
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    relax += __shfl_down_sync(0xffffffffu, relax, o);
+    improve += __shfl_down_sync(0xffffffffu, improve, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (relax) atomicAdd(A.cnt + BC_SSSP_RELAX, relax);
+    if (improve) atomicAdd(A.cnt + BC_SSSP_IMPROVE, improve);
+  }
+}
+
+// ------------------------------------------------------------ set-up kernels
+
+__global__ void k_chunk_v0(const uint64_t* __restrict__ qoff, uint32_t nz_count, uint64_t nchunks,
+                           uint32_t cq, uint32_t* __restrict__ cv0) {
+  for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < nchunks;
+       c += (uint64_t)gridDim.x * blockDim.x)
+    cv0[c] = upper_owner(qoff, 0u, nz_count, c * (uint64_t)cq);
+}
+
+__global__ void k_chunk_bnd_flags(const uint64_t* __restrict__ qoff, uint32_t nz_count, uint32_t cq,
+                                  uint8_t* __restrict__ f) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nz_count; i += gridDim.x * blockDim.x)
+    f[i] = (qoff[i] / cq) != ((qoff[i + 1] - 1) / cq);
+}
+
+__global__ void k_fill_u64(unsigned long long* p, uint64_t n, unsigned long long v) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+// teleport mass of each query onto its seeds; sources at distance 0
+__global__ void k_batch_seed(const uint32_t* __restrict__ seed_ptr, const uint32_t* __restrict__ seeds,
+                             uint32_t nq, uint32_t qw, float one_minus_d, float* D,
+                             const uint32_t* __restrict__ sources, uint32_t ns,
+                             unsigned long long* dist, unsigned long long* fm_near, uint32_t* nl0,
+                             uint32_t* ncnt0) {
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nth = gridDim.x * blockDim.x;
+  for (uint32_t q = tid; q < nq; q += nth) {
+    const uint32_t a = seed_ptr[q], b = seed_ptr[q + 1];
+    const float mass = b > a ? one_minus_d / (float)(b - a) : 0.f;
+    for (uint32_t i = a; i < b; ++i) atomicAdd(D + (uint64_t)seeds[i] * qw + q, mass);
+  }
+  for (uint32_t s = tid; s < ns; s += nth) {
+    const uint32_t v = sources[s];
+    dist[(uint64_t)v * ns + s] = 0ull;
+    if (atomicOr(fm_near + v, 1ull << s) == 0ull) nl0[atomicAdd(ncnt0, 1u)] = v;
+  }
+}
+
+// control words of a fresh run
+__global__ void k_batch_init_ctl(uint32_t* ctl, unsigned long long* cnt, uint32_t nq, uint32_t ns,
+                                 double sdelta) {
+  const uint32_t t = threadIdx.x;
+  if (t < B_WORDS) ctl[t] = t == B_PPR_LIVE ? nq : (t == B_SSSP_LIVE ? (ns > 0 ? 1u : 0u) : 0u);
+  if (t < BC_WORDS)
+    cnt[t] = t == BC_MINFAR ? kInfBits : (t == BC_LIMIT ? dbits(sdelta) : 0ull);
+}
+
+// [n][qw] -> [nq][n]
+__global__ void k_ppr_out(const float* __restrict__ X, uint32_t n, uint32_t qw, uint32_t nq,
+                          float* __restrict__ out) {
+  __shared__ float tile[32][33];
+  for (uint32_t vb = blockIdx.x * 32; vb < n; vb += gridDim.x * 32) {
+    for (uint32_t qb = 0; qb < nq; qb += 32) {
+      const uint32_t v = vb + threadIdx.y, q = qb + threadIdx.x;
+      tile[threadIdx.y][threadIdx.x] = (v < n && q < nq) ? X[(uint64_t)v * qw + q] : 0.f;
+      __syncthreads();
+      const uint32_t q2 = qb + threadIdx.y, v2 = vb + threadIdx.x;
+      if (q2 < nq && v2 < n) out[(uint64_t)q2 * n + v2] = tile[threadIdx.x][threadIdx.y];
+      __syncthreads();
+    }
+  }
+}
+
+// [n][ns] ordered bits -> [ns][n] doubles
+__global__ void k_sssp_out(const unsigned long long* __restrict__ dist, uint32_t n, uint32_t ns,
+                           double* __restrict__ out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < (uint64_t)n * ns;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t s = (uint32_t)(i / n), v = (uint32_t)(i % n);
+    out[i] = bitsd(dist[(uint64_t)v * ns + s]);
+  }
+}
+
+}  // namespace
+
+// ================================================================ host side
+
+struct BatchState {
+  uint32_t n = 0;
+  // PPR capacity (qw columns) and SSSP capacity (ns sources)
+  uint32_t qw_cap = 0, ns_cap = 0;
+  float *X = nullptr, *D = nullptr, *PV0 = nullptr, *PV[2] = {nullptr, nullptr}, *ACC = nullptr;
+  uint8_t *act0 = nullptr, *act[2] = {nullptr, nullptr};
+  uint32_t *qstate = nullptr, *qrounds = nullptr;
+  double *qres = nullptr, *qres0 = nullptr, *qlast = nullptr;
+  unsigned long long *dist = nullptr, *fm_near = nullptr, *fm_far = nullptr;
+  uint32_t *nl[2] = {nullptr, nullptr}, *fl[2] = {nullptr, nullptr};
+  uint64_t lcap = 0;
+  uint32_t* ctl = nullptr;
+  unsigned long long* cnt = nullptr;
+  uint32_t *seed_ptr = nullptr, *seeds = nullptr, *sources = nullptr;
+  uint64_t seeds_cap = 0;
+  float* ppr_out = nullptr;
+  double* sssp_out = nullptr;
+  uint64_t ppr_out_cap = 0, sssp_out_cap = 0;
+  // chunk lists for the current schedule and graph
+  uint64_t chunk_gen = ~0ull;
+  uint32_t chunk_cq = 0;
+  uint32_t* chunk_v0 = nullptr;
+  uint64_t chunk_cap = 0, nchunks = 0;
+  uint32_t* bnd = nullptr;
+  uint32_t nbnd = 0;
+  // schedule
+  bool tuned = false;
+  uint64_t tuned_key = 0;
+  uint32_t cq = 8, bps = 2;
+  double sdelta = 32.0;
+  double tune_ms = 0.0;
+  // captured launch sequence
+  cudaGraphExec_t exec = nullptr;
+  uint64_t exec_key = 0;
+  bool graph_failed = false;
+  // last run
+  uint32_t nq = 0, ns = 0, qw = 0;
+  bool valid = false;
+  sg_batch_info info{};
+};
+
+static BatchState* bstate(sg_ctx* ctx) { return (BatchState*)ctx->batch_state; }
+
+static void bfree_arrays(BatchState& B) {
+  dfree(B.X); dfree(B.D); dfree(B.PV0); dfree(B.PV[0]); dfree(B.PV[1]); dfree(B.ACC);
+  dfree(B.act0); dfree(B.act[0]); dfree(B.act[1]);
+  dfree(B.qstate); dfree(B.qrounds); dfree(B.qres); dfree(B.qres0); dfree(B.qlast);
+  dfree(B.dist); dfree(B.fm_near); dfree(B.fm_far);
+  dfree(B.nl[0]); dfree(B.nl[1]); dfree(B.fl[0]); dfree(B.fl[1]);
+  dfree(B.ctl); dfree(B.cnt); dfree(B.seed_ptr); dfree(B.seeds); dfree(B.sources);
+  dfree(B.ppr_out); dfree(B.sssp_out); dfree(B.chunk_v0); dfree(B.bnd);
+  if (B.exec) cudaGraphExecDestroy(B.exec);
+  B.exec = nullptr;
+}
+
+sg_status batch_free(sg_ctx* ctx) {
+  BatchState* B = bstate(ctx);
+  if (B) {
+    bfree_arrays(*B);
+    delete B;
+  }
+  ctx->batch_state = nullptr;
+  return SG_OK;
+}
+
+static uint32_t pow2_at_least(uint32_t x) {
+  uint32_t p = 4;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+// Buffers for nq PPR queries (qw columns) and ns SSSP sources.
+static sg_status batch_reserve(sg_ctx* ctx, BatchState& B, uint32_t qw, uint32_t ns,
+                               uint64_t total_seeds) {
+  const uint32_t n = ctx->g.n;
+  if (B.n != n) {
+    bfree_arrays(B);
+    B = BatchState();
+    B.n = n;
+  }
+  if (qw > B.qw_cap) {
+    dfree(B.X); dfree(B.D); dfree(B.PV0); dfree(B.PV[0]); dfree(B.PV[1]); dfree(B.ACC);
+    const uint64_t cells = (uint64_t)n * qw;
+    SG_TRY(dalloc(ctx, &B.X, cells));
+    SG_TRY(dalloc(ctx, &B.D, cells));
+    SG_TRY(dalloc(ctx, &B.PV0, cells));
+    SG_TRY(dalloc(ctx, &B.PV[0], cells));
+    SG_TRY(dalloc(ctx, &B.PV[1], cells));
+    SG_TRY(dalloc(ctx, &B.ACC, cells));
+    SG_CUDA(ctx, cudaMemsetAsync(B.ACC, 0, 4 * cells, ctx->stream));
+    B.qw_cap = qw;
+    if (B.exec) cudaGraphExecDestroy(B.exec);
+    B.exec = nullptr;
+  }
+  if (!B.act0) {
+    SG_TRY(dalloc(ctx, &B.act0, n));
+    SG_TRY(dalloc(ctx, &B.act[0], n));
+    SG_TRY(dalloc(ctx, &B.act[1], n));
+    SG_TRY(dalloc(ctx, &B.qstate, kMaxQW));
+    SG_TRY(dalloc(ctx, &B.qrounds, kMaxQW));
+    SG_TRY(dalloc(ctx, &B.qres, kMaxQW));
+    SG_TRY(dalloc(ctx, &B.qres0, kMaxQW));
+    SG_TRY(dalloc(ctx, &B.qlast, kMaxQW));
+    SG_TRY(dalloc(ctx, &B.ctl, B_WORDS));
+    SG_TRY(dalloc(ctx, &B.cnt, BC_WORDS));
+    SG_TRY(dalloc(ctx, &B.seed_ptr, kMaxQW + 1));
+    SG_TRY(dalloc(ctx, &B.sources, kMaxNS));
+    SG_TRY(dalloc(ctx, &B.fm_near, n));
+    SG_TRY(dalloc(ctx, &B.fm_far, n));
+    // a vertex enters a list when its mask turns non-zero, at most twice per
+    // step (before and after its own mask is taken)
+    B.lcap = 2ull * n + 1024;
+    for (int i = 0; i < 2; ++i) {
+      SG_TRY(dalloc(ctx, &B.nl[i], B.lcap));
+      SG_TRY(dalloc(ctx, &B.fl[i], B.lcap));
+    }
+  }
+  if (ns > B.ns_cap) {
+    dfree(B.dist);
+    SG_TRY(dalloc(ctx, &B.dist, (uint64_t)n * ns));
+    B.ns_cap = ns;
+    if (B.exec) cudaGraphExecDestroy(B.exec);
+    B.exec = nullptr;
+  }
+  if (total_seeds > B.seeds_cap) {
+    dfree(B.seeds);
+    B.seeds_cap = std::max<uint64_t>(total_seeds, 4096);
+    SG_TRY(dalloc(ctx, &B.seeds, B.seeds_cap));
+    if (B.exec) cudaGraphExecDestroy(B.exec);
+    B.exec = nullptr;
+  }
+  return SG_OK;
+}
+
+static sg_status batch_chunks(sg_ctx* ctx, BatchState& B, uint32_t cq) {
+  DevGraph& g = ctx->g;
+  if (B.chunk_gen == g.gen && B.chunk_cq == cq) return SG_OK;
+  const uint64_t nch = (g.in_wl.quads + cq - 1) / cq;
+  if (nch + 1 > B.chunk_cap) {
+    dfree(B.chunk_v0);
+    B.chunk_cap = nch + 1024;
+    SG_TRY(dalloc(ctx, &B.chunk_v0, B.chunk_cap));
+  }
+  if (!B.bnd) SG_TRY(dalloc(ctx, &B.bnd, std::max<uint32_t>(ctx->g.n, 1)));
+  cudaStream_t st = ctx->stream;
+  if (nch) k_chunk_v0<<<grid_for(nch, 256), 256, 0, st>>>(g.in_wl.qoff, g.in_wl.nz_count, nch, cq, B.chunk_v0);
+  uint8_t* flags = nullptr;
+  uint64_t* d_cnt = nullptr;
+  SG_TRY(dalloc(ctx, &flags, std::max<uint32_t>(g.in_wl.nz_count, 1)));
+  SG_TRY(dalloc(ctx, &d_cnt, 1));
+  uint64_t h = 0;
+  if (g.in_wl.nz_count) {
+    k_chunk_bnd_flags<<<grid_for(g.in_wl.nz_count, 256), 256, 0, st>>>(g.in_wl.qoff, g.in_wl.nz_count, cq, flags);
+    sg_status s = cub_select_flagged_u32(ctx, g.in_wl.nz, flags, B.bnd, d_cnt, g.in_wl.nz_count);
+    if (s != SG_OK) {
+      dfree(flags);
+      dfree(d_cnt);
+      return s;
+    }
+    SG_CUDA(ctx, cudaMemcpyAsync(&h, d_cnt, 8, cudaMemcpyDeviceToHost, st));
+  }
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  dfree(flags);
+  dfree(d_cnt);
+  count_launch(ctx, 3);
+  B.nchunks = nch;
+  B.nbnd = (uint32_t)h;
+  B.chunk_cq = cq;
+  B.chunk_gen = g.gen;
+  if (B.exec) cudaGraphExecDestroy(B.exec);
+  B.exec = nullptr;
+  return SG_OK;
+}
+
+static BatchArgs batch_args(sg_ctx* ctx, BatchState& B, uint32_t nq, uint32_t ns, double sdelta,
+                            uint32_t max_iters) {
+  DevGraph& g = ctx->g;
+  BatchArgs A{};
+  A.n = g.n;
+  A.live_edges = g.m;
+  A.in_off = g.in.off; A.in_col = g.in.col; A.in_deg = g.in.deg; A.out_deg = g.out.deg;
+  A.nz = g.in_wl.nz; A.qoff = g.in_wl.qoff; A.nz_count = g.in_wl.nz_count; A.quads = g.in_wl.quads;
+  A.cq = B.chunk_cq; A.nchunks = B.nchunks; A.chunk_v0 = B.chunk_v0; A.bnd = B.bnd; A.nbnd = B.nbnd;
+  A.nq = nq;
+  A.qw = nq ? pow2_at_least(nq) : 0;
+  A.X = B.X; A.D = B.D; A.PV0 = B.PV0; A.PV[0] = B.PV[0]; A.PV[1] = B.PV[1]; A.ACC = B.ACC;
+  A.act0 = B.act0; A.act[0] = B.act[0]; A.act[1] = B.act[1];
+  A.qstate = B.qstate; A.qrounds = B.qrounds; A.qres = B.qres; A.qres0 = B.qres0; A.qlast = B.qlast;
+  A.damping = (float)ctx->opt.damping;
+  A.thr_v = (float)(ctx->opt.termcheck_threshold / (double)g.n);
+  A.tau = ctx->opt.termcheck_threshold;
+  A.max_rounds = ctx->opt.max_rounds > 0 ? (uint32_t)ctx->opt.max_rounds : 1000u;
+  A.ns = ns;
+  A.out_off = g.out.off; A.out_col = g.out.col; A.out_w = g.out.w;
+  A.dist = B.dist; A.fm_near = B.fm_near; A.fm_far = B.fm_far;
+  A.nl[0] = B.nl[0]; A.nl[1] = B.nl[1]; A.fl[0] = B.fl[0]; A.fl[1] = B.fl[1];
+  A.lcap = B.lcap;
+  A.sdelta = sdelta;
+  A.ctl = B.ctl;
+  A.cnt = B.cnt;
+  A.spin_limit = 40ll * 1000 * 1000;
+  A.max_iters = max_iters;
+  return A;
+}
+
+// State reset + seed scatter + persistent kernel + result transposes, all
+// kernels and memsets on the context stream (capturable into a CUDA graph).
+static sg_status batch_sequence(sg_ctx* ctx, BatchState& B, const BatchArgs& A, uint32_t bps,
+                                bool outputs) {
+  cudaStream_t st = ctx->stream;
+  const uint32_t n = A.n;
+  if (A.nq > 0) {
+    const uint64_t bytes = 4ull * n * A.qw;
+    SG_CUDA(ctx, cudaMemsetAsync(A.X, 0, bytes, st));
+    SG_CUDA(ctx, cudaMemsetAsync(A.D, 0, bytes, st));
+    SG_CUDA(ctx, cudaMemsetAsync(A.PV[0], 0, bytes, st));
+    SG_CUDA(ctx, cudaMemsetAsync(A.PV[1], 0, bytes, st));
+    SG_CUDA(ctx, cudaMemsetAsync(A.act[0], 0, n, st));
+    SG_CUDA(ctx, cudaMemsetAsync(A.act[1], 0, n, st));
+    SG_CUDA(ctx, cudaMemsetAsync(A.qstate, 0, 4 * kMaxQW, st));
+    SG_CUDA(ctx, cudaMemsetAsync(A.qrounds, 0, 4 * kMaxQW, st));
+    SG_CUDA(ctx, cudaMemsetAsync(A.qres, 0, 8 * kMaxQW, st));
+    SG_CUDA(ctx, cudaMemsetAsync(A.qres0, 0, 8 * kMaxQW, st));
+    SG_CUDA(ctx, cudaMemsetAsync(A.qlast, 0, 8 * kMaxQW, st));
+  }
+  if (A.ns > 0) {
+    k_fill_u64<<<grid_for((uint64_t)n * A.ns, 256), 256, 0, st>>>(A.dist, (uint64_t)n * A.ns, kInfBits);
+    SG_CUDA(ctx, cudaMemsetAsync(A.fm_near, 0, 8ull * n, st));
+    SG_CUDA(ctx, cudaMemsetAsync(A.fm_far, 0, 8ull * n, st));
+  }
+  k_batch_init_ctl<<<1, 32, 0, st>>>(A.ctl, A.cnt, A.nq, A.ns, A.sdelta);
+  k_batch_seed<<<grid_for(std::max(A.nq, A.ns), 128), 128, 0, st>>>(
+      B.seed_ptr, B.seeds, A.nq, A.qw, (float)(1.0 - ctx->opt.damping), A.D, B.sources, A.ns,
+      A.dist, A.fm_near, A.nl[0], A.ctl + B_NCNT0);
+  const int F = A.qw > 128 ? 2 : 1;
+  const void* fn = F == 2 ? (const void*)k_batch<2> : (const void*)k_batch<1>;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(bps * ctx->num_sms);
+  cfg.blockDim = dim3(BT);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  BatchArgs a = A;
+  void* args[] = {&a};
+  SG_CUDA(ctx, cudaLaunchKernelExC(&cfg, fn, args));
+  if (outputs) {
+    if (A.nq > 0) {
+      k_ppr_out<<<std::min<uint32_t>((n + 31) / 32, 4096), dim3(32, 32), 0, st>>>(A.X, n, A.qw, A.nq,
+                                                                               B.ppr_out);
+    }
+    if (A.ns > 0)
+      k_sssp_out<<<grid_for((uint64_t)n * A.ns, 256), 256, 0, st>>>(A.dist, n, A.ns, B.sssp_out);
+  }
+  SG_CUDA(ctx, cudaGetLastError());
+  count_launch(ctx, 3 + (A.ns > 0) + (outputs ? (A.nq > 0) + (A.ns > 0) : 0));
+  return SG_OK;
+}
+
+static int max_bps(sg_ctx* ctx, uint32_t qw) {
+  int b = 0;
+  const void* fn = qw > 128 ? (const void*)k_batch<2> : (const void*)k_batch<1>;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, BT, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return b;
+}
+
+// Runs one sequence directly (no graph) and waits; returns its device time.
+static sg_status batch_trial(sg_ctx* ctx, BatchState& B, const BatchArgs& A, uint32_t bps,
+                             float* ms) {
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+  SG_TRY(batch_sequence(ctx, B, A, bps, false));
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  uint32_t err = 0;
+  SG_CUDA(ctx, cudaMemcpy(&err, A.ctl + B_ERR, 4, cudaMemcpyDeviceToHost));
+  if (err == 1u) return fail(ctx, SG_ERR_TIMEOUT, "batched kernel: grid barrier wait expired");
+  if (err == 2u) return fail(ctx, SG_ERR_OOM, "batched kernel: frontier list overflow");
+  SG_CUDA(ctx, cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+  return SG_OK;
+}
+
+// In-house autotuner: times candidate schedules on the caller's batch.
+//   PPR  : chunk quads x blocks per SM, a few rounds each (a round's cost is
+//          about constant once the queries have spread)
+//   SSSP : bucket width, full runs at the chosen blocks per SM
+static sg_status batch_tune(sg_ctx* ctx, BatchState& B, uint32_t nq, uint32_t ns) {
+  const auto t0 = std::chrono::steady_clock::now();
+  const uint32_t qw = nq ? pow2_at_least(nq) : 0;
+  const int mb = std::max(1, std::min(4, max_bps(ctx, qw)));
+  uint32_t best_cq = 8, best_bps = (uint32_t)std::min(mb, 2);
+  if (nq > 0) {
+    float best = 1e30f;
+    for (uint32_t cq : {2u, 4u, 8u, 16u, 32u}) {
+      SG_TRY(batch_chunks(ctx, B, cq));
+      for (int bps = 1; bps <= mb; bps *= 2) {
+        const BatchArgs A = batch_args(ctx, B, nq, 0, B.sdelta, 6);
+        float ms = 0.f;
+        SG_TRY(batch_trial(ctx, B, A, (uint32_t)bps, &ms));
+        if (ms < best) {
+          best = ms;
+          best_cq = cq;
+          best_bps = (uint32_t)bps;
+        }
+      }
+    }
+  }
+  B.cq = best_cq;
+  B.bps = best_bps;
+  SG_TRY(batch_chunks(ctx, B, B.cq));
+  if (ns > 0) {
+    float best = 1e30f;
+    double best_d = 32.0;
+    for (double dl : {8.0, 16.0, 32.0, 64.0, 128.0}) {
+      const BatchArgs A = batch_args(ctx, B, 0, ns, dl, 1u << 30);
+      float ms = 0.f;
+      SG_TRY(batch_trial(ctx, B, A, B.bps, &ms));
+      if (ms < best) {
+        best = ms;
+        best_d = dl;
+      }
+    }
+    B.sdelta = best_d;
+  }
+  B.tuned = true;
+  B.tune_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return SG_OK;
+}
+
+sg_status batch_run(sg_ctx* ctx, const sg_batch_spec* spec, float* ppr_out, double* sssp_out,
+                    bool retune) {
+  DevGraph& g = ctx->g;
+  if (!g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
+  const uint32_t nq = spec->ppr_queries, ns = spec->sssp_sources;
+  if (nq > kMaxQW) return fail(ctx, SG_ERR_INVALID, "at most 256 PPR queries per batch");
+  if (ns > kMaxNS) return fail(ctx, SG_ERR_INVALID, "at most 64 SSSP sources per batch");
+  if (nq == 0 && ns == 0) return fail(ctx, SG_ERR_INVALID, "empty batch");
+  if (ns > 0 && !g.weighted) return fail(ctx, SG_ERR_INVALID, "SSSP needs a weighted graph");
+  if (nq > 0 && (!spec->ppr_seed_ptr || !spec->ppr_seeds))
+    return fail(ctx, SG_ERR_INVALID, "PPR seeds missing");
+  if (ns > 0 && !spec->sources) return fail(ctx, SG_ERR_INVALID, "SSSP sources missing");
+  uint64_t total = 0;
+  if (nq > 0) {
+    if (spec->ppr_seed_ptr[0] != 0) return fail(ctx, SG_ERR_INVALID, "seed_ptr[0] must be 0");
+    for (uint32_t q = 0; q < nq; ++q) {
+      if (spec->ppr_seed_ptr[q + 1] <= spec->ppr_seed_ptr[q])
+        return fail(ctx, SG_ERR_INVALID, "every PPR query needs at least one seed");
+    }
+    total = spec->ppr_seed_ptr[nq];
+    for (uint64_t i = 0; i < total; ++i)
+      if (spec->ppr_seeds[i] >= g.n) return fail(ctx, SG_ERR_INVALID, "seed vertex >= n");
+  }
+  for (uint32_t s = 0; s < ns; ++s)
+    if (spec->sources[s] >= g.n) return fail(ctx, SG_ERR_INVALID, "source vertex >= n");
+  if (!ctx->batch_state) ctx->batch_state = new BatchState();
+  BatchState& B = *bstate(ctx);
+  const uint32_t qw = nq ? pow2_at_least(nq) : 0;
+  SG_TRY(batch_reserve(ctx, B, qw, ns, total));
+  if ((uint64_t)nq * g.n > B.ppr_out_cap) {
+    dfree(B.ppr_out);
+    SG_TRY(dalloc(ctx, &B.ppr_out, (uint64_t)nq * g.n));
+    B.ppr_out_cap = (uint64_t)nq * g.n;
+    if (B.exec) cudaGraphExecDestroy(B.exec);
+    B.exec = nullptr;
+  }
+  if ((uint64_t)ns * g.n > B.sssp_out_cap) {
+    dfree(B.sssp_out);
+    SG_TRY(dalloc(ctx, &B.sssp_out, (uint64_t)ns * g.n));
+    B.sssp_out_cap = (uint64_t)ns * g.n;
+    if (B.exec) cudaGraphExecDestroy(B.exec);
+    B.exec = nullptr;
+  }
+  cudaStream_t st = ctx->stream;
+  if (nq > 0) {
+    SG_CUDA(ctx, cudaMemcpyAsync(B.seed_ptr, spec->ppr_seed_ptr, 4ull * (nq + 1), cudaMemcpyHostToDevice, st));
+    SG_CUDA(ctx, cudaMemcpyAsync(B.seeds, spec->ppr_seeds, 4ull * total, cudaMemcpyHostToDevice, st));
+  }
+  if (ns > 0)
+    SG_CUDA(ctx, cudaMemcpyAsync(B.sources, spec->sources, 4ull * ns, cudaMemcpyHostToDevice, st));
+  // schedule
+  const uint64_t tkey = ((uint64_t)g.n << 20) ^ ((uint64_t)qw << 8) ^ ns;
+  if (retune || !B.tuned || B.tuned_key != tkey) {
+    SG_TRY(batch_tune(ctx, B, nq, ns));
+    B.tuned_key = tkey;
+  }
+  SG_TRY(batch_chunks(ctx, B, B.cq));
+  const BatchArgs A = batch_args(ctx, B, nq, ns, B.sdelta, 1u << 30);
+  // captured launch sequence, keyed by everything baked into it
+  const uint64_t key = tkey ^ (g.gen * 0x9E3779B97F4A7C15ull) ^ ((uint64_t)B.cq << 40) ^
+                       ((uint64_t)B.bps << 48) ^ ((uint64_t)(B.sdelta * 16) << 52) ^
+                       ((uint64_t)nq << 28);
+  bool used_graph = false;
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+  if (!B.graph_failed) {
+    if (!B.exec || B.exec_key != key) {
+      if (B.exec) cudaGraphExecDestroy(B.exec);
+      B.exec = nullptr;
+      cudaGraph_t graph = nullptr;
+      bool ok = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      sg_status seq = SG_OK;
+      if (ok) seq = batch_sequence(ctx, B, A, B.bps, true);
+      const cudaError_t ec = ok ? cudaStreamEndCapture(st, &graph) : cudaErrorUnknown;
+      ok = ok && seq == SG_OK && ec == cudaSuccess && graph != nullptr;
+      if (ok) ok = cudaGraphInstantiate(&B.exec, graph, 0) == cudaSuccess;
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      if (!ok) {
+        B.exec = nullptr;
+        B.graph_failed = true;  // launch the same sequence directly from now on
+        ctx->err.clear();
+      } else {
+        B.exec_key = key;
+      }
+    }
+    if (B.exec) {
+      // the event was recorded before the capture; record again for timing
+      SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+      SG_CUDA(ctx, cudaGraphLaunch(B.exec, st));
+      used_graph = true;
+    }
+  }
+  if (!used_graph) SG_TRY(batch_sequence(ctx, B, A, B.bps, true));
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+  uint32_t h_ctl[B_WORDS];
+  unsigned long long h_cnt[BC_WORDS];
+  SG_CUDA(ctx, cudaMemcpyAsync(h_ctl, B.ctl, sizeof(h_ctl), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaMemcpyAsync(h_cnt, B.cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  B.nq = nq;
+  B.ns = ns;
+  B.qw = qw;
+  sg_batch_info& I = B.info;
+  std::memset(&I, 0, sizeof(I));
+  I.ppr_queries = nq;
+  I.sssp_sources = ns;
+  I.chunk_quads = B.cq;
+  I.blocks_per_sm = B.bps;
+  I.sssp_bucket = B.sdelta;
+  I.graph_launch = used_graph ? 1 : 0;
+  I.tune_ms = B.tune_ms;
+  I.iterations = h_ctl[B_ITER];
+  I.ppr_pulls = h_ctl[B_ITERS_PPR];
+  I.sssp_steps = h_ctl[B_ITERS_SSSP];
+  I.sssp_scans = h_ctl[B_SCANS];
+  I.ppr_not_converged = h_ctl[B_NOTCONV];
+  I.ppr_edge_visits = h_cnt[BC_PPR_EDGES];
+  I.sssp_relaxations = h_cnt[BC_SSSP_RELAX];
+  I.sssp_improvements = h_cnt[BC_SSSP_IMPROVE];
+  I.elapsed_ms = ms;
+  ctx->stats.elapsed_ms = ms;
+  ctx->stats.edges_relaxed = h_cnt[BC_PPR_EDGES] + h_cnt[BC_SSSP_RELAX];
+  if (h_ctl[B_ERR] == 1u) return fail(ctx, SG_ERR_TIMEOUT, "batched kernel: grid barrier wait expired");
+  if (h_ctl[B_ERR] == 2u) return fail(ctx, SG_ERR_OOM, "batched kernel: frontier list overflow");
+  if (h_ctl[B_PPR_LIVE] != 0 || h_ctl[B_SSSP_LIVE] != 0)
+    return fail(ctx, SG_ERR_NOT_CONVERGED, "batched kernel: iteration cap reached");
+  B.valid = true;
+  if (ppr_out && nq > 0)
+    SG_CUDA(ctx, cudaMemcpyAsync(ppr_out, B.ppr_out, 4ull * nq * g.n, cudaMemcpyDeviceToHost, st));
+  if (sssp_out && ns > 0)
+    SG_CUDA(ctx, cudaMemcpyAsync(sssp_out, B.sssp_out, 8ull * ns * g.n, cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  if (h_ctl[B_NOTCONV]) return fail(ctx, SG_ERR_NOT_CONVERGED, "a PPR query reached the round cap");
+  return SG_OK;
+}
+
+sg_status batch_info(sg_ctx* ctx, sg_batch_info* out) {
+  BatchState* B = bstate(ctx);
+  if (!B || !B->valid) return fail(ctx, SG_ERR_STATE, "no batch has run");
+  *out = B->info;
+  return SG_OK;
+}
+
+sg_status batch_query_stats(sg_ctx* ctx, int32_t* rounds, double* residual) {
+  BatchState* B = bstate(ctx);
+  if (!B || !B->valid) return fail(ctx, SG_ERR_STATE, "no batch has run");
+  if (B->nq == 0) return SG_OK;
+  std::vector<uint32_t> r(B->nq);
+  std::vector<double> res(B->nq);
+  SG_CUDA(ctx, cudaMemcpy(r.data(), B->qrounds, 4ull * B->nq, cudaMemcpyDeviceToHost));
+  SG_CUDA(ctx, cudaMemcpy(res.data(), B->qlast, 8ull * B->nq, cudaMemcpyDeviceToHost));
+  for (uint32_t q = 0; q < B->nq; ++q) {
+    if (rounds) rounds[q] = (int32_t)r[q] + 1;  // + the first activation, as sg_pr_peval counts
+    if (residual) residual[q] = res[q];
+  }
+  return SG_OK;
+}
+
+sg_status batch_device_outputs(sg_ctx* ctx, const float** ppr, const double** sssp) {
+  BatchState* B = bstate(ctx);
+  if (!B || !B->valid) return fail(ctx, SG_ERR_STATE, "no batch has run");
+  if (ppr) *ppr = B->ppr_out;
+  if (sssp) *sssp = B->sssp_out;
+  return SG_OK;
+}
+
+}  // namespace sg

@@ -106,6 +106,7 @@ sg_status sg_options_default(sg_options* o) {
   o->compress_threshold = 1.0;   // flags.cc:67
   o->sssp_delta = 0.0;
   o->slack = 0.125;
+  o->adjoint_rel_tol = 1e-7;
   return SG_OK;
 }
 
@@ -149,6 +150,8 @@ sg_status sg_ctx_destroy(sg_ctx* ctx) {
   pr_free(ctx);
   sssp_free(ctx);
   summary_free(ctx);
+  batch_free(ctx);
+  adjoint_free(ctx);
   graph_free(ctx);
   DevBatch& B = ctx->batch;
   dfree(B.raw); dfree(B.key); dfree(B.key2); dfree(B.val); dfree(B.val2);
@@ -242,6 +245,8 @@ sg_status sg_graph_load_csr(sg_ctx* ctx, uint32_t n, const uint64_t* row_ptr,
     pr_free(ctx);
     sssp_free(ctx);
     summary_free(ctx);
+  batch_free(ctx);
+  adjoint_free(ctx);
     return load_csr(ctx, n, row_ptr, col, w);
   }
   SG_CATCH(ctx)
@@ -258,6 +263,8 @@ sg_status sg_graph_generate_rmat(sg_ctx* ctx, int scale, uint64_t edges, double 
     pr_free(ctx);
     sssp_free(ctx);
     summary_free(ctx);
+  batch_free(ctx);
+  adjoint_free(ctx);
     return generate_rmat(ctx, scale, edges, a, b, c, seed, weight_kind, wlo, whi);
   }
   SG_CATCH(ctx)
@@ -429,6 +436,119 @@ sg_status sg_sssp_parents(sg_ctx* ctx, uint32_t* out) {
                                ctx->stream));
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return SG_OK;
+}
+
+sg_status sg_ppr(sg_ctx* ctx, uint32_t n_seeds, const uint32_t* seeds, float* out) {
+  SG_GUARD(ctx);
+  try {
+    if (!seeds || n_seeds == 0) return fail(ctx, SG_ERR_INVALID, "PPR needs seeds");
+    if (!ctx->g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
+    for (uint32_t i = 0; i < n_seeds; ++i)
+      if (seeds[i] >= ctx->g.n) return fail(ctx, SG_ERR_INVALID, "seed vertex >= n");
+    sg_status st = pr_alloc(ctx);
+    if (st != SG_OK) return st;
+    uint32_t* d_seeds = nullptr;
+    st = dalloc(ctx, &d_seeds, n_seeds);
+    if (st != SG_OK) return st;
+    if (cudaMemcpyAsync(d_seeds, seeds, 4ull * n_seeds, cudaMemcpyHostToDevice, ctx->stream) !=
+        cudaSuccess) {
+      dfree(d_seeds);
+      return fail(ctx, SG_ERR_CUDA, "seed upload failed");
+    }
+    st = pr_run_personalized(ctx, d_seeds, n_seeds);
+    kprof_flush(ctx);
+    cudaStreamSynchronize(ctx->stream);
+    dfree(d_seeds);
+    ctx->pr.valid = false;  // a personalized result is no IncEval state
+    if (st != SG_OK && st != SG_ERR_NOT_CONVERGED) return st;
+    sg_status c = copy_out_f32(ctx, ctx->pr.x, out);
+    return c != SG_OK ? c : st;
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_batch_run(sg_ctx* ctx, const sg_batch_spec* spec, float* ppr_out, double* sssp_out) {
+  SG_GUARD(ctx);
+  if (!spec) return fail(ctx, SG_ERR_INVALID, "null batch spec");
+  try {
+    return batch_run(ctx, spec, ppr_out, sssp_out, false);
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_batch_tune_run(sg_ctx* ctx, const sg_batch_spec* spec, float* ppr_out,
+                            double* sssp_out) {
+  SG_GUARD(ctx);
+  if (!spec) return fail(ctx, SG_ERR_INVALID, "null batch spec");
+  try {
+    return batch_run(ctx, spec, ppr_out, sssp_out, true);
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_batch_info_get(sg_ctx* ctx, sg_batch_info* out) {
+  SG_GUARD(ctx);
+  if (!out) return fail(ctx, SG_ERR_INVALID, "null output");
+  return batch_info(ctx, out);
+}
+
+sg_status sg_batch_query_stats(sg_ctx* ctx, int32_t* rounds, double* residual) {
+  SG_GUARD(ctx);
+  try {
+    return batch_query_stats(ctx, rounds, residual);
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_batch_outputs_device(sg_ctx* ctx, const float** ppr, const double** sssp) {
+  SG_GUARD(ctx);
+  return batch_device_outputs(ctx, ppr, sssp);
+}
+
+sg_status sg_pr_weighted(sg_ctx* ctx, const float* tele, float* x_out) {
+  SG_GUARD(ctx);
+  try {
+    sg_status st = pr_weighted_forward(ctx, tele, x_out);
+    kprof_flush(ctx);
+    return st;
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_pr_adjoint(sg_ctx* ctx, const float* dl_dx, float* dl_dw, float* dl_dtele) {
+  SG_GUARD(ctx);
+  if (!dl_dx) return fail(ctx, SG_ERR_INVALID, "null dL/dx");
+  try {
+    sg_status st = pr_adjoint(ctx, dl_dx, false, dl_dw, dl_dtele);
+    kprof_flush(ctx);
+    return st;
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_pr_adjoint_device(sg_ctx* ctx, const float* d_dl_dx, float* dl_dw, float* dl_dtele) {
+  SG_GUARD(ctx);
+  if (!d_dl_dx) return fail(ctx, SG_ERR_INVALID, "null dL/dx");
+  try {
+    sg_status st = pr_adjoint(ctx, d_dl_dx, true, dl_dw, dl_dtele);
+    kprof_flush(ctx);
+    return st;
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_adjoint_info_get(sg_ctx* ctx, sg_adjoint_info* out) {
+  SG_GUARD(ctx);
+  if (!out) return fail(ctx, SG_ERR_INVALID, "null output");
+  return adjoint_info(ctx, out);
+}
+
+sg_status sg_adjoint_values(sg_ctx* ctx, float* x, float* lambda) {
+  SG_GUARD(ctx);
+  try {
+    return adjoint_values(ctx, x, lambda);
+  }
+  SG_CATCH(ctx)
 }
 
 }  // extern "C"

@@ -26,23 +26,33 @@ struct DevCSR {
   uint64_t* pool_tail = nullptr;  // device counter: first free slot
 };
 
+// Edge-balanced work lists over one direction of adjacency: vertices with
+// degree > 0, the exclusive prefix of their 4-edge quads, the owner of the
+// first quad of each kPullTileQuads tile and the vertices whose quads span
+// tiles.  Rebuilt when the adjacency changes.
+struct PullLists {
+  uint32_t* nz = nullptr;       // [n]
+  uint64_t* qoff = nullptr;     // [n + 1]
+  uint32_t nz_count = 0;
+  uint64_t quads = 0;
+  uint32_t* tile_v0 = nullptr;  // owner (index into nz) of each tile's first quad
+  uint64_t ntiles = 0;
+  uint64_t tile_cap = 0;
+  uint32_t* bnd = nullptr;      // vertices whose quads span tiles
+  uint32_t bnd_count = 0;
+  uint32_t n_alloc = 0;
+  uint64_t gen = ~0ull;         // graph generation the lists describe
+};
+
 struct DevGraph {
   uint32_t n = 0;
   uint64_t m = 0;  // live edges (host mirror of the device count)
   bool weighted = false;
   bool valid = false;
   DevCSR out, in;
-  // Edge-balanced work lists over the in-CSR: vertices with in-degree > 0 and
-  // the exclusive prefix of their 4-edge quads.  Rebuilt after each update.
-  uint32_t* in_nz = nullptr;     // [n]
-  uint64_t* in_qoff = nullptr;   // [n + 1]
-  uint32_t in_nz_count = 0;
-  uint64_t in_quads = 0;
-  uint32_t* in_tile_v0 = nullptr;  // owner (index into in_nz) of each tile's first quad
-  uint64_t in_ntiles = 0;
-  uint64_t tile_cap = 0;
-  uint32_t* in_bnd = nullptr;      // vertices whose quads span tiles
-  uint32_t in_bnd_count = 0;
+  PullLists in_wl;   // over the in-CSR (PageRank pulls); rebuilt after each update
+  PullLists out_wl;  // over the out-CSR (adjoint pulls); built on demand
+  uint64_t gen = 0;  // bumped whenever the adjacency changes
 };
 
 // Normalized update batch kept on the device between apply and IncEval.
@@ -81,6 +91,7 @@ struct DevBatch {
 
 struct PrState {
   bool valid = false;
+  uint32_t n_alloc = 0;
   float* x = nullptr;      // values_
   float* delta = nullptr;  // deltas_
   float* acc = nullptr;    // per-round incoming sums (pull)
@@ -149,6 +160,8 @@ struct sg_ctx {
   size_t cub_tmp_bytes = 0;
   int num_sms = 0;
   void* summary = nullptr;  // summary.cu: summarized graph (compress = 1)
+  void* batch_state = nullptr;  // batch.cu: batched PPR / SSSP queries
+  void* adjoint_state = nullptr;  // adjoint.cu: weighted PageRank + adjoint
 };
 
 namespace sg {
@@ -201,6 +214,12 @@ sg_status graph_build_from_sorted_keys(sg_ctx* ctx, uint32_t n, uint64_t m,
                                        uint64_t* d_keys, float* d_w,
                                        bool weighted);
 sg_status graph_rebuild_worklists(sg_ctx* ctx);
+// out-CSR work lists for pulls along out-edges (built when stale)
+sg_status graph_out_worklists(sg_ctx* ctx);
+void pull_lists_free(PullLists& L);
+// packed out-CSR with rows sorted by neighbour (the order of
+// sg_graph_download_csr), into caller-owned device arrays
+sg_status packed_sorted_out(sg_ctx* ctx, uint64_t* d_rp, uint32_t* d_col);
 sg_status apply_updates_device(sg_ctx* ctx, uint64_t count,
                                const sg_update* upd, bool on_device);
 
@@ -208,6 +227,28 @@ sg_status apply_updates_device(sg_ctx* ctx, uint64_t count,
 sg_status pr_free(sg_ctx* ctx);
 sg_status pr_alloc(sg_ctx* ctx);
 sg_status pr_run(sg_ctx* ctx, bool inc);
+// buffers and direction of one delta-PageRank run (pagerank.cu)
+struct PrBufs {
+  float* x;
+  float* delta;
+  float* pv0;      // [n]
+  float* pvb;      // [2n]
+  uint32_t* misc;  // 8 words
+  double* res;     // 4 words
+  unsigned long long* cnt;  // 4 words
+};
+struct PrRunSpec {
+  PrBufs buf;
+  const PullLists* lists;
+  const DevCSR* csr;          // pulled direction
+  bool weighted;              // gather push value x edge weight
+  const uint32_t* scale_deg;  // push value d*delta/deg[v]; null: d*delta
+  double tau;                 // residual test (sum |delta| < tau)
+};
+sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R);
+// personalized PageRank of one query: teleport mass (1-d) spread uniformly
+// over the seeds (device array), plain rounds to the residual test
+sg_status pr_run_personalized(sg_ctx* ctx, const uint32_t* d_seeds, uint32_t n_seeds);
 // called by the applier for each affected source vertex group
 struct PrAmendArgs {
   float* x;
@@ -232,6 +273,21 @@ struct SsspAmendArgs {
 SsspAmendArgs sssp_amend_args(sg_ctx* ctx);
 sg_status sssp_collect_adds(sg_ctx* ctx);
 sg_status sssp_download(sg_ctx* ctx, double* out);
+
+// adjoint.cu
+sg_status adjoint_free(sg_ctx* ctx);
+sg_status pr_weighted_forward(sg_ctx* ctx, const float* tele_host, float* x_out);
+sg_status pr_adjoint(sg_ctx* ctx, const float* dl_dx, bool on_device, float* dl_dw, float* dl_dt);
+sg_status adjoint_info(sg_ctx* ctx, sg_adjoint_info* out);
+sg_status adjoint_values(sg_ctx* ctx, float* x, float* lam);
+
+// batch.cu
+sg_status batch_free(sg_ctx* ctx);
+sg_status batch_run(sg_ctx* ctx, const sg_batch_spec* spec, float* ppr_out, double* sssp_out,
+                    bool retune);
+sg_status batch_info(sg_ctx* ctx, sg_batch_info* out);
+sg_status batch_query_stats(sg_ctx* ctx, int32_t* rounds, double* residual);
+sg_status batch_device_outputs(sg_ctx* ctx, const float** ppr, const double** sssp);
 
 // summary.cu
 sg_status summary_free(sg_ctx* ctx);

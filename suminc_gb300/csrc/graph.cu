@@ -187,11 +187,11 @@ sg_status graph_free(sg_ctx* ctx) {
   DevGraph& g = ctx->g;
   csr_free(g.out);
   csr_free(g.in);
-  dfree(g.in_nz);
-  dfree(g.in_qoff);
-  dfree(g.in_tile_v0);
-  dfree(g.in_bnd);
+  pull_lists_free(g.in_wl);
+  pull_lists_free(g.out_wl);
+  const uint64_t gen = g.gen;  // generations keep growing across graphs
   g = DevGraph();
+  g.gen = gen + 1;
   return SG_OK;
 }
 
@@ -258,9 +258,6 @@ sg_status graph_build_from_sorted_keys(sg_ctx* ctx, uint32_t n, uint64_t m,
   SG_TRY(build_direction(ctx, g.in, n, m, rk2, rw2, weighted));
   dfree(rk2);
   dfree(rw2);
-  SG_TRY(dalloc(ctx, &g.in_nz, n));
-  SG_TRY(dalloc(ctx, &g.in_qoff, (uint64_t)n + 1));
-  SG_TRY(dalloc(ctx, &g.in_bnd, n));
   g.valid = true;
   return graph_rebuild_worklists(ctx);
 }
@@ -327,36 +324,64 @@ __global__ void k_bnd_flags(const uint64_t* __restrict__ qoff, uint32_t nz_count
     f[i] = (qoff[i] / kPullTileQuads) != ((qoff[i + 1] - 1) / kPullTileQuads);
 }
 
-sg_status graph_rebuild_worklists(sg_ctx* ctx) {
+void pull_lists_free(PullLists& L) {
+  dfree(L.nz);
+  dfree(L.qoff);
+  dfree(L.tile_v0);
+  dfree(L.bnd);
+  L = PullLists();
+}
+
+static sg_status build_lists(sg_ctx* ctx, const DevCSR& c, PullLists& L) {
   DevGraph& g = ctx->g;
-  SG_TRY(worklist_dir(ctx, g.in, g.in_nz, g.in_qoff, &g.in_nz_count, &g.in_quads));
-  g.in_ntiles = (g.in_quads + kPullTileQuads - 1) / kPullTileQuads;
-  if (g.in_ntiles + 1 > g.tile_cap) {
-    dfree(g.in_tile_v0);
-    g.tile_cap = g.in_ntiles + g.in_ntiles / 8 + 1024;
-    SG_TRY(dalloc(ctx, &g.in_tile_v0, g.tile_cap));
+  const uint32_t n = g.n;
+  if (!L.nz || L.n_alloc != n) {
+    pull_lists_free(L);
+    SG_TRY(dalloc(ctx, &L.nz, n));
+    SG_TRY(dalloc(ctx, &L.qoff, (uint64_t)n + 1));
+    SG_TRY(dalloc(ctx, &L.bnd, n));
+    L.n_alloc = n;
   }
-  if (g.in_ntiles)
-    k_tile_v0<<<grid_for(g.in_ntiles, 256), 256, 0, ctx->stream>>>(g.in_qoff, g.in_nz_count,
-                                                                    g.in_ntiles, g.in_tile_v0);
-  // boundary vertices: in_nz entries whose quads cross a tile edge
+  SG_TRY(worklist_dir(ctx, c, L.nz, L.qoff, &L.nz_count, &L.quads));
+  L.ntiles = (L.quads + kPullTileQuads - 1) / kPullTileQuads;
+  if (L.ntiles + 1 > L.tile_cap) {
+    dfree(L.tile_v0);
+    L.tile_cap = L.ntiles + L.ntiles / 8 + 1024;
+    SG_TRY(dalloc(ctx, &L.tile_v0, L.tile_cap));
+  }
+  if (L.ntiles)
+    k_tile_v0<<<grid_for(L.ntiles, 256), 256, 0, ctx->stream>>>(L.qoff, L.nz_count, L.ntiles,
+                                                                 L.tile_v0);
+  // boundary vertices: nz entries whose quads cross a tile edge
   uint8_t* flags = nullptr;
   uint64_t* cnt = nullptr;
-  SG_TRY(dalloc(ctx, &flags, std::max<uint32_t>(g.in_nz_count, 1)));
+  SG_TRY(dalloc(ctx, &flags, std::max<uint32_t>(L.nz_count, 1)));
   SG_TRY(dalloc(ctx, &cnt, 1));
   uint64_t h = 0;
-  if (g.in_nz_count) {
-    k_bnd_flags<<<grid_for(g.in_nz_count, 256), 256, 0, ctx->stream>>>(g.in_qoff, g.in_nz_count,
-                                                                        flags);
-    SG_TRY(select_flagged(ctx, g.in_nz, flags, g.in_bnd, cnt, g.in_nz_count));
+  if (L.nz_count) {
+    k_bnd_flags<<<grid_for(L.nz_count, 256), 256, 0, ctx->stream>>>(L.qoff, L.nz_count, flags);
+    SG_TRY(select_flagged(ctx, L.nz, flags, L.bnd, cnt, L.nz_count));
     SG_CUDA(ctx, cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, ctx->stream));
   }
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  g.in_bnd_count = (uint32_t)h;
+  L.bnd_count = (uint32_t)h;
+  L.gen = g.gen;
   dfree(flags);
   dfree(cnt);
   count_launch(ctx, 8);
   return SG_OK;
+}
+
+sg_status graph_rebuild_worklists(sg_ctx* ctx) {
+  DevGraph& g = ctx->g;
+  g.gen++;
+  return build_lists(ctx, g.in, g.in_wl);
+}
+
+sg_status graph_out_worklists(sg_ctx* ctx) {
+  DevGraph& g = ctx->g;
+  if (g.out_wl.nz && g.out_wl.gen == g.gen && g.out_wl.n_alloc == g.n) return SG_OK;
+  return build_lists(ctx, g.out, g.out_wl);
 }
 
 // ------------------------------------------------------------ R-MAT
@@ -526,6 +551,31 @@ __global__ void k_deg64(const uint32_t* __restrict__ deg, uint32_t n, uint64_t* 
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i <= n;
        i += (uint64_t)gridDim.x * blockDim.x)
     o[i] = i < n ? deg[i] : 0;
+}
+
+sg_status packed_sorted_out(sg_ctx* ctx, uint64_t* d_rp, uint32_t* d_col) {
+  DevGraph& g = ctx->g;
+  const uint32_t n = g.n;
+  const uint64_t m = g.m;
+  uint64_t* d64 = nullptr;
+  uint32_t* c1 = nullptr;
+  SG_TRY(dalloc(ctx, &d64, (uint64_t)n + 1));
+  SG_TRY(dalloc(ctx, &c1, m));
+  k_deg64<<<grid_for((uint64_t)n + 1, 256), 256, 0, ctx->stream>>>(g.out.deg, n, d64);
+  SG_TRY(exclusive_sum(ctx, d64, d_rp, (uint64_t)n + 1));
+  k_pack_rows<<<grid_for((uint64_t)n * 32, 256), 256, 0, ctx->stream>>>(g.out, n, d_rp, c1, nullptr);
+  size_t bytes = 0;
+  SG_CUDA(ctx, cub::DeviceSegmentedSort::SortKeys(nullptr, bytes, c1, d_col, (int64_t)m,
+                                                  (int64_t)n, d_rp, d_rp + 1, ctx->stream));
+  SG_TRY(ensure_cub_tmp(ctx, bytes));
+  bytes = ctx->cub_tmp_bytes;
+  SG_CUDA(ctx, cub::DeviceSegmentedSort::SortKeys(ctx->cub_tmp, bytes, c1, d_col, (int64_t)m,
+                                                  (int64_t)n, d_rp, d_rp + 1, ctx->stream));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  dfree(d64);
+  dfree(c1);
+  count_launch(ctx, 4);
+  return SG_OK;
 }
 
 sg_status download_csr(sg_ctx* ctx, uint64_t* row_ptr, uint32_t* col, float* w) {

@@ -49,8 +49,9 @@ struct PrArgs {
   double tau;       // threshold
   int max_rounds;
   uint64_t live_edges;
-  const uint32_t* out_deg;
-  const uint32_t* in_deg;
+  const uint32_t* scale_deg;  // push value d*delta/deg (PageRank); null: d*delta,
+                              // the edge weights are applied in the gather
+  const uint32_t* pull_deg;   // live degree of the pulled direction
   float* x;
   float* delta;
   float* pv0;       // push values of the first round
@@ -67,8 +68,12 @@ __device__ __forceinline__ uint32_t activate(const PrArgs& A, uint32_t v, float 
   if (fabsf(dl) > A.thr_v) {
     A.x[v] += dl;
     A.delta[v] = 0.f;
-    const uint32_t od = A.out_deg[v];
-    pv_next[v] = od > 0 ? A.damping * dl / (float)od : 0.f;
+    if (A.scale_deg) {
+      const uint32_t od = A.scale_deg[v];
+      pv_next[v] = od > 0 ? A.damping * dl / (float)od : 0.f;
+    } else {
+      pv_next[v] = A.damping * dl;
+    }
     return 1;
   }
   A.delta[v] = dl;
@@ -87,7 +92,7 @@ __global__ void __launch_bounds__(VT) k_pr_vertex(PrArgs A) {
     res += r;
     // vertices without in-edges never change again: their leftover delta is
     // a constant part of every later residual
-    if (A.in_deg[v] == 0) res0 += fabs((double)A.delta[v]);
+    if (A.pull_deg[v] == 0) res0 += fabs((double)A.delta[v]);
     A.pvb[0][v] = 0.f;
     A.pvb[1][v] = 0.f;
   }
@@ -113,12 +118,15 @@ struct PullArgs {
   uint32_t nz_count;
   uint64_t quads;
   uint64_t ntiles;
-  const uint64_t* off;     // in-CSR
+  const uint64_t* off;     // the pulled CSR (in-CSR for PageRank)
   const uint32_t* col;
+  const float* w;          // its weights (weighted pulls only)
 };
 
 // pull number p reads pvb[p & 1] (or pv0 for p == 0) and writes the next
-// push values into pvb[(p + 1) & 1]
+// push values into pvb[(p + 1) & 1].  W: multiply each gathered push value
+// by the edge weight (weighted PageRank and its adjoint).
+template <bool W>
 __global__ void __launch_bounds__(PT_THREADS) k_pr_pull(PrArgs A, PullArgs P, int p) {
   __shared__ uint64_t sq[PT_TILE + 2];
   __shared__ uint32_t snz[PT_TILE + 1];
@@ -158,7 +166,7 @@ __global__ void __launch_bounds__(PT_THREADS) k_pr_pull(PrArgs A, PullArgs P, in
       uint32_t v = snz[i];
       uint64_t base = P.off[v];
       uint64_t qbeg = sq[i], qend = sq[i + 1];
-      uint32_t deg = A.in_deg[v];
+      uint32_t deg = A.pull_deg[v];
       float acc = 0.f;
       for (uint64_t q = qa; q < qb; ++q) {
         if (q >= qend) {
@@ -171,15 +179,24 @@ __global__ void __launch_bounds__(PT_THREADS) k_pr_pull(PrArgs A, PullArgs P, in
           base = P.off[v];
           qbeg = sq[i];
           qend = sq[i + 1];
-          deg = A.in_deg[v];
+          deg = A.pull_deg[v];
         }
         const uint32_t k = (uint32_t)(q - qbeg) * 4;
         const uint4 c4 = *reinterpret_cast<const uint4*>(P.col + base + k);
-        float s = pv[c4.x];  // the last quad of a vertex may be partial
-        if (k + 1 < deg) s += pv[c4.y];
-        if (k + 2 < deg) s += pv[c4.z];
-        if (k + 3 < deg) s += pv[c4.w];
-        acc += s;
+        if (W) {
+          const float4 w4 = *reinterpret_cast<const float4*>(P.w + base + k);
+          float s = pv[c4.x] * w4.x;  // the last quad of a vertex may be partial
+          if (k + 1 < deg) s += pv[c4.y] * w4.y;
+          if (k + 2 < deg) s += pv[c4.z] * w4.z;
+          if (k + 3 < deg) s += pv[c4.w] * w4.w;
+          acc += s;
+        } else {
+          float s = pv[c4.x];  // the last quad of a vertex may be partial
+          if (k + 1 < deg) s += pv[c4.y];
+          if (k + 2 < deg) s += pv[c4.z];
+          if (k + 3 < deg) s += pv[c4.w];
+          acc += s;
+        }
       }
       if (acc != 0.f) atomicAdd(&sacc[i], acc);
     }
@@ -273,6 +290,12 @@ __global__ void __launch_bounds__(VT) k_pr_residual(uint32_t n, const float* del
   if (threadIdx.x == 0) atomicAdd(&res[R_ACC], b);
 }
 
+__global__ void k_pr_seed(const uint32_t* __restrict__ seeds, uint32_t cnt, float* delta,
+                          float mass) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+    atomicAdd(delta + seeds[i], mass);
+}
+
 sg_status pr_free(sg_ctx* ctx) {
   PrState& s = ctx->pr;
   dfree(s.x); dfree(s.delta); dfree(s.acc); dfree(s.pv); dfree(s.frontier);
@@ -284,6 +307,10 @@ sg_status pr_free(sg_ctx* ctx) {
 sg_status pr_alloc(sg_ctx* ctx) {
   PrState& s = ctx->pr;
   const uint32_t n = std::max(ctx->g.n, summary_rows(ctx));  // mirror rows too
+  if (s.x && s.n_alloc == n) {  // same size: keep the buffers
+    s.valid = false;
+    return SG_OK;
+  }
   pr_free(ctx);
   SG_TRY(dalloc(ctx, &s.x, n));
   SG_TRY(dalloc(ctx, &s.delta, n));
@@ -292,6 +319,7 @@ sg_status pr_alloc(sg_ctx* ctx) {
   SG_TRY(dalloc(ctx, &s.d_misc, M_WORDS));
   SG_TRY(dalloc(ctx, &s.d_res, R_WORDS));
   SG_TRY(dalloc(ctx, &s.d_cnt, C_WORDS));
+  s.n_alloc = n;
   return SG_OK;
 }
 
@@ -303,6 +331,8 @@ PrAmendArgs pr_amend_args(sg_ctx* ctx) {
   a.damping = (float)ctx->opt.damping;
   return a;
 }
+
+static sg_status pr_rounds(sg_ctx* ctx);
 
 // Runs rounds until the residual test passes (or the round cap).  inc=false
 // starts from init_v / init_c; inc=true continues from the amended state.
@@ -319,42 +349,68 @@ sg_status pr_run(sg_ctx* ctx, bool inc) {
   } else if (!s.valid) {
     return fail(ctx, SG_ERR_STATE, "PageRank IncEval before PEval");
   }
-  SG_CUDA(ctx, cudaMemsetAsync(s.d_misc, 0, sizeof(uint32_t) * M_WORDS, st));
-  SG_CUDA(ctx, cudaMemsetAsync(s.d_res, 0, sizeof(double) * R_WORDS, st));
-  SG_CUDA(ctx, cudaMemsetAsync(s.d_cnt, 0, sizeof(unsigned long long) * C_WORDS, st));
+  return pr_rounds(ctx);
+}
+
+// Personalized PageRank (ppr/ppr.h's teleport to a seed set): x = 0, delta =
+// (1-d)/|seeds| on the seeds, then the same rounds.
+sg_status pr_run_personalized(sg_ctx* ctx, const uint32_t* d_seeds, uint32_t n_seeds) {
+  DevGraph& g = ctx->g;
+  PrState& s = ctx->pr;
+  if (!g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
+  if (n_seeds == 0) return fail(ctx, SG_ERR_INVALID, "personalized PageRank needs seeds");
+  cudaStream_t st = ctx->stream;
+  if (!s.x) SG_TRY(pr_alloc(ctx));
+  k_pr_init<<<grid_for(g.n, 256), 256, 0, st>>>(g.n, s.x, s.delta, 0.f);
+  k_pr_seed<<<grid_for(n_seeds, 256), 256, 0, st>>>(
+      d_seeds, n_seeds, s.delta, (float)((1.0 - ctx->opt.damping) / (double)n_seeds));
+  count_launch(ctx, 2);
+  return pr_rounds(ctx);
+}
+
+sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R) {
+  DevGraph& g = ctx->g;
+  cudaStream_t st = ctx->stream;
+  const PrBufs& s = R.buf;
+  const PullLists& L = *R.lists;
+  SG_CUDA(ctx, cudaMemsetAsync(s.misc, 0, sizeof(uint32_t) * M_WORDS, st));
+  SG_CUDA(ctx, cudaMemsetAsync(s.res, 0, sizeof(double) * R_WORDS, st));
+  SG_CUDA(ctx, cudaMemsetAsync(s.cnt, 0, sizeof(unsigned long long) * C_WORDS, st));
 
   PrArgs A;
   A.n = g.n;
   A.damping = (float)ctx->opt.damping;
-  A.thr_v = (float)(ctx->opt.termcheck_threshold / (double)g.n);
-  A.tau = ctx->opt.termcheck_threshold;
+  A.thr_v = (float)(R.tau / (double)g.n);
+  A.tau = R.tau;
   A.max_rounds = ctx->opt.max_rounds > 0 ? ctx->opt.max_rounds : 1000;
   A.live_edges = g.m;
-  A.out_deg = g.out.deg;
-  A.in_deg = g.in.deg;
+  A.scale_deg = R.scale_deg;
+  A.pull_deg = R.csr->deg;
   A.x = s.x;
   A.delta = s.delta;
-  A.pv0 = s.acc;
-  A.pvb[0] = s.pv;
-  A.pvb[1] = s.pv + g.n;
-  A.misc = s.d_misc;
-  A.res = s.d_res;
-  A.cnt = (unsigned long long*)s.d_cnt;
+  A.pv0 = s.pv0;
+  A.pvb[0] = s.pvb;
+  A.pvb[1] = s.pvb + g.n;
+  A.misc = s.misc;
+  A.res = s.res;
+  A.cnt = s.cnt;
 
   PullArgs P;
-  P.nz = g.in_nz;
-  P.qoff = g.in_qoff;
-  P.tile_v0 = g.in_tile_v0;
-  P.nz_count = g.in_nz_count;
-  P.quads = g.in_quads;
-  P.ntiles = g.in_ntiles;
-  P.off = g.in.off;
-  P.col = g.in.col;
+  P.nz = L.nz;
+  P.qoff = L.qoff;
+  P.tile_v0 = L.tile_v0;
+  P.nz_count = L.nz_count;
+  P.quads = L.quads;
+  P.ntiles = L.ntiles;
+  P.off = R.csr->off;
+  P.col = R.csr->col;
+  P.w = R.weighted ? R.csr->w : nullptr;
 
   const unsigned vblocks = grid_for(g.n, VT, ctx->num_sms * 8);
   const unsigned pblocks =
       (unsigned)std::min<uint64_t>(std::max<uint64_t>(P.ntiles, 1), (uint64_t)ctx->num_sms * 8);
-  const unsigned fblocks = grid_for(std::max<uint32_t>(g.in_bnd_count, 1), VT, ctx->num_sms * 2);
+  const unsigned fblocks = grid_for(std::max<uint32_t>(L.bnd_count, 1), VT, ctx->num_sms * 2);
+  const int kpull = R.weighted ? SG_K_ADJOINT : SG_K_PR_PULL;
 
   SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
   kprof_begin(ctx);
@@ -362,39 +418,39 @@ sg_status pr_run(sg_ctx* ctx, bool inc) {
   kprof_end(ctx, SG_K_PR_VERTEX);
   uint32_t h_misc[M_WORDS] = {0};
   int pull = 0;
-  if (g.in_quads > 0) {
+  if (L.quads > 0) {
     // the first pull distributes the first round's activations
     const int chunk = 4;
     for (;;) {
       for (int r = 0; r < chunk; ++r, ++pull) {
         kprof_begin(ctx);
-        k_pr_pull<<<pblocks, PT_THREADS, 0, st>>>(A, P, pull);
-        kprof_end(ctx, SG_K_PR_PULL);
+        if (R.weighted) k_pr_pull<true><<<pblocks, PT_THREADS, 0, st>>>(A, P, pull);
+        else k_pr_pull<false><<<pblocks, PT_THREADS, 0, st>>>(A, P, pull);
+        kprof_end(ctx, kpull);
         kprof_begin(ctx);
-        k_pr_fixup<<<fblocks, VT, 0, st>>>(A, g.in_bnd, g.in_bnd_count, pull);
+        k_pr_fixup<<<fblocks, VT, 0, st>>>(A, L.bnd, L.bnd_count, pull);
         kprof_end(ctx, SG_K_PR_VERTEX);
       }
       SG_CUDA(ctx, cudaGetLastError());
-      SG_CUDA(ctx, cudaMemcpyAsync(h_misc, s.d_misc, sizeof(h_misc), cudaMemcpyDeviceToHost, st));
+      SG_CUDA(ctx, cudaMemcpyAsync(h_misc, s.misc, sizeof(h_misc), cudaMemcpyDeviceToHost, st));
       SG_CUDA(ctx, cudaStreamSynchronize(st));
       if (h_misc[M_DONE]) break;
       if (pull > 2 * A.max_rounds + 64) break;  // host-side guard
     }
   }
   // final residual over every vertex
-  SG_CUDA(ctx, cudaMemsetAsync(s.d_res, 0, sizeof(double), st));
-  k_pr_residual<<<vblocks, VT, 0, st>>>(g.n, s.delta, s.d_res);
+  SG_CUDA(ctx, cudaMemsetAsync(s.res, 0, sizeof(double), st));
+  k_pr_residual<<<vblocks, VT, 0, st>>>(g.n, s.delta, s.res);
   count_launch(ctx);
   SG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
   double h_res[R_WORDS];
   unsigned long long h_cnt[C_WORDS];
-  SG_CUDA(ctx, cudaMemcpyAsync(h_res, s.d_res, sizeof(h_res), cudaMemcpyDeviceToHost, st));
-  SG_CUDA(ctx, cudaMemcpyAsync(h_cnt, s.d_cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
-  SG_CUDA(ctx, cudaMemcpyAsync(h_misc, s.d_misc, sizeof(h_misc), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaMemcpyAsync(h_res, s.res, sizeof(h_res), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaMemcpyAsync(h_cnt, s.cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaMemcpyAsync(h_misc, s.misc, sizeof(h_misc), cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-  s.valid = true;
   ctx->stats.rounds = (int32_t)h_misc[M_ROUNDS] + 1;
   ctx->stats.converged = h_misc[M_NOTCONV] ? 0 : 1;
   ctx->stats.residual = h_res[R_ACC];
@@ -407,6 +463,27 @@ sg_status pr_run(sg_ctx* ctx, bool inc) {
   if (h_misc[M_NOTCONV])
     return fail(ctx, SG_ERR_NOT_CONVERGED, "PageRank reached the round cap");
   return SG_OK;
+}
+
+static sg_status pr_rounds(sg_ctx* ctx) {
+  DevGraph& g = ctx->g;
+  PrState& s = ctx->pr;
+  PrRunSpec R;
+  R.buf.x = s.x;
+  R.buf.delta = s.delta;
+  R.buf.pv0 = s.acc;
+  R.buf.pvb = s.pv;
+  R.buf.misc = s.d_misc;
+  R.buf.res = s.d_res;
+  R.buf.cnt = (unsigned long long*)s.d_cnt;
+  R.lists = &g.in_wl;
+  R.csr = &g.in;
+  R.weighted = false;
+  R.scale_deg = g.out.deg;
+  R.tau = ctx->opt.termcheck_threshold;
+  const sg_status st = pr_rounds_ex(ctx, R);
+  if (st == SG_OK || st == SG_ERR_NOT_CONVERGED) s.valid = true;
+  return st;
 }
 
 }  // namespace sg

@@ -365,6 +365,13 @@ sg_status sssp_free(sg_ctx* ctx) {
 static sg_status sssp_alloc(sg_ctx* ctx) {
   SsspState& s = ctx->sp;
   const uint32_t n = ctx->g.n;
+  if (s.dist && s.n_alloc == n && s.far_cap >= ctx->g.m + (uint64_t)n + 1024) {
+    // same graph size: keep the buffers, drop the result
+    s.valid = false;
+    s.has_pending = false;
+    s.padd_bound = 0;
+    return SG_OK;
+  }
   sssp_free(ctx);
   SG_TRY(dalloc(ctx, &s.dist, n));
   SG_TRY(dalloc(ctx, &s.parent, n));
