@@ -56,9 +56,10 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-rounds", type=int, default=3)
     p.add_argument("--no-clocks", action="store_true")
-    p.add_argument("--workload", default="inceval", choices=["inceval", "batched"],
+    p.add_argument("--workload", default="inceval", choices=["inceval", "batched", "adjoint"],
                    help="inceval: the headline IncEval line; batched: 256 PPR + 64 SSSP "
-                        "queries in one persistent launch vs looping the single-query path")
+                        "queries in one persistent launch vs looping the single-query path; "
+                        "adjoint: weighted PageRank forward vs forward + adjoint")
     p.add_argument("--batch-scale", type=int, default=22)
     p.add_argument("--ppr-queries", type=int, default=256)
     p.add_argument("--sssp-sources", type=int, default=64)
@@ -512,14 +513,179 @@ def run_batched(args, D: Dist):
     return result
 
 
+def run_adjoint(args, D: Dist):
+    """Weighted PageRank forward alone vs forward + adjoint (gradients wrt
+    every edge weight and the teleport vector), R-MAT scale 22 with
+    column-normalised float weights, loss over 10,000 targets."""
+    import torch
+    import oracle
+    import suminc_gb300 as sg
+
+    dev = D.local
+    n = 1 << args.batch_scale
+    E = n * args.edge_factor
+    ctx = sg.Context(dev)
+    ctx.generate_rmat(args.batch_scale, E, seed=args.seed, weight_kind=2, wlo=0.1, whi=1.0)
+    ctx.normalize_weights()
+    rng = np.random.default_rng(args.seed + 11)
+    tgt = rng.choice(n, size=10000, replace=False)
+    y = rng.uniform(0.0, 2.0 / n, size=10000).astype(np.float32)
+    tele = np.full(n, 1.0 / n, np.float32)
+    x_pin = torch.empty(n, dtype=torch.float32).pin_memory()
+    g_pin = torch.empty(n, dtype=torch.float32).pin_memory()
+    dw_pin = torch.empty(E, dtype=torch.float32).pin_memory()
+    dt_pin = torch.empty(n, dtype=torch.float32).pin_memory()
+    import ctypes as C
+    lib, h = ctx._lib, ctx._h
+
+    def fwd():
+        sg._check(lib.sg_pr_weighted(h, tele.ctypes.data_as(C.c_void_p),
+                                     C.c_void_p(x_pin.data_ptr())), ctx, "sg_pr_weighted")
+
+    def bwd():
+        x = x_pin.numpy()
+        g = g_pin.numpy()
+        g[:] = 0.0
+        g[tgt] = x[tgt] - y
+        sg._check(lib.sg_pr_adjoint(h, C.c_void_p(g_pin.data_ptr()), C.c_void_p(dw_pin.data_ptr()),
+                                    C.c_void_p(dt_pin.data_ptr())), ctx, "sg_pr_adjoint")
+
+    K, W = args.steps, args.warmup
+    for _ in range(W):
+        fwd()
+        bwd()
+    clocks = Clocks(dev, not args.no_clocks)
+    ctx.synchronize()
+    ctx.record_event(0)
+    f_edges = 0
+    f_dev_ms = 0.0
+    for _ in range(K):
+        fwd()
+        ai = ctx.adjoint_info()
+        f_edges += ai["forward_edges"]
+        f_dev_ms += ai["forward_ms"]
+    ctx.record_event(1)
+    ctx.synchronize()
+    t_f = ctx.elapsed_ms(0, 1)
+    ctx.record_event(2)
+    fb_edges = 0
+    a_dev_ms = 0.0
+    for _ in range(K):
+        fwd()
+        bwd()
+        ai = ctx.adjoint_info()
+        fb_edges += ai["forward_edges"] + ai["adjoint_edges"] + ai["gradient_edges"]
+        a_dev_ms += ai["adjoint_ms"]
+    ctx.record_event(3)
+    ctx.synchronize()
+    t_fb = ctx.elapsed_ms(2, 3)
+    clk = clocks.stop()
+    info = ctx.adjoint_info()
+    # per-kernel device time of the adjoint's weighted pull (profiled run)
+    ctx.set_profile(0xFF)
+    ctx.reset_stats()
+    fwd()
+    bwd()
+    st = ctx.stats()
+    ctx.set_profile(0)
+    kms, kl = st["kernel_ms"], st["kernel_launches"]
+    ctx.close()
+
+    # accuracy on a scale-12 induced subgraph: the first 4096 vertices, weights
+    # re-normalised; GPU adjoint vs the FP64 transposed solve and central
+    # differences on 64 random edges
+    sub = 4096
+    with sg.Context(dev) as c2:
+        c2.generate_rmat(args.batch_scale, E, seed=args.seed, weight_kind=2, wlo=0.1, whi=1.0)
+        rp, col, w = c2.download_csr()
+    keep_rows = rp[: sub + 1]
+    cols = col[: int(keep_rows[-1])]
+    ws = w[: int(keep_rows[-1])].astype(np.float64)
+    srcs = np.repeat(np.arange(sub), np.diff(keep_rows).astype(np.int64))
+    mask = cols < sub
+    srcs, cols, ws = srcs[mask], cols[mask], ws[mask]
+    srp = np.zeros(sub + 1, np.uint64)
+    np.add.at(srp, srcs + 1, 1)
+    srp = np.cumsum(srp).astype(np.uint64)
+    ssum = np.bincount(srcs, weights=ws, minlength=sub)
+    ws = ws / ssum[srcs]
+    stele = np.full(sub, 1.0 / sub)
+    srng = np.random.default_rng(3)
+    stgt = srng.choice(sub, size=1000, replace=False)
+    sy = srng.uniform(0.0, 2.0 / sub, size=1000)
+    with sg.Context(dev) as c3:
+        c3.load_csr(srp, cols.astype(np.uint32), ws.astype(np.float32))
+        xs = c3.pr_weighted(stele.astype(np.float32))
+        gs = np.zeros(sub)
+        gs[stgt] = xs[stgt] - sy
+        dws, dts = c3.pr_adjoint(gs.astype(np.float32))
+        _, lam32 = c3.adjoint_values()
+    w32 = ws.astype(np.float32).astype(np.float64)
+    lam64 = oracle.pr_adjoint_solve(srp, cols, w32, gs)
+    x64 = oracle.pr_fixed_point(srp, cols, w32, tele=stele)
+    dw64 = 0.85 * lam64[cols] * x64[srcs]
+    rel_lam = float(np.abs(lam32 - lam64).sum() / np.abs(lam64).sum())
+    rel_dw = float(np.abs(dws - dw64).sum() / np.abs(dw64).sum())
+    hstep = 1e-4
+    fd_err = []
+    for e in srng.choice(len(cols), size=64, replace=False):
+        wp = w32.copy(); wp[e] += hstep
+        wm = w32.copy(); wm[e] -= hstep
+        lp = 0.5 * np.sum((oracle.pr_fixed_point(srp, cols, wp, tele=stele, tol=1e-15)[stgt] - sy) ** 2)
+        lm = 0.5 * np.sum((oracle.pr_fixed_point(srp, cols, wm, tele=stele, tol=1e-15)[stgt] - sy) ** 2)
+        fd = (lp - lm) / (2 * hstep)
+        fd_err.append(abs(float(dws[e]) - fd) / max(abs(fd), 1e-30))
+
+    peak, peak_kind = measured_peaks()
+    # adjoint class = weighted pulls along out-edges (4 B neighbour + 4 B
+    # weight + 4 B push value per edge) + the gradient pass (4 B neighbour +
+    # 4 B lambda + 4 B dL/dw per edge; x_u once per row)
+    adj_pull_ms = kms.get("adjoint", 0.0)
+    adj_launches = kl.get("adjoint", 0)
+    adj_bytes = 12 * info["adjoint_edges"] + 12 * info["gradient_edges"]
+    achieved = adj_bytes / (adj_pull_ms * 1e-3) / 1e9 if adj_pull_ms else None
+    result = {
+        "metric": "PageRank adjoint: forward + backward vs forward alone",
+        "value": round(fb_edges / (t_fb * 1e-3) / 1e9, 4), "unit": "GTEPS",
+        "n_gpus": D.ws, "steps": K, "warmup": W, "ms_per_step": round(t_fb / K, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic R-MAT (seeded), float weights U[0.1, 1.0] column-normalised",
+        "config": {"workload": f"PageRank adjoint, R-MAT scale {args.batch_scale}",
+                   "vertices": n, "edges": E, "damping": 0.85, "loss_targets": 10000,
+                   "targets": "uniform, t_v ~ U[0, 2/N]", "termcheck_threshold": 1e-6,
+                   "adjoint_rel_tol": 1e-7, "parallelism": "single GPU",
+                   "l2": "graph larger than L2, no flush"},
+        "forward_ms": round(t_f / K, 3), "forward_backward_ms": round(t_fb / K, 3),
+        "backward_over_forward": round((t_fb - t_f) / t_f, 3),
+        "device_ms": {"forward": round(f_dev_ms / K, 3), "adjoint_and_gradients": round(a_dev_ms / K, 3)},
+        "rounds": {"forward": info["forward_rounds"], "adjoint": info["adjoint_rounds"]},
+        "accuracy_scale12_subgraph": {"lambda_rel_l1_vs_fp64": rel_lam, "dw_rel_l1_vs_fp64": rel_dw,
+                                      "fd_64_edges_max_rel_err": max(fd_err),
+                                      "fd_64_edges_median_rel_err": float(np.median(fd_err))},
+        "e2e": {"value": round(fb_edges / (t_fb * 1e-3) / 1e9, 4), "unit": "GTEPS",
+                "h2d_bytes_per_step": int(8 * n), "d2h_bytes_per_step": int(4 * n + 4 * E + 4 * n),
+                "ms_per_step": round(t_fb / K, 3)},
+        "gpu_launches": int(st["launches_total"]),
+        "roofline": {"bound": "hbm", "kernel": "k_pr_pull<weighted> (adjoint)",
+                     "achieved": round(achieved, 1) if achieved else None, "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "traffic": None,
+                     "avg_launch_ms": round(adj_pull_ms / adj_launches, 4) if adj_launches else None,
+                     "algorithmic_bytes": int(adj_bytes), "launches": int(adj_launches)},
+    }
+    if clk:
+        result["clocks"] = clk
+    return result
+
+
 def main():
     args = parse()
     D = Dist()
     if args.impl == "reference":
         run_reference(args, D)
         return
-    if args.workload == "batched":
-        result = run_batched(args, D)
+    if args.workload in ("batched", "adjoint"):
+        result = run_batched(args, D) if args.workload == "batched" else run_adjoint(args, D)
         if D.rank == 0:
             print(json.dumps(result), flush=True)
         return

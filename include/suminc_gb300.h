@@ -327,6 +327,10 @@ sg_status sg_batch_outputs_device(sg_ctx* ctx, const float** ppr,
  * gather, to the same residual test.  x_out: host float[n] or NULL. */
 sg_status sg_pr_weighted(sg_ctx* ctx, const float* tele, float* x_out);
 
+/* Column-normalises the weights: every edge weight w_uv is divided by the
+ * sum of u's out-edge weights (rows with weight sum 0 are left alone). */
+sg_status sg_graph_normalize_weights(sg_ctx* ctx);
+
 /* Adjoint of the last sg_pr_weighted on the current graph: given
  * dl_dx = dL/dx (host float[n]) solves lambda = dl_dx + d M^T lambda by the
  * transposed delta iteration (pulls along out-edges) to a residual below

@@ -84,7 +84,10 @@ def pr_amend(old, new, x, delta, damping=0.85):
 
 
 def pr_fixed_point(rp, col, w=None, damping=0.85, tele=None, tol=1e-12, max_iter=100000):
-    rp, col, w = _csr(rp, col, w)
+    """FP64 Jacobi solve of x = (1-d) t + d M x; unweighted: M[v][u] =
+    1/outdeg(u); weighted: M[v][u] = w_uv (taken in FP64)."""
+    rp, col, _ = _csr(rp, col)
+    w = None if w is None else np.ascontiguousarray(w, np.float64)
     n = len(rp) - 1
     x = np.zeros(n, np.float64)
     t = None if tele is None else np.ascontiguousarray(tele, np.float64)
@@ -93,7 +96,9 @@ def pr_fixed_point(rp, col, w=None, damping=0.85, tele=None, tol=1e-12, max_iter
 
 
 def pr_adjoint_solve(rp, col, w, g, damping=0.85, tol=1e-13, max_iter=100000):
-    rp, col, w = _csr(rp, col, w)
+    """FP64 solve of lambda = g + d M^T lambda (M[v][u] = w_uv)."""
+    rp, col, _ = _csr(rp, col)
+    w = np.ascontiguousarray(w, np.float64)
     n = len(rp) - 1
     lam = np.zeros(n, np.float64)
     g = np.ascontiguousarray(g, np.float64)

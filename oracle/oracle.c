@@ -38,13 +38,13 @@ static void atomic_add_f32(float* a, float b) {
   *a += b;
 }
 
-/* in-CSR (transpose) of an out-CSR; caller frees */
-static void transpose(uint32_t n, const uint64_t* rp, const uint32_t* col, const float* w,
-                      uint64_t** trp, uint32_t** tcol, float** tw) {
+/* in-CSR (transpose) of an out-CSR with FP64 weights; caller frees */
+static void transpose(uint32_t n, const uint64_t* rp, const uint32_t* col, const double* w,
+                      uint64_t** trp, uint32_t** tcol, double** tw) {
   const uint64_t m = rp[n];
   uint64_t* r = (uint64_t*)calloc((size_t)n + 1, sizeof(uint64_t));
   uint32_t* c = (uint32_t*)malloc(sizeof(uint32_t) * (m ? m : 1));
-  float* ww = w ? (float*)malloc(sizeof(float) * (m ? m : 1)) : NULL;
+  double* ww = w ? (double*)malloc(sizeof(double) * (m ? m : 1)) : NULL;
   for (uint64_t e = 0; e < m; ++e) r[col[e] + 1]++;
   for (uint32_t v = 0; v < n; ++v) r[v + 1] += r[v];
   uint64_t* pos = (uint64_t*)malloc(sizeof(uint64_t) * ((size_t)n + 1));
@@ -159,11 +159,11 @@ void or_pr_amend(uint32_t n, const uint64_t* rp_old, const uint32_t* col_old,
 
 /* x = (1-d) * t + d * P^T x, P_uv = 1/outdeg(u) (or w_uv when w != NULL);
  * t = uniform 1/N when tele == NULL.  Returns iterations. */
-int or_pr_fixed_point(uint32_t n, const uint64_t* rp, const uint32_t* col, const float* w,
+int or_pr_fixed_point(uint32_t n, const uint64_t* rp, const uint32_t* col, const double* w,
                       double damping, const double* tele, double tol, int max_iter, double* x) {
   uint64_t* trp;
   uint32_t* tcol;
-  float* tw = NULL;
+  double* tw = NULL;
   transpose(n, rp, col, w, &trp, &tcol, w ? &tw : NULL);
   double* y = (double*)malloc(sizeof(double) * n);
   double* pv = (double*)malloc(sizeof(double) * n);
@@ -181,7 +181,7 @@ int or_pr_fixed_point(uint32_t n, const uint64_t* rp, const uint32_t* col, const
       double s = tele ? (1.0 - damping) * tele[v] : (1.0 - damping) / (double)n;
       for (uint64_t e = trp[v]; e < trp[v + 1]; ++e) {
         const uint32_t u = tcol[e];
-        if (w) s += pv[u] * (double)tw[e];
+        if (w) s += pv[u] * tw[e];
         else if (rp[u + 1] > rp[u]) s += pv[u];
       }
       diff += fabs(s - x[v]);
@@ -204,7 +204,7 @@ int or_pr_fixed_point(uint32_t n, const uint64_t* rp, const uint32_t* col, const
 /* Adjoint: lambda = g + d * P lambda, i.e. the transposed system of the
  * forward x = (1-d) t + d P^T x (weights w_uv on edge u->v).
  * lambda_u = g_u + d * sum_{v in out(u)} w_uv * lambda_v. */
-int or_pr_adjoint_solve(uint32_t n, const uint64_t* rp, const uint32_t* col, const float* w,
+int or_pr_adjoint_solve(uint32_t n, const uint64_t* rp, const uint32_t* col, const double* w,
                         double damping, const double* g, double tol, int max_iter,
                         double* lam) {
   double* y = (double*)malloc(sizeof(double) * n);
@@ -215,7 +215,7 @@ int or_pr_adjoint_solve(uint32_t n, const uint64_t* rp, const uint32_t* col, con
 #pragma omp parallel for schedule(dynamic, 1024) reduction(+ : diff)
     for (int64_t u = 0; u < (int64_t)n; ++u) {
       double s = g[u];
-      for (uint64_t e = rp[u]; e < rp[u + 1]; ++e) s += damping * (double)w[e] * lam[col[e]];
+      for (uint64_t e = rp[u]; e < rp[u + 1]; ++e) s += damping * w[e] * lam[col[e]];
       diff += fabs(s - lam[u]);
       y[u] = s;
     }

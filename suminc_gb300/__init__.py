@@ -114,6 +114,23 @@ class BatchInfo(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class AdjointInfo(C.Structure):
+    _fields_ = [
+        ("forward_rounds", C.c_int32),
+        ("adjoint_rounds", C.c_int32),
+        ("forward_ms", C.c_double),
+        ("adjoint_ms", C.c_double),
+        ("forward_residual", C.c_double),
+        ("adjoint_residual", C.c_double),
+        ("forward_edges", C.c_uint64),
+        ("adjoint_edges", C.c_uint64),
+        ("gradient_edges", C.c_uint64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class Stats(C.Structure):
     _fields_ = [
         ("rounds", C.c_int32),
@@ -187,6 +204,12 @@ _SIGS = {
                              _P, _P, _P, C.POINTER(C.c_int32), C.POINTER(C.c_double)], C.c_int),
     "sg_summary_build": ([_P, C.c_uint32, _P, _P], C.c_int),
     "sg_ppr": ([_P, C.c_uint32, _P, _P], C.c_int),
+    "sg_pr_weighted": ([_P, _P, _P], C.c_int),
+    "sg_graph_normalize_weights": ([_P], C.c_int),
+    "sg_pr_adjoint": ([_P, _P, _P, _P], C.c_int),
+    "sg_pr_adjoint_device": ([_P, _P, _P, _P], C.c_int),
+    "sg_adjoint_info_get": ([_P, C.POINTER(AdjointInfo)], C.c_int),
+    "sg_adjoint_values": ([_P, _P, _P], C.c_int),
     "sg_batch_run": ([_P, C.POINTER(BatchSpec), _P, _P], C.c_int),
     "sg_batch_tune_run": ([_P, C.POINTER(BatchSpec), _P, _P], C.c_int),
     "sg_batch_info_get": ([_P, C.POINTER(BatchInfo)], C.c_int),
@@ -410,6 +433,35 @@ class Context:
         _check(self._lib.sg_batch_query_stats(self._h, _ptr(r), _ptr(res)), self,
                "sg_batch_query_stats")
         return r, res
+
+    # -- weighted PageRank and its adjoint ---------------------------------
+    def normalize_weights(self):
+        _check(self._lib.sg_graph_normalize_weights(self._h), self, "sg_graph_normalize_weights")
+
+    def pr_weighted(self, tele=None, out=True):
+        t = None if tele is None else np.ascontiguousarray(tele, np.float32)
+        x = np.empty(self.n, np.float32) if out else None
+        _check(self._lib.sg_pr_weighted(self._h, _ptr(t), _ptr(x)), self, "sg_pr_weighted")
+        return x
+
+    def pr_adjoint(self, dl_dx, out=True):
+        """Returns (dL/dw in download_csr edge order, dL/dtele)."""
+        g = np.ascontiguousarray(dl_dx, np.float32)
+        dw = np.empty(self.m, np.float32) if out else None
+        dt = np.empty(self.n, np.float32) if out else None
+        _check(self._lib.sg_pr_adjoint(self._h, _ptr(g), _ptr(dw), _ptr(dt)), self, "sg_pr_adjoint")
+        return dw, dt
+
+    def adjoint_info(self) -> dict:
+        info = AdjointInfo()
+        _check(self._lib.sg_adjoint_info_get(self._h, C.byref(info)), self, "sg_adjoint_info_get")
+        return info.as_dict()
+
+    def adjoint_values(self):
+        x = np.empty(self.n, np.float32)
+        lam = np.empty(self.n, np.float32)
+        _check(self._lib.sg_adjoint_values(self._h, _ptr(x), _ptr(lam)), self, "sg_adjoint_values")
+        return x, lam
 
     # -- SSSP -------------------------------------------------------------
     def sssp_peval(self, source=0, out=True):

@@ -158,6 +158,7 @@ sg_status pr_weighted_forward(sg_ctx* ctx, const float* tele_host, float* x_out)
   R.weighted = true;
   R.scale_deg = nullptr;
   R.tau = ctx->opt.termcheck_threshold;
+  R.kclass = SG_K_PR_PULL;
   const sg_status rs = pr_rounds_ex(ctx, R);
   if (rs != SG_OK && rs != SG_ERR_NOT_CONVERGED) return rs;
   S.info.forward_rounds = ctx->stats.rounds;
@@ -222,6 +223,7 @@ sg_status pr_adjoint(sg_ctx* ctx, const float* dl_dx_host, bool on_device, float
     // relative stop: the remaining adjoint mass below 1e-7 of |g| (FP32
     // resolution of the accumulated values)
     R.tau = gsum * ctx->opt.adjoint_rel_tol;
+    R.kclass = SG_K_ADJOINT;
     rs = pr_rounds_ex(ctx, R);
     if (rs != SG_OK && rs != SG_ERR_NOT_CONVERGED) return rs;
     S.info.adjoint_rounds = ctx->stats.rounds;

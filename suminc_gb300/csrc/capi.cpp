@@ -505,6 +505,14 @@ sg_status sg_batch_outputs_device(sg_ctx* ctx, const float** ppr, const double**
   return batch_device_outputs(ctx, ppr, sssp);
 }
 
+sg_status sg_graph_normalize_weights(sg_ctx* ctx) {
+  SG_GUARD(ctx);
+  try {
+    return normalize_out_weights(ctx);
+  }
+  SG_CATCH(ctx)
+}
+
 sg_status sg_pr_weighted(sg_ctx* ctx, const float* tele, float* x_out) {
   SG_GUARD(ctx);
   try {

@@ -220,6 +220,8 @@ void pull_lists_free(PullLists& L);
 // packed out-CSR with rows sorted by neighbour (the order of
 // sg_graph_download_csr), into caller-owned device arrays
 sg_status packed_sorted_out(sg_ctx* ctx, uint64_t* d_rp, uint32_t* d_col);
+// divide every edge weight by its source's out-weight sum (both directions)
+sg_status normalize_out_weights(sg_ctx* ctx);
 sg_status apply_updates_device(sg_ctx* ctx, uint64_t count,
                                const sg_update* upd, bool on_device);
 
@@ -244,6 +246,7 @@ struct PrRunSpec {
   bool weighted;              // gather push value x edge weight
   const uint32_t* scale_deg;  // push value d*delta/deg[v]; null: d*delta
   double tau;                 // residual test (sum |delta| < tau)
+  int kclass;                 // profiler class of the pull kernel
 };
 sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R);
 // personalized PageRank of one query: teleport mass (1-d) spread uniformly

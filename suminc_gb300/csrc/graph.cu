@@ -553,6 +553,56 @@ __global__ void k_deg64(const uint32_t* __restrict__ deg, uint32_t n, uint64_t* 
     o[i] = i < n ? deg[i] : 0;
 }
 
+// ------------------------------------------------------------ weights
+
+__global__ void k_row_wsum(const DevCSR c, uint32_t n, float* __restrict__ s) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint64_t wv = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; wv < n;
+       wv += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+    const uint32_t v = (uint32_t)wv;
+    const uint64_t o = c.off[v];
+    const uint32_t d = c.deg[v];
+    double acc = 0.0;
+    for (uint32_t k = lane; k < d; k += 32) acc += (double)c.w[o + k];
+#pragma unroll
+    for (int x = 16; x > 0; x >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, x);
+    if (lane == 0) s[v] = (float)acc;
+  }
+}
+
+// out-CSR: w /= s[row]; in-CSR: w /= s[source] (col holds the source)
+__global__ void k_row_wscale(const DevCSR c, uint32_t n, const float* __restrict__ s, bool by_col) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint64_t wv = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; wv < n;
+       wv += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+    const uint32_t v = (uint32_t)wv;
+    const uint64_t o = c.off[v];
+    const uint32_t d = c.deg[v];
+    for (uint32_t k = lane; k < d; k += 32) {
+      const float t = by_col ? s[c.col[o + k]] : s[v];
+      if (t > 0.f) c.w[o + k] /= t;
+    }
+  }
+}
+
+sg_status normalize_out_weights(sg_ctx* ctx) {
+  DevGraph& g = ctx->g;
+  if (!g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
+  if (!g.weighted) return fail(ctx, SG_ERR_INVALID, "graph has no weights");
+  float* s = nullptr;
+  SG_TRY(dalloc(ctx, &s, g.n));
+  const unsigned b = grid_for((uint64_t)g.n * 32, 256);
+  k_row_wsum<<<b, 256, 0, ctx->stream>>>(g.out, g.n, s);
+  k_row_wscale<<<b, 256, 0, ctx->stream>>>(g.in, g.n, s, true);
+  k_row_wscale<<<b, 256, 0, ctx->stream>>>(g.out, g.n, s, false);
+  count_launch(ctx, 3);
+  SG_CUDA(ctx, cudaGetLastError());
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  dfree(s);
+  g.gen++;  // values derived from the weights are stale
+  return SG_OK;
+}
+
 sg_status packed_sorted_out(sg_ctx* ctx, uint64_t* d_rp, uint32_t* d_col) {
   DevGraph& g = ctx->g;
   const uint32_t n = g.n;

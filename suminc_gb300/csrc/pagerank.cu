@@ -410,7 +410,7 @@ sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R) {
   const unsigned pblocks =
       (unsigned)std::min<uint64_t>(std::max<uint64_t>(P.ntiles, 1), (uint64_t)ctx->num_sms * 8);
   const unsigned fblocks = grid_for(std::max<uint32_t>(L.bnd_count, 1), VT, ctx->num_sms * 2);
-  const int kpull = R.weighted ? SG_K_ADJOINT : SG_K_PR_PULL;
+  const int kpull = R.kclass;
 
   SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
   kprof_begin(ctx);
@@ -481,6 +481,7 @@ static sg_status pr_rounds(sg_ctx* ctx) {
   R.weighted = false;
   R.scale_deg = g.out.deg;
   R.tau = ctx->opt.termcheck_threshold;
+  R.kclass = SG_K_PR_PULL;
   const sg_status st = pr_rounds_ex(ctx, R);
   if (st == SG_OK || st == SG_ERR_NOT_CONVERGED) s.valid = true;
   return st;

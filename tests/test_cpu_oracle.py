@@ -60,3 +60,41 @@ def test_adjoint_solve_matches_dense_linear_algebra():
     x = oracle.pr_fixed_point(rp, col, w)
     x_ref = np.linalg.solve(np.eye(n) - 0.85 * P.T, np.full(n, 0.15 / n))
     assert np.abs(x - x_ref).max() < 1e-12
+
+
+def test_oracle_adjoint_matches_central_differences():
+    """FP64 transposed solve + dL/dw_uv = d*lambda_v*x_u against central
+    differences of the FP64 fixed point (pins the adjoint the GPU is
+    checked against)."""
+    import suminc_gb300 as sg
+    rp, col, w = sg.rmat_host(8, 2000, seed=3, weight_kind=2, wlo=0.1, whi=1.0)
+    n = len(rp) - 1
+    w = w.astype(np.float64)
+    src = np.repeat(np.arange(n), np.diff(rp).astype(np.int64))
+    s = np.bincount(src, weights=w, minlength=n)
+    w = w / s[src]
+    tele = np.full(n, 1.0 / n)
+    rng = np.random.default_rng(1)
+    tgt = rng.choice(n, size=60, replace=False)
+    y = rng.uniform(0, 2.0 / n, size=60)
+
+    def loss(ww, tt):
+        x = oracle.pr_fixed_point(rp, col, ww, tele=tt, tol=1e-15)
+        return 0.5 * np.sum((x[tgt] - y) ** 2), x
+
+    L0, x = loss(w, tele)
+    g = np.zeros(n)
+    g[tgt] = x[tgt] - y
+    lam = oracle.pr_adjoint_solve(rp, col, w, g, tol=1e-16)
+    dw = 0.85 * lam[col] * x[src]
+    h = 1e-5
+    for e in rng.choice(len(col), size=12, replace=False):
+        wp = w.copy(); wp[e] += h
+        wm = w.copy(); wm[e] -= h
+        fd = (loss(wp, tele)[0] - loss(wm, tele)[0]) / (2 * h)
+        assert abs(dw[e] - fd) <= 1e-6 * abs(fd) + 1e-9 * np.abs(dw).max()
+    v = int(tgt[0])
+    tp = tele.copy(); tp[v] += h
+    tm = tele.copy(); tm[v] -= h
+    fd = (loss(w, tp)[0] - loss(w, tm)[0]) / (2 * h)
+    assert abs(0.15 * lam[v] - fd) <= 1e-6 * abs(fd) + 1e-12
