@@ -380,6 +380,29 @@ sg_status sg_pr_peval_noalloc(uint32_t n, uint64_t m, const uint64_t* d_row_ptr,
                               float* d_values, float* d_deltas,
                               int32_t* rounds_out, double* residual_out);
 
+/* ------------------------------------------------ the reference's files */
+
+/* Loads a graph from the reference's text files: efile lines "u v" or
+ * "u v w" (oids; w read when weighted != 0), vfile one oid per line (NULL:
+ * the oids seen in efile).  Vertex ids are the ranks of the distinct oids
+ * (oids 0..N-1 keep their value), as the reference's vertex map
+ * (grape/vertex_map/global_vertex_map.h:145-166); a repeated (u, v) keeps
+ * its first line. */
+sg_status sg_graph_load_files(sg_ctx* ctx, const char* efile, const char* vfile,
+                              int weighted);
+/* oid of every vertex id (host uint64_t[n]). */
+sg_status sg_graph_vertex_oids(sg_ctx* ctx, uint64_t* oids);
+/* Names the vertices of a graph loaded from arrays: oids[v] for v < n,
+ * strictly increasing (the vertex map's order); the update and cluster
+ * files are then read in these oids. */
+sg_status sg_graph_set_vertex_oids(sg_ctx* ctx, const uint64_t* oids);
+/* Applies an update file ("a u v [w]" / "d u v" lines, oids;
+ * grape/fragment/inc_fragment_builder.h:38-70) as one batch. */
+sg_status sg_apply_update_file(sg_ctx* ctx, const char* path);
+/* sg_summary_build from a cluster file (records "size oid_1 ... oid_size",
+ * the <efile>.c_<max_node_num> file of compressor_base.h:3174-3243). */
+sg_status sg_summary_build_file(sg_ctx* ctx, const char* path);
+
 /* ------------------------------------------------------ host utilities
  * (no GPU needed; used to make inputs identical on every side) */
 

@@ -204,6 +204,11 @@ _SIGS = {
                              _P, _P, _P, C.POINTER(C.c_int32), C.POINTER(C.c_double)], C.c_int),
     "sg_summary_build": ([_P, C.c_uint32, _P, _P], C.c_int),
     "sg_ppr": ([_P, C.c_uint32, _P, _P], C.c_int),
+    "sg_graph_load_files": ([_P, C.c_char_p, C.c_char_p, C.c_int], C.c_int),
+    "sg_graph_vertex_oids": ([_P, _P], C.c_int),
+    "sg_graph_set_vertex_oids": ([_P, _P], C.c_int),
+    "sg_apply_update_file": ([_P, C.c_char_p], C.c_int),
+    "sg_summary_build_file": ([_P, C.c_char_p], C.c_int),
     "sg_pr_weighted": ([_P, _P, _P], C.c_int),
     "sg_graph_normalize_weights": ([_P], C.c_int),
     "sg_pr_adjoint": ([_P, _P, _P, _P], C.c_int),
@@ -397,6 +402,28 @@ class Context:
         info = SummaryInfo()
         _check(self._lib.sg_summary_info_get(self._h, C.byref(info)), self, "sg_summary_info_get")
         return info.as_dict()
+
+    # -- the reference's text files ---------------------------------------
+    def load_files(self, efile, vfile=None, weighted=False):
+        _check(self._lib.sg_graph_load_files(self._h, efile.encode(),
+                                             vfile.encode() if vfile else None, int(weighted)),
+               self, "sg_graph_load_files")
+
+    def vertex_oids(self):
+        o = np.empty(self.n, np.uint64)
+        _check(self._lib.sg_graph_vertex_oids(self._h, _ptr(o)), self, "sg_graph_vertex_oids")
+        return o
+
+    def set_vertex_oids(self, oids):
+        o = np.ascontiguousarray(oids, np.uint64)
+        _check(self._lib.sg_graph_set_vertex_oids(self._h, _ptr(o)), self, "sg_graph_set_vertex_oids")
+
+    def apply_update_file(self, path):
+        _check(self._lib.sg_apply_update_file(self._h, path.encode()), self, "sg_apply_update_file")
+
+    def summary_build_file(self, path):
+        _check(self._lib.sg_summary_build_file(self._h, path.encode()), self,
+               "sg_summary_build_file")
 
     # -- personalized PageRank and batches -------------------------------
     def ppr(self, seeds, out=True):

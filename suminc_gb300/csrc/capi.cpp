@@ -245,8 +245,9 @@ sg_status sg_graph_load_csr(sg_ctx* ctx, uint32_t n, const uint64_t* row_ptr,
     pr_free(ctx);
     sssp_free(ctx);
     summary_free(ctx);
-  batch_free(ctx);
-  adjoint_free(ctx);
+    batch_free(ctx);
+    adjoint_free(ctx);
+    ctx->oids.clear();
     return load_csr(ctx, n, row_ptr, col, w);
   }
   SG_CATCH(ctx)
@@ -263,8 +264,9 @@ sg_status sg_graph_generate_rmat(sg_ctx* ctx, int scale, uint64_t edges, double 
     pr_free(ctx);
     sssp_free(ctx);
     summary_free(ctx);
-  batch_free(ctx);
-  adjoint_free(ctx);
+    batch_free(ctx);
+    adjoint_free(ctx);
+    ctx->oids.clear();
     return generate_rmat(ctx, scale, edges, a, b, c, seed, weight_kind, wlo, whi);
   }
   SG_CATCH(ctx)
@@ -555,6 +557,80 @@ sg_status sg_adjoint_values(sg_ctx* ctx, float* x, float* lambda) {
   SG_GUARD(ctx);
   try {
     return adjoint_values(ctx, x, lambda);
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_graph_load_files(sg_ctx* ctx, const char* efile, const char* vfile, int weighted) {
+  SG_GUARD(ctx);
+  if (!efile) return fail(ctx, SG_ERR_INVALID, "null edge file name");
+  try {
+    pr_free(ctx);
+    sssp_free(ctx);
+    summary_free(ctx);
+    batch_free(ctx);
+    adjoint_free(ctx);
+    ctx->oids.clear();
+    return load_files(ctx, efile, vfile, weighted != 0);
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_graph_vertex_oids(sg_ctx* ctx, uint64_t* oids) {
+  SG_GUARD(ctx);
+  if (!oids) return fail(ctx, SG_ERR_INVALID, "null output");
+  if (!ctx->g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
+  for (uint32_t v = 0; v < ctx->g.n; ++v) oids[v] = ctx->oids.empty() ? v : ctx->oids[v];
+  return SG_OK;
+}
+
+sg_status sg_graph_set_vertex_oids(sg_ctx* ctx, const uint64_t* oids) {
+  SG_GUARD(ctx);
+  if (!oids) return fail(ctx, SG_ERR_INVALID, "null oids");
+  if (!ctx->g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
+  try {
+    const uint32_t n = ctx->g.n;
+    bool identity = true;
+    for (uint32_t v = 0; v < n; ++v) {
+      if (v > 0 && oids[v] <= oids[v - 1])
+        return fail(ctx, SG_ERR_INVALID, "oids must be strictly increasing");
+      identity = identity && oids[v] == v;
+    }
+    ctx->oids.clear();
+    if (!identity) ctx->oids.assign(oids, oids + n);
+    return SG_OK;
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_apply_update_file(sg_ctx* ctx, const char* path) {
+  SG_GUARD(ctx);
+  if (!path) return fail(ctx, SG_ERR_INVALID, "null update file name");
+  if (!ctx->g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
+  try {
+    std::vector<sg_update> upd;
+    sg_status st = read_update_file(ctx, path, &upd);
+    if (st != SG_OK) return st;
+    if (upd.empty()) return SG_OK;
+    return sg_apply_updates(ctx, upd.size(), upd.data());
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_summary_build_file(sg_ctx* ctx, const char* path) {
+  SG_GUARD(ctx);
+  if (!path) return fail(ctx, SG_ERR_INVALID, "null cluster file name");
+  if (!ctx->g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
+  try {
+    std::vector<std::vector<uint32_t>> cl;
+    sg_status st = read_cluster_file(ctx, path, &cl);
+    if (st != SG_OK) return st;
+    std::vector<uint32_t> ptr(cl.size() + 1, 0), mem;
+    for (size_t i = 0; i < cl.size(); ++i) {
+      ptr[i + 1] = ptr[i] + (uint32_t)cl[i].size();
+      mem.insert(mem.end(), cl[i].begin(), cl[i].end());
+    }
+    return sg_summary_build(ctx, (uint32_t)cl.size(), ptr.data(), mem.empty() ? nullptr : mem.data());
   }
   SG_CATCH(ctx)
 }

@@ -27,19 +27,22 @@ struct DevCSR {
 };
 
 // Edge-balanced work lists over one direction of adjacency: vertices with
-// degree > 0, the exclusive prefix of their 4-edge quads, the owner of the
-// first quad of each kPullTileQuads tile and the vertices whose quads span
-// tiles.  Rebuilt when the adjacency changes.
+// degree > 0 (with their segment offset and degree in the same order), the
+// exclusive prefix of their 4-edge quads, the owner of the first quad of
+// each kWarpTileQuads tile and the vertices whose quads span tiles.  Rebuilt
+// when the adjacency changes.
 struct PullLists {
   uint32_t* nz = nullptr;       // [n]
   uint64_t* qoff = nullptr;     // [n + 1]
+  uint64_t* off_nz = nullptr;   // [n] segment offset of nz[i]
+  uint32_t* deg_nz = nullptr;   // [n] live degree of nz[i]
   uint32_t nz_count = 0;
   uint64_t quads = 0;
-  uint32_t* tile_v0 = nullptr;  // owner (index into nz) of each tile's first quad
-  uint64_t ntiles = 0;
-  uint64_t tile_cap = 0;
-  uint32_t* bnd = nullptr;      // vertices whose quads span tiles
-  uint32_t bnd_count = 0;
+  uint32_t* wtile_v0 = nullptr; // owner (index into nz) of each tile's first quad
+  uint64_t nwtiles = 0;
+  uint64_t wtile_cap = 0;
+  uint32_t* wbnd = nullptr;     // vertices whose quads span tiles
+  uint32_t wbnd_count = 0;
   uint32_t n_alloc = 0;
   uint64_t gen = ~0ull;         // graph generation the lists describe
 };
@@ -162,6 +165,7 @@ struct sg_ctx {
   void* summary = nullptr;  // summary.cu: summarized graph (compress = 1)
   void* batch_state = nullptr;  // batch.cu: batched PPR / SSSP queries
   void* adjoint_state = nullptr;  // adjoint.cu: weighted PageRank + adjoint
+  std::vector<uint64_t> oids;     // io.cpp: vid -> oid when loaded from files (empty: identity)
 };
 
 namespace sg {
@@ -276,6 +280,12 @@ struct SsspAmendArgs {
 SsspAmendArgs sssp_amend_args(sg_ctx* ctx);
 sg_status sssp_collect_adds(sg_ctx* ctx);
 sg_status sssp_download(sg_ctx* ctx, double* out);
+
+// io.cpp: the reference's text formats
+sg_status load_files(sg_ctx* ctx, const char* efile, const char* vfile, bool weighted);
+sg_status read_update_file(sg_ctx* ctx, const char* path, std::vector<sg_update>* out);
+sg_status read_cluster_file(sg_ctx* ctx, const char* path,
+                            std::vector<std::vector<uint32_t>>* clusters);
 
 // adjoint.cu
 sg_status adjoint_free(sg_ctx* ctx);

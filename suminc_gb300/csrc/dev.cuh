@@ -10,8 +10,8 @@
 
 namespace sg {
 
-// 4-edge quads per tile of the edge-balanced pull over the in-CSR
-constexpr uint32_t kPullTileQuads = 1024;
+// 4-edge quads per tile of the warp-level pull (one quad per lane)
+constexpr uint32_t kWarpTileQuads = 32;
 
 // Blocks for a grid-stride loop over n items: at most 16 resident CTAs per
 // SM of the 152-SM part (the loop covers the rest).

@@ -312,24 +312,66 @@ static sg_status worklist_dir(sg_ctx* ctx, const DevCSR& c, uint32_t* nz,
 }
 
 __global__ void k_tile_v0(const uint64_t* __restrict__ qoff, uint32_t nz_count, uint64_t ntiles,
-                          uint32_t* __restrict__ tv0) {
+                          uint32_t tq, uint32_t* __restrict__ tv0) {
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < ntiles;
        t += (uint64_t)gridDim.x * blockDim.x)
-    tv0[t] = upper_owner(qoff, 0u, nz_count, t * (uint64_t)kPullTileQuads);
+    tv0[t] = upper_owner(qoff, 0u, nz_count, t * (uint64_t)tq);
 }
 
-__global__ void k_bnd_flags(const uint64_t* __restrict__ qoff, uint32_t nz_count,
+__global__ void k_bnd_flags(const uint64_t* __restrict__ qoff, uint32_t nz_count, uint32_t tq,
                             uint8_t* __restrict__ f) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nz_count; i += gridDim.x * blockDim.x)
-    f[i] = (qoff[i] / kPullTileQuads) != ((qoff[i + 1] - 1) / kPullTileQuads);
+    f[i] = (qoff[i] / tq) != ((qoff[i + 1] - 1) / tq);
+}
+
+__global__ void k_nz_meta(const uint32_t* __restrict__ nz, uint32_t cnt, const uint64_t* __restrict__ off,
+                          const uint32_t* __restrict__ deg, uint64_t* __restrict__ off_nz,
+                          uint32_t* __restrict__ deg_nz) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const uint32_t v = nz[i];
+    off_nz[i] = off[v];
+    deg_nz[i] = deg[v];
+  }
 }
 
 void pull_lists_free(PullLists& L) {
   dfree(L.nz);
   dfree(L.qoff);
-  dfree(L.tile_v0);
-  dfree(L.bnd);
+  dfree(L.off_nz);
+  dfree(L.deg_nz);
+  dfree(L.wtile_v0);
+  dfree(L.wbnd);
   L = PullLists();
+}
+
+// owners of the first quad of every tq-quad tile, and the vertices whose
+// quads cross a tile edge
+static sg_status tile_lists(sg_ctx* ctx, PullLists& L, uint32_t tq, uint32_t** tv0,
+                            uint64_t* ntiles, uint64_t* cap, uint32_t* bnd, uint32_t* bnd_count) {
+  *ntiles = (L.quads + tq - 1) / tq;
+  if (*ntiles + 1 > *cap) {
+    dfree(*tv0);
+    *cap = *ntiles + *ntiles / 8 + 1024;
+    SG_TRY(dalloc(ctx, tv0, *cap));
+  }
+  if (*ntiles)
+    k_tile_v0<<<grid_for(*ntiles, 256), 256, 0, ctx->stream>>>(L.qoff, L.nz_count, *ntiles, tq, *tv0);
+  uint8_t* flags = nullptr;
+  uint64_t* cnt = nullptr;
+  SG_TRY(dalloc(ctx, &flags, std::max<uint32_t>(L.nz_count, 1)));
+  SG_TRY(dalloc(ctx, &cnt, 1));
+  uint64_t h = 0;
+  if (L.nz_count) {
+    k_bnd_flags<<<grid_for(L.nz_count, 256), 256, 0, ctx->stream>>>(L.qoff, L.nz_count, tq, flags);
+    SG_TRY(select_flagged(ctx, L.nz, flags, bnd, cnt, L.nz_count));
+    SG_CUDA(ctx, cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *bnd_count = (uint32_t)h;
+  dfree(flags);
+  dfree(cnt);
+  count_launch(ctx, 4);
+  return SG_OK;
 }
 
 static sg_status build_lists(sg_ctx* ctx, const DevCSR& c, PullLists& L) {
@@ -339,36 +381,18 @@ static sg_status build_lists(sg_ctx* ctx, const DevCSR& c, PullLists& L) {
     pull_lists_free(L);
     SG_TRY(dalloc(ctx, &L.nz, n));
     SG_TRY(dalloc(ctx, &L.qoff, (uint64_t)n + 1));
-    SG_TRY(dalloc(ctx, &L.bnd, n));
+    SG_TRY(dalloc(ctx, &L.wbnd, n));
+    SG_TRY(dalloc(ctx, &L.off_nz, n));
+    SG_TRY(dalloc(ctx, &L.deg_nz, n));
     L.n_alloc = n;
   }
   SG_TRY(worklist_dir(ctx, c, L.nz, L.qoff, &L.nz_count, &L.quads));
-  L.ntiles = (L.quads + kPullTileQuads - 1) / kPullTileQuads;
-  if (L.ntiles + 1 > L.tile_cap) {
-    dfree(L.tile_v0);
-    L.tile_cap = L.ntiles + L.ntiles / 8 + 1024;
-    SG_TRY(dalloc(ctx, &L.tile_v0, L.tile_cap));
-  }
-  if (L.ntiles)
-    k_tile_v0<<<grid_for(L.ntiles, 256), 256, 0, ctx->stream>>>(L.qoff, L.nz_count, L.ntiles,
-                                                                 L.tile_v0);
-  // boundary vertices: nz entries whose quads cross a tile edge
-  uint8_t* flags = nullptr;
-  uint64_t* cnt = nullptr;
-  SG_TRY(dalloc(ctx, &flags, std::max<uint32_t>(L.nz_count, 1)));
-  SG_TRY(dalloc(ctx, &cnt, 1));
-  uint64_t h = 0;
-  if (L.nz_count) {
-    k_bnd_flags<<<grid_for(L.nz_count, 256), 256, 0, ctx->stream>>>(L.qoff, L.nz_count, flags);
-    SG_TRY(select_flagged(ctx, L.nz, flags, L.bnd, cnt, L.nz_count));
-    SG_CUDA(ctx, cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, ctx->stream));
-  }
-  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  L.bnd_count = (uint32_t)h;
+  if (L.nz_count)
+    k_nz_meta<<<grid_for(L.nz_count, 256), 256, 0, ctx->stream>>>(L.nz, L.nz_count, c.off, c.deg,
+                                                                   L.off_nz, L.deg_nz);
+  SG_TRY(tile_lists(ctx, L, kWarpTileQuads, &L.wtile_v0, &L.nwtiles, &L.wtile_cap, L.wbnd,
+                    &L.wbnd_count));
   L.gen = g.gen;
-  dfree(flags);
-  dfree(cnt);
-  count_launch(ctx, 8);
   return SG_OK;
 }
 
@@ -524,7 +548,34 @@ sg_status load_csr(sg_ctx* ctx, uint32_t n, const uint64_t* row_ptr,
     dfree(keys2); dfree(d_w2);
     return fail(ctx, SG_ERR_INVALID, "column index >= n");
   }
-  sg_status st = graph_build_from_sorted_keys(ctx, n, m, keys2, d_w2, w != nullptr);
+  // a repeated (u, v) pair keeps its first occurrence (the sort is stable)
+  uint64_t m_u = m;
+  if (m > 1) {
+    uint8_t* fl = nullptr;
+    uint64_t *kd = nullptr, *cnt = nullptr;
+    float* wd = nullptr;
+    SG_TRY(dalloc(ctx, &fl, m));
+    SG_TRY(dalloc(ctx, &kd, m));
+    SG_TRY(dalloc(ctx, &cnt, 1));
+    k_first_flags<<<grid_for(m, 256), 256, 0, ctx->stream>>>(keys2, m, ~0ull, fl);
+    SG_TRY(select_flagged(ctx, keys2, fl, kd, cnt, m));
+    if (w) {
+      SG_TRY(dalloc(ctx, &wd, m));
+      SG_TRY(select_flagged(ctx, d_w2, fl, wd, cnt, m));
+    }
+    SG_CUDA(ctx, cudaMemcpyAsync(&m_u, cnt, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    count_launch(ctx, 3);
+    dfree(fl);
+    dfree(cnt);
+    dfree(keys2);
+    keys2 = kd;
+    if (w) {
+      dfree(d_w2);
+      d_w2 = wd;
+    }
+  }
+  sg_status st = graph_build_from_sorted_keys(ctx, n, m_u, keys2, d_w2, w != nullptr);
   dfree(keys2);
   dfree(d_w2);
   return st;

@@ -10,12 +10,14 @@
 // Round structure:
 //   k_pr_vertex   first round of every run: activation of every vertex from
 //                 the current delta (PEval init or the amended IncEval state)
-//   k_pr_pull     dense pull over the in-CSR, edge-balanced in tiles of
-//                 PT_TILE 4-edge quads (128-bit neighbour loads, gathers of
-//                 pv, shared-memory sums).  A vertex whose quads all lie in
-//                 the tile is updated in the tile's epilogue (incoming sum,
-//                 residual, activation, next push value); a vertex spanning
-//                 tiles gets its partial sums by atomicAdd
+//   k_pr_pull_warp  dense pull over the in-CSR, edge-balanced in warp tiles
+//                 of 32 4-edge quads (one 128-bit neighbour load and four
+//                 push-value gathers per lane, owners found by popc over the
+//                 tile's segment starts, segmented shuffle sums).  A vertex
+//                 whose quads all lie in the tile is updated by the first
+//                 lane of its run (incoming sum, residual, activation, next
+//                 push value); a vertex spanning tiles gets its partial sums
+//                 by atomicAdd
 //   k_pr_fixup    updates the tile-spanning vertices; its last block makes
 //                 the termination decision on the device
 // Push values are double-buffered by pull index.  When the residual passes
@@ -108,117 +110,113 @@ __global__ void __launch_bounds__(VT) k_pr_vertex(PrArgs A) {
 }
 
 constexpr int PT_THREADS = 256;
-constexpr int PT_QPT = kPullTileQuads / PT_THREADS;  // quads per thread, contiguous
-constexpr int PT_TILE = kPullTileQuads;              // quads per tile
 
-struct PullArgs {
-  const uint32_t* nz;      // vertices with in-degree > 0, in id order
-  const uint64_t* qoff;    // [nz_count + 1] quad prefix
-  const uint32_t* tile_v0; // owner (nz index) of each tile's first quad
+// Warp-level pull: a warp takes a tile of kWarpTileQuads quads, one quad per
+// lane.  The up-to-32 owners of the tile are loaded one per lane (first
+// quad, segment offset and degree from nz-ordered copies, so a lane's
+// neighbour load depends on one load only; the owner's delta and degree
+// for the epilogue are fetched alongside, off the gather's critical path).
+// A lane finds its owner from the mask of segment starts (popc), gathers its
+// four push values, and a segmented shuffle reduction leaves each owner's
+// sum in the first lane of its segment.  Owners whose quads all lie in the
+// tile are finished there (no shared memory, no block barrier); the others
+// add their partial sums to delta by atomicAdd and are finished by
+// k_pr_fixup.  The next tile's first owner is prefetched.
+struct WarpPullArgs {
+  const uint32_t* nz;
+  const uint64_t* qoff;
+  const uint64_t* off_nz;   // segment offset of nz[i]
+  const uint32_t* deg_nz;   // live degree of nz[i]
+  const uint32_t* wtile_v0;
   uint32_t nz_count;
   uint64_t quads;
   uint64_t ntiles;
-  const uint64_t* off;     // the pulled CSR (in-CSR for PageRank)
   const uint32_t* col;
-  const float* w;          // its weights (weighted pulls only)
+  const float* w;
 };
 
-// pull number p reads pvb[p & 1] (or pv0 for p == 0) and writes the next
-// push values into pvb[(p + 1) & 1].  W: multiply each gathered push value
-// by the edge weight (weighted PageRank and its adjoint).
+// 8 CTAs of 256 threads per SM: 32 registers per thread, full occupancy
+// (measured faster than 6 CTAs without spills)
 template <bool W>
-__global__ void __launch_bounds__(PT_THREADS) k_pr_pull(PrArgs A, PullArgs P, int p) {
-  __shared__ uint64_t sq[PT_TILE + 2];
-  __shared__ uint32_t snz[PT_TILE + 1];
-  __shared__ float sacc[PT_TILE + 1];
+__global__ void __launch_bounds__(PT_THREADS, 8) k_pr_pull_warp(PrArgs A, WarpPullArgs P, int p) {
   __shared__ double s_red[PT_THREADS / 32];
   if (A.misc[M_DONE]) return;
   const bool drain = A.misc[M_PENDING] != 0;
   const float* __restrict__ pv = p == 0 ? A.pv0 : ((p & 1) ? A.pvb[1] : A.pvb[0]);
   float* pv_next = (p & 1) ? A.pvb[0] : A.pvb[1];
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * PT_THREADS) >> 5;
   double res = 0.0;
   unsigned long long visits = 0;
-  for (uint64_t tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x) {
-    const uint64_t q0 = tile * PT_TILE;
-    const uint64_t q1 = min(q0 + (uint64_t)PT_TILE, P.quads);
-    const uint32_t v0 = P.tile_v0[tile];
-    uint32_t v1;
-    if (tile + 1 < P.ntiles) {
-      const uint32_t nv = P.tile_v0[tile + 1];
-      v1 = P.qoff[nv] < q1 ? nv : nv - 1;
-    } else {
-      v1 = P.nz_count - 1;
-    }
-    const uint32_t cnt = v1 - v0 + 1;
-    for (uint32_t i = threadIdx.x; i <= cnt; i += PT_THREADS) {
-      sq[i] = P.qoff[v0 + i];
-      if (i < cnt) {
-        snz[i] = P.nz[v0 + i];
-        sacc[i] = 0.f;
+  uint64_t t = ((uint64_t)blockIdx.x * PT_THREADS + threadIdx.x) >> 5;
+  uint32_t i0 = t < P.ntiles ? P.wtile_v0[t] : 0u;
+  for (; t < P.ntiles; t += nwarps) {
+    const uint64_t base = t * kWarpTileQuads;
+    const uint64_t q = base + lane;
+    const bool valid = q < P.quads;
+    // owner candidate i0 + lane
+    const uint32_t ic = min(i0 + lane, P.nz_count);
+    const bool real = ic < P.nz_count;
+    const uint64_t qb_c = P.qoff[ic];
+    const uint64_t qe_c = P.qoff[min(ic + 1, P.nz_count)];
+    const uint64_t off_c = real ? P.off_nz[ic] : 0ull;
+    const uint32_t deg_c = real ? P.deg_nz[ic] : 0u;
+    const uint32_t v_c = real ? P.nz[ic] : 0u;
+    // prefetch the next tile's first owner
+    const uint64_t tn = t + nwarps;
+    const uint32_t i0_next = tn < P.ntiles ? P.wtile_v0[tn] : 0u;
+    const bool starts = lane > 0 && real && qb_c < base + kWarpTileQuads;
+    const unsigned heads = __reduce_or_sync(0xffffffffu, starts ? 1u << (uint32_t)(qb_c - base) : 0u);
+    const uint32_t k = __popc(heads & (0xffffffffu >> (31 - lane)));
+    const uint64_t qb = __shfl_sync(0xffffffffu, qb_c, k);
+    const uint64_t off = __shfl_sync(0xffffffffu, off_c, k);
+    const uint32_t deg = __shfl_sync(0xffffffffu, deg_c, k);
+    // epilogue operands of the candidate owners, loaded before the gathers
+    const bool cand_used = real && (lane == 0 || starts);
+    const float dl_c = cand_used ? A.delta[v_c] : 0.f;
+    float sum = 0.f;
+    if (valid) {
+      const uint32_t kk = (uint32_t)(q - qb) * 4;
+      const uint4 c4 = *reinterpret_cast<const uint4*>(P.col + off + kk);
+      if (W) {
+        const float4 w4 = *reinterpret_cast<const float4*>(P.w + off + kk);
+        sum = pv[c4.x] * w4.x;  // the last quad of a vertex may be partial
+        if (kk + 1 < deg) sum += pv[c4.y] * w4.y;
+        if (kk + 2 < deg) sum += pv[c4.z] * w4.z;
+        if (kk + 3 < deg) sum += pv[c4.w] * w4.w;
+      } else {
+        sum = pv[c4.x];
+        if (kk + 1 < deg) sum += pv[c4.y];
+        if (kk + 2 < deg) sum += pv[c4.z];
+        if (kk + 3 < deg) sum += pv[c4.w];
       }
     }
-    __syncthreads();
-    // contiguous quads of this thread, owners walked in order
-    const uint64_t qa = q0 + (uint64_t)threadIdx.x * PT_QPT;
-    const uint64_t qb = min(qa + PT_QPT, q1);
-    if (qa < qb) {
-      uint32_t i = upper_owner(sq, 0u, cnt, qa);
-      uint32_t v = snz[i];
-      uint64_t base = P.off[v];
-      uint64_t qbeg = sq[i], qend = sq[i + 1];
-      uint32_t deg = A.pull_deg[v];
-      float acc = 0.f;
-      for (uint64_t q = qa; q < qb; ++q) {
-        if (q >= qend) {
-          if (acc != 0.f) atomicAdd(&sacc[i], acc);
-          acc = 0.f;
-          do {
-            ++i;
-          } while (q >= sq[i + 1]);
-          v = snz[i];
-          base = P.off[v];
-          qbeg = sq[i];
-          qend = sq[i + 1];
-          deg = A.pull_deg[v];
-        }
-        const uint32_t k = (uint32_t)(q - qbeg) * 4;
-        const uint4 c4 = *reinterpret_cast<const uint4*>(P.col + base + k);
-        if (W) {
-          const float4 w4 = *reinterpret_cast<const float4*>(P.w + base + k);
-          float s = pv[c4.x] * w4.x;  // the last quad of a vertex may be partial
-          if (k + 1 < deg) s += pv[c4.y] * w4.y;
-          if (k + 2 < deg) s += pv[c4.z] * w4.z;
-          if (k + 3 < deg) s += pv[c4.w] * w4.w;
-          acc += s;
-        } else {
-          float s = pv[c4.x];  // the last quad of a vertex may be partial
-          if (k + 1 < deg) s += pv[c4.y];
-          if (k + 2 < deg) s += pv[c4.z];
-          if (k + 3 < deg) s += pv[c4.w];
-          acc += s;
-        }
-      }
-      if (acc != 0.f) atomicAdd(&sacc[i], acc);
+    // segmented suffix sums: the first lane of each owner's run gets its total
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float ts = __shfl_down_sync(0xffffffffu, sum, o);
+      const uint32_t tk = __shfl_down_sync(0xffffffffu, k, o);
+      if (lane + o < 32 && tk == k) sum += ts;
     }
-    __syncthreads();
-    // epilogue: vertices entirely inside the tile are final for this round
-    for (uint32_t i = threadIdx.x; i < cnt; i += PT_THREADS) {
-      const uint32_t v = snz[i];
-      const float s = sacc[i];
-      const bool interior = sq[i] >= q0 && sq[i + 1] <= q1;
+    const uint32_t v = __shfl_sync(0xffffffffu, v_c, k);
+    const uint64_t qe = __shfl_sync(0xffffffffu, qe_c, k);
+    const float dl0 = __shfl_sync(0xffffffffu, dl_c, k);
+    const bool head = valid && (lane == 0 || ((heads >> lane) & 1u));
+    if (head) {
+      const bool interior = qb >= base && qe <= base + kWarpTileQuads;
       if (interior) {
-        const float dl = A.delta[v] + s;
+        const float dl = dl0 + sum;
         if (drain) {
           A.delta[v] = dl;
           res += fabs((double)dl);
         } else {
           visits += activate(A, v, dl, pv_next, res);
         }
-      } else if (s != 0.f) {
-        atomicAdd(&A.delta[v], s);
+      } else if (sum != 0.f) {
+        atomicAdd(&A.delta[v], sum);
       }
     }
-    __syncthreads();
+    i0 = i0_next;
   }
   const double b = block_sum<PT_THREADS>(res, s_red);
   if (threadIdx.x == 0 && b != 0.0) atomicAdd(&A.res[R_ACC], b);
@@ -395,21 +393,25 @@ sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R) {
   A.res = s.res;
   A.cnt = s.cnt;
 
-  PullArgs P;
-  P.nz = L.nz;
-  P.qoff = L.qoff;
-  P.tile_v0 = L.tile_v0;
-  P.nz_count = L.nz_count;
-  P.quads = L.quads;
-  P.ntiles = L.ntiles;
-  P.off = R.csr->off;
-  P.col = R.csr->col;
-  P.w = R.weighted ? R.csr->w : nullptr;
+  WarpPullArgs WP;
+  WP.nz = L.nz;
+  WP.qoff = L.qoff;
+  WP.off_nz = L.off_nz;
+  WP.deg_nz = L.deg_nz;
+  WP.wtile_v0 = L.wtile_v0;
+  WP.nz_count = L.nz_count;
+  WP.quads = L.quads;
+  WP.ntiles = L.nwtiles;
+  WP.col = R.csr->col;
+  WP.w = R.weighted ? R.csr->w : nullptr;
+  const uint32_t* bnd = L.wbnd;
+  const uint32_t nbnd = L.wbnd_count;
 
   const unsigned vblocks = grid_for(g.n, VT, ctx->num_sms * 8);
-  const unsigned pblocks =
-      (unsigned)std::min<uint64_t>(std::max<uint64_t>(P.ntiles, 1), (uint64_t)ctx->num_sms * 8);
-  const unsigned fblocks = grid_for(std::max<uint32_t>(L.bnd_count, 1), VT, ctx->num_sms * 2);
+  const unsigned wblocks = (unsigned)std::min<uint64_t>(
+      std::max<uint64_t>((L.nwtiles + PT_THREADS / 32 - 1) / (PT_THREADS / 32), 1),
+      (uint64_t)ctx->num_sms * 8);
+  const unsigned fblocks = grid_for(std::max<uint32_t>(nbnd, 1), VT, ctx->num_sms * 2);
   const int kpull = R.kclass;
 
   SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
@@ -424,11 +426,11 @@ sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R) {
     for (;;) {
       for (int r = 0; r < chunk; ++r, ++pull) {
         kprof_begin(ctx);
-        if (R.weighted) k_pr_pull<true><<<pblocks, PT_THREADS, 0, st>>>(A, P, pull);
-        else k_pr_pull<false><<<pblocks, PT_THREADS, 0, st>>>(A, P, pull);
+        if (R.weighted) k_pr_pull_warp<true><<<wblocks, PT_THREADS, 0, st>>>(A, WP, pull);
+        else k_pr_pull_warp<false><<<wblocks, PT_THREADS, 0, st>>>(A, WP, pull);
         kprof_end(ctx, kpull);
         kprof_begin(ctx);
-        k_pr_fixup<<<fblocks, VT, 0, st>>>(A, L.bnd, L.bnd_count, pull);
+        k_pr_fixup<<<fblocks, VT, 0, st>>>(A, bnd, nbnd, pull);
         kprof_end(ctx, SG_K_PR_VERTEX);
       }
       SG_CUDA(ctx, cudaGetLastError());
