@@ -3,8 +3,8 @@
 // the workers use: InnerVertices, GetInnerVerticesNum, GetId,
 // GetOutgoingAdjList with neighbor / data, init_c, GetInitDelta).
 //
-// usage: adaptor_test <efile> <update_pr> <update_sssp> <out_pr> <out_sssp>
-//   efile lines "u v w" with oids 10 * vid + 7
+// usage: adaptor_test <efile> <update_pr> <update_sssp> <out_pr> <out_sssp> <n>
+//   efile lines "u v w" with oids 10 * vid + 7; n vertices
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -87,12 +87,13 @@ class SSSPIngress {
 }  // namespace grape
 
 int main(int argc, char** argv) {
-  if (argc != 6) {
-    std::fprintf(stderr, "usage: %s efile update_pr update_sssp out_pr out_sssp\n", argv[0]);
+  if (argc != 7) {
+    std::fprintf(stderr, "usage: %s efile update_pr update_sssp out_pr out_sssp n\n", argv[0]);
     return 2;
   }
   using FragW = grape::Fragment<uint16_t>;
   auto frag = std::make_shared<FragW>();
+  frag->out.resize((size_t)std::stoul(argv[6]));
   std::ifstream in(argv[1]);
   std::string line;
   while (std::getline(in, line)) {

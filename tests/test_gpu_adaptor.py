@@ -59,7 +59,7 @@ def test_cpp_workers_match_c_abi(binary, tmp_path):
     write_updates(tmp_path / "sssp.update", uss, True)
     opr, oss = tmp_path / "pr.out", tmp_path / "sssp.out"
     r = subprocess.run([binary, str(ef), str(tmp_path / "pr.update"), str(tmp_path / "sssp.update"),
-                        str(opr), str(oss)], capture_output=True, text=True)
+                        str(opr), str(oss), str(n)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     pr = np.loadtxt(opr)
     ss = np.loadtxt(oss)
