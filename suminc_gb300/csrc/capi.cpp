@@ -400,7 +400,8 @@ sg_status sg_summary_info_get(sg_ctx* ctx, sg_summary_info* out) {
 sg_status sg_sssp_peval(sg_ctx* ctx, uint32_t source, double* out) {
   SG_GUARD(ctx);
   try {
-    sg_status st = sssp_run_peval(ctx, source);
+    sg_status st = ctx->opt.compress && ctx->summary ? sssp_summarized(ctx, source)
+                                                     : sssp_run_peval(ctx, source);
     kprof_flush(ctx);
     if (st != SG_OK) return st;
     if (out) return sssp_download(ctx, out);

@@ -280,6 +280,21 @@ struct SsspAmendArgs {
 SsspAmendArgs sssp_amend_args(sg_ctx* ctx);
 sg_status sssp_collect_adds(sg_ctx* ctx);
 sg_status sssp_download(sg_ctx* ctx, double* out);
+// delta-stepping over another padded CSR (the summarized graph)
+struct SsspView {
+  uint32_t n;
+  uint64_t m;
+  const uint64_t* off;
+  const uint32_t* deg;
+  const uint32_t* col;
+  const float* w;
+};
+sg_status sssp_run_view(sg_ctx* ctx, const SsspView& G, const uint32_t* h_seeds,
+                        const double* h_seed_dist, uint32_t nseeds, unsigned long long* dist,
+                        unsigned long long* h_cnt);
+// prepares ctx->sp for a result written from outside (buffers, no run)
+sg_status sssp_prepare_external(sg_ctx* ctx, uint32_t source);
+sg_status sssp_finish_external(sg_ctx* ctx, const unsigned long long* h_cnt, float ms);
 
 // io.cpp: the reference's text formats
 sg_status load_files(sg_ctx* ctx, const char* efile, const char* vfile, bool weighted);
@@ -307,6 +322,7 @@ sg_status summary_free(sg_ctx* ctx);
 sg_status summary_build(sg_ctx* ctx, const std::vector<std::vector<uint32_t>>& clusters);
 sg_status summary_after_apply(sg_ctx* ctx);
 sg_status pr_summarized(sg_ctx* ctx, bool inc);
+sg_status sssp_summarized(sg_ctx* ctx, uint32_t source);
 uint32_t summary_rows(sg_ctx* ctx);  // rows incl. mirrors, 0 without a summary
 sg_status summary_info(sg_ctx* ctx, sg_summary_info* out);
 

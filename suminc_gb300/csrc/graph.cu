@@ -217,7 +217,8 @@ static sg_status build_direction(sg_ctx* ctx, DevCSR& c, uint32_t n, uint64_t m,
   SG_CUDA(ctx, cudaMemcpyAsync(&total, c.off + n, sizeof(uint64_t),
                                cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  uint64_t pool_extra = std::max<uint64_t>(total / 16, 1u << 20);
+  // room for relocated segments; a batch that may not fit repacks first
+  uint64_t pool_extra = std::max<uint64_t>(total / 16, 1024);
   c.pool_cap = total + pool_extra;
   SG_TRY(dalloc(ctx, &c.col, c.pool_cap));
   if (weighted) SG_TRY(dalloc(ctx, &c.w, c.pool_cap));
@@ -824,6 +825,97 @@ __global__ void k_inv_keys(const uint32_t* __restrict__ s, const uint32_t* __res
 }
 
 
+// ------------------------------------------------------------ repack
+//
+// Segments that outgrow their capacity move to the pool tail and leave their
+// old slots unused.  Before a batch whose worst case no longer fits the free
+// tail, a direction is repacked: fresh capacities with slack, live entries
+// copied in vertex order, a new pool with room for the batch.
+
+// slots a batch may need in one direction: every vertex with actions could
+// move, with its live entries plus the actions' inserts and slack
+__global__ void k_batch_need(const uint32_t* __restrict__ gv, const uint32_t* __restrict__ gb,
+                             const uint32_t* __restrict__ ge, uint64_t n_grp,
+                             const uint32_t* __restrict__ deg, unsigned long long* need) {
+  unsigned long long acc = 0;
+  for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < n_grp;
+       g += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t d1 = (uint64_t)deg[gv[g]] + (ge[g] - gb[g]);
+    acc += ((d1 + d1 / 8 + 4 + 3) & ~3ull);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc) atomicAdd(need, acc);
+}
+
+__global__ void k_repack_rows(const uint64_t* __restrict__ off_old, const uint32_t* __restrict__ deg,
+                              const uint32_t* __restrict__ col_old, const float* __restrict__ w_old,
+                              uint32_t n, const uint64_t* __restrict__ off_new,
+                              uint32_t* __restrict__ col_new, float* __restrict__ w_new) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint64_t wv = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; wv < n;
+       wv += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+    const uint32_t v = (uint32_t)wv;
+    const uint64_t a = off_old[v], b = off_new[v];
+    const uint32_t d = deg[v];
+    for (uint32_t k = lane; k < d; k += 32) {
+      col_new[b + k] = col_old[a + k];
+      if (w_new) w_new[b + k] = w_old[a + k];
+    }
+  }
+}
+
+static sg_status repack_direction(sg_ctx* ctx, DevCSR& c, uint64_t batch_need) {
+  const uint32_t n = ctx->g.n;
+  const float slack = (float)(ctx->opt.slack >= 0 ? ctx->opt.slack : 0.125);
+  cudaStream_t st = ctx->stream;
+  uint64_t *cap64 = nullptr, *off_new = nullptr;
+  SG_TRY(dalloc(ctx, &cap64, (uint64_t)n + 1));
+  SG_TRY(dalloc(ctx, &off_new, (uint64_t)n + 1));
+  k_capacity<<<grid_for(n, 256), 256, 0, st>>>(c.deg, n, slack, cap64, c.cap);
+  SG_CUDA(ctx, cudaMemsetAsync(cap64 + n, 0, sizeof(uint64_t), st));
+  SG_TRY(exclusive_sum(ctx, cap64, off_new, (uint64_t)n + 1));
+  uint64_t total = 0;
+  SG_CUDA(ctx, cudaMemcpyAsync(&total, off_new + n, 8, cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  const uint64_t extra = std::max<uint64_t>({total / 16, 1024ull, 2 * batch_need});
+  const uint64_t pool = total + extra;
+  uint32_t* col_new = nullptr;
+  float* w_new = nullptr;
+  SG_TRY(dalloc(ctx, &col_new, pool));
+  if (c.w) SG_TRY(dalloc(ctx, &w_new, pool));
+  k_repack_rows<<<grid_for((uint64_t)n * 32, 256), 256, 0, st>>>(c.off, c.deg, c.col, c.w, n, off_new,
+                                                                col_new, w_new);
+  SG_CUDA(ctx, cudaMemcpyAsync(c.pool_tail, &total, 8, cudaMemcpyHostToDevice, st));
+  SG_CUDA(ctx, cudaGetLastError());
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  dfree(c.off);
+  dfree(c.col);
+  dfree(c.w);
+  dfree(cap64);
+  c.off = off_new;
+  c.col = col_new;
+  c.w = w_new;
+  c.pool_cap = pool;
+  count_launch(ctx, 4);
+  return SG_OK;
+}
+
+// Repacks each direction whose free tail cannot hold the batch's worst case.
+static sg_status ensure_pool(sg_ctx* ctx, DevCSR& c, const uint32_t* gv, const uint32_t* gb,
+                             const uint32_t* ge, uint64_t n_grp, unsigned long long* d_need) {
+  SG_CUDA(ctx, cudaMemsetAsync(d_need, 0, 8, ctx->stream));
+  if (n_grp)
+    k_batch_need<<<grid_for(n_grp, 256), 256, 0, ctx->stream>>>(gv, gb, ge, n_grp, c.deg, d_need);
+  unsigned long long need = 0, tail = 0;
+  SG_CUDA(ctx, cudaMemcpyAsync(&need, d_need, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaMemcpyAsync(&tail, c.pool_tail, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  count_launch(ctx);
+  if (tail + need <= c.pool_cap) return SG_OK;
+  return repack_direction(ctx, c, need);
+}
+
 constexpr uint32_t kApplyChunk = 1024;  // segment entries per find / amend work item
 
 struct ApplyDirArgs {
@@ -1210,6 +1302,12 @@ sg_status apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* upd
   SG_TRY(sort_pairs(ctx, B.key, B.key2, B.val, B.perm, n_runs));
   SG_TRY(make_groups(ctx, B.a_dst, B.perm, n_runs, B.igrp_vertex, B.igrp_begin, B.igrp_end,
                      &B.n_igrp));
+  // room for the batch's worst case in each direction (repack when short)
+  {
+    unsigned long long* d_need = (unsigned long long*)B.d_count + 3;
+    SG_TRY(ensure_pool(ctx, g.out, B.grp_vertex, B.grp_begin, B.grp_end, B.n_grp, d_need));
+    SG_TRY(ensure_pool(ctx, g.in, B.igrp_vertex, B.igrp_begin, B.igrp_end, B.n_igrp, d_need));
+  }
   // patch the out direction (with application amends), then the in direction
   ApplyDirArgs A{};
   A.c = g.out;

@@ -461,6 +461,27 @@ static double auto_delta(sg_ctx* ctx) {
   return 32.0;
 }
 
+// Launches the persistent kernel (cooperative) for the given arguments and
+// reads its control words back.
+static sg_status sssp_launch_args(sg_ctx* ctx, SsspArgs& A, uint32_t* h_ctl) {
+  int bps = 0;
+  SG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_sssp_persistent, 256, 0));
+  if (bps < 1) return fail(ctx, SG_ERR_CUDA, "persistent SSSP kernel cannot be resident");
+  bps = std::min(bps, 4);
+  const unsigned blocks = (unsigned)(bps * ctx->num_sms);
+  void* args[] = {&A};
+  kprof_begin(ctx);
+  SG_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_sssp_persistent, dim3(blocks), dim3(256), args,
+                                           0, ctx->stream));
+  kprof_end(ctx, SG_K_SSSP);
+  SG_CUDA(ctx, cudaMemcpyAsync(h_ctl, A.ctl, sizeof(uint32_t) * S_WORDS, cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h_ctl[S_ERR] == 2u) return fail(ctx, SG_ERR_OOM, "SSSP far queue overflow");
+  if (h_ctl[S_ERR]) return fail(ctx, SG_ERR_TIMEOUT, "SSSP grid barrier wait expired");
+  return SG_OK;
+}
+
 // Runs the persistent kernel from the current ctl / queues.
 static sg_status sssp_launch(sg_ctx* ctx) {
   SsspState& s = ctx->sp;
@@ -477,24 +498,75 @@ static sg_status sssp_launch(sg_ctx* ctx) {
   A.iter_base = s.iter_base;
   A.fcap = s.far_cap;
   A.spin_limit = 40ll * 1000 * 1000;  // ~2-4 s of polling
-  int bps = 0;
-  SG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_sssp_persistent, 256, 0));
-  if (bps < 1) return fail(ctx, SG_ERR_CUDA, "persistent SSSP kernel cannot be resident");
-  bps = std::min(bps, 4);
-  const unsigned blocks = (unsigned)(bps * ctx->num_sms);
-  void* args[] = {&A};
-  kprof_begin(ctx);
-  SG_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_sssp_persistent, dim3(blocks), dim3(256), args,
-                                           0, ctx->stream));
-  kprof_end(ctx, SG_K_SSSP);
   uint32_t h_ctl[S_WORDS];
-  SG_CUDA(ctx, cudaMemcpyAsync(h_ctl, s.d_ctl, sizeof(h_ctl), cudaMemcpyDeviceToHost, ctx->stream));
-  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  SG_TRY(sssp_launch_args(ctx, A, h_ctl));
   // stamps must keep growing across launches
   s.iter_base += h_ctl[S_ITERS] + h_ctl[S_SPLITS] + 4;
-  if (h_ctl[S_ERR] == 2u) return fail(ctx, SG_ERR_OOM, "SSSP far queue overflow");
-  if (h_ctl[S_ERR]) return fail(ctx, SG_ERR_TIMEOUT, "SSSP grid barrier wait expired");
   return SG_OK;
+}
+
+__global__ void k_sssp_seed_list(const uint32_t* __restrict__ v, const double* __restrict__ d,
+                                 uint32_t cnt, unsigned long long* dist, uint32_t* far) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    atomicMin(dist + v[i], dbits(d[i]));
+    far[i] = v[i];
+  }
+}
+
+// Delta-stepping over a caller-given padded CSR view (segments 16-byte
+// aligned, readable in quads) from a list of seeds with start distances.
+// Temporary queues are allocated for the call.  dist: device [G.n].
+sg_status sssp_run_view(sg_ctx* ctx, const SsspView& G, const uint32_t* h_seeds,
+                        const double* h_seed_dist, uint32_t nseeds, unsigned long long* dist,
+                        unsigned long long* h_cnt) {
+  cudaStream_t st = ctx->stream;
+  const uint32_t n = G.n;
+  uint32_t *stamp = nullptr, *fstamp = nullptr, *reset = nullptr, *q0 = nullptr, *q1 = nullptr,
+           *q2 = nullptr, *far = nullptr, *far2 = nullptr, *ctl = nullptr, *sv = nullptr;
+  unsigned long long* cnt = nullptr;
+  double* sd = nullptr;
+  const uint64_t fcap = G.m + (uint64_t)n + nseeds + 1024;
+  SG_TRY(dalloc(ctx, &stamp, n));
+  SG_TRY(dalloc(ctx, &fstamp, n));
+  SG_TRY(dalloc(ctx, &reset, n));
+  SG_TRY(dalloc(ctx, &q0, n));
+  SG_TRY(dalloc(ctx, &q1, n));
+  SG_TRY(dalloc(ctx, &q2, n));
+  SG_TRY(dalloc(ctx, &far, fcap));
+  SG_TRY(dalloc(ctx, &far2, fcap));
+  SG_TRY(dalloc(ctx, &ctl, S_WORDS));
+  SG_TRY(dalloc(ctx, &cnt, SC_WORDS));
+  SG_TRY(dalloc(ctx, &sv, std::max<uint32_t>(nseeds, 1)));
+  SG_TRY(dalloc(ctx, &sd, std::max<uint32_t>(nseeds, 1)));
+  k_sssp_init<<<grid_for(n, 256), 256, 0, st>>>(n, dist, stamp, fstamp, reset);
+  SG_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(uint32_t) * S_WORDS, st));
+  SG_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * SC_WORDS, st));
+  if (nseeds) {
+    SG_CUDA(ctx, cudaMemcpyAsync(sv, h_seeds, 4ull * nseeds, cudaMemcpyHostToDevice, st));
+    SG_CUDA(ctx, cudaMemcpyAsync(sd, h_seed_dist, 8ull * nseeds, cudaMemcpyHostToDevice, st));
+    k_sssp_seed_list<<<grid_for(nseeds, 256), 256, 0, st>>>(sv, sd, nseeds, dist, far);
+    SG_CUDA(ctx, cudaMemcpyAsync(ctl + S_F0, &nseeds, 4, cudaMemcpyHostToDevice, st));
+  }
+  count_launch(ctx, 2);
+  SsspArgs A;
+  A.n = n;
+  A.off = G.off; A.deg = G.deg; A.col = G.col; A.w = G.w;
+  A.dist = dist; A.stamp = stamp; A.fstamp = fstamp;
+  A.nq[0] = q0; A.nq[1] = q1; A.nq[2] = q2;
+  A.fq[0] = far; A.fq[1] = far2;
+  A.ctl = ctl;
+  A.cnt = cnt;
+  A.delta = auto_delta(ctx);
+  A.iter_base = 1;
+  A.fcap = fcap;
+  A.spin_limit = 40ll * 1000 * 1000;
+  uint32_t h_ctl[S_WORDS];
+  sg_status rs = sssp_launch_args(ctx, A, h_ctl);
+  if (rs == SG_OK && h_cnt)
+    SG_CUDA(ctx, cudaMemcpy(h_cnt, cnt, sizeof(unsigned long long) * SC_WORDS, cudaMemcpyDeviceToHost));
+  dfree(stamp); dfree(fstamp); dfree(reset); dfree(q0); dfree(q1); dfree(q2);
+  dfree(far); dfree(far2); dfree(ctl); dfree(cnt); dfree(sv); dfree(sd);
+  return rs;
 }
 
 sg_status sssp_compute_parents(sg_ctx* ctx) {
@@ -542,6 +614,38 @@ sg_status sssp_run_peval(sg_ctx* ctx, uint32_t source) {
   float ms = 0.f;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   fill_stats(ctx, h_cnt);
+  ctx->stats.elapsed_ms = ms;
+  ctx->stats.rounds = 0;
+  ctx->stats.converged = 1;
+  ctx->stats.reset_vertices = 0;
+  s.valid = true;
+  s.has_pending = false;
+  return SG_OK;
+}
+
+// A PEval whose distances are computed elsewhere (the summarized graph):
+// buffers and tags as sssp_run_peval sets them, distances left to the caller.
+sg_status sssp_prepare_external(sg_ctx* ctx, uint32_t source) {
+  DevGraph& g = ctx->g;
+  if (!g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
+  if (!g.weighted) return fail(ctx, SG_ERR_INVALID, "SSSP needs a weighted graph");
+  if (source >= g.n) return fail(ctx, SG_ERR_INVALID, "source >= n");
+  SG_TRY(sssp_alloc(ctx));
+  SsspState& s = ctx->sp;
+  s.source = source;
+  s.delta_width = auto_delta(ctx);
+  s.iter_base = 1;
+  k_sssp_init<<<grid_for(g.n, 256), 256, 0, ctx->stream>>>(g.n, s.dist, s.stamp, s.fstamp, s.reset);
+  count_launch(ctx);
+  SG_CUDA(ctx, cudaGetLastError());
+  return SG_OK;
+}
+
+sg_status sssp_finish_external(sg_ctx* ctx, const unsigned long long* h_cnt, float ms) {
+  SsspState& s = ctx->sp;
+  SG_TRY(sssp_compute_parents(ctx));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (h_cnt) fill_stats(ctx, h_cnt);
   ctx->stats.elapsed_ms = ms;
   ctx->stats.rounds = 0;
   ctx->stats.converged = 1;

@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <unordered_map>
 
 #include "ctx.h"
@@ -64,6 +65,17 @@ struct SummaryDev {
   float *bound = nullptr, *spnode = nullptr, *old_x = nullptr;
   double* d_res = nullptr;
   std::vector<uint32_t> pending_clusters;  // touched since the last IncEval
+  // SSSP over the summary: shortcut distances per supernode (entry -> exit /
+  // out-mirror, entry -> inner member), the summarized CSR and the
+  // correction lists; built on first use, repaired after each batch
+  bool sssp_ready = false;
+  std::vector<std::vector<std::pair<uint32_t, double>>> sp_bound_d, sp_inner_d;
+  uint64_t *sk_off = nullptr, *sk_coff = nullptr;
+  uint32_t *sk_deg = nullptr, *sk_col = nullptr, *sk_crow = nullptr, *sk_cv = nullptr;
+  float *sk_w = nullptr, *sk_cd = nullptr;
+  uint64_t sk_m = 0;
+  uint32_t sk_ncorr = 0;
+  bool sk_stale = true;
 };
 
 static SummaryDev* sdev(sg_ctx* ctx) { return (SummaryDev*)ctx->summary; }
@@ -79,6 +91,8 @@ static void sfree(SummaryDev& D) {
   dfree(D.cm_off); dfree(D.sub_off); dfree(D.cm_v); dfree(D.sub_nbr);
   dfree(D.bound_list); dfree(D.bl_off);
   dfree(D.bound); dfree(D.spnode); dfree(D.old_x); dfree(D.d_res);
+  dfree(D.sk_off); dfree(D.sk_coff); dfree(D.sk_deg); dfree(D.sk_col); dfree(D.sk_crow);
+  dfree(D.sk_cv); dfree(D.sk_w); dfree(D.sk_cd);
 }
 
 sg_status summary_free(sg_ctx* ctx) {
@@ -401,6 +415,8 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return SG_OK;
 }
+
+static sg_status sssp_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector<uint32_t>& spids);
 
 // ------------------------------------------------------ build entry point
 
@@ -833,6 +849,15 @@ sg_status summary_after_apply(sg_ctx* ctx) {
   summary_node_types(S);
   summary_sketch_csr(S, D->out);
   SG_TRY(upload_sketch(ctx, *D));
+  if (D->sssp_ready && ctx->g.weighted) {
+    // shortcut distances of the touched supernodes; new supernodes get theirs
+    if (D->sp_bound_d.size() < S.supernodes.size()) {
+      D->sp_bound_d.resize(S.supernodes.size());
+      D->sp_inner_d.resize(S.supernodes.size());
+    }
+    SG_TRY(sssp_shortcuts(ctx, *D, sps));
+  }
+  D->sk_stale = true;
   return SG_OK;
 }
 
@@ -867,6 +892,341 @@ sg_status summary_info(sg_ctx* ctx, sg_summary_info* o) {
   for (uint32_t v = 0; v < S.old_n; ++v)
     if (S.node_type[v] >= 0 && S.node_type[v] < 7) o->node_type_count[(int)S.node_type[v]]++;
   return SG_OK;
+}
+
+// ================================================== SSSP over the summary
+//
+// The summarized traversal of SumSyncTraversalWorker (sum_sync_traversal_worker.h:
+// 1097-1233, correction :1322-1403) with the shortcuts of TravCompressor
+// (build_trav_index_mirror / run_to_convergence_mirror /
+// fianl_build_trav_index_mirror, trav_compressor.h:244-430): for every
+// supernode, the shortest distances inside its cluster from its entry (or
+// in-mirror) to the exits and out-mirrors (bound shortcuts) and to the other
+// members (inner shortcuts).  The summarized graph has one row per vertex and
+// mirror: entries carry their bound shortcuts, exits and unclustered vertices
+// their edges out of the cluster, masters a 0-weight edge to their in-mirrors,
+// out-mirrors one to their master; inner members have no row.  Delta-stepping
+// over it gives every non-inner vertex its exact distance (a shortest path
+// enters a cluster through an entry and leaves through an exit); the
+// correction then sets each inner member to the smallest entry distance plus
+// inner shortcut.  A source inside a cluster is first expanded inside its
+// cluster and seeds the run with its exits and members.
+
+// One CTA per job: Bellman-Ford inside the cluster from the job's source,
+// distances as ordered bits in shared memory.
+__global__ void __launch_bounds__(128) k_sssp_shortcuts(const uint32_t* __restrict__ job_cl,
+                                                        const uint32_t* __restrict__ job_src,
+                                                        const uint64_t* __restrict__ cl_off,
+                                                        const uint64_t* __restrict__ adj_off,
+                                                        const uint32_t* __restrict__ adj_nbr,
+                                                        const float* __restrict__ adj_w,
+                                                        const uint64_t* __restrict__ out_off,
+                                                        double* __restrict__ out, uint32_t njobs) {
+  extern __shared__ unsigned long long sd[];
+  __shared__ int s_changed;
+  const uint32_t j = blockIdx.x;
+  if (j >= njobs) return;
+  const uint32_t c = job_cl[j];
+  const uint64_t l0 = cl_off[c];
+  const uint32_t L = (uint32_t)(cl_off[c + 1] - l0);
+  const uint32_t src = job_src[j];
+  for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) sd[i] = i == src ? 0ull : kInfBits;
+  __syncthreads();
+  for (uint32_t round = 0; round <= L; ++round) {
+    if (threadIdx.x == 0) s_changed = 0;
+    __syncthreads();
+    int changed = 0;
+    for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) {
+      const unsigned long long di = sd[i];
+      if (di >= kInfBits) continue;
+      const double dv = bitsd(di);
+      for (uint64_t e = adj_off[l0 + i]; e < adj_off[l0 + i + 1]; ++e) {
+        const unsigned long long cb = dbits(dv + (double)adj_w[e]);
+        const uint32_t t = adj_nbr[e];
+        if (cb < sd[t] && cb < atomicMin(&sd[t], cb)) changed = 1;
+      }
+    }
+    if (changed) s_changed = 1;
+    __syncthreads();
+    const int any = s_changed;
+    __syncthreads();
+    if (!any) break;
+  }
+  const uint64_t o = out_off[j];
+  for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) out[o + i] = bitsd(sd[i]);
+}
+
+// Runs one shortcut job per (cluster, local source) pair; dist[j] gets the
+// local distances of job j in the order of cluster_ids.
+static sg_status sssp_cluster_jobs(sg_ctx* ctx, SummaryDev& D,
+                                   const std::vector<std::pair<uint32_t, uint32_t>>& jobs,
+                                   std::vector<std::vector<double>>* dist) {
+  Summary& S = D.S;
+  dist->assign(jobs.size(), {});
+  if (jobs.empty()) return SG_OK;
+  if (S.subgraph_w.empty() && !S.subgraph.empty())
+    return fail(ctx, SG_ERR_INVALID, "SSSP over the summary needs edge weights");
+  std::unordered_map<uint32_t, uint32_t> cl_index;
+  std::vector<uint32_t> cls;
+  for (auto& jb : jobs)
+    if (cl_index.emplace(jb.first, (uint32_t)cls.size()).second) cls.push_back(jb.first);
+  std::vector<uint64_t> cl_off(cls.size() + 1, 0), adj_off(1, 0);
+  std::vector<uint32_t> adj_nbr;
+  std::vector<float> adj_w;
+  std::vector<uint32_t> local_of(S.all_n, 0xFFFFFFFFu);
+  size_t maxL = 1;
+  for (size_t k = 0; k < cls.size(); ++k) {
+    const auto& nodes = S.cluster_ids[cls[k]];
+    for (uint32_t i = 0; i < nodes.size(); ++i) local_of[nodes[i]] = i;
+    for (uint32_t v : nodes) {
+      const auto& nb = S.subgraph[v];
+      const auto& wt = S.subgraph_w[v];
+      for (size_t e = 0; e < nb.size(); ++e) {
+        if (local_of[nb[e]] == 0xFFFFFFFFu) continue;
+        adj_nbr.push_back(local_of[nb[e]]);
+        adj_w.push_back(wt[e]);
+      }
+      adj_off.push_back(adj_nbr.size());
+    }
+    cl_off[k + 1] = cl_off[k] + nodes.size();
+    maxL = std::max(maxL, nodes.size());
+    for (uint32_t v : nodes) local_of[v] = 0xFFFFFFFFu;
+  }
+  std::vector<uint32_t> job_cl(jobs.size()), job_src(jobs.size());
+  std::vector<uint64_t> out_off(jobs.size() + 1, 0);
+  for (size_t j = 0; j < jobs.size(); ++j) {
+    const uint32_t k = cl_index[jobs[j].first];
+    job_cl[j] = k;
+    job_src[j] = jobs[j].second;
+    out_off[j + 1] = out_off[j] + (cl_off[k + 1] - cl_off[k]);
+  }
+  const size_t smem = maxL * sizeof(unsigned long long);
+  if (smem > 200 * 1024) return fail(ctx, SG_ERR_UNSUPPORTED, "cluster too large for the shortcut kernel");
+  uint32_t *d_cl = nullptr, *d_src = nullptr, *d_nbr = nullptr;
+  uint64_t *d_cloff = nullptr, *d_adjoff = nullptr, *d_outoff = nullptr;
+  float* d_w = nullptr;
+  double* d_out = nullptr;
+  SG_TRY(upload(ctx, &d_cl, job_cl));
+  SG_TRY(upload(ctx, &d_src, job_src));
+  SG_TRY(upload(ctx, &d_nbr, adj_nbr));
+  SG_TRY(upload(ctx, &d_w, adj_w));
+  SG_TRY(upload(ctx, &d_cloff, cl_off));
+  SG_TRY(upload(ctx, &d_adjoff, adj_off));
+  SG_TRY(upload(ctx, &d_outoff, out_off));
+  SG_TRY(dalloc(ctx, &d_out, std::max<uint64_t>(out_off.back(), 1)));
+  if (smem > 48 * 1024)
+    SG_CUDA(ctx, cudaFuncSetAttribute(k_sssp_shortcuts, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  kprof_begin(ctx);
+  k_sssp_shortcuts<<<(unsigned)jobs.size(), 128, smem, ctx->stream>>>(
+      d_cl, d_src, d_cloff, d_adjoff, d_nbr, d_w, d_outoff, d_out, (uint32_t)jobs.size());
+  kprof_end(ctx, SG_K_SUMMARY);
+  SG_CUDA(ctx, cudaGetLastError());
+  std::vector<double> all(out_off.back());
+  SG_CUDA(ctx, cudaMemcpyAsync(all.data(), d_out, 8 * all.size(), cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  dfree(d_cl); dfree(d_src); dfree(d_nbr); dfree(d_w); dfree(d_cloff); dfree(d_adjoff);
+  dfree(d_outoff); dfree(d_out);
+  for (size_t j = 0; j < jobs.size(); ++j)
+    (*dist)[j].assign(all.begin() + out_off[j], all.begin() + out_off[j + 1]);
+  return SG_OK;
+}
+
+static bool is_out_mirror(const Summary& S, uint32_t c, uint32_t v) {
+  const auto& om = S.cluster_out_mirror_ids[c];
+  return v >= S.old_n && std::find(om.begin(), om.end(), v) != om.end();
+}
+
+static uint32_t local_index(const std::vector<uint32_t>& nodes, uint32_t v) {
+  for (uint32_t i = 0; i < nodes.size(); ++i)
+    if (nodes[i] == v) return i;
+  return 0;
+}
+
+// Bound and inner shortcut distances of the given supernodes
+// (fianl_build_trav_index_mirror, trav_compressor.h:366-430).
+static sg_status sssp_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector<uint32_t>& spids) {
+  Summary& S = D.S;
+  D.sp_bound_d.resize(S.supernodes.size());
+  D.sp_inner_d.resize(S.supernodes.size());
+  std::vector<std::pair<uint32_t, uint32_t>> jobs;
+  std::vector<uint32_t> jsp;
+  for (uint32_t sp : spids) {
+    const Supernode& n = S.supernodes[sp];
+    D.sp_bound_d[sp].clear();
+    D.sp_inner_d[sp].clear();
+    if (n.id == Summary::kIdDefault) continue;
+    jobs.push_back({n.ids, local_index(S.cluster_ids[n.ids], n.id)});
+    jsp.push_back(sp);
+  }
+  std::vector<std::vector<double>> dist;
+  SG_TRY(sssp_cluster_jobs(ctx, D, jobs, &dist));
+  const double inf = std::numeric_limits<double>::infinity();
+  for (size_t j = 0; j < jobs.size(); ++j) {
+    const uint32_t sp = jsp[j];
+    const uint32_t c = S.supernodes[sp].ids;
+    const auto& nodes = S.cluster_ids[c];
+    const uint32_t inner = (uint32_t)S.supernode_ids[c].size();
+    for (uint32_t i = 0; i < nodes.size(); ++i) {
+      const double d = dist[j][i];
+      if (!(d < inf)) continue;
+      const uint32_t v = nodes[i];
+      if (i >= inner) {
+        if (is_out_mirror(S, c, v))
+          D.sp_bound_d[sp].push_back({S.mirror_master(v), d});  // out-mirror: its master
+      } else if (S.out_bound[v]) {
+        D.sp_bound_d[sp].push_back({v, d});
+      } else {
+        D.sp_inner_d[sp].push_back({v, d});
+      }
+    }
+  }
+  D.sk_stale = true;
+  return SG_OK;
+}
+
+// The summarized CSR (padded to quads) and the correction lists.
+static sg_status sssp_sketch(sg_ctx* ctx, SummaryDev& D) {
+  Summary& S = D.S;
+  const HostAdj& out = D.out;
+  const uint32_t all = S.all_n, n = S.old_n;
+  std::vector<std::vector<std::pair<uint32_t, float>>> rows(all);
+  for (size_t i = 0; i < S.cluster_in_mirror_ids.size(); ++i)
+    for (uint32_t m : S.cluster_in_mirror_ids[i]) rows[S.mirror_master(m)].push_back({m, 0.f});
+  for (uint32_t sp = 0; sp < S.supernodes.size(); ++sp) {
+    const Supernode& nd = S.supernodes[sp];
+    if (nd.id == Summary::kIdDefault || sp >= D.sp_bound_d.size()) continue;
+    for (auto& e : D.sp_bound_d[sp]) rows[nd.id].push_back({e.first, (float)e.second});
+  }
+  for (uint32_t u = 0; u < n; ++u)
+    for (uint64_t e = S.ib_off[u]; e < S.ib_off[u + 1]; ++e)
+      rows[u].push_back({S.ib_nbr[e], S.ib_w.empty() ? 1.f : S.ib_w[e]});
+  std::vector<uint64_t> off(all);
+  std::vector<uint32_t> deg(all);
+  uint64_t pos = 0;
+  for (uint32_t u = 0; u < all; ++u) {
+    off[u] = pos;
+    deg[u] = (uint32_t)rows[u].size();
+    pos += (deg[u] + 3u) & ~3u;
+  }
+  std::vector<uint32_t> col(pos + 4, 0);
+  std::vector<float> w(pos + 4, 0.f);
+  for (uint32_t u = 0; u < all; ++u)
+    for (uint32_t k = 0; k < deg[u]; ++k) {
+      col[off[u] + k] = rows[u][k].first;
+      w[off[u] + k] = rows[u][k].second;
+    }
+  std::vector<uint64_t> coff(1, 0);
+  std::vector<uint32_t> crow, cv;
+  std::vector<float> cd;
+  for (uint32_t sp = 0; sp < S.supernodes.size(); ++sp) {
+    const Supernode& nd = S.supernodes[sp];
+    if (nd.id == Summary::kIdDefault || sp >= D.sp_inner_d.size() || D.sp_inner_d[sp].empty()) continue;
+    crow.push_back(nd.id);
+    for (auto& e : D.sp_inner_d[sp]) {
+      cv.push_back(e.first);
+      cd.push_back((float)e.second);
+    }
+    coff.push_back(cv.size());
+  }
+  SG_TRY(upload(ctx, &D.sk_off, off));
+  SG_TRY(upload(ctx, &D.sk_deg, deg));
+  SG_TRY(upload(ctx, &D.sk_col, col));
+  SG_TRY(upload(ctx, &D.sk_w, w));
+  SG_TRY(upload(ctx, &D.sk_coff, coff));
+  SG_TRY(upload(ctx, &D.sk_crow, crow));
+  SG_TRY(upload(ctx, &D.sk_cv, cv));
+  SG_TRY(upload(ctx, &D.sk_cd, cd));
+  D.sk_m = pos;
+  D.sk_ncorr = (uint32_t)crow.size();
+  D.sk_stale = false;
+  return SG_OK;
+}
+
+// inner member <- min over its cluster's entries of entry distance + shortcut
+__global__ void k_sssp_correct(uint32_t nrows, const uint64_t* __restrict__ coff,
+                               const uint32_t* __restrict__ crow, const uint32_t* __restrict__ cv,
+                               const float* __restrict__ cd, unsigned long long* dist) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint64_t wv = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; wv < nrows;
+       wv += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+    const unsigned long long de = dist[crow[wv]];
+    if (de >= kInfBits) continue;
+    const double d0 = bitsd(de);
+    for (uint64_t e = coff[wv] + lane; e < coff[wv + 1]; e += 32)
+      atomicMin(dist + cv[e], dbits(d0 + (double)cd[e]));
+  }
+}
+
+__global__ void k_copy_u64(const unsigned long long* a, uint64_t n, unsigned long long* b) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    b[i] = a[i];
+}
+
+sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
+  SummaryDev* Dp = sdev(ctx);
+  if (!Dp || !Dp->valid) return fail(ctx, SG_ERR_STATE, "compress=1 needs sg_summary_build first");
+  SummaryDev& D = *Dp;
+  Summary& S = D.S;
+  if (!ctx->g.weighted) return fail(ctx, SG_ERR_INVALID, "SSSP needs a weighted graph");
+  if (source >= S.old_n) return fail(ctx, SG_ERR_INVALID, "source >= n");
+  cudaStream_t st = ctx->stream;
+  SG_CUDA(ctx, cudaEventRecord(ctx->kev0, st));
+  if (!D.sssp_ready) {
+    std::vector<uint32_t> all_sp(S.supernodes.size());
+    for (uint32_t i = 0; i < all_sp.size(); ++i) all_sp[i] = i;
+    SG_TRY(sssp_shortcuts(ctx, D, all_sp));
+    D.sssp_ready = true;
+  }
+  if (D.sk_stale) SG_TRY(sssp_sketch(ctx, D));
+  // seeds: the source, expanded inside its cluster when it is a member
+  std::vector<uint32_t> seeds;
+  std::vector<double> sdist;
+  const uint32_t c = S.id2spids[source];
+  if (c != Summary::kIdDefault && c < S.cluster_ids.size()) {
+    std::vector<std::vector<double>> dist;
+    const auto& nodes = S.cluster_ids[c];
+    SG_TRY(sssp_cluster_jobs(ctx, D, {{c, local_index(nodes, source)}}, &dist));
+    const double inf = std::numeric_limits<double>::infinity();
+    for (uint32_t i = 0; i < nodes.size(); ++i) {
+      if (!(dist[0][i] < inf)) continue;
+      const uint32_t v = nodes[i];
+      if (v < S.old_n) {
+        seeds.push_back(v);
+      } else if (is_out_mirror(S, c, v)) {
+        seeds.push_back(S.mirror_master(v));
+      } else {
+        continue;
+      }
+      sdist.push_back(dist[0][i]);
+    }
+  } else {
+    seeds.push_back(source);
+    sdist.push_back(0.0);
+  }
+  SG_TRY(sssp_prepare_external(ctx, source));
+  unsigned long long* dist = nullptr;
+  SG_TRY(dalloc(ctx, &dist, S.all_n));
+  SsspView G{S.all_n, D.sk_m, D.sk_off, D.sk_deg, D.sk_col, D.sk_w};
+  unsigned long long h_cnt[4] = {0, 0, 0, 0};
+  sg_status rs = sssp_run_view(ctx, G, seeds.data(), sdist.data(), (uint32_t)seeds.size(), dist, h_cnt);
+  if (rs != SG_OK) {
+    dfree(dist);
+    return rs;
+  }
+  if (D.sk_ncorr)
+    k_sssp_correct<<<grid_for((uint64_t)D.sk_ncorr * 32, 256), 256, 0, st>>>(
+        D.sk_ncorr, D.sk_coff, D.sk_crow, D.sk_cv, D.sk_cd, dist);
+  k_copy_u64<<<grid_for(S.old_n, 256), 256, 0, st>>>(dist, S.old_n, ctx->sp.dist);
+  count_launch(ctx, 2);
+  SG_CUDA(ctx, cudaGetLastError());
+  SG_CUDA(ctx, cudaEventRecord(ctx->kev1, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->kev0, ctx->kev1);
+  dfree(dist);
+  return sssp_finish_external(ctx, h_cnt, ms);
 }
 
 }  // namespace sg

@@ -99,3 +99,21 @@ def test_invalid_update_is_rejected(ctx):
     assert e.value.status == sg.SG_ERR_INVALID
     r2, c2, _ = ctx.download_csr()
     assert np.array_equal(c2, col)
+
+
+def test_pool_repacks_under_many_inserts():
+    """No slack and insert-heavy batches: segments keep moving to the pool
+    tail until a batch no longer fits and the direction is repacked; the
+    graph and the incremental SSSP stay exact throughout."""
+    with sg.Context(0, slack=0.0) as ctx:
+        ctx.generate_rmat(10, 4000, seed=3, weight_kind=1)
+        rp, col, w = ctx.download_csr()
+        hg = sg.HostGraph(rp, col, w)
+        ctx.sssp_peval(0, out=False)
+        for i in range(12):
+            ctx.apply_updates(hg.gen_updates(3000, 200, 100, seed=10 + i))
+            nrp, ncol, nw = hg.csr()
+            drp, dcol, dw = ctx.download_csr()
+            assert np.array_equal(drp, nrp) and np.array_equal(dcol, ncol)
+            assert np.array_equal(dw, nw)
+            assert np.array_equal(ctx.sssp_inceval(), oracle.dijkstra(nrp, ncol, nw, 0))

@@ -90,3 +90,29 @@ def test_plain_pagerank_and_sssp_match_reference(name):
         # exact distances: the reference's Ingress traversal worker (its
         # summarized worker deviates on planted2600, see test_cpu_golden)
         assert np.array_equal(d2, fx["ref_sssp_plain_inc"])
+
+
+@pytest.mark.parametrize("name,source", [("rmat12", 0), ("planted2600", 0), ("planted2600", 5),
+                                         ("planted2600", 2500)])
+def test_summarized_sssp_is_exact(name, source):
+    """SSSP over the summary (shortcut distances, summarized delta-stepping,
+    inner correction) equals Dijkstra; also for a source inside a cluster."""
+    fx = load(name)
+    rp, col, w = fx["row_ptr"], fx["col"], fx["w"]
+    with sg.Context(0, compress=1) as ctx:
+        ctx.load_csr(rp, col, w)
+        ctx.summary_build(fx["clusters"])
+        d = ctx.sssp_peval(source)
+        assert np.array_equal(d, oracle.dijkstra(rp, col, w, source))
+        if source == 0:
+            assert np.array_equal(d, fx["ref_sssp_sum_peval"])
+        # IncEval after the batch, then a fresh summarized PEval on the
+        # repaired summary
+        ctx.apply_updates(fx["updates_sssp"])
+        nrp, ncol, nw = oracle.apply_updates_reference(rp, col, w, fx["updates_sssp"])
+        d_new = oracle.dijkstra(nrp, ncol, nw, source)
+        assert np.array_equal(ctx.sssp_inceval(), d_new)
+        assert np.array_equal(ctx.sssp_peval(source), d_new)
+        parents = ctx.sssp_parents()
+        reach = np.isfinite(d_new) & (np.arange(len(d_new)) != source)
+        assert np.all(parents[reach] < len(d_new))
