@@ -752,6 +752,7 @@ def run_sssp(args, D: Dist):
                    "batch_changes": 100000, "batch_mix": "40% insert / 40% delete / 20% re-weight",
                    "summary": "plain graph (no cluster file at this scale)",
                    "l2": "graph larger than L2, no flush", "parallelism": "single GPU"},
+        "graph_gteps": round(E * K / (t_ms * 1e-3) / 1e9, 4),
         "reset_vertices_per_step": resets,
         "peval_ms": round(pe["elapsed_ms"], 3),
         "exact_vs_dijkstra": exact,

@@ -399,6 +399,13 @@ sg_status sg_graph_set_vertex_oids(sg_ctx* ctx, const uint64_t* oids);
 /* Applies an update file ("a u v [w]" / "d u v" lines, oids;
  * grape/fragment/inc_fragment_builder.h:38-70) as one batch. */
 sg_status sg_apply_update_file(sg_ctx* ctx, const char* path);
+/* Saves / loads the summary's cluster state in the reference's serialized
+ * layout (serialize_cluster / de_serialize_cluster, compressor_base.h:
+ * 2987-3158): the supernode candidates and mirrors chosen from the
+ * clustering, so a later run on the same graph skips that step.  Loading
+ * rebuilds everything after it (exits, subgraphs, shortcuts, sketch). */
+sg_status sg_summary_save(sg_ctx* ctx, const char* path);
+sg_status sg_summary_load(sg_ctx* ctx, const char* path);
 /* sg_summary_build from a cluster file (records "size oid_1 ... oid_size",
  * the <efile>.c_<max_node_num> file of compressor_base.h:3174-3243). */
 sg_status sg_summary_build_file(sg_ctx* ctx, const char* path);
@@ -447,6 +454,15 @@ sg_status sg_util_greedy_clusters(uint32_t n, const uint64_t* row_ptr,
                                   uint32_t* n_clusters);
 
 /* Packed copy of the mirror (rows sorted). */
+/* The summary's cluster state for a clustering, in the reference's
+ * serialized layout (as sg_summary_save writes it), computed on the host.
+ * out: buffer of *size bytes or NULL (then only *size is set). */
+sg_status sg_util_summary_serialize(uint32_t n, const uint64_t* row_ptr,
+                                    const uint32_t* col, uint32_t n_clusters,
+                                    const uint32_t* cluster_ptr,
+                                    const uint32_t* members, int min_node_num,
+                                    int mirror_k, double compress_threshold,
+                                    uint8_t* out, uint64_t* size);
 sg_status sg_hostgraph_num_edges(const sg_hostgraph* g, uint64_t* m);
 sg_status sg_hostgraph_csr(const sg_hostgraph* g, uint64_t* row_ptr,
                            uint32_t* col, float* w);

@@ -209,6 +209,8 @@ _SIGS = {
     "sg_graph_set_vertex_oids": ([_P, _P], C.c_int),
     "sg_apply_update_file": ([_P, C.c_char_p], C.c_int),
     "sg_summary_build_file": ([_P, C.c_char_p], C.c_int),
+    "sg_summary_save": ([_P, C.c_char_p], C.c_int),
+    "sg_summary_load": ([_P, C.c_char_p], C.c_int),
     "sg_pr_weighted": ([_P, _P, _P], C.c_int),
     "sg_graph_normalize_weights": ([_P], C.c_int),
     "sg_pr_adjoint": ([_P, _P, _P, _P], C.c_int),
@@ -221,6 +223,8 @@ _SIGS = {
     "sg_batch_query_stats": ([_P, _P, _P], C.c_int),
     "sg_batch_outputs_device": ([_P, C.POINTER(_P), C.POINTER(_P)], C.c_int),
     "sg_summary_info_get": ([_P, C.POINTER(SummaryInfo)], C.c_int),
+    "sg_util_summary_serialize": ([C.c_uint32, _P, _P, C.c_uint32, _P, _P, C.c_int, C.c_int,
+                                   C.c_double, _P, C.POINTER(C.c_uint64)], C.c_int),
     "sg_util_greedy_clusters": ([C.c_uint32, _P, _P, C.c_int, C.c_int, C.c_uint64, _P, _P,
                                  C.POINTER(C.c_uint32)], C.c_int),
 }
@@ -421,6 +425,12 @@ class Context:
     def apply_update_file(self, path):
         _check(self._lib.sg_apply_update_file(self._h, path.encode()), self, "sg_apply_update_file")
 
+    def summary_save(self, path):
+        _check(self._lib.sg_summary_save(self._h, path.encode()), self, "sg_summary_save")
+
+    def summary_load(self, path):
+        _check(self._lib.sg_summary_load(self._h, path.encode()), self, "sg_summary_load")
+
     def summary_build_file(self, path):
         _check(self._lib.sg_summary_build_file(self._h, path.encode()), self,
                "sg_summary_build_file")
@@ -522,6 +532,29 @@ def rmat_host(scale, edges, a=0.57, b=0.19, c=0.19, seed=1, weight_kind=0, wlo=1
     _check(lib.sg_util_rmat_host(scale, edges, a, b, c, seed, weight_kind, wlo, whi, _ptr(rp),
                                  _ptr(col), _ptr(w)), None, "sg_util_rmat_host")
     return rp, col, w
+
+
+def summary_serialize_host(row_ptr, col, clusters, min_node_num=8, mirror_k=4,
+                           compress_threshold=1.0) -> bytes:
+    """The summary's cluster state in the reference's serialized layout,
+    computed on the host (no GPU)."""
+    lib = load_library()
+    rp = np.ascontiguousarray(row_ptr, np.uint64)
+    col = np.ascontiguousarray(col, np.uint32)
+    cp = np.zeros(len(clusters) + 1, np.uint32)
+    for i, c in enumerate(clusters):
+        cp[i + 1] = cp[i] + len(c)
+    mem = (np.concatenate([np.asarray(c, np.uint32) for c in clusters])
+           if len(clusters) else np.zeros(1, np.uint32))
+    size = C.c_uint64(0)
+    args = (len(rp) - 1, _ptr(rp), _ptr(col), len(clusters), _ptr(cp), _ptr(mem), min_node_num,
+            mirror_k, compress_threshold)
+    _check(lib.sg_util_summary_serialize(*args, None, C.byref(size)), None,
+           "sg_util_summary_serialize")
+    buf = np.zeros(size.value, np.uint8)
+    _check(lib.sg_util_summary_serialize(*args, _ptr(buf), C.byref(size)), None,
+           "sg_util_summary_serialize")
+    return buf.tobytes()
 
 
 def greedy_clusters(row_ptr, col, max_node_num=150, min_node_num=8, seed=1):

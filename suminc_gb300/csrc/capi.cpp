@@ -618,6 +618,43 @@ sg_status sg_apply_update_file(sg_ctx* ctx, const char* path) {
   SG_CATCH(ctx)
 }
 
+sg_status sg_summary_save(sg_ctx* ctx, const char* path) {
+  SG_GUARD(ctx);
+  if (!path) return fail(ctx, SG_ERR_INVALID, "null path");
+  try {
+    std::vector<uint8_t> blob;
+    sg_status st = summary_serialized(ctx, &blob);
+    if (st != SG_OK) return st;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(ctx, SG_ERR_INVALID, std::string("cannot write ") + path);
+    const size_t wr = std::fwrite(blob.data(), 1, blob.size(), f);
+    std::fclose(f);
+    if (wr != blob.size()) return fail(ctx, SG_ERR_INVALID, std::string("short write to ") + path);
+    return SG_OK;
+  }
+  SG_CATCH(ctx)
+}
+
+sg_status sg_summary_load(sg_ctx* ctx, const char* path) {
+  SG_GUARD(ctx);
+  if (!path) return fail(ctx, SG_ERR_INVALID, "null path");
+  if (!ctx->g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
+  try {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(ctx, SG_ERR_INVALID, std::string("cannot read ") + path);
+    std::vector<uint8_t> blob;
+    uint8_t buf[1 << 16];
+    size_t got;
+    while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0) blob.insert(blob.end(), buf, buf + got);
+    std::fclose(f);
+    pr_free(ctx);
+    sg_status st = summary_build_serialized(ctx, blob);
+    kprof_flush(ctx);
+    return st;
+  }
+  SG_CATCH(ctx)
+}
+
 sg_status sg_summary_build_file(sg_ctx* ctx, const char* path) {
   SG_GUARD(ctx);
   if (!path) return fail(ctx, SG_ERR_INVALID, "null cluster file name");

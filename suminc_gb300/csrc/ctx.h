@@ -321,6 +321,9 @@ sg_status batch_device_outputs(sg_ctx* ctx, const float** ppr, const double** ss
 sg_status summary_free(sg_ctx* ctx);
 sg_status summary_build(sg_ctx* ctx, const std::vector<std::vector<uint32_t>>& clusters);
 sg_status summary_after_apply(sg_ctx* ctx);
+// the reference's serialized cluster state (serialize_cluster layout)
+sg_status summary_build_serialized(sg_ctx* ctx, const std::vector<uint8_t>& blob);
+sg_status summary_serialized(sg_ctx* ctx, std::vector<uint8_t>* blob);
 sg_status pr_summarized(sg_ctx* ctx, bool inc);
 sg_status sssp_summarized(sg_ctx* ctx, uint32_t source);
 uint32_t summary_rows(sg_ctx* ctx);  // rows incl. mirrors, 0 without a summary

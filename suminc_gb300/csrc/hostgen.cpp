@@ -324,3 +324,39 @@ extern "C" sg_status sg_util_greedy_clusters(uint32_t n, const uint64_t* row_ptr
     return SG_ERR_OOM;
   }
 }
+
+// The summary's cluster state (supernode candidates and mirrors chosen from a
+// clustering) in the reference's serialized layout, computed on the host:
+// lets the construction be compared byte for byte with the reference's
+// serialize_cluster output without a GPU.
+extern "C" sg_status sg_util_summary_serialize(uint32_t n, const uint64_t* row_ptr,
+                                               const uint32_t* col, uint32_t n_clusters,
+                                               const uint32_t* cluster_ptr,
+                                               const uint32_t* members, int min_node_num,
+                                               int mirror_k, double compress_threshold,
+                                               uint8_t* out, uint64_t* size) {
+  if (!row_ptr || !size || n == 0 || (n_clusters && (!cluster_ptr || !members)))
+    return SG_ERR_INVALID;
+  try {
+    HostAdj adj, in;
+    host_adj_from_csr(n, row_ptr, col, nullptr, adj);
+    host_transpose(adj, in);
+    std::vector<std::vector<uint32_t>> cl(n_clusters);
+    for (uint32_t i = 0; i < n_clusters; ++i) {
+      if (cluster_ptr[i + 1] < cluster_ptr[i]) return SG_ERR_INVALID;
+      cl[i].assign(members + cluster_ptr[i], members + cluster_ptr[i + 1]);
+    }
+    Summary S;
+    const uint64_t im = summary_init_by_clusters(S, adj, in, cl, min_node_num, mirror_k,
+                                                 compress_threshold);
+    const std::vector<uint8_t> b = summary_serialize_init(S, im);
+    if (out) {
+      if (*size < b.size()) return SG_ERR_INVALID;
+      std::memcpy(out, b.data(), b.size());
+    }
+    *size = b.size();
+    return SG_OK;
+  } catch (const std::bad_alloc&) {
+    return SG_ERR_OOM;
+  }
+}

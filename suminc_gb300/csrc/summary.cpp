@@ -6,6 +6,7 @@
 #include "summary.h"
 
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 #include <set>
 #include <unordered_map>
@@ -257,9 +258,9 @@ std::vector<std::vector<uint32_t>> greedy_clusters(const HostAdj& out, const Hos
 // mirror selection of get_init_supernode_by_clusters (:3253-3611) and
 // final_build_supernode (:3616-3783).
 
-void summary_from_clusters(Summary& S, const HostAdj& out, const HostAdj& in,
-                           const std::vector<std::vector<uint32_t>>& clusters_in,
-                           int min_node_num, int mirror_k, double compress_threshold) {
+uint64_t summary_init_by_clusters(Summary& S, const HostAdj& out, const HostAdj& in,
+                                  const std::vector<std::vector<uint32_t>>& clusters_in,
+                                  int min_node_num, int mirror_k, double compress_threshold) {
   const uint32_t n = out.n;
   S = Summary();
   S.old_n = n;
@@ -399,9 +400,15 @@ void summary_from_clusters(Summary& S, const HostAdj& out, const HostAdj& in,
     }
   }
 
-  // final_build_supernode
+  return (uint64_t)mirror_node_num;
+}
+
+// final_build_supernode (compressor_base.h:3616-3783) from the state above
+// (or the same state read back from a serialized summary).
+void summary_final_build(Summary& S, const HostAdj& in, uint64_t init_mirror_num) {
+  const uint32_t n = S.old_n;
   S.all_n = n;
-  const uint64_t cap_all = (uint64_t)n + (uint64_t)mirror_node_num;
+  const uint64_t cap_all = (uint64_t)n + init_mirror_num;
   S.Fc_map.assign(cap_all, Summary::kIdDefault);
   S.vid2in_mirror_mids.assign(n, {});
   const uint32_t n_clusters = (uint32_t)S.supernode_ids.size();
@@ -754,6 +761,102 @@ void summary_inc_entries(Summary& S, const HostAdj& new_out, const HostAdj& new_
   std::sort(S.update_cluster_ids.begin(), S.update_cluster_ids.end());
   S.update_source_id.assign(upd_s.begin(), upd_s.end());
   std::sort(S.update_source_id.begin(), S.update_source_id.end());
+}
+
+void summary_from_clusters(Summary& S, const HostAdj& out, const HostAdj& in,
+                           const std::vector<std::vector<uint32_t>>& clusters, int min_node_num,
+                           int mirror_k, double compress_threshold) {
+  const uint64_t m = summary_init_by_clusters(S, out, in, clusters, min_node_num, mirror_k,
+                                              compress_threshold);
+  summary_final_build(S, in, m);
+}
+
+// serialize_cluster / de_serialize_cluster (compressor_base.h:2987-3158):
+// the state between get_init_supernode_by_clusters and final_build_supernode,
+// native-endian: u32 init_mirror_num, u32 clusters; per cluster the member,
+// cluster, source, in-mirror and out-mirror lists as (u32 count, u32 ids...);
+// then Fc (i32) and id2spids (u32) of every vertex; then i32 -1.
+static void put_u32(std::vector<uint8_t>& b, uint32_t x) {
+  const uint8_t* p = reinterpret_cast<const uint8_t*>(&x);
+  b.insert(b.end(), p, p + 4);
+}
+
+template <typename C>
+static void put_list(std::vector<uint8_t>& b, const C& c) {
+  put_u32(b, (uint32_t)c.size());
+  for (uint32_t v : c) put_u32(b, v);
+}
+
+std::vector<uint8_t> summary_serialize_init(const Summary& S, uint64_t init_mirror_num) {
+  std::vector<uint8_t> b;
+  put_u32(b, (uint32_t)init_mirror_num);
+  const uint32_t nc = (uint32_t)S.supernode_ids.size();
+  put_u32(b, nc);
+  for (uint32_t i = 0; i < nc; ++i) {
+    put_list(b, S.supernode_ids[i]);
+    put_list(b, S.cluster_ids[i]);
+    put_list(b, S.supernode_source[i]);
+    put_list(b, S.supernode_in_mirror[i]);
+    put_list(b, S.supernode_out_mirror[i]);
+  }
+  for (uint32_t v = 0; v < S.old_n; ++v) put_u32(b, (uint32_t)S.Fc[v]);
+  for (uint32_t v = 0; v < S.old_n; ++v) put_u32(b, S.id2spids[v]);
+  put_u32(b, 0xFFFFFFFFu);
+  return b;
+}
+
+bool summary_deserialize_init(Summary& S, uint32_t n, const std::vector<uint8_t>& b,
+                              uint64_t* init_mirror_num) {
+  size_t p = 0;
+  auto get = [&](uint32_t* x) {
+    if (p + 4 > b.size()) return false;
+    std::memcpy(x, b.data() + p, 4);
+    p += 4;
+    return true;
+  };
+  auto get_list = [&](std::vector<uint32_t>& out) {
+    uint32_t c = 0;
+    if (!get(&c) || (uint64_t)c * 4 > b.size() - p) return false;
+    out.resize(c);
+    for (uint32_t i = 0; i < c; ++i) {
+      get(&out[i]);
+      if (out[i] >= n) return false;
+    }
+    return true;
+  };
+  S = Summary();
+  S.old_n = n;
+  uint32_t im = 0, nc = 0;
+  if (!get(&im) || !get(&nc)) return false;
+  S.supernode_ids.resize(nc);
+  S.cluster_ids.resize(nc);
+  S.supernode_source.resize(nc);
+  S.supernode_in_mirror.resize(nc);
+  S.supernode_out_mirror.resize(nc);
+  std::vector<uint32_t> tmp;
+  for (uint32_t i = 0; i < nc; ++i) {
+    if (!get_list(S.supernode_ids[i]) || !get_list(S.cluster_ids[i]) ||
+        !get_list(S.supernode_source[i]))
+      return false;
+    if (!get_list(tmp)) return false;
+    S.supernode_in_mirror[i].insert(tmp.begin(), tmp.end());
+    if (!get_list(tmp)) return false;
+    S.supernode_out_mirror[i].insert(tmp.begin(), tmp.end());
+  }
+  S.Fc.resize(n);
+  S.id2spids.resize(n);
+  for (uint32_t v = 0; v < n; ++v) {
+    uint32_t x;
+    if (!get(&x)) return false;
+    S.Fc[v] = (int32_t)x;
+  }
+  for (uint32_t v = 0; v < n; ++v)
+    if (!get(&S.id2spids[v])) return false;
+  uint32_t eof = 0;
+  if (!get(&eof) || eof != 0xFFFFFFFFu || p != b.size()) return false;
+  S.out_bound.assign(n, 0);
+  *init_mirror_num = im;
+  return true;
 }
 
 }  // namespace sg

@@ -76,6 +76,8 @@ struct SummaryDev {
   uint64_t sk_m = 0;
   uint32_t sk_ncorr = 0;
   bool sk_stale = true;
+  // the construction's state between its two halves, serialized
+  std::vector<uint8_t> init_blob;
 };
 
 static SummaryDev* sdev(sg_ctx* ctx) { return (SummaryDev*)ctx->summary; }
@@ -420,7 +422,10 @@ static sg_status sssp_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector<ui
 
 // ------------------------------------------------------ build entry point
 
-sg_status summary_build(sg_ctx* ctx, const std::vector<std::vector<uint32_t>>& clusters) {
+// Shared tail of both builds: host graph copy, then `first_half` fills the
+// state between the construction's halves (from a clustering or a file).
+template <typename FIRST>
+static sg_status summary_build_with(sg_ctx* ctx, FIRST first_half) {
   if (!ctx->g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
   summary_free(ctx);
   SummaryDev* D = new SummaryDev();
@@ -435,8 +440,10 @@ sg_status summary_build(sg_ctx* ctx, const std::vector<std::vector<uint32_t>>& c
   host_adj_from_csr(n, rp.data(), col.data(), ctx->g.weighted ? w.data() : nullptr, D->out);
   host_transpose(D->out, D->in);
   Summary& S = D->S;
-  summary_from_clusters(S, D->out, D->in, clusters, ctx->opt.min_node_num, ctx->opt.mirror_k,
-                        ctx->opt.compress_threshold);
+  uint64_t init_mirrors = 0;
+  SG_TRY(first_half(*D, &init_mirrors));
+  D->init_blob = summary_serialize_init(S, init_mirrors);
+  summary_final_build(S, D->in, init_mirrors);
   summary_judge_out_bound(S, D->out, nullptr);
   summary_build_subgraph(S, D->out, D->in, nullptr);
   std::vector<uint32_t> all_sp(S.supernodes.size());
@@ -448,6 +455,29 @@ sg_status summary_build(sg_ctx* ctx, const std::vector<std::vector<uint32_t>>& c
   D->all_n = S.all_n;
   SG_TRY(upload_sketch(ctx, *D));
   D->valid = true;
+  return SG_OK;
+}
+
+sg_status summary_build(sg_ctx* ctx, const std::vector<std::vector<uint32_t>>& clusters) {
+  return summary_build_with(ctx, [&](SummaryDev& D, uint64_t* im) {
+    *im = summary_init_by_clusters(D.S, D.out, D.in, clusters, ctx->opt.min_node_num,
+                                   ctx->opt.mirror_k, ctx->opt.compress_threshold);
+    return SG_OK;
+  });
+}
+
+sg_status summary_build_serialized(sg_ctx* ctx, const std::vector<uint8_t>& blob) {
+  return summary_build_with(ctx, [&](SummaryDev& D, uint64_t* im) {
+    if (!summary_deserialize_init(D.S, ctx->g.n, blob, im))
+      return fail(ctx, SG_ERR_INVALID, "serialized summary does not fit this graph");
+    return SG_OK;
+  });
+}
+
+sg_status summary_serialized(sg_ctx* ctx, std::vector<uint8_t>* blob) {
+  SummaryDev* D = sdev(ctx);
+  if (!D || !D->valid) return fail(ctx, SG_ERR_STATE, "no summary built");
+  *blob = D->init_blob;
   return SG_OK;
 }
 

@@ -77,6 +77,16 @@ std::vector<std::vector<uint32_t>> greedy_clusters(const HostAdj& out, const Hos
                                                    int max_node_num, int min_node_num,
                                                    uint64_t seed);
 
+// The two halves of the construction: supernode candidates and mirrors from
+// the clustering (returns the mirror count), then the final build.
+uint64_t summary_init_by_clusters(Summary& S, const HostAdj& out, const HostAdj& in,
+                                  const std::vector<std::vector<uint32_t>>& clusters,
+                                  int min_node_num, int mirror_k, double compress_threshold);
+void summary_final_build(Summary& S, const HostAdj& in, uint64_t init_mirror_num);
+// The state between the halves, in the reference's serialized layout.
+std::vector<uint8_t> summary_serialize_init(const Summary& S, uint64_t init_mirror_num);
+bool summary_deserialize_init(Summary& S, uint32_t n, const std::vector<uint8_t>& b,
+                              uint64_t* init_mirror_num);
 // Supernodes, mirrors and bookkeeping from a clustering.
 void summary_from_clusters(Summary& S, const HostAdj& out, const HostAdj& in,
                            const std::vector<std::vector<uint32_t>>& clusters, int min_node_num,

@@ -17,6 +17,8 @@ Each case writes <case>.npz with:
                   sssp_plain_inc              IngressSyncTraversalWorker (compress=0)
   stats         json: counters the reference logged while building its
                 summary (node types, supernodes, mirrors, sketch edges)
+  ref_serialized_summary  the bytes of the reference's serialize_cluster file
+                (written with serialization_cmp_prefix)
 """
 from __future__ import annotations
 
@@ -175,8 +177,16 @@ def make_case(name, rp, col, w, exe, seed, clusters=None):
         write_updates(upd_pr_path, upd_pr, False)
         upd_ss_path = os.path.join(d, "sssp.update")
         write_updates(upd_ss_path, upd_ss, True)
-        res["pr_sum_peval"], log = run_ref(exe, d, "pagerank", REF_FLAGS_PR)
+        ser_dir = os.path.join(d, "ser")
+        os.makedirs(ser_dir)
+        res["pr_sum_peval"], log = run_ref(exe, d, "pagerank",
+                                           dict(REF_FLAGS_PR, serialization_cmp_prefix=ser_dir))
         stats["pr_peval"] = parse_stats(log)
+        ser_files = sorted(os.listdir(ser_dir))
+        if len(ser_files) != 1:
+            raise RuntimeError(f"expected one serialized summary, found {ser_files}")
+        with open(os.path.join(ser_dir, ser_files[0]), "rb") as f:
+            ref_serialized = np.frombuffer(f.read(), dtype=np.uint8)
         res["pr_sum_inc"], log = run_ref(exe, d, "pagerank", REF_FLAGS_PR, upd_pr_path)
         stats["pr_inc"] = parse_stats(log)
         res["pr_plain_inc"], log = run_ref(exe, d, "pagerank_plain", dict(REF_FLAGS_PR, compress="0"),
@@ -198,6 +208,7 @@ def make_case(name, rp, col, w, exe, seed, clusters=None):
                         input_sha256=input_hash(rp, col, w), row_ptr=rp, col=col, w=w,
                         clusters_ptr=cp, clusters_members=mem, updates_pr=upd_pr,
                         updates_sssp=upd_ss, stats=json.dumps(stats),
+                        ref_serialized_summary=ref_serialized,
                         **{f"ref_{k}": v for k, v in res.items()})
     print(name, {k: (len(v), float(np.nansum(np.where(np.isfinite(v), v, 0)))) for k, v in res.items()},
           "clusters", len(clusters))

@@ -83,3 +83,15 @@ def test_greedy_clusters_regenerate():
     cp, mem = fx["clusters_ptr"], fx["clusters_members"]
     ref = [mem[cp[i]:cp[i + 1]] for i in range(len(cp) - 1)]
     assert len(cl) == len(ref) and all(np.array_equal(a, b) for a, b in zip(cl, ref))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_summary_cluster_state_is_byte_identical_to_reference(name):
+    """The supernode candidates and mirrors chosen from the clustering, in
+    the reference's serialize_cluster layout, equal the bytes the reference
+    wrote for the same graph and cluster file."""
+    fx = load(name)
+    cp, mem = fx["clusters_ptr"], fx["clusters_members"]
+    clusters = [mem[cp[i]:cp[i + 1]] for i in range(len(cp) - 1)]
+    ours = sg.summary_serialize_host(fx["row_ptr"], fx["col"], clusters, 8, 4, 1.0)
+    assert ours == fx["ref_serialized_summary"].tobytes()

@@ -116,3 +116,29 @@ def test_summarized_sssp_is_exact(name, source):
         parents = ctx.sssp_parents()
         reach = np.isfinite(d_new) & (np.arange(len(d_new)) != source)
         assert np.all(parents[reach] < len(d_new))
+
+
+@pytest.mark.parametrize("name", ["rmat12", "planted2600"])
+def test_summary_save_and_load_reference_file(name, tmp_path):
+    """sg_summary_save writes the reference's serialized cluster state;
+    loading the reference's own file rebuilds the same summary and values."""
+    fx = load(name)
+    saved = tmp_path / "ours.bin"
+    with sg.Context(0, compress=1) as ctx:
+        ctx.load_csr(fx["row_ptr"], fx["col"])
+        ctx.summary_build(fx["clusters"])
+        info0 = ctx.summary_info()
+        ctx.summary_save(str(saved))
+    assert saved.read_bytes() == fx["ref_serialized_summary"].tobytes()
+    ref_file = tmp_path / "ref.bin"
+    ref_file.write_bytes(fx["ref_serialized_summary"].tobytes())
+    with sg.Context(0, compress=1) as ctx:
+        ctx.load_csr(fx["row_ptr"], fx["col"])
+        ctx.summary_load(str(ref_file))
+        assert ctx.summary_info() == info0
+        x = ctx.pr_peval()
+        assert np.abs(x - fx["ref_pr_sum_peval"]).sum() <= TOL_REF
+        bad = tmp_path / "bad.bin"
+        bad.write_bytes(fx["ref_serialized_summary"].tobytes()[:-4])
+        with pytest.raises(sg.SgError):
+            ctx.summary_load(str(bad))
