@@ -511,6 +511,11 @@ class Context:
         _check(self._lib.sg_sssp_inceval(self._h, _ptr(d)), self, "sg_sssp_inceval")
         return d
 
+    def sssp_distances(self):
+        d = np.empty(self.n, np.float64)
+        _check(self._lib.sg_sssp_distances(self._h, _ptr(d)), self, "sg_sssp_distances")
+        return d
+
     def sssp_parents(self):
         p = np.empty(self.n, np.uint32)
         _check(self._lib.sg_sssp_parents(self._h, _ptr(p)), self, "sg_sssp_parents")

@@ -987,19 +987,9 @@ static sg_status batch_sequence(sg_ctx* ctx, BatchState& B, const BatchArgs& A, 
       A.dist, A.fm_near, A.nl[0], A.ctl + B_NCNT0);
   const int F = A.qw > 128 ? 2 : 1;
   const void* fn = F == 2 ? (const void*)k_batch<2> : (const void*)k_batch<1>;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(bps * ctx->num_sms);
-  cfg.blockDim = dim3(BT);
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeCooperative;
-  attr[0].val.cooperative = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
   BatchArgs a = A;
   void* args[] = {&a};
-  SG_CUDA(ctx, cudaLaunchKernelExC(&cfg, fn, args));
+  SG_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(bps * ctx->num_sms), dim3(BT), args, 0, st));
   if (outputs) {
     if (A.nq > 0) {
       k_ppr_out<<<std::min<uint32_t>((n + 31) / 32, 4096), dim3(32, 32), 0, st>>>(A.X, n, A.qw, A.nq,

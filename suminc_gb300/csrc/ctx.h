@@ -119,8 +119,8 @@ struct SsspState {
   uint32_t* far2 = nullptr;
   uint64_t far_cap = 0;
   uint32_t* reset = nullptr;      // reset marks for IncEval
-  uint32_t* list = nullptr;       // reset vertices of the current IncEval
-  uint32_t* seeds = nullptr;      // reset seeds found by the applier
+  uint32_t* seeds = nullptr;      // reset seeds found by the applier; the
+                                  // reset BFS appends the rest of the list
   uint32_t* seed_cnt = nullptr;   // [0] seeds, [1] BFS level counter
   uint32_t* d_ctl = nullptr;      // control words of the persistent kernel
   unsigned long long* d_cnt = nullptr;
@@ -129,6 +129,13 @@ struct SsspState {
   uint64_t padd_cap = 0;
   uint64_t padd_bound = 0;        // host upper bound of the pending count
   uint32_t iter_base = 1;         // queue tags grow across launches
+  // IncEval: vertices with a changed distance and the parent refresh set
+  uint32_t* chg_mark = nullptr;
+  uint32_t* chg_list = nullptr;
+  uint32_t* par_mark = nullptr;
+  uint32_t* par_list = nullptr;
+  uint32_t* inc_ctl = nullptr;    // [0..3] reset-BFS barrier / next, [4] changed, [5] refresh
+  uint32_t chg_tag = 0;
   bool has_pending = false;       // a batch was applied since the last run
   double delta_width = 0;
 };

@@ -46,7 +46,18 @@ struct SsspArgs {
   uint32_t iter_base;    // stamps start above this value
   uint64_t fcap;         // far queue capacity
   long long spin_limit;
+  // IncEval only (null in PEval): every vertex whose distance improves is
+  // listed once (tag chg_tag) for the parent refresh
+  uint32_t* chg_mark;
+  uint32_t* chg_list;
+  uint32_t* chg_cnt;
+  uint32_t chg_tag;
 };
+
+__device__ __forceinline__ void note_change(const SsspArgs& A, uint32_t x) {
+  if (A.chg_mark && atomicExch(A.chg_mark + x, A.chg_tag) != A.chg_tag)
+    A.chg_list[atomicAdd(A.chg_cnt, 1u)] = x;
+}
 
 __device__ __forceinline__ bool grid_sync(const SsspArgs& A) {
   __syncthreads();
@@ -111,6 +122,7 @@ __device__ __forceinline__ void relax_queue(const SsspArgs& A, const uint32_t* q
             const unsigned long long old = atomicMin(A.dist + x, nb);
             if (nb < old) {
               improve++;
+              note_change(A, x);
               if (nd < thr) {
                 to_near = atomicExch(A.stamp + x, tag) != tag;
               } else {
@@ -258,41 +270,153 @@ __global__ void k_sssp_parents(uint32_t n, uint32_t source, const uint64_t* __re
   }
 }
 
-// Reset BFS over the shortest-path tree: children of reset vertices whose
-// parent is the reset vertex (deltaCompute, sum_sync_traversal_worker.h:
-// 183-226).
-__global__ void k_sssp_reset_step(const uint32_t* __restrict__ cur, uint32_t cn,
-                                  const uint64_t* __restrict__ off, const uint32_t* __restrict__ deg,
-                                  const uint32_t* __restrict__ col,
-                                  const uint32_t* __restrict__ parent, uint32_t* __restrict__ reset,
-                                  uint32_t* __restrict__ next, uint32_t* __restrict__ next_cnt) {
+// The same over a list of vertices (IncEval: only vertices whose parent can
+// have changed).
+__global__ void k_sssp_parents_list(const uint32_t* __restrict__ list, uint32_t cnt, uint32_t source,
+                                    const uint64_t* __restrict__ off, const uint32_t* __restrict__ deg,
+                                    const uint32_t* __restrict__ col, const float* __restrict__ w,
+                                    const unsigned long long* __restrict__ dist,
+                                    uint32_t* __restrict__ parent) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cn; i += nwarps) {
-    const uint32_t x = cur[i];
-    const uint32_t d = deg[x];
-    const uint64_t base = off[x];
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += nwarps) {
+    const uint32_t v = list[i];
+    const unsigned long long dvb = dist[v];
+    uint32_t best = kInvalidVid;
+    if (v != source && dvb < kInfBits) {
+      const uint32_t d = deg[v];
+      const uint64_t base = off[v];
+      for (uint32_t k = lane; k < d; k += 32) {
+        const uint32_t u = col[base + k];
+        const unsigned long long dub = dist[u];
+        if (dub < kInfBits && dbits(bitsd(dub) + (double)w[base + k]) == dvb && u < best) best = u;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_down_sync(0xffffffffu, best, o));
+    }
+    if (lane == 0) parent[v] = best;
+  }
+}
+
+// Vertices whose parent (smallest tight in-neighbour) can change: those with
+// a changed distance, their out-neighbours, and heads of changed edges.
+__global__ void k_parent_candidates(const uint32_t* __restrict__ chg, uint32_t nchg,
+                                    const uint32_t* __restrict__ heads, uint32_t nheads,
+                                    const uint64_t* __restrict__ off, const uint32_t* __restrict__ deg,
+                                    const uint32_t* __restrict__ col, uint32_t* __restrict__ mark,
+                                    uint32_t tag, uint32_t* __restrict__ out, uint32_t* __restrict__ cnt) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nchg + nheads; i += nwarps) {
+    const uint32_t u = i < nchg ? chg[i] : heads[i - nchg];
+    bool take = lane == 0 && atomicExch(mark + u, tag) != tag;
+    uint32_t s0 = warp_append(take, cnt);
+    if (take) out[s0] = u;
+    if (i >= nchg) continue;
+    const uint32_t d = deg[u];
+    const uint64_t base = off[u];
     for (uint32_t kb = 0; kb < d; kb += 32) {
       const uint32_t k = kb + lane;
-      bool take = false;
-      uint32_t y = 0;
+      uint32_t v = 0;
+      take = false;
       if (k < d) {
-        y = col[base + k];
-        take = parent[y] == x && y != x && atomicExch(reset + y, 1u) == 0u;
+        v = col[base + k];
+        take = atomicExch(mark + v, tag) != tag;
       }
-      const uint32_t s = warp_append(take, next_cnt);
-      if (take) next[s] = y;
+      const uint32_t s1 = warp_append(take, cnt);
+      if (take) out[s1] = v;
     }
   }
 }
 
-__global__ void k_sssp_reset_apply(const uint32_t* __restrict__ list, uint32_t cnt,
-                                   unsigned long long* __restrict__ dist,
-                                   uint32_t* __restrict__ parent) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
-    const uint32_t v = list[i];
-    dist[v] = kInfBits;
-    parent[v] = kInvalidVid;
+// Reset BFS over the shortest-path tree in one cooperative launch: level by
+// level, children whose parent is a reset vertex join the list (deltaCompute,
+// sum_sync_traversal_worker.h:183-226); then the whole list is reset and
+// recorded as changed.  ctl: [0] bar count, [1] bar gen, [2] err, [3] next.
+struct ResetArgs {
+  const uint32_t* seed_cnt;
+  uint32_t* list;
+  uint32_t cap;
+  const uint64_t* off;
+  const uint32_t* deg;
+  const uint32_t* col;
+  uint32_t* parent;
+  uint32_t* reset;
+  unsigned long long* dist;
+  uint32_t* ctl;
+  uint32_t* chg_mark;
+  uint32_t* chg_list;
+  uint32_t* chg_cnt;
+  uint32_t chg_tag;
+  long long spin_limit;
+};
+
+__device__ __forceinline__ bool reset_sync(const ResetArgs& A) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile uint32_t* gen = A.ctl + 1;
+    const uint32_t g = *gen;
+    __threadfence();
+    if (atomicAdd(A.ctl + 0, 1u) == gridDim.x - 1) {
+      A.ctl[0] = 0;
+      __threadfence();
+      atomicAdd(A.ctl + 1, 1u);
+    } else {
+      long long spins = 0;
+      while (*gen == g) {
+        if (++spins > A.spin_limit) {
+          atomicExch(A.ctl + 2, 1u);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *(volatile uint32_t*)(A.ctl + 2) == 0;
+}
+
+__global__ void __launch_bounds__(256) k_sssp_reset_all(ResetArgs A) {
+  __shared__ uint32_t s_end;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  uint32_t begin = 0;
+  uint32_t end = min(*(volatile const uint32_t*)A.seed_cnt, A.cap);
+  while (end > begin) {
+    for (uint32_t i = begin + wid; i < end; i += nwarps) {
+      const uint32_t x = __ldcg(A.list + i);
+      const uint32_t d = A.deg[x];
+      const uint64_t base = A.off[x];
+      for (uint32_t kb = 0; kb < d; kb += 32) {
+        const uint32_t k = kb + lane;
+        bool take = false;
+        uint32_t y = 0;
+        if (k < d) {
+          y = A.col[base + k];
+          take = __ldcg(A.parent + y) == x && y != x && atomicExch(A.reset + y, 1u) == 0u;
+        }
+        const uint32_t s0 = warp_append(take, A.ctl + 3);
+        if (take) {
+          if (s0 < A.cap) A.list[s0] = y;
+          else atomicExch(A.ctl + 2, 2u);
+        }
+      }
+    }
+    if (!reset_sync(A)) return;
+    if (threadIdx.x == 0) s_end = min(*(volatile uint32_t*)(A.ctl + 3), A.cap);
+    __syncthreads();
+    begin = end;
+    end = s_end;
+    if (!reset_sync(A)) return;
+  }
+  // reset the whole list (the BFS above read the old parents)
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
+    const uint32_t v = A.list[i];
+    A.dist[v] = kInfBits;
+    A.parent[v] = kInvalidVid;
+    if (atomicExch(A.chg_mark + v, A.chg_tag) != A.chg_tag) A.chg_list[atomicAdd(A.chg_cnt, 1u)] = v;
   }
 }
 
@@ -301,7 +425,8 @@ __global__ void k_sssp_reseed(const uint32_t* __restrict__ list, uint32_t cnt,
                               const uint64_t* __restrict__ off, const uint32_t* __restrict__ deg,
                               const uint32_t* __restrict__ col, const float* __restrict__ w,
                               unsigned long long* __restrict__ dist, uint32_t* __restrict__ fq,
-                              uint32_t* __restrict__ fq_cnt) {
+                              uint32_t* __restrict__ fq_cnt, uint32_t* chg_mark, uint32_t* chg_list,
+                              uint32_t* chg_cnt, uint32_t chg_tag) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += nwarps) {
@@ -323,7 +448,11 @@ __global__ void k_sssp_reseed(const uint32_t* __restrict__ list, uint32_t cnt,
     }
     if (lane == 0 && best < kInfBits) {
       const unsigned long long old = atomicMin(dist + v, best);
-      if (best < old) fq[atomicAdd(fq_cnt, 1u)] = v;
+      if (best < old) {
+        fq[atomicAdd(fq_cnt, 1u)] = v;
+        if (chg_mark && atomicExch(chg_mark + v, chg_tag) != chg_tag)
+          chg_list[atomicAdd(chg_cnt, 1u)] = v;
+      }
     }
   }
 }
@@ -355,9 +484,10 @@ sg_status sssp_free(sg_ctx* ctx) {
   dfree(s.dist); dfree(s.parent); dfree(s.stamp);
   dfree(s.q[0]); dfree(s.q[1]); dfree(s.q[2]); dfree(s.far2); dfree(s.reset);
   dfree(s.d_ctl); dfree(s.d_cnt);
-  dfree(s.fstamp); dfree(s.list); dfree(s.seeds); dfree(s.seed_cnt); dfree(s.far);
+  dfree(s.fstamp); dfree(s.seeds); dfree(s.seed_cnt); dfree(s.far);
   dfree(s.out);
   dfree(s.padd_dst);
+  dfree(s.chg_mark); dfree(s.chg_list); dfree(s.par_mark); dfree(s.par_list); dfree(s.inc_ctl);
   s = SsspState();
   return SG_OK;
 }
@@ -387,11 +517,18 @@ static sg_status sssp_alloc(sg_ctx* ctx) {
   SG_TRY(dalloc(ctx, &s.far, fcap));
   SG_TRY(dalloc(ctx, &s.far2, fcap));
   s.far_cap = fcap;
-  SG_TRY(dalloc(ctx, &s.list, n));
   SG_TRY(dalloc(ctx, &s.seeds, n));
   SG_TRY(dalloc(ctx, &s.seed_cnt, 4));
   SG_TRY(dalloc(ctx, &s.d_ctl, S_WORDS));
   SG_TRY(dalloc(ctx, &s.d_cnt, SC_WORDS));
+  SG_TRY(dalloc(ctx, &s.chg_mark, n));
+  SG_TRY(dalloc(ctx, &s.chg_list, n));
+  SG_TRY(dalloc(ctx, &s.par_mark, n));
+  SG_TRY(dalloc(ctx, &s.par_list, n));
+  SG_TRY(dalloc(ctx, &s.inc_ctl, 8));
+  SG_CUDA(ctx, cudaMemsetAsync(s.chg_mark, 0, 4ull * n, ctx->stream));
+  SG_CUDA(ctx, cudaMemsetAsync(s.par_mark, 0, 4ull * n, ctx->stream));
+  s.chg_tag = 0;
   s.n_alloc = n;
   return SG_OK;
 }
@@ -482,8 +619,9 @@ static sg_status sssp_launch_args(sg_ctx* ctx, SsspArgs& A, uint32_t* h_ctl) {
   return SG_OK;
 }
 
-// Runs the persistent kernel from the current ctl / queues.
-static sg_status sssp_launch(sg_ctx* ctx) {
+// Runs the persistent kernel from the current ctl / queues; `track` lists
+// every improved vertex (IncEval).
+static sg_status sssp_launch(sg_ctx* ctx, bool track) {
   SsspState& s = ctx->sp;
   DevGraph& g = ctx->g;
   SsspArgs A;
@@ -498,6 +636,10 @@ static sg_status sssp_launch(sg_ctx* ctx) {
   A.iter_base = s.iter_base;
   A.fcap = s.far_cap;
   A.spin_limit = 40ll * 1000 * 1000;  // ~2-4 s of polling
+  A.chg_mark = track ? s.chg_mark : nullptr;
+  A.chg_list = s.chg_list;
+  A.chg_cnt = s.inc_ctl + 4;
+  A.chg_tag = s.chg_tag;
   uint32_t h_ctl[S_WORDS];
   SG_TRY(sssp_launch_args(ctx, A, h_ctl));
   // stamps must keep growing across launches
@@ -560,6 +702,10 @@ sg_status sssp_run_view(sg_ctx* ctx, const SsspView& G, const uint32_t* h_seeds,
   A.iter_base = 1;
   A.fcap = fcap;
   A.spin_limit = 40ll * 1000 * 1000;
+  A.chg_mark = nullptr;
+  A.chg_list = nullptr;
+  A.chg_cnt = nullptr;
+  A.chg_tag = 0;
   uint32_t h_ctl[S_WORDS];
   sg_status rs = sssp_launch_args(ctx, A, h_ctl);
   if (rs == SG_OK && h_cnt)
@@ -605,7 +751,7 @@ sg_status sssp_run_peval(sg_ctx* ctx, uint32_t source) {
   SG_CUDA(ctx, cudaMemcpyAsync(s.dist + source, &zero, 8, cudaMemcpyHostToDevice, st));
   SG_CUDA(ctx, cudaMemcpyAsync(s.far, &source, 4, cudaMemcpyHostToDevice, st));
   SG_CUDA(ctx, cudaMemcpyAsync(s.d_ctl + S_F0, &one, 4, cudaMemcpyHostToDevice, st));
-  SG_TRY(sssp_launch(ctx));
+  SG_TRY(sssp_launch(ctx, false));
   SG_TRY(sssp_compute_parents(ctx));
   SG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
   unsigned long long h_cnt[SC_WORDS];
@@ -655,38 +801,64 @@ sg_status sssp_finish_external(sg_ctx* ctx, const unsigned long long* h_cnt, flo
   return SG_OK;
 }
 
+__global__ void k_inc_start(const uint32_t* seed_cnt, uint32_t* inc_ctl) {
+  inc_ctl[0] = 0;
+  inc_ctl[1] = 0;
+  inc_ctl[2] = 0;
+  inc_ctl[3] = seed_cnt[0];
+  inc_ctl[4] = 0;
+  inc_ctl[5] = 0;
+}
+
 sg_status sssp_run_inceval(sg_ctx* ctx) {
   DevGraph& g = ctx->g;
   SsspState& s = ctx->sp;
   if (!s.valid) return fail(ctx, SG_ERR_STATE, "SSSP IncEval before PEval");
   cudaStream_t st = ctx->stream;
   SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
-  uint32_t h_seed[4] = {0, 0, 0, 0};
-  if (s.has_pending) {
-    SG_CUDA(ctx, cudaMemcpyAsync(h_seed, s.seed_cnt, sizeof(h_seed), cudaMemcpyDeviceToHost, st));
-    SG_CUDA(ctx, cudaStreamSynchronize(st));
+  if (!s.has_pending) SG_CUDA(ctx, cudaMemsetAsync(s.seed_cnt, 0, 4 * sizeof(uint32_t), st));
+  if (++s.chg_tag == 0) {  // tags wrapped: clear the marks
+    SG_CUDA(ctx, cudaMemsetAsync(s.chg_mark, 0, 4ull * g.n, st));
+    SG_CUDA(ctx, cudaMemsetAsync(s.par_mark, 0, 4ull * g.n, st));
+    s.chg_tag = 1;
   }
-  // 1. reset BFS: list = seeds, then children level by level
-  uint32_t total = h_seed[0];
-  if (total > 0) {
-    SG_CUDA(ctx, cudaMemcpyAsync(s.list, s.seeds, 4ull * total, cudaMemcpyDeviceToDevice, st));
-    uint32_t begin = 0, end = total;
-    while (end > begin) {
-      SG_CUDA(ctx, cudaMemsetAsync(s.seed_cnt + 1, 0, 4, st));
-      k_sssp_reset_step<<<grid_for((uint64_t)(end - begin) * 32, 256), 256, 0, st>>>(
-          s.list + begin, end - begin, g.out.off, g.out.deg, g.out.col, s.parent, s.reset,
-          s.list + end, s.seed_cnt + 1);
-      uint32_t nn = 0;
-      SG_CUDA(ctx, cudaMemcpyAsync(&nn, s.seed_cnt + 1, 4, cudaMemcpyDeviceToHost, st));
-      SG_CUDA(ctx, cudaStreamSynchronize(st));
-      begin = end;
-      end += nn;
-    }
-    total = end;
-    k_sssp_reset_apply<<<grid_for(total, 256), 256, 0, st>>>(s.list, total, s.dist, s.parent);
+  // 1. reset BFS over the tree from the applier's seeds, in one launch; the
+  //    list grows in place behind the seeds
+  k_inc_start<<<1, 1, 0, st>>>(s.seed_cnt, s.inc_ctl);
+  {
+    ResetArgs R;
+    R.seed_cnt = s.seed_cnt;
+    R.list = s.seeds;
+    R.cap = g.n;
+    R.off = g.out.off; R.deg = g.out.deg; R.col = g.out.col;
+    R.parent = s.parent;
+    R.reset = s.reset;
+    R.dist = s.dist;
+    R.ctl = s.inc_ctl;
+    R.chg_mark = s.chg_mark;
+    R.chg_list = s.chg_list;
+    R.chg_cnt = s.inc_ctl + 4;
+    R.chg_tag = s.chg_tag;
+    R.spin_limit = 40ll * 1000 * 1000;
+    int bps = 0;
+    SG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_sssp_reset_all, 256, 0));
+    if (bps < 1) return fail(ctx, SG_ERR_CUDA, "reset kernel cannot be resident");
+    bps = std::min(bps, 2);
+    void* args[] = {&R};
+    SG_CUDA(ctx, cudaLaunchCooperativeKernel((void*)k_sssp_reset_all, dim3(bps * ctx->num_sms),
+                                             dim3(256), args, 0, st));
+    count_launch(ctx, 2);
   }
+  uint32_t h_inc[8], h_seed[4];
+  SG_CUDA(ctx, cudaMemcpyAsync(h_inc, s.inc_ctl, sizeof(h_inc), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaMemcpyAsync(h_seed, s.seed_cnt, sizeof(h_seed), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  if (h_inc[2] == 1u) return fail(ctx, SG_ERR_TIMEOUT, "reset BFS grid barrier wait expired");
+  if (h_inc[2] == 2u) return fail(ctx, SG_ERR_INVALID, "reset list overflow");
+  const uint32_t total = h_inc[3];
+  const uint32_t nadd = s.has_pending ? h_seed[2] : 0u;
   // 2. far queue <- re-seeded reset vertices and heads of added edges
-  const uint64_t need_far = (uint64_t)total + h_seed[2] + g.n + 1024;
+  const uint64_t need_far = (uint64_t)total + nadd + g.n + 1024;
   if (need_far > s.far_cap) {
     dfree(s.far);
     dfree(s.far2);
@@ -699,15 +871,33 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
   SG_CUDA(ctx, cudaMemsetAsync(s.d_cnt, 0, sizeof(unsigned long long) * SC_WORDS, st));
   if (total > 0)
     k_sssp_reseed<<<grid_for((uint64_t)total * 32, 256), 256, 0, st>>>(
-        s.list, total, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.far, s.d_ctl + S_F0);
-  if (s.has_pending && h_seed[2] > 0)
-    k_sssp_reseed<<<grid_for((uint64_t)h_seed[2] * 32, 256), 256, 0, st>>>(
-        s.padd_dst, h_seed[2], g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.far, s.d_ctl + S_F0);
+        s.seeds, total, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.far, s.d_ctl + S_F0,
+        s.chg_mark, s.chg_list, s.inc_ctl + 4, s.chg_tag);
+  if (nadd > 0)
+    k_sssp_reseed<<<grid_for((uint64_t)nadd * 32, 256), 256, 0, st>>>(
+        s.padd_dst, nadd, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.far, s.d_ctl + S_F0,
+        s.chg_mark, s.chg_list, s.inc_ctl + 4, s.chg_tag);
   SG_CUDA(ctx, cudaGetLastError());
-  // 3. delta-stepping from the seeds
-  SG_TRY(sssp_launch(ctx));
-  if (total > 0) k_clear_marks<<<grid_for(total, 256), 256, 0, st>>>(s.list, total, s.reset);
-  SG_TRY(sssp_compute_parents(ctx));
+  // 3. delta-stepping from the seeds, listing every improved vertex
+  SG_TRY(sssp_launch(ctx, true));
+  if (total > 0) k_clear_marks<<<grid_for(total, 256), 256, 0, st>>>(s.seeds, total, s.reset);
+  // 4. parents of the vertices whose smallest tight in-neighbour can change
+  uint32_t nchg = 0;
+  SG_CUDA(ctx, cudaMemcpyAsync(&nchg, s.inc_ctl + 4, 4, cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  if (nchg + nadd > 0) {
+    k_parent_candidates<<<grid_for((uint64_t)(nchg + nadd) * 32, 256), 256, 0, st>>>(
+        s.chg_list, nchg, s.padd_dst, nadd, g.out.off, g.out.deg, g.out.col, s.par_mark, s.chg_tag,
+        s.par_list, s.inc_ctl + 5);
+    uint32_t npar = 0;
+    SG_CUDA(ctx, cudaMemcpyAsync(&npar, s.inc_ctl + 5, 4, cudaMemcpyDeviceToHost, st));
+    SG_CUDA(ctx, cudaStreamSynchronize(st));
+    if (npar > 0)
+      k_sssp_parents_list<<<grid_for((uint64_t)npar * 32, 256), 256, 0, st>>>(
+          s.par_list, npar, s.source, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.parent);
+    count_launch(ctx, 2);
+  }
+  SG_CUDA(ctx, cudaGetLastError());
   SG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
   unsigned long long h_cnt[SC_WORDS];
   SG_CUDA(ctx, cudaMemcpyAsync(h_cnt, s.d_cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));

@@ -85,3 +85,30 @@ def test_unweighted_graph_is_rejected(ctx):
     with pytest.raises(sg.SgError) as e:
         ctx.sssp_peval(0)
     assert e.value.status == sg.SG_ERR_INVALID
+
+
+def _min_tight_parents(rp, col, w, d, source):
+    n = len(rp) - 1
+    src = np.repeat(np.arange(n), np.diff(rp).astype(np.int64))
+    tight = np.isfinite(d[src]) & (d[src] + w.astype(np.float64) == d[col])
+    par = np.full(n, 0xFFFFFFFF, np.uint64)
+    np.minimum.at(par, col[tight], src[tight].astype(np.uint64))
+    par[source] = 0xFFFFFFFF
+    par[~np.isfinite(d)] = 0xFFFFFFFF
+    return par.astype(np.uint32)
+
+
+def test_parents_stay_min_tight_across_inceval(ctx):
+    """IncEval refreshes parents only where they can change (changed
+    distances, their out-neighbours, heads of changed edges); the result must
+    equal the smallest tight in-neighbour everywhere."""
+    ctx.generate_rmat(13, 16 << 13, seed=31, weight_kind=1)
+    rp, col, w = ctx.download_csr()
+    hg = sg.HostGraph(rp, col, w)
+    ctx.sssp_peval(0, out=False)
+    for i in range(4):
+        ctx.apply_updates(hg.gen_updates(400, 400, 150, seed=40 + i))
+        d = ctx.sssp_inceval()
+        nrp, ncol, nw = hg.csr()
+        assert np.array_equal(d, oracle.dijkstra(nrp, ncol, nw, 0))
+        assert np.array_equal(ctx.sssp_parents(), _min_tight_parents(nrp, ncol, nw, d, 0))
