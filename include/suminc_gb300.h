@@ -86,7 +86,8 @@ typedef struct sg_stats {
   uint64_t reset_vertices;  /* SSSP IncEval: vertices reset by deletions     */
   uint64_t launches_total;  /* kernels launched by the library since reset   */
   uint64_t edges_pull;      /* relaxations done by dense pull rounds         */
-  uint64_t edges_push;      /* relaxations done by sparse push rounds        */
+  uint64_t edges_push;      /* relaxations by push rounds (0: every PageRank
+                               round is a dense pull)                       */
 } sg_stats;
 
 /* kernel classes reported in sg_stats.kernel_ms / kernel_launches */

@@ -97,13 +97,11 @@ struct PrState {
   uint32_t n_alloc = 0;
   float* x = nullptr;      // values_
   float* delta = nullptr;  // deltas_
-  float* acc = nullptr;    // per-round incoming sums (pull)
-  float* pv = nullptr;     // per-vertex push value d*delta/outdeg this round
-  uint32_t* frontier = nullptr;   // active vertices with outdeg > 0
-  uint32_t* d_misc = nullptr;     // [0] frontier size, [1] done, [2] pending, [3] blocks done
+  float* acc = nullptr;    // push values of the first round (pv0)
+  float* pv = nullptr;     // push values d*delta/outdeg of later rounds, 2n (by parity)
+  uint32_t* d_misc = nullptr;     // round control words (pagerank.cu M_*)
   double* d_res = nullptr;        // [0] residual accumulator, [1] last residual
   uint64_t* d_cnt = nullptr;      // [0] edges relaxed, [1] vertex visits
-  bool dense_all = true;
 };
 
 struct SsspState {

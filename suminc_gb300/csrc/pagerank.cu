@@ -137,7 +137,7 @@ struct WarpPullArgs {
 
 // 8 CTAs of 256 threads per SM: 32 registers per thread, full occupancy
 // (measured faster than 6 CTAs without spills)
-template <bool W, bool PF>
+template <bool W>
 __global__ void __launch_bounds__(PT_THREADS, 8) k_pr_pull_warp(PrArgs A, WarpPullArgs P, int p) {
   __shared__ double s_red[PT_THREADS / 32];
   if (A.misc[M_DONE]) return;
@@ -174,12 +174,6 @@ __global__ void __launch_bounds__(PT_THREADS, 8) k_pr_pull_warp(PrArgs A, WarpPu
     // epilogue operands of the candidate owners, loaded before the gathers
     const bool cand_used = real && (lane == 0 || starts);
     const float dl_c = cand_used ? A.delta[v_c] : 0.f;
-    float x_c = 0.f;
-    uint32_t od_c = 0;
-    if (PF && cand_used) {
-      x_c = A.x[v_c];
-      od_c = A.scale_deg ? A.scale_deg[v_c] : 1u;
-    }
     float sum = 0.f;
     if (valid) {
       const uint32_t kk = (uint32_t)(q - qb) * 4;
@@ -207,12 +201,6 @@ __global__ void __launch_bounds__(PT_THREADS, 8) k_pr_pull_warp(PrArgs A, WarpPu
     const uint32_t v = __shfl_sync(0xffffffffu, v_c, k);
     const uint64_t qe = __shfl_sync(0xffffffffu, qe_c, k);
     const float dl0 = __shfl_sync(0xffffffffu, dl_c, k);
-    float x0 = 0.f;
-    uint32_t od0 = 0;
-    if (PF) {
-      x0 = __shfl_sync(0xffffffffu, x_c, k);
-      od0 = __shfl_sync(0xffffffffu, od_c, k);
-    }
     const bool head = valid && (lane == 0 || ((heads >> lane) & 1u));
     if (head) {
       const bool interior = qb >= base && qe <= base + kWarpTileQuads;
@@ -221,18 +209,6 @@ __global__ void __launch_bounds__(PT_THREADS, 8) k_pr_pull_warp(PrArgs A, WarpPu
         if (drain) {
           A.delta[v] = dl;
           res += fabs((double)dl);
-        } else if (PF) {
-          // activation with the prefetched value and degree
-          res += fabs((double)dl);
-          if (fabsf(dl) > A.thr_v) {
-            A.x[v] = x0 + dl;
-            A.delta[v] = 0.f;
-            pv_next[v] = A.scale_deg ? (od0 > 0 ? A.damping * dl / (float)od0 : 0.f) : A.damping * dl;
-            visits++;
-          } else {
-            A.delta[v] = dl;
-            pv_next[v] = 0.f;
-          }
         } else {
           visits += activate(A, v, dl, pv_next, res);
         }
@@ -320,7 +296,7 @@ __global__ void k_pr_seed(const uint32_t* __restrict__ seeds, uint32_t cnt, floa
 
 sg_status pr_free(sg_ctx* ctx) {
   PrState& s = ctx->pr;
-  dfree(s.x); dfree(s.delta); dfree(s.acc); dfree(s.pv); dfree(s.frontier);
+  dfree(s.x); dfree(s.delta); dfree(s.acc); dfree(s.pv);
   dfree(s.d_misc); dfree(s.d_res); dfree(s.d_cnt);
   s = PrState();
   return SG_OK;
@@ -450,13 +426,8 @@ sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R) {
     for (;;) {
       for (int r = 0; r < chunk; ++r, ++pull) {
         kprof_begin(ctx);
-        if (ctx->opt.reserved[1] == 1) {
-          if (R.weighted) k_pr_pull_warp<true, true><<<wblocks, PT_THREADS, 0, st>>>(A, WP, pull);
-          else k_pr_pull_warp<false, true><<<wblocks, PT_THREADS, 0, st>>>(A, WP, pull);
-        } else {
-          if (R.weighted) k_pr_pull_warp<true, false><<<wblocks, PT_THREADS, 0, st>>>(A, WP, pull);
-          else k_pr_pull_warp<false, false><<<wblocks, PT_THREADS, 0, st>>>(A, WP, pull);
-        }
+        if (R.weighted) k_pr_pull_warp<true><<<wblocks, PT_THREADS, 0, st>>>(A, WP, pull);
+        else k_pr_pull_warp<false><<<wblocks, PT_THREADS, 0, st>>>(A, WP, pull);
         kprof_end(ctx, kpull);
         kprof_begin(ctx);
         k_pr_fixup<<<fblocks, VT, 0, st>>>(A, bnd, nbnd, pull);

@@ -117,3 +117,48 @@ def test_pool_repacks_under_many_inserts():
             assert np.array_equal(drp, nrp) and np.array_equal(dcol, ncol)
             assert np.array_equal(dw, nw)
             assert np.array_equal(ctx.sssp_inceval(), oracle.dijkstra(nrp, ncol, nw, 0))
+
+
+def test_graph_emptied_and_refilled_by_batches():
+    """Every edge deleted (m = 0, no pull work), then edges back: PageRank
+    and SSSP IncEval stay exact, and an empty batch changes nothing."""
+    rp = np.array([0, 2, 3, 3, 4], np.uint64)
+    col = np.array([1, 2, 2, 0], np.uint32)
+    w = np.array([1, 5, 1, 2], np.float32)
+    with sg.Context(0) as ctx:
+        ctx.load_csr(rp, col, w)
+        ctx.pr_peval(out=False)
+        ctx.apply_updates(np.zeros(0, sg.UPDATE_DTYPE))
+        hg = sg.HostGraph(rp, col, w)
+        dels = np.zeros(4, sg.UPDATE_DTYPE)
+        for i, (u, v) in enumerate([(0, 1), (0, 2), (1, 2), (3, 0)]):
+            dels[i] = (u, v, 0.0, 1)
+        ctx.apply_updates(dels)
+        assert ctx.m == 0
+        x = ctx.pr_inceval()
+        assert np.abs(x - oracle.pr_fixed_point(np.zeros(5, np.uint64), np.zeros(0, np.uint32))).sum() <= 1e-5
+        adds = np.zeros(3, sg.UPDATE_DTYPE)
+        for i, (u, v, ww) in enumerate([(2, 3, 4.0), (3, 1, 1.0), (0, 3, 9.0)]):
+            adds[i] = (u, v, ww, 0)
+        ctx.apply_updates(adds)
+        nrp = np.array([0, 1, 1, 2, 3], np.uint64)
+        ncol = np.array([3, 3, 1], np.uint32)
+        nw = np.array([9, 4, 1], np.float32)
+        x = ctx.pr_inceval()
+        assert np.abs(x - oracle.pr_fixed_point(nrp, ncol)).sum() <= 1e-5
+    with sg.Context(0) as ctx:
+        ctx.load_csr(rp, col, w)
+        ctx.sssp_peval(0, out=False)
+        ctx.apply_updates(dels)
+        d = ctx.sssp_inceval()
+        assert d[0] == 0 and np.all(np.isinf(d[1:]))
+        ctx.apply_updates(adds)
+        assert np.array_equal(ctx.sssp_inceval(), oracle.dijkstra(nrp, ncol, nw, 0))
+
+
+def test_single_vertex_graph():
+    with sg.Context(0) as ctx:
+        ctx.load_csr(np.array([0, 0], np.uint64), np.zeros(0, np.uint32), np.zeros(0, np.float32))
+        x = ctx.pr_peval()
+        assert abs(float(x[0]) - 0.15) < 1e-6
+        assert ctx.sssp_peval(0)[0] == 0.0
