@@ -583,6 +583,29 @@ def run_adjoint(args, D: Dist):
     t_fb = ctx.elapsed_ms(2, 3)
     clk = clocks.stop()
     info = ctx.adjoint_info()
+    # the plain-loop alternative: central differences over teleport entries,
+    # two forward solves per parameter on the same GPU (FP32), against the
+    # adjoint's dL/dtele from the last backward
+    dt_adj = dt_pin.numpy().copy()
+    fd_params = [int(v) for v in tgt[:8]]
+    fd_h = 1.0 / n  # x is linear in tele and L quadratic: no truncation error
+    x_base = None
+    ctx.synchronize()
+    ctx.record_event(4)
+    fd_vals = []
+    for v in fd_params:
+        l2 = []
+        for sign in (1.0, -1.0):
+            tp = tele.copy()
+            tp[v] += sign * fd_h
+            xs = ctx.pr_weighted(tp)
+            l2.append(0.5 * float(np.sum((xs[tgt].astype(np.float64) - y) ** 2)))
+        fd_vals.append((l2[0] - l2[1]) / (2 * fd_h))
+    ctx.record_event(5)
+    ctx.synchronize()
+    fd_ms = ctx.elapsed_ms(4, 5)
+    fd_rel = [abs(fd_vals[i] - float(dt_adj[v])) / max(abs(float(dt_adj[v])), 1e-30)
+              for i, v in enumerate(fd_params)]
     # per-kernel device time of the adjoint's weighted pull (profiled run)
     ctx.set_profile(0xFF)
     ctx.reset_stats()
@@ -659,6 +682,15 @@ def run_adjoint(args, D: Dist):
                    "l2": "graph larger than L2, no flush"},
         "forward_ms": round(t_f / K, 3), "forward_backward_ms": round(t_fb / K, 3),
         "backward_over_forward": round((t_fb - t_f) / t_f, 3),
+        "vs_plain_loop": {
+            "path": "central differences over teleport entries, 2 x sg_pr_weighted per "
+                    "parameter on the same GPU (FP32), step 1/N",
+            "params_timed": len(fd_params), "loop_ms": round(fd_ms, 2),
+            "loop_ms_per_param": round(fd_ms / len(fd_params), 3),
+            "adjoint_params": int(n + E),
+            "speedup_for_all_params": round((fd_ms / len(fd_params)) * (n + E) / (t_fb / K), 1),
+            "speedup_for_64_params": round((fd_ms / len(fd_params)) * 64 / (t_fb / K), 2),
+            "fd_rel_err_vs_adjoint_max": max(fd_rel)},
         "device_ms": {"forward": round(f_dev_ms / K, 3), "adjoint_and_gradients": round(a_dev_ms / K, 3)},
         "rounds": {"forward": info["forward_rounds"], "adjoint": info["adjoint_rounds"]},
         "accuracy_scale12_subgraph": {"lambda_rel_l1_vs_fp64": rel_lam, "dw_rel_l1_vs_fp64": rel_dw,

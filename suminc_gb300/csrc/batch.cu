@@ -1029,30 +1029,42 @@ static sg_status batch_trial(sg_ctx* ctx, BatchState& B, const BatchArgs& A, uin
 }
 
 // In-house autotuner: times candidate schedules on the caller's batch.
-//   PPR  : chunk quads x blocks per SM; each candidate runs 4 and 12
-//          iterations and is scored by the difference, the cost of 8 rounds
-//          once the queries have spread (the first rounds are sparse and
-//          would favour the wrong schedule)
-//   SSSP : bucket width, full runs at the chosen blocks per SM
+//   PPR  : chunk size at 2 CTAs per SM, then CTAs per SM at that chunk size;
+//          each candidate runs 4 and 12 iterations and is scored by the
+//          difference, the cost of 8 rounds once the queries have spread
+//          (the first rounds are sparse and would favour the wrong schedule)
+//   SSSP : bucket width, full runs at the chosen CTAs per SM
 static sg_status batch_tune(sg_ctx* ctx, BatchState& B, uint32_t nq, uint32_t ns) {
   const auto t0 = std::chrono::steady_clock::now();
   const uint32_t qw = nq ? pow2_at_least(nq) : 0;
   const int mb = std::max(1, std::min(4, max_bps(ctx, qw)));
-  uint32_t best_cq = 8, best_bps = (uint32_t)std::min(mb, 2);
+  uint32_t best_cq = 32, best_bps = (uint32_t)std::min(mb, 2);
   if (nq > 0) {
-    float best = 1e30f;
-    for (uint32_t cq : {4u, 8u, 16u, 32u, 64u, 128u}) {
+    auto score = [&](uint32_t cq, uint32_t bps, float* ms) -> sg_status {
       SG_TRY(batch_chunks(ctx, B, cq));
-      for (int bps = 1; bps <= mb; ++bps) {
-        float ms_short = 0.f, ms_long = 0.f;
-        SG_TRY(batch_trial(ctx, B, batch_args(ctx, B, nq, 0, B.sdelta, 4), (uint32_t)bps, &ms_short));
-        SG_TRY(batch_trial(ctx, B, batch_args(ctx, B, nq, 0, B.sdelta, 12), (uint32_t)bps, &ms_long));
-        const float ms = ms_long - ms_short;
-        if (ms < best) {
-          best = ms;
-          best_cq = cq;
-          best_bps = (uint32_t)bps;
-        }
+      float ms_short = 0.f, ms_long = 0.f;
+      SG_TRY(batch_trial(ctx, B, batch_args(ctx, B, nq, 0, B.sdelta, 4), bps, &ms_short));
+      SG_TRY(batch_trial(ctx, B, batch_args(ctx, B, nq, 0, B.sdelta, 12), bps, &ms_long));
+      *ms = ms_long - ms_short;
+      return SG_OK;
+    };
+    float best = 1e30f;
+    for (uint32_t cq : {8u, 16u, 32u, 64u, 128u, 256u, 512u}) {
+      float ms = 0.f;
+      SG_TRY(score(cq, best_bps, &ms));
+      if (ms < best) {
+        best = ms;
+        best_cq = cq;
+      }
+    }
+    const uint32_t bps0 = best_bps;
+    for (int bps = 1; bps <= mb; ++bps) {
+      if ((uint32_t)bps == bps0) continue;
+      float ms = 0.f;
+      SG_TRY(score(best_cq, (uint32_t)bps, &ms));
+      if (ms < best) {
+        best = ms;
+        best_bps = (uint32_t)bps;
       }
     }
   }
@@ -1062,7 +1074,7 @@ static sg_status batch_tune(sg_ctx* ctx, BatchState& B, uint32_t nq, uint32_t ns
   if (ns > 0) {
     float best = 1e30f;
     double best_d = 32.0;
-    for (double dl : {16.0, 32.0, 64.0, 128.0, 256.0, 512.0}) {
+    for (double dl : {32.0, 64.0, 128.0, 256.0, 512.0, 1024.0, 2048.0}) {
       const BatchArgs A = batch_args(ctx, B, 0, ns, dl, 1u << 30);
       float ms = 0.f;
       SG_TRY(batch_trial(ctx, B, A, B.bps, &ms));
