@@ -277,12 +277,14 @@ def run_ours(args, D: Dist):
     ctx.record_event(0)
     relax = 0
     rounds = []
+    visits = []
     for i in range(W, W + K):
         ctx.apply_updates_ptr(bsz, dev_b[i].data_ptr(), True)
         ctx.pr_inceval_into(None)
         st = ctx.stats()
         relax += st["edges_relaxed"]
         rounds.append(st["rounds"])
+        visits.append(int(st["vertex_visits"]))
     ctx.record_event(1)
     ctx.synchronize()
     D.barrier()
@@ -371,6 +373,7 @@ def run_ours(args, D: Dist):
                 "ms_per_step": round(te_ms / K, 4)},
         "gpu_launches": int(launches),
         "rounds_per_step": rounds,
+        "activations_per_step": visits,
         "relaxations_per_step": int(relax / K),
         "graph_gteps": round(E * K / (t_ms_max * 1e-3) / 1e9, 4),
         "peval": {"rounds": peval_stats["rounds"], "ms": round(peval_stats["elapsed_ms"], 3)},
