@@ -41,6 +41,9 @@ sys.path.insert(0, ROOT)
 L2_BYTES = 126 * 1024 * 1024
 BYTES_PER_RELAXED_EDGE = 12   # 4 B neighbour + 4 B delta read + 4 B delta write
 BYTES_PER_VERTEX_VISIT = 24   # 8 B row offset + 4 B delta read/reset + 8 B value RMW
+# DRAM bytes (read + write) per k_pr_pull_warp launch on the default
+# workload, from one ncu capture (profiles/pr_pull_warp_rmat24_dram.md)
+PULL_DRAM_BYTES_RMAT24 = 2.07e9
 
 
 def parse():
@@ -339,10 +342,15 @@ def run_ours(args, D: Dist):
         bytes_per_launch = BYTES_PER_VERTEX_VISIT * n
     peak, peak_kind = measured_peaks()
     achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
+    traffic = (PULL_DRAM_BYTES_RMAT24 if (dom == "pr_pull" and args.scale == 24
+                                          and args.edge_factor == 16) else None)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                "traffic": None, "avg_launch_ms": round(avg_ms, 4),
+                "traffic": traffic,
+                "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum, one "
+                                   "capture of this workload" if traffic else None),
+                "avg_launch_ms": round(avg_ms, 4),
                 "algorithmic_bytes_per_launch": int(bytes_per_launch),
                 "kernels": kernels}
 
