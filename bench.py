@@ -60,11 +60,12 @@ def parse():
     p.add_argument("--cpu-sample-rounds", type=int, default=3)
     p.add_argument("--no-clocks", action="store_true")
     p.add_argument("--workload", default="inceval",
-                   choices=["inceval", "batched", "adjoint", "sssp"],
+                   choices=["inceval", "batched", "adjoint", "sssp", "summarized"],
                    help="inceval: the headline IncEval line; batched: 256 PPR + 64 SSSP "
                         "queries in one persistent launch vs looping the single-query path; "
                         "adjoint: weighted PageRank forward vs forward + adjoint; sssp: "
-                        "incremental SSSP at R-MAT scale 20")
+                        "incremental SSSP at R-MAT scale 20; summarized: PageRank and SSSP "
+                        "over the summarized graph of a community graph vs the plain graph")
     p.add_argument("--batch-scale", type=int, default=22)
     p.add_argument("--ppr-queries", type=int, default=256)
     p.add_argument("--sssp-sources", type=int, default=64)
@@ -833,14 +834,111 @@ def run_sssp(args, D: Dist):
     return result
 
 
+def community_graph(n_comm, size, seed):
+    """Directed graph with planted communities (vectorised, seeded): inside
+    each community every member links to ~8 random members; the last 3
+    members of each community link to the first 3 members of 4 random other
+    communities.  Integer weights U[1, 100].  Returns CSR and the
+    communities (the cluster file)."""
+    rng = np.random.default_rng(seed)
+    n = n_comm * size
+    deg_in = 8
+    src_i = np.repeat(np.arange(n, dtype=np.int64), deg_in)
+    dst_i = (src_i // size) * size + rng.integers(0, size, size=src_i.size)
+    exits = (np.arange(n_comm, dtype=np.int64)[:, None] * size + np.arange(size - 3, size)).ravel()
+    src_x = np.repeat(exits, 4)
+    oc = rng.integers(0, n_comm, size=src_x.size)
+    dst_x = oc * size + rng.integers(0, 3, size=src_x.size)
+    src = np.concatenate([src_i, src_x])
+    dst = np.concatenate([dst_i, dst_x])
+    keep = src != dst
+    key = np.unique(src[keep] * n + dst[keep])
+    src, dst = key // n, key % n
+    rp = np.zeros(n + 1, np.uint64)
+    np.add.at(rp, src + 1, 1)
+    rp = np.cumsum(rp).astype(np.uint64)
+    col = dst.astype(np.uint32)
+    w = (1 + (src * 2654435761 + dst * 40503) % 100).astype(np.float32)
+    comms = [np.arange(c * size, (c + 1) * size, dtype=np.uint32) for c in range(n_comm)]
+    return rp, col, w, comms
+
+
+def run_summarized(args, D: Dist):
+    """The summarized graph at scale: PageRank PEval/IncEval and SSSP PEval with
+    compress=1 (supernodes, shortcuts computed on the GPU) against compress=0
+    on the same community graph and batches."""
+    import oracle
+    import suminc_gb300 as sg
+
+    dev = D.local
+    n_comm = 1 << max(args.batch_scale - 5, 4)  # communities of 32..40 members
+    rp, col, w, comms = community_graph(n_comm, 40, args.seed)
+    n, E = len(rp) - 1, len(col)
+    hg = sg.HostGraph(rp, col, w)
+    bsz = max(1000, E // 1000)
+    batches = [hg.gen_updates(bsz // 2, bsz - bsz // 2, 0, seed=700 + i) for i in range(args.steps)]
+    out = {}
+    for mode in (1, 0):
+        ctx = sg.Context(dev, compress=mode)
+        ctx.load_csr(rp, col, w)
+        t0 = time.perf_counter()
+        if mode:
+            ctx.summary_build(comms)
+            info = ctx.summary_info()
+        build_s = time.perf_counter() - t0
+        ctx.pr_peval(out=False)
+        pe = ctx.stats()
+        d0 = ctx.sssp_peval(0)
+        sp = ctx.stats()
+        inc_ms, rounds = [], []
+        for b in batches:
+            ctx.apply_updates(b)
+            ctx.pr_inceval_into(None)
+            st = ctx.stats()
+            inc_ms.append(st["elapsed_ms"])
+            rounds.append(st["rounds"])
+        x = ctx.pr_values()
+        out[mode] = {"peval_ms": round(pe["elapsed_ms"], 3), "peval_rounds": pe["rounds"],
+                     "sssp_peval_ms": round(sp["elapsed_ms"], 3),
+                     "inceval_ms": [round(v, 3) for v in inc_ms], "inceval_rounds": rounds,
+                     "build_s": round(build_s, 2), "x": x, "d0": d0}
+        if mode:
+            out[mode]["summary"] = {k: info[k] for k in ("clusters", "supernodes", "shortcut_edges",
+                                                         "boundary_edges", "all_rows")}
+        ctx.close()
+    nrp, ncol, nw = hg.csr()
+    xs = oracle.pr_fixed_point(nrp, ncol)
+    d_ref = oracle.dijkstra(rp, col, w, 0)
+    l1 = {m: float(np.abs(out[m]["x"] - xs).sum()) for m in (0, 1)}
+    exact = {m: bool(np.array_equal(out[m]["d0"], d_ref)) for m in (0, 1)}
+    for m in (0, 1):
+        del out[m]["x"], out[m]["d0"]
+    s_inc = float(np.mean(out[1]["inceval_ms"]))
+    p_inc = float(np.mean(out[0]["inceval_ms"]))
+    return {
+        "metric": "PageRank IncEval over the summarized graph (ms per batch)",
+        "value": round(s_inc, 3), "unit": "ms", "n_gpus": D.ws, "steps": args.steps, "warmup": 0,
+        "ms_per_step": round(s_inc, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic community graph (seeded)",
+        "config": {"workload": f"summarized PageRank / SSSP, {n_comm} communities of 40",
+                   "vertices": n, "edges": E, "batch_changes": bsz,
+                   "clusters": "the planted communities (cluster file)",
+                   "parallelism": "single GPU"},
+        "summarized": out[1], "plain": out[0],
+        "summarized_over_plain_inceval": round(s_inc / p_inc, 3),
+        "pr_l1_vs_fp64": l1, "sssp_exact_vs_dijkstra": exact,
+    }
+
+
 def main():
     args = parse()
     D = Dist()
     if args.impl == "reference":
         run_reference(args, D)
         return
-    if args.workload in ("batched", "adjoint", "sssp"):
-        result = {"batched": run_batched, "adjoint": run_adjoint, "sssp": run_sssp}[args.workload](args, D)
+    if args.workload in ("batched", "adjoint", "sssp", "summarized"):
+        result = {"batched": run_batched, "adjoint": run_adjoint, "sssp": run_sssp,
+                  "summarized": run_summarized}[args.workload](args, D)
         if D.rank == 0:
             print(json.dumps(result), flush=True)
         return
