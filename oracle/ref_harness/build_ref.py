@@ -50,5 +50,25 @@ def build(verbose: bool = False) -> str | None:
     return exe
 
 
+def check_adaptor(verbose: bool = False) -> bool | None:
+    """Compiles adaptor_check.cc (the C++ workers over the reference's own
+    fragment and app types) with -fsyntax-only; None without the checkout."""
+    if not os.path.isdir(REF):
+        return None
+    stubs = os.path.join(HERE, "stubs")
+    repo = os.path.dirname(os.path.dirname(HERE))
+    inc = ["-I" + stubs, "-I" + REF, "-I" + os.path.join(REF, "examples/analytical_apps"),
+           "-I" + os.path.join(REF, "cudaCode"), "-I" + os.path.join(REF, "thirdparty"),
+           "-I" + os.path.join(CUDA, "include"), "-I" + os.path.join(repo, "include")]
+    # C++17 for the adaptor's `if constexpr`
+    flags = ["-std=c++17", "-fsyntax-only", "-fopenmp", "-DOPENMP", "-w", "-include",
+             os.path.join(stubs, "force.h")]
+    p = subprocess.run(["g++", *flags, *inc, os.path.join(HERE, "adaptor_check.cc")],
+                       capture_output=True, text=True)
+    if verbose or p.returncode:
+        sys.stderr.write(p.stdout + p.stderr[-20000:])
+    return p.returncode == 0
+
+
 if __name__ == "__main__":
     print(build(verbose=True))

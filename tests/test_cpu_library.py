@@ -92,3 +92,18 @@ def test_null_and_invalid_arguments_are_rejected():
     assert lib.sg_get_stats(None, None) == sg.SG_ERR_INVALID
     assert lib.sg_options_default(None) == sg.SG_ERR_INVALID
     assert lib.sg_util_rmat_host(0, 10, 0.57, 0.19, 0.19, 1, 0, 1.0, 1.0, None, None, None) == sg.SG_ERR_INVALID
+
+
+def test_cpp_workers_compile_against_the_reference_types():
+    """include/suminc_gb300_worker.hpp instantiated with the reference's own
+    ImmutableEdgecutFragment, PageRankIngress and SSSPIngress (compile only;
+    skipped where the reference checkout is absent)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "build_ref", os.path.join(ROOT, "oracle", "ref_harness", "build_ref.py"))
+    build_ref = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(build_ref)
+    ok = build_ref.check_adaptor()
+    if ok is None:
+        pytest.skip("reference checkout not available")
+    assert ok
