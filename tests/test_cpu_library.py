@@ -5,6 +5,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 import suminc_gb300 as sg
 
