@@ -93,7 +93,7 @@ typedef struct sg_stats {
 /* kernel classes reported in sg_stats.kernel_ms / kernel_launches */
 enum {
   SG_K_PR_PULL = 0,   /* dense pull round (edge-balanced gather)     */
-  SG_K_PR_PUSH = 1,   /* sparse push round (frontier scatter)        */
+  SG_K_SUM_LOCAL = 1, /* summary: cluster-local precompute           */
   SG_K_PR_VERTEX = 2, /* vertex update / residual / frontier build   */
   SG_K_APPLY = 3,     /* delta-graph applier                         */
   SG_K_SSSP = 4,      /* delta-stepping persistent kernel            */

@@ -47,7 +47,7 @@ SG_UPD_DEL = 1
 
 UPDATE_DTYPE = np.dtype([("src", "<u4"), ("dst", "<u4"), ("weight", "<f4"), ("op", "<u4")])
 
-K_NAMES = ["pr_pull", "pr_push", "pr_vertex", "apply", "sssp", "summary", "batch", "adjoint"]
+K_NAMES = ["pr_pull", "sum_local", "pr_vertex", "apply", "sssp", "summary", "batch", "adjoint"]
 
 
 class Options(C.Structure):

@@ -148,13 +148,15 @@ __global__ void __launch_bounds__(PT_THREADS, 8) k_pr_pull_warp(PrArgs A, WarpPu
   const float* __restrict__ pv = p == 0 ? A.pv0 : ((p & 1) ? A.pvb[1] : A.pvb[0]);
   float* pv_next = (p & 1) ? A.pvb[0] : A.pvb[1];
   const uint32_t lane = threadIdx.x & 31;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * PT_THREADS) >> 5;
+  // tiles are 32 quads, so tile indices fit 32 bits for any graph in HBM
+  const uint32_t nwarps = (gridDim.x * PT_THREADS) >> 5;
+  const uint32_t ntiles = (uint32_t)P.ntiles;
   double res = 0.0;
-  unsigned long long visits = 0;
-  uint64_t t = ((uint64_t)blockIdx.x * PT_THREADS + threadIdx.x) >> 5;
-  uint32_t i0 = t < P.ntiles ? P.wtile_v0[t] : 0u;
-  for (; t < P.ntiles; t += nwarps) {
-    const uint64_t base = t * kWarpTileQuads;
+  uint32_t visits = 0;
+  uint32_t t = (blockIdx.x * PT_THREADS + threadIdx.x) >> 5;
+  uint32_t i0 = t < ntiles ? P.wtile_v0[t] : 0u;
+  for (; t < ntiles; t += nwarps) {
+    const uint64_t base = (uint64_t)t * kWarpTileQuads;
     const uint64_t q = base + lane;
     const bool valid = q < P.quads;
     // owner candidate i0 + lane
@@ -166,57 +168,64 @@ __global__ void __launch_bounds__(PT_THREADS, 8) k_pr_pull_warp(PrArgs A, WarpPu
     const uint32_t deg_c = real ? P.deg_nz[ic] : 0u;
     const uint32_t v_c = real ? P.nz[ic] : 0u;
     // prefetch the next tile's first owner
-    const uint64_t tn = t + nwarps;
-    const uint32_t i0_next = tn < P.ntiles ? P.wtile_v0[tn] : 0u;
+    const uint32_t tn = t + nwarps;
+    const uint32_t i0_next = tn < ntiles && tn > t ? P.wtile_v0[tn] : 0u;
     const bool starts = lane > 0 && real && qb_c < base + kWarpTileQuads;
     const unsigned heads = __reduce_or_sync(0xffffffffu, starts ? 1u << (uint32_t)(qb_c - base) : 0u);
     const uint32_t k = __popc(heads & (0xffffffffu >> (31 - lane)));
-    const uint64_t qb = __shfl_sync(0xffffffffu, qb_c, k);
-    const uint64_t off = __shfl_sync(0xffffffffu, off_c, k);
-    const uint32_t deg = __shfl_sync(0xffffffffu, deg_c, k);
+    // Per owner, two shuffled operands: the edge index of quad 0 of the
+    // address space (segment offset - 4 x first quad, so a lane's first edge
+    // is that + 4q) and the owner's edge count from the tile's first edge,
+    // clamped (only whether a lane's quad is partial matters).
+    const uint64_t ebase_c = off_c - 4ull * qb_c;
+    const int64_t eend_raw = 4ll * (int64_t)(qb_c - base) + (int64_t)deg_c;
+    const int eend_c = (int)(eend_raw < 4ll * kWarpTileQuads + 8 ? eend_raw : 4ll * kWarpTileQuads + 8);
+    const uint64_t ebase = __shfl_sync(0xffffffffu, ebase_c, k);
+    const int rem = __shfl_sync(0xffffffffu, eend_c, k) - 4 * (int)lane;
     // epilogue operands of the candidate owners, loaded before the gathers
     const bool cand_used = real && (lane == 0 || starts);
     const float dl_c = cand_used ? A.delta[v_c] : 0.f;
+    const bool interior = qb_c >= base && qe_c <= base + kWarpTileQuads;
+    const uint32_t run0 = lane == 0 ? 0u : (uint32_t)(qb_c - base) & 31u;
     float sum = 0.f;
     if (valid) {
-      const uint32_t kk = (uint32_t)(q - qb) * 4;
-      const uint4 c4 = ld_u4_hint(P.col + off + kk, l2_stream);
+      const uint4 c4 = ld_u4_hint(P.col + ebase + 4ull * q, l2_stream);
       if (W) {
-        const float4 w4 = ld_f4_hint(P.w + off + kk, l2_stream);
+        const float4 w4 = ld_f4_hint(P.w + ebase + 4ull * q, l2_stream);
         sum = pv[c4.x] * w4.x;  // the last quad of a vertex may be partial
-        if (kk + 1 < deg) sum += pv[c4.y] * w4.y;
-        if (kk + 2 < deg) sum += pv[c4.z] * w4.z;
-        if (kk + 3 < deg) sum += pv[c4.w] * w4.w;
+        if (rem > 1) sum += pv[c4.y] * w4.y;
+        if (rem > 2) sum += pv[c4.z] * w4.z;
+        if (rem > 3) sum += pv[c4.w] * w4.w;
       } else {
         sum = pv[c4.x];
-        if (kk + 1 < deg) sum += pv[c4.y];
-        if (kk + 2 < deg) sum += pv[c4.z];
-        if (kk + 3 < deg) sum += pv[c4.w];
+        if (rem > 1) sum += pv[c4.y];
+        if (rem > 2) sum += pv[c4.z];
+        if (rem > 3) sum += pv[c4.w];
       }
     }
-    // segmented suffix sums: the first lane of each owner's run gets its total
+    // segmented suffix sums: the first lane of each owner's run gets its
+    // total; a lane adds lane + o while no segment starts in (lane, lane + o]
+    const unsigned above = heads & ~(0xffffffffu >> (31 - lane));
+    const uint32_t seg_end = above ? (uint32_t)__ffs(above) - 1u : 32u;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const float ts = __shfl_down_sync(0xffffffffu, sum, o);
-      const uint32_t tk = __shfl_down_sync(0xffffffffu, k, o);
-      if (lane + o < 32 && tk == k) sum += ts;
+      if (lane + o < seg_end) sum += ts;
     }
-    const uint32_t v = __shfl_sync(0xffffffffu, v_c, k);
-    const uint64_t qe = __shfl_sync(0xffffffffu, qe_c, k);
-    const float dl0 = __shfl_sync(0xffffffffu, dl_c, k);
-    const bool head = valid && (lane == 0 || ((heads >> lane) & 1u));
-    if (head) {
-      const bool interior = qb >= base && qe <= base + kWarpTileQuads;
+    // each candidate owner takes its total from its run's first lane and
+    // finishes itself
+    const float tot = __shfl_sync(0xffffffffu, sum, run0);
+    if (cand_used) {
       if (interior) {
-        const float dl = dl0 + sum;
+        const float dl = dl_c + tot;
         if (drain) {
-          A.delta[v] = dl;
+          A.delta[v_c] = dl;
           res += fabs((double)dl);
         } else {
-          visits += activate(A, v, dl, pv_next, res);
+          visits += activate(A, v_c, dl, pv_next, res);
         }
-      } else if (sum != 0.f) {
-        atomicAdd(&A.delta[v], sum);
+      } else if (tot != 0.f) {
+        atomicAdd(&A.delta[v_c], tot);
       }
     }
     i0 = i0_next;
@@ -225,7 +234,7 @@ __global__ void __launch_bounds__(PT_THREADS, 8) k_pr_pull_warp(PrArgs A, WarpPu
   if (threadIdx.x == 0 && b != 0.0) atomicAdd(&A.res[R_ACC], b);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) visits += __shfl_down_sync(0xffffffffu, visits, o);
-  if ((threadIdx.x & 31) == 0 && visits) atomicAdd(&A.cnt[C_VISITS], visits);
+  if ((threadIdx.x & 31) == 0 && visits) atomicAdd(&A.cnt[C_VISITS], (unsigned long long)visits);
 }
 
 // Tile-spanning vertices, then the round's termination decision.
