@@ -337,8 +337,6 @@ def run_ours(args, D: Dist):
     avg_ms = kms[dom] / kl[dom]
     if dom == "pr_pull":
         bytes_per_launch = BYTES_PER_RELAXED_EDGE * pe_pull / kl[dom]
-    elif dom == "pr_push":
-        bytes_per_launch = BYTES_PER_RELAXED_EDGE * pe_push / kl[dom]
     else:
         bytes_per_launch = BYTES_PER_VERTEX_VISIT * n
     peak, peak_kind = measured_peaks()
@@ -877,6 +875,7 @@ def run_summarized(args, D: Dist):
     hg = sg.HostGraph(rp, col, w)
     bsz = max(1000, E // 1000)
     batches = [hg.gen_updates(bsz // 2, bsz - bsz // 2, 0, seed=700 + i) for i in range(args.steps)]
+    prof_batch = hg.gen_updates(bsz // 2, bsz - bsz // 2, 0, seed=799)
     out = {}
     for mode in (1, 0):
         ctx = sg.Context(dev, compress=mode)
@@ -892,18 +891,31 @@ def run_summarized(args, D: Dist):
         sp_first = ctx.stats()
         d0 = ctx.sssp_peval(0)  # shortcut distances and sketch now built
         sp = ctx.stats()
-        inc_ms, rounds = [], []
+        inc_ms, rounds, apply_ms = [], [], []
         for b in batches:
-            ctx.apply_updates(b)
+            t1 = time.perf_counter()
+            ctx.apply_updates(b)  # with compress=1 this includes the summary repair
+            apply_ms.append((time.perf_counter() - t1) * 1e3)
             ctx.pr_inceval_into(None)
             st = ctx.stats()
             inc_ms.append(st["elapsed_ms"])
             rounds.append(st["rounds"])
+        # one more batch (the same one in both modes) with CUDA events around
+        # every kernel class
+        ctx.set_profile(0xFF)
+        ctx.apply_updates(prof_batch)
+        ctx.reset_stats()
+        ctx.pr_inceval_into(None)
+        stp = ctx.stats()
+        ctx.set_profile(0)
+        kms = {k: round(v, 3) for k, v in stp["kernel_ms"].items() if v}
         x = ctx.pr_values()
         out[mode] = {"peval_ms": round(pe["elapsed_ms"], 3), "peval_rounds": pe["rounds"],
+                     "inceval_kernel_ms": kms, "inceval_profiled_ms": round(stp["elapsed_ms"], 3),
                      "sssp_peval_ms": round(sp["elapsed_ms"], 3),
                      "sssp_peval_first_ms": round(sp_first["elapsed_ms"], 3),
                      "inceval_ms": [round(v, 3) for v in inc_ms], "inceval_rounds": rounds,
+                     "apply_ms": [round(v, 3) for v in apply_ms],
                      "build_s": round(build_s, 2), "x": x, "d0": d0}
         if mode:
             out[mode]["summary"] = {k: info[k] for k in ("clusters", "supernodes", "shortcut_edges",
@@ -912,6 +924,8 @@ def run_summarized(args, D: Dist):
     nrp, ncol, nw = hg.csr()
     xs = oracle.pr_fixed_point(nrp, ncol)
     d_ref = oracle.dijkstra(rp, col, w, 0)
+    # both contexts applied the same batches (the profiled one last); hg holds
+    # the graph after them
     l1 = {m: float(np.abs(out[m]["x"] - xs).sum()) for m in (0, 1)}
     exact = {m: bool(np.array_equal(out[m]["d0"], d_ref)) for m in (0, 1)}
     for m in (0, 1):

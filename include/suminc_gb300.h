@@ -361,9 +361,8 @@ sg_status sg_adjoint_values(sg_ctx* ctx, float* x, float* lambda);
 
 /* PageRank PEval that allocates nothing -- no counterpart in the reference.
  * For callers that cannot call cudaMalloc: a process whose device memory is
- * owned by another framework's pool, code running while a stream is being
- * captured, or latency-bound loops that must not hit cudaMalloc's implicit
- * synchronisation.  The caller passes a packed CSR (d_row_ptr[n+1],
+ * owned by another framework's pool, or latency-bound loops that must not
+ * hit cudaMalloc's implicit synchronisation.  The caller passes a packed CSR (d_row_ptr[n+1],
  * d_col[m]) and the outputs (d_values[n], d_deltas[n]) in device memory of
  * the current device, and a stream (NULL = default stream); the result is
  * the delta-accumulative PageRank of sg_pr_peval (L1 residual below

@@ -1,8 +1,7 @@
 // Allocation-free PageRank PEval.
 //
 // Some callers cannot allocate device memory: a process whose device memory
-// belongs to another framework's pool, code that runs while a stream is
-// being captured into a CUDA graph, or a latency-bound loop where the
+// belongs to another framework's pool, or a latency-bound loop where the
 // implicit synchronisation of cudaMalloc / cudaFree is not allowed.  For
 // them this file provides sg_pr_peval_noalloc: the caller passes the graph
 // and the output buffers in device memory, and the only scratch the

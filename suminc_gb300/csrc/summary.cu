@@ -37,6 +37,19 @@ void host_transpose(const HostAdj& out, HostAdj& in);
 void host_adj_from_csr(uint32_t n, const uint64_t* rp, const uint32_t* col, const float* w,
                        HostAdj& out);
 
+// cluster precompute staged in shared memory: clusters of up to kStageCap
+// members (8-bit local indices) and kStageEdges local edges, one per warp
+constexpr int kStageCap = 160;
+constexpr int kStageEdges = 2048;
+constexpr int kStageWarps = 8;
+
+struct StageLists {
+  const uint64_t* lin_off;   // per cm_v position: local in-edges
+  const uint8_t* lin_src;    // their tails, as local indices
+  const uint64_t* lout_off;  // per cm_v position: edges to out-mirrors
+  const uint32_t* lout_dst;
+};
+
 struct SummaryDev {
   bool valid = false;
   uint32_t old_n = 0, all_n = 0;
@@ -59,11 +72,15 @@ struct SummaryDev {
   // cluster precompute: members and subgraph CSR
   uint64_t *cm_off = nullptr, *sub_off = nullptr;
   uint32_t *cm_v = nullptr, *sub_nbr = nullptr;
+  uint64_t *lin_off = nullptr, *lout_off = nullptr;  // per cm_v position (staged clusters)
+  uint8_t* lin_src = nullptr;
+  uint32_t* lout_dst = nullptr;
   uint32_t *bound_list = nullptr;  // exit members per cluster (cm layout)
   uint64_t* bl_off = nullptr;
   // state
   float *bound = nullptr, *spnode = nullptr, *old_x = nullptr;
   double* d_res = nullptr;
+  uint32_t* sctl = nullptr;  // summarized rounds: done flag, blocks finished, rounds run
   std::vector<uint32_t> pending_clusters;  // touched since the last IncEval
   // SSSP over the summary: shortcut distances per supernode (entry -> exit /
   // out-mirror, entry -> inner member), the summarized CSR and the
@@ -91,8 +108,9 @@ static void sfree(SummaryDev& D) {
   dfree(D.corr_sp); dfree(D.corr_c);
   dfree(D.id_off); dfree(D.iv_off); dfree(D.id_nbr); dfree(D.iv_nbr); dfree(D.id_w); dfree(D.iv_w);
   dfree(D.cm_off); dfree(D.sub_off); dfree(D.cm_v); dfree(D.sub_nbr);
+  dfree(D.lin_off); dfree(D.lin_src); dfree(D.lout_off); dfree(D.lout_dst);
   dfree(D.bound_list); dfree(D.bl_off);
-  dfree(D.bound); dfree(D.spnode); dfree(D.old_x); dfree(D.d_res);
+  dfree(D.bound); dfree(D.spnode); dfree(D.old_x); dfree(D.d_res); dfree(D.sctl);
   dfree(D.sk_off); dfree(D.sk_coff); dfree(D.sk_deg); dfree(D.sk_col); dfree(D.sk_crow);
   dfree(D.sk_cv); dfree(D.sk_w); dfree(D.sk_cd);
 }
@@ -402,10 +420,52 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
     for (uint32_t t : S.subgraph[v]) subn.push_back(t);
     subo.push_back(subn.size());
   }
+  // Per member position of cm_v, for clusters of at most kStageCap members:
+  // the local in-edges inside the cluster (tails as 8-bit local indices) and
+  // the out-edges to the cluster's out-mirrors (global ids).  Larger clusters
+  // keep empty lists and use the subgraph CSR.
+  std::vector<uint64_t> lino(1, 0), louto(1, 0);
+  std::vector<uint8_t> lins;
+  std::vector<uint32_t> loutd;
+  {
+    std::vector<uint32_t> slot(all, ~0u);
+    std::vector<std::vector<uint8_t>> inl;
+    for (size_t c = 0; c < S.supernode_ids.size(); ++c) {
+      const auto& M = S.supernode_ids[c];
+      const size_t m = M.size();
+      if (m > (size_t)kStageCap) {
+        for (size_t i = 0; i < m; ++i) {
+          lino.push_back(lins.size());
+          louto.push_back(loutd.size());
+        }
+        continue;
+      }
+      for (size_t j = 0; j < m; ++j) slot[M[j]] = (uint32_t)j;
+      inl.assign(m, {});
+      for (size_t i = 0; i < m; ++i) {
+        for (uint32_t t : S.subgraph[M[i]]) {
+          if (t < all && slot[t] != ~0u && M[slot[t]] == t)
+            inl[slot[t]].push_back((uint8_t)i);
+          else
+            loutd.push_back(t);
+        }
+        louto.push_back(loutd.size());
+      }
+      for (size_t j = 0; j < m; ++j) {
+        lins.insert(lins.end(), inl[j].begin(), inl[j].end());
+        lino.push_back(lins.size());
+      }
+      for (size_t j = 0; j < m; ++j) slot[M[j]] = ~0u;
+    }
+  }
   SG_TRY(upload(ctx, &D.cm_off, cmo));
   SG_TRY(upload(ctx, &D.cm_v, cmv));
   SG_TRY(upload(ctx, &D.sub_off, subo));
   SG_TRY(upload(ctx, &D.sub_nbr, subn));
+  SG_TRY(upload(ctx, &D.lin_off, lino));
+  SG_TRY(upload(ctx, &D.lin_src, lins));
+  SG_TRY(upload(ctx, &D.lout_off, louto));
+  SG_TRY(upload(ctx, &D.lout_dst, loutd));
   SG_TRY(upload(ctx, &D.bl_off, blo));
   SG_TRY(upload(ctx, &D.bound_list, bl));
   if (!D.bound) {
@@ -413,6 +473,7 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
     SG_TRY(dalloc(ctx, &D.spnode, all));
     SG_TRY(dalloc(ctx, &D.old_x, n));
     SG_TRY(dalloc(ctx, &D.d_res, 2));
+    SG_TRY(dalloc(ctx, &D.sctl, 4));
   }
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return SG_OK;
@@ -497,7 +558,17 @@ struct SumArgs {
   const uint32_t* out_deg_all;
   const uint8_t* ntype;
   unsigned long long* cnt;  // [0] edges, [1] shortcut edges
+  // on-device termination of the summarized rounds: sctl [0] done, [1] blocks
+  // finished in the residual pass, [2] rounds run; sres [0] running sum,
+  // [1] the last round's residual
+  uint32_t* sctl;
+  double* sres;
+  double tau;
 };
+
+__device__ __forceinline__ bool rounds_done(const SumArgs& A) {
+  return *(volatile uint32_t*)A.sctl != 0u;
+}
 
 // mass a (mirror) entry receives goes along its shortcuts into exit buffers
 __device__ __forceinline__ void entry_push(const SumArgs& A, uint32_t u, float d, uint32_t lane,
@@ -511,6 +582,7 @@ __device__ __forceinline__ void entry_push(const SumArgs& A, uint32_t u, float d
 }
 
 __global__ void __launch_bounds__(256) k_sum_entries(SumArgs A, const uint32_t* list, uint32_t cnt) {
+  if (rounds_done(A)) return;
   const uint32_t lane = threadIdx.x & 31;
   unsigned long long sc = 0;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt;
@@ -528,6 +600,7 @@ __global__ void __launch_bounds__(256) k_sum_entries(SumArgs A, const uint32_t* 
 }
 
 __global__ void __launch_bounds__(256) k_sum_exits(SumArgs A, const uint32_t* list, uint32_t cnt) {
+  if (rounds_done(A)) return;
   const uint32_t lane = threadIdx.x & 31;
   unsigned long long ed = 0, sc = 0;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt;
@@ -568,6 +641,7 @@ __global__ void __launch_bounds__(256) k_sum_exits(SumArgs A, const uint32_t* li
 }
 
 __global__ void __launch_bounds__(256) k_sum_singles(SumArgs A, const uint32_t* list, uint32_t cnt) {
+  if (rounds_done(A)) return;
   const uint32_t lane = threadIdx.x & 31;
   unsigned long long ed = 0;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt;
@@ -591,19 +665,38 @@ __global__ void __launch_bounds__(256) k_sum_singles(SumArgs A, const uint32_t* 
 }
 
 __global__ void k_sum_omirror(SumArgs A, const uint32_t* list, const uint32_t* master, uint32_t cnt) {
+  if (rounds_done(A)) return;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
     const uint32_t m = list[i];
     if (fabsf(A.bound[m]) > A.thr_v) atomicAdd(&A.delta[master[i]], atomicExch(&A.bound[m], 0.f));
   }
 }
 
-__global__ void __launch_bounds__(256) k_sum_residual(uint32_t n, const float* delta, double* res) {
+// residual of a summarized round and, in its last block, the termination
+// decision (termCheck, sum_sync_iter_worker.h:2873-2912)
+__global__ void __launch_bounds__(256) k_sum_residual_decide(SumArgs A, uint32_t n) {
   __shared__ double s_red[8];
+  __shared__ bool s_last;
+  if (rounds_done(A)) return;
   double r = 0.0;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
-    r += fabs((double)delta[v]);
+    r += fabs((double)A.delta[v]);
   const double b = block_sum<256>(r, s_red);
-  if (threadIdx.x == 0) atomicAdd(res, b);
+  if (threadIdx.x == 0) {
+    if (b != 0.0) atomicAdd(A.sres, b);
+    __threadfence();
+    s_last = atomicAdd(A.sctl + 1, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    const double R = atomicAdd(A.sres, 0.0);
+    A.sres[0] = 0.0;
+    A.sres[1] = R;
+    A.sctl[1] = 0;
+    A.sctl[2] += 1;
+    if (R < A.tau) A.sctl[0] = 1;
+  }
 }
 
 // correction through inner_delta / inner_value (warp per row)
@@ -628,22 +721,85 @@ __global__ void __launch_bounds__(256) k_sum_correct(SumArgs A, uint32_t all_n, 
   }
 }
 
-// cluster-local convergence of the current deltas (CTA per cluster)
+// Cluster-local convergence of the current deltas (the precompute of
+// iter_compressor.h:534-785: local iteration of each supernode until its delta
+// mass falls under the per-vertex threshold times its size, at most 100 steps).
+// One warp per cluster.  A cluster of up to kStageCap members and
+// kStageEdges local edges is staged in shared memory and iterated in two
+// phases per step with no atomics inside the cluster: each member takes its
+// delta and publishes its push value (sending to the cluster's out-mirrors,
+// which only this cluster writes, by global atomics), then each member sums
+// the push values of its local in-edges.  Larger clusters push on global
+// memory.  A member belongs to one cluster and the list holds each cluster
+// once, so the staged copy is the only writer of its members' deltas.
 __global__ void __launch_bounds__(256) k_sum_precompute(SumArgs A, const uint32_t* clusters,
                                                         uint32_t n_cl, const uint64_t* cm_off,
                                                         const uint32_t* cm_v,
                                                         const uint64_t* sub_off,
-                                                        const uint32_t* sub_nbr, double thr_v) {
-  __shared__ double s_diff;
-  for (uint32_t k = blockIdx.x; k < n_cl; k += gridDim.x) {
+                                                        const uint32_t* sub_nbr, StageLists L,
+                                                        double thr_v) {
+  __shared__ float s_d[kStageWarps][kStageCap];
+  __shared__ float s_x[kStageWarps][kStageCap];
+  __shared__ float s_pv[kStageWarps][kStageCap];
+  __shared__ float s_deg[kStageWarps][kStageCap];
+  __shared__ uint16_t s_lo[kStageWarps][kStageCap + 2];
+  __shared__ uint8_t s_ls[kStageWarps][kStageEdges];
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n_cl; k += nwarps) {
     const uint32_t c = clusters[k];
     const uint64_t b = cm_off[c], e = cm_off[c + 1];
-    const double thr = thr_v * (double)(e - b);
+    const uint32_t m = (uint32_t)(e - b);
+    const double thr = thr_v * (double)m;
+    const uint64_t l0 = L.lin_off[b], nl = L.lin_off[e] - l0;
+    if (m <= (uint32_t)kStageCap && nl <= (uint64_t)kStageEdges) {
+      for (uint32_t i = lane; i < m; i += 32) {
+        const uint32_t v = cm_v[b + i];
+        s_d[w][i] = A.delta[v];
+        s_x[w][i] = 0.f;
+        s_deg[w][i] = (float)A.out_deg_all[v];
+        s_lo[w][i + 1] = (uint16_t)(L.lin_off[b + i + 1] - l0);
+      }
+      if (lane == 0) s_lo[w][0] = 0;
+      for (uint32_t j = lane; j < (uint32_t)nl; j += 32) s_ls[w][j] = L.lin_src[l0 + j];
+      __syncwarp();
+      for (int step = 1;; ++step) {
+        double diff = 0.0;
+        for (uint32_t i = lane; i < m; i += 32) {
+          const float ts = s_d[w][i];
+          float pv = 0.f;
+          if (ts != 0.f) {
+            s_d[w][i] = 0.f;
+            s_x[w][i] += ts;
+            diff += fabs((double)ts);
+            pv = ts * A.damping / s_deg[w][i];
+            for (uint64_t f = L.lout_off[b + i]; f < L.lout_off[b + i + 1]; ++f)
+              atomicAdd(&A.delta[L.lout_dst[f]], pv);
+          }
+          s_pv[w][i] = pv;
+        }
+        __syncwarp();
+        for (uint32_t j = lane; j < m; j += 32) {
+          float acc = 0.f;
+          for (uint32_t f = s_lo[w][j]; f < s_lo[w][j + 1]; ++f) acc += s_pv[w][s_ls[w][f]];
+          if (acc != 0.f) s_d[w][j] += acc;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) diff += __shfl_xor_sync(0xffffffffu, diff, o);
+        __syncwarp();  // this step's sums are visible to the next step's reads
+        if (diff <= thr || step > 100) break;
+      }
+      for (uint32_t i = lane; i < m; i += 32) {
+        const uint32_t v = cm_v[b + i];
+        A.delta[v] = s_d[w][i];
+        A.x[v] += s_x[w][i];
+      }
+      __syncwarp();
+      continue;
+    }
     for (int step = 1;; ++step) {
-      if (threadIdx.x == 0) s_diff = 0.0;
-      __syncthreads();
       double diff = 0.0;
-      for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+      for (uint64_t i = b + lane; i < e; i += 32) {
         const uint32_t v = cm_v[i];
         const float ts = atomicExch(&A.delta[v], 0.f);
         if (ts == 0.f) continue;
@@ -652,11 +808,10 @@ __global__ void __launch_bounds__(256) k_sum_precompute(SumArgs A, const uint32_
         const float outv = ts * A.damping / (float)A.out_deg_all[v];
         for (uint64_t f = sub_off[v]; f < sub_off[v + 1]; ++f) atomicAdd(&A.delta[sub_nbr[f]], outv);
       }
-      if (diff != 0.0) atomicAdd(&s_diff, diff);
-      __syncthreads();
-      const double d = s_diff;
-      __syncthreads();
-      if (d <= thr || step > 100) break;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) diff += __shfl_xor_sync(0xffffffffu, diff, o);
+      __syncwarp();  // this step's pushes are visible to the next step's reads
+      if (diff <= thr || step > 100) break;
     }
   }
 }
@@ -723,6 +878,9 @@ static SumArgs sum_args(sg_ctx* ctx, SummaryDev& D, unsigned long long* cnt) {
   A.out_deg_all = D.out_deg_all;
   A.ntype = D.ntype;
   A.cnt = cnt;
+  A.sctl = D.sctl;
+  A.sres = D.d_res;
+  A.tau = ctx->opt.termcheck_threshold;
   return A;
 }
 
@@ -738,9 +896,12 @@ static sg_status first_step(sg_ctx* ctx, SummaryDev& D, const std::vector<uint32
   uint32_t* d_cls = nullptr;
   SG_TRY(upload(ctx, &d_cls, cls));
   k_stash_x<<<grid_for(D.old_n, 256), 256, 0, st>>>(D.old_n, ctx->pr.x, D.old_x, 0);
-  k_sum_precompute<<<std::min<uint32_t>((uint32_t)cls.size(), ctx->num_sms * 8), 256, 0, st>>>(
+  kprof_begin(ctx);
+  k_sum_precompute<<<grid_for((uint64_t)cls.size() * 32, 32 * kStageWarps), 32 * kStageWarps, 0, st>>>(
       A, d_cls, (uint32_t)cls.size(), D.cm_off, D.cm_v, D.sub_off, D.sub_nbr,
+      StageLists{D.lin_off, D.lin_src, D.lout_off, D.lout_dst},
       ctx->opt.termcheck_threshold / (double)D.old_n);
+  kprof_end(ctx, SG_K_SUM_LOCAL);
   k_sum_bound_push<<<std::min<uint32_t>((uint32_t)cls.size(), ctx->num_sms * 8), 256, 0, st>>>(
       A, d_cls, (uint32_t)cls.size(), D.bl_off, D.bound_list);
   if (D.n_omirror)
@@ -759,27 +920,31 @@ static sg_status summarized_rounds(sg_ctx* ctx, SummaryDev& D, unsigned long lon
                                    int* rounds_out) {
   cudaStream_t st = ctx->stream;
   SumArgs A = sum_args(ctx, D, cnt);
-  const double tau = ctx->opt.termcheck_threshold;
   const int cap = ctx->opt.max_rounds > 0 ? ctx->opt.max_rounds : 1000;
-  int r = 0;
-  for (; r < cap; ++r) {
-    kprof_begin(ctx);
-    if (D.n_entry) k_sum_entries<<<grid_for((uint64_t)D.n_entry * 32, 256), 256, 0, st>>>(A, D.l_entry, D.n_entry);
-    if (D.n_exit) k_sum_exits<<<grid_for((uint64_t)D.n_exit * 32, 256), 256, 0, st>>>(A, D.l_exit, D.n_exit);
-    if (D.n_single) k_sum_singles<<<grid_for((uint64_t)D.n_single * 32, 256), 256, 0, st>>>(A, D.l_single, D.n_single);
-    if (D.n_omirror) k_sum_omirror<<<grid_for(D.n_omirror, 256), 256, 0, st>>>(A, D.l_omirror, D.omirror_master, D.n_omirror);
-    SG_CUDA(ctx, cudaMemsetAsync(D.d_res, 0, 8, st));
-    k_sum_residual<<<grid_for(D.old_n, 256), 256, 0, st>>>(D.old_n, ctx->pr.delta, D.d_res);
-    kprof_end(ctx, SG_K_SUMMARY);
-    count_launch(ctx, 4);
-    double R = 0;
-    SG_CUDA(ctx, cudaMemcpyAsync(&R, D.d_res, 8, cudaMemcpyDeviceToHost, st));
-    SG_CUDA(ctx, cudaStreamSynchronize(st));
-    if (R < tau) {
-      ++r;
-      break;
+  // rounds in chunks of 4 with the residual test on the device; once it
+  // passes, the chunk's remaining kernels return at once
+  SG_CUDA(ctx, cudaMemsetAsync(D.sctl, 0, 4 * sizeof(uint32_t), st));
+  SG_CUDA(ctx, cudaMemsetAsync(D.d_res, 0, 2 * sizeof(double), st));
+  const unsigned rblocks = grid_for(D.old_n, 256, ctx->num_sms * 4);
+  uint32_t h_ctl[4] = {0, 0, 0, 0};
+  int launched = 0;
+  while (launched < cap) {
+    for (int c = 0; c < 4 && launched < cap; ++c, ++launched) {
+      kprof_begin(ctx);
+      if (D.n_entry) k_sum_entries<<<grid_for((uint64_t)D.n_entry * 32, 256), 256, 0, st>>>(A, D.l_entry, D.n_entry);
+      if (D.n_exit) k_sum_exits<<<grid_for((uint64_t)D.n_exit * 32, 256), 256, 0, st>>>(A, D.l_exit, D.n_exit);
+      if (D.n_single) k_sum_singles<<<grid_for((uint64_t)D.n_single * 32, 256), 256, 0, st>>>(A, D.l_single, D.n_single);
+      if (D.n_omirror) k_sum_omirror<<<grid_for(D.n_omirror, 256), 256, 0, st>>>(A, D.l_omirror, D.omirror_master, D.n_omirror);
+      k_sum_residual_decide<<<rblocks, 256, 0, st>>>(A, D.old_n);
+      kprof_end(ctx, SG_K_SUMMARY);
+      count_launch(ctx, 1 + (D.n_entry > 0) + (D.n_exit > 0) + (D.n_single > 0) + (D.n_omirror > 0));
     }
+    SG_CUDA(ctx, cudaGetLastError());
+    SG_CUDA(ctx, cudaMemcpyAsync(h_ctl, D.sctl, sizeof(h_ctl), cudaMemcpyDeviceToHost, st));
+    SG_CUDA(ctx, cudaStreamSynchronize(st));
+    if (h_ctl[0]) break;
   }
+  const int r = (int)h_ctl[2];
   k_sum_correct<<<grid_for((uint64_t)D.all_n * 32, 256), 256, 0, st>>>(
       A, D.all_n, D.corr_sp, D.corr_c, D.id_off, D.id_nbr, D.id_w, D.iv_off, D.iv_nbr, D.iv_w);
   count_launch(ctx);

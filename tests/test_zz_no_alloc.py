@@ -1,8 +1,7 @@
 """The allocation-free PageRank entry point (sg_pr_peval_noalloc).
 
 It serves callers that cannot allocate device memory (memory owned by
-another framework's pool, work issued during stream capture, loops that must
-not synchronise on cudaMalloc): they hand in the graph and the outputs in
+another framework's pool, loops that must not synchronise on cudaMalloc): they hand in the graph and the outputs in
 device memory, and the kernels use a fixed scratch array inside the library.
 Checked through the C ABI against sg_pr_peval on the same graph, on two calls
 in a row (the scratch array is shared and must be re-initialised by every
