@@ -275,6 +275,80 @@ void host_transpose(const HostAdj& out, HostAdj& in) {
     }
 }
 
+bool host_adj_patch(HostAdj& a, const std::vector<AdjOp>& ops) {
+  const uint32_t n = a.n;
+  const bool weighted = !a.w.empty();
+  for (const AdjOp& op : ops)
+    if (op.row >= n || op.col >= n) return false;
+  // new row pointers: old offsets shifted by the net insertions so far
+  std::vector<uint64_t> rp(n + 1);
+  rp[0] = 0;
+  {
+    int64_t shift = 0;
+    size_t k = 0;
+    for (uint32_t v = 0; v < n; ++v) {
+      for (; k < ops.size() && ops[k].row == v; ++k)
+        shift += ops[k].kind == AdjOp::kInsert ? 1 : (ops[k].kind == AdjOp::kRemove ? -1 : 0);
+      rp[v + 1] = (uint64_t)((int64_t)a.rp[v + 1] + shift);
+    }
+  }
+  std::vector<uint32_t> col(rp[n]);
+  std::vector<float> w(weighted ? rp[n] : 0);
+  uint32_t next = 0;  // first row not yet copied
+  size_t k = 0;
+  while (k < ops.size()) {
+    const uint32_t r = ops[k].row;
+    size_t ke = k;
+    while (ke < ops.size() && ops[ke].row == r) ++ke;
+    // rows next..r-1 are unchanged: one bulk move
+    if (r > next) {
+      const uint64_t b = a.rp[next], e = a.rp[r];
+      std::copy(a.col.begin() + b, a.col.begin() + e, col.begin() + rp[next]);
+      if (weighted) std::copy(a.w.begin() + b, a.w.begin() + e, w.begin() + rp[next]);
+    }
+    // merge row r with its changes (every write checked against the row's
+    // new extent, so an op that does not fit cannot write past it)
+    uint64_t i = a.rp[r], o = rp[r];
+    const uint64_t ie = a.rp[r + 1], oe = rp[r + 1];
+    auto emit = [&](uint32_t c, float wv) {
+      if (o >= oe) return false;
+      col[o] = c;
+      if (weighted) w[o] = wv;
+      ++o;
+      return true;
+    };
+    for (size_t j = k; j < ke; ++j) {
+      const AdjOp& op = ops[j];
+      for (; i < ie && a.col[i] < op.col; ++i)
+        if (!emit(a.col[i], weighted ? a.w[i] : 0.f)) return false;
+      const bool here = i < ie && a.col[i] == op.col;
+      if (op.kind == AdjOp::kRemove) {
+        if (!here) return false;
+        ++i;
+      } else if (op.kind == AdjOp::kSetWeight) {
+        if (!here || !emit(op.col, op.w)) return false;
+        ++i;
+      } else {
+        if (here || !emit(op.col, op.w)) return false;
+      }
+    }
+    for (; i < ie; ++i)
+      if (!emit(a.col[i], weighted ? a.w[i] : 0.f)) return false;
+    if (o != oe) return false;
+    next = r + 1;
+    k = ke;
+  }
+  if (next < n) {
+    const uint64_t b = a.rp[next], e = a.rp[n];
+    std::copy(a.col.begin() + b, a.col.begin() + e, col.begin() + rp[next]);
+    if (weighted) std::copy(a.w.begin() + b, a.w.begin() + e, w.begin() + rp[next]);
+  }
+  a.rp.swap(rp);
+  a.col.swap(col);
+  a.w.swap(w);
+  return true;
+}
+
 void host_adj_from_csr(uint32_t n, const uint64_t* rp, const uint32_t* col, const float* w,
                        HostAdj& out) {
   out.n = n;

@@ -521,12 +521,17 @@ void summary_judge_out_bound(Summary& S, const HostAdj& out, const std::vector<u
         }
       }
   };
+  // a cluster's judgement writes only its own members (parallel); the
+  // in-mirror masters live in other clusters (serial)
   if (only) {
-    for (uint32_t j : *only) judge(j);
-    for (uint32_t j : *only)
+    const std::vector<uint32_t>& L = *only;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long long k = 0; k < (long long)L.size(); ++k) judge(L[k]);
+    for (uint32_t j : L)
       for (uint32_t v : S.supernode_in_mirror[j]) S.out_bound[v] = 1;
   } else {
-    for (uint32_t j = 0; j < nc; ++j) judge(j);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long long j = 0; j < (long long)nc; ++j) judge((uint32_t)j);
     for (uint32_t j = 0; j < nc; ++j)
       for (uint32_t v : S.supernode_in_mirror[j]) S.out_bound[v] = 1;
   }
@@ -574,10 +579,15 @@ void summary_build_subgraph(Summary& S, const HostAdj& out, const HostAdj& in,
       }
     }
   };
+  // a cluster writes the rows of its own members and mirrors only; the
+  // lists hold each cluster once
   if (only) {
-    for (uint32_t i : *only) build(i);
+    const std::vector<uint32_t>& L = *only;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long long k = 0; k < (long long)L.size(); ++k) build(L[k]);
   } else {
-    for (uint32_t i = 0; i < S.supernode_ids.size(); ++i) build(i);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long long i = 0; i < (long long)S.supernode_ids.size(); ++i) build((uint32_t)i);
   }
 }
 
@@ -609,18 +619,22 @@ void summary_node_types(Summary& S) {
 void summary_sketch_csr(Summary& S, const HostAdj& out) {
   const uint32_t all = S.all_n, n = S.old_n;
   const bool weighted = !out.w.empty();
-  // sync edges
-  std::vector<std::vector<uint32_t>> syncE(all);
-  for (size_t i = 0; i < S.cluster_in_mirror_ids.size(); ++i) {
-    for (uint32_t m : S.cluster_in_mirror_ids[i]) syncE[S.mirror_master(m)].push_back(m);
-    for (uint32_t m : S.cluster_out_mirror_ids[i]) syncE[m].push_back(S.mirror_master(m));
-  }
+  // sync edges: master -> its in-mirrors, out-mirror -> its master, in the
+  // order of the clusters and their mirror lists (counting sort)
   S.sync_off.assign(all + 1, 0);
-  for (uint32_t i = 0; i < all; ++i) S.sync_off[i + 1] = S.sync_off[i] + syncE[i].size();
-  S.sync_nbr.clear();
-  S.sync_nbr.reserve(S.sync_off[all]);
-  for (uint32_t i = 0; i < all; ++i)
-    for (uint32_t m : syncE[i]) S.sync_nbr.push_back(m);
+  for (size_t i = 0; i < S.cluster_in_mirror_ids.size(); ++i) {
+    for (uint32_t m : S.cluster_in_mirror_ids[i]) S.sync_off[S.mirror_master(m) + 1]++;
+    for (uint32_t m : S.cluster_out_mirror_ids[i]) S.sync_off[m + 1]++;
+  }
+  for (uint32_t i = 0; i < all; ++i) S.sync_off[i + 1] += S.sync_off[i];
+  S.sync_nbr.assign(S.sync_off[all], 0);
+  {
+    std::vector<uint64_t> pos(S.sync_off.begin(), S.sync_off.end() - 1);
+    for (size_t i = 0; i < S.cluster_in_mirror_ids.size(); ++i) {
+      for (uint32_t m : S.cluster_in_mirror_ids[i]) S.sync_nbr[pos[S.mirror_master(m)]++] = m;
+      for (uint32_t m : S.cluster_out_mirror_ids[i]) S.sync_nbr[pos[m]++] = S.mirror_master(m);
+    }
+  }
   // shortcut and boundary edges
   auto is_row = [&](uint32_t i) -> const Supernode* {
     if (i >= n) {
@@ -641,39 +655,58 @@ void summary_sketch_csr(Summary& S, const HostAdj& out) {
     }
     return ids != out_ids && om.count(x) == 0;
   };
+  // 0: no boundary row, 1: filtered out-edges, 2: all out-edges
+  auto ib_mode = [&](uint32_t i) -> int {
+    if (i >= n) return 0;
+    const char t = S.node_type[i];
+    if (t == kOnlyOut || t == kBothOutIn || t == kBothOutInMaster || t == kOutMaster) return 1;
+    return t == kSingle ? 2 : 0;
+  };
+  // two passes over the rows (counts, then fills at prefix offsets)
   S.is_off.assign(all + 1, 0);
   S.ib_off.assign(all + 1, 0);
-  S.is_nbr.clear();
-  S.is_w.clear();
-  S.ib_nbr.clear();
-  S.ib_w.clear();
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (long long ii = 0; ii < (long long)all; ++ii) {
+    const uint32_t i = (uint32_t)ii;
+    if (const Supernode* sp = is_row(i)) S.is_off[i + 1] = sp->bound_delta.size();
+    const int mode = ib_mode(i);
+    uint64_t c = 0;
+    if (mode == 2) {
+      c = out.deg(i);
+    } else if (mode == 1) {
+      for (uint64_t e = out.rp[i]; e < out.rp[i + 1]; ++e) c += ib_take(i, out.col[e]);
+    }
+    S.ib_off[i + 1] = c;
+  }
   for (uint32_t i = 0; i < all; ++i) {
+    S.is_off[i + 1] += S.is_off[i];
+    S.ib_off[i + 1] += S.ib_off[i];
+  }
+  S.is_nbr.assign(S.is_off[all], 0);
+  S.is_w.assign(S.is_off[all], 0.f);
+  S.ib_nbr.assign(S.ib_off[all], 0);
+  S.ib_w.assign(weighted ? S.ib_off[all] : 0, 0.f);
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (long long ii = 0; ii < (long long)all; ++ii) {
+    const uint32_t i = (uint32_t)ii;
     if (const Supernode* sp = is_row(i)) {
       std::vector<std::pair<uint32_t, double>> row = sp->bound_delta;
       std::stable_sort(row.begin(), row.end(),
                        [](const auto& a, const auto& b) { return a.first < b.first; });
+      uint64_t k = S.is_off[i];
       for (auto& e : row) {
-        S.is_nbr.push_back(e.first);
-        S.is_w.push_back((float)e.second);
+        S.is_nbr[k] = e.first;
+        S.is_w[k++] = (float)e.second;
       }
     }
-    S.is_off[i + 1] = S.is_nbr.size();
-    if (i < n) {
-      const char t = S.node_type[i];
-      if (t == kOnlyOut || t == kBothOutIn || t == kBothOutInMaster || t == kOutMaster) {
-        for (uint64_t e = out.rp[i]; e < out.rp[i + 1]; ++e)
-          if (ib_take(i, out.col[e])) {
-            S.ib_nbr.push_back(out.col[e]);
-            if (weighted) S.ib_w.push_back(out.w[e]);
-          }
-      } else if (t == kSingle) {
-        for (uint64_t e = out.rp[i]; e < out.rp[i + 1]; ++e) {
-          S.ib_nbr.push_back(out.col[e]);
-          if (weighted) S.ib_w.push_back(out.w[e]);
-        }
+    const int mode = ib_mode(i);
+    uint64_t k = S.ib_off[i];
+    for (uint64_t e = mode ? out.rp[i] : 0; mode && e < out.rp[i + 1]; ++e)
+      if (mode == 2 || ib_take(i, out.col[e])) {
+        S.ib_nbr[k] = out.col[e];
+        if (weighted) S.ib_w[k] = out.w[e];
+        ++k;
       }
-    }
-    S.ib_off[i + 1] = S.ib_nbr.size();
   }
 }
 

@@ -69,7 +69,8 @@ struct SummaryDev {
   uint64_t *id_off = nullptr, *iv_off = nullptr;
   uint32_t *id_nbr = nullptr, *iv_nbr = nullptr;
   float *id_w = nullptr, *iv_w = nullptr;
-  // cluster precompute: members and subgraph CSR
+  // cluster precompute: members (cm layout: clusters in order) and, per
+  // member position, the subgraph out-edges of clusters that are not staged
   uint64_t *cm_off = nullptr, *sub_off = nullptr;
   uint32_t *cm_v = nullptr, *sub_nbr = nullptr;
   uint64_t *lin_off = nullptr, *lout_off = nullptr;  // per cm_v position (staged clusters)
@@ -224,28 +225,55 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
     const uint32_t c = S.supernodes[sp].ids;
     if (cl_index.emplace(c, (uint32_t)cls.size()).second) cls.push_back(c);
   }
-  std::vector<uint64_t> cl_off(cls.size() + 1, 0), adj_off(1, 0);
-  std::vector<uint32_t> cl_inner(cls.size()), adj_nbr;
-  std::vector<float> div;
+  // local problems, one per cluster: nodes (members, then mirrors), the
+  // divisor of each, and the subgraph edges as local indices; built in two
+  // parallel passes (sizes, then fills at prefix offsets).  A node's local
+  // index is kept in local_of; nodes of different clusters are distinct.
+  const size_t ncl = cls.size();
+  std::vector<uint64_t> cl_off(ncl + 1, 0), cl_adj(ncl + 1, 0);
+  std::vector<uint32_t> cl_inner(ncl);
   std::vector<uint32_t> local_of(S.all_n, 0xFFFFFFFFu);
   size_t maxL = 1;
-  for (size_t k = 0; k < cls.size(); ++k) {
-    const uint32_t c = cls[k];
-    const auto& nodes = S.cluster_ids[c];  // members first, then mirror ids
-    const uint32_t inner = (uint32_t)S.supernode_ids[c].size();
-    cl_inner[k] = inner;
-    for (uint32_t i = 0; i < nodes.size(); ++i) local_of[nodes[i]] = i;
+  for (size_t k = 0; k < ncl; ++k) {
+    const auto& nodes = S.cluster_ids[cls[k]];  // members first, then mirror ids
+    cl_off[k + 1] = cl_off[k] + nodes.size();
+    maxL = std::max(maxL, nodes.size());
+  }
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long k = 0; k < (long long)ncl; ++k) {
+    const auto& nodes = S.cluster_ids[cls[k]];
+    uint64_t ne = 0;
+    for (uint32_t i = 0; i < nodes.size(); ++i) {
+      local_of[nodes[i]] = i;
+      ne += S.subgraph[nodes[i]].size();
+    }
+    cl_adj[k + 1] = ne;
+    cl_inner[k] = (uint32_t)S.supernode_ids[cls[k]].size();
+  }
+  for (size_t k = 0; k < ncl; ++k) cl_adj[k + 1] += cl_adj[k];
+  std::vector<uint64_t> adj_off(cl_off[ncl] + 1);
+  std::vector<uint32_t> adj_nbr(cl_adj[ncl]);
+  std::vector<float> div(cl_off[ncl]);
+  bool foreign = false;
+#pragma omp parallel for schedule(dynamic, 256) reduction(|| : foreign)
+  for (long long k = 0; k < (long long)ncl; ++k) {
+    const auto& nodes = S.cluster_ids[cls[k]];
+    uint64_t e = cl_adj[k];
     for (uint32_t i = 0; i < nodes.size(); ++i) {
       const uint32_t v = nodes[i];
       const uint32_t master = v < S.old_n ? v : S.mirror_master(v);
-      div.push_back((float)std::max<uint64_t>(D.out.deg(master), 1));
-      for (uint32_t t : S.subgraph[v]) adj_nbr.push_back(local_of[t]);
-      adj_off.push_back(adj_nbr.size());
+      div[cl_off[k] + i] = (float)std::max<uint64_t>(D.out.deg(master), 1);
+      adj_off[cl_off[k] + i] = e;
+      for (uint32_t t : S.subgraph[v]) {
+        const uint32_t l = local_of[t];
+        // every subgraph edge stays inside its cluster's nodes
+        if (l >= nodes.size() || nodes[l] != t) foreign = true;
+        adj_nbr[e++] = l < nodes.size() ? l : 0u;
+      }
     }
-    cl_off[k + 1] = cl_off[k] + nodes.size();
-    maxL = std::max(maxL, nodes.size());
-    for (uint32_t v : nodes) local_of[v] = 0xFFFFFFFFu;
   }
+  adj_off[cl_off[ncl]] = cl_adj[ncl];
+  if (foreign) return fail(ctx, SG_ERR_STATE, "subgraph edge leaves its cluster");
   std::vector<uint32_t> sp_cluster(spids.size()), sp_src(spids.size());
   std::vector<uint64_t> out_off(spids.size() + 1, 0);
   for (size_t j = 0; j < spids.size(); ++j) {
@@ -253,10 +281,8 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
     const uint32_t k = cl_index[sp.ids];
     sp_cluster[j] = k;
     const auto& nodes = S.cluster_ids[sp.ids];
-    uint32_t src = 0;
-    for (uint32_t i = 0; i < nodes.size(); ++i)
-      if (nodes[i] == sp.id) src = i;
-    sp_src[j] = src;
+    const uint32_t l = local_of[sp.id];
+    sp_src[j] = (l < nodes.size() && nodes[l] == sp.id) ? l : 0u;
     out_off[j + 1] = out_off[j] + (cl_off[k + 1] - cl_off[k]);
   }
   const size_t smem = 3 * maxL * sizeof(double);
@@ -302,8 +328,10 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   dfree(d_spc); dfree(d_src); dfree(d_inner); dfree(d_adj); dfree(d_cloff); dfree(d_adjoff);
   dfree(d_outoff); dfree(d_div); dfree(d_val); dfree(d_del);
-  // fianl_build_iter_index_for_mirror (iter_compressor.h:433-491)
-  for (size_t j = 0; j < spids.size(); ++j) {
+  // fianl_build_iter_index_for_mirror (iter_compressor.h:433-491); each
+  // supernode writes only its own lists
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long j = 0; j < (long long)spids.size(); ++j) {
     Supernode& sp = S.supernodes[spids[j]];
     const uint32_t c = sp.ids;
     const auto& nodes = S.cluster_ids[c];
@@ -323,8 +351,8 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
     }
     const auto& om = S.cluster_out_mirror_ids[c];
     for (uint32_t m : om) {
-      uint32_t i = 0;
-      while (nodes[i] != m) ++i;
+      const uint32_t i = local_of[m];
+      if (i >= nodes.size() || nodes[i] != m) continue;
       const double v = val[o + i] + del[o + i];
       if (v != 0.0) sp.bound_delta.push_back({m, v});
     }
@@ -345,8 +373,9 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
   SG_TRY(upload(ctx, &D.sync_off, S.sync_off));
   SG_TRY(upload(ctx, &D.sync_nbr, S.sync_nbr));
   std::vector<uint32_t> odeg(all);
-  for (uint32_t v = 0; v < all; ++v)
-    odeg[v] = (uint32_t)D.out.deg(v < n ? v : S.mirror_master(v));
+#pragma omp parallel for schedule(static)
+  for (long long v = 0; v < (long long)all; ++v)
+    odeg[v] = (uint32_t)D.out.deg(v < n ? (uint32_t)v : S.mirror_master((uint32_t)v));
   SG_TRY(upload(ctx, &D.out_deg_all, odeg));
   std::vector<uint32_t> le, lx, ls;
   std::vector<uint8_t> nt(n);
@@ -374,25 +403,33 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
   D.n_omirror = (uint32_t)om.size();
   // correction tables
   std::vector<uint32_t> csp(all, 0xFFFFFFFFu), cc(all, 0);
-  std::vector<uint64_t> ido(1, 0), ivo(1, 0);
-  std::vector<uint32_t> idn, ivn;
-  std::vector<float> idw, ivw;
-  for (uint32_t sp = 0; sp < S.supernodes.size(); ++sp) {
-    const Supernode& s = S.supernodes[sp];
-    for (auto& e : s.inner_delta) {
-      idn.push_back(e.first);
-      idw.push_back((float)e.second);
-    }
-    for (auto& e : s.inner_value) {
-      ivn.push_back(e.first);
-      ivw.push_back((float)e.second);
-    }
-    ido.push_back(idn.size());
-    ivo.push_back(ivn.size());
+  const size_t nsp = S.supernodes.size();
+  std::vector<uint64_t> ido(nsp + 1, 0), ivo(nsp + 1, 0);
+  for (size_t sp = 0; sp < nsp; ++sp) {
+    ido[sp + 1] = ido[sp] + S.supernodes[sp].inner_delta.size();
+    ivo[sp + 1] = ivo[sp] + S.supernodes[sp].inner_value.size();
   }
-  for (uint32_t u = 0; u < all; ++u) {
+  std::vector<uint32_t> idn(ido[nsp]), ivn(ivo[nsp]);
+  std::vector<float> idw(ido[nsp]), ivw(ivo[nsp]);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (long long sp = 0; sp < (long long)nsp; ++sp) {
+    const Supernode& s = S.supernodes[sp];
+    uint64_t k = ido[sp];
+    for (auto& e : s.inner_delta) {
+      idn[k] = e.first;
+      idw[k++] = (float)e.second;
+    }
+    k = ivo[sp];
+    for (auto& e : s.inner_value) {
+      ivn[k] = e.first;
+      ivw[k++] = (float)e.second;
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (long long uu = 0; uu < (long long)all; ++uu) {
+    const uint32_t u = (uint32_t)uu;
     const uint32_t sp = S.Fc_map[u];
-    if (sp == Summary::kIdDefault || sp >= S.supernodes.size()) continue;
+    if (sp == Summary::kIdDefault || sp >= nsp) continue;
     if (S.supernodes[sp].id != u) continue;
     csp[u] = sp;
     cc[u] = (uint32_t)S.supernode_ids[S.id2spids[u]].size();
@@ -405,59 +442,94 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
   SG_TRY(upload(ctx, &D.iv_nbr, ivn));
   SG_TRY(upload(ctx, &D.id_w, idw));
   SG_TRY(upload(ctx, &D.iv_w, ivw));
-  // cluster members and subgraph CSR (over all rows)
-  std::vector<uint64_t> cmo(1, 0), subo(1, 0), blo(1, 0);
-  std::vector<uint32_t> cmv, subn, bl;
-  for (size_t c = 0; c < S.supernode_ids.size(); ++c) {
-    for (uint32_t v : S.supernode_ids[c]) {
-      cmv.push_back(v);
-      if (S.out_bound[v]) bl.push_back(v);
+  // Cluster members, exits and the precompute lists, all per member
+  // position of the cm layout, built in two parallel passes (counts, then
+  // fills at prefix offsets).  Clusters of at most kStageCap members get
+  // their local in-edges (tails as 8-bit local indices) and their edges to
+  // out-mirrors; clusters that are not staged (more members, or more local
+  // edges than kStageEdges) get their subgraph out-edges instead.
+  const size_t ncl = S.supernode_ids.size();
+  std::vector<uint64_t> cmo(ncl + 1, 0), blo(ncl + 1, 0), c_lin(ncl + 1, 0), c_lout(ncl + 1, 0),
+      c_sub(ncl + 1, 0);
+  std::vector<uint8_t> slot(n, 0);
+  // a head inside a small cluster c (members carry their local slot)
+  auto is_local = [&](uint32_t t, size_t c, const std::vector<uint32_t>& M) {
+    return t < n && S.id2spids[t] == (uint32_t)c && slot[t] < M.size() && M[slot[t]] == t;
+  };
+#pragma omp parallel for schedule(dynamic, 512)
+  for (long long c = 0; c < (long long)ncl; ++c) {
+    const auto& M = S.supernode_ids[c];
+    const size_t m = M.size();
+    uint64_t nb = 0, nin = 0, nout = 0, nall = 0;
+    for (size_t j = 0; j < m; ++j) {
+      if (m <= (size_t)kStageCap) slot[M[j]] = (uint8_t)j;
+      nb += S.out_bound[M[j]] != 0;
     }
-    cmo.push_back(cmv.size());
-    blo.push_back(bl.size());
-  }
-  for (uint32_t v = 0; v < all; ++v) {
-    for (uint32_t t : S.subgraph[v]) subn.push_back(t);
-    subo.push_back(subn.size());
-  }
-  // Per member position of cm_v, for clusters of at most kStageCap members:
-  // the local in-edges inside the cluster (tails as 8-bit local indices) and
-  // the out-edges to the cluster's out-mirrors (global ids).  Larger clusters
-  // keep empty lists and use the subgraph CSR.
-  std::vector<uint64_t> lino(1, 0), louto(1, 0);
-  std::vector<uint8_t> lins;
-  std::vector<uint32_t> loutd;
-  {
-    std::vector<uint32_t> slot(all, ~0u);
-    std::vector<std::vector<uint8_t>> inl;
-    for (size_t c = 0; c < S.supernode_ids.size(); ++c) {
-      const auto& M = S.supernode_ids[c];
-      const size_t m = M.size();
-      if (m > (size_t)kStageCap) {
-        for (size_t i = 0; i < m; ++i) {
-          lino.push_back(lins.size());
-          louto.push_back(loutd.size());
-        }
-        continue;
-      }
-      for (size_t j = 0; j < m; ++j) slot[M[j]] = (uint32_t)j;
-      inl.assign(m, {});
-      for (size_t i = 0; i < m; ++i) {
+    for (size_t i = 0; i < m; ++i) {
+      nall += S.subgraph[M[i]].size();
+      if (m <= (size_t)kStageCap)
         for (uint32_t t : S.subgraph[M[i]]) {
-          if (t < all && slot[t] != ~0u && M[slot[t]] == t)
-            inl[slot[t]].push_back((uint8_t)i);
-          else
-            loutd.push_back(t);
+          if (is_local(t, c, M)) ++nin; else ++nout;
         }
-        louto.push_back(loutd.size());
+    }
+    cmo[c + 1] = m;
+    blo[c + 1] = nb;
+    const bool staged = m <= (size_t)kStageCap && nin <= (uint64_t)kStageEdges;
+    c_lin[c + 1] = m <= (size_t)kStageCap ? nin : 0;
+    c_lout[c + 1] = m <= (size_t)kStageCap ? nout : 0;
+    c_sub[c + 1] = staged ? 0 : nall;
+  }
+  for (size_t c = 0; c < ncl; ++c) {
+    cmo[c + 1] += cmo[c];
+    blo[c + 1] += blo[c];
+    c_lin[c + 1] += c_lin[c];
+    c_lout[c + 1] += c_lout[c];
+    c_sub[c + 1] += c_sub[c];
+  }
+  const uint64_t npos = cmo[ncl];
+  std::vector<uint32_t> cmv(npos), bl(blo[ncl]), loutd(c_lout[ncl]), subn(c_sub[ncl]);
+  std::vector<uint8_t> lins(c_lin[ncl]);
+  std::vector<uint64_t> lino(npos + 1), louto(npos + 1), subo(npos + 1);
+#pragma omp parallel for schedule(dynamic, 512)
+  for (long long c = 0; c < (long long)ncl; ++c) {
+    const auto& M = S.supernode_ids[c];
+    const size_t m = M.size();
+    const uint64_t p0 = cmo[c];
+    uint64_t nb = blo[c];
+    for (size_t j = 0; j < m; ++j) {
+      cmv[p0 + j] = M[j];
+      if (S.out_bound[M[j]]) bl[nb++] = M[j];
+    }
+    const bool small = m <= (size_t)kStageCap;
+    const bool staged = small && c_lin[c + 1] - c_lin[c] <= (uint64_t)kStageEdges;
+    // local in-edges: counts per head, then tails in increasing local order
+    uint32_t cnt[kStageCap + 1];
+    if (small) {
+      for (size_t j = 0; j <= m; ++j) cnt[j] = 0;
+      for (size_t i = 0; i < m; ++i)
+        for (uint32_t t : S.subgraph[M[i]])
+          if (is_local(t, c, M)) ++cnt[slot[t] + 1];
+      for (size_t j = 0; j < m; ++j) cnt[j + 1] += cnt[j];
+      for (size_t j = 0; j < m; ++j) lino[p0 + j] = c_lin[c] + cnt[j];
+      for (size_t i = 0; i < m; ++i)
+        for (uint32_t t : S.subgraph[M[i]])
+          if (is_local(t, c, M)) lins[c_lin[c] + cnt[slot[t]]++] = (uint8_t)i;
+    } else {
+      for (size_t j = 0; j < m; ++j) lino[p0 + j] = c_lin[c];
+    }
+    uint64_t no = c_lout[c], ns = c_sub[c];
+    for (size_t i = 0; i < m; ++i) {
+      louto[p0 + i] = no;
+      subo[p0 + i] = ns;
+      for (uint32_t t : S.subgraph[M[i]]) {
+        if (small && !is_local(t, c, M)) loutd[no++] = t;
+        if (!staged) subn[ns++] = t;
       }
-      for (size_t j = 0; j < m; ++j) {
-        lins.insert(lins.end(), inl[j].begin(), inl[j].end());
-        lino.push_back(lins.size());
-      }
-      for (size_t j = 0; j < m; ++j) slot[M[j]] = ~0u;
     }
   }
+  lino[npos] = c_lin[ncl];
+  louto[npos] = c_lout[ncl];
+  subo[npos] = c_sub[ncl];
   SG_TRY(upload(ctx, &D.cm_off, cmo));
   SG_TRY(upload(ctx, &D.cm_v, cmv));
   SG_TRY(upload(ctx, &D.sub_off, subo));
@@ -806,7 +878,7 @@ __global__ void __launch_bounds__(256) k_sum_precompute(SumArgs A, const uint32_
         A.x[v] += ts;
         diff += fabs((double)ts);
         const float outv = ts * A.damping / (float)A.out_deg_all[v];
-        for (uint64_t f = sub_off[v]; f < sub_off[v + 1]; ++f) atomicAdd(&A.delta[sub_nbr[f]], outv);
+        for (uint64_t f = sub_off[i]; f < sub_off[i + 1]; ++f) atomicAdd(&A.delta[sub_nbr[f]], outv);
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) diff += __shfl_xor_sync(0xffffffffu, diff, o);
@@ -1005,25 +1077,48 @@ sg_status summary_after_apply(sg_ctx* ctx) {
   // deleted / added pairs of the batch (actions are small; copy to host)
   const uint64_t na = B.n_act;
   std::vector<uint32_t> as(na), ad(na), ak(na), af(na);
+  std::vector<float> aw(na);
   SG_CUDA(ctx, cudaMemcpyAsync(as.data(), B.a_src, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaMemcpyAsync(ad.data(), B.a_dst, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaMemcpyAsync(ak.data(), B.a_kind, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaMemcpyAsync(af.data(), B.a_found, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaMemcpyAsync(aw.data(), B.a_w, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   std::vector<std::pair<uint32_t, uint32_t>> deleted, added;
+  std::vector<AdjOp> ops_out, ops_in;
   for (uint64_t i = 0; i < na; ++i) {
-    if ((ak[i] & 1u) && af[i] != kInvalidVid) deleted.push_back({as[i], ad[i]});
+    const bool found = af[i] != kInvalidVid;
+    if ((ak[i] & 1u) && found) deleted.push_back({as[i], ad[i]});
     if (ak[i] & 2u) added.push_back({as[i], ad[i]});
+    // the applier's effect: a delete of a present edge removes it, an add
+    // sets the weight of a present edge or inserts an absent one
+    uint8_t kind = 255;
+    if (ak[i] == 1u && found) kind = AdjOp::kRemove;
+    else if ((ak[i] & 2u) && found) kind = AdjOp::kSetWeight;
+    else if (ak[i] & 2u) kind = AdjOp::kInsert;
+    if (kind == 255) continue;
+    ops_out.push_back({as[i], ad[i], aw[i], kind});
+    ops_in.push_back({ad[i], as[i], aw[i], kind});
   }
-  // new graph on the host
+  // the new graph on the host: the batch merged into the host copy (rows
+  // stay sorted), else a fresh download
   const uint32_t n = ctx->g.n;
-  const uint64_t m = ctx->g.m;
-  std::vector<uint64_t> rp(n + 1);
-  std::vector<uint32_t> col(m);
-  std::vector<float> w(ctx->g.weighted ? m : 0);
-  SG_TRY(download_csr(ctx, rp.data(), col.data(), ctx->g.weighted ? w.data() : nullptr));
-  host_adj_from_csr(n, rp.data(), col.data(), ctx->g.weighted ? w.data() : nullptr, D->out);
-  host_transpose(D->out, D->in);
+  auto by_row_col = [](const AdjOp& a, const AdjOp& b) {
+    return a.row != b.row ? a.row < b.row : a.col < b.col;
+  };
+  std::sort(ops_out.begin(), ops_out.end(), by_row_col);
+  std::sort(ops_in.begin(), ops_in.end(), by_row_col);
+  const bool patched = D->out.n == n && D->in.n == n && host_adj_patch(D->out, ops_out) &&
+                       host_adj_patch(D->in, ops_in);
+  if (!patched || D->out.rp[n] != ctx->g.m) {
+    const uint64_t m = ctx->g.m;
+    std::vector<uint64_t> rp(n + 1);
+    std::vector<uint32_t> col(m);
+    std::vector<float> w(ctx->g.weighted ? m : 0);
+    SG_TRY(download_csr(ctx, rp.data(), col.data(), ctx->g.weighted ? w.data() : nullptr));
+    host_adj_from_csr(n, rp.data(), col.data(), ctx->g.weighted ? w.data() : nullptr, D->out);
+    host_transpose(D->out, D->in);
+  }
   Summary& S = D->S;
   summary_inc_entries(S, D->out, D->in, deleted, added);
   {
@@ -1165,28 +1260,56 @@ static sg_status sssp_cluster_jobs(sg_ctx* ctx, SummaryDev& D,
   std::vector<uint32_t> cls;
   for (auto& jb : jobs)
     if (cl_index.emplace(jb.first, (uint32_t)cls.size()).second) cls.push_back(jb.first);
-  std::vector<uint64_t> cl_off(cls.size() + 1, 0), adj_off(1, 0);
-  std::vector<uint32_t> adj_nbr;
-  std::vector<float> adj_w;
+  // local problems per cluster (nodes, weighted subgraph edges as local
+  // indices; edges to nodes outside the cluster's list are dropped), built in
+  // two parallel passes; nodes of different clusters are distinct
+  const size_t ncl = cls.size();
+  std::vector<uint64_t> cl_off(ncl + 1, 0), cl_adj(ncl + 1, 0);
   std::vector<uint32_t> local_of(S.all_n, 0xFFFFFFFFu);
   size_t maxL = 1;
-  for (size_t k = 0; k < cls.size(); ++k) {
+  for (size_t k = 0; k < ncl; ++k) {
     const auto& nodes = S.cluster_ids[cls[k]];
-    for (uint32_t i = 0; i < nodes.size(); ++i) local_of[nodes[i]] = i;
-    for (uint32_t v : nodes) {
-      const auto& nb = S.subgraph[v];
-      const auto& wt = S.subgraph_w[v];
-      for (size_t e = 0; e < nb.size(); ++e) {
-        if (local_of[nb[e]] == 0xFFFFFFFFu) continue;
-        adj_nbr.push_back(local_of[nb[e]]);
-        adj_w.push_back(wt[e]);
-      }
-      adj_off.push_back(adj_nbr.size());
-    }
     cl_off[k + 1] = cl_off[k] + nodes.size();
     maxL = std::max(maxL, nodes.size());
-    for (uint32_t v : nodes) local_of[v] = 0xFFFFFFFFu;
   }
+  auto local = [&](const std::vector<uint32_t>& nodes, uint32_t t) {
+    const uint32_t l = local_of[t];
+    return (l < nodes.size() && nodes[l] == t) ? l : 0xFFFFFFFFu;
+  };
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long k = 0; k < (long long)ncl; ++k) {
+    const auto& nodes = S.cluster_ids[cls[k]];
+    for (uint32_t i = 0; i < nodes.size(); ++i) local_of[nodes[i]] = i;
+  }
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long k = 0; k < (long long)ncl; ++k) {
+    const auto& nodes = S.cluster_ids[cls[k]];
+    uint64_t ne = 0;
+    for (uint32_t v : nodes)
+      for (uint32_t t : S.subgraph[v]) ne += local(nodes, t) != 0xFFFFFFFFu;
+    cl_adj[k + 1] = ne;
+  }
+  for (size_t k = 0; k < ncl; ++k) cl_adj[k + 1] += cl_adj[k];
+  std::vector<uint64_t> adj_off(cl_off[ncl] + 1);
+  std::vector<uint32_t> adj_nbr(cl_adj[ncl]);
+  std::vector<float> adj_w(cl_adj[ncl]);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long k = 0; k < (long long)ncl; ++k) {
+    const auto& nodes = S.cluster_ids[cls[k]];
+    uint64_t o = cl_adj[k];
+    for (uint32_t i = 0; i < nodes.size(); ++i) {
+      adj_off[cl_off[k] + i] = o;
+      const auto& nb = S.subgraph[nodes[i]];
+      const auto& wt = S.subgraph_w[nodes[i]];
+      for (size_t e = 0; e < nb.size(); ++e) {
+        const uint32_t l = local(nodes, nb[e]);
+        if (l == 0xFFFFFFFFu) continue;
+        adj_nbr[o] = l;
+        adj_w[o++] = wt[e];
+      }
+    }
+  }
+  adj_off[cl_off[ncl]] = cl_adj[ncl];
   std::vector<uint32_t> job_cl(jobs.size()), job_src(jobs.size());
   std::vector<uint64_t> out_off(jobs.size() + 1, 0);
   for (size_t j = 0; j < jobs.size(); ++j) {
@@ -1222,7 +1345,8 @@ static sg_status sssp_cluster_jobs(sg_ctx* ctx, SummaryDev& D,
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   dfree(d_cl); dfree(d_src); dfree(d_nbr); dfree(d_w); dfree(d_cloff); dfree(d_adjoff);
   dfree(d_outoff); dfree(d_out);
-  for (size_t j = 0; j < jobs.size(); ++j)
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long j = 0; j < (long long)jobs.size(); ++j)
     (*dist)[j].assign(all.begin() + out_off[j], all.begin() + out_off[j + 1]);
   return SG_OK;
 }
@@ -1257,7 +1381,9 @@ static sg_status sssp_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector<ui
   std::vector<std::vector<double>> dist;
   SG_TRY(sssp_cluster_jobs(ctx, D, jobs, &dist));
   const double inf = std::numeric_limits<double>::infinity();
-  for (size_t j = 0; j < jobs.size(); ++j) {
+  // each job writes its own supernode's lists
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long j = 0; j < (long long)jobs.size(); ++j) {
     const uint32_t sp = jsp[j];
     const uint32_t c = S.supernodes[sp].ids;
     const auto& nodes = S.cluster_ids[c];

@@ -21,6 +21,22 @@ struct HostAdj {
   uint64_t deg(uint32_t v) const { return rp[v + 1] - rp[v]; }
 };
 
+// One change to a host adjacency (row, col), from the device applier's
+// normalized actions: remove an edge that exists, set the weight of one
+// that exists, or insert one that does not.
+struct AdjOp {
+  enum Kind : uint8_t { kRemove = 0, kSetWeight = 1, kInsert = 2 };
+  uint32_t row, col;
+  float w;
+  uint8_t kind;
+};
+
+// Patches `a` (rows sorted by column) with `ops` sorted by (row, col); rows
+// stay sorted.  Rows without changes are moved in bulk.  Returns false, with
+// `a` unchanged, when an op does not fit `a` (an insert of an edge that
+// exists, a removal of one that does not).
+bool host_adj_patch(HostAdj& a, const std::vector<AdjOp>& ops);
+
 // node types (grape/types.h:70-78)
 enum NodeTypeCode : char {
   kSingle = 0, kOnlyOut = 1, kOnlyIn = 2, kBothOutIn = 3, kInner = 4, kOutMaster = 5,

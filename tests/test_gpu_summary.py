@@ -142,3 +142,57 @@ def test_summary_save_and_load_reference_file(name, tmp_path):
         bad.write_bytes(fx["ref_serialized_summary"].tobytes()[:-4])
         with pytest.raises(sg.SgError):
             ctx.summary_load(str(bad))
+
+
+def _mixed_communities(seed=3):
+    """Planted communities of three kinds: 40 members with ~8 inner out-edges
+    each, 200 members (more than a warp-staged cluster holds), and 120
+    members with ~24 inner out-edges each (more local edges than staging
+    holds); three exits per community link to four other communities."""
+    rng = np.random.default_rng(seed)
+    spec = [(40, 8)] * 60 + [(200, 8)] * 6 + [(120, 24)] * 4
+    rng.shuffle(spec)
+    starts = np.cumsum([0] + [s for s, _ in spec])
+    n = int(starts[-1])
+    src, dst = [], []
+    for c, (size, deg) in enumerate(spec):
+        b = starts[c]
+        s = np.repeat(np.arange(b, b + size), deg)
+        src.append(s)
+        dst.append(b + rng.integers(0, size, size=s.size))
+        x = np.repeat(np.arange(b + size - 3, b + size), 4)
+        oc = rng.integers(0, len(spec), size=x.size)
+        src.append(x)
+        dst.append(starts[oc] + rng.integers(0, 3, size=x.size))
+    src, dst = np.concatenate(src), np.concatenate(dst)
+    keep = src != dst
+    key = np.unique(src[keep] * n + dst[keep])
+    src, dst = key // n, key % n
+    rp = np.concatenate([[0], np.cumsum(np.bincount(src, minlength=n))]).astype(np.uint64)
+    col = dst.astype(np.uint32)
+    comms = [np.arange(starts[c], starts[c + 1], dtype=np.uint32) for c in range(len(spec))]
+    return rp, col, comms
+
+
+def test_summarized_pagerank_staged_and_global_clusters():
+    """The cluster precompute stages small clusters in shared memory and
+    iterates the others (too many members or too many local edges) on global
+    memory: PEval and two IncEvals over a summary holding all three kinds
+    stay within the FP64 bound and agree with the plain path."""
+    rp, col, comms = _mixed_communities()
+    hg = sg.HostGraph(rp, col)
+    with sg.Context(0, compress=1) as ctx, sg.Context(0) as plain:
+        ctx.load_csr(rp, col)
+        ctx.summary_build(comms)
+        plain.load_csr(rp, col)
+        x = ctx.pr_peval()
+        assert np.abs(x - oracle.pr_fixed_point(rp, col)).sum() <= TOL_FIXED
+        assert np.abs(x - plain.pr_peval()).sum() <= TOL_REF
+        for seed in (11, 12):
+            batch = hg.gen_updates(150, 150, 0, seed=seed)
+            nrp, ncol, _ = hg.csr()
+            ctx.apply_updates(batch)
+            plain.apply_updates(batch)
+            x2 = ctx.pr_inceval()
+            assert np.abs(x2 - oracle.pr_fixed_point(nrp, ncol)).sum() <= TOL_FIXED
+            assert np.abs(x2 - plain.pr_inceval()).sum() <= TOL_REF
