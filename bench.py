@@ -59,6 +59,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-rounds", type=int, default=3)
     p.add_argument("--no-clocks", action="store_true")
+    p.add_argument("--pull-hubs", type=int, default=0,
+                   help="hub cache of the PageRank pull: 0 automatic, -1 none, k at most k")
     p.add_argument("--workload", default="inceval",
                    choices=["inceval", "batched", "adjoint", "sssp", "summarized"],
                    help="inceval: the headline IncEval line; batched: 256 PPR + 64 SSSP "
@@ -253,7 +255,7 @@ def run_ours(args, D: Dist):
     n = 1 << args.scale
     E = n * args.edge_factor
     bsz = int(round(E * args.batch_frac))
-    ctx = sg.Context(dev)
+    ctx = sg.Context(dev, pull_hubs=args.pull_hubs)
     ctx.generate_rmat(args.scale, E, seed=args.seed)
     ctx.pr_peval(out=False)
     peval_stats = ctx.stats()

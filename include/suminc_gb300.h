@@ -67,7 +67,11 @@ typedef struct sg_options {
   double sssp_delta;          /* delta-stepping bucket width, 0 = automatic  */
   double slack;               /* extra adjacency capacity per vertex (0.125) */
   double adjoint_rel_tol;     /* adjoint stop: residual < tol * sum|dL/dx|   */
-  int32_t reserved[8];
+  int32_t pull_hubs;          /* push values of the highest out-degree vertices
+                                 each pull CTA keeps in shared memory: 0 =
+                                 automatic (up to 26,624), -1 = none, k > 0 =
+                                 at most k                                  */
+  int32_t reserved[7];
 } sg_options;
 
 /* Counters of the last PEval / IncEval / batch call. */

@@ -64,7 +64,8 @@ class Options(C.Structure):
         ("sssp_delta", C.c_double),
         ("slack", C.c_double),
         ("adjoint_rel_tol", C.c_double),
-        ("reserved", C.c_int32 * 8),
+        ("pull_hubs", C.c_int32),
+        ("reserved", C.c_int32 * 7),
     ]
 
 

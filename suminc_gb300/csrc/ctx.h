@@ -47,6 +47,20 @@ struct PullLists {
   uint64_t gen = ~0ull;         // graph generation the lists describe
 };
 
+// Hub cache of the PageRank pull: the vertices with the highest out-degree
+// (their push values are gathered most often) and a copy of the in-CSR
+// column pool in which a hub's id is replaced by 0x80000000 | its slot.
+struct HubView {
+  uint32_t* ids = nullptr;   // [k] hub of each slot, ascending ids
+  uint32_t* slot = nullptr;  // [n] slot of each vertex, ~0u if none
+  uint32_t* col = nullptr;   // [cap] encoded copy of the in-CSR col pool
+  uint32_t k = 0;
+  uint32_t kmax = 0;         // the cap the set was chosen under
+  bool chosen = false;
+  uint64_t cap = 0;
+  uint64_t gen = ~0ull;      // graph generation the copy reflects
+};
+
 struct DevGraph {
   uint32_t n = 0;
   uint64_t m = 0;  // live edges (host mirror of the device count)
@@ -55,6 +69,7 @@ struct DevGraph {
   DevCSR out, in;
   PullLists in_wl;   // over the in-CSR (PageRank pulls); rebuilt after each update
   PullLists out_wl;  // over the out-CSR (adjoint pulls); built on demand
+  HubView hub;       // hub cache of the in-CSR pull; chosen on first use
   uint64_t gen = 0;  // bumped whenever the adjacency changes
 };
 

@@ -189,6 +189,9 @@ sg_status graph_free(sg_ctx* ctx) {
   csr_free(g.in);
   pull_lists_free(g.in_wl);
   pull_lists_free(g.out_wl);
+  dfree(g.hub.ids);
+  dfree(g.hub.slot);
+  dfree(g.hub.col);
   const uint64_t gen = g.gen;  // generations keep growing across graphs
   g = DevGraph();
   g.gen = gen + 1;

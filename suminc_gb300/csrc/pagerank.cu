@@ -133,23 +133,49 @@ struct WarpPullArgs {
   uint64_t ntiles;
   const uint32_t* col;
   const float* w;
+  const uint32_t* hub_ids;  // hub cache: vertex of each slot (HUB kernels)
+  uint32_t nhub;
 };
 
-// 8 CTAs of 256 threads per SM: 32 registers per thread, full occupancy
-// (measured faster than 6 CTAs without spills)
-template <bool W>
-__global__ void __launch_bounds__(PT_THREADS, 8) k_pr_pull_warp(PrArgs A, WarpPullArgs P, int p) {
+// Hub cache: the pull gathers the push value of every in-neighbour, and the
+// vertices with the highest out-degree take a large share of those gathers
+// (R-MAT scale 24: the top 26,624 of 16.8 M vertices take a third).  A CTA
+// copies their push values into shared memory once per launch and the pull
+// reads an encoded column copy in which a hub's id is 0x80000000 | slot.
+// 104 KB of floats per CTA, 1024 threads, two CTAs per SM.
+constexpr uint32_t kHubMax = 26624;
+constexpr uint32_t kHubMin = 1024;  // fewer hubs than this: no cache
+constexpr int kHubThreads = 1024;
+
+// Without the hub cache: 8 CTAs of 256 threads per SM, 32 registers per
+// thread, full occupancy (measured faster than 6 CTAs without spills).  With
+// it: 2 CTAs of 1024 threads per SM, the same 32 registers, and the hubs'
+// push values in dynamic shared memory.
+template <bool W, bool HUB>
+__global__ void __launch_bounds__(HUB ? kHubThreads : PT_THREADS, HUB ? 2 : 8)
+    k_pr_pull_warp(PrArgs A, WarpPullArgs P, int p) {
+  constexpr int NT = HUB ? kHubThreads : PT_THREADS;
   // neighbour ids and weights are streamed once per pull: evict-first in L2,
   // so the gathered push values stay resident (2.6 % faster at scale 24)
   const unsigned long long l2_stream = l2_evict_first_policy();
-  __shared__ double s_red[PT_THREADS / 32];
+  extern __shared__ float s_hub[];
+  __shared__ double s_red[NT / 32];
   if (A.misc[M_DONE]) return;
   const bool drain = A.misc[M_PENDING] != 0;
   const float* __restrict__ pv = p == 0 ? A.pv0 : ((p & 1) ? A.pvb[1] : A.pvb[0]);
   float* pv_next = (p & 1) ? A.pvb[0] : A.pvb[1];
+  if (HUB) {
+    for (uint32_t h = threadIdx.x; h < P.nhub; h += NT) s_hub[h] = pv[P.hub_ids[h]];
+    __syncthreads();
+  }
+  // a column is a vertex id, or with the hub cache 0x80000000 | slot
+  auto gather = [&](uint32_t c) -> float {
+    if (HUB && (c & 0x80000000u)) return s_hub[c & 0x7fffffffu];
+    return pv[c];
+  };
   const uint32_t lane = threadIdx.x & 31;
   // tiles are 32 quads, so tile indices fit 32 bits for any graph in HBM
-  const uint32_t nwarps = (gridDim.x * PT_THREADS) >> 5;
+  const uint32_t nwarps = (gridDim.x * NT) >> 5;
   const uint32_t ntiles = (uint32_t)P.ntiles;
   double res = 0.0;
   uint32_t visits = 0;
@@ -192,15 +218,15 @@ __global__ void __launch_bounds__(PT_THREADS, 8) k_pr_pull_warp(PrArgs A, WarpPu
       const uint4 c4 = ld_u4_hint(P.col + ebase + 4ull * q, l2_stream);
       if (W) {
         const float4 w4 = ld_f4_hint(P.w + ebase + 4ull * q, l2_stream);
-        sum = pv[c4.x] * w4.x;  // the last quad of a vertex may be partial
-        if (rem > 1) sum += pv[c4.y] * w4.y;
-        if (rem > 2) sum += pv[c4.z] * w4.z;
-        if (rem > 3) sum += pv[c4.w] * w4.w;
+        sum = gather(c4.x) * w4.x;  // the last quad of a vertex may be partial
+        if (rem > 1) sum += gather(c4.y) * w4.y;
+        if (rem > 2) sum += gather(c4.z) * w4.z;
+        if (rem > 3) sum += gather(c4.w) * w4.w;
       } else {
-        sum = pv[c4.x];
-        if (rem > 1) sum += pv[c4.y];
-        if (rem > 2) sum += pv[c4.z];
-        if (rem > 3) sum += pv[c4.w];
+        sum = gather(c4.x);
+        if (rem > 1) sum += gather(c4.y);
+        if (rem > 2) sum += gather(c4.z);
+        if (rem > 3) sum += gather(c4.w);
       }
     }
     // segmented suffix sums: the first lane of each owner's run gets its
@@ -230,11 +256,151 @@ __global__ void __launch_bounds__(PT_THREADS, 8) k_pr_pull_warp(PrArgs A, WarpPu
     }
     i0 = i0_next;
   }
-  const double b = block_sum<PT_THREADS>(res, s_red);
+  const double b = block_sum<NT>(res, s_red);
   if (threadIdx.x == 0 && b != 0.0) atomicAdd(&A.res[R_ACC], b);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) visits += __shfl_down_sync(0xffffffffu, visits, o);
   if ((threadIdx.x & 31) == 0 && visits) atomicAdd(&A.cnt[C_VISITS], (unsigned long long)visits);
+}
+
+// ---------------------------------------------------------- hub cache set-up
+
+__global__ void k_count_deg_ge(const uint32_t* __restrict__ deg, uint32_t n, uint32_t d,
+                               unsigned long long* cnt) {
+  uint32_t c = 0;
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    c += deg[v] >= d;
+  c = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(cnt, (unsigned long long)c);
+}
+
+__global__ void k_flag_deg_ge(const uint32_t* __restrict__ deg, uint32_t n, uint32_t d,
+                              uint8_t* __restrict__ f, uint32_t* __restrict__ iota) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    f[v] = deg[v] >= d;
+    iota[v] = v;
+  }
+}
+
+__global__ void k_hub_slots(const uint32_t* __restrict__ ids, uint32_t k, uint32_t* __restrict__ slot) {
+  for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < k; h += gridDim.x * blockDim.x)
+    slot[ids[h]] = h;
+}
+
+// encoded column copy: hubs as 0x80000000 | slot, other entries unchanged
+__global__ void k_hub_encode(const uint32_t* __restrict__ col, uint64_t cap,
+                             const uint32_t* __restrict__ slot, uint32_t n,
+                             uint32_t* __restrict__ out) {
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < cap;
+       e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = col[e];
+    const uint32_t h = c < n ? slot[c] : ~0u;
+    out[e] = h != ~0u ? (0x80000000u | h) : c;
+  }
+}
+
+sg_status cub_select_flagged_u32(sg_ctx* ctx, const uint32_t* in, const uint8_t* flags,
+                                 uint32_t* out, uint64_t* d_count, uint64_t n);
+
+// Chooses the hubs: every vertex whose out-degree reaches the smallest
+// threshold (at least 2) that leaves at most kmax of them.
+static sg_status hub_choose(sg_ctx* ctx, uint32_t kmax) {
+  DevGraph& g = ctx->g;
+  HubView& H = g.hub;
+  cudaStream_t st = ctx->stream;
+  dfree(H.ids);
+  dfree(H.slot);
+  dfree(H.col);
+  H = HubView();
+  H.chosen = true;
+  H.kmax = kmax;
+  if (kmax < kHubMin || g.n < 4 * kHubMin) return SG_OK;
+  unsigned long long* d_cnt = nullptr;
+  SG_TRY(dalloc(ctx, &d_cnt, 1));
+  auto count = [&](uint32_t d, unsigned long long* out) -> sg_status {
+    SG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, 8, st));
+    k_count_deg_ge<<<grid_for(g.n, 256), 256, 0, st>>>(g.out.deg, g.n, d, d_cnt);
+    SG_CUDA(ctx, cudaMemcpyAsync(out, d_cnt, 8, cudaMemcpyDeviceToHost, st));
+    SG_CUDA(ctx, cudaStreamSynchronize(st));
+    return SG_OK;
+  };
+  unsigned long long c = 0;
+  SG_TRY(count(2, &c));
+  uint32_t d = 2;
+  if (c > kmax) {
+    // count(lo) > kmax >= count(hi); degrees are below 2^32
+    uint64_t lo = 2, hi = 1ull << 32;
+    while (hi - lo > 1) {
+      const uint64_t mid = (lo + hi) / 2;
+      SG_TRY(count((uint32_t)std::min<uint64_t>(mid, 0xFFFFFFFFull), &c));
+      if (c <= kmax) hi = mid; else lo = mid;
+    }
+    d = (uint32_t)std::min<uint64_t>(hi, 0xFFFFFFFFull);
+    SG_TRY(count(d, &c));
+  }
+  if (c < kHubMin) {
+    dfree(d_cnt);
+    return SG_OK;
+  }
+  const uint32_t k = (uint32_t)c;
+  uint8_t* flags = nullptr;
+  uint32_t* iota = nullptr;
+  uint64_t* d_sel = nullptr;
+  SG_TRY(dalloc(ctx, &flags, g.n));
+  SG_TRY(dalloc(ctx, &iota, g.n));
+  SG_TRY(dalloc(ctx, &d_sel, 1));
+  SG_TRY(dalloc(ctx, &H.ids, k));
+  SG_TRY(dalloc(ctx, &H.slot, g.n));
+  k_flag_deg_ge<<<grid_for(g.n, 256), 256, 0, st>>>(g.out.deg, g.n, d, flags, iota);
+  SG_TRY(cub_select_flagged_u32(ctx, iota, flags, H.ids, d_sel, g.n));
+  SG_CUDA(ctx, cudaMemsetAsync(H.slot, 0xFF, 4ull * g.n, st));
+  k_hub_slots<<<grid_for(k, 256), 256, 0, st>>>(H.ids, k, H.slot);
+  SG_CUDA(ctx, cudaGetLastError());
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  dfree(flags);
+  dfree(iota);
+  dfree(d_sel);
+  dfree(d_cnt);
+  H.k = k;
+  return SG_OK;
+}
+
+// The hub view for the current in-CSR: hubs chosen once per graph (or when
+// the cap changes), the encoded column copy refreshed when the adjacency
+// has changed since.  Returns null when the cache is off or too small.
+static sg_status hub_view(sg_ctx* ctx, const HubView** out) {
+  DevGraph& g = ctx->g;
+  HubView& H = g.hub;
+  *out = nullptr;
+  const int opt = ctx->opt.pull_hubs;
+  const uint32_t kmax = opt < 0 ? 0u : (opt == 0 ? kHubMax : std::min<uint32_t>((uint32_t)opt, kHubMax));
+  if (!H.chosen || H.kmax != kmax) SG_TRY(hub_choose(ctx, kmax));
+  if (H.k == 0) return SG_OK;
+  if (H.gen != g.gen || H.cap != g.in.pool_cap || !H.col) {
+    if (H.cap != g.in.pool_cap || !H.col) {
+      dfree(H.col);
+      H.col = nullptr;
+      SG_TRY(dalloc(ctx, &H.col, std::max<uint64_t>(g.in.pool_cap, 1)));
+      H.cap = g.in.pool_cap;
+    }
+    k_hub_encode<<<grid_for(H.cap, 256), 256, 0, ctx->stream>>>(g.in.col, H.cap, H.slot, g.n,
+                                                                  H.col);
+    count_launch(ctx);
+    SG_CUDA(ctx, cudaGetLastError());
+    H.gen = g.gen;
+  }
+  static bool s_attr[64] = {};
+  if (ctx->device >= 0 && ctx->device < 64 && !s_attr[ctx->device]) {
+    SG_CUDA(ctx, cudaFuncSetAttribute(k_pr_pull_warp<false, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(kHubMax * sizeof(float))));
+    SG_CUDA(ctx, cudaFuncSetAttribute(k_pr_pull_warp<true, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(kHubMax * sizeof(float))));
+    s_attr[ctx->device] = true;
+  }
+  *out = &H;
+  return SG_OK;
 }
 
 // Tile-spanning vertices, then the round's termination decision.
@@ -416,17 +582,29 @@ sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R) {
   WP.ntiles = L.nwtiles;
   WP.col = R.csr->col;
   WP.w = R.weighted ? R.csr->w : nullptr;
+  WP.hub_ids = nullptr;
+  WP.nhub = 0;
   const uint32_t* bnd = L.wbnd;
   const uint32_t nbnd = L.wbnd_count;
 
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+  // the hub cache serves pulls over the in-CSR (its encoded column copy)
+  const HubView* hub = nullptr;
+  if (R.csr == &g.in && L.quads > 0) SG_TRY(hub_view(ctx, &hub));
+  if (hub) {
+    WP.col = hub->col;
+    WP.hub_ids = hub->ids;
+    WP.nhub = hub->k;
+  }
+  const int pt = hub ? kHubThreads : PT_THREADS;
+  const size_t hub_smem = hub ? (size_t)hub->k * sizeof(float) : 0;
   const unsigned vblocks = grid_for(g.n, VT, ctx->num_sms * 8);
   const unsigned wblocks = (unsigned)std::min<uint64_t>(
-      std::max<uint64_t>((L.nwtiles + PT_THREADS / 32 - 1) / (PT_THREADS / 32), 1),
-      (uint64_t)ctx->num_sms * 8);
+      std::max<uint64_t>((L.nwtiles + pt / 32 - 1) / (pt / 32), 1),
+      (uint64_t)ctx->num_sms * (hub ? 2 : 8));
   const unsigned fblocks = grid_for(std::max<uint32_t>(nbnd, 1), VT, ctx->num_sms * 2);
   const int kpull = R.kclass;
 
-  SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
   kprof_begin(ctx);
   k_pr_vertex<<<vblocks, VT, 0, st>>>(A);
   kprof_end(ctx, SG_K_PR_VERTEX);
@@ -438,8 +616,13 @@ sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R) {
     for (;;) {
       for (int r = 0; r < chunk; ++r, ++pull) {
         kprof_begin(ctx);
-        if (R.weighted) k_pr_pull_warp<true><<<wblocks, PT_THREADS, 0, st>>>(A, WP, pull);
-        else k_pr_pull_warp<false><<<wblocks, PT_THREADS, 0, st>>>(A, WP, pull);
+        if (hub) {
+          if (R.weighted) k_pr_pull_warp<true, true><<<wblocks, pt, hub_smem, st>>>(A, WP, pull);
+          else k_pr_pull_warp<false, true><<<wblocks, pt, hub_smem, st>>>(A, WP, pull);
+        } else {
+          if (R.weighted) k_pr_pull_warp<true, false><<<wblocks, pt, 0, st>>>(A, WP, pull);
+          else k_pr_pull_warp<false, false><<<wblocks, pt, 0, st>>>(A, WP, pull);
+        }
         kprof_end(ctx, kpull);
         kprof_begin(ctx);
         k_pr_fixup<<<fblocks, VT, 0, st>>>(A, bnd, nbnd, pull);

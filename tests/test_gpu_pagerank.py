@@ -82,3 +82,28 @@ def test_inceval_before_peval_is_a_state_error(ctx):
     with pytest.raises(sg.SgError) as e:
         ctx.pr_inceval()
     assert e.value.status == sg.SG_ERR_STATE
+
+
+def test_pull_hub_cache_matches_uncached_pull():
+    """The pull that keeps the push values of the highest out-degree
+    vertices in shared memory (reading an encoded copy of the in-CSR
+    columns) against the pull without that cache, over PEval and IncEvals
+    after batches (each batch makes the encoded copy stale)."""
+    scale = 16
+    n = 1 << scale
+    with sg.Context(0) as a, sg.Context(0, pull_hubs=-1) as b:
+        a.generate_rmat(scale, 16 * n, seed=7)
+        rp, col, _ = a.download_csr(weights=False)
+        b.load_csr(rp, col)
+        xa, xb = a.pr_peval(), b.pr_peval()
+        assert np.abs(xa - xb).sum() <= 5e-6
+        assert np.abs(xa - oracle.pr_fixed_point(rp, col)).sum() <= TOL_FIXED
+        hg = sg.HostGraph(rp, col)
+        for k in range(3):
+            upd = hg.gen_updates(2000, 2000, seed=90 + k)
+            a.apply_updates(upd)
+            b.apply_updates(upd)
+            xa, xb = a.pr_inceval(), b.pr_inceval()
+            assert np.abs(xa - xb).sum() <= 5e-6, k
+            nrp, ncol, _ = hg.csr()
+            assert np.abs(xa - oracle.pr_fixed_point(nrp, ncol)).sum() <= TOL_FIXED, k
