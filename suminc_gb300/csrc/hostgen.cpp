@@ -294,20 +294,16 @@ bool host_adj_patch(HostAdj& a, const std::vector<AdjOp>& ops) {
   }
   std::vector<uint32_t> col(rp[n]);
   std::vector<float> w(weighted ? rp[n] : 0);
-  uint32_t next = 0;  // first row not yet copied
-  size_t k = 0;
-  while (k < ops.size()) {
-    const uint32_t r = ops[k].row;
-    size_t ke = k;
-    while (ke < ops.size() && ops[ke].row == r) ++ke;
-    // rows next..r-1 are unchanged: one bulk move
-    if (r > next) {
-      const uint64_t b = a.rp[next], e = a.rp[r];
-      std::copy(a.col.begin() + b, a.col.begin() + e, col.begin() + rp[next]);
-      if (weighted) std::copy(a.w.begin() + b, a.w.begin() + e, w.begin() + rp[next]);
-    }
-    // merge row r with its changes (every write checked against the row's
-    // new extent, so an op that does not fit cannot write past it)
+  // rows r0..r1-1 unchanged: one bulk move
+  auto move_rows = [&](uint32_t r0, uint32_t r1) {
+    if (r1 <= r0) return;
+    const uint64_t b = a.rp[r0], e = a.rp[r1];
+    std::copy(a.col.begin() + b, a.col.begin() + e, col.begin() + rp[r0]);
+    if (weighted) std::copy(a.w.begin() + b, a.w.begin() + e, w.begin() + rp[r0]);
+  };
+  // row r merged with ops[k, ke) (every write checked against the row's new
+  // extent, so an op that does not fit cannot write past it)
+  auto merge_row = [&](uint32_t r, size_t k, size_t ke) {
     uint64_t i = a.rp[r], o = rp[r];
     const uint64_t ie = a.rp[r + 1], oe = rp[r + 1];
     auto emit = [&](uint32_t c, float wv) {
@@ -334,15 +330,31 @@ bool host_adj_patch(HostAdj& a, const std::vector<AdjOp>& ops) {
     }
     for (; i < ie; ++i)
       if (!emit(a.col[i], weighted ? a.w[i] : 0.f)) return false;
-    if (o != oe) return false;
-    next = r + 1;
-    k = ke;
+    return o == oe;
+  };
+  // row ranges in parallel, each with its slice of the ops
+  const int64_t chunks = std::max<int64_t>(1, std::min<int64_t>(256, n / 4096));
+  bool ok = true;
+#pragma omp parallel for schedule(dynamic, 1) reduction(&& : ok)
+  for (int64_t ch = 0; ch < chunks; ++ch) {
+    const uint32_t r0 = (uint32_t)((uint64_t)n * ch / chunks);
+    const uint32_t r1 = (uint32_t)((uint64_t)n * (ch + 1) / chunks);
+    auto row_lt = [](const AdjOp& op, uint32_t r) { return op.row < r; };
+    size_t k = std::lower_bound(ops.begin(), ops.end(), r0, row_lt) - ops.begin();
+    const size_t kend = std::lower_bound(ops.begin(), ops.end(), r1, row_lt) - ops.begin();
+    uint32_t next = r0;
+    while (k < kend && ok) {
+      const uint32_t r = ops[k].row;
+      size_t ke = k;
+      while (ke < kend && ops[ke].row == r) ++ke;
+      move_rows(next, r);
+      ok = merge_row(r, k, ke);
+      next = r + 1;
+      k = ke;
+    }
+    if (ok) move_rows(next, r1);
   }
-  if (next < n) {
-    const uint64_t b = a.rp[next], e = a.rp[n];
-    std::copy(a.col.begin() + b, a.col.begin() + e, col.begin() + rp[next]);
-    if (weighted) std::copy(a.w.begin() + b, a.w.begin() + e, w.begin() + rp[next]);
-  }
+  if (!ok) return false;
   a.rp.swap(rp);
   a.col.swap(col);
   a.w.swap(w);

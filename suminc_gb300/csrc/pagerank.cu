@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(HUB ? kHubThreads : PT_THREADS, HUB ? 2 : 8)
   const uint32_t ntiles = (uint32_t)P.ntiles;
   double res = 0.0;
   uint32_t visits = 0;
-  uint32_t t = (blockIdx.x * PT_THREADS + threadIdx.x) >> 5;
+  uint32_t t = (blockIdx.x * NT + threadIdx.x) >> 5;
   uint32_t i0 = t < ntiles ? P.wtile_v0[t] : 0u;
   for (; t < ntiles; t += nwarps) {
     const uint64_t base = (uint64_t)t * kWarpTileQuads;

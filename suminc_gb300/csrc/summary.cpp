@@ -718,7 +718,20 @@ void summary_inc_entries(Summary& S, const HostAdj& new_out, const HostAdj& new_
                          const std::vector<std::pair<uint32_t, uint32_t>>& deleted,
                          const std::vector<std::pair<uint32_t, uint32_t>>& added) {
   (void)new_out;
-  std::unordered_set<uint32_t> upd_c, upd_s;
+  // touched clusters and supernode sources: marks plus the list of marked
+  // ids (sorted at the end, so the order of marking does not matter)
+  std::vector<uint8_t> mark_c(S.supernode_ids.size(), 0), mark_s(S.all_n, 0);
+  std::vector<uint32_t> list_c, list_s;
+  struct {
+    std::vector<uint8_t>& mark;
+    std::vector<uint32_t>& list;
+    void insert(uint32_t x) {
+      if (x < mark.size() && !mark[x]) {
+        mark[x] = 1;
+        list.push_back(x);
+      }
+    }
+  } upd_c{mark_c, list_c}, upd_s{mark_s, list_s};
   std::vector<uint32_t> delete_spid;
   auto touch_source = [&](uint32_t u) {
     const uint32_t src_id = S.id2spids[u];
@@ -790,9 +803,9 @@ void summary_inc_entries(Summary& S, const HostAdj& new_out, const HostAdj& new_
     S.supernodes[delete_spid[i]].clear();
     S.supernodes[delete_spid[i]].id = Summary::kIdDefault;
   }
-  S.update_cluster_ids.assign(upd_c.begin(), upd_c.end());
+  S.update_cluster_ids = list_c;
   std::sort(S.update_cluster_ids.begin(), S.update_cluster_ids.end());
-  S.update_source_id.assign(upd_s.begin(), upd_s.end());
+  S.update_source_id = list_s;
   std::sort(S.update_source_id.begin(), S.update_source_id.end());
 }
 
