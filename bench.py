@@ -60,7 +60,7 @@ def parse():
     p.add_argument("--cpu-sample-rounds", type=int, default=3)
     p.add_argument("--no-clocks", action="store_true")
     p.add_argument("--pull-hubs", type=int, default=0,
-                   help="hub cache of the PageRank pull: 0 automatic, -1 none, k at most k")
+                   help="hub cache of the PageRank pull: 0 automatic, -1 none, k at most k (16384 cap)")
     p.add_argument("--workload", default="inceval",
                    choices=["inceval", "batched", "adjoint", "sssp", "summarized"],
                    help="inceval: the headline IncEval line; batched: 256 PPR + 64 SSSP "

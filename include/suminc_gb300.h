@@ -69,8 +69,8 @@ typedef struct sg_options {
   double adjoint_rel_tol;     /* adjoint stop: residual < tol * sum|dL/dx|   */
   int32_t pull_hubs;          /* push values of the highest out-degree vertices
                                  each pull CTA keeps in shared memory: 0 =
-                                 automatic (up to 26,624), -1 = none, k > 0 =
-                                 at most k                                  */
+                                 automatic (up to 12,288), -1 = none, k > 0 =
+                                 at most min(k, 16,384)                     */
   int32_t reserved[7];
 } sg_options;
 

@@ -139,11 +139,15 @@ struct WarpPullArgs {
 
 // Hub cache: the pull gathers the push value of every in-neighbour, and the
 // vertices with the highest out-degree take a large share of those gathers
-// (R-MAT scale 24: the top 26,624 of 16.8 M vertices take a third).  A CTA
+// (R-MAT scale 24: the top 13,312 of 16.8 M vertices take 27 %).  A CTA
 // copies their push values into shared memory once per launch and the pull
 // reads an encoded column copy in which a hub's id is 0x80000000 | slot.
-// 104 KB of floats per CTA, 1024 threads, two CTAs per SM.
-constexpr uint32_t kHubMax = 26624;
+// 1024 threads, two CTAs per SM.  Shared memory comes out of the same array
+// as L1, which the other gathers need: at scale 24 the pull takes 1.12 ms
+// without the cache, 1.05 ms with 2,048 hubs, 0.995 ms with 12,288 (48 KB per
+// CTA), 1.00 ms with 16,384 and 2.36 ms with 26,624 (104 KB per CTA).
+constexpr uint32_t kHubAuto = 12288;
+constexpr uint32_t kHubMax = 16384;
 constexpr uint32_t kHubMin = 1024;  // fewer hubs than this: no cache
 constexpr int kHubThreads = 1024;
 
@@ -373,7 +377,7 @@ static sg_status hub_view(sg_ctx* ctx, const HubView** out) {
   HubView& H = g.hub;
   *out = nullptr;
   const int opt = ctx->opt.pull_hubs;
-  const uint32_t kmax = opt < 0 ? 0u : (opt == 0 ? kHubMax : std::min<uint32_t>((uint32_t)opt, kHubMax));
+  const uint32_t kmax = opt < 0 ? 0u : (opt == 0 ? kHubAuto : std::min<uint32_t>((uint32_t)opt, kHubMax));
   if (!H.chosen || H.kmax != kmax) SG_TRY(hub_choose(ctx, kmax));
   if (H.k == 0) return SG_OK;
   if (H.gen != g.gen || H.cap != g.in.pool_cap || !H.col) {

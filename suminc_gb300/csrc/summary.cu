@@ -151,11 +151,16 @@ struct ShortcutArgs {
   double* out_delta;
   float damping;
   double thr_per_node;          // threshold / N
+  const uint32_t* jobs;         // the jobs this launch runs (null: all)
+  const uint64_t* lin_off;      // warp kernel: per local node, its in-edges
+  const uint8_t* lin_src;       // from members (local indices)
 };
 
-__global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A) {
+// One CTA per supernode job (clusters of any size).
+__global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njobs) {
   extern __shared__ double sm[];
-  const uint32_t s = blockIdx.x;
+  if (blockIdx.x >= njobs) return;
+  const uint32_t s = A.jobs ? A.jobs[blockIdx.x] : blockIdx.x;
   if (s >= A.n_sp) return;
   const uint32_t c = A.sp_cluster[s];
   const uint64_t l0 = A.cl_off[c];
@@ -210,6 +215,78 @@ __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A) {
   for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) {
     A.out_value[o + i] = value[i];
     A.out_delta[o + i] = delta[i];
+  }
+}
+
+// One warp per supernode job for clusters of at most kStageCap local nodes:
+// the same iteration as k_shortcuts (a unit of delta at the entry, Jacobi
+// steps in FP64 until the members' delta mass is at most thr x members or
+// 101 steps) in two phases per step without atomics: members take their
+// delta and publish d * delta / div, then every node sums the published
+// values of its in-edges from members (mirrors keep what they hold).
+__global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t njobs) {
+  __shared__ double s_val[kStageWarps][kStageCap];
+  __shared__ double s_del[kStageWarps][kStageCap];
+  __shared__ double s_pv[kStageWarps][kStageCap];
+  const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const double d = (double)A.damping;
+  for (uint32_t jj = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; jj < njobs; jj += nwarps) {
+    const uint32_t s = A.jobs[jj];
+    const uint32_t c = A.sp_cluster[s];
+    const uint64_t l0 = A.cl_off[c];
+    const uint32_t L = (uint32_t)(A.cl_off[c + 1] - l0);
+    const uint32_t inner = A.cl_inner[c];
+    const uint32_t src = A.sp_src[s];
+    double* val = s_val[w];
+    double* del = s_del[w];
+    double* pv = s_pv[w];
+    for (uint32_t i = lane; i < L; i += 32) {
+      val[i] = 0.0;
+      del[i] = (i == src) ? 1.0 : 0.0;
+    }
+    __syncwarp();
+    // an in-mirror entry first sends its unit along its edges into the cluster
+    if (src >= inner) {
+      if (lane == 0) {
+        const double outv = d / (double)A.div[l0 + src];
+        for (uint64_t e = A.adj_off[l0 + src]; e < A.adj_off[l0 + src + 1]; ++e)
+          del[A.adj_nbr[e]] += outv;
+        val[src] += 1.0;
+        del[src] = 0.0;
+      }
+      __syncwarp();
+    }
+    const double thr = A.thr_per_node * (double)inner;
+    for (int step = 1;; ++step) {
+      double diff = 0.0;
+      for (uint32_t i = lane; i < inner; i += 32) {
+        const double ts = del[i];
+        double out = 0.0;
+        if (ts != 0.0) {
+          val[i] += ts;
+          diff += fabs(ts);
+          out = ts * d / (double)A.div[l0 + i];
+        }
+        pv[i] = out;
+      }
+      __syncwarp();
+      for (uint32_t j = lane; j < L; j += 32) {
+        double acc = 0.0;
+        for (uint64_t f = A.lin_off[l0 + j]; f < A.lin_off[l0 + j + 1]; ++f) acc += pv[A.lin_src[f]];
+        del[j] = (j < inner ? 0.0 : del[j]) + acc;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) diff += __shfl_xor_sync(0xffffffffu, diff, o);
+      __syncwarp();
+      if (diff <= thr || step > 100) break;
+    }
+    const uint64_t o = A.out_off[s];
+    for (uint32_t i = lane; i < L; i += 32) {
+      A.out_value[o + i] = val[i];
+      A.out_delta[o + i] = del[i];
+    }
+    __syncwarp();
   }
 }
 
@@ -285,12 +362,66 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
     sp_src[j] = (l < nodes.size() && nodes[l] == sp.id) ? l : 0u;
     out_off[j + 1] = out_off[j] + (cl_off[k + 1] - cl_off[k]);
   }
-  const size_t smem = 3 * maxL * sizeof(double);
+  // in-edges from members per local node of clusters with at most
+  // kStageCap nodes (warp kernel), in two parallel passes
+  std::vector<uint64_t> cl_lin(ncl + 1, 0);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long k = 0; k < (long long)ncl; ++k) {
+    const uint64_t L = cl_off[k + 1] - cl_off[k];
+    if (L > (uint64_t)kStageCap) continue;
+    uint64_t c = 0;
+    for (uint32_t i = 0; i < cl_inner[k]; ++i)
+      c += adj_off[cl_off[k] + i + 1] - adj_off[cl_off[k] + i];
+    cl_lin[k + 1] = c;
+  }
+  for (size_t k = 0; k < ncl; ++k) cl_lin[k + 1] += cl_lin[k];
+  std::vector<uint64_t> lin_off(cl_off[ncl] + 1);
+  std::vector<uint8_t> lin_src(cl_lin[ncl]);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long k = 0; k < (long long)ncl; ++k) {
+    const uint64_t b = cl_off[k];
+    const uint32_t L = (uint32_t)(cl_off[k + 1] - b);
+    if (L > (uint32_t)kStageCap) {
+      for (uint32_t j = 0; j < L; ++j) lin_off[b + j] = cl_lin[k];
+      continue;
+    }
+    uint32_t cnt[kStageCap + 1];
+    for (uint32_t j = 0; j <= L; ++j) cnt[j] = 0;
+    for (uint32_t i = 0; i < cl_inner[k]; ++i)
+      for (uint64_t e = adj_off[b + i]; e < adj_off[b + i + 1]; ++e) ++cnt[adj_nbr[e] + 1];
+    for (uint32_t j = 0; j < L; ++j) cnt[j + 1] += cnt[j];
+    for (uint32_t j = 0; j < L; ++j) lin_off[b + j] = cl_lin[k] + cnt[j];
+    for (uint32_t i = 0; i < cl_inner[k]; ++i)
+      for (uint64_t e = adj_off[b + i]; e < adj_off[b + i + 1]; ++e)
+        lin_src[cl_lin[k] + cnt[adj_nbr[e]]++] = (uint8_t)i;
+  }
+  lin_off[cl_off[ncl]] = cl_lin[ncl];
+  std::vector<uint32_t> warp_jobs, block_jobs;
+  size_t maxL_block = 1;
+  for (size_t j = 0; j < spids.size(); ++j) {
+    const uint32_t k = sp_cluster[j];
+    const uint64_t L = cl_off[k + 1] - cl_off[k];
+    if (L <= (uint64_t)kStageCap) {
+      warp_jobs.push_back((uint32_t)j);
+    } else {
+      block_jobs.push_back((uint32_t)j);
+      maxL_block = std::max<size_t>(maxL_block, L);
+    }
+  }
+  (void)maxL;
+  const size_t smem = 3 * maxL_block * sizeof(double);
   if (smem > 200 * 1024) return fail(ctx, SG_ERR_UNSUPPORTED, "cluster too large for the shortcut kernel");
   uint32_t *d_spc = nullptr, *d_src = nullptr, *d_inner = nullptr, *d_adj = nullptr;
   uint64_t *d_cloff = nullptr, *d_adjoff = nullptr, *d_outoff = nullptr;
   float* d_div = nullptr;
   double *d_val = nullptr, *d_del = nullptr;
+  uint32_t *d_wjobs = nullptr, *d_bjobs = nullptr;
+  uint64_t* d_linoff = nullptr;
+  uint8_t* d_linsrc = nullptr;
+  SG_TRY(upload(ctx, &d_wjobs, warp_jobs));
+  SG_TRY(upload(ctx, &d_bjobs, block_jobs));
+  SG_TRY(upload(ctx, &d_linoff, lin_off));
+  SG_TRY(upload(ctx, &d_linsrc, lin_src));
   SG_TRY(upload(ctx, &d_spc, sp_cluster));
   SG_TRY(upload(ctx, &d_src, sp_src));
   SG_TRY(upload(ctx, &d_inner, cl_inner));
@@ -315,11 +446,21 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
   A.out_delta = d_del;
   A.damping = (float)ctx->opt.damping;
   A.thr_per_node = ctx->opt.termcheck_threshold / (double)S.old_n;
+  A.lin_off = d_linoff;
+  A.lin_src = d_linsrc;
   if (smem > 48 * 1024)
     SG_CUDA(ctx, cudaFuncSetAttribute(k_shortcuts, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   kprof_begin(ctx);
-  k_shortcuts<<<A.n_sp, 128, smem, ctx->stream>>>(A);
+  if (!warp_jobs.empty()) {
+    A.jobs = d_wjobs;
+    k_shortcuts_warp<<<grid_for((uint64_t)warp_jobs.size() * 32, 32 * kStageWarps), 32 * kStageWarps,
+                       0, ctx->stream>>>(A, (uint32_t)warp_jobs.size());
+  }
+  if (!block_jobs.empty()) {
+    A.jobs = d_bjobs;
+    k_shortcuts<<<(unsigned)block_jobs.size(), 128, smem, ctx->stream>>>(A, (uint32_t)block_jobs.size());
+  }
   kprof_end(ctx, SG_K_SUMMARY);
   SG_CUDA(ctx, cudaGetLastError());
   std::vector<double> val(out_off.back()), del(out_off.back());
@@ -328,6 +469,7 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   dfree(d_spc); dfree(d_src); dfree(d_inner); dfree(d_adj); dfree(d_cloff); dfree(d_adjoff);
   dfree(d_outoff); dfree(d_div); dfree(d_val); dfree(d_del);
+  dfree(d_wjobs); dfree(d_bjobs); dfree(d_linoff); dfree(d_linsrc);
   // fianl_build_iter_index_for_mirror (iter_compressor.h:433-491); each
   // supernode writes only its own lists
 #pragma omp parallel for schedule(dynamic, 256)
