@@ -228,6 +228,7 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
   __shared__ double s_val[kStageWarps][kStageCap];
   __shared__ double s_del[kStageWarps][kStageCap];
   __shared__ double s_pv[kStageWarps][kStageCap];
+  __shared__ double s_f[kStageWarps][kStageCap];
   const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   const double d = (double)A.damping;
@@ -241,9 +242,11 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
     double* val = s_val[w];
     double* del = s_del[w];
     double* pv = s_pv[w];
+    double* f = s_f[w];  // d / div per node: one FP64 division per node and job
     for (uint32_t i = lane; i < L; i += 32) {
       val[i] = 0.0;
       del[i] = (i == src) ? 1.0 : 0.0;
+      f[i] = d / (double)A.div[l0 + i];
     }
     __syncwarp();
     // an in-mirror entry first sends its unit along its edges into the cluster
@@ -266,7 +269,7 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
         if (ts != 0.0) {
           val[i] += ts;
           diff += fabs(ts);
-          out = ts * d / (double)A.div[l0 + i];
+          out = ts * f[i];
         }
         pv[i] = out;
       }
