@@ -24,6 +24,7 @@ struct DevCSR {
   float* w = nullptr;           // null for unweighted graphs
   uint64_t pool_cap = 0;        // total slots allocated
   uint64_t* pool_tail = nullptr;  // device counter: first free slot
+  uint64_t layout = 0;          // bumped when a repack moves every segment
 };
 
 // Edge-balanced work lists over one direction of adjacency: vertices with
@@ -59,6 +60,7 @@ struct HubView {
   bool chosen = false;
   uint64_t cap = 0;
   uint64_t gen = ~0ull;      // graph generation the copy reflects
+  uint64_t layout = 0;       // in-CSR layout the copy reflects
 };
 
 struct DevGraph {
@@ -253,6 +255,9 @@ sg_status apply_updates_device(sg_ctx* ctx, uint64_t count,
 sg_status pr_free(sg_ctx* ctx);
 sg_status pr_alloc(sg_ctx* ctx);
 sg_status pr_run(sg_ctx* ctx, bool inc);
+// after an apply (the generation already bumped): re-encodes the hub view's
+// copy of the given in-rows when it was current before the batch
+sg_status pr_hub_after_apply(sg_ctx* ctx, const uint32_t* rows, uint64_t nrows);
 // buffers and direction of one delta-PageRank run (pagerank.cu)
 struct PrBufs {
   float* x;

@@ -898,6 +898,7 @@ static sg_status repack_direction(sg_ctx* ctx, DevCSR& c, uint64_t batch_need) {
   dfree(cap64);
   c.off = off_new;
   c.col = col_new;
+  c.layout++;
   c.w = w_new;
   c.pool_cap = pool;
   count_launch(ctx, 4);
@@ -1374,6 +1375,7 @@ sg_status apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* upd
   }
   g.m = (uint64_t)((long long)g.m + dm);
   SG_TRY(graph_rebuild_worklists(ctx));
+  SG_TRY(pr_hub_after_apply(ctx, B.igrp_vertex, B.n_igrp));
   return SG_OK;
 }
 

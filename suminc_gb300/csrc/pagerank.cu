@@ -303,8 +303,46 @@ __global__ void k_hub_encode(const uint32_t* __restrict__ col, uint64_t cap,
   }
 }
 
+// the live entries of the given rows only (block per row: in-rows of hubs
+// hold up to millions of entries)
+__global__ void __launch_bounds__(256) k_hub_encode_rows(const uint64_t* __restrict__ off,
+                                                         const uint32_t* __restrict__ deg,
+                                                         const uint32_t* __restrict__ col,
+                                                         const uint32_t* __restrict__ slot, uint32_t n,
+                                                         const uint32_t* __restrict__ rows,
+                                                         uint64_t nrows, uint32_t* __restrict__ out) {
+  for (uint64_t r = blockIdx.x; r < nrows; r += gridDim.x) {
+    const uint32_t v = rows[r];
+    const uint64_t b = off[v], e = b + deg[v];
+    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+      const uint32_t c = col[i];
+      const uint32_t h = c < n ? slot[c] : ~0u;
+      out[i] = h != ~0u ? (0x80000000u | h) : c;
+    }
+  }
+}
+
 sg_status cub_select_flagged_u32(sg_ctx* ctx, const uint32_t* in, const uint8_t* flags,
                                  uint32_t* out, uint64_t* d_count, uint64_t n);
+
+sg_status pr_hub_after_apply(sg_ctx* ctx, const uint32_t* rows, uint64_t nrows) {
+  DevGraph& g = ctx->g;
+  HubView& H = g.hub;
+  // only a copy that reflected the adjacency right before this batch (one
+  // generation back) in the same layout can be patched; others stay stale
+  // and are re-encoded in full by the next pull
+  if (!H.col || H.k == 0 || H.gen + 1 != g.gen || H.layout != g.in.layout ||
+      H.cap != g.in.pool_cap)
+    return SG_OK;
+  if (nrows)
+    k_hub_encode_rows<<<(unsigned)std::min<uint64_t>(nrows, (uint64_t)ctx->num_sms * 16), 256, 0,
+                        ctx->stream>>>(g.in.off, g.in.deg, g.in.col, H.slot, g.n, rows, nrows,
+                                       H.col);
+  count_launch(ctx);
+  SG_CUDA(ctx, cudaGetLastError());
+  H.gen = g.gen;
+  return SG_OK;
+}
 
 // Chooses the hubs: every vertex whose out-degree reaches the smallest
 // threshold (at least 2) that leaves at most kmax of them.
@@ -392,6 +430,7 @@ static sg_status hub_view(sg_ctx* ctx, const HubView** out) {
     count_launch(ctx);
     SG_CUDA(ctx, cudaGetLastError());
     H.gen = g.gen;
+    H.layout = g.in.layout;
   }
   static bool s_attr[64] = {};
   if (ctx->device >= 0 && ctx->device < 64 && !s_attr[ctx->device]) {
