@@ -43,7 +43,7 @@ BYTES_PER_RELAXED_EDGE = 12   # 4 B neighbour + 4 B delta read + 4 B delta write
 BYTES_PER_VERTEX_VISIT = 24   # 8 B row offset + 4 B delta read/reset + 8 B value RMW
 # DRAM bytes (read + write) per k_pr_pull_warp launch on the default
 # workload, from one ncu capture (profiles/pr_pull_warp_rmat24_dram.md)
-PULL_DRAM_BYTES_RMAT24 = 2.07e9
+PULL_DRAM_BYTES_RMAT24 = 2.06e9
 
 
 def parse():
