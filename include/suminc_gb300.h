@@ -262,6 +262,16 @@ sg_status sg_sssp_distances(sg_ctx* ctx, double* out);
  * keeps (grape/utils/dependency_data.h:12-33). */
 sg_status sg_sssp_parents(sg_ctx* ctx, uint32_t* out);
 
+/* Failure detection of the device-side waits (no counterpart in the
+ * reference, which has none).  Every wait in the persistent kernels (the
+ * grid barrier of SSSP, its reset BFS and the batched kernel) spins a
+ * bounded number of times, then records an error word and returns, and the
+ * host call reports SG_ERR_TIMEOUT with the context still usable.  This
+ * entry point runs that barrier with four CTAs: skip_one_block = 0 lets all
+ * arrive (SG_OK); 1 keeps one away, so the wait runs out after about 10 ms
+ * (SG_ERR_TIMEOUT). */
+sg_status sg_debug_barrier_probe(sg_ctx* ctx, int32_t skip_one_block);
+
 /* ------------------------------------------- personalized PageRank, batches */
 
 /* Personalized PageRank of one query on the plain graph: teleport mass

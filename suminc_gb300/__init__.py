@@ -193,6 +193,7 @@ _SIGS = {
     "sg_sssp_inceval": ([_P, _P], C.c_int),
     "sg_sssp_distances": ([_P, _P], C.c_int),
     "sg_sssp_parents": ([_P, _P], C.c_int),
+    "sg_debug_barrier_probe": ([_P, C.c_int32], C.c_int),
     "sg_util_rmat_host": ([C.c_int, C.c_uint64, C.c_double, C.c_double, C.c_double, C.c_uint64,
                            C.c_int, C.c_double, C.c_double, _P, _P, _P], C.c_int),
     "sg_hostgraph_create": ([C.c_uint32, _P, _P, _P, C.POINTER(_P)], C.c_int),
@@ -516,6 +517,12 @@ class Context:
         d = np.empty(self.n, np.float64)
         _check(self._lib.sg_sssp_distances(self._h, _ptr(d)), self, "sg_sssp_distances")
         return d
+
+    def barrier_probe(self, skip_one_block: bool) -> int:
+        """Runs the persistent kernels' bounded grid barrier with one CTA kept
+        away (or none); returns the status code, SG_ERR_TIMEOUT when the wait
+        ran out."""
+        return int(self._lib.sg_debug_barrier_probe(self._h, 1 if skip_one_block else 0))
 
     def sssp_parents(self):
         p = np.empty(self.n, np.uint32)

@@ -431,6 +431,11 @@ sg_status sg_sssp_distances(sg_ctx* ctx, double* out) {
   SG_CATCH(ctx)
 }
 
+sg_status sg_debug_barrier_probe(sg_ctx* ctx, int32_t skip_one_block) {
+  SG_GUARD(ctx);
+  return sssp_barrier_probe(ctx, skip_one_block);
+}
+
 sg_status sg_sssp_parents(sg_ctx* ctx, uint32_t* out) {
   SG_GUARD(ctx);
   if (!out) return fail(ctx, SG_ERR_INVALID, "null output");

@@ -255,6 +255,9 @@ sg_status apply_updates_device(sg_ctx* ctx, uint64_t count,
 sg_status pr_free(sg_ctx* ctx);
 sg_status pr_alloc(sg_ctx* ctx);
 sg_status pr_run(sg_ctx* ctx, bool inc);
+// failure detection: the persistent kernels' grid barrier, met by a few CTAs
+// (skip: one CTA never arrives, the bounded waits run out)
+sg_status sssp_barrier_probe(sg_ctx* ctx, int skip);
 // after an apply (the generation already bumped): re-encodes the hub view's
 // copy of the given in-rows when it was current before the batch
 sg_status pr_hub_after_apply(sg_ctx* ctx, const uint32_t* rows, uint64_t nrows);

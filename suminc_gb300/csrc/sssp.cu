@@ -85,6 +85,14 @@ __device__ __forceinline__ bool grid_sync(const SsspArgs& A) {
   return *(volatile uint32_t*)(A.ctl + S_ERR) == 0;
 }
 
+// Failure detection of the grid barrier above: a few CTAs meet at it; with
+// `skip` the last CTA leaves without arriving, so the others' bounded waits
+// run out and set the error word instead of hanging the GPU.
+__global__ void k_barrier_probe(SsspArgs A, int skip) {
+  if (skip && blockIdx.x == gridDim.x - 1) return;
+  grid_sync(A);
+}
+
 // Relaxes the out-edges of every vertex in `q` (warp per vertex, 4-edge
 // quads, 128-bit loads of neighbour and weight arrays).
 __device__ __forceinline__ void relax_queue(const SsspArgs& A, const uint32_t* q, uint32_t qn,
@@ -920,6 +928,24 @@ sg_status sssp_download(sg_ctx* ctx, double* out) {
   k_dist_to_double<<<grid_for(n, 256), 256, 0, ctx->stream>>>(n, s.dist, s.out);
   SG_CUDA(ctx, cudaMemcpyAsync(out, s.out, 8ull * n, cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return SG_OK;
+}
+
+sg_status sssp_barrier_probe(sg_ctx* ctx, int skip) {
+  uint32_t* ctl = nullptr;
+  SG_TRY(dalloc(ctx, &ctl, S_WORDS));
+  SG_CUDA(ctx, cudaMemsetAsync(ctl, 0, 4 * S_WORDS, ctx->stream));
+  SsspArgs A{};
+  A.ctl = ctl;
+  A.spin_limit = 100000;  // about 10 ms of polling
+  k_barrier_probe<<<4, 128, 0, ctx->stream>>>(A, skip ? 1 : 0);
+  count_launch(ctx);
+  SG_CUDA(ctx, cudaGetLastError());
+  uint32_t err = 0;
+  SG_CUDA(ctx, cudaMemcpyAsync(&err, ctl + S_ERR, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  dfree(ctl);
+  if (err) return fail(ctx, SG_ERR_TIMEOUT, "grid barrier wait expired (probe)");
   return SG_OK;
 }
 

@@ -112,3 +112,19 @@ def test_parents_stay_min_tight_across_inceval(ctx):
         nrp, ncol, nw = hg.csr()
         assert np.array_equal(d, oracle.dijkstra(nrp, ncol, nw, 0))
         assert np.array_equal(ctx.sssp_parents(), _min_tight_parents(nrp, ncol, nw, d, 0))
+
+
+def test_grid_barrier_wait_runs_out_and_context_survives(ctx):
+    """Failure detection without a GPU fault: the persistent kernels' grid
+    barrier with one CTA kept away gives up after its bounded spin and the
+    call reports SG_ERR_TIMEOUT; with every CTA present it passes; the
+    context keeps working afterwards (SSSP and PageRank on a small graph)."""
+    assert ctx.barrier_probe(False) == sg.SG_OK
+    assert ctx.barrier_probe(True) == sg.SG_ERR_TIMEOUT
+    assert ctx.barrier_probe(False) == sg.SG_OK
+    scale = 10
+    ctx.generate_rmat(scale, 8 << scale, seed=3, weight_kind=1)
+    rp, col, w = ctx.download_csr(weights=True)
+    assert np.array_equal(ctx.sssp_peval(0), oracle.dijkstra(rp, col, w, 0))
+    x = ctx.pr_peval()
+    assert np.abs(x - oracle.pr_fixed_point(rp, col)).sum() <= 1e-5
