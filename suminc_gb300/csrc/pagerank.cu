@@ -422,7 +422,13 @@ static sg_status hub_view(sg_ctx* ctx, const HubView** out) {
     if (H.cap != g.in.pool_cap || !H.col) {
       dfree(H.col);
       H.col = nullptr;
-      SG_TRY(dalloc(ctx, &H.col, std::max<uint64_t>(g.in.pool_cap, 1)));
+      H.cap = 0;
+      // the copy is an optimisation: without room for it the pull runs
+      // uncached (the cudaMalloc error is cleared by dalloc)
+      if (dalloc(ctx, &H.col, std::max<uint64_t>(g.in.pool_cap, 1)) != SG_OK) {
+        H.col = nullptr;
+        return SG_OK;
+      }
       H.cap = g.in.pool_cap;
     }
     k_hub_encode<<<grid_for(H.cap, 256), 256, 0, ctx->stream>>>(g.in.col, H.cap, H.slot, g.n,
