@@ -798,12 +798,30 @@ def run_sssp(args, D: Dist):
     st = ctx.stats()
     prof["sssp_kernel_ms"] = st["kernel_ms"]["sssp"] / len(extra)
     ctx.set_profile(0)
+    # CPU baseline: the reference's incremental stage restated in the oracle
+    # (deltaCompute over the deleted and re-weighted edges, a round from every
+    # finite vertex, the traversal) on all host threads, for one more batch,
+    # from the GPU's converged distances and parents
+    d_prev, p_prev = ctx.sssp_distances(), ctx.sssp_parents()
+    orp, ocol, _ = hg.csr()
+    cb = hg.gen_updates(40000, 40000, 10000, seed=950)
     nrp, ncol, nw = hg.csr()
+    old_keys = np.repeat(np.arange(n, dtype=np.int64), np.diff(orp).astype(np.int64)) * n + ocol
+    ckeys = cb["src"].astype(np.int64) * n + cb["dst"].astype(np.int64)
+    if not np.all(old_keys[1:] > old_keys[:-1]):
+        old_keys = np.sort(old_keys)
+    pos = np.minimum(np.searchsorted(old_keys, ckeys), len(old_keys) - 1)
+    gone = (cb["op"] == 1) | ((cb["op"] == 0) & (old_keys[pos] == ckeys))
     t1 = time.perf_counter()
-    ref = oracle.dijkstra(nrp, ncol, nw, 0)
-    dij_s = time.perf_counter() - t1
+    d_cpu, _, cst = oracle.sssp_inceval((orp, ocol), (nrp, ncol, nw),
+                                        (cb["src"][gone], cb["dst"][gone]), d_prev, p_prev)
+    cpu_s = time.perf_counter() - t1
+    ctx.apply_updates(cb)
+    sg._check(ctx._lib.sg_sssp_inceval(ctx._h, None), ctx, "sg_sssp_inceval")
     d_last = ctx.sssp_distances()
+    ref = oracle.dijkstra(nrp, ncol, nw, 0)
     exact = bool(np.array_equal(d_last, ref))
+    cpu_exact = bool(np.array_equal(d_cpu, ref))
     ctx.close()
     result = {
         "metric": "GTEPS for SSSP incremental re-eval (IncEval)",
@@ -824,10 +842,13 @@ def run_sssp(args, D: Dist):
         "e2e": {"value": round(D.sum(relax_e) / (te_ms * 1e-3) / 1e9, 4), "unit": "GTEPS",
                 "h2d_bytes_per_step": 16 * 100000, "d2h_bytes_per_step": 8 * n,
                 "ms_per_step": round(te_ms / K, 3)},
-        "cpu_baseline": {"value": round(E / dij_s / 1e9, 4), "unit": "GTEPS (graph edges / s)",
-                         "cores": 1, "kind": "port",
-                         "sample": f"FP64 Dijkstra recompute on the host after the last batch "
-                                   f"({dij_s:.2f} s)"},
+        "cpu_baseline": {"value": round(cst["edges"] / cpu_s / 1e9, 4), "unit": "GTEPS",
+                         "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"one IncEval of the reference's plain incremental SSSP "
+                                   f"(oracle restatement of deltaCompute + traversal) after a "
+                                   f"100,000-change batch: {cst['edges']} relaxations, "
+                                   f"{int(cst['residual'])} reset vertices, {cpu_s:.3f} s; "
+                                   f"distances equal Dijkstra: {cpu_exact}"},
     }
     if clk:
         result["clocks"] = clk

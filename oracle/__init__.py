@@ -44,6 +44,12 @@ def lib():
         L.or_pr_adjoint_solve.restype = C.c_int
         L.or_dijkstra.argtypes = [C.c_uint32, P, P, P, C.c_uint32, P]
         L.or_dijkstra.restype = C.c_int
+        L.or_sssp_peval.argtypes = [C.c_uint32, P, P, P, C.c_uint32, C.c_int, P, P,
+                                    C.POINTER(OrStats)]
+        L.or_sssp_peval.restype = C.c_int
+        L.or_sssp_inceval.argtypes = [C.c_uint32, P, P, P, P, P, C.c_uint64, P, P, C.c_int, P, P,
+                                      C.POINTER(OrStats)]
+        L.or_sssp_inceval.restype = C.c_int
         _lib = L
     return _lib
 
@@ -112,3 +118,39 @@ def dijkstra(rp, col, w, source=0):
     d = np.empty(n, np.float64)
     lib().or_dijkstra(n, _p(rp), _p(col), _p(w), source, _p(d))
     return d
+
+
+def sssp_peval(rp, col, w, source=0, threads=0):
+    """The reference's SSSP traversal from `source` (integer weights):
+    returns (distances f64 with inf, parents u32, stats)."""
+    rp, col, w = _csr(rp, col, w)
+    n = len(rp) - 1
+    d = np.empty(n, np.float64)
+    par = np.empty(n, np.uint32)
+    st = OrStats()
+    if lib().or_sssp_peval(n, _p(rp), _p(col), _p(w), source, threads, _p(d), _p(par),
+                           C.byref(st)):
+        raise ValueError("or_sssp_peval: bad source or non-integer weights")
+    return d, par, {k: getattr(st, k) for k, _ in OrStats._fields_}
+
+
+def sssp_inceval(old, new, deleted, dist, parent, threads=0):
+    """The reference's incremental SSSP stage (deltaCompute, then one round
+    from every vertex with a finite delta, then the traversal) after a batch:
+    `old` = (row_ptr, col) before it, `new` = (row_ptr, col, w) after it,
+    `deleted` = (src, dst) arrays of the removed edges (a re-weighted edge is
+    a removal plus an insert, as in the reference's update files).  Returns
+    (distances, parents, stats); stats["residual"] holds the reset count."""
+    rpo, colo, _ = _csr(*old[:2])
+    rp, col, w = _csr(*new[:3])
+    n = len(rp) - 1
+    ds = np.ascontiguousarray(deleted[0], np.uint32)
+    dd = np.ascontiguousarray(deleted[1], np.uint32)
+    d = np.array(dist, np.float64, copy=True)
+    par = np.array(parent, np.uint32, copy=True)
+    st = OrStats()
+    if lib().or_sssp_inceval(n, _p(rpo), _p(colo), _p(rp), _p(col), _p(w), len(ds), _p(ds),
+                             _p(dd), threads, _p(d), _p(par), C.byref(st)):
+        raise ValueError("or_sssp_inceval: non-integer weights")
+    return d, par, {k: getattr(st, k) for k, _ in OrStats._fields_}
+

