@@ -340,18 +340,24 @@ static int int_weights(uint64_t m, const float* w, uint32_t** wi) {
   return 0;
 }
 
-/* frontier rounds from `front` (count *nf, flags in `inq`) until empty */
+/* Frontier rounds from `front` until empty.  A vertex enters round r+1's
+ * frontier whenever its key improves during round r (once per round, by
+ * the stamp r+1), whether or not it is also in round r's frontier: a pop
+ * that cleared a flag could otherwise race with an improvement and lose it
+ * (the store-load pattern that weakly ordered hosts expose).  Rounds are
+ * separated by the parallel loop's barrier. */
 static void traverse(uint32_t n, const uint64_t* rp, const uint32_t* col, const uint32_t* w,
                      uint32_t* value, uint64_t* key, uint32_t* front, uint64_t nf, uint32_t* next,
-                     uint8_t* inq, or_stats* st) {
+                     uint32_t* stamp, uint32_t round, or_stats* st) {
   uint64_t edges = 0, visits = 0;
   int rounds = 0;
+  (void)n;
   while (nf) {
     uint64_t nn = 0;
+    const uint32_t tag = round + 1;
 #pragma omp parallel for schedule(dynamic, 256) reduction(+ : edges, visits)
     for (uint64_t i = 0; i < nf; ++i) {
       const uint32_t u = front[i];
-      inq[u] = 0;
       const uint64_t k = __atomic_load_n(key + u, __ATOMIC_RELAXED);
       const uint32_t d = (uint32_t)(k >> 32);
       if (k == OR_INF_KEY || !(d < value[u])) continue;  /* CombineValueDelta */
@@ -362,17 +368,18 @@ static void traverse(uint32_t n, const uint64_t* rp, const uint32_t* col, const 
         if (c >= 0xFFFFFFFFull) continue;
         ++edges;
         const uint32_t v = col[e];
-        if (key_min(key + v, (c << 32) | u) && !__atomic_exchange_n(inq + v, 1, __ATOMIC_RELAXED)) {
+        if (key_min(key + v, (c << 32) | u) &&
+            __atomic_exchange_n(stamp + v, tag, __ATOMIC_RELAXED) != tag) {
           const uint64_t p = __atomic_fetch_add(&nn, 1, __ATOMIC_RELAXED);
           next[p] = v;
         }
       }
     }
-    /* the next frontier's vertices were flagged; the flags clear on pop */
     uint32_t* t = front;
     front = next;
     next = t;
     nf = nn;
+    ++round;
     ++rounds;
   }
   st->rounds += rounds;
@@ -400,19 +407,19 @@ int or_sssp_peval(uint32_t n, const uint64_t* rp, const uint32_t* col, const flo
   uint64_t* key = (uint64_t*)malloc(sizeof(uint64_t) * n);
   uint32_t* f0 = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)n + 1));
   uint32_t* f1 = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)n + 1));
-  uint8_t* inq = (uint8_t*)calloc(n, 1);
+  uint32_t* stamp = (uint32_t*)calloc(n, sizeof(uint32_t));
   for (uint32_t v = 0; v < n; ++v) {
     value[v] = 0xFFFFFFFFu;
     key[v] = OR_INF_KEY;
   }
   key[source] = ((uint64_t)0 << 32) | OR_NO_PARENT;
   f0[0] = source;
-  inq[source] = 1;
+  stamp[source] = 1;
   memset(st, 0, sizeof(*st));
-  traverse(n, rp, col, wi, value, key, f0, 1, f1, inq, st);
+  traverse(n, rp, col, wi, value, key, f0, 1, f1, stamp, 1, st);
   st->converged = 1;
   finish_sssp(n, value, key, dist, parent);
-  free(wi); free(value); free(key); free(f0); free(f1); free(inq);
+  free(wi); free(value); free(key); free(f0); free(f1); free(stamp);
   return 0;
 }
 
@@ -427,7 +434,8 @@ int or_sssp_inceval(uint32_t n, const uint64_t* rp_old, const uint32_t* col_old,
   uint64_t* key = (uint64_t*)malloc(sizeof(uint64_t) * n);
   uint32_t* f0 = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)n + 1));
   uint32_t* f1 = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)n + 1));
-  uint8_t* inq = (uint8_t*)calloc(n, 1);
+  uint8_t* inq = (uint8_t*)calloc(n, 1);     /* reset marks */
+  uint32_t* stamp = (uint32_t*)calloc(n, sizeof(uint32_t));
   for (uint32_t v = 0; v < n; ++v) {
     const int fin = isfinite(dist[v]);
     value[v] = fin ? (uint32_t)dist[v] : 0xFFFFFFFFu;
@@ -467,8 +475,8 @@ int or_sssp_inceval(uint32_t n, const uint64_t* rp_old, const uint32_t* col_old,
     f1 = t;
     nf = nn;
   }
-  memset(inq, 0, n);
-  /* one round from every vertex with a finite delta, over the new graph */
+  /* one round from every vertex with a finite delta, over the new graph;
+   * improved vertices form the traversal's first frontier (stamp 1) */
   uint64_t nn = 0, edges = 0;
 #pragma omp parallel for schedule(dynamic, 1024) reduction(+ : edges)
   for (uint32_t u = 0; u < n; ++u) {
@@ -480,17 +488,17 @@ int or_sssp_inceval(uint32_t n, const uint64_t* rp_old, const uint32_t* col_old,
       if (c >= 0xFFFFFFFFull) continue;
       ++edges;
       const uint32_t v = col[e];
-      if (key_min(key + v, (c << 32) | u) && !__atomic_exchange_n(inq + v, 1, __ATOMIC_RELAXED)) {
+      if (key_min(key + v, (c << 32) | u) && __atomic_exchange_n(stamp + v, 1u, __ATOMIC_RELAXED) != 1u) {
         const uint64_t p = __atomic_fetch_add(&nn, 1, __ATOMIC_RELAXED);
         f1[p] = v;
       }
     }
   }
   st->edges += edges;
-  traverse(n, rp, col, wi, value, key, f1, nn, f0, inq, st);
+  traverse(n, rp, col, wi, value, key, f1, nn, f0, stamp, 1, st);
   st->converged = 1;
   st->residual = (double)n_reset;  /* reset vertices */
   finish_sssp(n, value, key, dist, parent);
-  free(wi); free(value); free(key); free(f0); free(f1); free(inq);
+  free(wi); free(value); free(key); free(f0); free(f1); free(inq); free(stamp);
   return 0;
 }
