@@ -150,6 +150,11 @@ struct SsspState {
   uint32_t* par_mark = nullptr;
   uint32_t* par_list = nullptr;
   uint32_t* inc_ctl = nullptr;    // [0..3] reset-BFS barrier / next, [4] changed, [5] refresh
+  // rows too long for one warp, deferred to a kernel in which every CTA
+  // scans a share of each: the rows, a per-row result and the count
+  uint32_t* hv_list = nullptr;
+  unsigned long long* hv_best = nullptr;
+  uint32_t* hv_cnt = nullptr;
   uint32_t chg_tag = 0;
   bool has_pending = false;       // a batch was applied since the last run
   double delta_width = 0;

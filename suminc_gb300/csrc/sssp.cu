@@ -29,6 +29,38 @@ enum {
 };
 enum { SC_EDGES = 0, SC_IMPROVE = 1, SC_VISITS = 2, SC_MIN = 3, SC_WORDS = 4 };
 
+// Rows (in- or out-adjacency) longer than kHeavyRow are left by the warp
+// kernels to a second kernel in which every CTA scans a share of each such
+// row: a hub's row on one warp would be the tail of the launch.  A deferred
+// row keeps its vertex and a 64-bit result (a distance key or a vertex id,
+// reduced by atomicMin).
+constexpr uint32_t kHeavyRow = 4096;
+
+struct HeavyRows {
+  uint32_t* list;
+  unsigned long long* best;
+  uint32_t* cnt;
+  uint32_t cap;
+};
+
+// called by one lane; false when the list is full (the warp then scans the
+// row itself)
+__device__ __forceinline__ bool defer_heavy(const HeavyRows& H, uint32_t v, unsigned long long init) {
+  const uint32_t s = atomicAdd(H.cnt, 1u);
+  if (s >= H.cap) return false;
+  H.list[s] = v;
+  H.best[s] = init;
+  return true;
+}
+
+__device__ __forceinline__ uint32_t heavy_count(const HeavyRows& H) { return min(*H.cnt, H.cap); }
+
+// warp-uniform: whether lane 0 deferred the row
+__device__ __forceinline__ bool warp_defer(const HeavyRows& H, uint32_t v, unsigned long long init) {
+  const bool ok = (threadIdx.x & 31) == 0 ? defer_heavy(H, v, init) : false;
+  return __shfl_sync(0xffffffffu, ok, 0);
+}
+
 struct SsspArgs {
   uint32_t n;
   const uint64_t* off;
@@ -280,13 +312,15 @@ __global__ void k_sssp_parents(uint32_t n, uint32_t source, const uint64_t* __re
 
 // The same over a list of vertices (IncEval: only vertices whose parent can
 // have changed).
-__global__ void k_sssp_parents_list(const uint32_t* __restrict__ list, uint32_t cnt, uint32_t source,
-                                    const uint64_t* __restrict__ off, const uint32_t* __restrict__ deg,
+__global__ void k_sssp_parents_list(const uint32_t* __restrict__ list, const uint32_t* cnt_dev,
+                                    uint32_t source, const uint64_t* __restrict__ off,
+                                    const uint32_t* __restrict__ deg,
                                     const uint32_t* __restrict__ col, const float* __restrict__ w,
                                     const unsigned long long* __restrict__ dist,
-                                    uint32_t* __restrict__ parent) {
+                                    uint32_t* __restrict__ parent, HeavyRows H) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t cnt = *cnt_dev;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += nwarps) {
     const uint32_t v = list[i];
     const unsigned long long dvb = dist[v];
@@ -294,6 +328,7 @@ __global__ void k_sssp_parents_list(const uint32_t* __restrict__ list, uint32_t 
     if (v != source && dvb < kInfBits) {
       const uint32_t d = deg[v];
       const uint64_t base = off[v];
+      if (d > kHeavyRow && warp_defer(H, v, kInvalidVid)) continue;
       for (uint32_t k = lane; k < d; k += 32) {
         const uint32_t u = col[base + k];
         const unsigned long long dub = dist[u];
@@ -306,34 +341,107 @@ __global__ void k_sssp_parents_list(const uint32_t* __restrict__ list, uint32_t 
   }
 }
 
-// Vertices whose parent (smallest tight in-neighbour) can change: those with
-// a changed distance, their out-neighbours, and heads of changed edges.
-__global__ void k_parent_candidates(const uint32_t* __restrict__ chg, uint32_t nchg,
-                                    const uint32_t* __restrict__ heads, uint32_t nheads,
-                                    const uint64_t* __restrict__ off, const uint32_t* __restrict__ deg,
-                                    const uint32_t* __restrict__ col, uint32_t* __restrict__ mark,
-                                    uint32_t tag, uint32_t* __restrict__ out, uint32_t* __restrict__ cnt) {
+// The parent of every vertex is its smallest tight in-neighbour.  After an
+// IncEval it can change only for (a) vertices whose distance changed (reset
+// or improved), (b) heads of inserted or re-weighted edges, and (c) vertices
+// that gain a smaller tight in-neighbour among the changed vertices: a
+// vertex whose distance is unchanged keeps a tight parent, since that parent
+// is unchanged too (a parent that got shorter would shorten the child; one
+// that got longer was reset with its subtree).  (a) and (b) are recomputed
+// in full over the in-row, (c) by a push over the changed vertices'
+// out-edges.
+
+// the vertices of (a) and (b), each once by the parent marks
+__global__ void k_parent_list(const uint32_t* __restrict__ chg, uint32_t nchg,
+                              const uint32_t* __restrict__ heads, uint32_t nheads,
+                              uint32_t* __restrict__ mark, uint32_t tag, uint32_t* __restrict__ out,
+                              uint32_t* __restrict__ cnt) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nchg + nheads;
+       i += gridDim.x * blockDim.x) {
+    const uint32_t u = i < nchg ? chg[i] : heads[i - nchg];
+    if (atomicExch(mark + u, tag) != tag) out[atomicAdd(cnt, 1u)] = u;
+  }
+}
+
+// every CTA: its share of each deferred in-row, smallest tight in-neighbour
+__global__ void __launch_bounds__(256) k_heavy_parent_scan(HeavyRows H, uint32_t source,
+                                                           const uint64_t* __restrict__ off,
+                                                           const uint32_t* __restrict__ deg,
+                                                           const uint32_t* __restrict__ col,
+                                                           const float* __restrict__ w,
+                                                           const unsigned long long* __restrict__ dist) {
+  const uint32_t nh = heavy_count(H);
+  for (uint32_t h = 0; h < nh; ++h) {
+    const uint32_t v = H.list[h];
+    const unsigned long long dvb = dist[v];
+    if (v == source || dvb >= kInfBits) continue;
+    const uint32_t d = deg[v];
+    const uint64_t base = off[v];
+    uint32_t best = kInvalidVid;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < d; k += gridDim.x * blockDim.x) {
+      const uint32_t u = col[base + k];
+      const unsigned long long dub = dist[u];
+      if (dub < kInfBits && dbits(bitsd(dub) + (double)w[base + k]) == dvb && u < best) best = u;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_down_sync(0xffffffffu, best, o));
+    if ((threadIdx.x & 31) == 0 && best != kInvalidVid)
+      atomicMin(H.best + h, (unsigned long long)best);
+  }
+}
+
+__global__ void k_heavy_parent_apply(HeavyRows H, uint32_t* __restrict__ parent) {
+  const uint32_t nh = heavy_count(H);
+  for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += gridDim.x * blockDim.x)
+    parent[H.list[h]] = (uint32_t)H.best[h];
+}
+
+// (c): a changed vertex u lowers the parent of an unchanged out-neighbour v
+// when the edge is tight (warp per changed vertex; long out-rows deferred)
+__device__ __forceinline__ void push_parent(uint32_t u, unsigned long long dub, uint32_t v, float wv,
+                                            uint32_t source, const unsigned long long* dist,
+                                            const uint32_t* chg_mark, uint32_t tag,
+                                            uint32_t* parent) {
+  if (v == source || chg_mark[v] == tag) return;
+  if (dbits(bitsd(dub) + (double)wv) == dist[v]) atomicMin(parent + v, u);
+}
+
+__global__ void k_parent_push(const uint32_t* __restrict__ chg, uint32_t nchg, uint32_t source,
+                              const uint64_t* __restrict__ off, const uint32_t* __restrict__ deg,
+                              const uint32_t* __restrict__ col, const float* __restrict__ w,
+                              const unsigned long long* __restrict__ dist,
+                              const uint32_t* __restrict__ chg_mark, uint32_t tag,
+                              uint32_t* __restrict__ parent, HeavyRows H) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nchg + nheads; i += nwarps) {
-    const uint32_t u = i < nchg ? chg[i] : heads[i - nchg];
-    bool take = lane == 0 && atomicExch(mark + u, tag) != tag;
-    uint32_t s0 = warp_append(take, cnt);
-    if (take) out[s0] = u;
-    if (i >= nchg) continue;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nchg; i += nwarps) {
+    const uint32_t u = chg[i];
+    const unsigned long long dub = dist[u];
+    if (dub >= kInfBits) continue;
+    const uint32_t d = deg[u];
+    if (d > kHeavyRow && warp_defer(H, u, 0ull)) continue;
+    const uint64_t base = off[u];
+    for (uint32_t k = lane; k < d; k += 32)
+      push_parent(u, dub, col[base + k], w[base + k], source, dist, chg_mark, tag, parent);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_heavy_parent_push(HeavyRows H, uint32_t source,
+                                                           const uint64_t* __restrict__ off,
+                                                           const uint32_t* __restrict__ deg,
+                                                           const uint32_t* __restrict__ col,
+                                                           const float* __restrict__ w,
+                                                           const unsigned long long* __restrict__ dist,
+                                                           const uint32_t* __restrict__ chg_mark,
+                                                           uint32_t tag, uint32_t* __restrict__ parent) {
+  const uint32_t nh = heavy_count(H);
+  for (uint32_t h = 0; h < nh; ++h) {
+    const uint32_t u = H.list[h];
+    const unsigned long long dub = dist[u];
     const uint32_t d = deg[u];
     const uint64_t base = off[u];
-    for (uint32_t kb = 0; kb < d; kb += 32) {
-      const uint32_t k = kb + lane;
-      uint32_t v = 0;
-      take = false;
-      if (k < d) {
-        v = col[base + k];
-        take = atomicExch(mark + v, tag) != tag;
-      }
-      const uint32_t s1 = warp_append(take, cnt);
-      if (take) out[s1] = v;
-    }
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < d; k += gridDim.x * blockDim.x)
+      push_parent(u, dub, col[base + k], w[base + k], source, dist, chg_mark, tag, parent);
   }
 }
 
@@ -428,19 +536,67 @@ __global__ void __launch_bounds__(256) k_sssp_reset_all(ResetArgs A) {
   }
 }
 
+// every CTA: its share of each deferred in-row, min over the in-neighbours
+// of dist[u] + w (as distance bits)
+__global__ void __launch_bounds__(256) k_heavy_reseed_scan(HeavyRows H, const uint64_t* __restrict__ off,
+                                                           const uint32_t* __restrict__ deg,
+                                                           const uint32_t* __restrict__ col,
+                                                           const float* __restrict__ w,
+                                                           const unsigned long long* __restrict__ dist) {
+  const uint32_t nh = heavy_count(H);
+  for (uint32_t h = 0; h < nh; ++h) {
+    const uint32_t v = H.list[h];
+    const uint32_t d = deg[v];
+    const uint64_t base = off[v];
+    unsigned long long best = kInfBits;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < d; k += gridDim.x * blockDim.x) {
+      const unsigned long long du = dist[col[base + k]];
+      if (du < kInfBits) {
+        const unsigned long long nb = dbits(bitsd(du) + (double)w[base + k]);
+        best = nb < best ? nb : best;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long t = __shfl_down_sync(0xffffffffu, best, o);
+      best = t < best ? t : best;
+    }
+    if ((threadIdx.x & 31) == 0 && best < kInfBits) atomicMin(H.best + h, best);
+  }
+}
+
+__global__ void k_heavy_reseed_apply(HeavyRows H, unsigned long long* __restrict__ dist,
+                                     uint32_t* __restrict__ fq, uint32_t* __restrict__ fq_cnt,
+                                     uint32_t* chg_mark, uint32_t* chg_list, uint32_t* chg_cnt,
+                                     uint32_t chg_tag) {
+  const uint32_t nh = heavy_count(H);
+  for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += gridDim.x * blockDim.x) {
+    const uint32_t v = H.list[h];
+    const unsigned long long best = H.best[h];
+    if (best >= kInfBits) continue;
+    const unsigned long long old = atomicMin(dist + v, best);
+    if (best < old) {
+      fq[atomicAdd(fq_cnt, 1u)] = v;
+      if (chg_mark && atomicExch(chg_mark + v, chg_tag) != chg_tag)
+        chg_list[atomicAdd(chg_cnt, 1u)] = v;
+    }
+  }
+}
+
 // Re-seed reset vertices from their in-neighbours (pull) and queue them.
 __global__ void k_sssp_reseed(const uint32_t* __restrict__ list, uint32_t cnt,
                               const uint64_t* __restrict__ off, const uint32_t* __restrict__ deg,
                               const uint32_t* __restrict__ col, const float* __restrict__ w,
                               unsigned long long* __restrict__ dist, uint32_t* __restrict__ fq,
                               uint32_t* __restrict__ fq_cnt, uint32_t* chg_mark, uint32_t* chg_list,
-                              uint32_t* chg_cnt, uint32_t chg_tag) {
+                              uint32_t* chg_cnt, uint32_t chg_tag, HeavyRows H) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += nwarps) {
     const uint32_t v = list[i];
     const uint32_t d = deg[v];
     const uint64_t base = off[v];
+    if (d > kHeavyRow && warp_defer(H, v, kInfBits)) continue;
     unsigned long long best = kInfBits;
     for (uint32_t k = lane; k < d; k += 32) {
       const unsigned long long du = dist[col[base + k]];
@@ -496,6 +652,7 @@ sg_status sssp_free(sg_ctx* ctx) {
   dfree(s.out);
   dfree(s.padd_dst);
   dfree(s.chg_mark); dfree(s.chg_list); dfree(s.par_mark); dfree(s.par_list); dfree(s.inc_ctl);
+  dfree(s.hv_list); dfree(s.hv_best); dfree(s.hv_cnt);
   s = SsspState();
   return SG_OK;
 }
@@ -534,6 +691,9 @@ static sg_status sssp_alloc(sg_ctx* ctx) {
   SG_TRY(dalloc(ctx, &s.par_mark, n));
   SG_TRY(dalloc(ctx, &s.par_list, n));
   SG_TRY(dalloc(ctx, &s.inc_ctl, 8));
+  SG_TRY(dalloc(ctx, &s.hv_list, n));
+  SG_TRY(dalloc(ctx, &s.hv_best, n));
+  SG_TRY(dalloc(ctx, &s.hv_cnt, 4));
   SG_CUDA(ctx, cudaMemsetAsync(s.chg_mark, 0, 4ull * n, ctx->stream));
   SG_CUDA(ctx, cudaMemsetAsync(s.par_mark, 0, 4ull * n, ctx->stream));
   s.chg_tag = 0;
@@ -877,14 +1037,23 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
   }
   SG_CUDA(ctx, cudaMemsetAsync(s.d_ctl, 0, sizeof(uint32_t) * S_WORDS, st));
   SG_CUDA(ctx, cudaMemsetAsync(s.d_cnt, 0, sizeof(unsigned long long) * SC_WORDS, st));
-  if (total > 0)
-    k_sssp_reseed<<<grid_for((uint64_t)total * 32, 256), 256, 0, st>>>(
-        s.seeds, total, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.far, s.d_ctl + S_F0,
-        s.chg_mark, s.chg_list, s.inc_ctl + 4, s.chg_tag);
-  if (nadd > 0)
-    k_sssp_reseed<<<grid_for((uint64_t)nadd * 32, 256), 256, 0, st>>>(
-        s.padd_dst, nadd, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.far, s.d_ctl + S_F0,
-        s.chg_mark, s.chg_list, s.inc_ctl + 4, s.chg_tag);
+  const HeavyRows H{s.hv_list, s.hv_best, s.hv_cnt, g.n};
+  const unsigned heavy_grid = ctx->num_sms * 4;
+  // re-seed a list: warps pull the short in-rows, every CTA a share of the
+  // long ones, then the long rows' results are applied
+  auto reseed = [&](const uint32_t* list, uint32_t cnt) -> sg_status {
+    SG_CUDA(ctx, cudaMemsetAsync(s.hv_cnt, 0, 4, st));
+    k_sssp_reseed<<<grid_for((uint64_t)cnt * 32, 256), 256, 0, st>>>(
+        list, cnt, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.far, s.d_ctl + S_F0,
+        s.chg_mark, s.chg_list, s.inc_ctl + 4, s.chg_tag, H);
+    k_heavy_reseed_scan<<<heavy_grid, 256, 0, st>>>(H, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist);
+    k_heavy_reseed_apply<<<4, 256, 0, st>>>(H, s.dist, s.far, s.d_ctl + S_F0, s.chg_mark,
+                                            s.chg_list, s.inc_ctl + 4, s.chg_tag);
+    count_launch(ctx, 3);
+    return SG_OK;
+  };
+  if (total > 0) SG_TRY(reseed(s.seeds, total));
+  if (nadd > 0) SG_TRY(reseed(s.padd_dst, nadd));
   SG_CUDA(ctx, cudaGetLastError());
   // 3. delta-stepping from the seeds, listing every improved vertex
   SG_TRY(sssp_launch(ctx, true));
@@ -894,16 +1063,29 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
   SG_CUDA(ctx, cudaMemcpyAsync(&nchg, s.inc_ctl + 4, 4, cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   if (nchg + nadd > 0) {
-    k_parent_candidates<<<grid_for((uint64_t)(nchg + nadd) * 32, 256), 256, 0, st>>>(
-        s.chg_list, nchg, s.padd_dst, nadd, g.out.off, g.out.deg, g.out.col, s.par_mark, s.chg_tag,
-        s.par_list, s.inc_ctl + 5);
-    uint32_t npar = 0;
-    SG_CUDA(ctx, cudaMemcpyAsync(&npar, s.inc_ctl + 5, 4, cudaMemcpyDeviceToHost, st));
-    SG_CUDA(ctx, cudaStreamSynchronize(st));
-    if (npar > 0)
-      k_sssp_parents_list<<<grid_for((uint64_t)npar * 32, 256), 256, 0, st>>>(
-          s.par_list, npar, s.source, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.parent);
-    count_launch(ctx, 2);
+    // (a) + (b) in full, long in-rows by every CTA; then (c) by a push
+    SG_CUDA(ctx, cudaMemsetAsync(s.inc_ctl + 5, 0, 4, st));
+    SG_CUDA(ctx, cudaMemsetAsync(s.hv_cnt, 0, 4, st));
+    k_parent_list<<<grid_for(nchg + nadd, 256), 256, 0, st>>>(s.chg_list, nchg, s.padd_dst, nadd,
+                                                              s.par_mark, s.chg_tag, s.par_list,
+                                                              s.inc_ctl + 5);
+    k_sssp_parents_list<<<ctx->num_sms * 8, 256, 0, st>>>(s.par_list, s.inc_ctl + 5, s.source,
+                                                          g.in.off, g.in.deg, g.in.col, g.in.w,
+                                                          s.dist, s.parent, H);
+    k_heavy_parent_scan<<<heavy_grid, 256, 0, st>>>(H, s.source, g.in.off, g.in.deg, g.in.col,
+                                                    g.in.w, s.dist);
+    k_heavy_parent_apply<<<4, 256, 0, st>>>(H, s.parent);
+    count_launch(ctx, 4);
+    if (nchg > 0) {
+      SG_CUDA(ctx, cudaMemsetAsync(s.hv_cnt, 0, 4, st));
+      k_parent_push<<<grid_for((uint64_t)nchg * 32, 256), 256, 0, st>>>(
+          s.chg_list, nchg, s.source, g.out.off, g.out.deg, g.out.col, g.out.w, s.dist, s.chg_mark,
+          s.chg_tag, s.parent, H);
+      k_heavy_parent_push<<<heavy_grid, 256, 0, st>>>(H, s.source, g.out.off, g.out.deg, g.out.col,
+                                                      g.out.w, s.dist, s.chg_mark, s.chg_tag,
+                                                      s.parent);
+      count_launch(ctx, 2);
+    }
   }
   SG_CUDA(ctx, cudaGetLastError());
   SG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
