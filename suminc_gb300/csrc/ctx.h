@@ -152,6 +152,8 @@ struct SsspState {
   uint32_t* inc_ctl = nullptr;    // [0..3] reset-BFS barrier / next, [4] changed, [5] refresh
   // rows too long for one warp, deferred to a kernel in which every CTA
   // scans a share of each: the rows, a per-row result and the count
+  uint32_t* seed_mark = nullptr;  // re-seed: each head once per IncEval (tag)
+  uint32_t seed_tag = 0;
   uint32_t* hv_list = nullptr;
   unsigned long long* hv_best = nullptr;
   uint32_t* hv_cnt = nullptr;

@@ -589,11 +589,15 @@ __global__ void k_sssp_reseed(const uint32_t* __restrict__ list, uint32_t cnt,
                               const uint32_t* __restrict__ col, const float* __restrict__ w,
                               unsigned long long* __restrict__ dist, uint32_t* __restrict__ fq,
                               uint32_t* __restrict__ fq_cnt, uint32_t* chg_mark, uint32_t* chg_list,
-                              uint32_t* chg_cnt, uint32_t chg_tag, HeavyRows H) {
+                              uint32_t* chg_cnt, uint32_t chg_tag, HeavyRows H,
+                              uint32_t* __restrict__ seen, uint32_t seen_tag) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt; i += nwarps) {
     const uint32_t v = list[i];
+    // a head listed more than once (several new edges into it) is pulled once
+    const bool dup = lane == 0 && atomicExch(seen + v, seen_tag) == seen_tag;
+    if (__shfl_sync(0xffffffffu, dup, 0)) continue;
     const uint32_t d = deg[v];
     const uint64_t base = off[v];
     if (d > kHeavyRow && warp_defer(H, v, kInfBits)) continue;
@@ -652,7 +656,7 @@ sg_status sssp_free(sg_ctx* ctx) {
   dfree(s.out);
   dfree(s.padd_dst);
   dfree(s.chg_mark); dfree(s.chg_list); dfree(s.par_mark); dfree(s.par_list); dfree(s.inc_ctl);
-  dfree(s.hv_list); dfree(s.hv_best); dfree(s.hv_cnt);
+  dfree(s.hv_list); dfree(s.hv_best); dfree(s.hv_cnt); dfree(s.seed_mark);
   s = SsspState();
   return SG_OK;
 }
@@ -694,6 +698,9 @@ static sg_status sssp_alloc(sg_ctx* ctx) {
   SG_TRY(dalloc(ctx, &s.hv_list, n));
   SG_TRY(dalloc(ctx, &s.hv_best, n));
   SG_TRY(dalloc(ctx, &s.hv_cnt, 4));
+  SG_TRY(dalloc(ctx, &s.seed_mark, n));
+  SG_CUDA(ctx, cudaMemsetAsync(s.seed_mark, 0, 4ull * n, ctx->stream));
+  s.seed_tag = 0;
   SG_CUDA(ctx, cudaMemsetAsync(s.chg_mark, 0, 4ull * n, ctx->stream));
   SG_CUDA(ctx, cudaMemsetAsync(s.par_mark, 0, 4ull * n, ctx->stream));
   s.chg_tag = 0;
@@ -1038,6 +1045,10 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
   SG_CUDA(ctx, cudaMemsetAsync(s.d_ctl, 0, sizeof(uint32_t) * S_WORDS, st));
   SG_CUDA(ctx, cudaMemsetAsync(s.d_cnt, 0, sizeof(unsigned long long) * SC_WORDS, st));
   const HeavyRows H{s.hv_list, s.hv_best, s.hv_cnt, g.n};
+  if (++s.seed_tag == 0) {  // tags wrapped: clear the marks
+    SG_CUDA(ctx, cudaMemsetAsync(s.seed_mark, 0, 4ull * g.n, st));
+    s.seed_tag = 1;
+  }
   const unsigned heavy_grid = ctx->num_sms * 4;
   // re-seed a list: warps pull the short in-rows, every CTA a share of the
   // long ones, then the long rows' results are applied
@@ -1045,7 +1056,7 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
     SG_CUDA(ctx, cudaMemsetAsync(s.hv_cnt, 0, 4, st));
     k_sssp_reseed<<<grid_for((uint64_t)cnt * 32, 256), 256, 0, st>>>(
         list, cnt, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist, s.far, s.d_ctl + S_F0,
-        s.chg_mark, s.chg_list, s.inc_ctl + 4, s.chg_tag, H);
+        s.chg_mark, s.chg_list, s.inc_ctl + 4, s.chg_tag, H, s.seed_mark, s.seed_tag);
     k_heavy_reseed_scan<<<heavy_grid, 256, 0, st>>>(H, g.in.off, g.in.deg, g.in.col, g.in.w, s.dist);
     k_heavy_reseed_apply<<<4, 256, 0, st>>>(H, s.dist, s.far, s.d_ctl + S_F0, s.chg_mark,
                                             s.chg_list, s.inc_ctl + 4, s.chg_tag);
