@@ -465,6 +465,8 @@ struct ResetArgs {
   uint32_t* chg_cnt;
   uint32_t chg_tag;
   long long spin_limit;
+  uint32_t* hv;       // two halves of hv_half entries: long rows deferred by a level
+  uint32_t hv_half;
 };
 
 __device__ __forceinline__ bool reset_sync(const ResetArgs& A) {
@@ -493,38 +495,72 @@ __device__ __forceinline__ bool reset_sync(const ResetArgs& A) {
   return *(volatile uint32_t*)(A.ctl + 2) == 0;
 }
 
+// children of x whose parent is x join the list (warp w of nw scans the
+// row's 32-entry chunks w, w + nw, ...)
+__device__ __forceinline__ void reset_scan_row(const ResetArgs& A, uint32_t x, uint32_t w,
+                                               uint32_t nw) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t d = A.deg[x];
+  const uint64_t base = A.off[x];
+  for (uint64_t kb = (uint64_t)w * 32; kb < d; kb += (uint64_t)nw * 32) {
+    const uint64_t k = kb + lane;
+    bool take = false;
+    uint32_t y = 0;
+    if (k < d) {
+      y = A.col[base + k];
+      take = __ldcg(A.parent + y) == x && y != x && atomicExch(A.reset + y, 1u) == 0u;
+    }
+    const uint32_t s0 = warp_append(take, A.ctl + 3);
+    if (take) {
+      if (s0 < A.cap) A.list[s0] = y;
+      else atomicExch(A.ctl + 2, 2u);
+    }
+  }
+}
+
+// Each level: warps scan the short out-rows of the level's vertices, and
+// every warp of the grid scans a share of each long row deferred by the
+// previous level (a hub's row on one warp would hold the level's barrier).
+// Children found from a deferred row join one level late, which the
+// closure does not mind.  ctl [6], [7]: deferred counts by level parity.
 __global__ void __launch_bounds__(256) k_sssp_reset_all(ResetArgs A) {
-  __shared__ uint32_t s_end;
+  __shared__ uint32_t s_end, s_hv;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   uint32_t begin = 0;
   uint32_t end = min(*(volatile const uint32_t*)A.seed_cnt, A.cap);
-  while (end > begin) {
+  uint32_t hv_prev = 0;
+  for (uint32_t lvl = 0; end > begin || hv_prev > 0; ++lvl) {
+    const uint32_t cur = lvl & 1;
+    uint32_t* hv_cur = A.hv + (size_t)cur * A.hv_half;
+    const uint32_t* hv_old = A.hv + (size_t)(cur ^ 1) * A.hv_half;
     for (uint32_t i = begin + wid; i < end; i += nwarps) {
       const uint32_t x = __ldcg(A.list + i);
-      const uint32_t d = A.deg[x];
-      const uint64_t base = A.off[x];
-      for (uint32_t kb = 0; kb < d; kb += 32) {
-        const uint32_t k = kb + lane;
-        bool take = false;
-        uint32_t y = 0;
-        if (k < d) {
-          y = A.col[base + k];
-          take = __ldcg(A.parent + y) == x && y != x && atomicExch(A.reset + y, 1u) == 0u;
+      if (A.deg[x] > kHeavyRow) {
+        bool deferred = false;
+        if (lane == 0) {
+          const uint32_t s = atomicAdd(A.ctl + 6 + cur, 1u);
+          deferred = s < A.hv_half;
+          if (deferred) hv_cur[s] = x;
         }
-        const uint32_t s0 = warp_append(take, A.ctl + 3);
-        if (take) {
-          if (s0 < A.cap) A.list[s0] = y;
-          else atomicExch(A.ctl + 2, 2u);
-        }
+        if (__shfl_sync(0xffffffffu, deferred, 0)) continue;
       }
+      reset_scan_row(A, x, 0, 1);
     }
+    for (uint32_t h = 0; h < hv_prev; ++h) reset_scan_row(A, __ldcg(hv_old + h), wid, nwarps);
     if (!reset_sync(A)) return;
-    if (threadIdx.x == 0) s_end = min(*(volatile uint32_t*)(A.ctl + 3), A.cap);
+    if (threadIdx.x == 0) {
+      s_end = min(*(volatile uint32_t*)(A.ctl + 3), A.cap);
+      s_hv = min(*(volatile uint32_t*)(A.ctl + 6 + cur), A.hv_half);
+    }
     __syncthreads();
     begin = end;
     end = s_end;
+    hv_prev = s_hv;
+    // the previous level's deferred list is consumed: its counter serves
+    // the next level
+    if (blockIdx.x == 0 && threadIdx.x == 0) A.ctl[6 + (cur ^ 1)] = 0;
     if (!reset_sync(A)) return;
   }
   // reset the whole list (the BFS above read the old parents)
@@ -983,6 +1019,8 @@ __global__ void k_inc_start(const uint32_t* seed_cnt, uint32_t* inc_ctl) {
   inc_ctl[3] = seed_cnt[0];
   inc_ctl[4] = 0;
   inc_ctl[5] = 0;
+  inc_ctl[6] = 0;
+  inc_ctl[7] = 0;
 }
 
 sg_status sssp_run_inceval(sg_ctx* ctx) {
@@ -1015,6 +1053,8 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
     R.chg_cnt = s.inc_ctl + 4;
     R.chg_tag = s.chg_tag;
     R.spin_limit = 40ll * 1000 * 1000;
+    R.hv = s.hv_list;
+    R.hv_half = g.n / 2;
     int bps = 0;
     SG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_sssp_reset_all, 256, 0));
     if (bps < 1) return fail(ctx, SG_ERR_CUDA, "reset kernel cannot be resident");
