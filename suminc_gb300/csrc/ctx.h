@@ -265,9 +265,10 @@ sg_status pr_run(sg_ctx* ctx, bool inc);
 // failure detection: the persistent kernels' grid barrier, met by a few CTAs
 // (skip: one CTA never arrives, the bounded waits run out)
 sg_status sssp_barrier_probe(sg_ctx* ctx, int skip);
-// after an apply (the generation already bumped): re-encodes the hub view's
-// copy of the given in-rows when it was current before the batch
-sg_status pr_hub_after_apply(sg_ctx* ctx, const uint32_t* rows, uint64_t nrows);
+// after an apply (the generation already bumped): the hub view's copy is
+// current again when the applier patched it (patched), else its touched
+// in-rows are re-encoded when it was current before the batch
+sg_status pr_hub_after_apply(sg_ctx* ctx, const uint32_t* rows, uint64_t nrows, bool patched);
 // buffers and direction of one delta-PageRank run (pagerank.cu)
 struct PrBufs {
   float* x;

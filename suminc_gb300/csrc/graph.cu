@@ -950,10 +950,24 @@ struct ApplyDirArgs {
   uint32_t* sp_reset;
   uint32_t* sp_seeds;
   uint32_t* sp_seed_count;
+  // the PageRank pull's encoded column copy (in direction; null when none
+  // is current): every column write is mirrored there, hubs encoded
+  uint32_t* col2;
+  const uint32_t* hub_slot;
+  uint32_t n;
   // bookkeeping
   unsigned long long* d_dm;  // signed edge-count change (two's complement)
   uint32_t* d_err;
 };
+
+// a column write, mirrored into the encoded copy when there is one
+__device__ __forceinline__ void put_col(const ApplyDirArgs& A, uint64_t p, uint32_t x) {
+  A.c.col[p] = x;
+  if (A.col2) {
+    const uint32_t h = x < A.n ? A.hub_slot[x] : ~0u;
+    A.col2[p] = h != ~0u ? (0x80000000u | h) : x;
+  }
+}
 
 __device__ __forceinline__ uint32_t act_at(const ApplyDirArgs& A, uint32_t j) {
   return A.perm ? A.perm[j] : j;
@@ -1015,7 +1029,7 @@ __global__ void __launch_bounds__(256) k_apply_find(ApplyDirArgs A) {
       const uint32_t a = act_at(A, (uint32_t)j);
       const uint32_t kind = A.a_kind[a];
       A.a_pos[a] = k;
-      if (kind == 1u) A.c.col[base + k] = kInvalidVid;
+      if (kind == 1u) put_col(A, base + k, kInvalidVid);
       else if ((kind & 2u) && A.c.w) A.c.w[base + k] = A.a_w[a];
     }
   }
@@ -1151,7 +1165,7 @@ __global__ void __launch_bounds__(256) k_apply_finish(ApplyDirArgs A) {
       const uint32_t mask = __ballot_sync(0xffffffffu, live);
       if (live) {
         const uint32_t h = A.a_tmp[b + r + __popc(mask & lanemask_lt())];
-        A.c.col[base + h] = cval;
+        put_col(A, base + h, cval);
         if (A.c.w) A.c.w[base + h] = wv;
       }
       r += __popc(mask);
@@ -1173,7 +1187,7 @@ __global__ void __launch_bounds__(256) k_apply_finish(ApplyDirArgs A) {
         continue;  // insertions dropped; host reports SG_ERR_OOM
       }
       for (uint32_t k = lane; k < newlen; k += 32) {
-        A.c.col[nb + k] = A.c.col[base + k];
+        put_col(A, nb + k, A.c.col[base + k]);
         if (A.c.w) A.c.w[nb + k] = A.c.w[base + k];
       }
       __syncwarp();
@@ -1195,7 +1209,7 @@ __global__ void __launch_bounds__(256) k_apply_finish(ApplyDirArgs A) {
       const uint32_t mask = __ballot_sync(0xffffffffu, ins);
       const uint32_t pos = wp + __popc(mask & lanemask_lt());
       if (ins) {
-        A.c.col[base + pos] = A.a_nbr[a];
+        put_col(A, base + pos, A.a_nbr[a]);
         if (A.c.w) A.c.w[base + pos] = A.a_w[a];
       }
       wp += __popc(mask);
@@ -1340,6 +1354,15 @@ sg_status apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* upd
   I.chunk_off = B.chunk_off + (B.cap + 1);
   I.out_dir = false;
   I.pr_x = nullptr; I.pr_delta = nullptr; I.sp_parent = nullptr;
+  // the hub view's copy, when it reflects the adjacency before this batch in
+  // the layout the batch edits (no repack above), is patched alongside
+  const HubView& hv = g.hub;
+  const bool patch_view = hv.col && hv.k > 0 && hv.gen == g.gen && hv.layout == g.in.layout &&
+                          hv.cap == g.in.pool_cap;
+  A.col2 = nullptr; A.hub_slot = nullptr; A.n = g.n;
+  I.col2 = patch_view ? hv.col : nullptr;
+  I.hub_slot = patch_view ? hv.slot : nullptr;
+  I.n = g.n;
   // work items: ceil(degree / chunk) per group and direction
   k_apply_chunks<<<grid_for(A.n_grp + 1, 256), 256, 0, ctx->stream>>>(A, B.nch);
   SG_TRY(exclusive_sum(ctx, B.nch, B.chunk_off, A.n_grp + 1));
@@ -1375,7 +1398,7 @@ sg_status apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* upd
   }
   g.m = (uint64_t)((long long)g.m + dm);
   SG_TRY(graph_rebuild_worklists(ctx));
-  SG_TRY(pr_hub_after_apply(ctx, B.igrp_vertex, B.n_igrp));
+  SG_TRY(pr_hub_after_apply(ctx, B.igrp_vertex, B.n_igrp, patch_view));
   return SG_OK;
 }
 

@@ -325,9 +325,13 @@ __global__ void __launch_bounds__(256) k_hub_encode_rows(const uint64_t* __restr
 sg_status cub_select_flagged_u32(sg_ctx* ctx, const uint32_t* in, const uint8_t* flags,
                                  uint32_t* out, uint64_t* d_count, uint64_t n);
 
-sg_status pr_hub_after_apply(sg_ctx* ctx, const uint32_t* rows, uint64_t nrows) {
+sg_status pr_hub_after_apply(sg_ctx* ctx, const uint32_t* rows, uint64_t nrows, bool patched) {
   DevGraph& g = ctx->g;
   HubView& H = g.hub;
+  if (patched && H.col && H.gen + 1 == g.gen && H.layout == g.in.layout && H.cap == g.in.pool_cap) {
+    H.gen = g.gen;
+    return SG_OK;
+  }
   // only a copy that reflected the adjacency right before this batch (one
   // generation back) in the same layout can be patched; others stay stale
   // and are re-encoded in full by the next pull
