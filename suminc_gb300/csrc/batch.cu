@@ -887,6 +887,7 @@ static sg_status batch_reserve(sg_ctx* ctx, BatchState& B, uint32_t qw, uint32_t
 
 static sg_status batch_chunks(sg_ctx* ctx, BatchState& B, uint32_t cq) {
   DevGraph& g = ctx->g;
+  SG_TRY(graph_in_worklists(ctx));
   if (B.chunk_gen == g.gen && B.chunk_cq == cq) return SG_OK;
   const uint64_t nch = (g.in_wl.quads + cq - 1) / cq;
   if (nch + 1 > B.chunk_cap) {

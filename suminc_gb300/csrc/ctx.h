@@ -249,6 +249,7 @@ sg_status graph_build_from_sorted_keys(sg_ctx* ctx, uint32_t n, uint64_t m,
 sg_status graph_rebuild_worklists(sg_ctx* ctx);
 // out-CSR work lists for pulls along out-edges (built when stale)
 sg_status graph_out_worklists(sg_ctx* ctx);
+sg_status graph_in_worklists(sg_ctx* ctx);  // current in-CSR pull lists
 void pull_lists_free(PullLists& L);
 // packed out-CSR with rows sorted by neighbour (the order of
 // sg_graph_download_csr), into caller-owned device arrays

@@ -400,9 +400,15 @@ static sg_status build_lists(sg_ctx* ctx, const DevCSR& c, PullLists& L) {
   return SG_OK;
 }
 
+// the adjacency changed: work lists are rebuilt by their next user
 sg_status graph_rebuild_worklists(sg_ctx* ctx) {
+  ctx->g.gen++;
+  return SG_OK;
+}
+
+sg_status graph_in_worklists(sg_ctx* ctx) {
   DevGraph& g = ctx->g;
-  g.gen++;
+  if (g.in_wl.nz && g.in_wl.gen == g.gen && g.in_wl.n_alloc == g.n) return SG_OK;
   return build_lists(ctx, g.in, g.in_wl);
 }
 

@@ -600,6 +600,7 @@ sg_status pr_run_personalized(sg_ctx* ctx, const uint32_t* d_seeds, uint32_t n_s
 sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R) {
   DevGraph& g = ctx->g;
   cudaStream_t st = ctx->stream;
+  if (R.lists == &g.in_wl) SG_TRY(graph_in_worklists(ctx));
   const PrBufs& s = R.buf;
   const PullLists& L = *R.lists;
   SG_CUDA(ctx, cudaMemsetAsync(s.misc, 0, sizeof(uint32_t) * M_WORDS, st));
