@@ -14,10 +14,13 @@
 //                 of 32 4-edge quads (one 128-bit neighbour load and four
 //                 push-value gathers per lane, owners found by popc over the
 //                 tile's segment starts, segmented shuffle sums).  A vertex
-//                 whose quads all lie in the tile is updated by the first
-//                 lane of its run (incoming sum, residual, activation, next
-//                 push value); a vertex spanning tiles gets its partial sums
-//                 by atomicAdd
+//                 whose quads all lie in the tile is updated by its owner
+//                 lane (incoming sum, residual, activation, next push
+//                 value); a vertex spanning tiles gets its partial sums by
+//                 atomicAdd.  With the hub cache (the default on graphs
+//                 with enough high out-degree vertices) each CTA first copies
+//                 the hubs' push values into shared memory and reads an
+//                 encoded column copy in which a hub's id is its slot
 //   k_pr_fixup    updates the tile-spanning vertices; its last block makes
 //                 the termination decision on the device
 // Push values are double-buffered by pull index.  When the residual passes
