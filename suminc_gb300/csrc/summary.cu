@@ -88,6 +88,7 @@ struct SummaryDev {
   // correction lists; built on first use, repaired after each batch
   bool sssp_ready = false;
   std::vector<std::vector<std::pair<uint32_t, double>>> sp_bound_d, sp_inner_d;
+  std::vector<uint32_t> sssp_pending;  // supernodes touched since, repaired on the next SSSP use
   uint64_t *sk_off = nullptr, *sk_coff = nullptr;
   uint32_t *sk_deg = nullptr, *sk_col = nullptr, *sk_crow = nullptr, *sk_cv = nullptr;
   float *sk_w = nullptr, *sk_cd = nullptr;
@@ -1285,12 +1286,9 @@ sg_status summary_after_apply(sg_ctx* ctx) {
   summary_sketch_csr(S, D->out);
   SG_TRY(upload_sketch(ctx, *D));
   if (D->sssp_ready && ctx->g.weighted) {
-    // shortcut distances of the touched supernodes; new supernodes get theirs
-    if (D->sp_bound_d.size() < S.supernodes.size()) {
-      D->sp_bound_d.resize(S.supernodes.size());
-      D->sp_inner_d.resize(S.supernodes.size());
-    }
-    SG_TRY(sssp_shortcuts(ctx, *D, sps));
+    // shortcut distances of the touched supernodes are repaired by the next
+    // SSSP query over the summary (a PageRank-only caller never pays them)
+    D->sssp_pending.insert(D->sssp_pending.end(), sps.begin(), sps.end());
   }
   D->sk_stale = true;
   return SG_OK;
@@ -1644,6 +1642,24 @@ sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
     for (uint32_t i = 0; i < all_sp.size(); ++i) all_sp[i] = i;
     SG_TRY(sssp_shortcuts(ctx, D, all_sp));
     D.sssp_ready = true;
+    D.sssp_pending.clear();
+  }
+  if (!D.sssp_pending.empty()) {
+    // supernodes touched by the batches since the last query; new
+    // supernodes get their lists
+    std::vector<uint32_t>& P = D.sssp_pending;
+    std::sort(P.begin(), P.end());
+    P.erase(std::unique(P.begin(), P.end()), P.end());
+    P.erase(std::remove_if(P.begin(), P.end(),
+                           [&](uint32_t sp) { return sp >= S.supernodes.size(); }),
+            P.end());
+    if (D.sp_bound_d.size() < S.supernodes.size()) {
+      D.sp_bound_d.resize(S.supernodes.size());
+      D.sp_inner_d.resize(S.supernodes.size());
+    }
+    SG_TRY(sssp_shortcuts(ctx, D, P));
+    P.clear();
+    D.sk_stale = true;
   }
   if (D.sk_stale) SG_TRY(sssp_sketch(ctx, D));
   // seeds: the source, expanded inside its cluster when it is a member
