@@ -25,6 +25,7 @@ enum {
   S_ERR = 7,
   S_ITERS = 8,
   S_SPLITS = 9,
+  S_H0 = 10, S_H1 = 11, S_H2 = 12,   // deferred long-row counts (slots as near)
   S_WORDS = 16
 };
 enum { SC_EDGES = 0, SC_IMPROVE = 1, SC_VISITS = 2, SC_MIN = 3, SC_WORDS = 4 };
@@ -84,6 +85,12 @@ struct SsspArgs {
   uint32_t* chg_list;
   uint32_t* chg_cnt;
   uint32_t chg_tag;
+  // vertices of a near queue with out-rows longer than kHeavyRow are
+  // deferred to the next iteration, in which every warp relaxes a share of
+  // each (null: relaxed by one warp); three slots of hcap, rotating as the
+  // near queues
+  uint32_t* hq[3];
+  uint32_t hcap;
 };
 
 __device__ __forceinline__ void note_change(const SsspArgs& A, uint32_t x) {
@@ -125,60 +132,92 @@ __global__ void k_barrier_probe(SsspArgs A, int skip) {
   grid_sync(A);
 }
 
-// Relaxes the out-edges of every vertex in `q` (warp per vertex, 4-edge
-// quads, 128-bit loads of neighbour and weight arrays).
-__device__ __forceinline__ void relax_queue(const SsspArgs& A, const uint32_t* q, uint32_t qn,
-                                            double thr, uint32_t* nq_next, uint32_t* nq_cnt,
-                                            uint32_t* fq, uint32_t* fq_cnt, uint32_t tag,
-                                            unsigned long long& edges,
-                                            unsigned long long& improve) {
+// Relaxes one 128-edge chunk (4-edge quad per lane, 128-bit loads of
+// neighbour and weight arrays) of vertex v's out-row; improved vertices go
+// to the next near queue (inside the window) or the far queue.
+__device__ __forceinline__ void relax_chunk(const SsspArgs& A, uint64_t base, uint32_t d, uint32_t kb,
+                                            double dv, double thr, uint32_t* nq_next,
+                                            uint32_t* nq_cnt, uint32_t* fq, uint32_t* fq_cnt,
+                                            uint32_t tag, unsigned long long& improve) {
   const uint32_t lane = threadIdx.x & 31;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < qn; i += nwarps) {
-    const uint32_t v = __ldcg(q + i);
-    const double dv = bitsd(__ldcg(A.dist + v));
-    const uint32_t d = A.deg[v];
-    const uint64_t base = A.off[v];
-    if (lane == 0) edges += d;
-    for (uint32_t kb = 0; kb < d; kb += 128) {
-      const uint32_t k = kb + lane * 4;
-      uint32_t cc[4] = {kInvalidVid, kInvalidVid, kInvalidVid, kInvalidVid};
-      float ww[4] = {0.f, 0.f, 0.f, 0.f};
-      if (k < d) {
-        const uint4 c4 = *reinterpret_cast<const uint4*>(A.col + base + k);
-        const float4 w4 = *reinterpret_cast<const float4*>(A.w + base + k);
-        cc[0] = c4.x; cc[1] = k + 1 < d ? c4.y : kInvalidVid;
-        cc[2] = k + 2 < d ? c4.z : kInvalidVid; cc[3] = k + 3 < d ? c4.w : kInvalidVid;
-        ww[0] = w4.x; ww[1] = w4.y; ww[2] = w4.z; ww[3] = w4.w;
-      }
+  const uint32_t k = kb + lane * 4;
+  uint32_t cc[4] = {kInvalidVid, kInvalidVid, kInvalidVid, kInvalidVid};
+  float ww[4] = {0.f, 0.f, 0.f, 0.f};
+  if (k < d) {
+    const uint4 c4 = *reinterpret_cast<const uint4*>(A.col + base + k);
+    const float4 w4 = *reinterpret_cast<const float4*>(A.w + base + k);
+    cc[0] = c4.x; cc[1] = k + 1 < d ? c4.y : kInvalidVid;
+    cc[2] = k + 2 < d ? c4.z : kInvalidVid; cc[3] = k + 3 < d ? c4.w : kInvalidVid;
+    ww[0] = w4.x; ww[1] = w4.y; ww[2] = w4.z; ww[3] = w4.w;
+  }
 #pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        bool to_near = false, to_far = false;
-        const uint32_t x = cc[t];
-        if (x != kInvalidVid) {
-          const double nd = dv + (double)ww[t];
-          const unsigned long long nb = dbits(nd);
-          if (nb < A.dist[x]) {
-            const unsigned long long old = atomicMin(A.dist + x, nb);
-            if (nb < old) {
-              improve++;
-              note_change(A, x);
-              if (nd < thr) {
-                to_near = atomicExch(A.stamp + x, tag) != tag;
-              } else {
-                to_far = true;
-              }
-            }
+  for (int t = 0; t < 4; ++t) {
+    bool to_near = false, to_far = false;
+    const uint32_t x = cc[t];
+    if (x != kInvalidVid) {
+      const double nd = dv + (double)ww[t];
+      const unsigned long long nb = dbits(nd);
+      if (nb < A.dist[x]) {
+        const unsigned long long old = atomicMin(A.dist + x, nb);
+        if (nb < old) {
+          improve++;
+          note_change(A, x);
+          if (nd < thr) {
+            to_near = atomicExch(A.stamp + x, tag) != tag;
+          } else {
+            to_far = true;
           }
-        }
-        const uint32_t sn = warp_append(to_near, nq_cnt);
-        if (to_near) nq_next[sn] = x;
-        const uint32_t sf = warp_append(to_far, fq_cnt);
-        if (to_far) {
-          if (sf < A.fcap) fq[sf] = x; else atomicExch(A.ctl + S_ERR, 2u);
         }
       }
     }
+    const uint32_t sn = warp_append(to_near, nq_cnt);
+    if (to_near) nq_next[sn] = x;
+    const uint32_t sf = warp_append(to_far, fq_cnt);
+    if (to_far) {
+      if (sf < A.fcap) fq[sf] = x; else atomicExch(A.ctl + S_ERR, 2u);
+    }
+  }
+}
+
+// Relaxes the out-edges of every vertex in `q` (warp per vertex) and a
+// share of every long row deferred by the previous iteration (`hq`, `hn`:
+// all warps of the grid split each); long rows of `q` are deferred to
+// `hq_next` when the heavy slots are in use.
+__device__ __forceinline__ void relax_queue(const SsspArgs& A, const uint32_t* q, uint32_t qn,
+                                            const uint32_t* hq, uint32_t hn, uint32_t* hq_next,
+                                            uint32_t* hq_cnt, double thr, uint32_t* nq_next,
+                                            uint32_t* nq_cnt, uint32_t* fq, uint32_t* fq_cnt,
+                                            uint32_t tag, unsigned long long& edges,
+                                            unsigned long long& improve) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  for (uint32_t i = wid; i < qn; i += nwarps) {
+    const uint32_t v = __ldcg(q + i);
+    const uint32_t d = A.deg[v];
+    if (d > kHeavyRow && hq_next) {
+      bool deferred = false;
+      if (lane == 0) {
+        const uint32_t s = atomicAdd(hq_cnt, 1u);
+        deferred = s < A.hcap;
+        if (deferred) hq_next[s] = v;
+      }
+      if (__shfl_sync(0xffffffffu, deferred, 0)) continue;
+    }
+    const double dv = bitsd(__ldcg(A.dist + v));
+    const uint64_t base = A.off[v];
+    if (lane == 0) edges += d;
+    for (uint32_t kb = 0; kb < d; kb += 128)
+      relax_chunk(A, base, d, kb, dv, thr, nq_next, nq_cnt, fq, fq_cnt, tag, improve);
+  }
+  for (uint32_t h = 0; h < hn; ++h) {
+    const uint32_t v = __ldcg(hq + h);
+    const uint32_t d = A.deg[v];
+    const double dv = bitsd(__ldcg(A.dist + v));
+    const uint64_t base = A.off[v];
+    if (wid == 0 && lane == 0) edges += d;
+    for (uint64_t kb = (uint64_t)wid * 128; kb < d; kb += (uint64_t)nwarps * 128)
+      relax_chunk(A, base, d, (uint32_t)kb, dv, thr, nq_next, nq_cnt, fq, fq_cnt, tag, improve);
   }
 }
 
@@ -196,7 +235,8 @@ __global__ void __launch_bounds__(256) k_sssp_persistent(SsspArgs A) {
   for (;;) {
     const uint32_t rs = it % 3, ws = (it + 1) % 3, cs = (it + 2) % 3;
     const uint32_t qn = *(volatile uint32_t*)(A.ctl + S_Q0 + rs);
-    if (qn == 0) {
+    const uint32_t hn = A.hq[0] ? min(*(volatile uint32_t*)(A.ctl + S_H0 + rs), A.hcap) : 0u;
+    if (qn == 0 && hn == 0) {
       // bucket advance: smallest far distance decides the next window
       const uint32_t fn = *(volatile uint32_t*)(A.ctl + S_F0 + fslot);
       if (fn == 0) break;
@@ -262,11 +302,13 @@ __global__ void __launch_bounds__(256) k_sssp_persistent(SsspArgs A) {
     // read slot rs keeps its count until it becomes cs again.
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       A.ctl[S_Q0 + cs] = 0;
+      A.ctl[S_H0 + cs] = 0;
       A.ctl[S_ITERS] = it + 1;
       A.ctl[S_SPLITS] = seq + 1;
     }
-    relax_queue(A, A.nq[rs], qn, thr, A.nq[ws], A.ctl + S_Q0 + ws, A.fq[fslot],
-                A.ctl + S_F0 + fslot, A.iter_base + (++seq), edges, improve);
+    relax_queue(A, A.nq[rs], qn, A.hq[rs], hn, A.hq[ws], A.ctl + S_H0 + ws, thr, A.nq[ws],
+                A.ctl + S_Q0 + ws, A.fq[fslot], A.ctl + S_F0 + fslot, A.iter_base + (++seq),
+                edges, improve);
     if (!(ok = grid_sync(A))) break;
     ++it;
   }
@@ -847,6 +889,10 @@ static sg_status sssp_launch(sg_ctx* ctx, bool track) {
   A.iter_base = s.iter_base;
   A.fcap = s.far_cap;
   A.spin_limit = 40ll * 1000 * 1000;  // ~2-4 s of polling
+  // deferred long rows: three slots of the long-row buffer (free while the
+  // persistent kernel runs)
+  A.hcap = g.n / 3;
+  for (int i = 0; i < 3; ++i) A.hq[i] = A.hcap ? s.hv_list + (size_t)i * A.hcap : nullptr;
   A.chg_mark = track ? s.chg_mark : nullptr;
   A.chg_list = s.chg_list;
   A.chg_cnt = s.inc_ctl + 4;
@@ -913,6 +959,8 @@ sg_status sssp_run_view(sg_ctx* ctx, const SsspView& G, const uint32_t* h_seeds,
   A.iter_base = 1;
   A.fcap = fcap;
   A.spin_limit = 40ll * 1000 * 1000;
+  A.hq[0] = A.hq[1] = A.hq[2] = nullptr;  // one warp per row on this view
+  A.hcap = 0;
   A.chg_mark = nullptr;
   A.chg_list = nullptr;
   A.chg_cnt = nullptr;
