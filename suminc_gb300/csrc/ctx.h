@@ -141,6 +141,9 @@ struct SsspState {
   unsigned long long* d_cnt = nullptr;
   double* out = nullptr;          // staging for FP64 output
   uint32_t* padd_dst = nullptr;   // heads of edges added since the last run
+  uint32_t* padd_src = nullptr;   // their tails and weights
+  float* padd_w = nullptr;
+  uint32_t pending_batches = 0;   // batches applied since the last run
   uint64_t padd_cap = 0;
   uint64_t padd_bound = 0;        // host upper bound of the pending count
   uint32_t iter_base = 1;         // queue tags grow across launches

@@ -703,6 +703,42 @@ __global__ void k_sssp_reseed(const uint32_t* __restrict__ list, uint32_t cnt,
   }
 }
 
+// One batch since the last run: relax its new edges from their tails'
+// current distances.
+__global__ void k_sssp_relax_adds(const uint32_t* __restrict__ ps, const uint32_t* __restrict__ pd,
+                                  const float* __restrict__ pw, uint32_t cnt,
+                                  unsigned long long* __restrict__ dist, uint32_t* __restrict__ fq,
+                                  uint32_t* __restrict__ fq_cnt, uint32_t* chg_mark, uint32_t* chg_list,
+                                  uint32_t* chg_cnt, uint32_t chg_tag) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const unsigned long long du = dist[ps[i]];
+    if (du >= kInfBits) continue;
+    const uint32_t v = pd[i];
+    const unsigned long long nb = dbits(bitsd(du) + (double)pw[i]);
+    const unsigned long long old = atomicMin(dist + v, nb);
+    if (nb < old) {
+      fq[atomicAdd(fq_cnt, 1u)] = v;
+      if (chg_mark && atomicExch(chg_mark + v, chg_tag) != chg_tag)
+        chg_list[atomicAdd(chg_cnt, 1u)] = v;
+    }
+  }
+}
+
+// One batch since the last run: a new edge lowers the parent of its head
+// when the head's distance did not change and the edge is tight.
+__global__ void k_parent_adds(const uint32_t* __restrict__ ps, const uint32_t* __restrict__ pd,
+                              const float* __restrict__ pw, uint32_t cnt, uint32_t source,
+                              const unsigned long long* __restrict__ dist,
+                              const uint32_t* __restrict__ chg_mark, uint32_t tag,
+                              uint32_t* __restrict__ parent) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const uint32_t u = ps[i], v = pd[i];
+    const unsigned long long du = dist[u];
+    if (du >= kInfBits || v == source || chg_mark[v] == tag) continue;
+    if (dbits(bitsd(du) + (double)pw[i]) == dist[v]) atomicMin(parent + v, u);
+  }
+}
+
 __global__ void k_sssp_init(uint32_t n, unsigned long long* dist, uint32_t* stamp,
                             uint32_t* fstamp, uint32_t* reset) {
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
@@ -733,6 +769,8 @@ sg_status sssp_free(sg_ctx* ctx) {
   dfree(s.fstamp); dfree(s.seeds); dfree(s.seed_cnt); dfree(s.far);
   dfree(s.out);
   dfree(s.padd_dst);
+  dfree(s.padd_src);
+  dfree(s.padd_w);
   dfree(s.chg_mark); dfree(s.chg_list); dfree(s.par_mark); dfree(s.par_list); dfree(s.inc_ctl);
   dfree(s.hv_list); dfree(s.hv_best); dfree(s.hv_cnt); dfree(s.seed_mark);
   s = SsspState();
@@ -798,29 +836,39 @@ SsspAmendArgs sssp_amend_args(sg_ctx* ctx) {
     // first batch since the last run: empty seed list and pending adds
     cudaMemsetAsync(s.seed_cnt, 0, 4 * sizeof(uint32_t), ctx->stream);
     s.padd_bound = 0;
+    s.pending_batches = 0;
   }
-  if (s.valid) s.has_pending = true;
+  if (s.valid) {
+    s.has_pending = true;
+    s.pending_batches++;
+  }
   return a;
 }
 
-__global__ void k_collect_adds(const uint32_t* __restrict__ a_dst, const uint32_t* __restrict__ a_kind,
-                               uint64_t n_act, uint32_t* __restrict__ pd, uint32_t* __restrict__ cnt) {
+__global__ void k_collect_adds(const uint32_t* __restrict__ a_src, const uint32_t* __restrict__ a_dst,
+                               const float* __restrict__ a_w, const uint32_t* __restrict__ a_kind,
+                               uint64_t n_act, uint32_t* __restrict__ ps, uint32_t* __restrict__ pd,
+                               float* __restrict__ pw, uint32_t* __restrict__ cnt) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_act;
        i += (uint64_t)gridDim.x * blockDim.x) {
     if (!(a_kind[i] & 2u)) continue;
-    pd[atomicAdd(cnt, 1u)] = a_dst[i];
+    const uint32_t s = atomicAdd(cnt, 1u);
+    ps[s] = a_src[i];
+    pd[s] = a_dst[i];
+    pw[s] = a_w[i];
   }
 }
 
 // Called by the applier after the batch's actions are known: remembers the
-// heads of added (or re-weighted) edges for the next IncEval.  The
-// reference re-sends from every finite vertex after the reset
-// (sum_sync_traversal_worker.h:323-332); only these heads and the reset
-// vertices can get a shorter distance, so IncEval re-seeds them by a pull
-// over their in-edges in the graph as it is then.  Pulling (rather than
-// relaxing the recorded edges) stays exact when a later batch deletes or
-// re-weights an edge before the IncEval, and runs after the reset, so a
-// tail reset by the same batch lends no stale distance to its head.
+// added (or re-weighted) edges for the next IncEval.  The reference re-sends
+// from every finite vertex after the reset (sum_sync_traversal_worker.h:
+// 323-332); only these edges' heads and the reset vertices can get a
+// shorter distance.  When one batch separates the IncEval from the last
+// run, the recorded edges are exactly the graph's new edges and IncEval
+// relaxes them (after the reset, so a tail reset by the same batch lends no
+// stale distance); after several batches a later one may have deleted or
+// re-weighted a recorded edge, so IncEval re-seeds the heads by a pull over
+// their in-edges in the graph as it is then.
 sg_status sssp_collect_adds(sg_ctx* ctx) {
   SsspState& s = ctx->sp;
   const DevBatch& B = ctx->batch;
@@ -829,18 +877,27 @@ sg_status sssp_collect_adds(sg_ctx* ctx) {
   if (need > s.padd_cap) {
     // grow, keeping the pending entries
     const uint64_t ncap = std::max<uint64_t>(need * 2, 4096);
-    uint32_t* nd = nullptr;
+    uint32_t *nd = nullptr, *ns = nullptr;
+    float* nw = nullptr;
     SG_TRY(dalloc(ctx, &nd, ncap));
+    SG_TRY(dalloc(ctx, &ns, ncap));
+    SG_TRY(dalloc(ctx, &nw, ncap));
     if (s.padd_bound) {
       SG_CUDA(ctx, cudaMemcpyAsync(nd, s.padd_dst, 4 * s.padd_bound, cudaMemcpyDeviceToDevice, ctx->stream));
+      SG_CUDA(ctx, cudaMemcpyAsync(ns, s.padd_src, 4 * s.padd_bound, cudaMemcpyDeviceToDevice, ctx->stream));
+      SG_CUDA(ctx, cudaMemcpyAsync(nw, s.padd_w, 4 * s.padd_bound, cudaMemcpyDeviceToDevice, ctx->stream));
       SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
     dfree(s.padd_dst);
+    dfree(s.padd_src);
+    dfree(s.padd_w);
     s.padd_dst = nd;
+    s.padd_src = ns;
+    s.padd_w = nw;
     s.padd_cap = ncap;
   }
-  k_collect_adds<<<grid_for(B.n_act, 256), 256, 0, ctx->stream>>>(B.a_dst, B.a_kind, B.n_act,
-                                                                 s.padd_dst, s.seed_cnt + 2);
+  k_collect_adds<<<grid_for(B.n_act, 256), 256, 0, ctx->stream>>>(
+      B.a_src, B.a_dst, B.a_w, B.a_kind, B.n_act, s.padd_src, s.padd_dst, s.padd_w, s.seed_cnt + 2);
   SG_CUDA(ctx, cudaGetLastError());
   s.padd_bound = need;
   return SG_OK;
@@ -1151,8 +1208,17 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
     count_launch(ctx, 3);
     return SG_OK;
   };
+  // one batch: relax its new edges; several: pull their heads' in-rows
+  const bool one_batch = s.pending_batches == 1;
   if (total > 0) SG_TRY(reseed(s.seeds, total));
-  if (nadd > 0) SG_TRY(reseed(s.padd_dst, nadd));
+  if (nadd > 0 && one_batch) {
+    k_sssp_relax_adds<<<grid_for(nadd, 256), 256, 0, st>>>(
+        s.padd_src, s.padd_dst, s.padd_w, nadd, s.dist, s.far, s.d_ctl + S_F0, s.chg_mark,
+        s.chg_list, s.inc_ctl + 4, s.chg_tag);
+    count_launch(ctx);
+  } else if (nadd > 0) {
+    SG_TRY(reseed(s.padd_dst, nadd));
+  }
   SG_CUDA(ctx, cudaGetLastError());
   // 3. delta-stepping from the seeds, listing every improved vertex
   SG_TRY(sssp_launch(ctx, true));
@@ -1165,9 +1231,12 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
     // (a) + (b) in full, long in-rows by every CTA; then (c) by a push
     SG_CUDA(ctx, cudaMemsetAsync(s.inc_ctl + 5, 0, 4, st));
     SG_CUDA(ctx, cudaMemsetAsync(s.hv_cnt, 0, 4, st));
-    k_parent_list<<<grid_for(nchg + nadd, 256), 256, 0, st>>>(s.chg_list, nchg, s.padd_dst, nadd,
-                                                              s.par_mark, s.chg_tag, s.par_list,
-                                                              s.inc_ctl + 5);
+    // heads of new edges in full only after several batches (with one, the
+    // new edges themselves are checked below)
+    const uint32_t nheads = one_batch ? 0u : nadd;
+    k_parent_list<<<grid_for(nchg + nheads, 256), 256, 0, st>>>(s.chg_list, nchg, s.padd_dst,
+                                                                nheads, s.par_mark, s.chg_tag,
+                                                                s.par_list, s.inc_ctl + 5);
     k_sssp_parents_list<<<ctx->num_sms * 8, 256, 0, st>>>(s.par_list, s.inc_ctl + 5, s.source,
                                                           g.in.off, g.in.deg, g.in.col, g.in.w,
                                                           s.dist, s.parent, H);
@@ -1184,6 +1253,12 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
                                                       g.out.w, s.dist, s.chg_mark, s.chg_tag,
                                                       s.parent);
       count_launch(ctx, 2);
+    }
+    if (one_batch && nadd > 0) {
+      k_parent_adds<<<grid_for(nadd, 256), 256, 0, st>>>(s.padd_src, s.padd_dst, s.padd_w, nadd,
+                                                         s.source, s.dist, s.chg_mark, s.chg_tag,
+                                                         s.parent);
+      count_launch(ctx);
     }
   }
   SG_CUDA(ctx, cudaGetLastError());
