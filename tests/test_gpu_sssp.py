@@ -128,3 +128,62 @@ def test_grid_barrier_wait_runs_out_and_context_survives(ctx):
     assert np.array_equal(ctx.sssp_peval(0), oracle.dijkstra(rp, col, w, 0))
     x = ctx.pr_peval()
     assert np.abs(x - oracle.pr_fixed_point(rp, col)).sum() <= 1e-5
+
+
+def _hub_graph(n=40000, deg=6, hubs=(0, 7, 11), hub_deg=12000, seed=5):
+    """A sparse random graph plus a few hubs with long out- and in-rows
+    (longer than one warp takes: rows are split over the grid above 4,096
+    entries); integer weights in [1, 100]."""
+    rng = np.random.default_rng(seed)
+    src = [np.repeat(np.arange(n), deg)]
+    dst = [rng.integers(0, n, n * deg)]
+    for h in hubs:
+        src += [np.full(hub_deg, h), rng.integers(0, n, hub_deg)]
+        dst += [rng.integers(0, n, hub_deg), np.full(hub_deg, h)]
+    src, dst = np.concatenate(src), np.concatenate(dst)
+    keep = src != dst
+    key = np.unique(src[keep].astype(np.int64) * n + dst[keep])
+    s, d = key // n, key % n
+    rp = np.concatenate([[0], np.cumsum(np.bincount(s, minlength=n))]).astype(np.uint64)
+    w = (1 + (s * 2654435761 + d * 40503) % 100).astype(np.float32)
+    return rp, d.astype(np.uint32), w
+
+
+def _drop_edges(rp, col, w, pairs):
+    n = len(rp) - 1
+    src = np.repeat(np.arange(n), np.diff(rp).astype(np.int64))
+    key = src.astype(np.int64) * n + col
+    keep = ~np.isin(key, [u * n + v for u, v in pairs])
+    rp2 = np.concatenate([[0], np.cumsum(np.bincount(src[keep], minlength=n))]).astype(np.uint64)
+    return rp2, col[keep], w[keep]
+
+
+@pytest.mark.parametrize("batches_per_inceval", [1, 2])
+def test_inceval_with_long_rows(ctx, batches_per_inceval):
+    """Hubs whose rows are split over the grid (reset BFS, re-seed pulls,
+    parent pulls, the persistent kernel's deferred rows): the first batch
+    deletes the hubs' tree edges so their subtrees reset and their long
+    in-rows are pulled; IncEval after one batch (new edges relaxed directly)
+    and after two (heads pulled) stays bit-exact with min-tight parents."""
+    rp, col, w = _hub_graph()
+    ctx.load_csr(rp, col, w)
+    d = ctx.sssp_peval(0)
+    assert np.array_equal(d, oracle.dijkstra(rp, col, w, 0))
+    par = ctx.sssp_parents()
+    assert np.array_equal(par, _min_tight_parents(rp, col, w, d, 0))
+    cut = [(int(par[h]), h) for h in (7, 11)]
+    forced = np.array([(u, v, 0.0, 1) for u, v in cut], sg.UPDATE_DTYPE)
+    rp, col, w = _drop_edges(rp, col, w, cut)
+    hg = sg.HostGraph(rp, col, w)
+    for b in range(3):
+        for k in range(batches_per_inceval):
+            upd = hg.gen_updates(1500, 1500, 500, seed=100 + 10 * b + k)
+            if b == 0 and k == 0:
+                upd = np.concatenate([forced, upd])
+            ctx.apply_updates(upd)
+        d = ctx.sssp_inceval()
+        nrp, ncol, nw = hg.csr()
+        assert np.array_equal(d, oracle.dijkstra(nrp, ncol, nw, 0)), b
+        assert np.array_equal(ctx.sssp_parents(), _min_tight_parents(nrp, ncol, nw, d, 0))
+        if b == 0:
+            assert ctx.stats()["reset_vertices"] > 1000
