@@ -52,6 +52,9 @@ typedef struct sg_update {
 
 /* Runtime options; the fields mirror the reference's gflags
  * (examples/analytical_apps/flags.cc:28-70). */
+/* sg_options.message_type */
+enum { SG_MSG_PUSH = 0, SG_MSG_PULL = 1 };
+
 typedef struct sg_options {
   double damping;             /* PageRankIngress::d (pagerank_ingress.h:23) */
   double termcheck_threshold; /* FLAGS_termcheck_threshold: stop when the L1
@@ -71,7 +74,13 @@ typedef struct sg_options {
                                  each pull CTA keeps in shared memory: 0 =
                                  automatic (up to 12,288), -1 = none, k > 0 =
                                  at most min(k, 16,384)                     */
-  int32_t reserved[7];
+  int32_t message_type;       /* FLAGS_message_type for PageRank: 0 = push
+                                 (SumSyncIterWorker / IngressSyncIterWorker),
+                                 1 = pull (SumSyncIterWorkerPull: synchronous
+                                 in-neighbour rounds, Σ|x - x_prev| stop
+                                 test, 200-step cap; with compress = 1 the
+                                 summary must have no mirrors)              */
+  int32_t reserved[6];
 } sg_options;
 
 /* Counters of the last PEval / IncEval / batch call. */

@@ -4,7 +4,8 @@
 // (examples/analytical_apps/ingress.h:71-177), and writes the per-vertex
 // results as little-endian float64 to --out.
 //
-// usage: ref_driver <pagerank|pagerank_plain|sssp|sssp_plain> <out.bin> flag=value ...
+// usage: ref_driver <pagerank|pagerank_pull|pagerank_plain|sssp|sssp_plain> <out.bin> flag=value ...
+// (pagerank_pull runs SumSyncIterWorkerPull, the message_type=pull worker)
 //        (flags as in examples/analytical_apps/flags.cc)
 #include <gflags/gflags.h>
 #include <glog/logging.h>
@@ -24,6 +25,7 @@
 #include "grape/grape.h"
 #include "grape/worker/ingress_sync_iter_worker.h"
 #include "grape/worker/sum_sync_iter_worker.h"
+#include "grape/worker/sum_sync_iter_worker_pull.h"
 #include "grape/worker/ingress_sync_traversal_worker.h"
 #include "grape/worker/sum_sync_traversal_worker.h"
 #include "pagerank/pagerank_ingress.h"
@@ -103,7 +105,7 @@ int main(int argc, char** argv) {
       pe.thread_num = FLAGS_app_concurrency;
       setWorkers(FLAGS_app_concurrency);
     }
-    if (app == "pagerank" || app == "pagerank_plain") {
+    if (app == "pagerank" || app == "pagerank_pull" || app == "pagerank_plain") {
       using G = grape::ImmutableEdgecutFragment<int32_t, uint32_t, grape::EmptyType,
                                                 grape::EmptyType, grape::LoadStrategy::kBothOutIn>;
       using A = PR<G, float>;
@@ -112,6 +114,11 @@ int main(int argc, char** argv) {
       auto a = std::make_shared<A>();
       if (app == "pagerank") {
         grape::SumSyncIterWorker<A> w(a, frag);
+        w.Init(cs, pe);
+        w.Query();
+        w.Finalize();
+      } else if (app == "pagerank_pull") {
+        grape::SumSyncIterWorkerPull<A> w(a, frag);
         w.Init(cs, pe);
         w.Query();
         w.Finalize();

@@ -40,6 +40,9 @@ SG_ERR_NOT_CONVERGED = 5
 SG_ERR_TIMEOUT = 6
 SG_ERR_UNSUPPORTED = 7
 SG_ERR_TOO_LARGE = 8
+
+SG_MSG_PUSH = 0
+SG_MSG_PULL = 1
 PR_NOALLOC_MAX_VERTICES = 1 << 22
 
 SG_UPD_ADD = 0
@@ -65,7 +68,8 @@ class Options(C.Structure):
         ("slack", C.c_double),
         ("adjoint_rel_tol", C.c_double),
         ("pull_hubs", C.c_int32),
-        ("reserved", C.c_int32 * 7),
+        ("message_type", C.c_int32),
+        ("reserved", C.c_int32 * 6),
     ]
 
 

@@ -120,7 +120,8 @@ sg_status sg_ctx_create(int device, const sg_options* opt, sg_ctx** out) {
     return SG_ERR_OOM;
   }
   if (opt) ctx->opt = *opt; else sg_options_default(&ctx->opt);
-  if (!(ctx->opt.damping > 0.0 && ctx->opt.damping < 1.0) || !(ctx->opt.termcheck_threshold > 0.0)) {
+  if (!(ctx->opt.damping > 0.0 && ctx->opt.damping < 1.0) || !(ctx->opt.termcheck_threshold > 0.0) ||
+      (ctx->opt.message_type != SG_MSG_PUSH && ctx->opt.message_type != SG_MSG_PULL)) {
     delete ctx;
     return SG_ERR_INVALID;
   }
@@ -152,6 +153,7 @@ sg_status sg_ctx_destroy(sg_ctx* ctx) {
   summary_free(ctx);
   batch_free(ctx);
   adjoint_free(ctx);
+  pull_free(ctx);
   graph_free(ctx);
   DevBatch& B = ctx->batch;
   dfree(B.raw); dfree(B.key); dfree(B.key2); dfree(B.val); dfree(B.val2);
@@ -247,6 +249,7 @@ sg_status sg_graph_load_csr(sg_ctx* ctx, uint32_t n, const uint64_t* row_ptr,
     summary_free(ctx);
     batch_free(ctx);
     adjoint_free(ctx);
+    pull_free(ctx);
     ctx->oids.clear();
     return load_csr(ctx, n, row_ptr, col, w);
   }
@@ -266,6 +269,7 @@ sg_status sg_graph_generate_rmat(sg_ctx* ctx, int scale, uint64_t edges, double 
     summary_free(ctx);
     batch_free(ctx);
     adjoint_free(ctx);
+    pull_free(ctx);
     ctx->oids.clear();
     return generate_rmat(ctx, scale, edges, a, b, c, seed, weight_kind, wlo, whi);
   }
@@ -327,7 +331,8 @@ sg_status sg_pr_peval(sg_ctx* ctx, float* out) {
     ctx->pr.valid = false;
     sg_status st = pr_alloc(ctx);
     if (st != SG_OK) return st;
-    if (ctx->opt.compress) st = pr_summarized(ctx, false);
+    if (ctx->opt.message_type == SG_MSG_PULL) st = pr_pull_worker(ctx, false);
+    else if (ctx->opt.compress) st = pr_summarized(ctx, false);
     else st = pr_run(ctx, false);
     kprof_flush(ctx);
     if (st != SG_OK && st != SG_ERR_NOT_CONVERGED) return st;
@@ -340,7 +345,9 @@ sg_status sg_pr_peval(sg_ctx* ctx, float* out) {
 sg_status sg_pr_inceval(sg_ctx* ctx, float* out) {
   SG_GUARD(ctx);
   try {
-    sg_status st = ctx->opt.compress ? pr_summarized(ctx, true) : pr_run(ctx, true);
+    sg_status st = ctx->opt.message_type == SG_MSG_PULL ? pr_pull_worker(ctx, true)
+                   : ctx->opt.compress                   ? pr_summarized(ctx, true)
+                                                         : pr_run(ctx, true);
     kprof_flush(ctx);
     if (st != SG_OK && st != SG_ERR_NOT_CONVERGED) return st;
     sg_status c = copy_out_f32(ctx, ctx->pr.x, out);
@@ -576,6 +583,7 @@ sg_status sg_graph_load_files(sg_ctx* ctx, const char* efile, const char* vfile,
     summary_free(ctx);
     batch_free(ctx);
     adjoint_free(ctx);
+    pull_free(ctx);
     ctx->oids.clear();
     return load_files(ctx, efile, vfile, weighted != 0);
   }

@@ -197,6 +197,7 @@ struct sg_ctx {
   void* summary = nullptr;  // summary.cu: summarized graph (compress = 1)
   void* batch_state = nullptr;  // batch.cu: batched PPR / SSSP queries
   void* adjoint_state = nullptr;  // adjoint.cu: weighted PageRank + adjoint
+  void* pull_state = nullptr;     // pull.cu: PageRank with message_type = pull
   std::vector<uint64_t> oids;     // io.cpp: vid -> oid when loaded from files (empty: identity)
 };
 
@@ -365,6 +366,30 @@ sg_status summary_after_apply(sg_ctx* ctx);
 sg_status summary_build_serialized(sg_ctx* ctx, const std::vector<uint8_t>& blob);
 sg_status summary_serialized(sg_ctx* ctx, std::vector<uint8_t>* blob);
 sg_status pr_summarized(sg_ctx* ctx, bool inc);
+
+// SumSyncIterWorkerPull's per-vertex in-indexes over the summary, on the
+// device (built on first use after each summary change).  Vertex classes: 0
+// out node, 1 exit only, 2 entry only, 3 entry and exit, 4 inner member.
+struct PullView {
+  uint32_t n = 0;
+  const uint8_t* cls = nullptr;
+  const uint64_t* ie_off = nullptr;  // classes 2, 3: in-edges from other clusters
+  const uint32_t* ie_nbr = nullptr;
+  const uint64_t* iv_off = nullptr;  // bound_delta + inner_value shortcuts ending here
+  const uint32_t* iv_src = nullptr;  // (the supernode's entry)
+  const float* iv_w = nullptr;
+  const uint64_t* id_off = nullptr;  // inner_delta shortcuts ending here
+  const uint32_t* id_src = nullptr;
+  const float* id_w = nullptr;
+  uint64_t round_edges = 0;  // entries one summarized round reads
+  uint64_t round_shortcuts = 0;  // of which shortcut (value index) entries
+  uint64_t corr_entries = 0;
+};
+sg_status summary_pull_view(sg_ctx* ctx, PullView* out);
+
+// pull.cu: PageRank with message_type = pull
+sg_status pr_pull_worker(sg_ctx* ctx, bool inc);
+sg_status pull_free(sg_ctx* ctx);
 sg_status sssp_summarized(sg_ctx* ctx, uint32_t source);
 uint32_t summary_rows(sg_ctx* ctx);  // rows incl. mirrors, 0 without a summary
 sg_status summary_info(sg_ctx* ctx, sg_summary_info* out);

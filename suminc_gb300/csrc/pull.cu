@@ -1,0 +1,433 @@
+// PageRank with message_type = pull (SumSyncIterWorkerPull,
+// grape/worker/sum_sync_iter_worker_pull.h; pull functions
+// pagerank_ingress.h:210-310): synchronous rounds in which every vertex
+// gathers from its in-neighbours the values they published the round
+// before, so no round writes another vertex's state and no atomics are
+// needed.
+//
+//   init             last_values = x; with a summary, per vertex class (out
+//                    node: x += delta; exit / inner: delta parked for the
+//                    correction; entry: delta handed to its supernode)
+//                    (:510-535, :1343-1360)
+//   summarized round out nodes gather along all in-edges, entries along
+//                    in-edges from other clusters into their supernode's
+//                    index value, exits gather the entries' index values
+//                    through the shortcut weights (:757-980)
+//   correction       parked deltas return, inner vertices take their value
+//                    and delta shares of the accumulated entry mass
+//                    (:1045-1131)
+//   plain round      every vertex gathers along all in-edges (:600-630)
+//   stop test        sum |last_values - x| < termcheck_threshold, or the
+//                    step counter passes 200 (:1044, termCheck :1430-1462)
+//
+// One group of 8 lanes per vertex; the published values of a round live in
+// two buffers used by round parity (last_deltas_ / last_index_values_).  The
+// residual is summed in FP64 per block and by the last block to finish, which
+// also takes the stop decision; kernels of a chunk launched after the
+// decision return at once, so the host reads the control words once per
+// chunk.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "ctx.h"
+#include "dev.cuh"
+
+namespace sg {
+
+namespace {
+
+constexpr int kPT = 256;         // threads per block
+constexpr int kPG = 8;           // lanes per vertex
+constexpr int kGroupsPerWarp = 32 / kPG;
+constexpr int kStepCap = 200;    // `step > 200` (sum_sync_iter_worker_pull.h:1044)
+constexpr int kChunk = 8;        // rounds launched per host check
+
+// control words: [0] stop, [1] blocks finished, [2] rounds of the stage,
+// [3] residual test passed
+enum { P_STOP = 0, P_DONE_BLOCKS = 1, P_ROUNDS = 2, P_PASSED = 3, P_WORDS = 4 };
+
+struct PullState {
+  uint32_t n_alloc = 0;
+  float* ld = nullptr;     // published d*delta/outdeg, 2n (round parity)
+  float* li = nullptr;     // published supernode index values, 2n
+  float* lastx = nullptr;  // last_values
+  float* spd = nullptr;    // spnode_datas
+  float* bsave = nullptr;  // bound_deltas
+  double* part = nullptr;  // per-block residual sums
+  double* res = nullptr;   // last residual
+  uint32_t* ctl = nullptr;
+  uint32_t nblocks = 0;
+};
+
+PullState* pstate(sg_ctx* ctx) { return (PullState*)ctx->pull_state; }
+
+void pfree_arrays(PullState& P) {
+  dfree(P.ld); dfree(P.li); dfree(P.lastx); dfree(P.spd); dfree(P.bsave);
+  dfree(P.part); dfree(P.res); dfree(P.ctl);
+}
+
+struct PullArgs {
+  uint32_t n;
+  float d;
+  double tau;
+  const uint64_t* in_off;  // graph in-CSR segments
+  const uint32_t* in_deg;
+  const uint32_t* in_col;
+  const uint32_t* outdeg;
+  PullView V;              // summary in-indexes (cls null: no summary)
+  float* x;
+  float* delta;
+  float* ld;
+  float* li;
+  float* lastx;
+  float* spd;
+  float* bsave;
+  double* part;
+  double* res;
+  uint32_t* ctl;
+};
+
+__device__ __forceinline__ float group_sum(float v) {
+#pragma unroll
+  for (int o = kPG / 2; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, kPG);
+  return v;
+}
+
+__device__ __forceinline__ float publish(float dl, uint32_t od, float d) {
+  return od ? dl * d / (float)od : 0.f;
+}
+
+// Block sum of `r`, then the last block to finish sums the block partials in
+// a fixed order and decides whether the stage stops.
+__device__ void residual_and_decide(const PullArgs& A, double r, int step_base) {
+  __shared__ double s_w[kPT / 32];
+  __shared__ bool s_last;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+  if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = r;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int i = 0; i < kPT / 32; ++i) t += s_w[i];
+    A.part[blockIdx.x] = t;
+    __threadfence();
+    s_last = atomicAdd(&A.ctl[P_DONE_BLOCKS], 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  double t = 0;
+  for (uint32_t i = threadIdx.x; i < gridDim.x; i += kPT) t += ((volatile double*)A.part)[i];
+#pragma unroll
+  for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0;
+    for (int i = 0; i < kPT / 32; ++i) tot += s_w[i];
+    const uint32_t step = A.ctl[P_ROUNDS] + 1;
+    A.ctl[P_ROUNDS] = step;
+    *A.res = tot;
+    const bool passed = tot < A.tau;
+    A.ctl[P_PASSED] = passed ? 1u : 0u;
+    if (passed || step_base + (int)step > kStepCap) A.ctl[P_STOP] = 1u;
+    A.ctl[P_DONE_BLOCKS] = 0u;
+  }
+}
+
+// init: last_values = x, then the class rules (COMP) or x += delta for all.
+template <bool COMP>
+__global__ void __launch_bounds__(kPT) k_pull_init(PullArgs A) {
+  for (uint32_t v = blockIdx.x * kPT + threadIdx.x; v < A.n; v += gridDim.x * kPT) {
+    float x = A.x[v], dl = A.delta[v];
+    A.lastx[v] = x;
+    const uint32_t t = COMP ? A.V.cls[v] : 0u;
+    float nd = 0.f, nl = 0.f;
+    if (t == 0) {
+      x += dl;
+      nd = dl;
+    } else if (t == 1 || t == 4) {
+      A.bsave[v] = dl;
+      dl = 0.f;
+    } else {  // 2, 3: the delta becomes the supernode's index value
+      nl = dl;
+      dl = 0.f;
+    }
+    A.x[v] = x;
+    A.delta[v] = dl;
+    A.ld[v] = publish(nd, A.outdeg[v], A.d);
+    if (COMP) {
+      A.li[v] = nl;
+      A.spd[v] = nl;
+    }
+  }
+}
+
+// One round.  COMP: the summarized round by vertex class; else every vertex
+// is an out node (plain round).
+template <bool COMP>
+__global__ void __launch_bounds__(kPT) k_pull_round(PullArgs A, int parity, int step_base) {
+  if (((volatile uint32_t*)A.ctl)[P_STOP]) return;
+  const float* __restrict__ ldi = A.ld + (size_t)parity * A.n;
+  float* __restrict__ ldo = A.ld + (size_t)(parity ^ 1) * A.n;
+  const float* __restrict__ lii = A.li + (size_t)parity * A.n;
+  float* __restrict__ lio = A.li + (size_t)(parity ^ 1) * A.n;
+  const uint32_t lane = threadIdx.x & (kPG - 1);
+  const uint64_t warp = ((uint64_t)blockIdx.x * kPT + threadIdx.x) >> 5;
+  const uint64_t nwarps = (uint64_t)gridDim.x * (kPT / 32);
+  const uint32_t gw = (threadIdx.x & 31) / kPG;
+  double r = 0;
+  // every lane of a warp runs the same trip count (the group sums shuffle
+  // across the whole warp)
+  for (uint64_t base = warp * kGroupsPerWarp; base < A.n; base += nwarps * kGroupsPerWarp) {
+    const uint64_t v64 = base + gw;
+    const bool act = v64 < A.n;
+    const uint32_t v = act ? (uint32_t)v64 : 0u;
+    const uint32_t t = (COMP && act) ? A.V.cls[v] : 0u;
+    float a = 0.f, b = 0.f;
+    if (act) {
+      if (t == 0) {
+        const uint64_t o = A.in_off[v];
+        const uint32_t dg = A.in_deg[v];
+        for (uint32_t e = lane; e < dg; e += kPG) a += ldi[A.in_col[o + e]];
+      } else if (t == 2 || t == 3) {
+        for (uint64_t e = A.V.ie_off[v] + lane; e < A.V.ie_off[v + 1]; e += kPG)
+          a += ldi[A.V.ie_nbr[e]];
+      }
+      if (COMP && (t == 1 || t == 3)) {
+        for (uint64_t e = A.V.iv_off[v] + lane; e < A.V.iv_off[v + 1]; e += kPG)
+          b += lii[A.V.iv_src[e]] * A.V.iv_w[e];
+      }
+    }
+    a = group_sum(a);
+    if (COMP) b = group_sum(b);
+    if (act && lane == 0) {
+      float x = A.x[v];
+      float nd = 0.f, nl = 0.f;
+      if (t == 0) {
+        x += a;
+        A.delta[v] = a;
+        nd = a;
+      } else if (t == 1) {
+        x += b;
+        A.delta[v] = b;
+        nd = b;
+      } else if (t == 2) {
+        A.spd[v] += a;
+        nl = a;
+      } else if (t == 3) {
+        A.spd[v] += a;
+        nl = a;
+        x += b;
+        A.delta[v] = b;
+        nd = b;
+      }
+      ldo[v] = publish(nd, A.outdeg[v], A.d);
+      if (COMP) lio[v] = nl;
+      A.x[v] = x;
+      r += fabs((double)A.lastx[v] - (double)x);
+      A.lastx[v] = x;
+    }
+  }
+  residual_and_decide(A, r, step_base);
+}
+
+// Correction after the summarized rounds; publishes d*delta/outdeg for the
+// first plain round into ld[0].
+__global__ void __launch_bounds__(kPT) k_pull_correct(PullArgs A) {
+  const uint32_t lane = threadIdx.x & (kPG - 1);
+  const uint64_t warp = ((uint64_t)blockIdx.x * kPT + threadIdx.x) >> 5;
+  const uint64_t nwarps = (uint64_t)gridDim.x * (kPT / 32);
+  const uint32_t gw = (threadIdx.x & 31) / kPG;
+  for (uint64_t base = warp * kGroupsPerWarp; base < A.n; base += nwarps * kGroupsPerWarp) {
+    const uint64_t v64 = base + gw;
+    const bool act = v64 < A.n;
+    const uint32_t v = act ? (uint32_t)v64 : 0u;
+    const uint32_t t = act ? A.V.cls[v] : 0u;
+    float bv = 0.f, bd = 0.f;
+    if (act && (t == 2 || t == 4))
+      for (uint64_t e = A.V.iv_off[v] + lane; e < A.V.iv_off[v + 1]; e += kPG)
+        bv += A.spd[A.V.iv_src[e]] * A.V.iv_w[e];
+    if (act && t >= 1)
+      for (uint64_t e = A.V.id_off[v] + lane; e < A.V.id_off[v + 1]; e += kPG)
+        bd += A.spd[A.V.id_src[e]] * A.V.id_w[e];
+    bv = group_sum(bv);
+    bd = group_sum(bd);
+    if (act && lane == 0) {
+      float x = A.x[v], dl = A.delta[v];
+      if (t == 1 || t == 4) {
+        dl = A.bsave[v];
+        x += dl;
+      }
+      if (t == 2 || t == 4) x += bv;
+      if (t >= 1) {
+        x += bd;
+        dl += bd;
+      }
+      A.x[v] = x;
+      A.delta[v] = dl;
+      A.ld[v] = publish(dl, A.outdeg[v], A.d);
+    }
+  }
+}
+
+// The worker's values include the delta each vertex gathered last (x +=
+// delta on arrival); the library's state keeps x without the pending delta
+// (the push workers' convention, which AmendValue and IncEval build on).
+__global__ void k_pull_finish(uint32_t n, float* x, const float* delta) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    x[v] -= delta[v];
+}
+
+__global__ void k_pull_start(uint32_t n, float* x, float* delta, float init_c) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    x[v] = 0.f;
+    delta[v] = init_c;
+  }
+}
+
+sg_status preserve(sg_ctx* ctx, uint32_t n) {
+  if (!ctx->pull_state) ctx->pull_state = new PullState();
+  PullState& P = *pstate(ctx);
+  if (P.n_alloc == n && P.ld) return SG_OK;
+  pfree_arrays(P);
+  P = PullState();
+  P.nblocks = (uint32_t)ctx->num_sms * 8;
+  SG_TRY(dalloc(ctx, &P.ld, 2ull * n));
+  SG_TRY(dalloc(ctx, &P.li, 2ull * n));
+  SG_TRY(dalloc(ctx, &P.lastx, n));
+  SG_TRY(dalloc(ctx, &P.spd, n));
+  SG_TRY(dalloc(ctx, &P.bsave, n));
+  SG_TRY(dalloc(ctx, &P.part, P.nblocks));
+  SG_TRY(dalloc(ctx, &P.res, 1));
+  SG_TRY(dalloc(ctx, &P.ctl, P_WORDS));
+  P.n_alloc = n;
+  return SG_OK;
+}
+
+// Rounds of one stage until the stop word is set; returns the rounds run and
+// whether the residual test passed.
+template <bool COMP>
+sg_status stage(sg_ctx* ctx, const PullArgs& A, int step_base, int klass, uint32_t* rounds,
+                bool* passed) {
+  cudaStream_t st = ctx->stream;
+  const PullState& P = *pstate(ctx);
+  SG_CUDA(ctx, cudaMemsetAsync(A.ctl, 0, sizeof(uint32_t) * P_WORDS, st));
+  uint32_t h[P_WORDS] = {0, 0, 0, 0};
+  int launched = 0;
+  const int cap = kStepCap + 2;
+  while (launched < cap) {
+    kprof_begin(ctx);
+    int c = 0;
+    for (; c < kChunk && launched < cap; ++c, ++launched)
+      k_pull_round<COMP><<<P.nblocks, kPT, 0, st>>>(A, launched & 1, step_base);
+    kprof_end(ctx, klass);
+    count_launch(ctx, c);
+    SG_CUDA(ctx, cudaGetLastError());
+    SG_CUDA(ctx, cudaMemcpyAsync(h, A.ctl, sizeof(h), cudaMemcpyDeviceToHost, st));
+    SG_CUDA(ctx, cudaStreamSynchronize(st));
+    if (h[P_STOP]) break;
+  }
+  *rounds = h[P_ROUNDS];
+  *passed = h[P_PASSED] != 0;
+  return SG_OK;
+}
+
+}  // namespace
+
+sg_status pull_free(sg_ctx* ctx) {
+  PullState* P = pstate(ctx);
+  if (P) {
+    pfree_arrays(*P);
+    delete P;
+  }
+  ctx->pull_state = nullptr;
+  return SG_OK;
+}
+
+// PEval (inc = false: x = 0, delta = (1-d)/N) or IncEval (the amended state)
+// of the pull worker.  With compress = 1 the summarized stage, the
+// correction and then the plain stage run (Query's batch / inc stages,
+// sum_sync_iter_worker_pull.h:243-1400); with compress = 0 only the plain
+// stage.
+sg_status pr_pull_worker(sg_ctx* ctx, bool inc) {
+  DevGraph& g = ctx->g;
+  PrState& s = ctx->pr;
+  if (!g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
+  const bool comp = ctx->opt.compress != 0;
+  PullView V;
+  if (comp) SG_TRY(summary_pull_view(ctx, &V));
+  if (inc && !s.valid) return fail(ctx, SG_ERR_STATE, "PageRank IncEval before PEval");
+  if (!s.x) SG_TRY(pr_alloc(ctx));
+  const uint32_t n = g.n;
+  SG_TRY(preserve(ctx, n));
+  PullState& P = *pstate(ctx);
+  cudaStream_t st = ctx->stream;
+  PullArgs A;
+  A.n = n;
+  A.d = (float)ctx->opt.damping;
+  A.tau = ctx->opt.termcheck_threshold;
+  A.in_off = g.in.off;
+  A.in_deg = g.in.deg;
+  A.in_col = g.in.col;
+  A.outdeg = g.out.deg;
+  A.V = V;
+  A.x = s.x;
+  A.delta = s.delta;
+  A.ld = P.ld;
+  A.li = P.li;
+  A.lastx = P.lastx;
+  A.spd = P.spd;
+  A.bsave = P.bsave;
+  A.part = P.part;
+  A.res = P.res;
+  A.ctl = P.ctl;
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+  const unsigned vb = grid_for(n, kPT);
+  if (!inc) {
+    k_pull_start<<<vb, kPT, 0, st>>>(n, s.x, s.delta,
+                                     (float)((1.0 - ctx->opt.damping) / (double)n));
+    count_launch(ctx);
+  }
+  uint32_t rc = 0, rp = 0;
+  bool passed = false;
+  if (comp) {
+    k_pull_init<true><<<vb, kPT, 0, st>>>(A);
+    count_launch(ctx);
+    SG_TRY(stage<true>(ctx, A, 0, SG_K_SUMMARY, &rc, &passed));
+    k_pull_correct<<<P.nblocks, kPT, 0, st>>>(A);
+    count_launch(ctx);
+    // `continue` skips ++step: the first plain round repeats the last step
+    SG_TRY(stage<false>(ctx, A, (int)rc - 1, SG_K_PR_PULL, &rp, &passed));
+  } else {
+    k_pull_init<false><<<vb, kPT, 0, st>>>(A);
+    count_launch(ctx);
+    SG_TRY(stage<false>(ctx, A, 0, SG_K_PR_PULL, &rp, &passed));
+  }
+  k_pull_finish<<<vb, kPT, 0, st>>>(n, s.x, s.delta);
+  count_launch(ctx);
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
+  double res = 0;
+  SG_CUDA(ctx, cudaMemcpyAsync(&res, P.res, sizeof(double), cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  s.valid = true;
+  sg_stats& S = ctx->stats;
+  S.rounds = (int32_t)(rc + rp);
+  S.converged = passed ? 1 : 0;
+  S.residual = res;
+  S.shortcut_edges = (uint64_t)rc * V.round_shortcuts;
+  S.edges_relaxed = (uint64_t)rc * V.round_edges + (comp ? V.corr_entries : 0) + (uint64_t)rp * g.m;
+  S.edges_pull = S.edges_relaxed;
+  S.edges_push = 0;
+  S.vertex_visits = (uint64_t)(rc + rp) * n;
+  S.elapsed_ms = ms;
+  S.live_edges = g.m;
+  if (!passed) return fail(ctx, SG_ERR_NOT_CONVERGED, "pull PageRank reached the 200-step cap");
+  return SG_OK;
+}
+
+}  // namespace sg

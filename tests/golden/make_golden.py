@@ -19,6 +19,14 @@ Each case writes <case>.npz with:
                 summary (node types, supernodes, mirrors, sketch edges)
   ref_serialized_summary  the bytes of the reference's serialize_cluster file
                 (written with serialization_cmp_prefix)
+
+    python tests/golden/make_golden.py --pull
+runs the message_type=pull worker (SumSyncIterWorkerPull) on the inputs of
+the cases above, with mirror_k large enough that no mirror is made, and
+writes pull_pr.npz: params (flags), <case>_input_sha256 and
+<case>_ref_pr_pull_peval.  Its IncEval is not recorded: with an update file
+the reference's pull worker stops with a segmentation fault inside
+inc_run (after inc_compute_index_mirror_spid) on both cases.
 """
 from __future__ import annotations
 
@@ -214,12 +222,39 @@ def make_case(name, rp, col, w, exe, seed, clusters=None):
           "clusters", len(clusters))
 
 
+PULL_MIRROR_K = "1000000000"
+
+
+def make_pull(exe):
+    flags = dict(REF_FLAGS_PR, message_type="pull", mirror_k=PULL_MIRROR_K)
+    out = {"params": json.dumps({"flags_pr_pull": flags})}
+    for name in ("rmat12", "planted2600"):
+        z = np.load(os.path.join(HERE, f"{name}.npz"))
+        rp, col, w = z["row_ptr"], z["col"], z["w"]
+        cp, mem = z["clusters_ptr"], z["clusters_members"]
+        with tempfile.TemporaryDirectory() as d:
+            write_graph(d, rp, col, w)
+            with open(os.path.join(d, "g.e.c_150"), "w") as f:
+                for i in range(len(cp) - 1):
+                    c = mem[cp[i]:cp[i + 1]]
+                    f.write(" ".join([str(len(c))] + [str(int(v)) for v in c]) + "\n")
+            res, log = run_ref(exe, d, "pagerank_pull", flags)
+        out[f"{name}_input_sha256"] = str(z["input_sha256"])
+        out[f"{name}_ref_pr_pull_peval"] = res
+        out[f"{name}_stats"] = json.dumps(parse_stats(log))
+        print(name, "pull", len(res), float(res.sum()))
+    np.savez_compressed(os.path.join(HERE, "pull_pr.npz"), **out)
+
+
 def main():
     sys.path.insert(0, os.path.join(ROOT, "oracle", "ref_harness"))
     import build_ref
     exe = build_ref.build()
     if exe is None:
         raise SystemExit("reference checkout or harness build unavailable")
+    if "--pull" in sys.argv[1:]:
+        make_pull(exe)
+        return
     rp, col, w = sg.rmat_host(12, 16 << 12, seed=1, weight_kind=1, wlo=1, whi=100)
     make_case("rmat12", rp, col, w, exe, seed=1)
     rp, col, w = planted_graph()

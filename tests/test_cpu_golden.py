@@ -118,3 +118,16 @@ def test_sssp_restatement_matches_reference(name):
     reach = np.isfinite(d1) & (np.arange(len(d1)) != 0)
     p = par1[reach]
     assert np.all(p < len(d1))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_reference_pull_worker_against_fp64(name):
+    """The message_type=pull worker's PEval (pull_pr.npz, run on the same
+    inputs without mirrors) lies within the PageRank bound of the FP64 fixed
+    point."""
+    fx = load(name)
+    p = np.load(os.path.join(HERE, "pull_pr.npz"))
+    assert str(p[f"{name}_input_sha256"]) == str(fx["input_sha256"])
+    assert json.loads(str(p[f"{name}_stats"]))["mirror_node_cnt"] == [0]
+    x = p[f"{name}_ref_pr_pull_peval"]
+    assert np.abs(x - oracle.pr_fixed_point(fx["row_ptr"], fx["col"])).sum() <= 1e-5
