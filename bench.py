@@ -949,8 +949,26 @@ def run_summarized(args, D: Dist):
             out[mode]["summary"] = {k: info[k] for k in ("clusters", "supernodes", "shortcut_edges",
                                                          "boundary_edges", "all_rows")}
         ctx.close()
+    # the pull worker (message_type=pull) over a summary without mirrors
+    ctx = sg.Context(dev, compress=1, message_type=sg.SG_MSG_PULL, mirror_k=1 << 30)
+    ctx.load_csr(rp, col, w)
+    ctx.summary_build(comms)
+    ctx.pr_peval(out=False)
+    pe = ctx.stats()
+    inc_ms, rounds = [], []
+    for b in batches + [prof_batch]:
+        ctx.apply_updates(b)
+        ctx.pr_inceval_into(None)
+        st = ctx.stats()
+        inc_ms.append(st["elapsed_ms"])
+        rounds.append(st["rounds"])
+    out["pull"] = {"peval_ms": round(pe["elapsed_ms"], 3), "peval_rounds": pe["rounds"],
+                   "inceval_ms": [round(v, 3) for v in inc_ms[:-1]],
+                   "inceval_rounds": rounds[:-1], "x": ctx.pr_values()}
+    ctx.close()
     nrp, ncol, nw = hg.csr()
     xs = oracle.pr_fixed_point(nrp, ncol)
+    out["pull"]["l1_vs_fp64"] = float(np.abs(out["pull"].pop("x") - xs).sum())
     d_ref = oracle.dijkstra(rp, col, w, 0)
     # both contexts applied the same batches (the profiled one last); hg holds
     # the graph after them
@@ -969,7 +987,7 @@ def run_summarized(args, D: Dist):
                    "vertices": n, "edges": E, "batch_changes": bsz,
                    "clusters": "the planted communities (cluster file)",
                    "parallelism": "single GPU"},
-        "summarized": out[1], "plain": out[0],
+        "summarized": out[1], "plain": out[0], "summarized_pull": out["pull"],
         "summarized_over_plain_inceval": round(s_inc / p_inc, 3),
         "pr_l1_vs_fp64": l1, "sssp_exact_vs_dijkstra": exact,
     }

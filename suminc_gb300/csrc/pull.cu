@@ -18,7 +18,19 @@
 //                    (:1045-1131)
 //   plain round      every vertex gathers along all in-edges (:600-630)
 //   stop test        sum |last_values - x| < termcheck_threshold, or the
-//                    step counter passes 200 (:1044, termCheck :1430-1462)
+//                    step counter passes 200 (:1044, termCheck :1430-1462);
+//                    in the summarized stage the mass that reached the
+//                    entries this round counts too (below)
+//
+// The summarized stage is a two-round pipeline (entries gather from exits,
+// exits gather from the entries' index values of the round before), and an
+// entry's arrivals change no value until the correction.  The reference's
+// test on values alone therefore passes in the round after the exits last
+// moved while the entries hold mass in flight; the correction never hands
+// the exits their share of it, and that mass is lost (on a graph of 64
+// planted communities the reference stops after 2 summarized rounds and
+// ends 1.5e-3 in L1 from the fixed point).  Counting the entries' arrivals
+// keeps the stage running until they are below the threshold too.
 //
 // One group of 8 lanes per vertex; the published values of a round live in
 // two buffers used by round parity (last_deltas_ / last_index_values_).  The
@@ -217,9 +229,11 @@ __global__ void __launch_bounds__(kPT) k_pull_round(PullArgs A, int parity, int 
       } else if (t == 2) {
         A.spd[v] += a;
         nl = a;
+        r += fabs((double)a);
       } else if (t == 3) {
         A.spd[v] += a;
         nl = a;
+        r += fabs((double)a);
         x += b;
         A.delta[v] = b;
         nd = b;

@@ -24,7 +24,11 @@ Each case writes <case>.npz with:
 runs the message_type=pull worker (SumSyncIterWorkerPull) on the inputs of
 the cases above, with mirror_k large enough that no mirror is made, and
 writes pull_pr.npz: params (flags), <case>_input_sha256 and
-<case>_ref_pr_pull_peval.  Its IncEval is not recorded: with an update file
+<case>_ref_pr_pull_peval; plus community64 (64 planted communities of 40,
+bench.py's community generator, seed 1) with its inputs
+community64_row_ptr / _col / _clusters_ptr / _clusters_members, on which the
+reference's pull worker ends its summarized stage after two rounds and
+stays 1.5e-3 in L1 from the fixed point.  Its IncEval is not recorded: with an update file
 the reference's pull worker stops with a segmentation fault inside
 inc_run (after inc_compute_index_mirror_spid) on both cases.
 """
@@ -243,6 +247,22 @@ def make_pull(exe):
         out[f"{name}_ref_pr_pull_peval"] = res
         out[f"{name}_stats"] = json.dumps(parse_stats(log))
         print(name, "pull", len(res), float(res.sum()))
+    import bench
+    rp, col, w, comms = bench.community_graph(64, 40, 1)
+    cp = np.zeros(len(comms) + 1, np.uint32)
+    for i, c in enumerate(comms):
+        cp[i + 1] = cp[i] + len(c)
+    mem = np.concatenate(comms).astype(np.uint32)
+    with tempfile.TemporaryDirectory() as d:
+        write_graph(d, rp, col, w)
+        with open(os.path.join(d, "g.e.c_150"), "w") as f:
+            for c in comms:
+                f.write(" ".join([str(len(c))] + [str(int(v)) for v in c]) + "\n")
+        res, log = run_ref(exe, d, "pagerank_pull", flags)
+    out.update(community64_row_ptr=rp, community64_col=col, community64_clusters_ptr=cp,
+               community64_clusters_members=mem, community64_ref_pr_pull_peval=res,
+               community64_stats=json.dumps(parse_stats(log)))
+    print("community64", "pull", len(res), float(res.sum()))
     np.savez_compressed(os.path.join(HERE, "pull_pr.npz"), **out)
 
 

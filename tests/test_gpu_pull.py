@@ -56,6 +56,32 @@ def test_pull_summarized_peval_matches_reference_and_inceval_converges(name):
             assert np.abs(x - oracle.pr_fixed_point(rp, col)).sum() <= TOL_FIXED, b
 
 
+def test_pull_counts_mass_in_flight_at_entries():
+    """64 planted communities, where the reference's pull worker stops its
+    summarized stage with mass in flight at the entries (1.5e-3 from the
+    fixed point): the device worker counts the entries' arrivals in its stop
+    test and agrees with the CPU restatement that does the same; PEval and
+    two IncEvals stay within the FP64 bound."""
+    from oracle import pull
+    z = np.load(os.path.join(HERE, "pull_pr.npz"))
+    rp, col = z["community64_row_ptr"], z["community64_col"]
+    cp, mem = z["community64_clusters_ptr"], z["community64_clusters_members"]
+    clusters = [mem[cp[i]:cp[i + 1]] for i in range(len(cp) - 1)]
+    x_oracle, _ = pull.pr_pull_summarized(rp, col, clusters, count_entry_arrivals=True)
+    hg = sg.HostGraph(rp, col)
+    with sg.Context(0, compress=1, message_type=sg.SG_MSG_PULL, mirror_k=1 << 30) as ctx:
+        ctx.load_csr(rp, col)
+        ctx.summary_build(clusters)
+        x = ctx.pr_peval()
+        assert np.abs(x - x_oracle).sum() <= TOL_REF
+        assert np.abs(x - oracle.pr_fixed_point(rp, col)).sum() <= TOL_FIXED
+        for seed in (1, 2):
+            ctx.apply_updates(hg.gen_updates(200, 200, 0, seed=seed))
+            nrp, ncol, _ = hg.csr()
+            x = ctx.pr_inceval()
+            assert np.abs(x - oracle.pr_fixed_point(nrp, ncol)).sum() <= TOL_FIXED
+
+
 def test_pull_plain_rounds():
     """compress = 0: every vertex gathers along all its in-edges each round;
     PEval and two IncEvals within the FP64 bound, and equal to the push
