@@ -381,6 +381,8 @@ struct PullView {
   const uint64_t* id_off = nullptr;  // inner_delta shortcuts ending here
   const uint32_t* id_src = nullptr;
   const float* id_w = nullptr;
+  const uint32_t* act = nullptr;  // the vertices of classes 0-3 (the rounds' rows)
+  uint32_t n_act = 0;
   uint64_t round_edges = 0;  // entries one summarized round reads
   uint64_t round_shortcuts = 0;  // of which shortcut (value index) entries
   uint64_t corr_entries = 0;

@@ -16,11 +16,19 @@
 //   correction       parked deltas return, inner vertices take their value
 //                    and delta shares of the accumulated entry mass
 //                    (:1045-1131)
-//   plain round      every vertex gathers along all in-edges (:600-630)
-//   stop test        sum |last_values - x| < termcheck_threshold, or the
-//                    step counter passes 200 (:1044, termCheck :1430-1462);
-//                    in the summarized stage the mass that reached the
-//                    entries this round counts too (below)
+//   plain round      every vertex gathers along all in-edges (:600-630):
+//                    the same round as the library's dense pull rounds
+//                    (pagerank.cu: gather the published d*delta/outdeg, add
+//                    the sum to x, stop when the gathered sum |delta| is
+//                    below termcheck_threshold), which therefore run this
+//                    stage, and all of compress = 0
+//   stop test        summarized stage: sum |last_values - x| <
+//                    termcheck_threshold, or the step counter passes 200
+//                    (:1044, termCheck :1430-1462), where the mass that
+//                    reached the entries this round counts too (below); the
+//                    plain stage stops as the dense pull rounds do (its sum
+//                    |last_values - x| is the gathered sum |delta|), within
+//                    max_rounds
 //
 // The summarized stage is a two-round pipeline (entries gather from exits,
 // exits gather from the entries' index values of the round before), and an
@@ -32,8 +40,10 @@
 // ends 1.5e-3 in L1 from the fixed point).  Counting the entries' arrivals
 // keeps the stage running until they are below the threshold too.
 //
-// One group of 8 lanes per vertex; the published values of a round live in
-// two buffers used by round parity (last_deltas_ / last_index_values_).  The
+// The summarized rounds visit the vertices of classes 0-3 only (inner
+// members neither gather nor publish until the correction), one group of 8
+// lanes per vertex; the published values of a round live in two buffers
+// used by round parity (last_deltas_ / last_index_values_).  The
 // residual is summed in FP64 per block and by the last block to finish, which
 // also takes the stop decision; kernels of a chunk launched after the
 // decision return at once, so the host reads the control words once per
@@ -112,7 +122,7 @@ __device__ __forceinline__ float publish(float dl, uint32_t od, float d) {
 
 // Block sum of `r`, then the last block to finish sums the block partials in
 // a fixed order and decides whether the stage stops.
-__device__ void residual_and_decide(const PullArgs& A, double r, int step_base) {
+__device__ void residual_and_decide(const PullArgs& A, double r) {
   __shared__ double s_w[kPT / 32];
   __shared__ bool s_last;
 #pragma unroll
@@ -144,18 +154,18 @@ __device__ void residual_and_decide(const PullArgs& A, double r, int step_base) 
     *A.res = tot;
     const bool passed = tot < A.tau;
     A.ctl[P_PASSED] = passed ? 1u : 0u;
-    if (passed || step_base + (int)step > kStepCap) A.ctl[P_STOP] = 1u;
+    if (passed || step > (uint32_t)kStepCap) A.ctl[P_STOP] = 1u;
     A.ctl[P_DONE_BLOCKS] = 0u;
   }
 }
 
-// init: last_values = x, then the class rules (COMP) or x += delta for all.
-template <bool COMP>
+// init: last_values = x, then the class rules; both parities of the
+// published buffers start defined (inner members never write theirs).
 __global__ void __launch_bounds__(kPT) k_pull_init(PullArgs A) {
   for (uint32_t v = blockIdx.x * kPT + threadIdx.x; v < A.n; v += gridDim.x * kPT) {
     float x = A.x[v], dl = A.delta[v];
     A.lastx[v] = x;
-    const uint32_t t = COMP ? A.V.cls[v] : 0u;
+    const uint32_t t = A.V.cls[v];
     float nd = 0.f, nl = 0.f;
     if (t == 0) {
       x += dl;
@@ -170,17 +180,15 @@ __global__ void __launch_bounds__(kPT) k_pull_init(PullArgs A) {
     A.x[v] = x;
     A.delta[v] = dl;
     A.ld[v] = publish(nd, A.outdeg[v], A.d);
-    if (COMP) {
-      A.li[v] = nl;
-      A.spd[v] = nl;
-    }
+    A.ld[A.n + v] = 0.f;
+    A.li[v] = nl;
+    A.li[A.n + v] = 0.f;
+    A.spd[v] = nl;
   }
 }
 
-// One round.  COMP: the summarized round by vertex class; else every vertex
-// is an out node (plain round).
-template <bool COMP>
-__global__ void __launch_bounds__(kPT) k_pull_round(PullArgs A, int parity, int step_base) {
+// One summarized round over the vertices of classes 0-3.
+__global__ void __launch_bounds__(kPT) k_pull_round(PullArgs A, int parity) {
   if (((volatile uint32_t*)A.ctl)[P_STOP]) return;
   const float* __restrict__ ldi = A.ld + (size_t)parity * A.n;
   float* __restrict__ ldo = A.ld + (size_t)(parity ^ 1) * A.n;
@@ -190,31 +198,30 @@ __global__ void __launch_bounds__(kPT) k_pull_round(PullArgs A, int parity, int 
   const uint64_t warp = ((uint64_t)blockIdx.x * kPT + threadIdx.x) >> 5;
   const uint64_t nwarps = (uint64_t)gridDim.x * (kPT / 32);
   const uint32_t gw = (threadIdx.x & 31) / kPG;
+  const uint32_t cnt = A.V.n_act;
   double r = 0;
   // every lane of a warp runs the same trip count (the group sums shuffle
   // across the whole warp)
-  for (uint64_t base = warp * kGroupsPerWarp; base < A.n; base += nwarps * kGroupsPerWarp) {
-    const uint64_t v64 = base + gw;
-    const bool act = v64 < A.n;
-    const uint32_t v = act ? (uint32_t)v64 : 0u;
-    const uint32_t t = (COMP && act) ? A.V.cls[v] : 0u;
+  for (uint64_t base = warp * kGroupsPerWarp; base < cnt; base += nwarps * kGroupsPerWarp) {
+    const uint64_t i = base + gw;
+    const bool act = i < cnt;
+    const uint32_t v = act ? A.V.act[i] : 0u;
+    const uint32_t t = act ? A.V.cls[v] : 4u;
     float a = 0.f, b = 0.f;
-    if (act) {
-      if (t == 0) {
-        const uint64_t o = A.in_off[v];
-        const uint32_t dg = A.in_deg[v];
-        for (uint32_t e = lane; e < dg; e += kPG) a += ldi[A.in_col[o + e]];
-      } else if (t == 2 || t == 3) {
-        for (uint64_t e = A.V.ie_off[v] + lane; e < A.V.ie_off[v + 1]; e += kPG)
-          a += ldi[A.V.ie_nbr[e]];
-      }
-      if (COMP && (t == 1 || t == 3)) {
-        for (uint64_t e = A.V.iv_off[v] + lane; e < A.V.iv_off[v + 1]; e += kPG)
-          b += lii[A.V.iv_src[e]] * A.V.iv_w[e];
-      }
+    if (t == 0) {
+      const uint64_t o = A.in_off[v];
+      const uint32_t dg = A.in_deg[v];
+      for (uint32_t e = lane; e < dg; e += kPG) a += ldi[A.in_col[o + e]];
+    } else if (t == 2 || t == 3) {
+      for (uint64_t e = A.V.ie_off[v] + lane; e < A.V.ie_off[v + 1]; e += kPG)
+        a += ldi[A.V.ie_nbr[e]];
+    }
+    if (t == 1 || t == 3) {
+      for (uint64_t e = A.V.iv_off[v] + lane; e < A.V.iv_off[v + 1]; e += kPG)
+        b += lii[A.V.iv_src[e]] * A.V.iv_w[e];
     }
     a = group_sum(a);
-    if (COMP) b = group_sum(b);
+    b = group_sum(b);
     if (act && lane == 0) {
       float x = A.x[v];
       float nd = 0.f, nl = 0.f;
@@ -226,30 +233,28 @@ __global__ void __launch_bounds__(kPT) k_pull_round(PullArgs A, int parity, int 
         x += b;
         A.delta[v] = b;
         nd = b;
-      } else if (t == 2) {
+      } else {  // 2, 3
         A.spd[v] += a;
         nl = a;
         r += fabs((double)a);
-      } else if (t == 3) {
-        A.spd[v] += a;
-        nl = a;
-        r += fabs((double)a);
-        x += b;
-        A.delta[v] = b;
-        nd = b;
+        if (t == 3) {
+          x += b;
+          A.delta[v] = b;
+          nd = b;
+        }
       }
       ldo[v] = publish(nd, A.outdeg[v], A.d);
-      if (COMP) lio[v] = nl;
+      lio[v] = nl;
       A.x[v] = x;
       r += fabs((double)A.lastx[v] - (double)x);
       A.lastx[v] = x;
     }
   }
-  residual_and_decide(A, r, step_base);
+  residual_and_decide(A, r);
 }
 
-// Correction after the summarized rounds; publishes d*delta/outdeg for the
-// first plain round into ld[0].
+// Correction after the summarized rounds; x then holds every vertex's
+// gathered delta, which the conversion below takes back out.
 __global__ void __launch_bounds__(kPT) k_pull_correct(PullArgs A) {
   const uint32_t lane = threadIdx.x & (kPG - 1);
   const uint64_t warp = ((uint64_t)blockIdx.x * kPT + threadIdx.x) >> 5;
@@ -280,19 +285,10 @@ __global__ void __launch_bounds__(kPT) k_pull_correct(PullArgs A) {
         x += bd;
         dl += bd;
       }
-      A.x[v] = x;
+      A.x[v] = x - dl;
       A.delta[v] = dl;
-      A.ld[v] = publish(dl, A.outdeg[v], A.d);
     }
   }
-}
-
-// The worker's values include the delta each vertex gathered last (x +=
-// delta on arrival); the library's state keeps x without the pending delta
-// (the push workers' convention, which AmendValue and IncEval build on).
-__global__ void k_pull_finish(uint32_t n, float* x, const float* delta) {
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
-    x[v] -= delta[v];
 }
 
 __global__ void k_pull_start(uint32_t n, float* x, float* delta, float init_c) {
@@ -301,6 +297,10 @@ __global__ void k_pull_start(uint32_t n, float* x, float* delta, float init_c) {
     delta[v] = init_c;
   }
 }
+
+// The worker adds a gathered delta to x on arrival; the library's state
+// keeps x without the pending delta (the convention of the dense pull
+// rounds, AmendValue and IncEval), so the correction stores x - delta.
 
 sg_status preserve(sg_ctx* ctx, uint32_t n) {
   if (!ctx->pull_state) ctx->pull_state = new PullState();
@@ -321,23 +321,21 @@ sg_status preserve(sg_ctx* ctx, uint32_t n) {
   return SG_OK;
 }
 
-// Rounds of one stage until the stop word is set; returns the rounds run and
-// whether the residual test passed.
-template <bool COMP>
-sg_status stage(sg_ctx* ctx, const PullArgs& A, int step_base, int klass, uint32_t* rounds,
-                bool* passed) {
+// Summarized rounds until the stop word is set; returns the rounds run.
+sg_status summarized_stage(sg_ctx* ctx, const PullArgs& A, uint32_t* rounds) {
   cudaStream_t st = ctx->stream;
   const PullState& P = *pstate(ctx);
   SG_CUDA(ctx, cudaMemsetAsync(A.ctl, 0, sizeof(uint32_t) * P_WORDS, st));
   uint32_t h[P_WORDS] = {0, 0, 0, 0};
   int launched = 0;
   const int cap = kStepCap + 2;
+  const unsigned blocks = std::max(1u, std::min(P.nblocks, (A.V.n_act + kPT / kPG - 1) / (kPT / kPG)));
   while (launched < cap) {
     kprof_begin(ctx);
     int c = 0;
     for (; c < kChunk && launched < cap; ++c, ++launched)
-      k_pull_round<COMP><<<P.nblocks, kPT, 0, st>>>(A, launched & 1, step_base);
-    kprof_end(ctx, klass);
+      k_pull_round<<<blocks, kPT, 0, st>>>(A, launched & 1);
+    kprof_end(ctx, SG_K_SUMMARY);
     count_launch(ctx, c);
     SG_CUDA(ctx, cudaGetLastError());
     SG_CUDA(ctx, cudaMemcpyAsync(h, A.ctl, sizeof(h), cudaMemcpyDeviceToHost, st));
@@ -345,7 +343,6 @@ sg_status stage(sg_ctx* ctx, const PullArgs& A, int step_base, int klass, uint32
     if (h[P_STOP]) break;
   }
   *rounds = h[P_ROUNDS];
-  *passed = h[P_PASSED] != 0;
   return SG_OK;
 }
 
@@ -362,17 +359,16 @@ sg_status pull_free(sg_ctx* ctx) {
 }
 
 // PEval (inc = false: x = 0, delta = (1-d)/N) or IncEval (the amended state)
-// of the pull worker.  With compress = 1 the summarized stage, the
-// correction and then the plain stage run (Query's batch / inc stages,
-// sum_sync_iter_worker_pull.h:243-1400); with compress = 0 only the plain
-// stage.
+// of the pull worker.  compress = 1: the summarized stage, the correction,
+// then the plain stage (Query's batch / inc stages,
+// sum_sync_iter_worker_pull.h:243-1400); compress = 0: the plain stage.
 sg_status pr_pull_worker(sg_ctx* ctx, bool inc) {
   DevGraph& g = ctx->g;
   PrState& s = ctx->pr;
   if (!g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
-  const bool comp = ctx->opt.compress != 0;
+  if (!ctx->opt.compress) return pr_run(ctx, inc);
   PullView V;
-  if (comp) SG_TRY(summary_pull_view(ctx, &V));
+  SG_TRY(summary_pull_view(ctx, &V));
   if (inc && !s.valid) return fail(ctx, SG_ERR_STATE, "PageRank IncEval before PEval");
   if (!s.x) SG_TRY(pr_alloc(ctx));
   const uint32_t n = g.n;
@@ -405,43 +401,30 @@ sg_status pr_pull_worker(sg_ctx* ctx, bool inc) {
                                      (float)((1.0 - ctx->opt.damping) / (double)n));
     count_launch(ctx);
   }
-  uint32_t rc = 0, rp = 0;
-  bool passed = false;
-  if (comp) {
-    k_pull_init<true><<<vb, kPT, 0, st>>>(A);
-    count_launch(ctx);
-    SG_TRY(stage<true>(ctx, A, 0, SG_K_SUMMARY, &rc, &passed));
-    k_pull_correct<<<P.nblocks, kPT, 0, st>>>(A);
-    count_launch(ctx);
-    // `continue` skips ++step: the first plain round repeats the last step
-    SG_TRY(stage<false>(ctx, A, (int)rc - 1, SG_K_PR_PULL, &rp, &passed));
-  } else {
-    k_pull_init<false><<<vb, kPT, 0, st>>>(A);
-    count_launch(ctx);
-    SG_TRY(stage<false>(ctx, A, 0, SG_K_PR_PULL, &rp, &passed));
-  }
-  k_pull_finish<<<vb, kPT, 0, st>>>(n, s.x, s.delta);
+  k_pull_init<<<vb, kPT, 0, st>>>(A);
   count_launch(ctx);
+  uint32_t rc = 0;
+  SG_TRY(summarized_stage(ctx, A, &rc));
+  kprof_begin(ctx);
+  k_pull_correct<<<P.nblocks, kPT, 0, st>>>(A);
+  kprof_end(ctx, SG_K_SUMMARY);
+  count_launch(ctx);
+  SG_CUDA(ctx, cudaGetLastError());
   SG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
-  double res = 0;
-  SG_CUDA(ctx, cudaMemcpyAsync(&res, P.res, sizeof(double), cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  // the plain stage: the library's dense pull rounds from this state
   s.valid = true;
+  const sg_status stt = pr_run(ctx, true);
   sg_stats& S = ctx->stats;
-  S.rounds = (int32_t)(rc + rp);
-  S.converged = passed ? 1 : 0;
-  S.residual = res;
+  S.rounds += (int32_t)rc;
   S.shortcut_edges = (uint64_t)rc * V.round_shortcuts;
-  S.edges_relaxed = (uint64_t)rc * V.round_edges + (comp ? V.corr_entries : 0) + (uint64_t)rp * g.m;
+  S.edges_relaxed += (uint64_t)rc * V.round_edges + V.corr_entries;
   S.edges_pull = S.edges_relaxed;
-  S.edges_push = 0;
-  S.vertex_visits = (uint64_t)(rc + rp) * n;
-  S.elapsed_ms = ms;
-  S.live_edges = g.m;
-  if (!passed) return fail(ctx, SG_ERR_NOT_CONVERGED, "pull PageRank reached the 200-step cap");
-  return SG_OK;
+  S.vertex_visits += (uint64_t)rc * V.n_act;
+  S.elapsed_ms += ms;
+  return stt;
 }
 
 }  // namespace sg

@@ -102,7 +102,7 @@ struct SummaryDev {
   PullView pv;
   uint8_t* p_cls = nullptr;
   uint64_t *p_ie_off = nullptr, *p_iv_off = nullptr, *p_id_off = nullptr;
-  uint32_t *p_ie_nbr = nullptr, *p_iv_src = nullptr, *p_id_src = nullptr;
+  uint32_t *p_ie_nbr = nullptr, *p_iv_src = nullptr, *p_id_src = nullptr, *p_act = nullptr;
   float *p_iv_w = nullptr, *p_id_w = nullptr;
 };
 
@@ -124,6 +124,7 @@ static void sfree(SummaryDev& D) {
   dfree(D.sk_cv); dfree(D.sk_w); dfree(D.sk_cd);
   dfree(D.p_cls); dfree(D.p_ie_off); dfree(D.p_iv_off); dfree(D.p_id_off);
   dfree(D.p_ie_nbr); dfree(D.p_iv_src); dfree(D.p_id_src); dfree(D.p_iv_w); dfree(D.p_id_w);
+  dfree(D.p_act);
 }
 
 sg_status summary_free(sg_ctx* ctx) {
@@ -1412,6 +1413,10 @@ static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
   uint64_t corr = id_off[n];
   for (uint32_t v = 0; v < n; ++v)
     if (cls[v] == 2 || cls[v] == 4) corr += iv_off[v + 1] - iv_off[v];
+  std::vector<uint32_t> act;
+  for (uint32_t v = 0; v < n; ++v)
+    if (cls[v] != 4) act.push_back(v);
+  SG_TRY(upload(ctx, &D.p_act, act));
   SG_TRY(upload(ctx, &D.p_cls, cls));
   SG_TRY(upload(ctx, &D.p_ie_off, ie_off));
   SG_TRY(upload(ctx, &D.p_ie_nbr, ie_nbr));
@@ -1424,6 +1429,8 @@ static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
   PullView& V = D.pv;
   V.n = n;
   V.cls = D.p_cls;
+  V.act = D.p_act;
+  V.n_act = (uint32_t)act.size();
   V.ie_off = D.p_ie_off; V.ie_nbr = D.p_ie_nbr;
   V.iv_off = D.p_iv_off; V.iv_src = D.p_iv_src; V.iv_w = D.p_iv_w;
   V.id_off = D.p_id_off; V.id_src = D.p_id_src; V.id_w = D.p_id_w;
