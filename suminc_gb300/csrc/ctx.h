@@ -367,24 +367,28 @@ sg_status summary_build_serialized(sg_ctx* ctx, const std::vector<uint8_t>& blob
 sg_status summary_serialized(sg_ctx* ctx, std::vector<uint8_t>* blob);
 sg_status pr_summarized(sg_ctx* ctx, bool inc);
 
-// SumSyncIterWorkerPull's per-vertex in-indexes over the summary, on the
-// device (built on first use after each summary change).  Vertex classes: 0
-// out node, 1 exit only, 2 entry only, 3 entry and exit, 4 inner member.
+// SumSyncIterWorkerPull's in-indexes over the summary, on the device (built
+// on first use after each summary change).  Vertex classes: 0 out node, 1
+// exit only, 2 entry only, 3 entry and exit, 4 inner member.
 struct PullView {
   uint32_t n = 0;
   const uint8_t* cls = nullptr;
-  const uint64_t* ie_off = nullptr;  // classes 2, 3: in-edges from other clusters
-  const uint32_t* ie_nbr = nullptr;
-  const uint64_t* iv_off = nullptr;  // bound_delta + inner_value shortcuts ending here
-  const uint32_t* iv_src = nullptr;  // (the supernode's entry)
-  const float* iv_w = nullptr;
-  const uint64_t* id_off = nullptr;  // inner_delta shortcuts ending here
-  const uint32_t* id_src = nullptr;
-  const float* id_w = nullptr;
-  const uint32_t* act = nullptr;  // the vertices of classes 0-3 (the rounds' rows)
+  const uint32_t* act = nullptr;     // vertices of classes 0-3 (the rounds' rows)
   uint32_t n_act = 0;
-  uint64_t round_edges = 0;  // entries one summarized round reads
-  uint64_t round_shortcuts = 0;  // of which shortcut (value index) entries
+  const uint32_t* ent = nullptr;     // vertices of classes 2-3 (the entries)
+  uint32_t n_ent = 0;
+  const uint64_t* ie_off = nullptr;  // per vertex: in-edges from other clusters (2, 3)
+  const uint32_t* ie_nbr = nullptr;
+  const uint64_t* bd_off = nullptr;  // per vertex: bound_delta shortcuts ending here (1, 3)
+  const uint32_t* bd_src = nullptr;  // (the supernode's entry)
+  const float* bd_w = nullptr;
+  // the correction scatters each entry's supernode lists
+  const uint32_t* corr_sp = nullptr;  // row -> supernode
+  const uint64_t *id_off = nullptr, *iv_off = nullptr;  // per supernode
+  const uint32_t *id_nbr = nullptr, *iv_nbr = nullptr;
+  const float *id_w = nullptr, *iv_w = nullptr;
+  uint64_t round_edges = 0;      // entries one summarized round reads
+  uint64_t round_shortcuts = 0;  // of which shortcut entries
   uint64_t corr_entries = 0;
 };
 sg_status summary_pull_view(sg_ctx* ctx, PullView* out);

@@ -217,8 +217,8 @@ __global__ void __launch_bounds__(kPT) k_pull_round(PullArgs A, int parity) {
         a += ldi[A.V.ie_nbr[e]];
     }
     if (t == 1 || t == 3) {
-      for (uint64_t e = A.V.iv_off[v] + lane; e < A.V.iv_off[v + 1]; e += kPG)
-        b += lii[A.V.iv_src[e]] * A.V.iv_w[e];
+      for (uint64_t e = A.V.bd_off[v] + lane; e < A.V.bd_off[v + 1]; e += kPG)
+        b += lii[A.V.bd_src[e]] * A.V.bd_w[e];
     }
     a = group_sum(a);
     b = group_sum(b);
@@ -253,41 +253,35 @@ __global__ void __launch_bounds__(kPT) k_pull_round(PullArgs A, int parity) {
   residual_and_decide(A, r);
 }
 
-// Correction after the summarized rounds; x then holds every vertex's
-// gathered delta, which the conversion below takes back out.
-__global__ void __launch_bounds__(kPT) k_pull_correct(PullArgs A) {
-  const uint32_t lane = threadIdx.x & (kPG - 1);
-  const uint64_t warp = ((uint64_t)blockIdx.x * kPT + threadIdx.x) >> 5;
-  const uint64_t nwarps = (uint64_t)gridDim.x * (kPT / 32);
-  const uint32_t gw = (threadIdx.x & 31) / kPG;
-  for (uint64_t base = warp * kGroupsPerWarp; base < A.n; base += nwarps * kGroupsPerWarp) {
-    const uint64_t v64 = base + gw;
-    const bool act = v64 < A.n;
-    const uint32_t v = act ? (uint32_t)v64 : 0u;
-    const uint32_t t = act ? A.V.cls[v] : 0u;
-    float bv = 0.f, bd = 0.f;
-    if (act && (t == 2 || t == 4))
-      for (uint64_t e = A.V.iv_off[v] + lane; e < A.V.iv_off[v + 1]; e += kPG)
-        bv += A.spd[A.V.iv_src[e]] * A.V.iv_w[e];
-    if (act && t >= 1)
-      for (uint64_t e = A.V.id_off[v] + lane; e < A.V.id_off[v + 1]; e += kPG)
-        bd += A.spd[A.V.id_src[e]] * A.V.id_w[e];
-    bv = group_sum(bv);
-    bd = group_sum(bd);
-    if (act && lane == 0) {
-      float x = A.x[v], dl = A.delta[v];
-      if (t == 1 || t == 4) {
-        dl = A.bsave[v];
-        x += dl;
-      }
-      if (t == 2 || t == 4) x += bv;
-      if (t >= 1) {
-        x += bd;
-        dl += bd;
-      }
-      A.x[v] = x - dl;
-      A.delta[v] = dl;
+// Correction after the summarized rounds (:1045-1131), written in the
+// library's convention (x without the pending delta): exits and inner
+// members take back their parked delta, out nodes and exits with a delta
+// from the last round keep it pending; then every entry's accumulated mass
+// spreads through its supernode's inner_value (into x) and inner_delta
+// (into delta) lists.  The reference gathers the same products per target.
+__global__ void __launch_bounds__(kPT) k_pull_settle(PullArgs A) {
+  for (uint32_t v = blockIdx.x * kPT + threadIdx.x; v < A.n; v += gridDim.x * kPT) {
+    const uint32_t t = A.V.cls[v];
+    if (t == 1 || t == 4) {
+      A.delta[v] = A.bsave[v];
+    } else if (t == 0 || t == 3) {
+      A.x[v] -= A.delta[v];
     }
+  }
+}
+
+__global__ void __launch_bounds__(kPT) k_pull_spread(PullArgs A) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint32_t i = (blockIdx.x * kPT + threadIdx.x) >> 5; i < A.V.n_ent;
+       i += (gridDim.x * kPT) >> 5) {
+    const uint32_t u = A.V.ent[i];
+    const uint32_t sp = A.V.corr_sp[u];
+    const float m = A.spd[u];
+    if (sp == 0xFFFFFFFFu || m == 0.f) continue;
+    for (uint64_t e = A.V.iv_off[sp] + lane; e < A.V.iv_off[sp + 1]; e += 32)
+      atomicAdd(&A.x[A.V.iv_nbr[e]], m * A.V.iv_w[e]);
+    for (uint64_t e = A.V.id_off[sp] + lane; e < A.V.id_off[sp + 1]; e += 32)
+      atomicAdd(&A.delta[A.V.id_nbr[e]], m * A.V.id_w[e]);
   }
 }
 
@@ -300,7 +294,7 @@ __global__ void k_pull_start(uint32_t n, float* x, float* delta, float init_c) {
 
 // The worker adds a gathered delta to x on arrival; the library's state
 // keeps x without the pending delta (the convention of the dense pull
-// rounds, AmendValue and IncEval), so the correction stores x - delta.
+// rounds, AmendValue and IncEval), to which the correction converts.
 
 sg_status preserve(sg_ctx* ctx, uint32_t n) {
   if (!ctx->pull_state) ctx->pull_state = new PullState();
@@ -406,9 +400,11 @@ sg_status pr_pull_worker(sg_ctx* ctx, bool inc) {
   uint32_t rc = 0;
   SG_TRY(summarized_stage(ctx, A, &rc));
   kprof_begin(ctx);
-  k_pull_correct<<<P.nblocks, kPT, 0, st>>>(A);
+  k_pull_settle<<<vb, kPT, 0, st>>>(A);
+  if (V.n_ent)
+    k_pull_spread<<<grid_for((uint64_t)V.n_ent * 32, kPT), kPT, 0, st>>>(A);
   kprof_end(ctx, SG_K_SUMMARY);
-  count_launch(ctx);
+  count_launch(ctx, 1 + (V.n_ent > 0));
   SG_CUDA(ctx, cudaGetLastError());
   SG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));

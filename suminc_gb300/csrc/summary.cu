@@ -101,9 +101,9 @@ struct SummaryDev {
   bool pull_stale = true;
   PullView pv;
   uint8_t* p_cls = nullptr;
-  uint64_t *p_ie_off = nullptr, *p_iv_off = nullptr, *p_id_off = nullptr;
-  uint32_t *p_ie_nbr = nullptr, *p_iv_src = nullptr, *p_id_src = nullptr, *p_act = nullptr;
-  float *p_iv_w = nullptr, *p_id_w = nullptr;
+  uint64_t *p_ie_off = nullptr, *p_bd_off = nullptr;
+  uint32_t *p_ie_nbr = nullptr, *p_bd_src = nullptr, *p_act = nullptr, *p_ent = nullptr;
+  float* p_bd_w = nullptr;
 };
 
 static SummaryDev* sdev(sg_ctx* ctx) { return (SummaryDev*)ctx->summary; }
@@ -122,9 +122,8 @@ static void sfree(SummaryDev& D) {
   dfree(D.bound); dfree(D.spnode); dfree(D.old_x); dfree(D.d_res); dfree(D.sctl);
   dfree(D.sk_off); dfree(D.sk_coff); dfree(D.sk_deg); dfree(D.sk_col); dfree(D.sk_crow);
   dfree(D.sk_cv); dfree(D.sk_w); dfree(D.sk_cd);
-  dfree(D.p_cls); dfree(D.p_ie_off); dfree(D.p_iv_off); dfree(D.p_id_off);
-  dfree(D.p_ie_nbr); dfree(D.p_iv_src); dfree(D.p_id_src); dfree(D.p_iv_w); dfree(D.p_id_w);
-  dfree(D.p_act);
+  dfree(D.p_cls); dfree(D.p_ie_off); dfree(D.p_bd_off);
+  dfree(D.p_ie_nbr); dfree(D.p_bd_src); dfree(D.p_act); dfree(D.p_ent); dfree(D.p_bd_w);
 }
 
 sg_status summary_free(sg_ctx* ctx) {
@@ -1309,16 +1308,18 @@ sg_status summary_after_apply(sg_ctx* ctx) {
 
 // SumSyncIterWorkerPull's classification and in-indexes
 // (sum_sync_iter_worker_pull.h:286-509, rebuilt after each batch at
-// :1166-1342), from the summary's shortcut lists: classes 0 (no cluster), 2
-// (entry), 4 (member, no out-edge leaving the cluster), then 1 / 3 for
-// members with such an edge (3: also an entry).  Value index of v: every
-// (entry, w) of a bound_delta or inner_value list ending at v, supernodes in
-// index order, bound_delta before inner_value; delta index: inner_delta
-// likewise; both empty for class 0.  Entries (2, 3) also get their in-edges
-// from vertices of other clusters (id2spids differs), in row order.  The
-// worker indexes per-vertex arrays by the shortcut targets, which with
-// mirrors include out-mirror ids past the vertex range; a summary with
-// mirrors is refused.
+// :1166-1342): classes 0 (no cluster), 2 (entry), 4 (member, no out-edge
+// leaving the cluster), then 1 / 3 for members with such an edge (3: also
+// an entry).  The value index of an exit (1, 3) holds every (entry, w) of a
+// bound_delta list ending at it, supernodes in index order (the shortcut
+// construction puts exits in bound_delta and the other members in
+// inner_value, so no inner_value entry ends at an exit).  Entries (2, 3)
+// get their in-edges from vertices of other clusters, in row order.  The
+// worker's remaining indexes (inner_value ending at classes 2 / 4,
+// inner_delta at 1-4) only serve its correction, which scatters the
+// supernodes' own lists instead.  The worker indexes per-vertex arrays by
+// the shortcut targets, which with mirrors include out-mirror ids past the
+// vertex range; a summary with mirrors is refused.
 static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
   const Summary& S = D.S;
   const uint32_t n = S.old_n;
@@ -1336,55 +1337,27 @@ static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
     if (S.out_bound[i]) t = fc >= 0 && fc != Summary::kFcDefault ? 3 : 1;
     cls[i] = t;
   }
-  // shortcut lists, transposed: counts, offsets, then (key, src, w) per row
-  // sorted by key = (supernode, position) so the rows keep the list order
+  // bound_delta transposed: counts, offsets, then fills in supernode order
   const size_t nsp = S.supernodes.size();
-  struct Ent { uint64_t key; uint32_t src; float w; };
-  auto transpose = [&](bool value_index, std::vector<uint64_t>& off, std::vector<uint32_t>& src,
-                       std::vector<float>& wt) {
-    std::vector<uint64_t> cnt(n + 1, 0);
+  std::vector<uint64_t> bd_off(n + 1, 0);
+  for (size_t sp = 0; sp < nsp; ++sp)
+    for (const auto& e : S.supernodes[sp].bound_delta)
+      if (e.first < n && (cls[e.first] == 1 || cls[e.first] == 3)) ++bd_off[e.first + 1];
+  for (uint32_t v = 0; v < n; ++v) bd_off[v + 1] += bd_off[v];
+  std::vector<uint32_t> bd_src(bd_off[n]);
+  std::vector<float> bd_w(bd_off[n]);
+  {
+    std::vector<uint64_t> cur(bd_off.begin(), bd_off.end() - 1);
     for (size_t sp = 0; sp < nsp; ++sp) {
       const Supernode& P = S.supernodes[sp];
-      auto count = [&](const std::vector<std::pair<uint32_t, double>>& L) {
-        for (const auto& e : L)
-          if (e.first < n && cls[e.first] != 0) ++cnt[e.first + 1];
-      };
-      if (value_index) { count(P.bound_delta); count(P.inner_value); }
-      else count(P.inner_delta);
-    }
-    for (uint32_t v = 0; v < n; ++v) cnt[v + 1] += cnt[v];
-    off = cnt;
-    std::vector<Ent> ent(off[n]);
-    std::vector<uint64_t> cur(off.begin(), off.end() - 1);
-    for (size_t sp = 0; sp < nsp; ++sp) {
-      const Supernode& P = S.supernodes[sp];
-      uint64_t pos = 0;
-      auto put = [&](const std::vector<std::pair<uint32_t, double>>& L) {
-        for (const auto& e : L) {
-          const uint64_t k = ((uint64_t)sp << 32) | pos++;
-          if (e.first < n && cls[e.first] != 0) ent[cur[e.first]++] = {k, P.id, (float)e.second};
+      for (const auto& e : P.bound_delta)
+        if (e.first < n && (cls[e.first] == 1 || cls[e.first] == 3)) {
+          bd_src[cur[e.first]] = P.id;
+          bd_w[cur[e.first]++] = (float)e.second;
         }
-      };
-      if (value_index) { put(P.bound_delta); put(P.inner_value); }
-      else put(P.inner_delta);
     }
-    src.resize(off[n]);
-    wt.resize(off[n]);
-#pragma omp parallel for schedule(dynamic, 4096)
-    for (long long v = 0; v < (long long)n; ++v) {
-      std::sort(ent.begin() + off[v], ent.begin() + off[v + 1],
-                [](const Ent& a, const Ent& b) { return a.key < b.key; });
-      for (uint64_t e = off[v]; e < off[v + 1]; ++e) {
-        src[e] = ent[e].src;
-        wt[e] = ent[e].w;
-      }
-    }
-  };
-  std::vector<uint64_t> iv_off, id_off, ie_off(n + 1, 0);
-  std::vector<uint32_t> iv_src, id_src, ie_nbr;
-  std::vector<float> iv_w, id_w;
-  transpose(true, iv_off, iv_src, iv_w);
-  transpose(false, id_off, id_src, id_w);
+  }
+  std::vector<uint64_t> ie_off(n + 1, 0);
   const HostAdj& in = D.in;
 #pragma omp parallel for schedule(dynamic, 4096)
   for (long long v = 0; v < (long long)n; ++v) {
@@ -1395,7 +1368,7 @@ static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
     ie_off[v + 1] = k;
   }
   for (uint32_t v = 0; v < n; ++v) ie_off[v + 1] += ie_off[v];
-  ie_nbr.resize(ie_off[n]);
+  std::vector<uint32_t> ie_nbr(ie_off[n]);
 #pragma omp parallel for schedule(dynamic, 4096)
   for (long long v = 0; v < (long long)n; ++v) {
     if (cls[v] != 2 && cls[v] != 3) continue;
@@ -1404,38 +1377,41 @@ static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
     for (uint64_t e = in.rp[v]; e < in.rp[v + 1]; ++e)
       if (S.id2spids[in.col[e]] != c) ie_nbr[k++] = in.col[e];
   }
-  uint64_t round_edges = ie_off[n], round_sc = 0;
+  std::vector<uint32_t> act, ent;
+  uint64_t round_edges = ie_off[n] + bd_off[n], corr = 0;
   for (uint32_t v = 0; v < n; ++v) {
+    if (cls[v] == 4) continue;
+    act.push_back(v);
     if (cls[v] == 0) round_edges += in.deg(v);
-    if (cls[v] == 1 || cls[v] == 3) round_sc += iv_off[v + 1] - iv_off[v];
+    if (cls[v] == 2 || cls[v] == 3) {
+      ent.push_back(v);
+      const uint32_t sp = S.Fc_map[v];
+      if (sp < nsp) corr += S.supernodes[sp].inner_value.size() + S.supernodes[sp].inner_delta.size();
+    }
   }
-  round_edges += round_sc;
-  uint64_t corr = id_off[n];
-  for (uint32_t v = 0; v < n; ++v)
-    if (cls[v] == 2 || cls[v] == 4) corr += iv_off[v + 1] - iv_off[v];
-  std::vector<uint32_t> act;
-  for (uint32_t v = 0; v < n; ++v)
-    if (cls[v] != 4) act.push_back(v);
   SG_TRY(upload(ctx, &D.p_act, act));
+  SG_TRY(upload(ctx, &D.p_ent, ent));
   SG_TRY(upload(ctx, &D.p_cls, cls));
   SG_TRY(upload(ctx, &D.p_ie_off, ie_off));
   SG_TRY(upload(ctx, &D.p_ie_nbr, ie_nbr));
-  SG_TRY(upload(ctx, &D.p_iv_off, iv_off));
-  SG_TRY(upload(ctx, &D.p_iv_src, iv_src));
-  SG_TRY(upload(ctx, &D.p_iv_w, iv_w));
-  SG_TRY(upload(ctx, &D.p_id_off, id_off));
-  SG_TRY(upload(ctx, &D.p_id_src, id_src));
-  SG_TRY(upload(ctx, &D.p_id_w, id_w));
+  SG_TRY(upload(ctx, &D.p_bd_off, bd_off));
+  SG_TRY(upload(ctx, &D.p_bd_src, bd_src));
+  SG_TRY(upload(ctx, &D.p_bd_w, bd_w));
   PullView& V = D.pv;
+  V = PullView();
   V.n = n;
   V.cls = D.p_cls;
   V.act = D.p_act;
   V.n_act = (uint32_t)act.size();
+  V.ent = D.p_ent;
+  V.n_ent = (uint32_t)ent.size();
   V.ie_off = D.p_ie_off; V.ie_nbr = D.p_ie_nbr;
-  V.iv_off = D.p_iv_off; V.iv_src = D.p_iv_src; V.iv_w = D.p_iv_w;
-  V.id_off = D.p_id_off; V.id_src = D.p_id_src; V.id_w = D.p_id_w;
+  V.bd_off = D.p_bd_off; V.bd_src = D.p_bd_src; V.bd_w = D.p_bd_w;
+  V.corr_sp = D.corr_sp;
+  V.id_off = D.id_off; V.id_nbr = D.id_nbr; V.id_w = D.id_w;
+  V.iv_off = D.iv_off; V.iv_nbr = D.iv_nbr; V.iv_w = D.iv_w;
   V.round_edges = round_edges;
-  V.round_shortcuts = round_sc;
+  V.round_shortcuts = bd_off[n];
   V.corr_entries = corr;
   D.pull_stale = false;
   return SG_OK;
