@@ -42,7 +42,8 @@ L2_BYTES = 126 * 1024 * 1024
 BYTES_PER_RELAXED_EDGE = 12   # 4 B neighbour + 4 B delta read + 4 B delta write
 BYTES_PER_VERTEX_VISIT = 24   # 8 B row offset + 4 B delta read/reset + 8 B value RMW
 # DRAM bytes (read + write) per k_pr_pull_warp launch on the default
-# workload, from one ncu capture (profiles/pr_pull_warp_rmat24_dram.md)
+# workload (R-MAT scale 24), from one single-pass ncu capture of
+# dram__bytes_read.sum + dram__bytes_write.sum
 PULL_DRAM_BYTES_RMAT24 = 2.06e9
 
 

@@ -17,7 +17,7 @@
 // vertex whose initial delta is 0).
 //
 // Settings the reference takes from gflags are passed in GpuWorkerOptions;
-// a driver fills them from FLAGS_* (see INTEGRATION.md).
+// a driver fills them from its FLAGS_* of the same names.
 #pragma once
 
 #include <algorithm>
@@ -62,6 +62,7 @@ struct GpuWorkerOptions {
   int min_node_num = 8;              // FLAGS_min_node_num
   int mirror_k = 4;                  // FLAGS_mirror_k
   double compress_threshold = 1.0;   // FLAGS_compress_threshold
+  bool pull = false;                 // FLAGS_message_type == "pull" (PageRank)
   std::string cluster_file;          // <efile>.c_<max_node_num>; empty: no summary
   std::string update_file;           // FLAGS_efile_update; empty: PEval only
 };
@@ -164,6 +165,7 @@ class GpuWorkerBase {
     o.min_node_num = wopt_.min_node_num;
     o.mirror_k = wopt_.mirror_k;
     o.compress_threshold = wopt_.compress_threshold;
+    o.message_type = wopt_.pull ? SG_MSG_PULL : SG_MSG_PUSH;
     configure(o);
     ctx_.create(wopt_.device, o);
     std::vector<float> w;
