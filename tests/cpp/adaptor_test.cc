@@ -121,6 +121,21 @@ int main(int argc, char** argv) {
       w.Output(os);
       w.Finalize();
     }
+    if (argc > 7) {  // the pull worker over a summary (cluster file argv[7])
+      using App = grape::PageRankIngress<FragW, float>;
+      suminc_gb300::GpuWorkerOptions o;
+      o.compress = true;
+      o.pull = true;
+      o.mirror_k = 1 << 30;
+      o.cluster_file = argv[7];
+      o.update_file = argv[2];
+      suminc_gb300::GpuSumSyncIterWorker<App> w(std::make_shared<App>(), frag, o);
+      w.Init(0, 0);
+      w.Query();
+      std::ofstream os(std::string(argv[4]) + ".pull");
+      w.Output(os);
+      w.Finalize();
+    }
     {
       using App = grape::SSSPIngress<FragW, double>;
       auto app = std::make_shared<App>();

@@ -58,8 +58,13 @@ def test_cpp_workers_match_c_abi(binary, tmp_path):
     write_updates(tmp_path / "pr.update", upr, False)
     write_updates(tmp_path / "sssp.update", uss, True)
     opr, oss = tmp_path / "pr.out", tmp_path / "sssp.out"
+    clusters = sg.greedy_clusters(rp, col, 150, 8, seed=2)
+    cf = tmp_path / "g.e.c_150"
+    with open(cf, "w") as f:
+        for c in clusters:
+            f.write(" ".join([str(len(c))] + [str(int(v)) for v in oid(c)]) + "\n")
     r = subprocess.run([binary, str(ef), str(tmp_path / "pr.update"), str(tmp_path / "sssp.update"),
-                        str(opr), str(oss), str(n)], capture_output=True, text=True)
+                        str(opr), str(oss), str(n), str(cf)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     pr = np.loadtxt(opr)
     ss = np.loadtxt(oss)
@@ -72,3 +77,15 @@ def test_cpp_workers_match_c_abi(binary, tmp_path):
     assert np.abs(pr[:, 1] - x).max() <= 1e-6 * max(1.0, np.abs(x).max()) + 1e-9
     nrp, ncol, nw = hg2.csr()
     assert np.array_equal(ss[:, 1], oracle.dijkstra(nrp, ncol, nw, 3))
+    # message_type = pull over the summary: same file, same batch
+    pp = np.loadtxt(str(opr) + ".pull")
+    assert np.array_equal(pp[:, 0].astype(np.int64), oid(np.arange(n)))
+    with sg.Context(0, compress=1, message_type=sg.SG_MSG_PULL, mirror_k=1 << 30) as ctx:
+        ctx.load_csr(rp, col)
+        ctx.summary_build(clusters)
+        ctx.pr_peval(out=False)
+        ctx.apply_updates(upr)
+        xp = ctx.pr_inceval()
+    assert np.abs(pp[:, 1] - xp).sum() <= 2e-5
+    prp, pcol, _ = hg.csr()
+    assert np.abs(pp[:, 1] - oracle.pr_fixed_point(prp, pcol)).sum() <= 1e-5
