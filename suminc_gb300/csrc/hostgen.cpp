@@ -281,7 +281,8 @@ bool host_adj_patch(HostAdj& a, const std::vector<AdjOp>& ops) {
   for (const AdjOp& op : ops)
     if (op.row >= n || op.col >= n) return false;
   // new row pointers: old offsets shifted by the net insertions so far
-  std::vector<uint64_t> rp(n + 1);
+  std::vector<uint64_t>& rp = a.rp_spare;
+  rp.resize(n + 1);
   rp[0] = 0;
   {
     int64_t shift = 0;
@@ -292,8 +293,10 @@ bool host_adj_patch(HostAdj& a, const std::vector<AdjOp>& ops) {
       rp[v + 1] = (uint64_t)((int64_t)a.rp[v + 1] + shift);
     }
   }
-  std::vector<uint32_t> col(rp[n]);
-  std::vector<float> w(weighted ? rp[n] : 0);
+  std::vector<uint32_t>& col = a.col_spare;
+  std::vector<float>& w = a.w_spare;
+  col.resize(rp[n]);
+  w.resize(weighted ? rp[n] : 0);
   // rows r0..r1-1 unchanged: one bulk move
   auto move_rows = [&](uint32_t r0, uint32_t r1) {
     if (r1 <= r0) return;

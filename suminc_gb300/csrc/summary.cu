@@ -97,6 +97,7 @@ struct SummaryDev {
   bool sk_stale = true;
   // the construction's state between its two halves, serialized
   std::vector<uint8_t> init_blob;
+  std::unordered_map<const void*, uint64_t> dcap;  // reupload capacities
   // message_type = pull: per-vertex in-indexes (summary_pull_view)
   bool pull_stale = true;
   PullView pv;
@@ -124,6 +125,7 @@ static void sfree(SummaryDev& D) {
   dfree(D.sk_cv); dfree(D.sk_w); dfree(D.sk_cd);
   dfree(D.p_cls); dfree(D.p_ie_off); dfree(D.p_bd_off);
   dfree(D.p_ie_nbr); dfree(D.p_bd_src); dfree(D.p_act); dfree(D.p_ent); dfree(D.p_bd_w);
+  D.dcap.clear();
 }
 
 sg_status summary_free(sg_ctx* ctx) {
@@ -135,10 +137,53 @@ sg_status summary_free(sg_ctx* ctx) {
   return SG_OK;
 }
 
+// Host staging vectors that skip value-initialisation: the large per-batch
+// tables are written in full before they are uploaded, so zero-filling them
+// first only costs time.
 template <typename T>
-static sg_status upload(sg_ctx* ctx, T** d, const std::vector<T>& h) {
+struct NoInitAlloc : std::allocator<T> {
+  template <typename U>
+  struct rebind {
+    using other = NoInitAlloc<U>;
+  };
+  NoInitAlloc() noexcept = default;
+  template <typename U>
+  NoInitAlloc(const NoInitAlloc<U>&) noexcept {}
+  template <typename U>
+  void construct(U* p) noexcept {
+    ::new ((void*)p) U;
+  }
+  template <typename U, typename... Args>
+  void construct(U* p, Args&&... args) {
+    ::new ((void*)p) U(std::forward<Args>(args)...);
+  }
+};
+template <typename T>
+using hvec = std::vector<T, NoInitAlloc<T>>;
+
+template <typename T, typename A>
+static sg_status upload(sg_ctx* ctx, T** d, const std::vector<T, A>& h) {
   dfree(*d);
   SG_TRY(dalloc(ctx, d, std::max<size_t>(h.size(), 1)));
+  if (!h.empty())
+    SG_CUDA(ctx, cudaMemcpyAsync(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+  return SG_OK;
+}
+
+// The same for the tables rebuilt after every batch: the device array is
+// kept while it is large enough (capacities in D.dcap, with 1/8 slack), so
+// a batch costs a copy instead of a free, an allocation and a copy.
+template <typename T, typename A>
+static sg_status reupload(sg_ctx* ctx, SummaryDev& D, T** d, const std::vector<T, A>& h) {
+  const uint64_t need = std::max<size_t>(h.size(), 1);
+  auto it = D.dcap.find((const void*)d);
+  if (!*d || it == D.dcap.end() || it->second < need) {
+    dfree(*d);
+    const uint64_t cap = need + need / 8;
+    SG_TRY(dalloc(ctx, d, cap));
+    D.dcap[(const void*)d] = cap;
+  }
   if (!h.empty())
     SG_CUDA(ctx, cudaMemcpyAsync(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice,
                                  ctx->stream));
@@ -520,18 +565,18 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
 static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
   Summary& S = D.S;
   const uint32_t all = S.all_n, n = S.old_n;
-  SG_TRY(upload(ctx, &D.is_off, S.is_off));
-  SG_TRY(upload(ctx, &D.is_nbr, S.is_nbr));
-  SG_TRY(upload(ctx, &D.is_w, S.is_w));
-  SG_TRY(upload(ctx, &D.ib_off, S.ib_off));
-  SG_TRY(upload(ctx, &D.ib_nbr, S.ib_nbr));
-  SG_TRY(upload(ctx, &D.sync_off, S.sync_off));
-  SG_TRY(upload(ctx, &D.sync_nbr, S.sync_nbr));
+  SG_TRY(reupload(ctx, D, &D.is_off, S.is_off));
+  SG_TRY(reupload(ctx, D, &D.is_nbr, S.is_nbr));
+  SG_TRY(reupload(ctx, D, &D.is_w, S.is_w));
+  SG_TRY(reupload(ctx, D, &D.ib_off, S.ib_off));
+  SG_TRY(reupload(ctx, D, &D.ib_nbr, S.ib_nbr));
+  SG_TRY(reupload(ctx, D, &D.sync_off, S.sync_off));
+  SG_TRY(reupload(ctx, D, &D.sync_nbr, S.sync_nbr));
   std::vector<uint32_t> odeg(all);
 #pragma omp parallel for schedule(static)
   for (long long v = 0; v < (long long)all; ++v)
     odeg[v] = (uint32_t)D.out.deg(v < n ? (uint32_t)v : S.mirror_master((uint32_t)v));
-  SG_TRY(upload(ctx, &D.out_deg_all, odeg));
+  SG_TRY(reupload(ctx, D, &D.out_deg_all, odeg));
   std::vector<uint32_t> le, lx, ls;
   std::vector<uint8_t> nt(n);
   for (uint32_t v = 0; v < n; ++v) {
@@ -541,10 +586,10 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
     if (t == kOnlyOut || t == kBothOutIn || t == kOutMaster || t == kBothOutInMaster) lx.push_back(v);
     if (t == kSingle) ls.push_back(v);
   }
-  SG_TRY(upload(ctx, &D.ntype, nt));
-  SG_TRY(upload(ctx, &D.l_entry, le));
-  SG_TRY(upload(ctx, &D.l_exit, lx));
-  SG_TRY(upload(ctx, &D.l_single, ls));
+  SG_TRY(reupload(ctx, D, &D.ntype, nt));
+  SG_TRY(reupload(ctx, D, &D.l_entry, le));
+  SG_TRY(reupload(ctx, D, &D.l_exit, lx));
+  SG_TRY(reupload(ctx, D, &D.l_single, ls));
   D.n_entry = (uint32_t)le.size();
   D.n_exit = (uint32_t)lx.size();
   D.n_single = (uint32_t)ls.size();
@@ -553,8 +598,8 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
     om.push_back(m);
     omm.push_back(S.mirror_master(m));
   }
-  SG_TRY(upload(ctx, &D.l_omirror, om));
-  SG_TRY(upload(ctx, &D.omirror_master, omm));
+  SG_TRY(reupload(ctx, D, &D.l_omirror, om));
+  SG_TRY(reupload(ctx, D, &D.omirror_master, omm));
   D.n_omirror = (uint32_t)om.size();
   // correction tables
   std::vector<uint32_t> csp(all, 0xFFFFFFFFu), cc(all, 0);
@@ -564,8 +609,8 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
     ido[sp + 1] = ido[sp] + S.supernodes[sp].inner_delta.size();
     ivo[sp + 1] = ivo[sp] + S.supernodes[sp].inner_value.size();
   }
-  std::vector<uint32_t> idn(ido[nsp]), ivn(ivo[nsp]);
-  std::vector<float> idw(ido[nsp]), ivw(ivo[nsp]);
+  hvec<uint32_t> idn(ido[nsp]), ivn(ivo[nsp]);
+  hvec<float> idw(ido[nsp]), ivw(ivo[nsp]);
 #pragma omp parallel for schedule(dynamic, 1024)
   for (long long sp = 0; sp < (long long)nsp; ++sp) {
     const Supernode& s = S.supernodes[sp];
@@ -589,14 +634,14 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
     csp[u] = sp;
     cc[u] = (uint32_t)S.supernode_ids[S.id2spids[u]].size();
   }
-  SG_TRY(upload(ctx, &D.corr_sp, csp));
-  SG_TRY(upload(ctx, &D.corr_c, cc));
-  SG_TRY(upload(ctx, &D.id_off, ido));
-  SG_TRY(upload(ctx, &D.iv_off, ivo));
-  SG_TRY(upload(ctx, &D.id_nbr, idn));
-  SG_TRY(upload(ctx, &D.iv_nbr, ivn));
-  SG_TRY(upload(ctx, &D.id_w, idw));
-  SG_TRY(upload(ctx, &D.iv_w, ivw));
+  SG_TRY(reupload(ctx, D, &D.corr_sp, csp));
+  SG_TRY(reupload(ctx, D, &D.corr_c, cc));
+  SG_TRY(reupload(ctx, D, &D.id_off, ido));
+  SG_TRY(reupload(ctx, D, &D.iv_off, ivo));
+  SG_TRY(reupload(ctx, D, &D.id_nbr, idn));
+  SG_TRY(reupload(ctx, D, &D.iv_nbr, ivn));
+  SG_TRY(reupload(ctx, D, &D.id_w, idw));
+  SG_TRY(reupload(ctx, D, &D.iv_w, ivw));
   // Cluster members, exits and the precompute lists, all per member
   // position of the cm layout, built in two parallel passes (counts, then
   // fills at prefix offsets).  Clusters of at most kStageCap members get
@@ -642,9 +687,9 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
     c_sub[c + 1] += c_sub[c];
   }
   const uint64_t npos = cmo[ncl];
-  std::vector<uint32_t> cmv(npos), bl(blo[ncl]), loutd(c_lout[ncl]), subn(c_sub[ncl]);
-  std::vector<uint8_t> lins(c_lin[ncl]);
-  std::vector<uint64_t> lino(npos + 1), louto(npos + 1), subo(npos + 1);
+  hvec<uint32_t> cmv(npos), bl(blo[ncl]), loutd(c_lout[ncl]), subn(c_sub[ncl]);
+  hvec<uint8_t> lins(c_lin[ncl]);
+  hvec<uint64_t> lino(npos + 1), louto(npos + 1), subo(npos + 1);
 #pragma omp parallel for schedule(dynamic, 512)
   for (long long c = 0; c < (long long)ncl; ++c) {
     const auto& M = S.supernode_ids[c];
@@ -685,16 +730,16 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
   lino[npos] = c_lin[ncl];
   louto[npos] = c_lout[ncl];
   subo[npos] = c_sub[ncl];
-  SG_TRY(upload(ctx, &D.cm_off, cmo));
-  SG_TRY(upload(ctx, &D.cm_v, cmv));
-  SG_TRY(upload(ctx, &D.sub_off, subo));
-  SG_TRY(upload(ctx, &D.sub_nbr, subn));
-  SG_TRY(upload(ctx, &D.lin_off, lino));
-  SG_TRY(upload(ctx, &D.lin_src, lins));
-  SG_TRY(upload(ctx, &D.lout_off, louto));
-  SG_TRY(upload(ctx, &D.lout_dst, loutd));
-  SG_TRY(upload(ctx, &D.bl_off, blo));
-  SG_TRY(upload(ctx, &D.bound_list, bl));
+  SG_TRY(reupload(ctx, D, &D.cm_off, cmo));
+  SG_TRY(reupload(ctx, D, &D.cm_v, cmv));
+  SG_TRY(reupload(ctx, D, &D.sub_off, subo));
+  SG_TRY(reupload(ctx, D, &D.sub_nbr, subn));
+  SG_TRY(reupload(ctx, D, &D.lin_off, lino));
+  SG_TRY(reupload(ctx, D, &D.lin_src, lins));
+  SG_TRY(reupload(ctx, D, &D.lout_off, louto));
+  SG_TRY(reupload(ctx, D, &D.lout_dst, loutd));
+  SG_TRY(reupload(ctx, D, &D.bl_off, blo));
+  SG_TRY(reupload(ctx, D, &D.bound_list, bl));
   if (!D.bound) {
     SG_TRY(dalloc(ctx, &D.bound, all));
     SG_TRY(dalloc(ctx, &D.spnode, all));
@@ -1683,7 +1728,6 @@ static sg_status sssp_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector<ui
 // The summarized CSR (padded to quads) and the correction lists.
 static sg_status sssp_sketch(sg_ctx* ctx, SummaryDev& D) {
   Summary& S = D.S;
-  const HostAdj& out = D.out;
   const uint32_t all = S.all_n, n = S.old_n;
   std::vector<std::vector<std::pair<uint32_t, float>>> rows(all);
   for (size_t i = 0; i < S.cluster_in_mirror_ids.size(); ++i)

@@ -18,6 +18,11 @@ struct HostAdj {
   std::vector<uint64_t> rp;
   std::vector<uint32_t> col;
   std::vector<float> w;  // empty for unweighted graphs
+  // host_adj_patch writes the patched copy here and swaps: the buffers keep
+  // their size between batches, so no pass zero-fills a fresh array
+  std::vector<uint64_t> rp_spare;
+  std::vector<uint32_t> col_spare;
+  std::vector<float> w_spare;
   uint64_t deg(uint32_t v) const { return rp[v + 1] - rp[v]; }
 };
 

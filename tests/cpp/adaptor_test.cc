@@ -3,7 +3,8 @@
 // the workers use: InnerVertices, GetInnerVerticesNum, GetId,
 // GetOutgoingAdjList with neighbor / data, init_c, GetInitDelta).
 //
-// usage: adaptor_test <efile> <update_pr> <update_sssp> <out_pr> <out_sssp> <n>
+// usage: adaptor_test <efile> <update_pr> <update_sssp> <out_pr> <out_sssp> <n> [clusters]
+// (with a cluster file, also the pull worker over the summary into <out_pr>.pull)
 //   efile lines "u v w" with oids 10 * vid + 7; n vertices
 #include <cmath>
 #include <cstdio>
@@ -87,8 +88,9 @@ class SSSPIngress {
 }  // namespace grape
 
 int main(int argc, char** argv) {
-  if (argc != 7) {
-    std::fprintf(stderr, "usage: %s efile update_pr update_sssp out_pr out_sssp n\n", argv[0]);
+  if (argc != 7 && argc != 8) {
+    std::fprintf(stderr, "usage: %s efile update_pr update_sssp out_pr out_sssp n [clusters]\n",
+                 argv[0]);
     return 2;
   }
   using FragW = grape::Fragment<uint16_t>;
