@@ -521,7 +521,7 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
   }
   kprof_end(ctx, SG_K_SUMMARY);
   SG_CUDA(ctx, cudaGetLastError());
-  std::vector<double> val(out_off.back()), del(out_off.back());
+  hvec<double> val(out_off.back()), del(out_off.back());
   SG_CUDA(ctx, cudaMemcpyAsync(val.data(), d_val, 8 * val.size(), cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaMemcpyAsync(del.data(), d_del, 8 * del.size(), cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
