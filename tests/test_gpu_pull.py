@@ -141,3 +141,26 @@ def test_pull_refuses_summary_with_mirrors():
         with pytest.raises(sg.SgError) as e:
             ctx.pr_peval()
         assert e.value.status == sg.SG_ERR_INVALID
+
+
+def test_pull_empty_batch_and_no_kept_clusters():
+    """An empty batch leaves the pull worker's values where they were; a
+    summary that keeps no cluster (every vertex an out node) runs the
+    summarized stage over all in-edges and still converges."""
+    fx = load("planted2600")
+    rp, col = fx["row_ptr"], fx["col"]
+    x_star = oracle.pr_fixed_point(rp, col)
+    with sg.Context(0, compress=1, message_type=sg.SG_MSG_PULL, mirror_k=fx["mirror_k"]) as ctx:
+        ctx.load_csr(rp, col)
+        ctx.summary_build(fx["clusters"])
+        x0 = ctx.pr_peval()
+        ctx.apply_updates(np.zeros(0, sg.UPDATE_DTYPE))
+        x1 = ctx.pr_inceval()
+        assert np.abs(x1 - x0).sum() <= 2e-6
+        assert np.abs(x1 - x_star).sum() <= TOL_FIXED
+    with sg.Context(0, compress=1, message_type=sg.SG_MSG_PULL, mirror_k=fx["mirror_k"]) as ctx:
+        ctx.load_csr(rp, col)
+        ctx.summary_build([])
+        assert ctx.summary_info()["supernodes"] == 0
+        x = ctx.pr_peval()
+        assert np.abs(x - x_star).sum() <= TOL_FIXED
