@@ -144,7 +144,9 @@ def test_pull_refuses_summary_with_mirrors():
 
 
 def test_pull_empty_batch_and_no_kept_clusters():
-    """An empty batch leaves the pull worker's values where they were; a
+    """An empty batch moves the pull worker's values by no more than the
+    pending residual (another summarized stage and plain stage run from the
+    state PEval left, Σ|δ| < τ, so the change is within τ/(1-d)); a
     summary that keeps no cluster (every vertex an out node) runs the
     summarized stage over all in-edges and still converges."""
     fx = load("planted2600")
@@ -156,7 +158,7 @@ def test_pull_empty_batch_and_no_kept_clusters():
         x0 = ctx.pr_peval()
         ctx.apply_updates(np.zeros(0, sg.UPDATE_DTYPE))
         x1 = ctx.pr_inceval()
-        assert np.abs(x1 - x0).sum() <= 2e-6
+        assert np.abs(x1 - x0).sum() <= 1e-6 / (1 - 0.85)
         assert np.abs(x1 - x_star).sum() <= TOL_FIXED
     with sg.Context(0, compress=1, message_type=sg.SG_MSG_PULL, mirror_k=fx["mirror_k"]) as ctx:
         ctx.load_csr(rp, col)
