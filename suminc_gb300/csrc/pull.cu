@@ -41,8 +41,10 @@
 // keeps the stage running until they are below the threshold too.
 //
 // The summarized rounds visit the vertices of classes 0-3 only (inner
-// members neither gather nor publish until the correction), one group of 8
-// lanes per vertex; the published values of a round live in two buffers
+// members neither gather nor publish until the correction), one pair of
+// lanes per vertex (their rows are short: 4.0 ms of summarized rounds and
+// correction per IncEval at 5.2 M vertices with 8 lanes, 2.6 ms with 4,
+// 1.9 ms with 2); the published values of a round live in two buffers
 // used by round parity (last_deltas_ / last_index_values_).  The
 // residual is summed in FP64 per block and by the last block to finish, which
 // also takes the stop decision; kernels of a chunk launched after the
@@ -60,7 +62,7 @@ namespace sg {
 namespace {
 
 constexpr int kPT = 256;         // threads per block
-constexpr int kPG = 8;           // lanes per vertex
+constexpr int kPG = 2;           // lanes per vertex
 constexpr int kGroupsPerWarp = 32 / kPG;
 constexpr int kStepCap = 200;    // `step > 200` (sum_sync_iter_worker_pull.h:1044)
 constexpr int kChunk = 8;        // rounds launched per host check
