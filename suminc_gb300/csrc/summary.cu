@@ -1389,8 +1389,8 @@ static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
     for (const auto& e : S.supernodes[sp].bound_delta)
       if (e.first < n && (cls[e.first] == 1 || cls[e.first] == 3)) ++bd_off[e.first + 1];
   for (uint32_t v = 0; v < n; ++v) bd_off[v + 1] += bd_off[v];
-  std::vector<uint32_t> bd_src(bd_off[n]);
-  std::vector<float> bd_w(bd_off[n]);
+  hvec<uint32_t> bd_src(bd_off[n]);
+  hvec<float> bd_w(bd_off[n]);
   {
     std::vector<uint64_t> cur(bd_off.begin(), bd_off.end() - 1);
     for (size_t sp = 0; sp < nsp; ++sp) {
@@ -1413,7 +1413,7 @@ static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
     ie_off[v + 1] = k;
   }
   for (uint32_t v = 0; v < n; ++v) ie_off[v + 1] += ie_off[v];
-  std::vector<uint32_t> ie_nbr(ie_off[n]);
+  hvec<uint32_t> ie_nbr(ie_off[n]);
 #pragma omp parallel for schedule(dynamic, 4096)
   for (long long v = 0; v < (long long)n; ++v) {
     if (cls[v] != 2 && cls[v] != 3) continue;
@@ -1422,26 +1422,55 @@ static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
     for (uint64_t e = in.rp[v]; e < in.rp[v + 1]; ++e)
       if (S.id2spids[in.col[e]] != c) ie_nbr[k++] = in.col[e];
   }
-  std::vector<uint32_t> act, ent;
+  // the round's rows (classes 0-3) and the entries, in vertex order: counts
+  // per chunk, offsets, fills
+  const uint32_t nch = std::max<uint32_t>(1, std::min<uint32_t>(256, n / 16384));
+  std::vector<uint64_t> ca(nch + 1, 0), ce(nch + 1, 0), ced(nch, 0), ccr(nch, 0);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (long long ch = 0; ch < (long long)nch; ++ch) {
+    const uint32_t v0 = (uint32_t)((uint64_t)n * ch / nch), v1 = (uint32_t)((uint64_t)n * (ch + 1) / nch);
+    uint64_t a = 0, e = 0, ed = 0, cr = 0;
+    for (uint32_t v = v0; v < v1; ++v) {
+      if (cls[v] == 4) continue;
+      ++a;
+      if (cls[v] == 0) ed += in.deg(v);
+      if (cls[v] == 2 || cls[v] == 3) {
+        ++e;
+        const uint32_t sp = S.Fc_map[v];
+        if (sp < nsp) cr += S.supernodes[sp].inner_value.size() + S.supernodes[sp].inner_delta.size();
+      }
+    }
+    ca[ch + 1] = a;
+    ce[ch + 1] = e;
+    ced[ch] = ed;
+    ccr[ch] = cr;
+  }
   uint64_t round_edges = ie_off[n] + bd_off[n], corr = 0;
-  for (uint32_t v = 0; v < n; ++v) {
-    if (cls[v] == 4) continue;
-    act.push_back(v);
-    if (cls[v] == 0) round_edges += in.deg(v);
-    if (cls[v] == 2 || cls[v] == 3) {
-      ent.push_back(v);
-      const uint32_t sp = S.Fc_map[v];
-      if (sp < nsp) corr += S.supernodes[sp].inner_value.size() + S.supernodes[sp].inner_delta.size();
+  for (uint32_t ch = 0; ch < nch; ++ch) {
+    ca[ch + 1] += ca[ch];
+    ce[ch + 1] += ce[ch];
+    round_edges += ced[ch];
+    corr += ccr[ch];
+  }
+  hvec<uint32_t> act(ca[nch]), ent(ce[nch]);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (long long ch = 0; ch < (long long)nch; ++ch) {
+    const uint32_t v0 = (uint32_t)((uint64_t)n * ch / nch), v1 = (uint32_t)((uint64_t)n * (ch + 1) / nch);
+    uint64_t a = ca[ch], e = ce[ch];
+    for (uint32_t v = v0; v < v1; ++v) {
+      if (cls[v] == 4) continue;
+      act[a++] = v;
+      if (cls[v] == 2 || cls[v] == 3) ent[e++] = v;
     }
   }
-  SG_TRY(upload(ctx, &D.p_act, act));
-  SG_TRY(upload(ctx, &D.p_ent, ent));
-  SG_TRY(upload(ctx, &D.p_cls, cls));
-  SG_TRY(upload(ctx, &D.p_ie_off, ie_off));
-  SG_TRY(upload(ctx, &D.p_ie_nbr, ie_nbr));
-  SG_TRY(upload(ctx, &D.p_bd_off, bd_off));
-  SG_TRY(upload(ctx, &D.p_bd_src, bd_src));
-  SG_TRY(upload(ctx, &D.p_bd_w, bd_w));
+  SG_TRY(reupload(ctx, D, &D.p_act, act));
+  SG_TRY(reupload(ctx, D, &D.p_ent, ent));
+  SG_TRY(reupload(ctx, D, &D.p_cls, cls));
+  SG_TRY(reupload(ctx, D, &D.p_ie_off, ie_off));
+  SG_TRY(reupload(ctx, D, &D.p_ie_nbr, ie_nbr));
+  SG_TRY(reupload(ctx, D, &D.p_bd_off, bd_off));
+  SG_TRY(reupload(ctx, D, &D.p_bd_src, bd_src));
+  SG_TRY(reupload(ctx, D, &D.p_bd_w, bd_w));
   PullView& V = D.pv;
   V = PullView();
   V.n = n;
