@@ -373,8 +373,9 @@ sg_status pr_summarized(sg_ctx* ctx, bool inc);
 struct PullView {
   uint32_t n = 0;
   const uint8_t* cls = nullptr;
-  const uint32_t* act = nullptr;     // vertices of classes 0-3 (the rounds' rows)
-  uint32_t n_act = 0;
+  const uint32_t* act = nullptr;     // vertices of classes 0-3 (the rounds' rows),
+  uint32_t n_act = 0;                // those with more than 32 row entries first
+  uint32_t n_long = 0;
   const uint32_t* ent = nullptr;     // vertices of classes 2-3 (the entries)
   uint32_t n_ent = 0;
   const uint64_t* ie_off = nullptr;  // per vertex: in-edges from other clusters (2, 3)

@@ -41,10 +41,11 @@
 // keeps the stage running until they are below the threshold too.
 //
 // The summarized rounds visit the vertices of classes 0-3 only (inner
-// members neither gather nor publish until the correction), one pair of
-// lanes per vertex (their rows are short: 4.0 ms of summarized rounds and
-// correction per IncEval at 5.2 M vertices with 8 lanes, 2.6 ms with 4,
-// 1.9 ms with 2); the published values of a round live in two buffers
+// members neither gather nor publish until the correction), one lane per
+// vertex, except rows longer than a warp (a hub's in-edges), which take a
+// warp each (summarized rounds and correction per IncEval at 5.2 M vertices
+// of planted communities: 4.0 ms with 8 lanes per vertex, 2.6 ms with 4,
+// 1.9 ms with 2, 1.35 ms with 1); the published values of a round live in two buffers
 // used by round parity (last_deltas_ / last_index_values_).  The
 // residual is summed in FP64 per block and by the last block to finish, which
 // also takes the stop decision; kernels of a chunk launched after the
@@ -62,8 +63,6 @@ namespace sg {
 namespace {
 
 constexpr int kPT = 256;         // threads per block
-constexpr int kPG = 2;           // lanes per vertex
-constexpr int kGroupsPerWarp = 32 / kPG;
 constexpr int kStepCap = 200;    // `step > 200` (sum_sync_iter_worker_pull.h:1044)
 constexpr int kChunk = 8;        // rounds launched per host check
 
@@ -111,12 +110,6 @@ struct PullArgs {
   double* res;
   uint32_t* ctl;
 };
-
-__device__ __forceinline__ float group_sum(float v) {
-#pragma unroll
-  for (int o = kPG / 2; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, kPG);
-  return v;
-}
 
 __device__ __forceinline__ float publish(float dl, uint32_t od, float d) {
   return od ? dl * d / (float)od : 0.f;
@@ -189,68 +182,91 @@ __global__ void __launch_bounds__(kPT) k_pull_init(PullArgs A) {
   }
 }
 
-// One summarized round over the vertices of classes 0-3.
+// One summarized round over the vertices of classes 0-3: rows longer than
+// a warp (listed first) take a warp each, the others a lane each.
+struct RowSums {
+  float a, b;
+};
+
+__device__ __forceinline__ void round_finish(const PullArgs& A, uint32_t v, uint32_t t, float a,
+                                             float b, float* ldo, float* lio, double& r) {
+  float x = A.x[v];
+  float nd = 0.f, nl = 0.f;
+  if (t == 0) {
+    x += a;
+    A.delta[v] = a;
+    nd = a;
+  } else if (t == 1) {
+    x += b;
+    A.delta[v] = b;
+    nd = b;
+  } else {  // 2, 3
+    A.spd[v] += a;
+    nl = a;
+    r += fabs((double)a);
+    if (t == 3) {
+      x += b;
+      A.delta[v] = b;
+      nd = b;
+    }
+  }
+  ldo[v] = publish(nd, A.outdeg[v], A.d);
+  lio[v] = nl;
+  A.x[v] = x;
+  r += fabs((double)A.lastx[v] - (double)x);
+  A.lastx[v] = x;
+}
+
+// Sums of vertex v's rows over entries lane0, lane0 + step, ...
+__device__ __forceinline__ RowSums row_sums(const PullArgs& A, uint32_t v, uint32_t t,
+                                            const float* ldi, const float* lii, uint32_t lane0,
+                                            uint32_t step) {
+  float a = 0.f, b = 0.f;
+  if (t == 0) {
+    const uint64_t o = A.in_off[v];
+    const uint32_t dg = A.in_deg[v];
+    for (uint32_t e = lane0; e < dg; e += step) a += ldi[A.in_col[o + e]];
+  } else if (t == 2 || t == 3) {
+    for (uint64_t e = A.V.ie_off[v] + lane0; e < A.V.ie_off[v + 1]; e += step)
+      a += ldi[A.V.ie_nbr[e]];
+  }
+  if (t == 1 || t == 3) {
+    for (uint64_t e = A.V.bd_off[v] + lane0; e < A.V.bd_off[v + 1]; e += step)
+      b += lii[A.V.bd_src[e]] * A.V.bd_w[e];
+  }
+  return {a, b};
+}
+
 __global__ void __launch_bounds__(kPT) k_pull_round(PullArgs A, int parity) {
   if (((volatile uint32_t*)A.ctl)[P_STOP]) return;
   const float* __restrict__ ldi = A.ld + (size_t)parity * A.n;
   float* __restrict__ ldo = A.ld + (size_t)(parity ^ 1) * A.n;
   const float* __restrict__ lii = A.li + (size_t)parity * A.n;
   float* __restrict__ lio = A.li + (size_t)(parity ^ 1) * A.n;
-  const uint32_t lane = threadIdx.x & (kPG - 1);
-  const uint64_t warp = ((uint64_t)blockIdx.x * kPT + threadIdx.x) >> 5;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t gtid = (uint64_t)blockIdx.x * kPT + threadIdx.x;
+  const uint64_t warp = gtid >> 5;
   const uint64_t nwarps = (uint64_t)gridDim.x * (kPT / 32);
-  const uint32_t gw = (threadIdx.x & 31) / kPG;
-  const uint32_t cnt = A.V.n_act;
+  const uint32_t cnt = A.V.n_act, nlong = A.V.n_long;
   double r = 0;
-  // every lane of a warp runs the same trip count (the group sums shuffle
-  // across the whole warp)
-  for (uint64_t base = warp * kGroupsPerWarp; base < cnt; base += nwarps * kGroupsPerWarp) {
-    const uint64_t i = base + gw;
-    const bool act = i < cnt;
-    const uint32_t v = act ? A.V.act[i] : 0u;
-    const uint32_t t = act ? A.V.cls[v] : 4u;
-    float a = 0.f, b = 0.f;
-    if (t == 0) {
-      const uint64_t o = A.in_off[v];
-      const uint32_t dg = A.in_deg[v];
-      for (uint32_t e = lane; e < dg; e += kPG) a += ldi[A.in_col[o + e]];
-    } else if (t == 2 || t == 3) {
-      for (uint64_t e = A.V.ie_off[v] + lane; e < A.V.ie_off[v + 1]; e += kPG)
-        a += ldi[A.V.ie_nbr[e]];
+  // long rows: one warp per vertex (warp-uniform trip count)
+  for (uint64_t i = warp; i < nlong; i += nwarps) {
+    const uint32_t v = A.V.act[i];
+    const uint32_t t = A.V.cls[v];
+    RowSums s = row_sums(A, v, t, ldi, lii, lane, 32);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      s.a += __shfl_xor_sync(0xffffffffu, s.a, o);
+      s.b += __shfl_xor_sync(0xffffffffu, s.b, o);
     }
-    if (t == 1 || t == 3) {
-      for (uint64_t e = A.V.bd_off[v] + lane; e < A.V.bd_off[v + 1]; e += kPG)
-        b += lii[A.V.bd_src[e]] * A.V.bd_w[e];
-    }
-    a = group_sum(a);
-    b = group_sum(b);
-    if (act && lane == 0) {
-      float x = A.x[v];
-      float nd = 0.f, nl = 0.f;
-      if (t == 0) {
-        x += a;
-        A.delta[v] = a;
-        nd = a;
-      } else if (t == 1) {
-        x += b;
-        A.delta[v] = b;
-        nd = b;
-      } else {  // 2, 3
-        A.spd[v] += a;
-        nl = a;
-        r += fabs((double)a);
-        if (t == 3) {
-          x += b;
-          A.delta[v] = b;
-          nd = b;
-        }
-      }
-      ldo[v] = publish(nd, A.outdeg[v], A.d);
-      lio[v] = nl;
-      A.x[v] = x;
-      r += fabs((double)A.lastx[v] - (double)x);
-      A.lastx[v] = x;
-    }
+    if (lane == 0) round_finish(A, v, t, s.a, s.b, ldo, lio, r);
+  }
+  // the other rows: one lane per vertex
+  for (uint64_t i = nlong + gtid; i < cnt; i += nwarps * 32) {
+    const uint32_t v = A.V.act[i];
+    const uint32_t t = A.V.cls[v];
+    const RowSums s = row_sums(A, v, t, ldi, lii, 0, 1);
+    round_finish(A, v, t, s.a, s.b, ldo, lio, r);
   }
   residual_and_decide(A, r);
 }
@@ -325,7 +341,7 @@ sg_status summarized_stage(sg_ctx* ctx, const PullArgs& A, uint32_t* rounds) {
   uint32_t h[P_WORDS] = {0, 0, 0, 0};
   int launched = 0;
   const int cap = kStepCap + 2;
-  const unsigned blocks = std::max(1u, std::min(P.nblocks, (A.V.n_act + kPT / kPG - 1) / (kPT / kPG)));
+  const unsigned blocks = std::max(1u, std::min(P.nblocks, (A.V.n_act + kPT - 1) / kPT + A.V.n_long / (kPT / 32)));
   while (launched < cap) {
     kprof_begin(ctx);
     int c = 0;

@@ -1422,17 +1422,26 @@ static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
     for (uint64_t e = in.rp[v]; e < in.rp[v + 1]; ++e)
       if (S.id2spids[in.col[e]] != c) ie_nbr[k++] = in.col[e];
   }
-  // the round's rows (classes 0-3) and the entries, in vertex order: counts
-  // per chunk, offsets, fills
+  // the round's rows (classes 0-3; rows of more than 32 entries first, each
+  // group in vertex order) and the entries: counts per chunk, offsets, fills
+  auto row_len = [&](uint32_t v) -> uint64_t {
+    switch (cls[v]) {
+      case 0: return in.deg(v);
+      case 1: return bd_off[v + 1] - bd_off[v];
+      case 2: return ie_off[v + 1] - ie_off[v];
+      case 3: return ie_off[v + 1] - ie_off[v] + bd_off[v + 1] - bd_off[v];
+      default: return 0;
+    }
+  };
   const uint32_t nch = std::max<uint32_t>(1, std::min<uint32_t>(256, n / 16384));
-  std::vector<uint64_t> ca(nch + 1, 0), ce(nch + 1, 0), ced(nch, 0), ccr(nch, 0);
+  std::vector<uint64_t> cl_(nch + 1, 0), cs_(nch + 1, 0), ce(nch + 1, 0), ced(nch, 0), ccr(nch, 0);
 #pragma omp parallel for schedule(dynamic, 1)
   for (long long ch = 0; ch < (long long)nch; ++ch) {
     const uint32_t v0 = (uint32_t)((uint64_t)n * ch / nch), v1 = (uint32_t)((uint64_t)n * (ch + 1) / nch);
-    uint64_t a = 0, e = 0, ed = 0, cr = 0;
+    uint64_t lg = 0, sh = 0, e = 0, ed = 0, cr = 0;
     for (uint32_t v = v0; v < v1; ++v) {
       if (cls[v] == 4) continue;
-      ++a;
+      if (row_len(v) > 32) ++lg; else ++sh;
       if (cls[v] == 0) ed += in.deg(v);
       if (cls[v] == 2 || cls[v] == 3) {
         ++e;
@@ -1440,26 +1449,29 @@ static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
         if (sp < nsp) cr += S.supernodes[sp].inner_value.size() + S.supernodes[sp].inner_delta.size();
       }
     }
-    ca[ch + 1] = a;
+    cl_[ch + 1] = lg;
+    cs_[ch + 1] = sh;
     ce[ch + 1] = e;
     ced[ch] = ed;
     ccr[ch] = cr;
   }
   uint64_t round_edges = ie_off[n] + bd_off[n], corr = 0;
   for (uint32_t ch = 0; ch < nch; ++ch) {
-    ca[ch + 1] += ca[ch];
+    cl_[ch + 1] += cl_[ch];
+    cs_[ch + 1] += cs_[ch];
     ce[ch + 1] += ce[ch];
     round_edges += ced[ch];
     corr += ccr[ch];
   }
-  hvec<uint32_t> act(ca[nch]), ent(ce[nch]);
+  const uint64_t n_long = cl_[nch];
+  hvec<uint32_t> act(n_long + cs_[nch]), ent(ce[nch]);
 #pragma omp parallel for schedule(dynamic, 1)
   for (long long ch = 0; ch < (long long)nch; ++ch) {
     const uint32_t v0 = (uint32_t)((uint64_t)n * ch / nch), v1 = (uint32_t)((uint64_t)n * (ch + 1) / nch);
-    uint64_t a = ca[ch], e = ce[ch];
+    uint64_t lg = cl_[ch], sh = n_long + cs_[ch], e = ce[ch];
     for (uint32_t v = v0; v < v1; ++v) {
       if (cls[v] == 4) continue;
-      act[a++] = v;
+      if (row_len(v) > 32) act[lg++] = v; else act[sh++] = v;
       if (cls[v] == 2 || cls[v] == 3) ent[e++] = v;
     }
   }
@@ -1477,6 +1489,7 @@ static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
   V.cls = D.p_cls;
   V.act = D.p_act;
   V.n_act = (uint32_t)act.size();
+  V.n_long = (uint32_t)n_long;
   V.ent = D.p_ent;
   V.n_ent = (uint32_t)ent.size();
   V.ie_off = D.p_ie_off; V.ie_nbr = D.p_ie_nbr;
