@@ -58,7 +58,9 @@ def parse():
     p.add_argument("--batch-frac", type=float, default=0.001)
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--cpu-sample-rounds", type=int, default=3)
+    p.add_argument("--ref-budget-s", type=float, default=150.0,
+                   help="--impl reference: stop timing complete IncEvals once this many "
+                        "seconds are spent (at least two steps)")
     p.add_argument("--no-clocks", action="store_true")
     p.add_argument("--pull-hubs", type=int, default=0,
                    help="hub cache of the PageRank pull: 0 automatic, -1 none, k at most k (16384 cap)")
@@ -180,60 +182,90 @@ def make_batches(hg, count, size, seed0):
             for i in range(count)]
 
 
-def cpu_sample(rp_old, col_old, rp_new, col_new, x, delta, rounds):
-    """One bounded sample of the reference's IncEval on the host cores:
-    AmendValue(-1) over the old graph + AmendValue(+1) over the new graph +
-    `rounds` delta rounds.  Returns (relaxations, seconds)."""
+def cpu_inceval(cur, upd, x, delta, tau=1e-6):
+    """One complete IncEval of the reference's worker on the host cores: the
+    batch applied to the graph (the fragment rebuild of reloadGraph),
+    AmendValue(-1) over the old graph and AmendValue(+1) over the new one,
+    then delta rounds until sum|delta| < tau.  Returns (new graph, x, delta,
+    relaxations, seconds, rounds)."""
     import oracle
     t0 = time.perf_counter()
-    d2 = oracle.pr_amend((rp_old, col_old), (rp_new, col_new), x, delta)
-    _, _, st = oracle.ingress_pr(rp_new, col_new, x=x, delta=d2, max_rounds=rounds)
+    new = oracle.apply_updates(cur[0], cur[1], None, upd)[:2]
+    d2 = oracle.pr_amend(cur, new, x, delta)
+    x2, d3, st = oracle.ingress_pr(new[0], new[1], tau=tau, x=x, delta=d2)
     dt = time.perf_counter() - t0
-    relax = int(rp_old[-1]) + int(rp_new[-1]) + int(st["edges"])
-    return relax, dt
+    relax = int(cur[0][-1]) + int(new[0][-1]) + int(st["edges"])
+    return new, x2, d3, relax, dt, int(st["rounds"])
 
 
 def run_reference(args, D: Dist):
+    """The reference's worker restated on the CPU (oracle/), all host cores,
+    on the headline workload: the same graph and the same batches as the GPU
+    arm's device-resident steps.  Each step is one complete IncEval from a
+    converged state.  The library under test is not loaded."""
     if D.rank != 0:
         return
     import oracle
-    import suminc_gb300 as sg
     n = 1 << args.scale
     E = n * args.edge_factor
     bsz = int(round(E * args.batch_frac))
-    with sg.Context(D.local) as ctx:
-        ctx.generate_rmat(args.scale, E, seed=args.seed)
-        rp, col, _ = ctx.download_csr(weights=False)
-    hg = sg.HostGraph(rp, col)
-    # untimed: a few CPU rounds give a non-trivial starting state
-    x, delta, _ = oracle.ingress_pr(rp, col, max_rounds=args.cpu_sample_rounds)
-    cores = os.cpu_count() or 1
-    relax_t, time_t = 0, 0.0
+    half = bsz // 2
+    t0 = time.perf_counter()
+    rp, col, _ = oracle.rmat(args.scale, E, seed=args.seed)
+    gen_s = time.perf_counter() - t0
+    # PEval to convergence (untimed)
+    t0 = time.perf_counter()
+    x, delta, pst = oracle.ingress_pr(rp, col, tau=1e-6)
+    peval_s = time.perf_counter() - t0
+    W, K = args.warmup, args.steps
+    # the GPU arm draws batch i (seed 100 + i) from the graph after batches
+    # < i; warm-up batches are applied here with one IncEval over all of them
+    # (untimed), so the timed steps start from the same graph, converged
     cur = (rp, col)
-    for step in range(args.warmup + args.steps):
-        hg.gen_updates(bsz // 2, bsz - bsz // 2, 0, seed=1000 + step)
-        new = hg.csr()[:2]
-        relax, dt = cpu_sample(cur[0], cur[1], new[0], new[1], x, delta, args.cpu_sample_rounds)
-        cur = new
-        if step >= args.warmup:
-            relax_t += relax
-            time_t += dt
+    if W > 0:
+        g0 = cur
+        for i in range(W):
+            upd = oracle.gen_updates(cur[0], cur[1], half, bsz - half, 0, seed=100 + i)
+            cur = oracle.apply_updates(cur[0], cur[1], None, upd)[:2]
+        delta = oracle.pr_amend(g0, cur, x, delta)
+        x, delta, _ = oracle.ingress_pr(cur[0], cur[1], tau=1e-6, x=x, delta=delta)
+    relax_t, time_t, steps_ms, rounds = 0, 0.0, [], []
+    for i in range(W, W + K):
+        upd = oracle.gen_updates(cur[0], cur[1], half, bsz - half, 0, seed=100 + i)
+        cur, x, delta, relax, dt, r = cpu_inceval(cur, upd, x, delta)
+        relax_t += relax
+        time_t += dt
+        steps_ms.append(round(dt * 1e3, 1))
+        rounds.append(r)
+        # bounded sample: stop once the budget is spent (at least two steps)
+        if len(steps_ms) >= 2 and time_t > args.ref_budget_s:
+            break
+    k = len(steps_ms)
     gteps = relax_t / time_t / 1e9
-    sample = (f"per step: AmendValue(-1/+1) over the full scale-{args.scale} graph "
-              f"({E} edges) + {args.cpu_sample_rounds} delta rounds, after one "
-              f"{bsz}-change batch; {args.steps} steps after {args.warmup} warm-up")
+    res = oracle.pr_residual_l1(cur[0], cur[1], x)
+    cores = os.cpu_count() or 1
+    sample = (f"complete IncEvals (batch apply + AmendValue(-1/+1) + delta rounds to "
+              f"sum|delta| < 1e-6) of batches {W}..{W + k - 1}, the GPU arm's device-resident "
+              f"steps, from a converged PEval; {k} of the {K} steps within a "
+              f"{args.ref_budget_s:.0f} s budget")
     line = {
         "metric": "GTEPS for PR incremental re-eval (IncEval)",
         "value": round(gteps, 4), "unit": "GTEPS", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(time_t / args.steps * 1e3, 3),
+        "steps": K, "warmup": W, "steps_timed": k,
+        "ms_per_step": round(time_t / k * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic R-MAT (seeded)", "impl": "reference",
+        "data": "synthetic R-MAT (seeded), random update batches", "impl": "reference",
         "config": workload_config(args, n, E, bsz),
         "cpu_baseline": {"value": round(gteps, 4), "unit": "GTEPS", "cores": cores,
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(gteps, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "step_ms": steps_ms, "rounds_per_step": rounds,
+        "graph_gteps": round(E * k / time_t / 1e9, 4),
+        "setup_s": {"rmat": round(gen_s, 1), "peval": round(peval_s, 1),
+                    "peval_rounds": int(pst["rounds"])},
+        "accuracy": {"residual_l1": res, "l1_bound_vs_fixed_point": res / 0.15,
+                     "method": "||x - x*||_1 <= ||(1-d)/N + d P^T x - x||_1 / (1 - d), FP64"},
     }
     print(json.dumps(line), flush=True)
 
@@ -285,13 +317,21 @@ def run_ours(args, D: Dist):
     relax = 0
     rounds = []
     visits = []
+    step_ms, inc_ms = [], []
     for i in range(W, W + K):
+        # events 4/5 bracket the step on the library stream; IncEval has
+        # synchronised when it returns, so reading them adds no wait
+        ctx.record_event(4)
         ctx.apply_updates_ptr(bsz, dev_b[i].data_ptr(), True)
         ctx.pr_inceval_into(None)
+        ctx.record_event(5)
         st = ctx.stats()
         relax += st["edges_relaxed"]
         rounds.append(st["rounds"])
         visits.append(int(st["vertex_visits"]))
+        inc_ms.append(st["elapsed_ms"])
+        step_ms.append(ctx.elapsed_ms(4, 5))
+    repacks_value = ctx.stats()["repacks"]
     ctx.record_event(1)
     ctx.synchronize()
     D.barrier()
@@ -306,10 +346,16 @@ def run_ours(args, D: Dist):
     ctx.synchronize()
     ctx.record_event(2)
     relax_e = 0
+    step_e_ms = []
+    rep0 = ctx.stats()["repacks"]
     for i in range(K):
+        ctx.record_event(4)
         ctx.apply_updates_ptr(bsz, pin_b[i].data_ptr(), False)
         ctx.pr_inceval_into(out_pin.data_ptr())
+        ctx.record_event(5)
         relax_e += ctx.stats()["edges_relaxed"]
+        step_e_ms.append(ctx.elapsed_ms(4, 5))
+    repacks_e2e = ctx.stats()["repacks"] - rep0
     ctx.record_event(3)
     ctx.synchronize()
     D.barrier()
@@ -356,19 +402,30 @@ def run_ours(args, D: Dist):
                 "algorithmic_bytes_per_launch": int(bytes_per_launch),
                 "kernels": kernels}
 
+    # accuracy of the final state (after every timed and profiled batch):
+    # the FP64 residual of x on the final graph bounds ||x - x*||_1
+    import oracle
+    x = ctx.pr_values()
+    delta = ctx.pr_deltas()
+    fin = hg.csr()[:2]
+    res = oracle.pr_residual_l1(fin[0], fin[1], x)
+    accuracy = {"residual_l1": res, "l1_bound_vs_fixed_point": res / 0.15,
+                "tolerance": 1e-5, "within_tolerance": bool(res / 0.15 <= 1e-5),
+                "method": "||x - x*||_1 <= ||(1-d)/N + d P^T x - x||_1 / (1 - d), FP64 "
+                          "residual on the host over the final graph"}
     cpu = None
     if not args.no_cpu_baseline and D.rank == 0:
-        x = ctx.pr_values()
-        delta = ctx.pr_deltas()
-        old = hg.csr()[:2]
-        hg.gen_updates(bsz // 2, bsz - bsz // 2, 0, seed=99999)
-        new = hg.csr()[:2]
-        relax_c, dt = cpu_sample(old[0], old[1], new[0], new[1], x, delta, args.cpu_sample_rounds)
+        # one complete IncEval of the reference's worker restated on the host
+        # cores, from the GPU's converged state, on the next batch
+        upd = oracle.gen_updates(fin[0], fin[1], bsz // 2, bsz - bsz // 2, 0, seed=99999)
+        _, _, _, relax_c, dt, rc = cpu_inceval(fin, upd, x, delta)
         cpu = {"value": round(relax_c / dt / 1e9, 4), "unit": "GTEPS",
                "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": (f"one IncEval sample on the host: AmendValue(-1/+1) over the full "
-                          f"scale-{args.scale} graph + {args.cpu_sample_rounds} delta rounds "
-                          f"after a {bsz}-change batch ({dt:.1f} s)")}
+               "sample": (f"one complete IncEval on the host (batch apply + AmendValue(-1/+1) "
+                          f"over the scale-{args.scale} graph + {rc} delta rounds to "
+                          f"sum|delta| < 1e-6) after a {bsz}-change batch, from the GPU's "
+                          f"converged state ({dt:.1f} s)"),
+               "ms_per_step": round(dt * 1e3, 1)}
     ctx.close()
 
     result = {
@@ -385,6 +442,15 @@ def run_ours(args, D: Dist):
         "rounds_per_step": rounds,
         "activations_per_step": visits,
         "relaxations_per_step": int(relax / K),
+        "step_ms": {"value": [round(v, 3) for v in step_ms],
+                    "e2e": [round(v, 3) for v in step_e_ms],
+                    "inceval_only": [round(v, 3) for v in inc_ms],
+                    "value_median": round(statistics.median(step_ms), 3),
+                    "value_max": round(max(step_ms), 3),
+                    "e2e_median": round(statistics.median(step_e_ms), 3),
+                    "batches": {"value": [W, W + K - 1], "e2e": [W + K, W + 2 * K - 1]},
+                    "repacks": {"value": int(repacks_value), "e2e": int(repacks_e2e)}},
+        "accuracy": accuracy,
         "graph_gteps": round(E * K / (t_ms_max * 1e-3) / 1e9, 4),
         "peval": {"rounds": peval_stats["rounds"], "ms": round(peval_stats["elapsed_ms"], 3)},
         "roofline": roofline,

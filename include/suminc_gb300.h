@@ -101,6 +101,9 @@ typedef struct sg_stats {
   uint64_t edges_pull;      /* relaxations done by dense pull rounds         */
   uint64_t edges_push;      /* relaxations by push rounds (0: every PageRank
                                round is a dense pull)                       */
+  uint64_t repacks;         /* adjacency pool repacks since sg_reset_stats
+                               (a direction whose free tail could not hold a
+                               batch's worst case was rewritten)            */
 } sg_stats;
 
 /* kernel classes reported in sg_stats.kernel_ms / kernel_launches */
@@ -396,7 +399,11 @@ sg_status sg_adjoint_values(sg_ctx* ctx, float* x, float* lambda);
  * array's device address (cudaGetSymbolAddress) with that device current,
  * so make that first call before any stream capture.  Every call shares the
  * array: calls whose work overlaps on the GPU race and must be serialised
- * by the caller.  Returns SG_ERR_NOT_CONVERGED when max_rounds is reached. */
+ * by the caller.  Each round ends by reading two control words back to the
+ * host, which synchronises `stream`.  A CUDA error still pending from the
+ * caller's own work makes the call return SG_ERR_CUDA before it launches
+ * anything, and that error is left for the caller to collect.  Returns
+ * SG_ERR_NOT_CONVERGED when max_rounds is reached. */
 sg_status sg_pr_peval_noalloc(uint32_t n, uint64_t m, const uint64_t* d_row_ptr,
                               const uint32_t* d_col, double damping,
                               double threshold, int32_t max_rounds, void* stream,

@@ -50,6 +50,16 @@ def lib():
         L.or_sssp_inceval.argtypes = [C.c_uint32, P, P, P, P, P, C.c_uint64, P, P, C.c_int, P, P,
                                       C.POINTER(OrStats)]
         L.or_sssp_inceval.restype = C.c_int
+        L.or_rmat.argtypes = [C.c_int, C.c_uint64, C.c_double, C.c_double, C.c_double,
+                              C.c_uint64, C.c_int, C.c_double, C.c_double, P, P, P]
+        L.or_rmat.restype = C.c_int
+        L.or_gen_updates.argtypes = [C.c_uint32, P, P, C.c_uint64, C.c_uint64, C.c_uint64,
+                                     C.c_uint64, C.c_int, C.c_double, C.c_double, P]
+        L.or_gen_updates.restype = C.c_int
+        L.or_apply_updates.argtypes = [C.c_uint32, P, P, P, P, C.c_uint64, P, P, P]
+        L.or_apply_updates.restype = C.c_int
+        L.or_pr_residual_l1.argtypes = [C.c_uint32, P, P, C.c_double, P, C.POINTER(C.c_double)]
+        L.or_pr_residual_l1.restype = C.c_int
         _lib = L
     return _lib
 
@@ -154,3 +164,59 @@ def sssp_inceval(old, new, deleted, dist, parent, threads=0):
         raise ValueError("or_sssp_inceval: non-integer weights")
     return d, par, {k: getattr(st, k) for k, _ in OrStats._fields_}
 
+
+
+# update records: u32 src, u32 dst, f32 weight, u32 op (0 add, 1 delete)
+UPDATE_DTYPE = np.dtype([("src", "<u4"), ("dst", "<u4"), ("weight", "<f4"), ("op", "<u4")])
+
+
+def rmat(scale, edges, a=0.57, b=0.19, c=0.19, seed=1, weight_kind=0, wlo=1.0, whi=100.0):
+    """Seeded R-MAT graph (first `edges` distinct non-loop pairs of the draw
+    stream, rows sorted): (row_ptr u64, col u32, w f32 or None)."""
+    n = 1 << scale
+    rp = np.empty(n + 1, np.uint64)
+    col = np.empty(edges, np.uint32)
+    w = np.empty(edges, np.float32) if weight_kind else None
+    if lib().or_rmat(scale, edges, a, b, c, seed, weight_kind, wlo, whi, _p(rp), _p(col), _p(w)):
+        raise ValueError("or_rmat failed")
+    return rp, col, w
+
+
+def gen_updates(rp, col, n_ins, n_del, n_rew=0, seed=1, integer_weights=True, wlo=1.0,
+                whi=100.0):
+    """One update batch valid for the graph (rows sorted): deletes, re-weights
+    (delete + add), inserts, as UPDATE_DTYPE records."""
+    rp, col, _ = _csr(rp, col)
+    out = np.zeros(n_ins + n_del + 2 * n_rew, UPDATE_DTYPE)
+    if lib().or_gen_updates(len(rp) - 1, _p(rp), _p(col), n_ins, n_del, n_rew, seed,
+                            1 if integer_weights else 0, wlo, whi, _p(out)):
+        raise ValueError("or_gen_updates: sizes do not fit the graph")
+    return out
+
+
+def apply_updates(rp, col, w, upd):
+    """The graph after a batch, with the reference's update semantics:
+    (row_ptr, col, w or None)."""
+    rp, col, w = _csr(rp, col, w)
+    upd = np.ascontiguousarray(upd, UPDATE_DTYPE)
+    n = len(rp) - 1
+    rpn = np.empty(n + 1, np.uint64)
+    L = lib()
+    if L.or_apply_updates(n, _p(rp), _p(col), _p(w), _p(upd), len(upd), _p(rpn), None, None):
+        raise MemoryError("or_apply_updates")
+    coln = np.empty(int(rpn[-1]), np.uint32)
+    wn = np.empty(int(rpn[-1]), np.float32) if w is not None else None
+    if L.or_apply_updates(n, _p(rp), _p(col), _p(w), _p(upd), len(upd), _p(rpn), _p(coln),
+                          _p(wn)):
+        raise MemoryError("or_apply_updates")
+    return rpn, coln, wn
+
+
+def pr_residual_l1(rp, col, x, damping=0.85):
+    """|| (1-d)/N + d P^T x - x ||_1 in FP64; ||x - x*||_1 <= this / (1 - d)."""
+    rp, col, _ = _csr(rp, col)
+    x = np.ascontiguousarray(x, np.float32)
+    r = C.c_double()
+    if lib().or_pr_residual_l1(len(rp) - 1, _p(rp), _p(col), damping, _p(x), C.byref(r)):
+        raise MemoryError("or_pr_residual_l1")
+    return r.value

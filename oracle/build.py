@@ -1,4 +1,6 @@
-"""Builds the C oracle (test infrastructure) into oracle/_build/liboracle.so."""
+"""Builds the C oracle (test infrastructure) into oracle/_build/liboracle.so
+from oracle.c (the restated algorithms and FP64 solvers) and inputs.c (input
+generators, the batch semantics and the residual bound)."""
 from __future__ import annotations
 
 import os
@@ -15,12 +17,12 @@ def lib_path() -> str:
 
 def build(verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
-    src = os.path.join(HERE, "oracle.c")
+    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "inputs.c")]
     lib = lib_path()
-    if os.path.exists(lib) and os.path.getmtime(lib) >= os.path.getmtime(src):
+    if os.path.exists(lib) and os.path.getmtime(lib) >= max(os.path.getmtime(s) for s in srcs):
         return lib
-    cmd = ["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=c11",
-           src, "-o", lib, "-lm"]
+    cmd = ["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=gnu11",
+           *srcs, "-o", lib, "-lm"]
     p = subprocess.run(cmd, capture_output=True, text=True)
     if verbose or p.returncode:
         sys.stderr.write(p.stdout + p.stderr)

@@ -8,6 +8,9 @@ compiled: the harness runs the CPU path (-gpu_start=0) and the CUDA shim
 entry points are linked as no-ops (stubs/cuda_shim.cc).  Needs the reference
 checkout, g++ and the CUDA runtime library; the reference's build system
 (cmake, gcc-7 / Cilk Plus, MPI, glog, gflags) is not used.
+
+The checkout's location comes from --reference PATH or the SUMINC_REFERENCE
+environment variable; without either nothing is built.
 """
 from __future__ import annotations
 
@@ -16,13 +19,18 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("SUMINC_REFERENCE", "/root/reference")
+REF = os.environ.get("SUMINC_REFERENCE", "")
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
 CUDA = "/usr/local/cuda"
 
 
+def set_reference(path: str) -> None:
+    global REF
+    REF = path
+
+
 def build(verbose: bool = False) -> str | None:
-    if not os.path.isdir(REF):
+    if not REF or not os.path.isdir(REF):
         return None
     os.makedirs(OUT, exist_ok=True)
     exe = os.path.join(OUT, "ref_driver")
@@ -53,7 +61,7 @@ def build(verbose: bool = False) -> str | None:
 def check_adaptor(verbose: bool = False) -> bool | None:
     """Compiles adaptor_check.cc (the C++ workers over the reference's own
     fragment and app types) with -fsyntax-only; None without the checkout."""
-    if not os.path.isdir(REF):
+    if not REF or not os.path.isdir(REF):
         return None
     stubs = os.path.join(HERE, "stubs")
     repo = os.path.dirname(os.path.dirname(HERE))
@@ -71,4 +79,6 @@ def check_adaptor(verbose: bool = False) -> bool | None:
 
 
 if __name__ == "__main__":
+    if "--reference" in sys.argv:
+        set_reference(sys.argv[sys.argv.index("--reference") + 1])
     print(build(verbose=True))

@@ -153,6 +153,7 @@ class Stats(C.Structure):
         ("launches_total", C.c_uint64),
         ("edges_pull", C.c_uint64),
         ("edges_push", C.c_uint64),
+        ("repacks", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:

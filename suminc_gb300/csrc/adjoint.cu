@@ -247,7 +247,7 @@ sg_status pr_adjoint(sg_ctx* ctx, const float* dl_dx_host, bool on_device, float
   if (dl_dt) SG_CUDA(ctx, cudaMemcpyAsync(dl_dt, S.dt, 4ull * n, cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, e0, e1);
+  SG_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
   S.info.adjoint_ms = ms;
   S.info.gradient_edges = m;
   S.adj_valid = true;

@@ -1191,7 +1191,7 @@ sg_status batch_run(sg_ctx* ctx, const sg_batch_spec* spec, float* ppr_out, doub
   SG_CUDA(ctx, cudaMemcpyAsync(h_cnt, B.cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   B.nq = nq;
   B.ns = ns;
   B.qw = qw;

@@ -194,6 +194,7 @@ sg_status sg_get_stats(const sg_ctx* ctx, sg_stats* out) {
   if (!ctx || !out) return SG_ERR_INVALID;
   *out = ctx->stats;
   out->launches_total = ctx->launches;
+  out->repacks = ctx->repacks;
   return SG_OK;
 }
 
@@ -237,6 +238,7 @@ sg_status sg_reset_stats(sg_ctx* ctx) {
   kprof_flush(ctx);
   std::memset(&ctx->stats, 0, sizeof(ctx->stats));
   ctx->launches = 0;
+  ctx->repacks = 0;
   return SG_OK;
 }
 

@@ -191,6 +191,7 @@ struct sg_ctx {
   size_t kused = 0;
   int kopen = -1;
   uint64_t launches = 0;  // kernels launched by the library (all classes)
+  uint64_t repacks = 0;   // adjacency pool repacks since the last stats reset
   void* cub_tmp = nullptr;
   size_t cub_tmp_bytes = 0;
   int num_sms = 0;

@@ -908,6 +908,7 @@ static sg_status repack_direction(sg_ctx* ctx, DevCSR& c, uint64_t batch_need) {
   c.w = w_new;
   c.pool_cap = pool;
   count_launch(ctx, 4);
+  ctx->repacks++;
   return SG_OK;
 }
 

@@ -126,6 +126,10 @@ extern "C" sg_status sg_pr_peval_noalloc(uint32_t n, uint64_t m, const uint64_t*
     return SG_ERR_INVALID;
   if (n > kMaxVertices) return SG_ERR_TOO_LARGE;
   if (!(damping > 0.0 && damping < 1.0) || !(threshold > 0.0)) return SG_ERR_INVALID;
+  // an error the caller has not collected yet is left in place for the
+  // caller, and nothing is launched on top of it; every error seen below is
+  // then this call's own
+  if (cudaPeekAtLastError() != cudaSuccess) return SG_ERR_CUDA;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
     cudaGetLastError();

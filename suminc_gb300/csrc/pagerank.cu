@@ -704,7 +704,7 @@ sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R) {
   SG_CUDA(ctx, cudaMemcpyAsync(h_misc, s.misc, sizeof(h_misc), cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   ctx->stats.rounds = (int32_t)h_misc[M_ROUNDS] + 1;
   ctx->stats.converged = h_misc[M_NOTCONV] ? 0 : 1;
   ctx->stats.residual = h_res[R_ACC];

@@ -341,7 +341,11 @@ sg_status summarized_stage(sg_ctx* ctx, const PullArgs& A, uint32_t* rounds) {
   uint32_t h[P_WORDS] = {0, 0, 0, 0};
   int launched = 0;
   const int cap = kStepCap + 2;
-  const unsigned blocks = std::max(1u, std::min(P.nblocks, (A.V.n_act + kPT - 1) / kPT + A.V.n_long / (kPT / 32)));
+  // a lane per short row and a warp per long row (long rows are listed first;
+  // on a hub-dominated summary the long rows get their own warps even when
+  // there are fewer than a block's worth of them)
+  const unsigned blocks = std::max(
+      1u, std::min(P.nblocks, (A.V.n_act + kPT - 1) / kPT + (A.V.n_long + kPT / 32 - 1) / (kPT / 32)));
   while (launched < cap) {
     kprof_begin(ctx);
     int c = 0;
@@ -427,7 +431,7 @@ sg_status pr_pull_worker(sg_ctx* ctx, bool inc) {
   SG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   // the plain stage: the library's dense pull rounds from this state
   s.valid = true;
   const sg_status stt = pr_run(ctx, true);

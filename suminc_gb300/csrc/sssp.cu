@@ -1074,7 +1074,7 @@ sg_status sssp_run_peval(sg_ctx* ctx, uint32_t source) {
   SG_CUDA(ctx, cudaMemcpyAsync(h_cnt, s.d_cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   fill_stats(ctx, h_cnt);
   ctx->stats.elapsed_ms = ms;
   ctx->stats.rounds = 0;
@@ -1267,7 +1267,7 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
   SG_CUDA(ctx, cudaMemcpyAsync(h_cnt, s.d_cnt, sizeof(h_cnt), cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   fill_stats(ctx, h_cnt);
   ctx->stats.elapsed_ms = ms;
   ctx->stats.converged = 1;

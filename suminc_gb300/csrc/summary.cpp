@@ -45,8 +45,17 @@ struct Rng {
   uint64_t next() { return mix64(key + (ctr++)); }
 };
 
-bool contains(const std::set<uint32_t>& s, uint32_t v) { return s.find(v) != s.end(); }
-
+// Membership of the find's sets P (cluster), S (vertices with in-edges from
+// outside), B (vertices with out-edges to outside) and the visited marks are
+// vertex-indexed stamps equal to the find's number, and every vertex touched
+// by P keeps two counters: its in-edge entries from P and its out-edge
+// entries into P, updated when a vertex joins P.  The score of a candidate d
+// then needs no scan of the in-rows of its out-neighbours (or the out-rows of
+// its in-neighbours): "every in-edge of o comes from P or from d" is
+// in_deg(o) - (entries from P) - (entries from d) == 0.  The ordered sets
+// are kept as std::set for their iteration order, which decides the cluster
+// member order and the tie-breaking of the reference.  Scores, samples and
+// clusters are the same as with a scan of the adjacency.
 struct Greedy {
   const HostAdj& out;
   const HostAdj& in;
@@ -54,58 +63,102 @@ struct Greedy {
   std::vector<int32_t> Fc;
   std::vector<std::vector<uint32_t>> clusters;
   Rng rng;
+  uint32_t epoch = 0;
+  std::vector<uint32_t> st_p, st_s, st_b, st_vis, st_cnt;
+  std::vector<uint32_t> c_in_p, c_out_p;
 
   Greedy(const HostAdj& o, const HostAdj& i, int mx, uint64_t seed)
-      : out(o), in(i), max_node_num(mx), Fc(o.n, Summary::kFcDefault), rng(seed) {}
+      : out(o), in(i), max_node_num(mx), Fc(o.n, Summary::kFcDefault), rng(seed),
+        st_p(o.n, 0), st_s(o.n, 0), st_b(o.n, 0), st_vis(o.n, 0), st_cnt(o.n, 0),
+        c_in_p(o.n, 0), c_out_p(o.n, 0) {}
 
-  float check_score(uint32_t d, const std::set<uint32_t>& S, const std::set<uint32_t>& P,
-                    const std::set<uint32_t>& B, uint32_t inner, bool& is_s, bool& is_b,
-                    uint32_t& temp_inner, std::vector<uint32_t>& tS, std::vector<uint32_t>& tB) {
-    is_s = false;
-    is_b = false;
-    temp_inner = inner;
-    tS.clear();
-    tB.clear();
-    std::set<uint32_t> setS, setB;
-    uint32_t now_s = (uint32_t)S.size(), now_b = (uint32_t)B.size();
+  bool in_p(uint32_t v) const { return st_p[v] == epoch; }
+  bool in_s(uint32_t v) const { return st_s[v] == epoch; }
+  bool in_b(uint32_t v) const { return st_b[v] == epoch; }
+  uint64_t cin(uint32_t v) const { return st_cnt[v] == epoch ? c_in_p[v] : 0; }
+  uint64_t cout(uint32_t v) const { return st_cnt[v] == epoch ? c_out_p[v] : 0; }
+  void touch(uint32_t v) {
+    if (st_cnt[v] != epoch) {
+      st_cnt[v] = epoch;
+      c_in_p[v] = 0;
+      c_out_p[v] = 0;
+    }
+  }
+  // entries equal to x in the (sorted) row of v
+  static uint64_t mult(const HostAdj& a, uint32_t v, uint32_t x) {
+    const uint32_t* b = a.col.data() + a.rp[v];
+    const uint32_t* e = a.col.data() + a.rp[v + 1];
+    const auto r = std::equal_range(b, e, x);
+    return (uint64_t)(r.second - r.first);
+  }
+  void join(uint32_t d, std::set<uint32_t>& P) {
+    P.insert(d);
+    st_p[d] = epoch;
     for (uint64_t e = out.rp[d]; e < out.rp[d + 1]; ++e) {
-      const uint32_t o = out.col[e];
-      if (contains(S, o)) {
-        bool flag = true;
-        for (uint64_t f = in.rp[o]; f < in.rp[o + 1]; ++f) {
-          const uint32_t x = in.col[f];
-          if (!contains(P, x) && x != d) {
-            flag = false;
-            break;
-          }
-        }
-        if (flag) setS.insert(o);
-      }
-      if (!contains(P, o) && o != d) is_b = true;
-      else temp_inner += 1;
+      touch(out.col[e]);
+      c_in_p[out.col[e]]++;
     }
     for (uint64_t e = in.rp[d]; e < in.rp[d + 1]; ++e) {
-      const uint32_t i = in.col[e];
-      if (contains(B, i)) {
-        bool flag = true;
-        for (uint64_t f = out.rp[i]; f < out.rp[i + 1]; ++f) {
-          const uint32_t x = out.col[f];
-          if (!contains(P, x) && x != d) {
-            flag = false;
-            break;
-          }
-        }
-        if (flag) setB.insert(i);
-      }
-      if (contains(P, i)) temp_inner++;
-      else is_s = true;
+      touch(in.col[e]);
+      c_out_p[in.col[e]]++;
     }
-    now_s -= (uint32_t)setS.size();
-    now_b -= (uint32_t)setB.size();
+  }
+  void s_insert(std::set<uint32_t>& S, uint32_t v) { S.insert(v); st_s[v] = epoch; }
+  void s_erase(std::set<uint32_t>& S, uint32_t v) { S.erase(v); st_s[v] = 0; }
+  void b_insert(std::set<uint32_t>& B, uint32_t v) { B.insert(v); st_b[v] = epoch; }
+  void b_erase(std::set<uint32_t>& B, uint32_t v) { B.erase(v); st_b[v] = 0; }
+
+  // Members x of `set` (ascending) adjacent to d in `adj` row d whose rows in
+  // `other` hold no entry outside P other than d: by the set when it is much
+  // shorter than d's row, else by a pass over the row (sorted, so the result
+  // is ascending either way).
+  template <typename InSet, typename Count>
+  void closed_members(uint32_t d, const HostAdj& adj, const HostAdj& other,
+                      const std::set<uint32_t>& set, InSet member, Count from_p,
+                      std::vector<uint32_t>& res) const {
+    res.clear();
+    if (set.empty()) return;
+    const uint64_t b = adj.rp[d], e = adj.rp[d + 1];
+    if ((uint64_t)set.size() * 8 < e - b) {
+      for (uint32_t x : set) {
+        const uint64_t m = mult(adj, d, x);
+        if (m && other.deg(x) - from_p(x) - m == 0) res.push_back(x);
+      }
+      return;
+    }
+    for (uint64_t k = b; k < e;) {
+      const uint32_t x = adj.col[k];
+      uint64_t r = k + 1;
+      while (r < e && adj.col[r] == x) ++r;
+      if (member(x) && other.deg(x) - from_p(x) - (r - k) == 0) res.push_back(x);
+      k = r;
+    }
+  }
+
+  // compressor_base.h:1364-1440 (check_score): inner edges after adding d
+  // minus |S'| x |B'|
+  float check_score(uint32_t d, const std::set<uint32_t>& S, const std::set<uint32_t>& B,
+                    uint32_t inner, bool& is_s, bool& is_b, uint32_t& temp_inner,
+                    std::vector<uint32_t>& tS, std::vector<uint32_t>& tB) const {
+    temp_inner = inner;
+    // out-edges of d: into P or back to d are inner, any other makes d a B member
+    const uint64_t inner_out = cout(d) + mult(out, d, d);
+    temp_inner += (uint32_t)inner_out;
+    is_b = out.deg(d) > inner_out;
+    // in-edges of d: from P are inner, any other makes d an S member
+    const uint64_t inner_in = cin(d);
+    temp_inner += (uint32_t)inner_in;
+    is_s = in.deg(d) > inner_in;
+    // S members d points to whose in-edges then all come from P or d leave S;
+    // B members pointing to d whose out-edges all go to P or d leave B
+    closed_members(d, out, in, S, [&](uint32_t x) { return in_s(x); },
+                   [&](uint32_t x) { return cin(x); }, tS);
+    closed_members(d, in, out, B, [&](uint32_t x) { return in_b(x); },
+                   [&](uint32_t x) { return cout(x); }, tB);
+    uint32_t now_s = (uint32_t)S.size() - (uint32_t)tS.size();
+    uint32_t now_b = (uint32_t)B.size() - (uint32_t)tB.size();
     if (is_s) now_s++;
     if (is_b) now_b++;
-    tS.assign(setS.begin(), setS.end());
-    tB.assign(setB.begin(), setB.end());
     return (float)(temp_inner * 1.0 - (double)(uint32_t)(now_s * now_b));
   }
 
@@ -122,32 +175,37 @@ struct Greedy {
     }
   }
 
+  void push_neighbours(uint32_t u, CandidateQueue& D, uint64_t try_max_node) {
+    if (out.deg(u) >= try_max_node) return;
+    for (uint64_t e = out.rp[u]; e < out.rp[u + 1]; ++e) {
+      const uint32_t v = out.col[e];
+      if (Fc[v] == Summary::kFcDefault && !in_p(v) && st_vis[v] != epoch) {
+        D.push(v);
+        st_vis[v] = epoch;
+      }
+    }
+  }
+
   void find(uint32_t source, int now_min) {
     const uint64_t try_max_node = (uint64_t)max_node_num * 1000;
     const int try_max_step = max_node_num * 1000;
     const uint32_t sample_size = 32;
     const int try_sample_cnt = 3;
-    std::set<uint32_t> S, P, B, visited;
+    ++epoch;
+    std::set<uint32_t> S, P, B;
     CandidateQueue D;
     if (Fc[source] == Summary::kFcDefault) {
-      P.insert(source);
-      visited.insert(source);
-      if (out.deg(source) < try_max_node)
-        for (uint64_t e = out.rp[source]; e < out.rp[source + 1]; ++e) {
-          const uint32_t v = out.col[e];
-          if (Fc[v] == Summary::kFcDefault && !contains(P, v) && !contains(visited, v)) {
-            D.push(v);
-            visited.insert(v);
-          }
-        }
+      join(source, P);
+      st_vis[source] = epoch;
+      push_neighbours(source, D, try_max_node);
     }
     uint32_t inner_edge_num = 0;
     for (uint32_t u : P) {
       bool f = true;
       for (uint64_t e = out.rp[u]; e < out.rp[u + 1]; ++e) {
-        if (!contains(P, out.col[e])) {
+        if (!in_p(out.col[e])) {
           if (f) {
-            B.insert(u);
+            b_insert(B, u);
             f = false;
           }
         } else {
@@ -155,8 +213,8 @@ struct Greedy {
         }
       }
       for (uint64_t e = in.rp[u]; e < in.rp[u + 1]; ++e)
-        if (!contains(P, in.col[e])) {
-          S.insert(u);
+        if (!in_p(in.col[e])) {
+          s_insert(S, u);
           break;
         }
     }
@@ -181,8 +239,8 @@ struct Greedy {
         for (int i = 0; i < real; ++i) {
           bool is_s, is_b;
           uint32_t ti;
-          scores[i] = check_score(D.data[smp[i]], S, P, B, inner_edge_num, is_s, is_b, ti,
-                                  tS_vec[i], tB_vec[i]);
+          scores[i] = check_score(D.data[smp[i]], S, B, inner_edge_num, is_s, is_b, ti, tS_vec[i],
+                                  tB_vec[i]);
           is_s_vec[i] = is_s;
           is_b_vec[i] = is_b;
           inner_vec[i] = ti;
@@ -204,20 +262,13 @@ struct Greedy {
         cnt++;
       }
       if (!found) break;
-      if (is_b_vec[max_id]) B.insert(d);
-      for (uint32_t v : tB_vec[max_id]) B.erase(v);
-      if (is_s_vec[max_id]) S.insert(d);
-      for (uint32_t v : tS_vec[max_id]) S.erase(v);
+      if (is_b_vec[max_id]) b_insert(B, d);
+      for (uint32_t v : tB_vec[max_id]) b_erase(B, v);
+      if (is_s_vec[max_id]) s_insert(S, d);
+      for (uint32_t v : tS_vec[max_id]) s_erase(S, v);
       inner_edge_num = inner_vec[max_id];
-      P.insert(d);
-      if (out.deg(d) < try_max_node)
-        for (uint64_t e = out.rp[d]; e < out.rp[d + 1]; ++e) {
-          const uint32_t v = out.col[e];
-          if (Fc[v] == Summary::kFcDefault && !contains(P, v) && !contains(visited, v)) {
-            D.push(v);
-            visited.insert(v);
-          }
-        }
+      join(d, P);
+      push_neighbours(d, D, try_max_node);
     }
     if (P.size() >= (size_t)now_min) {
       if (S.empty()) S.insert(source);
@@ -228,7 +279,6 @@ struct Greedy {
     }
   }
 };
-
 }  // namespace
 
 std::vector<std::vector<uint32_t>> greedy_clusters(const HostAdj& out, const HostAdj& in,

@@ -1256,7 +1256,7 @@ sg_status pr_summarized(sg_ctx* ctx, bool inc) {
   SG_CUDA(ctx, cudaMemcpyAsync(hc, cnt, 16, cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   float ms_sum = 0.f;
-  cudaEventElapsedTime(&ms_sum, ctx->ev0, ctx->ev1);
+  SG_CUDA(ctx, cudaEventElapsedTime(&ms_sum, ctx->ev0, ctx->ev1));
   dfree(cnt);
   // the plain rounds finish the residual on the original graph
   s.valid = true;
@@ -1923,7 +1923,7 @@ sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
   SG_CUDA(ctx, cudaEventRecord(ctx->kev1, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, ctx->kev0, ctx->kev1);
+  SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->kev0, ctx->kev1));
   dfree(dist);
   return sssp_finish_external(ctx, h_cnt, ms);
 }

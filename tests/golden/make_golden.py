@@ -3,8 +3,9 @@
 reference's own CPU workers (built by oracle/ref_harness/build_ref.py from
 the reference checkout) on seeded inputs.
 
-Run here, where the reference checkout exists:
-    python tests/golden/make_golden.py
+Run where a reference checkout exists, naming it:
+    python tests/golden/make_golden.py --reference PATH
+(or with SUMINC_REFERENCE=PATH in the environment).
 Each case writes <case>.npz with:
   params        json: generator parameters and reference flags
   input_sha256  hash of the (row_ptr, col, weights) the case was run on
@@ -269,6 +270,8 @@ def make_pull(exe):
 def main():
     sys.path.insert(0, os.path.join(ROOT, "oracle", "ref_harness"))
     import build_ref
+    if "--reference" in sys.argv:
+        build_ref.set_reference(sys.argv[sys.argv.index("--reference") + 1])
     exe = build_ref.build()
     if exe is None:
         raise SystemExit("reference checkout or harness build unavailable")

@@ -1,6 +1,7 @@
 """The oracle restatement agrees with its own FP64 solvers and with the
 reference semantics it restates."""
 import numpy as np
+import pytest
 
 import oracle
 import suminc_gb300 as sg
@@ -98,3 +99,61 @@ def test_oracle_adjoint_matches_central_differences():
     tm = tele.copy(); tm[v] -= h
     fd = (loss(w, tp)[0] - loss(w, tm)[0]) / (2 * h)
     assert abs(0.15 * lam[v] - fd) <= 1e-6 * abs(fd) + 1e-12
+
+
+@pytest.mark.parametrize("scale,kind", [(12, 0), (12, 1), (12, 2), (16, 0), (16, 1)])
+def test_oracle_rmat_equals_library_host_generator(scale, kind):
+    """The oracle's R-MAT restatement (no library code) gives the same graph
+    and weights as the library's host twin of its device generator."""
+    lo, hi = (0.1, 1.0) if kind == 2 else (1.0, 100.0)
+    a = sg.rmat_host(scale, 16 << scale, seed=5, weight_kind=kind, wlo=lo, whi=hi)
+    b = oracle.rmat(scale, 16 << scale, seed=5, weight_kind=kind, wlo=lo, whi=hi)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    if kind:
+        assert np.array_equal(a[2], b[2])
+
+
+def test_oracle_updates_equal_library_batches_and_reference_semantics():
+    """Batches drawn by the oracle equal the library's HostGraph batches on the
+    same graph and seed; the oracle's apply equals the pure-Python restatement
+    of the reference's update semantics and the library's mirror."""
+    rp, col, w = sg.rmat_host(12, 16 << 12, seed=1, weight_kind=1)
+    hg = sg.HostGraph(rp, col, w)
+    cur = (rp, col, w)
+    for i in range(3):
+        u_lib = hg.gen_updates(300, 200, 100, seed=10 + i)
+        u_or = oracle.gen_updates(cur[0], cur[1], 300, 200, 100, seed=10 + i)
+        assert np.array_equal(u_lib, u_or)
+        nxt = oracle.apply_updates(*cur, u_or)
+        ref = oracle.apply_updates_reference(*cur, u_or)
+        assert all(np.array_equal(a, b) for a, b in zip(nxt, ref))
+        assert all(np.array_equal(a, b) for a, b in zip(nxt, hg.csr()))
+        cur = nxt
+
+
+def test_apply_updates_edge_cases():
+    # 0->1, 0->2, 1->2; batch: delete absent 2->0, add existing 0->1 (new
+    # weight), two adds of 1->0 (the first wins), delete + add of 1->2
+    rp = np.array([0, 2, 3, 3], np.uint64)
+    col = np.array([1, 2, 2], np.uint32)
+    w = np.array([5, 6, 7], np.float32)
+    upd = np.array([(2, 0, 0, 1), (0, 1, 9, 0), (1, 0, 3, 0), (1, 0, 4, 0), (1, 2, 0, 1),
+                    (1, 2, 8, 0)], dtype=oracle.UPDATE_DTYPE)
+    nrp, ncol, nw = oracle.apply_updates(rp, col, w, upd)
+    assert nrp.tolist() == [0, 2, 4, 4]
+    assert ncol.tolist() == [1, 2, 0, 2] and nw.tolist() == [9, 6, 3, 8]
+    ref = oracle.apply_updates_reference(rp, col, w, upd)
+    assert all(np.array_equal(a, b) for a, b in zip((nrp, ncol, nw), ref))
+    e = oracle.apply_updates(rp, col, w, np.zeros(0, oracle.UPDATE_DTYPE))
+    assert all(np.array_equal(a, b) for a, b in zip(e, (rp, col, w)))
+
+
+def test_residual_bound_holds():
+    """||x - x*||_1 <= residual / (1 - d) for the delta iteration's result."""
+    rp, col, _ = sg.rmat_host(12, 16 << 12, seed=4)
+    xf = oracle.pr_fixed_point(rp, col)
+    for tau in (1e-4, 1e-6):
+        x, _, _ = oracle.ingress_pr(rp, col, tau=tau)
+        bound = oracle.pr_residual_l1(rp, col, x) / 0.15
+        assert np.abs(x - xf).sum() <= bound * (1 + 1e-9) + 1e-12
+    assert oracle.pr_residual_l1(rp, col, xf.astype(np.float32)) < 1e-7
