@@ -52,10 +52,10 @@ struct PullLists {
 // (their push values are gathered most often) and a copy of the in-CSR
 // column pool in which a hub's id is replaced by 0x80000000 | its slot.
 struct HubView {
-  uint32_t* ids = nullptr;   // [k] hub of each slot, ascending ids
-  uint32_t* slot = nullptr;  // [n] slot of each vertex, ~0u if none
-  uint32_t* col = nullptr;   // [cap] encoded copy of the in-CSR col pool
-  uint32_t k = 0;
+  uint32_t* rank = nullptr;  // [n] position of each vertex in the pull's vertex
+                             // order (out-degree descending, ties by id)
+  uint32_t* col = nullptr;   // [cap] in-CSR col pool with ids replaced by ranks
+  uint32_t k = 0;            // hubs: ranks below k live in shared memory
   uint32_t kmax = 0;         // the cap the set was chosen under
   bool chosen = false;
   uint64_t cap = 0;

@@ -172,6 +172,10 @@ sg_status cub_sort_pairs_u64_u32(sg_ctx* ctx, const uint64_t* kin, uint64_t* kou
                                  const uint32_t* vin, uint32_t* vout, uint64_t n) {
   return sort_pairs(ctx, kin, kout, vin, vout, n);
 }
+sg_status cub_sort_pairs_u32_u32(sg_ctx* ctx, const uint32_t* kin, uint32_t* kout,
+                                 const uint32_t* vin, uint32_t* vout, uint64_t n) {
+  return sort_pairs(ctx, kin, kout, vin, vout, n);
+}
 
 static void csr_free(DevCSR& c) {
   dfree(c.off);
@@ -189,8 +193,7 @@ sg_status graph_free(sg_ctx* ctx) {
   csr_free(g.in);
   pull_lists_free(g.in_wl);
   pull_lists_free(g.out_wl);
-  dfree(g.hub.ids);
-  dfree(g.hub.slot);
+  dfree(g.hub.rank);
   dfree(g.hub.col);
   const uint64_t gen = g.gen;  // generations keep growing across graphs
   g = DevGraph();
@@ -958,9 +961,9 @@ struct ApplyDirArgs {
   uint32_t* sp_seeds;
   uint32_t* sp_seed_count;
   // the PageRank pull's encoded column copy (in direction; null when none
-  // is current): every column write is mirrored there, hubs encoded
+  // is current): every column write is mirrored there as the id's rank
   uint32_t* col2;
-  const uint32_t* hub_slot;
+  const uint32_t* hub_rank;
   uint32_t n;
   // bookkeeping
   unsigned long long* d_dm;  // signed edge-count change (two's complement)
@@ -970,10 +973,7 @@ struct ApplyDirArgs {
 // a column write, mirrored into the encoded copy when there is one
 __device__ __forceinline__ void put_col(const ApplyDirArgs& A, uint64_t p, uint32_t x) {
   A.c.col[p] = x;
-  if (A.col2) {
-    const uint32_t h = x < A.n ? A.hub_slot[x] : ~0u;
-    A.col2[p] = h != ~0u ? (0x80000000u | h) : x;
-  }
+  if (A.col2) A.col2[p] = x < A.n ? A.hub_rank[x] : x;
 }
 
 __device__ __forceinline__ uint32_t act_at(const ApplyDirArgs& A, uint32_t j) {
@@ -1366,9 +1366,9 @@ sg_status apply_updates_device(sg_ctx* ctx, uint64_t count, const sg_update* upd
   const HubView& hv = g.hub;
   const bool patch_view = hv.col && hv.k > 0 && hv.gen == g.gen && hv.layout == g.in.layout &&
                           hv.cap == g.in.pool_cap;
-  A.col2 = nullptr; A.hub_slot = nullptr; A.n = g.n;
+  A.col2 = nullptr; A.hub_rank = nullptr; A.n = g.n;
   I.col2 = patch_view ? hv.col : nullptr;
-  I.hub_slot = patch_view ? hv.slot : nullptr;
+  I.hub_rank = patch_view ? hv.rank : nullptr;
   I.n = g.n;
   // work items: ceil(degree / chunk) per group and direction
   k_apply_chunks<<<grid_for(A.n_grp + 1, 256), 256, 0, ctx->stream>>>(A, B.nch);

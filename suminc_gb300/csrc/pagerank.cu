@@ -61,6 +61,8 @@ struct PrArgs {
   float* delta;
   float* pv0;       // push values of the first round
   float* pvb[2];    // push values of later rounds, by pull parity
+  const uint32_t* rank;  // push values are indexed by rank[v] (the pull's
+                         // vertex order); null: by v
   uint32_t* misc;
   double* res;
   unsigned long long* cnt;
@@ -70,19 +72,20 @@ struct PrArgs {
 __device__ __forceinline__ uint32_t activate(const PrArgs& A, uint32_t v, float dl, float* pv_next,
                                              double& res) {
   res += fabs((double)dl);
+  const uint32_t r = A.rank ? A.rank[v] : v;
   if (fabsf(dl) > A.thr_v) {
     A.x[v] += dl;
     A.delta[v] = 0.f;
     if (A.scale_deg) {
       const uint32_t od = A.scale_deg[v];
-      pv_next[v] = od > 0 ? A.damping * dl / (float)od : 0.f;
+      pv_next[r] = od > 0 ? A.damping * dl / (float)od : 0.f;
     } else {
-      pv_next[v] = A.damping * dl;
+      pv_next[r] = A.damping * dl;
     }
     return 1;
   }
   A.delta[v] = dl;
-  pv_next[v] = 0.f;
+  pv_next[r] = 0.f;
   return 0;
 }
 
@@ -136,15 +139,18 @@ struct WarpPullArgs {
   uint64_t ntiles;
   const uint32_t* col;
   const float* w;
-  const uint32_t* hub_ids;  // hub cache: vertex of each slot (HUB kernels)
-  uint32_t nhub;
+  uint32_t nhub;            // hub cache: ranks below nhub (HUB kernels)
 };
 
-// Hub cache: the pull gathers the push value of every in-neighbour, and the
-// vertices with the highest out-degree take a large share of those gathers
-// (R-MAT scale 24: the top 13,312 of 16.8 M vertices take 27 %).  A CTA
-// copies their push values into shared memory once per launch and the pull
-// reads an encoded column copy in which a hub's id is 0x80000000 | slot.
+// Hub cache and vertex order: the pull gathers the push value of every
+// in-neighbour, and the vertices with the highest out-degree take a large
+// share of those gathers (R-MAT scale 24: the top 13,312 of 16.8 M vertices
+// take 27 %).  The HUB kernels index push values by rank (vertices sorted by
+// out-degree, highest first) and read an encoded column copy that holds the
+// ranks of the in-neighbours.  A CTA copies the push values of the lowest
+// ranks (the hubs) into shared memory once per launch; the next ranks are
+// contiguous in memory, so the L1 and L2 lines they occupy hold hot values
+// only (in vertex-id order a line of 32 push values holds one or two).
 // 1024 threads, two CTAs per SM.  Shared memory comes out of the same array
 // as L1, which the other gathers need: at scale 24 the pull takes 1.12 ms
 // without the cache, 1.05 ms with 2,048 hubs, 0.995 ms with 12,288 (48 KB per
@@ -172,12 +178,12 @@ __global__ void __launch_bounds__(HUB ? kHubThreads : PT_THREADS, HUB ? 2 : 8)
   const float* __restrict__ pv = p == 0 ? A.pv0 : ((p & 1) ? A.pvb[1] : A.pvb[0]);
   float* pv_next = (p & 1) ? A.pvb[0] : A.pvb[1];
   if (HUB) {
-    for (uint32_t h = threadIdx.x; h < P.nhub; h += NT) s_hub[h] = pv[P.hub_ids[h]];
+    for (uint32_t h = threadIdx.x; h < P.nhub; h += NT) s_hub[h] = pv[h];
     __syncthreads();
   }
-  // a column is a vertex id, or with the hub cache 0x80000000 | slot
+  // a column is a vertex id, or with the hub cache a rank
   auto gather = [&](uint32_t c) -> float {
-    if (HUB && (c & 0x80000000u)) return s_hub[c & 0x7fffffffu];
+    if (HUB && c < P.nhub) return s_hub[c];
     return pv[c];
   };
   const uint32_t lane = threadIdx.x & 31;
@@ -281,28 +287,28 @@ __global__ void k_count_deg_ge(const uint32_t* __restrict__ deg, uint32_t n, uin
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(cnt, (unsigned long long)c);
 }
 
-__global__ void k_flag_deg_ge(const uint32_t* __restrict__ deg, uint32_t n, uint32_t d,
-                              uint8_t* __restrict__ f, uint32_t* __restrict__ iota) {
+// sort keys: out-degree descending (complemented), values: vertex ids
+__global__ void k_rank_keys(const uint32_t* __restrict__ deg, uint32_t n, uint32_t* __restrict__ key,
+                            uint32_t* __restrict__ iota) {
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-    f[v] = deg[v] >= d;
+    key[v] = ~deg[v];
     iota[v] = v;
   }
 }
 
-__global__ void k_hub_slots(const uint32_t* __restrict__ ids, uint32_t k, uint32_t* __restrict__ slot) {
-  for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < k; h += gridDim.x * blockDim.x)
-    slot[ids[h]] = h;
+__global__ void k_rank_scatter(const uint32_t* __restrict__ order, uint32_t n, uint32_t* __restrict__ rank) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    rank[order[i]] = i;
 }
 
-// encoded column copy: hubs as 0x80000000 | slot, other entries unchanged
+// encoded column copy: every live id replaced by its rank
 __global__ void k_hub_encode(const uint32_t* __restrict__ col, uint64_t cap,
-                             const uint32_t* __restrict__ slot, uint32_t n,
+                             const uint32_t* __restrict__ rank, uint32_t n,
                              uint32_t* __restrict__ out) {
   for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < cap;
        e += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t c = col[e];
-    const uint32_t h = c < n ? slot[c] : ~0u;
-    out[e] = h != ~0u ? (0x80000000u | h) : c;
+    out[e] = c < n ? rank[c] : c;
   }
 }
 
@@ -311,7 +317,7 @@ __global__ void k_hub_encode(const uint32_t* __restrict__ col, uint64_t cap,
 __global__ void __launch_bounds__(256) k_hub_encode_rows(const uint64_t* __restrict__ off,
                                                          const uint32_t* __restrict__ deg,
                                                          const uint32_t* __restrict__ col,
-                                                         const uint32_t* __restrict__ slot, uint32_t n,
+                                                         const uint32_t* __restrict__ rank, uint32_t n,
                                                          const uint32_t* __restrict__ rows,
                                                          uint64_t nrows, uint32_t* __restrict__ out) {
   for (uint64_t r = blockIdx.x; r < nrows; r += gridDim.x) {
@@ -319,14 +325,13 @@ __global__ void __launch_bounds__(256) k_hub_encode_rows(const uint64_t* __restr
     const uint64_t b = off[v], e = b + deg[v];
     for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
       const uint32_t c = col[i];
-      const uint32_t h = c < n ? slot[c] : ~0u;
-      out[i] = h != ~0u ? (0x80000000u | h) : c;
+      out[i] = c < n ? rank[c] : c;
     }
   }
 }
 
-sg_status cub_select_flagged_u32(sg_ctx* ctx, const uint32_t* in, const uint8_t* flags,
-                                 uint32_t* out, uint64_t* d_count, uint64_t n);
+sg_status cub_sort_pairs_u32_u32(sg_ctx* ctx, const uint32_t* kin, uint32_t* kout, const uint32_t* vin,
+                                 uint32_t* vout, uint64_t n);
 
 sg_status pr_hub_after_apply(sg_ctx* ctx, const uint32_t* rows, uint64_t nrows, bool patched) {
   DevGraph& g = ctx->g;
@@ -343,7 +348,7 @@ sg_status pr_hub_after_apply(sg_ctx* ctx, const uint32_t* rows, uint64_t nrows, 
     return SG_OK;
   if (nrows)
     k_hub_encode_rows<<<(unsigned)std::min<uint64_t>(nrows, (uint64_t)ctx->num_sms * 16), 256, 0,
-                        ctx->stream>>>(g.in.off, g.in.deg, g.in.col, H.slot, g.n, rows, nrows,
+                        ctx->stream>>>(g.in.off, g.in.deg, g.in.col, H.rank, g.n, rows, nrows,
                                        H.col);
   count_launch(ctx);
   SG_CUDA(ctx, cudaGetLastError());
@@ -351,14 +356,15 @@ sg_status pr_hub_after_apply(sg_ctx* ctx, const uint32_t* rows, uint64_t nrows, 
   return SG_OK;
 }
 
-// Chooses the hubs: every vertex whose out-degree reaches the smallest
-// threshold (at least 2) that leaves at most kmax of them.
+// Chooses the vertex order and the hubs: ranks by out-degree, highest first
+// (ties by id); the hubs are the lowest min(kmax, vertices of out-degree >= 2)
+// ranks.  The order is kept while the graph takes batches (any order is
+// correct; this one is chosen for locality).
 static sg_status hub_choose(sg_ctx* ctx, uint32_t kmax) {
   DevGraph& g = ctx->g;
   HubView& H = g.hub;
   cudaStream_t st = ctx->stream;
-  dfree(H.ids);
-  dfree(H.slot);
+  dfree(H.rank);
   dfree(H.col);
   H = HubView();
   H.chosen = true;
@@ -366,57 +372,38 @@ static sg_status hub_choose(sg_ctx* ctx, uint32_t kmax) {
   if (kmax < kHubMin || g.n < 4 * kHubMin) return SG_OK;
   unsigned long long* d_cnt = nullptr;
   SG_TRY(dalloc(ctx, &d_cnt, 1));
-  auto count = [&](uint32_t d, unsigned long long* out) -> sg_status {
-    SG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, 8, st));
-    k_count_deg_ge<<<grid_for(g.n, 256), 256, 0, st>>>(g.out.deg, g.n, d, d_cnt);
-    SG_CUDA(ctx, cudaMemcpyAsync(out, d_cnt, 8, cudaMemcpyDeviceToHost, st));
-    SG_CUDA(ctx, cudaStreamSynchronize(st));
-    return SG_OK;
-  };
   unsigned long long c = 0;
-  SG_TRY(count(2, &c));
-  uint32_t d = 2;
-  if (c > kmax) {
-    // count(lo) > kmax >= count(hi); degrees are below 2^32
-    uint64_t lo = 2, hi = 1ull << 32;
-    while (hi - lo > 1) {
-      const uint64_t mid = (lo + hi) / 2;
-      SG_TRY(count((uint32_t)std::min<uint64_t>(mid, 0xFFFFFFFFull), &c));
-      if (c <= kmax) hi = mid; else lo = mid;
-    }
-    d = (uint32_t)std::min<uint64_t>(hi, 0xFFFFFFFFull);
-    SG_TRY(count(d, &c));
-  }
-  if (c < kHubMin) {
-    dfree(d_cnt);
-    return SG_OK;
-  }
-  const uint32_t k = (uint32_t)c;
-  uint8_t* flags = nullptr;
-  uint32_t* iota = nullptr;
-  uint64_t* d_sel = nullptr;
-  SG_TRY(dalloc(ctx, &flags, g.n));
+  SG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, 8, st));
+  k_count_deg_ge<<<grid_for(g.n, 256), 256, 0, st>>>(g.out.deg, g.n, 2, d_cnt);
+  SG_CUDA(ctx, cudaMemcpyAsync(&c, d_cnt, 8, cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  dfree(d_cnt);
+  const uint32_t k = (uint32_t)std::min<unsigned long long>(c, kmax);
+  if (k < kHubMin) return SG_OK;
+  uint32_t *key = nullptr, *key2 = nullptr, *iota = nullptr, *order = nullptr;
+  SG_TRY(dalloc(ctx, &key, g.n));
+  SG_TRY(dalloc(ctx, &key2, g.n));
   SG_TRY(dalloc(ctx, &iota, g.n));
-  SG_TRY(dalloc(ctx, &d_sel, 1));
-  SG_TRY(dalloc(ctx, &H.ids, k));
-  SG_TRY(dalloc(ctx, &H.slot, g.n));
-  k_flag_deg_ge<<<grid_for(g.n, 256), 256, 0, st>>>(g.out.deg, g.n, d, flags, iota);
-  SG_TRY(cub_select_flagged_u32(ctx, iota, flags, H.ids, d_sel, g.n));
-  SG_CUDA(ctx, cudaMemsetAsync(H.slot, 0xFF, 4ull * g.n, st));
-  k_hub_slots<<<grid_for(k, 256), 256, 0, st>>>(H.ids, k, H.slot);
+  SG_TRY(dalloc(ctx, &order, g.n));
+  SG_TRY(dalloc(ctx, &H.rank, g.n));
+  k_rank_keys<<<grid_for(g.n, 256), 256, 0, st>>>(g.out.deg, g.n, key, iota);
+  SG_TRY(cub_sort_pairs_u32_u32(ctx, key, key2, iota, order, g.n));
+  k_rank_scatter<<<grid_for(g.n, 256), 256, 0, st>>>(order, g.n, H.rank);
+  count_launch(ctx, 4);
   SG_CUDA(ctx, cudaGetLastError());
   SG_CUDA(ctx, cudaStreamSynchronize(st));
-  dfree(flags);
+  dfree(key);
+  dfree(key2);
   dfree(iota);
-  dfree(d_sel);
-  dfree(d_cnt);
+  dfree(order);
   H.k = k;
   return SG_OK;
 }
 
-// The hub view for the current in-CSR: hubs chosen once per graph (or when
-// the cap changes), the encoded column copy refreshed when the adjacency
-// has changed since.  Returns null when the cache is off or too small.
+// The hub view for the current in-CSR: order and hubs chosen once per graph
+// (or when the cap changes), the encoded column copy refreshed when the
+// adjacency has changed since.  Returns null when the cache is off or too
+// small.
 static sg_status hub_view(sg_ctx* ctx, const HubView** out) {
   DevGraph& g = ctx->g;
   HubView& H = g.hub;
@@ -438,7 +425,7 @@ static sg_status hub_view(sg_ctx* ctx, const HubView** out) {
       }
       H.cap = g.in.pool_cap;
     }
-    k_hub_encode<<<grid_for(H.cap, 256), 256, 0, ctx->stream>>>(g.in.col, H.cap, H.slot, g.n,
+    k_hub_encode<<<grid_for(H.cap, 256), 256, 0, ctx->stream>>>(g.in.col, H.cap, H.rank, g.n,
                                                                   H.col);
     count_launch(ctx);
     SG_CUDA(ctx, cudaGetLastError());
@@ -627,6 +614,7 @@ sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R) {
   A.misc = s.misc;
   A.res = s.res;
   A.cnt = s.cnt;
+  A.rank = nullptr;
 
   WarpPullArgs WP;
   WP.nz = L.nz;
@@ -639,7 +627,6 @@ sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R) {
   WP.ntiles = L.nwtiles;
   WP.col = R.csr->col;
   WP.w = R.weighted ? R.csr->w : nullptr;
-  WP.hub_ids = nullptr;
   WP.nhub = 0;
   const uint32_t* bnd = L.wbnd;
   const uint32_t nbnd = L.wbnd_count;
@@ -650,8 +637,8 @@ sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R) {
   if (R.csr == &g.in && L.quads > 0) SG_TRY(hub_view(ctx, &hub));
   if (hub) {
     WP.col = hub->col;
-    WP.hub_ids = hub->ids;
     WP.nhub = hub->k;
+    A.rank = hub->rank;  // push values in the pull's vertex order
   }
   const int pt = hub ? kHubThreads : PT_THREADS;
   const size_t hub_smem = hub ? (size_t)hub->k * sizeof(float) : 0;

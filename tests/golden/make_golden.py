@@ -154,14 +154,14 @@ def parse_stats(log):
     return st
 
 
-def run_ref(exe, d, app, flags, update=None):
+def run_ref(exe, d, app, flags, update=None, threads=4):
     out = os.path.join(d, f"{app}.bin")
     args = [exe, app, out] + [f"{k}={v}" for k, v in flags.items()]
     efile = "g_w.e" if app.startswith("sssp") else "g.e"
     args += [f"efile={os.path.join(d, efile)}", f"vfile={os.path.join(d, 'g.v')}"]
     if update:
         args.append(f"efile_update={update}")
-    env = dict(os.environ, CUDA_VISIBLE_DEVICES="", OMP_NUM_THREADS="4")
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="", OMP_NUM_THREADS=str(threads))
     p = subprocess.run(args, capture_output=True, text=True, env=env, timeout=3600)
     if p.returncode != 0:
         sys.stderr.write(p.stderr[-4000:])
@@ -267,6 +267,151 @@ def make_pull(exe):
     np.savez_compressed(os.path.join(HERE, "pull_pr.npz"), **out)
 
 
+# ----------------------------------------------------- workload-size cases
+#
+#   rmat16_pr.npz    PageRank on R-MAT scale 16 (65,536 vertices, 2^20 edges,
+#                    seed 1), greedy clusters (max 150, min 8, seed 1), one
+#                    10,000-change batch (50 % inserts / 50 % deletes, seed 2):
+#                    the reference's SumInc PEval and IncEval (compress=1) and
+#                    its plain Ingress IncEval (compress=0), values as float32
+#                    (the reference's value type, so exact).
+#   rmat20_sssp.npz  SSSP from vertex 0 on R-MAT scale 20 (1,048,576
+#                    vertices, 2^24 edges, integer weights U[1, 100], seed 1),
+#                    greedy clusters, one 100,000-change batch (40 % inserts,
+#                    40 % deletes, 20 % re-weights, seed 2): summarized PEval
+#                    and IncEval and the plain IncEval, distances as uint32
+#                    (0xFFFFFFFF = unreachable).
+# The inputs are not stored: tests regenerate the graph and the batch from the
+# seeds (oracle.rmat / oracle.gen_updates, or the library's generators, which
+# draw the same) and check them against the stored hashes.  The clusters are
+# stored (the greedy builder takes minutes at scale 20).
+
+def write_graph_fast(d, rp, col, w):
+    n = len(rp) - 1
+    src = np.repeat(np.arange(n, dtype=np.int64), np.diff(rp).astype(np.int64))
+    np.savetxt(os.path.join(d, "g.e"), np.stack([src, col.astype(np.int64)], 1), fmt="%d %d")
+    if w is not None:
+        np.savetxt(os.path.join(d, "g_w.e"),
+                   np.stack([src, col.astype(np.int64), w.astype(np.int64)], 1), fmt="%d %d %d")
+    np.savetxt(os.path.join(d, "g.v"), np.arange(n, dtype=np.int64), fmt="%d")
+
+
+def write_clusters(path, clusters):
+    with open(path, "w") as f:
+        for c in clusters:
+            f.write(" ".join([str(len(c))] + [str(int(v)) for v in c]) + "\n")
+
+
+def pack_clusters(clusters):
+    cp = np.zeros(len(clusters) + 1, np.uint32)
+    for i, c in enumerate(clusters):
+        cp[i + 1] = cp[i] + len(c)
+    mem = np.concatenate(clusters).astype(np.uint32) if clusters else np.zeros(0, np.uint32)
+    return cp, mem
+
+
+def update_hash(upd):
+    return hashlib.sha256(np.ascontiguousarray(upd).tobytes()).hexdigest()
+
+
+def make_rmat16_pr(exe, threads):
+    import oracle
+    rp, col, _ = oracle.rmat(16, 1 << 20, seed=1)
+    clusters = sg.greedy_clusters(rp, col, 150, 8, seed=1)
+    upd = oracle.gen_updates(rp, col, 5000, 5000, 0, seed=2)
+    flags = dict(REF_FLAGS_PR, app_concurrency=str(threads))
+    res, stats = {}, {}
+    with tempfile.TemporaryDirectory() as d:
+        write_graph_fast(d, rp, col, None)
+        write_clusters(os.path.join(d, "g.e.c_150"), clusters)
+        up = os.path.join(d, "pr.update")
+        write_updates(up, upd, False)
+        res["pr_sum_peval"], log = run_ref(exe, d, "pagerank", flags, threads=threads)
+        stats["pr_peval"] = parse_stats(log)
+        res["pr_sum_inc"], log = run_ref(exe, d, "pagerank", flags, up, threads=threads)
+        stats["pr_inc"] = parse_stats(log)
+        res["pr_plain_inc"], log = run_ref(exe, d, "pagerank_plain", dict(flags, compress="0"), up,
+                                           threads=threads)
+        stats["pr_plain"] = parse_stats(log)
+    cp, mem = pack_clusters(clusters)
+    params = {"graph": "oracle.rmat(16, 1 << 20, seed=1)", "clusters": "greedy(150, 8, seed=1)",
+              "updates": "oracle.gen_updates(rp, col, 5000, 5000, 0, seed=2)", "flags_pr": flags}
+    np.savez_compressed(os.path.join(HERE, "rmat16_pr.npz"), params=json.dumps(params),
+                        input_sha256=input_hash(rp, col, None), updates_sha256=update_hash(upd),
+                        clusters_ptr=cp, clusters_members=mem, stats=json.dumps(stats),
+                        **{f"ref_{k}": v.astype(np.float32) for k, v in res.items()})
+    print("rmat16_pr", {k: float(v.sum()) for k, v in res.items()}, "clusters", len(clusters))
+
+
+def as_u32_dist(d):
+    out = np.full(len(d), 0xFFFFFFFF, np.uint32)
+    fin = np.isfinite(d) & (d < 2147483647)
+    assert np.all(d[fin] == np.round(d[fin]))
+    out[fin] = d[fin].astype(np.uint32)
+    return out
+
+
+def make_rmat20_sssp(exe, threads, clusters_path=None):
+    import oracle
+    rp, col, w = oracle.rmat(20, 1 << 24, seed=1, weight_kind=1, wlo=1, whi=100)
+    if clusters_path:
+        z = np.load(clusters_path)
+        cp, mem = z["clusters_ptr"], z["clusters_members"]
+        clusters = [mem[cp[i]:cp[i + 1]] for i in range(len(cp) - 1)]
+    else:
+        clusters = sg.greedy_clusters(rp, col, 150, 8, seed=1)
+    upd = oracle.gen_updates(rp, col, 40000, 40000, 20000, seed=2)
+    flags = dict(REF_FLAGS_SSSP, app_concurrency=str(threads))
+    res, stats = {}, {}
+    with tempfile.TemporaryDirectory() as d:
+        write_graph_fast(d, rp, col, w)
+        write_clusters(os.path.join(d, "g.e.c_150"), clusters)
+        up = os.path.join(d, "sssp.update")
+        write_updates(up, upd, True)
+        res["sssp_sum_peval"], log = run_ref(exe, d, "sssp", flags, threads=threads)
+        stats["sssp_peval"] = parse_stats(log)
+        res["sssp_sum_inc"], log = run_ref(exe, d, "sssp", flags, up, threads=threads)
+        stats["sssp_inc"] = parse_stats(log)
+        res["sssp_plain_inc"], log = run_ref(exe, d, "sssp_plain", dict(flags, compress="0"), up,
+                                             threads=threads)
+        stats["sssp_plain"] = parse_stats(log)
+    cp, mem = pack_clusters(clusters)
+    params = {"graph": "oracle.rmat(20, 1 << 24, seed=1, weight_kind=1, wlo=1, whi=100)",
+              "clusters": "greedy(150, 8, seed=1)",
+              "updates": "oracle.gen_updates(rp, col, 40000, 40000, 20000, seed=2)",
+              "source": 0, "flags_sssp": flags}
+    np.savez_compressed(os.path.join(HERE, "rmat20_sssp.npz"), params=json.dumps(params),
+                        input_sha256=input_hash(rp, col, w), updates_sha256=update_hash(upd),
+                        clusters_ptr=cp, clusters_members=mem, stats=json.dumps(stats),
+                        **{f"ref_{k}": as_u32_dist(v) for k, v in res.items()})
+    print("rmat20_sssp", {k: int(np.isfinite(v).sum()) for k, v in res.items()},
+          "clusters", len(clusters))
+
+
+def make_rmat12_tight(exe):
+    """rmat12 with termcheck_threshold 1e-10: the reference's summarized PEval
+    and IncEval and its plain IncEval, to show L1 <= 1e-6 against the
+    reference where the stop rule allows it."""
+    z = np.load(os.path.join(HERE, "rmat12.npz"))
+    rp, col, w = z["row_ptr"], z["col"], z["w"]
+    cp, mem = z["clusters_ptr"], z["clusters_members"]
+    clusters = [mem[cp[i]:cp[i + 1]] for i in range(len(cp) - 1)]
+    flags = dict(REF_FLAGS_PR, termcheck_threshold="1e-10")
+    res = {}
+    with tempfile.TemporaryDirectory() as d:
+        write_graph(d, rp, col, w)
+        write_clusters(os.path.join(d, "g.e.c_150"), clusters)
+        up = os.path.join(d, "pr.update")
+        write_updates(up, z["updates_pr"], False)
+        res["pr_sum_peval"], _ = run_ref(exe, d, "pagerank", flags)
+        res["pr_sum_inc"], _ = run_ref(exe, d, "pagerank", flags, up)
+        res["pr_plain_inc"], _ = run_ref(exe, d, "pagerank_plain", dict(flags, compress="0"), up)
+    np.savez_compressed(os.path.join(HERE, "rmat12_tight.npz"), params=json.dumps({"flags_pr": flags}),
+                        input_sha256=str(z["input_sha256"]),
+                        **{f"ref_{k}": v.astype(np.float32) for k, v in res.items()})
+    print("rmat12_tight", {k: float(v.sum()) for k, v in res.items()})
+
+
 def main():
     sys.path.insert(0, os.path.join(ROOT, "oracle", "ref_harness"))
     import build_ref
@@ -277,6 +422,17 @@ def main():
         raise SystemExit("reference checkout or harness build unavailable")
     if "--pull" in sys.argv[1:]:
         make_pull(exe)
+        return
+    threads = os.cpu_count() or 4
+    if "--rmat16" in sys.argv[1:]:
+        make_rmat16_pr(exe, threads)
+        return
+    if "--rmat20" in sys.argv[1:]:
+        cl = sys.argv[sys.argv.index("--rmat20") + 1] if len(sys.argv) > sys.argv.index("--rmat20") + 1 else None
+        make_rmat20_sssp(exe, threads, cl if cl and cl.endswith(".npz") else None)
+        return
+    if "--tight" in sys.argv[1:]:
+        make_rmat12_tight(exe)
         return
     rp, col, w = sg.rmat_host(12, 16 << 12, seed=1, weight_kind=1, wlo=1, whi=100)
     make_case("rmat12", rp, col, w, exe, seed=1)

@@ -168,3 +168,57 @@ def test_reference_pull_worker_loses_mass_in_flight():
     assert np.abs(ref - x_star).sum() > 1e-3
     x, _ = pull.pr_pull_summarized(rp, col, clusters, count_entry_arrivals=True)
     assert np.abs(x - x_star).sum() <= 1e-5
+
+
+# ------------------------------------------------------ workload-size cases
+
+def _sha(*arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        if a is not None:
+            h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def test_rmat16_inputs_regenerate_and_reference_against_oracle():
+    """rmat16_pr: the graph and batch regenerate from their seeds (oracle
+    generators, no library code); the reference's results are within the
+    PageRank bounds of the FP64 fixed point and of the oracle's restatement;
+    its summary kept a handful of the greedy clusters."""
+    fx = load("rmat16_pr")
+    rp, col, _ = oracle.rmat(16, 1 << 20, seed=1)
+    assert _sha(rp, col) == str(fx["input_sha256"])
+    upd = oracle.gen_updates(rp, col, 5000, 5000, 0, seed=2)
+    assert _sha(upd) == str(fx["updates_sha256"])
+    x_star = oracle.pr_fixed_point(rp, col)
+    assert np.abs(fx["ref_pr_sum_peval"] - x_star).sum() < 1e-5
+    nrp, ncol, _ = oracle.apply_updates(rp, col, None, upd)
+    x_new = oracle.pr_fixed_point(nrp, ncol)
+    assert np.abs(fx["ref_pr_sum_inc"] - x_new).sum() < 1e-5
+    assert np.abs(fx["ref_pr_plain_inc"] - x_new).sum() < 1e-5
+    x, delta, _ = oracle.ingress_pr(rp, col, tau=1e-6)
+    d2 = oracle.pr_amend((rp, col), (nrp, ncol), x, delta)
+    x2, _, _ = oracle.ingress_pr(nrp, ncol, x=x, delta=d2, tau=1e-6)
+    assert np.abs(x2 - fx["ref_pr_plain_inc"]).sum() < 2e-5
+    st = json.loads(str(fx["stats"]))["pr_peval"]
+    assert st["spn_num"][0] > 0 and st["all_node_num"][0] == 1 << 16
+
+
+def test_tight_threshold_reference_against_fixed_point_and_oracle():
+    """rmat12_tight: at termcheck_threshold 1e-10 the reference is within 5e-7
+    of the FP64 fixed point (its FP32 values round at about 3e-11 each over
+    4,096 vertices) and the oracle's restatement within 1e-6 of it."""
+    base, fx = load("rmat12"), load("rmat12_tight")
+    assert str(fx["input_sha256"]) == str(base["input_sha256"])
+    rp, col = base["row_ptr"], base["col"]
+    x_star = oracle.pr_fixed_point(rp, col)
+    assert np.abs(fx["ref_pr_sum_peval"] - x_star).sum() < 5e-7
+    nrp, ncol, _ = after(base, "updates_pr")
+    x_new = oracle.pr_fixed_point(nrp, ncol)
+    assert np.abs(fx["ref_pr_sum_inc"] - x_new).sum() < 5e-7
+    assert np.abs(fx["ref_pr_plain_inc"] - x_new).sum() < 5e-7
+    x, delta, _ = oracle.ingress_pr(rp, col, tau=1e-10)
+    d2 = oracle.pr_amend((rp, col), (nrp, ncol), x, delta)
+    x2, _, _ = oracle.ingress_pr(nrp, ncol, x=x, delta=d2, tau=1e-10)
+    assert np.abs(x2 - fx["ref_pr_plain_inc"]).sum() < 1e-6
