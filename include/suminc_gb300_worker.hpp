@@ -175,7 +175,9 @@ class GpuWorkerBase {
                   ctx_.get(), "sg_graph_load_csr");
     detail::check(sg_graph_set_vertex_oids(ctx_.get(), oid_.data()), ctx_.get(),
                   "sg_graph_set_vertex_oids");
-    if (KIND == AppKind::kPageRank && wopt_.compress && !wopt_.cluster_file.empty())
+    // the summary both workers run over (SumSyncIterWorker and
+    // SumSyncTraversalWorker build their compressor in Init)
+    if (wopt_.compress && !wopt_.cluster_file.empty())
       detail::check(sg_summary_build_file(ctx_.get(), wopt_.cluster_file.c_str()), ctx_.get(),
                     "sg_summary_build_file");
   }

@@ -422,7 +422,10 @@ sg_status sg_sssp_peval(sg_ctx* ctx, uint32_t source, double* out) {
 sg_status sg_sssp_inceval(sg_ctx* ctx, double* out) {
   SG_GUARD(ctx);
   try {
-    sg_status st = sssp_run_inceval(ctx);
+    // over the summary once a summarized PEval has built its shortcut
+    // distances; else (compress = 0, or a PEval on the original graph) plain
+    sg_status st = ctx->opt.compress && sssp_summary_ready(ctx) ? sssp_summarized_inc(ctx)
+                                                                : sssp_run_inceval(ctx);
     kprof_flush(ctx);
     if (st != SG_OK) return st;
     if (out) return sssp_download(ctx, out);

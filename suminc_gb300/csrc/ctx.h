@@ -337,6 +337,18 @@ sg_status sssp_run_view(sg_ctx* ctx, const SsspView& G, const uint32_t* h_seeds,
 // prepares ctx->sp for a result written from outside (buffers, no run)
 sg_status sssp_prepare_external(sg_ctx* ctx, uint32_t source);
 sg_status sssp_finish_external(sg_ctx* ctx, const unsigned long long* h_cnt, float ms);
+// IncEval over the summary: the plain reset and re-seed, then the traversal
+// over the summary's view from a warm state, then the plain parents.
+struct SsspIncInfo {
+  uint32_t total = 0;  // reset vertices (s.seeds[0, total))
+  uint32_t nadd = 0;   // heads of added edges (s.padd_dst[0, nadd))
+  bool one_batch = false;
+};
+sg_status sssp_inc_prepare(sg_ctx* ctx, SsspIncInfo* info);
+sg_status sssp_run_view_warm(sg_ctx* ctx, const SsspView& G, const uint32_t* d_seeds,
+                             uint32_t nseeds, unsigned long long* dist, unsigned long long* h_cnt);
+sg_status sssp_inc_finish_external(sg_ctx* ctx, const SsspIncInfo& info,
+                                   const unsigned long long* h_cnt, float ms);
 
 // io.cpp: the reference's text formats
 sg_status load_files(sg_ctx* ctx, const char* efile, const char* vfile, bool weighted);
@@ -399,6 +411,8 @@ sg_status summary_pull_view(sg_ctx* ctx, PullView* out);
 sg_status pr_pull_worker(sg_ctx* ctx, bool inc);
 sg_status pull_free(sg_ctx* ctx);
 sg_status sssp_summarized(sg_ctx* ctx, uint32_t source);
+sg_status sssp_summarized_inc(sg_ctx* ctx);
+bool sssp_summary_ready(sg_ctx* ctx);
 uint32_t summary_rows(sg_ctx* ctx);  // rows incl. mirrors, 0 without a summary
 sg_status summary_info(sg_ctx* ctx, sg_summary_info* out);
 

@@ -1128,12 +1128,16 @@ __global__ void k_inc_start(const uint32_t* seed_cnt, uint32_t* inc_ctl) {
   inc_ctl[7] = 0;
 }
 
-sg_status sssp_run_inceval(sg_ctx* ctx) {
+// Steps 1 and 2 of the incremental stage (deltaCompute and the re-seed of
+// sum_sync_traversal_worker.h:113-352): the reset BFS over the shortest-path
+// tree, the pulls that give every reset vertex its best distance from the
+// vertices that kept theirs, and the relaxation of the batch's new edges.
+// The far queue holds the improved vertices.  Shared by the plain IncEval and
+// the IncEval over the summary.
+static sg_status inc_reset_seed(sg_ctx* ctx, SsspIncInfo* info) {
   DevGraph& g = ctx->g;
   SsspState& s = ctx->sp;
-  if (!s.valid) return fail(ctx, SG_ERR_STATE, "SSSP IncEval before PEval");
   cudaStream_t st = ctx->stream;
-  SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
   if (!s.has_pending) SG_CUDA(ctx, cudaMemsetAsync(s.seed_cnt, 0, 4 * sizeof(uint32_t), st));
   if (++s.chg_tag == 0) {  // tags wrapped: clear the marks
     SG_CUDA(ctx, cudaMemsetAsync(s.chg_mark, 0, 4ull * g.n, st));
@@ -1220,6 +1224,29 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
     SG_TRY(reseed(s.padd_dst, nadd));
   }
   SG_CUDA(ctx, cudaGetLastError());
+  info->total = total;
+  info->nadd = nadd;
+  info->one_batch = one_batch;
+  return SG_OK;
+}
+
+sg_status sssp_inc_prepare(sg_ctx* ctx, SsspIncInfo* info) {
+  if (!ctx->sp.valid) return fail(ctx, SG_ERR_STATE, "SSSP IncEval before PEval");
+  return inc_reset_seed(ctx, info);
+}
+
+sg_status sssp_run_inceval(sg_ctx* ctx) {
+  DevGraph& g = ctx->g;
+  SsspState& s = ctx->sp;
+  if (!s.valid) return fail(ctx, SG_ERR_STATE, "SSSP IncEval before PEval");
+  cudaStream_t st = ctx->stream;
+  SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
+  SsspIncInfo info;
+  SG_TRY(inc_reset_seed(ctx, &info));
+  const uint32_t total = info.total, nadd = info.nadd;
+  const bool one_batch = info.one_batch;
+  const HeavyRows H{s.hv_list, s.hv_best, s.hv_cnt, g.n};
+  const unsigned heavy_grid = ctx->num_sms * 4;
   // 3. delta-stepping from the seeds, listing every improved vertex
   SG_TRY(sssp_launch(ctx, true));
   if (total > 0) k_clear_marks<<<grid_for(total, 256), 256, 0, st>>>(s.seeds, total, s.reset);
@@ -1274,6 +1301,85 @@ sg_status sssp_run_inceval(sg_ctx* ctx) {
   ctx->stats.reset_vertices = total;
   s.has_pending = false;
   return SG_OK;
+}
+
+// The end of an IncEval whose distances were finished elsewhere (over the
+// summary): the reset marks cleared, every parent recomputed over the
+// in-rows, the counters of the traversal.
+sg_status sssp_inc_finish_external(sg_ctx* ctx, const SsspIncInfo& info,
+                                   const unsigned long long* h_cnt, float ms) {
+  SsspState& s = ctx->sp;
+  cudaStream_t st = ctx->stream;
+  if (info.total > 0) {
+    k_clear_marks<<<grid_for(info.total, 256), 256, 0, st>>>(s.seeds, info.total, s.reset);
+    count_launch(ctx);
+  }
+  SG_TRY(sssp_compute_parents(ctx));
+  count_launch(ctx);
+  SG_CUDA(ctx, cudaGetLastError());
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  if (h_cnt) fill_stats(ctx, h_cnt);
+  ctx->stats.elapsed_ms = ms;
+  ctx->stats.converged = 1;
+  ctx->stats.reset_vertices = info.total;
+  s.has_pending = false;
+  return SG_OK;
+}
+
+// Delta-stepping over a view from a warm state: `dist` (device [G.n]) holds
+// valid upper bounds, final for every vertex whose distance cannot change,
+// and the device list `d_seeds` holds the vertices whose out-rows must be
+// relaxed again.  Temporary queues are allocated for the call.
+sg_status sssp_run_view_warm(sg_ctx* ctx, const SsspView& G, const uint32_t* d_seeds,
+                             uint32_t nseeds, unsigned long long* dist, unsigned long long* h_cnt) {
+  cudaStream_t st = ctx->stream;
+  const uint32_t n = G.n;
+  uint32_t *stamp = nullptr, *fstamp = nullptr, *q0 = nullptr, *q1 = nullptr, *q2 = nullptr,
+           *far = nullptr, *far2 = nullptr, *ctl = nullptr;
+  unsigned long long* cnt = nullptr;
+  const uint64_t fcap = G.m + (uint64_t)n + nseeds + 1024;
+  SG_TRY(dalloc(ctx, &stamp, n));
+  SG_TRY(dalloc(ctx, &fstamp, n));
+  SG_TRY(dalloc(ctx, &q0, n));
+  SG_TRY(dalloc(ctx, &q1, n));
+  SG_TRY(dalloc(ctx, &q2, n));
+  SG_TRY(dalloc(ctx, &far, fcap));
+  SG_TRY(dalloc(ctx, &far2, fcap));
+  SG_TRY(dalloc(ctx, &ctl, S_WORDS));
+  SG_TRY(dalloc(ctx, &cnt, SC_WORDS));
+  SG_CUDA(ctx, cudaMemsetAsync(stamp, 0, 4ull * n, st));
+  SG_CUDA(ctx, cudaMemsetAsync(fstamp, 0, 4ull * n, st));
+  SG_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(uint32_t) * S_WORDS, st));
+  SG_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * SC_WORDS, st));
+  if (nseeds) {
+    SG_CUDA(ctx, cudaMemcpyAsync(far, d_seeds, 4ull * nseeds, cudaMemcpyDeviceToDevice, st));
+    SG_CUDA(ctx, cudaMemcpyAsync(ctl + S_F0, &nseeds, 4, cudaMemcpyHostToDevice, st));
+  }
+  SsspArgs A;
+  A.n = n;
+  A.off = G.off; A.deg = G.deg; A.col = G.col; A.w = G.w;
+  A.dist = dist; A.stamp = stamp; A.fstamp = fstamp;
+  A.nq[0] = q0; A.nq[1] = q1; A.nq[2] = q2;
+  A.fq[0] = far; A.fq[1] = far2;
+  A.ctl = ctl;
+  A.cnt = cnt;
+  A.delta = auto_delta(ctx);
+  A.iter_base = 1;
+  A.fcap = fcap;
+  A.spin_limit = 40ll * 1000 * 1000;
+  A.hq[0] = A.hq[1] = A.hq[2] = nullptr;  // one warp per row on this view
+  A.hcap = 0;
+  A.chg_mark = nullptr;
+  A.chg_list = nullptr;
+  A.chg_cnt = nullptr;
+  A.chg_tag = 0;
+  uint32_t h_ctl[S_WORDS];
+  sg_status rs = sssp_launch_args(ctx, A, h_ctl);
+  if (rs == SG_OK && h_cnt)
+    SG_CUDA(ctx, cudaMemcpy(h_cnt, cnt, sizeof(unsigned long long) * SC_WORDS, cudaMemcpyDeviceToHost));
+  dfree(stamp); dfree(fstamp); dfree(q0); dfree(q1); dfree(q2);
+  dfree(far); dfree(far2); dfree(ctl); dfree(cnt);
+  return rs;
 }
 
 sg_status sssp_download(sg_ctx* ctx, double* out) {

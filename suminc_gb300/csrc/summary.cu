@@ -95,6 +95,11 @@ struct SummaryDev {
   uint64_t sk_m = 0;
   uint32_t sk_ncorr = 0;
   bool sk_stale = true;
+  // IncEval over the summary: the rows whose shortcuts are relaxed again
+  // (every supernode's entry or in-mirror) and the in-mirrors with their
+  // masters (a mirror starts from its master's distance)
+  uint32_t *sk_spid = nullptr, *sk_imir = nullptr, *sk_imaster = nullptr;
+  uint32_t sk_nspid = 0, sk_nimir = 0;
   // the construction's state between its two halves, serialized
   std::vector<uint8_t> init_blob;
   std::unordered_map<const void*, uint64_t> dcap;  // reupload capacities
@@ -123,6 +128,7 @@ static void sfree(SummaryDev& D) {
   dfree(D.bound); dfree(D.spnode); dfree(D.old_x); dfree(D.d_res); dfree(D.sctl);
   dfree(D.sk_off); dfree(D.sk_coff); dfree(D.sk_deg); dfree(D.sk_col); dfree(D.sk_crow);
   dfree(D.sk_cv); dfree(D.sk_w); dfree(D.sk_cd);
+  dfree(D.sk_spid); dfree(D.sk_imir); dfree(D.sk_imaster);
   dfree(D.p_cls); dfree(D.p_ie_off); dfree(D.p_bd_off);
   dfree(D.p_ie_nbr); dfree(D.p_bd_src); dfree(D.p_act); dfree(D.p_ent); dfree(D.p_bd_w);
   D.dcap.clear();
@@ -1818,6 +1824,19 @@ static sg_status sssp_sketch(sg_ctx* ctx, SummaryDev& D) {
   SG_TRY(upload(ctx, &D.sk_crow, crow));
   SG_TRY(upload(ctx, &D.sk_cv, cv));
   SG_TRY(upload(ctx, &D.sk_cd, cd));
+  std::vector<uint32_t> spid, imir, imaster;
+  for (uint32_t sp = 0; sp < S.supernodes.size(); ++sp)
+    if (S.supernodes[sp].id != Summary::kIdDefault) spid.push_back(S.supernodes[sp].id);
+  for (size_t i = 0; i < S.cluster_in_mirror_ids.size(); ++i)
+    for (uint32_t m : S.cluster_in_mirror_ids[i]) {
+      imir.push_back(m);
+      imaster.push_back(S.mirror_master(m));
+    }
+  SG_TRY(upload(ctx, &D.sk_spid, spid));
+  SG_TRY(upload(ctx, &D.sk_imir, imir));
+  SG_TRY(upload(ctx, &D.sk_imaster, imaster));
+  D.sk_nspid = (uint32_t)spid.size();
+  D.sk_nimir = (uint32_t)imir.size();
   D.sk_m = pos;
   D.sk_ncorr = (uint32_t)crow.size();
   D.sk_stale = false;
@@ -1845,15 +1864,11 @@ __global__ void k_copy_u64(const unsigned long long* a, uint64_t n, unsigned lon
     b[i] = a[i];
 }
 
-sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
-  SummaryDev* Dp = sdev(ctx);
-  if (!Dp || !Dp->valid) return fail(ctx, SG_ERR_STATE, "compress=1 needs sg_summary_build first");
-  SummaryDev& D = *Dp;
+// Shortcut distances built on first use, repaired for the supernodes the
+// batches since the last query touched, and the summarized CSR rebuilt when
+// stale.
+static sg_status sssp_summary_refresh(sg_ctx* ctx, SummaryDev& D) {
   Summary& S = D.S;
-  if (!ctx->g.weighted) return fail(ctx, SG_ERR_INVALID, "SSSP needs a weighted graph");
-  if (source >= S.old_n) return fail(ctx, SG_ERR_INVALID, "source >= n");
-  cudaStream_t st = ctx->stream;
-  SG_CUDA(ctx, cudaEventRecord(ctx->kev0, st));
   if (!D.sssp_ready) {
     std::vector<uint32_t> all_sp(S.supernodes.size());
     for (uint32_t i = 0; i < all_sp.size(); ++i) all_sp[i] = i;
@@ -1879,6 +1894,19 @@ sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
     D.sk_stale = true;
   }
   if (D.sk_stale) SG_TRY(sssp_sketch(ctx, D));
+  return SG_OK;
+}
+
+sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
+  SummaryDev* Dp = sdev(ctx);
+  if (!Dp || !Dp->valid) return fail(ctx, SG_ERR_STATE, "compress=1 needs sg_summary_build first");
+  SummaryDev& D = *Dp;
+  Summary& S = D.S;
+  if (!ctx->g.weighted) return fail(ctx, SG_ERR_INVALID, "SSSP needs a weighted graph");
+  if (source >= S.old_n) return fail(ctx, SG_ERR_INVALID, "source >= n");
+  cudaStream_t st = ctx->stream;
+  SG_CUDA(ctx, cudaEventRecord(ctx->kev0, st));
+  SG_TRY(sssp_summary_refresh(ctx, D));
   // seeds: the source, expanded inside its cluster when it is a member
   std::vector<uint32_t> seeds;
   std::vector<double> sdist;
@@ -1926,6 +1954,107 @@ sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
   SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->kev0, ctx->kev1));
   dfree(dist);
   return sssp_finish_external(ctx, h_cnt, ms);
+}
+
+
+// ------------------------------------------- SSSP IncEval over the summary
+
+// rows below n: the plain distances after the reset; mirror rows: unreached
+__global__ void k_dist_all_init(const unsigned long long* __restrict__ dist, uint32_t n,
+                                uint32_t all_n, unsigned long long* __restrict__ dall) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < all_n; v += gridDim.x * blockDim.x)
+    dall[v] = v < n ? dist[v] : kInfBits;
+}
+
+// an in-mirror starts from its master's distance (their edge weighs 0)
+__global__ void k_dist_mirrors(const uint32_t* __restrict__ mir, const uint32_t* __restrict__ master,
+                               uint32_t cnt, unsigned long long* __restrict__ dall) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+    dall[mir[i]] = dall[master[i]];
+}
+
+bool sssp_summary_ready(sg_ctx* ctx) {
+  SummaryDev* D = sdev(ctx);
+  return D && D->valid && D->sssp_ready && ctx->g.weighted;
+}
+
+// The incremental stage of SumSyncTraversalWorker
+// (sum_sync_traversal_worker.h:1424-1690): deltaCompute's reset, then rounds
+// over the summary (boundary edges, entry -> exit shortcuts, master -> mirror
+// edges) instead of the original graph, then the correction of the inner
+// members through the entry -> member shortcuts.
+//   1. The reset BFS over the shortest-path tree and the re-seed pulls of the
+//      plain IncEval (shared code): every vertex whose distance can grow is
+//      reset and restarts from the best in-neighbour that kept its distance;
+//      the batch's new edges are relaxed.  Distances that are not reset are
+//      final or too long, never too short.
+//   2. Shortcut distances of the supernodes the batch touched are repaired and
+//      the summarized CSR is rebuilt.
+//   3. Delta-stepping over the summarized CSR from that warm state, seeded by
+//      the reset vertices, the heads of new edges and every supernode's entry
+//      (or in-mirror): a path into a cluster reaches its exits only through an
+//      entry's shortcut, and repaired shortcuts may be shorter.
+//   4. Inner members: the minimum over their cluster's entries of entry
+//      distance + shortcut (a reset member starts from its re-seed value, an
+//      upper bound).
+//   5. Parents over the in-rows of the original graph.
+// The result equals the plain IncEval's (Dijkstra on the new graph).
+sg_status sssp_summarized_inc(sg_ctx* ctx) {
+  SummaryDev* Dp = sdev(ctx);
+  if (!Dp || !Dp->valid) return fail(ctx, SG_ERR_STATE, "compress=1 needs sg_summary_build first");
+  SummaryDev& D = *Dp;
+  Summary& S = D.S;
+  if (!ctx->g.weighted) return fail(ctx, SG_ERR_INVALID, "SSSP needs a weighted graph");
+  cudaStream_t st = ctx->stream;
+  SG_CUDA(ctx, cudaEventRecord(ctx->kev0, st));
+  SsspIncInfo info;
+  SG_TRY(sssp_inc_prepare(ctx, &info));
+  SG_TRY(sssp_summary_refresh(ctx, D));
+  const uint32_t n = S.old_n, all = S.all_n;
+  SsspState& sp = ctx->sp;
+  unsigned long long* dall = nullptr;
+  uint32_t* seeds = nullptr;
+  const uint64_t nseeds = (uint64_t)info.total + info.nadd + D.sk_nspid;
+  SG_TRY(dalloc(ctx, &dall, all));
+  SG_TRY(dalloc(ctx, &seeds, std::max<uint64_t>(nseeds, 1)));
+  k_dist_all_init<<<grid_for(all, 256), 256, 0, st>>>(sp.dist, n, all, dall);
+  if (D.sk_nimir)
+    k_dist_mirrors<<<grid_for(D.sk_nimir, 256), 256, 0, st>>>(D.sk_imir, D.sk_imaster, D.sk_nimir,
+                                                            dall);
+  count_launch(ctx, 1 + (D.sk_nimir > 0));
+  uint64_t o = 0;
+  if (info.total)
+    SG_CUDA(ctx, cudaMemcpyAsync(seeds, sp.seeds, 4ull * info.total, cudaMemcpyDeviceToDevice, st));
+  o += info.total;
+  if (info.nadd)
+    SG_CUDA(ctx, cudaMemcpyAsync(seeds + o, sp.padd_dst, 4ull * info.nadd, cudaMemcpyDeviceToDevice,
+                                 st));
+  o += info.nadd;
+  if (D.sk_nspid)
+    SG_CUDA(ctx, cudaMemcpyAsync(seeds + o, D.sk_spid, 4ull * D.sk_nspid, cudaMemcpyDeviceToDevice,
+                                 st));
+  SsspView G{all, D.sk_m, D.sk_off, D.sk_deg, D.sk_col, D.sk_w};
+  unsigned long long h_cnt[4] = {0, 0, 0, 0};
+  sg_status rs = sssp_run_view_warm(ctx, G, seeds, (uint32_t)nseeds, dall, h_cnt);
+  if (rs != SG_OK) {
+    dfree(dall);
+    dfree(seeds);
+    return rs;
+  }
+  if (D.sk_ncorr)
+    k_sssp_correct<<<grid_for((uint64_t)D.sk_ncorr * 32, 256), 256, 0, st>>>(
+        D.sk_ncorr, D.sk_coff, D.sk_crow, D.sk_cv, D.sk_cd, dall);
+  k_copy_u64<<<grid_for(n, 256), 256, 0, st>>>(dall, n, sp.dist);
+  count_launch(ctx, 2);
+  SG_CUDA(ctx, cudaGetLastError());
+  SG_CUDA(ctx, cudaEventRecord(ctx->kev1, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  float ms = 0.f;
+  SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->kev0, ctx->kev1));
+  dfree(dall);
+  dfree(seeds);
+  ctx->stats.shortcut_edges = 0;
+  return sssp_inc_finish_external(ctx, info, h_cnt, ms);
 }
 
 }  // namespace sg

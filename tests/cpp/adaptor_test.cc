@@ -152,6 +152,22 @@ int main(int argc, char** argv) {
       w.Output(os);
       w.Finalize();
     }
+    if (argc > 7) {  // SSSP over the summary (cluster file argv[7])
+      using App = grape::SSSPIngress<FragW, double>;
+      auto app = std::make_shared<App>();
+      app->source = 3;
+      suminc_gb300::GpuWorkerOptions o;
+      o.compress = true;
+      o.cluster_file = argv[7];
+      o.update_file = argv[3];
+      suminc_gb300::GpuSumSyncTraversalWorker<App> w(app, frag, o);
+      w.Init(0);
+      w.Query();
+      std::ofstream os(std::string(argv[5]) + ".sum");
+      os.precision(17);
+      w.Output(os);
+      w.Finalize();
+    }
   } catch (const suminc_gb300::Error& e) {
     std::fprintf(stderr, "%s\n", e.what());
     return 1;

@@ -77,6 +77,10 @@ def test_cpp_workers_match_c_abi(binary, tmp_path):
     assert np.abs(pr[:, 1] - x).max() <= 1e-6 * max(1.0, np.abs(x).max()) + 1e-9
     nrp, ncol, nw = hg2.csr()
     assert np.array_equal(ss[:, 1], oracle.dijkstra(nrp, ncol, nw, 3))
+    # SSSP over the summary built from the same cluster file
+    sss = np.loadtxt(str(oss) + ".sum")
+    assert np.array_equal(sss[:, 0].astype(np.int64), oid(np.arange(n)))
+    assert np.array_equal(sss[:, 1], oracle.dijkstra(nrp, ncol, nw, 3))
     # message_type = pull over the summary: same file, same batch
     pp = np.loadtxt(str(opr) + ".pull")
     assert np.array_equal(pp[:, 0].astype(np.int64), oid(np.arange(n)))

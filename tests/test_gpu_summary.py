@@ -196,3 +196,47 @@ def test_summarized_pagerank_staged_and_global_clusters():
             x2 = ctx.pr_inceval()
             assert np.abs(x2 - oracle.pr_fixed_point(nrp, ncol)).sum() <= TOL_FIXED
             assert np.abs(x2 - plain.pr_inceval()).sum() <= TOL_REF
+
+
+@pytest.mark.parametrize("name,source", [("planted2600", 0), ("planted2600", 5), ("rmat12", 0)])
+def test_summarized_sssp_inceval_over_several_batches(name, source):
+    """IncEval over the summary (reset, rounds over boundary edges and
+    repaired shortcuts, inner correction) after each of several batches:
+    the fixture's batch, random changes, a deleted intra-cluster edge on a
+    shortest path, and an inserted intra-cluster edge that shortens an
+    entry -> exit shortcut; bit-exact against Dijkstra each time."""
+    fx = load(name)
+    rp, col, w = fx["row_ptr"], fx["col"], fx["w"]
+    cl = fx["clusters"]
+    cur = (rp, col, w)
+    with sg.Context(0, compress=1) as ctx:
+        ctx.load_csr(rp, col, w)
+        ctx.summary_build(cl)
+        ctx.sssp_peval(source)
+        for b in range(4):
+            if b == 0:
+                upd = fx["updates_sssp"]
+            elif b == 1:
+                upd = oracle.gen_updates(cur[0], cur[1], 60, 60, 30, seed=40 + b)
+            else:
+                d_now = oracle.dijkstra(*cur, source)
+                par = ctx.sssp_parents()
+                c = max(cl, key=len)
+                inside = set(int(v) for v in c)
+                if b == 2:
+                    # remove a shortest-path tree edge inside the cluster
+                    cand = [int(v) for v in c if int(par[v]) in inside and np.isfinite(d_now[v])]
+                    v = cand[len(cand) // 2] if cand else int(c[1])
+                    u = int(par[v]) if cand else int(c[0])
+                    upd = np.array([(u, v, 0, 1)], dtype=oracle.UPDATE_DTYPE)
+                else:
+                    # a short cut from the nearest member to the farthest one
+                    order = sorted((int(v) for v in c), key=lambda v: d_now[v])
+                    upd = np.array([(order[0], order[-1], 1, 0)], dtype=oracle.UPDATE_DTYPE)
+            cur = oracle.apply_updates(*cur, upd)
+            ctx.apply_updates(upd)
+            d1 = ctx.sssp_inceval()
+            assert np.array_equal(d1, oracle.dijkstra(*cur, source)), f"batch {b}"
+        parents = ctx.sssp_parents()
+        reach = np.isfinite(d1) & (np.arange(len(d1)) != source)
+        assert np.all(parents[reach] < len(d1))
