@@ -1897,6 +1897,39 @@ static sg_status sssp_summary_refresh(sg_ctx* ctx, SummaryDev& D) {
   return SG_OK;
 }
 
+// A source inside a cluster reaches the cluster's other members by paths
+// that pass through no entry, which no shortcut holds: its cluster is solved
+// locally from it (as the PEval of SumSyncTraversalWorker does for the
+// source's supernode), and every member (an out-mirror as its master) seeds
+// the traversal with its local distance.  *member is false for a source
+// outside the clusters (nothing added).
+static sg_status source_cluster_seeds(sg_ctx* ctx, SummaryDev& D, uint32_t source,
+                                      std::vector<uint32_t>* seeds, std::vector<double>* sdist,
+                                      bool* member) {
+  Summary& S = D.S;
+  *member = false;
+  const uint32_t c = S.id2spids[source];
+  if (c == Summary::kIdDefault || c >= S.cluster_ids.size()) return SG_OK;
+  *member = true;
+  std::vector<std::vector<double>> dist;
+  const auto& nodes = S.cluster_ids[c];
+  SG_TRY(sssp_cluster_jobs(ctx, D, {{c, local_index(nodes, source)}}, &dist));
+  const double inf = std::numeric_limits<double>::infinity();
+  for (uint32_t i = 0; i < nodes.size(); ++i) {
+    if (!(dist[0][i] < inf)) continue;
+    const uint32_t v = nodes[i];
+    if (v < S.old_n) {
+      seeds->push_back(v);
+    } else if (is_out_mirror(S, c, v)) {
+      seeds->push_back(S.mirror_master(v));
+    } else {
+      continue;
+    }
+    sdist->push_back(dist[0][i]);
+  }
+  return SG_OK;
+}
+
 sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
   SummaryDev* Dp = sdev(ctx);
   if (!Dp || !Dp->valid) return fail(ctx, SG_ERR_STATE, "compress=1 needs sg_summary_build first");
@@ -1910,25 +1943,9 @@ sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
   // seeds: the source, expanded inside its cluster when it is a member
   std::vector<uint32_t> seeds;
   std::vector<double> sdist;
-  const uint32_t c = S.id2spids[source];
-  if (c != Summary::kIdDefault && c < S.cluster_ids.size()) {
-    std::vector<std::vector<double>> dist;
-    const auto& nodes = S.cluster_ids[c];
-    SG_TRY(sssp_cluster_jobs(ctx, D, {{c, local_index(nodes, source)}}, &dist));
-    const double inf = std::numeric_limits<double>::infinity();
-    for (uint32_t i = 0; i < nodes.size(); ++i) {
-      if (!(dist[0][i] < inf)) continue;
-      const uint32_t v = nodes[i];
-      if (v < S.old_n) {
-        seeds.push_back(v);
-      } else if (is_out_mirror(S, c, v)) {
-        seeds.push_back(S.mirror_master(v));
-      } else {
-        continue;
-      }
-      sdist.push_back(dist[0][i]);
-    }
-  } else {
+  bool member = false;
+  SG_TRY(source_cluster_seeds(ctx, D, source, &seeds, &sdist, &member));
+  if (!member) {
     seeds.push_back(source);
     sdist.push_back(0.0);
   }
@@ -1966,6 +1983,13 @@ __global__ void k_dist_all_init(const unsigned long long* __restrict__ dist, uin
     dall[v] = v < n ? dist[v] : kInfBits;
 }
 
+// dist[v] <- min(dist[v], d) for a list of (vertex, distance)
+__global__ void k_dist_min_list(const uint32_t* __restrict__ v, const double* __restrict__ d,
+                                uint32_t cnt, unsigned long long* __restrict__ dall) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+    atomicMin(dall + v[i], dbits(d[i]));
+}
+
 // an in-mirror starts from its master's distance (their edge weighs 0)
 __global__ void k_dist_mirrors(const uint32_t* __restrict__ mir, const uint32_t* __restrict__ master,
                                uint32_t cnt, unsigned long long* __restrict__ dall) {
@@ -1994,6 +2018,9 @@ bool sssp_summary_ready(sg_ctx* ctx) {
 //      the reset vertices, the heads of new edges and every supernode's entry
 //      (or in-mirror): a path into a cluster reaches its exits only through an
 //      entry's shortcut, and repaired shortcuts may be shorter.
+//      A source inside a cluster also seeds its cluster's members with their
+//      distances from a local solve of the repaired cluster (paths from the
+//      source to its own cluster's members need no entry).
 //   4. Inner members: the minimum over their cluster's entries of entry
 //      distance + shortcut (a reset member starts from its re-seed value, an
 //      upper bound).
@@ -2033,9 +2060,35 @@ sg_status sssp_summarized_inc(sg_ctx* ctx) {
   if (D.sk_nspid)
     SG_CUDA(ctx, cudaMemcpyAsync(seeds + o, D.sk_spid, 4ull * D.sk_nspid, cudaMemcpyDeviceToDevice,
                                  st));
+  // the source's own cluster, solved locally on the repaired subgraph
+  std::vector<uint32_t> cs;
+  std::vector<double> cd;
+  bool member = false;
+  SG_TRY(source_cluster_seeds(ctx, D, sp.source, &cs, &cd, &member));
+  uint32_t* d_cs = nullptr;
+  double* d_cd = nullptr;
+  uint64_t nseeds_all = nseeds;
+  if (!cs.empty()) {
+    SG_TRY(dalloc(ctx, &d_cs, cs.size()));
+    SG_TRY(dalloc(ctx, &d_cd, cd.size()));
+    SG_CUDA(ctx, cudaMemcpyAsync(d_cs, cs.data(), 4ull * cs.size(), cudaMemcpyHostToDevice, st));
+    SG_CUDA(ctx, cudaMemcpyAsync(d_cd, cd.data(), 8ull * cd.size(), cudaMemcpyHostToDevice, st));
+    k_dist_min_list<<<grid_for(cs.size(), 256), 256, 0, st>>>(d_cs, d_cd, (uint32_t)cs.size(), dall);
+    count_launch(ctx);
+    uint32_t* s2 = nullptr;
+    SG_TRY(dalloc(ctx, &s2, nseeds + cs.size()));
+    if (nseeds) SG_CUDA(ctx, cudaMemcpyAsync(s2, seeds, 4ull * nseeds, cudaMemcpyDeviceToDevice, st));
+    SG_CUDA(ctx, cudaMemcpyAsync(s2 + nseeds, d_cs, 4ull * cs.size(), cudaMemcpyDeviceToDevice, st));
+    SG_CUDA(ctx, cudaStreamSynchronize(st));
+    dfree(seeds);
+    seeds = s2;
+    nseeds_all = nseeds + cs.size();
+  }
   SsspView G{all, D.sk_m, D.sk_off, D.sk_deg, D.sk_col, D.sk_w};
   unsigned long long h_cnt[4] = {0, 0, 0, 0};
-  sg_status rs = sssp_run_view_warm(ctx, G, seeds, (uint32_t)nseeds, dall, h_cnt);
+  sg_status rs = sssp_run_view_warm(ctx, G, seeds, (uint32_t)nseeds_all, dall, h_cnt);
+  dfree(d_cs);
+  dfree(d_cd);
   if (rs != SG_OK) {
     dfree(dall);
     dfree(seeds);
