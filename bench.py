@@ -296,8 +296,7 @@ def run_ours(args, D: Dist):
     hg = sg.HostGraph(rp0, col0)
     del rp0, col0
     K, W = args.steps, args.warmup
-    P = 2  # profiled steps for the per-kernel roofline
-    batches = make_batches(hg, W + 2 * K + P, bsz, 100)
+    batches = make_batches(hg, W + 2 * K, bsz, 100)
     # device-resident copies for `value`, pinned host copies for `e2e`
     dev_b = [torch.from_numpy(b.view(np.uint8)).to(f"cuda:{dev}") for b in batches[: W + K]]
     pin_b = [torch.from_numpy(b.view(np.uint8)).pin_memory() for b in batches[W + K: W + 2 * K]]
@@ -309,12 +308,16 @@ def run_ours(args, D: Dist):
     for i in range(W):
         ctx.apply_updates_ptr(bsz, dev_b[i].data_ptr(), True)
         ctx.pr_inceval_into(None)
-    # timed: device-resident batches
+    # timed: device-resident batches, with CUDA events around every kernel
+    # of the PageRank classes on the library stream (the per-launch
+    # duration of the dominant kernel for the roofline)
+    ctx.set_profile(0xFF)
     ctx.reset_stats()
     D.barrier()
     ctx.synchronize()
     ctx.record_event(0)
     relax = 0
+    pe_pull = 0
     rounds = []
     visits = []
     step_ms, inc_ms = [], []
@@ -327,6 +330,7 @@ def run_ours(args, D: Dist):
         ctx.record_event(5)
         st = ctx.stats()
         relax += st["edges_relaxed"]
+        pe_pull += st["edges_pull"]
         rounds.append(st["rounds"])
         visits.append(int(st["vertex_visits"]))
         inc_ms.append(st["elapsed_ms"])
@@ -336,7 +340,10 @@ def run_ours(args, D: Dist):
     ctx.synchronize()
     D.barrier()
     t_ms = ctx.elapsed_ms(0, 1)
-    launches = ctx.stats()["launches_total"]
+    st = ctx.stats()
+    launches = st["launches_total"]
+    kms, kl = st["kernel_ms"], st["kernel_launches"]
+    ctx.set_profile(0)
     t_ms_max = D.max(t_ms)
     relax_all = D.sum(relax)
     value = relax_all / (t_ms_max * 1e-3) / 1e9
@@ -363,22 +370,6 @@ def run_ours(args, D: Dist):
     e2e = D.sum(relax_e) / (te_ms * 1e-3) / 1e9
     clk = clocks.stop()
 
-    # profiled steps: the same work with CUDA events around every kernel of
-    # the PageRank classes; gives the per-launch duration of the dominant one
-    ctx.set_profile(0xFF)
-    ctx.reset_stats()
-    pe_pull = pe_push = 0
-    m_live = []
-    for i in range(W + 2 * K, W + 2 * K + P):
-        ctx.apply_updates(batches[i])
-        ctx.pr_inceval_into(None)
-        st = ctx.stats()
-        pe_pull += st["edges_pull"]
-        pe_push += st["edges_push"]
-        m_live.append(st["live_edges"])
-    st = ctx.stats()
-    ctx.set_profile(0)
-    kms, kl = st["kernel_ms"], st["kernel_launches"]
     total_k = sum(kms.values()) or 1.0
     kernels = {k: {"launches": kl[k], "ms": round(kms[k], 4), "share": round(kms[k] / total_k, 4)}
                for k in kms if kl[k]}
