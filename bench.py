@@ -393,7 +393,7 @@ def run_ours(args, D: Dist):
                 "algorithmic_bytes_per_launch": int(bytes_per_launch),
                 "kernels": kernels}
 
-    # accuracy of the final state (after every timed and profiled batch):
+    # accuracy of the final state (after every timed batch):
     # the FP64 residual of x on the final graph bounds ||x - x*||_1
     import oracle
     x = ctx.pr_values()
