@@ -412,6 +412,7 @@ sg_status pr_pull_worker(sg_ctx* ctx, bool inc);
 sg_status pull_free(sg_ctx* ctx);
 sg_status sssp_summarized(sg_ctx* ctx, uint32_t source);
 sg_status sssp_summarized_inc(sg_ctx* ctx);
+bool summary_no_supernodes(sg_ctx* ctx);
 bool sssp_summary_ready(sg_ctx* ctx);
 uint32_t summary_rows(sg_ctx* ctx);  // rows incl. mirrors, 0 without a summary
 sg_status summary_info(sg_ctx* ctx, sg_summary_info* out);

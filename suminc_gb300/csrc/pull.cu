@@ -382,7 +382,7 @@ sg_status pr_pull_worker(sg_ctx* ctx, bool inc) {
   DevGraph& g = ctx->g;
   PrState& s = ctx->pr;
   if (!g.valid) return fail(ctx, SG_ERR_STATE, "no graph loaded");
-  if (!ctx->opt.compress) return pr_run(ctx, inc);
+  if (!ctx->opt.compress || summary_no_supernodes(ctx)) return pr_run(ctx, inc);
   PullView V;
   SG_TRY(summary_pull_view(ctx, &V));
   if (inc && !s.valid) return fail(ctx, SG_ERR_STATE, "PageRank IncEval before PEval");

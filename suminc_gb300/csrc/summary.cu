@@ -1232,9 +1232,20 @@ static sg_status summarized_rounds(sg_ctx* ctx, SummaryDev& D, unsigned long lon
   return SG_OK;
 }
 
+// A summary whose benefit filter kept no cluster has no supernode, no
+// mirror and every vertex of type 0 (single), and no batch can add one (the
+// incremental repair works on the kept clusters): its summarized rounds are
+// the plain Ingress rounds over the whole graph.  Such a summary runs the
+// plain path (the dense pull), and its batches skip the host repair.
+bool summary_no_supernodes(sg_ctx* ctx) {
+  SummaryDev* D = sdev(ctx);
+  return D && D->valid && D->S.supernode_ids.empty();
+}
+
 sg_status pr_summarized(sg_ctx* ctx, bool inc) {
   SummaryDev* D = sdev(ctx);
   if (!D || !D->valid) return fail(ctx, SG_ERR_STATE, "compress=1 needs sg_summary_build first");
+  if (summary_no_supernodes(ctx)) return pr_run(ctx, inc);
   PrState& s = ctx->pr;
   cudaStream_t st = ctx->stream;
   unsigned long long* cnt = nullptr;
@@ -1279,6 +1290,7 @@ sg_status pr_summarized(sg_ctx* ctx, bool inc) {
 sg_status summary_after_apply(sg_ctx* ctx) {
   SummaryDev* D = sdev(ctx);
   if (!D || !D->valid) return SG_OK;
+  if (summary_no_supernodes(ctx)) return SG_OK;  // nothing to repair, ever
   const DevBatch& B = ctx->batch;
   // deleted / added pairs of the batch (actions are small; copy to host)
   const uint64_t na = B.n_act;
@@ -1937,6 +1949,7 @@ sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
   Summary& S = D.S;
   if (!ctx->g.weighted) return fail(ctx, SG_ERR_INVALID, "SSSP needs a weighted graph");
   if (source >= S.old_n) return fail(ctx, SG_ERR_INVALID, "source >= n");
+  if (summary_no_supernodes(ctx)) return sssp_run_peval(ctx, source);
   cudaStream_t st = ctx->stream;
   SG_CUDA(ctx, cudaEventRecord(ctx->kev0, st));
   SG_TRY(sssp_summary_refresh(ctx, D));

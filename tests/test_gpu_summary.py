@@ -240,3 +240,33 @@ def test_summarized_sssp_inceval_over_several_batches(name, source):
         parents = ctx.sssp_parents()
         reach = np.isfinite(d1) & (np.arange(len(d1)) != source)
         assert np.all(parents[reach] < len(d1))
+
+
+def test_summary_without_supernodes_runs_the_plain_path():
+    """Clusters the benefit filter rejects (groups of the highest-degree
+    vertices: few inner edges, many entries and exits) leave a summary with
+    no supernode; PageRank and SSSP over it equal the plain path, before and
+    after a batch, and the batch needs no repair."""
+    fx = load("rmat12")
+    rp, col, w = fx["row_ptr"], fx["col"], fx["w"]
+    deg = np.diff(rp).astype(np.int64) + np.bincount(col, minlength=len(rp) - 1)
+    top = np.argsort(-deg, kind="stable")[:64].astype(np.uint32)
+    groups = [np.sort(top[i:i + 8]) for i in range(0, 64, 8)]
+    upd = fx["updates_sssp"]
+    with sg.Context(0, compress=1) as ctx, sg.Context(0) as plain:
+        ctx.load_csr(rp, col, w)
+        ctx.summary_build(groups)
+        info = ctx.summary_info()
+        assert info["supernodes"] == 0 and info["clusters"] == 0
+        plain.load_csr(rp, col, w)
+        x = ctx.pr_peval()
+        assert np.abs(x - plain.pr_peval()).sum() <= TOL_REF
+        assert np.array_equal(ctx.sssp_peval(0), plain.sssp_peval(0))
+        ctx.apply_updates(upd)
+        plain.apply_updates(upd)
+        nrp, ncol, nw = oracle.apply_updates(rp, col, w, upd)
+        x2 = ctx.pr_inceval()
+        assert np.abs(x2 - oracle.pr_fixed_point(nrp, ncol)).sum() <= TOL_FIXED
+        d2 = ctx.sssp_inceval()
+        assert np.array_equal(d2, oracle.dijkstra(nrp, ncol, nw, 0))
+        assert np.array_equal(d2, plain.sssp_inceval())
