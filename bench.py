@@ -18,9 +18,14 @@ Metric: GTEPS = edge relaxations performed during IncEval / IncEval time.
 The graph (>1 GB per direction) is larger than the 126 MB L2, so no flush is
 needed between steps.
 
+The line also carries `summarized`: the same graph and first batches with
+compress = 1 (summary from the greedy builder's clusters of the low-degree
+subgraph, shortcut weights on the GPU, the batch apply that repairs the
+summary timed with each IncEval) and the summary's counters.
+
 --impl reference times the CPU restatement of the reference worker
-(oracle/: AmendValue(-1/+1) + delta rounds, OpenMP over every host core) on
-the same workload, one bounded sample per step.
+(oracle/, no library code: the same graph and batches, complete IncEvals
+from a converged PEval, OpenMP over every host core) within a time budget.
 """
 from __future__ import annotations
 
