@@ -1132,10 +1132,14 @@ def run_summarized(args, D: Dist):
         del out[m]["x"], out[m]["d0"]
     s_inc = float(np.mean(out[1]["inceval_ms"]))
     p_inc = float(np.mean(out[0]["inceval_ms"]))
+    # a batch's whole cost: the apply (with compress = 1 it repairs the
+    # summary on the host) plus the IncEval
+    s_step = float(np.mean(np.add(out[1]["apply_ms"], out[1]["inceval_ms"])))
+    p_step = float(np.mean(np.add(out[0]["apply_ms"], out[0]["inceval_ms"])))
     return {
-        "metric": "PageRank IncEval over the summarized graph (ms per batch)",
-        "value": round(s_inc, 3), "unit": "ms", "n_gpus": D.ws, "steps": args.steps, "warmup": 0,
-        "ms_per_step": round(s_inc, 3), "higher_is_better": False, "scaling": "weak",
+        "metric": "PageRank batch (apply + summary repair + IncEval) over the summarized graph (ms per batch)",
+        "value": round(s_step, 3), "unit": "ms", "n_gpus": D.ws, "steps": args.steps, "warmup": 0,
+        "ms_per_step": round(s_step, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic community graph (seeded)",
         "config": {"workload": f"summarized PageRank / SSSP, {n_comm} communities of 40",
                    "vertices": n, "edges": E, "batch_changes": bsz,
@@ -1143,6 +1147,8 @@ def run_summarized(args, D: Dist):
                    "parallelism": "single GPU"},
         "summarized": out[1], "plain": out[0], "summarized_pull": out["pull"],
         "summarized_over_plain_inceval": round(s_inc / p_inc, 3),
+        "step_ms": {"summarized": round(s_step, 3), "plain": round(p_step, 3),
+                    "summarized_over_plain": round(s_step / p_step, 3)},
         "pr_l1_vs_fp64": l1, "sssp_exact_vs_dijkstra": exact,
     }
 
