@@ -222,3 +222,28 @@ def test_tight_threshold_reference_against_fixed_point_and_oracle():
     d2 = oracle.pr_amend((rp, col), (nrp, ncol), x, delta)
     x2, _, _ = oracle.ingress_pr(nrp, ncol, x=x, delta=d2, tau=1e-10)
     assert np.abs(x2 - fx["ref_pr_plain_inc"]).sum() < 1e-6
+
+
+def _u32_dist(d):
+    out = np.full(len(d), 0xFFFFFFFF, np.uint32)
+    fin = np.isfinite(d)
+    out[fin] = d[fin].astype(np.uint32)
+    return out
+
+
+def test_rmat20_inputs_regenerate_and_reference_equals_dijkstra():
+    """rmat20_sssp: the weighted graph and the 100,000-change batch
+    regenerate from their seeds; the reference's summarized PEval and both of
+    its incremental workers equal FP64 Dijkstra bit for bit."""
+    fx = load("rmat20_sssp")
+    rp, col, w = oracle.rmat(20, 1 << 24, seed=1, weight_kind=1, wlo=1, whi=100)
+    assert _sha(rp, col, w) == str(fx["input_sha256"])
+    upd = oracle.gen_updates(rp, col, 40000, 40000, 20000, seed=2)
+    assert _sha(upd) == str(fx["updates_sha256"])
+    assert np.array_equal(_u32_dist(oracle.dijkstra(rp, col, w, 0)), fx["ref_sssp_sum_peval"])
+    nrp, ncol, nw = oracle.apply_updates(rp, col, w, upd)
+    d1 = _u32_dist(oracle.dijkstra(nrp, ncol, nw, 0))
+    assert np.array_equal(d1, fx["ref_sssp_plain_inc"])
+    assert np.array_equal(d1, fx["ref_sssp_sum_inc"])
+    st = json.loads(str(fx["stats"]))["sssp_peval"]
+    assert st["spn_num"][0] > 0
