@@ -1073,7 +1073,7 @@ def run_summarized(args, D: Dist):
         sp_first = ctx.stats()
         d0 = ctx.sssp_peval(0)  # shortcut distances and sketch now built
         sp = ctx.stats()
-        inc_ms, rounds, apply_ms = [], [], []
+        inc_ms, rounds, apply_ms, sssp_inc_ms = [], [], [], []
         for b in batches:
             t1 = time.perf_counter()
             ctx.apply_updates(b)  # with compress=1 this includes the summary repair
@@ -1082,6 +1082,11 @@ def run_summarized(args, D: Dist):
             st = ctx.stats()
             inc_ms.append(st["elapsed_ms"])
             rounds.append(st["rounds"])
+            # SSSP from 0 re-evaluated after the same batch (with compress=1
+            # over the summary: reset, rounds over the summarized CSR and
+            # repaired shortcuts, inner correction)
+            d1 = ctx.sssp_inceval()
+            sssp_inc_ms.append(ctx.stats()["elapsed_ms"])
         # one more batch (the same one in both modes) with CUDA events around
         # every kernel class
         ctx.set_profile(0xFF)
@@ -1098,7 +1103,8 @@ def run_summarized(args, D: Dist):
                      "sssp_peval_first_ms": round(sp_first["elapsed_ms"], 3),
                      "inceval_ms": [round(v, 3) for v in inc_ms], "inceval_rounds": rounds,
                      "apply_ms": [round(v, 3) for v in apply_ms],
-                     "build_s": round(build_s, 2), "x": x, "d0": d0}
+                     "sssp_inceval_ms": [round(v, 3) for v in sssp_inc_ms],
+                     "build_s": round(build_s, 2), "x": x, "d0": d0, "d1": d1}
         if mode:
             out[mode]["summary"] = {k: info[k] for k in ("clusters", "supernodes", "shortcut_edges",
                                                          "boundary_edges", "all_rows")}
@@ -1128,8 +1134,15 @@ def run_summarized(args, D: Dist):
     # the graph after them
     l1 = {m: float(np.abs(out[m]["x"] - xs).sum()) for m in (0, 1)}
     exact = {m: bool(np.array_equal(out[m]["d0"], d_ref)) for m in (0, 1)}
+    # the graph after the regular batches (before the profiled one): SSSP
+    # IncEval's last result against Dijkstra there
+    g1 = (rp, col, w)
+    for b in batches:
+        g1 = oracle.apply_updates(*g1, b)
+    d1_ref = oracle.dijkstra(*g1, 0)
+    exact_inc = {m: bool(np.array_equal(out[m]["d1"], d1_ref)) for m in (0, 1)}
     for m in (0, 1):
-        del out[m]["x"], out[m]["d0"]
+        del out[m]["x"], out[m]["d0"], out[m]["d1"]
     s_inc = float(np.mean(out[1]["inceval_ms"]))
     p_inc = float(np.mean(out[0]["inceval_ms"]))
     # a batch's whole cost: the apply (with compress = 1 it repairs the
@@ -1150,6 +1163,9 @@ def run_summarized(args, D: Dist):
         "step_ms": {"summarized": round(s_step, 3), "plain": round(p_step, 3),
                     "summarized_over_plain": round(s_step / p_step, 3)},
         "pr_l1_vs_fp64": l1, "sssp_exact_vs_dijkstra": exact,
+        "sssp_inceval_exact_vs_dijkstra": exact_inc,
+        "sssp_inceval_ms": {"summarized": round(float(np.mean(out[1]["sssp_inceval_ms"])), 3),
+                            "plain": round(float(np.mean(out[0]["sssp_inceval_ms"])), 3)},
     }
 
 
