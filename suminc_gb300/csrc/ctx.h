@@ -72,6 +72,8 @@ struct DevGraph {
   PullLists in_wl;   // over the in-CSR (PageRank pulls); rebuilt after each update
   PullLists out_wl;  // over the out-CSR (adjoint pulls); built on demand
   HubView hub;       // hub cache of the in-CSR pull; chosen on first use
+  HubView hub_out;   // the same for pulls over the out-CSR (the adjoint);
+                     // re-encoded in full after a batch
   uint64_t gen = 0;  // bumped whenever the adjacency changes
 };
 

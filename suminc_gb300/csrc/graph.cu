@@ -195,6 +195,8 @@ sg_status graph_free(sg_ctx* ctx) {
   pull_lists_free(g.out_wl);
   dfree(g.hub.rank);
   dfree(g.hub.col);
+  dfree(g.hub_out.rank);
+  dfree(g.hub_out.col);
   const uint64_t gen = g.gen;  // generations keep growing across graphs
   g = DevGraph();
   g.gen = gen + 1;

@@ -18,9 +18,10 @@
 //                 lane (incoming sum, residual, activation, next push
 //                 value); a vertex spanning tiles gets its partial sums by
 //                 atomicAdd.  With the hub cache (the default on graphs
-//                 with enough high out-degree vertices) each CTA first copies
-//                 the hubs' push values into shared memory and reads an
-//                 encoded column copy in which a hub's id is its slot
+//                 with enough high out-degree vertices) push values are
+//                 indexed by out-degree rank, each CTA first copies the
+//                 lowest ranks' push values into shared memory, and the pull
+//                 reads an encoded column copy that holds ranks
 //   k_pr_fixup    updates the tile-spanning vertices; its last block makes
 //                 the termination decision on the device
 // Push values are double-buffered by pull index.  When the residual passes
@@ -360,9 +361,8 @@ sg_status pr_hub_after_apply(sg_ctx* ctx, const uint32_t* rows, uint64_t nrows, 
 // (ties by id); the hubs are the lowest min(kmax, vertices of out-degree >= 2)
 // ranks.  The order is kept while the graph takes batches (any order is
 // correct; this one is chosen for locality).
-static sg_status hub_choose(sg_ctx* ctx, uint32_t kmax) {
+static sg_status hub_choose(sg_ctx* ctx, HubView& H, const uint32_t* hot_deg, uint32_t kmax) {
   DevGraph& g = ctx->g;
-  HubView& H = g.hub;
   cudaStream_t st = ctx->stream;
   dfree(H.rank);
   dfree(H.col);
@@ -374,7 +374,7 @@ static sg_status hub_choose(sg_ctx* ctx, uint32_t kmax) {
   SG_TRY(dalloc(ctx, &d_cnt, 1));
   unsigned long long c = 0;
   SG_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, 8, st));
-  k_count_deg_ge<<<grid_for(g.n, 256), 256, 0, st>>>(g.out.deg, g.n, 2, d_cnt);
+  k_count_deg_ge<<<grid_for(g.n, 256), 256, 0, st>>>(hot_deg, g.n, 2, d_cnt);
   SG_CUDA(ctx, cudaMemcpyAsync(&c, d_cnt, 8, cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   dfree(d_cnt);
@@ -386,7 +386,7 @@ static sg_status hub_choose(sg_ctx* ctx, uint32_t kmax) {
   SG_TRY(dalloc(ctx, &iota, g.n));
   SG_TRY(dalloc(ctx, &order, g.n));
   SG_TRY(dalloc(ctx, &H.rank, g.n));
-  k_rank_keys<<<grid_for(g.n, 256), 256, 0, st>>>(g.out.deg, g.n, key, iota);
+  k_rank_keys<<<grid_for(g.n, 256), 256, 0, st>>>(hot_deg, g.n, key, iota);
   SG_TRY(cub_sort_pairs_u32_u32(ctx, key, key2, iota, order, g.n));
   k_rank_scatter<<<grid_for(g.n, 256), 256, 0, st>>>(order, g.n, H.rank);
   count_launch(ctx, 4);
@@ -404,33 +404,33 @@ static sg_status hub_choose(sg_ctx* ctx, uint32_t kmax) {
 // (or when the cap changes), the encoded column copy refreshed when the
 // adjacency has changed since.  Returns null when the cache is off or too
 // small.
-static sg_status hub_view(sg_ctx* ctx, const HubView** out) {
+static sg_status hub_view(sg_ctx* ctx, HubView& H, const DevCSR& c, const uint32_t* hot_deg,
+                          const HubView** out) {
   DevGraph& g = ctx->g;
-  HubView& H = g.hub;
   *out = nullptr;
   const int opt = ctx->opt.pull_hubs;
   const uint32_t kmax = opt < 0 ? 0u : (opt == 0 ? kHubAuto : std::min<uint32_t>((uint32_t)opt, kHubMax));
-  if (!H.chosen || H.kmax != kmax) SG_TRY(hub_choose(ctx, kmax));
+  if (!H.chosen || H.kmax != kmax) SG_TRY(hub_choose(ctx, H, hot_deg, kmax));
   if (H.k == 0) return SG_OK;
-  if (H.gen != g.gen || H.cap != g.in.pool_cap || !H.col) {
-    if (H.cap != g.in.pool_cap || !H.col) {
+  if (H.gen != g.gen || H.cap != c.pool_cap || !H.col) {
+    if (H.cap != c.pool_cap || !H.col) {
       dfree(H.col);
       H.col = nullptr;
       H.cap = 0;
       // the copy is an optimisation: without room for it the pull runs
       // uncached (the cudaMalloc error is cleared by dalloc)
-      if (dalloc(ctx, &H.col, std::max<uint64_t>(g.in.pool_cap, 1)) != SG_OK) {
+      if (dalloc(ctx, &H.col, std::max<uint64_t>(c.pool_cap, 1)) != SG_OK) {
         H.col = nullptr;
         return SG_OK;
       }
-      H.cap = g.in.pool_cap;
+      H.cap = c.pool_cap;
     }
-    k_hub_encode<<<grid_for(H.cap, 256), 256, 0, ctx->stream>>>(g.in.col, H.cap, H.rank, g.n,
+    k_hub_encode<<<grid_for(H.cap, 256), 256, 0, ctx->stream>>>(c.col, H.cap, H.rank, g.n,
                                                                   H.col);
     count_launch(ctx);
     SG_CUDA(ctx, cudaGetLastError());
     H.gen = g.gen;
-    H.layout = g.in.layout;
+    H.layout = c.layout;
   }
   static bool s_attr[64] = {};
   if (ctx->device >= 0 && ctx->device < 64 && !s_attr[ctx->device]) {
@@ -634,7 +634,12 @@ sg_status pr_rounds_ex(sg_ctx* ctx, const PrRunSpec& R) {
   SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
   // the hub cache serves pulls over the in-CSR (its encoded column copy)
   const HubView* hub = nullptr;
-  if (R.csr == &g.in && L.quads > 0) SG_TRY(hub_view(ctx, &hub));
+  // pulls over the in-CSR gather the push values of in-neighbours (hot:
+  // high out-degree), the adjoint's pulls over the out-CSR those of
+  // out-neighbours (hot: high in-degree); each direction has its own view
+  if (R.csr == &g.in && L.quads > 0) SG_TRY(hub_view(ctx, g.hub, g.in, g.out.deg, &hub));
+  else if (R.csr == &g.out && L.quads > 0)
+    SG_TRY(hub_view(ctx, g.hub_out, g.out, g.in.deg, &hub));
   if (hub) {
     WP.col = hub->col;
     WP.nhub = hub->k;
