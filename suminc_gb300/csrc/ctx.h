@@ -48,13 +48,14 @@ struct PullLists {
   uint64_t gen = ~0ull;         // graph generation the lists describe
 };
 
-// Hub cache of the PageRank pull: the vertices with the highest out-degree
-// (their push values are gathered most often) and a copy of the in-CSR
-// column pool in which a hub's id is replaced by 0x80000000 | its slot.
+// Vertex order and hub cache of a PageRank pull: every vertex ranked by how
+// often its push value is gathered (its degree in the other direction,
+// highest first) and a copy of the pulled CSR's column pool holding ranks;
+// push values are indexed by rank and the lowest ranks sit in shared memory.
 struct HubView {
   uint32_t* rank = nullptr;  // [n] position of each vertex in the pull's vertex
-                             // order (out-degree descending, ties by id)
-  uint32_t* col = nullptr;   // [cap] in-CSR col pool with ids replaced by ranks
+                             // order (degree descending, ties by id)
+  uint32_t* col = nullptr;   // [cap] col pool with ids replaced by ranks
   uint32_t k = 0;            // hubs: ranks below k live in shared memory
   uint32_t kmax = 0;         // the cap the set was chosen under
   bool chosen = false;
