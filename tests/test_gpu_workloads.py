@@ -147,3 +147,25 @@ def test_tight_threshold_within_1e6_of_reference():
         ctx.apply_updates(base["updates_pr"])
         x3 = ctx.pr_inceval()
         assert np.abs(x3 - fx["ref_pr_plain_inc"]).sum() <= TOL_TIGHT
+
+
+def test_rmat22_incremental_pagerank_and_sssp_size_independent_checks():
+    """R-MAT scale 22 (67 M edges), two 0.1 % batches each: PageRank IncEval
+    within the FP64 residual bound of the fixed point (||x - x*||_1 <=
+    residual / (1 - d) <= 1e-5) and SSSP IncEval bit-exact against Dijkstra
+    on the final graph."""
+    scale, E = 22, 16 << 22
+    rp, col, w = oracle.rmat(scale, E, seed=5, weight_kind=1, wlo=1, whi=100)
+    with sg.Context(0) as ctx:
+        ctx.generate_rmat(scale, E, seed=5, weight_kind=1, wlo=1, whi=100)
+        ctx.pr_peval(out=False)
+        ctx.sssp_peval(0)
+        cur = (rp, col, w)
+        for i in range(2):
+            upd = oracle.gen_updates(cur[0], cur[1], E // 2000, E // 2000, 0, seed=60 + i)
+            cur = oracle.apply_updates(*cur, upd)
+            ctx.apply_updates(upd)
+            x = ctx.pr_inceval()
+            d = ctx.sssp_inceval()
+        assert oracle.pr_residual_l1(cur[0], cur[1], x) / 0.15 <= TOL_FIXED
+        assert np.array_equal(d, oracle.dijkstra(*cur, 0))
