@@ -41,6 +41,8 @@ struct AdjState {
   uint64_t dw_cap = 0;
   uint64_t* prp = nullptr;                 // packed sorted out-CSR
   uint32_t* pcol = nullptr;
+  uint32_t* psrc = nullptr;                // source of each packed entry
+  float *xs = nullptr, *ls = nullptr;      // x + delta, lambda + dlambda
   uint64_t packed_gen = ~0ull, packed_cap = 0;
   bool fwd_valid = false, adj_valid = false;
   uint64_t fwd_gen = 0;
@@ -52,7 +54,7 @@ static AdjState* astate(sg_ctx* ctx) { return (AdjState*)ctx->adjoint_state; }
 static void afree_arrays(AdjState& S) {
   dfree(S.x); dfree(S.delta); dfree(S.lam); dfree(S.dlam); dfree(S.pv0); dfree(S.pvb);
   dfree(S.misc); dfree(S.res); dfree(S.cnt); dfree(S.vec); dfree(S.dt); dfree(S.dw);
-  dfree(S.prp); dfree(S.pcol);
+  dfree(S.prp); dfree(S.pcol); dfree(S.psrc); dfree(S.xs); dfree(S.ls);
 }
 
 sg_status adjoint_free(sg_ctx* ctx) {
@@ -106,21 +108,26 @@ __global__ void k_adj_seed(uint32_t n, float* lam, float* dlam, const float* g, 
   if (threadIdx.x == 0 && b != 0.0) atomicAdd(gsum, b);
 }
 
-// dL/dw_uv = d * (lambda + dlambda)_v * (x + delta)_u over the packed rows
-__global__ void k_adj_grad_w(uint32_t n, const uint64_t* __restrict__ rp,
-                             const uint32_t* __restrict__ col, const float* __restrict__ lam,
-                             const float* __restrict__ dlam, const float* __restrict__ x,
-                             const float* __restrict__ delta, float d, float* __restrict__ dw) {
+// dL/dw_uv = d * (lambda + dlambda)_v * (x + delta)_u, a thread per packed
+// entry: the source and column streams are read once and coalesced, the
+// source's value is nearly coalesced (entries sorted by source), the
+// column's adjoint value is the one random gather per edge (both sums
+// formed once per vertex beforehand)
+__global__ void k_adj_grad_w(uint64_t m, const uint32_t* __restrict__ src,
+                             const uint32_t* __restrict__ col, const float* __restrict__ xs,
+                             const float* __restrict__ ls, float d, float* __restrict__ dw) {
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m;
+       e += (uint64_t)gridDim.x * blockDim.x)
+    dw[e] = d * xs[src[e]] * ls[col[e]];
+}
+
+// the source of every packed entry (warp per row; once per packing)
+__global__ void k_row_ids(uint32_t n, const uint64_t* __restrict__ rp, uint32_t* __restrict__ src) {
   const uint32_t lane = threadIdx.x & 31;
   for (uint64_t wv = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; wv < n;
        wv += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
-    const uint32_t u = (uint32_t)wv;
-    const float xu = d * (x[u] + delta[u]);
-    const uint64_t a = rp[u], b = rp[u + 1];
-    for (uint64_t e = a + lane; e < b; e += 32) {
-      const uint32_t v = col[e];
-      dw[e] = xu * (lam[v] + dlam[v]);
-    }
+    const uint64_t a = rp[wv], b = rp[wv + 1];
+    for (uint64_t e = a + lane; e < b; e += 32) src[e] = (uint32_t)wv;
   }
 }
 
@@ -189,13 +196,17 @@ sg_status pr_adjoint(sg_ctx* ctx, const float* dl_dx_host, bool on_device, float
   if (S.packed_gen != g.gen) {
     if (m + 1 > S.packed_cap) {
       dfree(S.pcol);
+      dfree(S.psrc);
       dfree(S.dw);
       S.packed_cap = m + 1;
       SG_TRY(dalloc(ctx, &S.pcol, S.packed_cap));
+      SG_TRY(dalloc(ctx, &S.psrc, S.packed_cap));
       SG_TRY(dalloc(ctx, &S.dw, S.packed_cap));
     }
     if (!S.prp) SG_TRY(dalloc(ctx, &S.prp, (uint64_t)n + 1));
     SG_TRY(packed_sorted_out(ctx, S.prp, S.pcol));
+    k_row_ids<<<grid_for((uint64_t)n * 32, 256), 256, 0, st>>>(n, S.prp, S.psrc);
+    count_launch(ctx);
     S.packed_gen = g.gen;
   }
   cudaEvent_t e0 = ctx->kev0, e1 = ctx->kev1;
@@ -235,9 +246,14 @@ sg_status pr_adjoint(sg_ctx* ctx, const float* dl_dx_host, bool on_device, float
     S.info.adjoint_edges = 0;
   }
   const float d = (float)ctx->opt.damping;
+  if (!S.xs) SG_TRY(dalloc(ctx, &S.xs, n));
+  if (!S.ls) SG_TRY(dalloc(ctx, &S.ls, n));
+  k_add<<<grid_for(n, 256), 256, 0, st>>>(n, S.x, S.delta, S.xs);
+  k_add<<<grid_for(n, 256), 256, 0, st>>>(n, S.lam, S.dlam, S.ls);
+  count_launch(ctx, 2);
   kprof_begin(ctx);
-  k_adj_grad_w<<<grid_for((uint64_t)n * 32, 256), 256, 0, st>>>(n, S.prp, S.pcol, S.lam, S.dlam,
-                                                                S.x, S.delta, d, S.dw);
+  k_adj_grad_w<<<grid_for(m, 256, ctx->num_sms * 16), 256, 0, st>>>(m, S.psrc, S.pcol, S.xs, S.ls,
+                                                                      d, S.dw);
   kprof_end(ctx, SG_K_ADJOINT);
   k_adj_grad_t<<<grid_for(n, 256), 256, 0, st>>>(n, S.lam, S.dlam, 1.f - d, S.dt);
   count_launch(ctx);
