@@ -22,7 +22,10 @@
 //                         (sum_sync_iter_worker.h:1385-1492)
 // after which the plain rounds of pagerank.cu finish the residual.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <unordered_map>
@@ -113,6 +116,32 @@ struct SummaryDev {
 };
 
 static SummaryDev* sdev(sg_ctx* ctx) { return (SummaryDev*)ctx->summary; }
+
+// Host phase times of the summary's maintenance, printed to stderr when the
+// environment sets SUMINC_GB300_TRACE (a diagnostic; off by default).
+struct PhaseTrace {
+  bool on;
+  const char* what;
+  std::chrono::steady_clock::time_point t0, t;
+  explicit PhaseTrace(const char* w) : what(w) {
+    static const bool env = std::getenv("SUMINC_GB300_TRACE") != nullptr;
+    on = env;
+    t0 = t = std::chrono::steady_clock::now();
+  }
+  void mark(const char* phase) {
+    if (!on) return;
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "[suminc_gb300] %s %s %.2f ms\n", what, phase,
+                 std::chrono::duration<double, std::milli>(now - t).count());
+    t = now;
+  }
+  ~PhaseTrace() {
+    if (on)
+      std::fprintf(stderr, "[suminc_gb300] %s total %.2f ms\n", what,
+                   std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
+                       .count());
+  }
+};
 
 static void sfree(SummaryDev& D) {
   dfree(D.is_off); dfree(D.ib_off); dfree(D.sync_off);
@@ -1291,6 +1320,7 @@ sg_status summary_after_apply(sg_ctx* ctx) {
   SummaryDev* D = sdev(ctx);
   if (!D || !D->valid) return SG_OK;
   if (summary_no_supernodes(ctx)) return SG_OK;  // nothing to repair, ever
+  PhaseTrace T("repair");
   const DevBatch& B = ctx->batch;
   // deleted / added pairs of the batch (actions are small; copy to host)
   const uint64_t na = B.n_act;
@@ -1326,6 +1356,7 @@ sg_status summary_after_apply(sg_ctx* ctx) {
   };
   std::sort(ops_out.begin(), ops_out.end(), by_row_col);
   std::sort(ops_in.begin(), ops_in.end(), by_row_col);
+  T.mark("actions");
   const bool patched = D->out.n == n && D->in.n == n && host_adj_patch(D->out, ops_out) &&
                        host_adj_patch(D->in, ops_in);
   if (!patched || D->out.rp[n] != ctx->g.m) {
@@ -1338,7 +1369,9 @@ sg_status summary_after_apply(sg_ctx* ctx) {
     host_transpose(D->out, D->in);
   }
   Summary& S = D->S;
+  T.mark("host graph patch");
   summary_inc_entries(S, D->out, D->in, deleted, added);
+  T.mark("entries");
   {
     std::vector<uint32_t> u = D->pending_clusters;
     u.insert(u.end(), S.update_cluster_ids.begin(), S.update_cluster_ids.end());
@@ -1348,15 +1381,20 @@ sg_status summary_after_apply(sg_ctx* ctx) {
   }
   summary_judge_out_bound(S, D->out, &S.update_cluster_ids);
   summary_build_subgraph(S, D->out, D->in, &S.update_cluster_ids);
+  T.mark("exits and subgraphs");
   std::vector<uint32_t> sps;
   for (uint32_t v : S.update_source_id) {
     const uint32_t sp = S.Fc_map[v];
     if (sp != Summary::kIdDefault && sp < S.supernodes.size()) sps.push_back(sp);
   }
   SG_TRY(compute_shortcuts(ctx, *D, sps));
+  T.mark("shortcut weights");
   summary_node_types(S);
+  T.mark("node types");
   summary_sketch_csr(S, D->out);
+  T.mark("sketch CSRs");
   SG_TRY(upload_sketch(ctx, *D));
+  T.mark("tables and uploads");
   if (D->sssp_ready && ctx->g.weighted) {
     // shortcut distances of the touched supernodes are repaired by the next
     // SSSP query over the summary (a PageRank-only caller never pays them)
@@ -1881,6 +1919,7 @@ __global__ void k_copy_u64(const unsigned long long* a, uint64_t n, unsigned lon
 // stale.
 static sg_status sssp_summary_refresh(sg_ctx* ctx, SummaryDev& D) {
   Summary& S = D.S;
+  PhaseTrace T("sssp summary");
   if (!D.sssp_ready) {
     std::vector<uint32_t> all_sp(S.supernodes.size());
     for (uint32_t i = 0; i < all_sp.size(); ++i) all_sp[i] = i;
@@ -1902,10 +1941,12 @@ static sg_status sssp_summary_refresh(sg_ctx* ctx, SummaryDev& D) {
       D.sp_inner_d.resize(S.supernodes.size());
     }
     SG_TRY(sssp_shortcuts(ctx, D, P));
+    T.mark("shortcut distances");
     P.clear();
     D.sk_stale = true;
   }
   if (D.sk_stale) SG_TRY(sssp_sketch(ctx, D));
+  T.mark("summarized CSR");
   return SG_OK;
 }
 
