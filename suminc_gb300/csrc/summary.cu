@@ -1827,32 +1827,54 @@ static sg_status sssp_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector<ui
 static sg_status sssp_sketch(sg_ctx* ctx, SummaryDev& D) {
   Summary& S = D.S;
   const uint32_t all = S.all_n, n = S.old_n;
-  std::vector<std::vector<std::pair<uint32_t, float>>> rows(all);
+  // rows in two passes: per row, master -> in-mirror edges first, then the
+  // supernode's shortcuts, then the boundary edges; rows padded to quads
+  std::vector<uint32_t> head(all, 0);  // mirror + shortcut entries per row
   for (size_t i = 0; i < S.cluster_in_mirror_ids.size(); ++i)
-    for (uint32_t m : S.cluster_in_mirror_ids[i]) rows[S.mirror_master(m)].push_back({m, 0.f});
+    for (uint32_t m : S.cluster_in_mirror_ids[i]) head[S.mirror_master(m)]++;
   for (uint32_t sp = 0; sp < S.supernodes.size(); ++sp) {
     const Supernode& nd = S.supernodes[sp];
     if (nd.id == Summary::kIdDefault || sp >= D.sp_bound_d.size()) continue;
-    for (auto& e : D.sp_bound_d[sp]) rows[nd.id].push_back({e.first, (float)e.second});
+    head[nd.id] += (uint32_t)D.sp_bound_d[sp].size();
   }
-  for (uint32_t u = 0; u < n; ++u)
-    for (uint64_t e = S.ib_off[u]; e < S.ib_off[u + 1]; ++e)
-      rows[u].push_back({S.ib_nbr[e], S.ib_w.empty() ? 1.f : S.ib_w[e]});
   std::vector<uint64_t> off(all);
   std::vector<uint32_t> deg(all);
+#pragma omp parallel for schedule(static)
+  for (long long uu = 0; uu < (long long)all; ++uu) {
+    const uint32_t u = (uint32_t)uu;
+    deg[u] = head[u] + (u < n ? (uint32_t)(S.ib_off[u + 1] - S.ib_off[u]) : 0u);
+  }
   uint64_t pos = 0;
   for (uint32_t u = 0; u < all; ++u) {
     off[u] = pos;
-    deg[u] = (uint32_t)rows[u].size();
     pos += (deg[u] + 3u) & ~3u;
   }
   std::vector<uint32_t> col(pos + 4, 0);
   std::vector<float> w(pos + 4, 0.f);
-  for (uint32_t u = 0; u < all; ++u)
-    for (uint32_t k = 0; k < deg[u]; ++k) {
-      col[off[u] + k] = rows[u][k].first;
-      w[off[u] + k] = rows[u][k].second;
+  std::vector<uint32_t> fill(all, 0);
+  for (size_t i = 0; i < S.cluster_in_mirror_ids.size(); ++i)
+    for (uint32_t m : S.cluster_in_mirror_ids[i]) {
+      const uint32_t u = S.mirror_master(m);
+      col[off[u] + fill[u]++] = m;  // weight 0
     }
+  for (uint32_t sp = 0; sp < S.supernodes.size(); ++sp) {
+    const Supernode& nd = S.supernodes[sp];
+    if (nd.id == Summary::kIdDefault || sp >= D.sp_bound_d.size()) continue;
+    for (auto& e : D.sp_bound_d[sp]) {
+      const uint64_t k = off[nd.id] + fill[nd.id]++;
+      col[k] = e.first;
+      w[k] = (float)e.second;
+    }
+  }
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (long long uu = 0; uu < (long long)n; ++uu) {
+    const uint32_t u = (uint32_t)uu;
+    uint64_t k = off[u] + head[u];
+    for (uint64_t e = S.ib_off[u]; e < S.ib_off[u + 1]; ++e, ++k) {
+      col[k] = S.ib_nbr[e];
+      w[k] = S.ib_w.empty() ? 1.f : S.ib_w[e];
+    }
+  }
   std::vector<uint64_t> coff(1, 0);
   std::vector<uint32_t> crow, cv;
   std::vector<float> cd;
