@@ -106,6 +106,13 @@ struct SummaryDev {
   // the construction's state between its two halves, serialized
   std::vector<uint8_t> init_blob;
   std::unordered_map<const void*, uint64_t> dcap;  // reupload capacities
+  // device staging of the shortcut and SSSP passes, kept between calls so a
+  // batch costs copies instead of frees and allocations (slot -> buffer)
+  struct Stage {
+    void* p = nullptr;
+    size_t cap = 0;
+  };
+  Stage stage[32];
   // message_type = pull: per-vertex in-indexes (summary_pull_view)
   bool pull_stale = true;
   PullView pv;
@@ -160,6 +167,10 @@ static void sfree(SummaryDev& D) {
   dfree(D.sk_spid); dfree(D.sk_imir); dfree(D.sk_imaster);
   dfree(D.p_cls); dfree(D.p_ie_off); dfree(D.p_bd_off);
   dfree(D.p_ie_nbr); dfree(D.p_bd_src); dfree(D.p_act); dfree(D.p_ent); dfree(D.p_bd_w);
+  for (auto& st : D.stage) {
+    dfree(st.p);
+    st = SummaryDev::Stage();
+  }
   D.dcap.clear();
 }
 
@@ -221,6 +232,44 @@ static sg_status reupload(sg_ctx* ctx, SummaryDev& D, T** d, const std::vector<T
   }
   if (!h.empty())
     SG_CUDA(ctx, cudaMemcpyAsync(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+  return SG_OK;
+}
+
+// Staging slots: the device buffer of a slot is kept and grown (1/8 slack)
+// across calls.  Callers synchronise before returning, so a slot is free
+// again at the next call.
+enum StageSlot {
+  ST_WJOBS, ST_BJOBS, ST_LINOFF, ST_LINSRC, ST_SPC, ST_SRC, ST_INNER, ST_ADJ, ST_CLOFF,
+  ST_ADJOFF, ST_OUTOFF, ST_DIV, ST_VAL, ST_DEL,
+  SS_CL, SS_SRC, SS_NBR, SS_W, SS_CLOFF, SS_ADJOFF, SS_OUTOFF, SS_OUT,
+  SI_DALL, SI_SEEDS, SI_CS, SI_CD, SI_S2, SP_DIST, ST_SLOTS
+};
+static_assert(ST_SLOTS <= 32, "staging slots");
+
+template <typename T>
+static sg_status stage_alloc(sg_ctx* ctx, SummaryDev& D, int slot, uint64_t count, T** out) {
+  SummaryDev::Stage& s = D.stage[slot];
+  const size_t need = (size_t)std::max<uint64_t>(count, 1) * sizeof(T);
+  if (s.cap < need) {
+    dfree(s.p);
+    s.p = nullptr;
+    s.cap = 0;
+    char* p = nullptr;
+    SG_TRY(dalloc(ctx, &p, need + need / 8));
+    s.p = p;
+    s.cap = need + need / 8;
+  }
+  *out = (T*)s.p;
+  return SG_OK;
+}
+
+template <typename T, typename A>
+static sg_status stage_up(sg_ctx* ctx, SummaryDev& D, int slot, const std::vector<T, A>& h,
+                          T** out) {
+  SG_TRY(stage_alloc(ctx, D, slot, h.size(), out));
+  if (!h.empty())
+    SG_CUDA(ctx, cudaMemcpyAsync(*out, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice,
                                  ctx->stream));
   return SG_OK;
 }
@@ -511,20 +560,20 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
   uint32_t *d_wjobs = nullptr, *d_bjobs = nullptr;
   uint64_t* d_linoff = nullptr;
   uint8_t* d_linsrc = nullptr;
-  SG_TRY(upload(ctx, &d_wjobs, warp_jobs));
-  SG_TRY(upload(ctx, &d_bjobs, block_jobs));
-  SG_TRY(upload(ctx, &d_linoff, lin_off));
-  SG_TRY(upload(ctx, &d_linsrc, lin_src));
-  SG_TRY(upload(ctx, &d_spc, sp_cluster));
-  SG_TRY(upload(ctx, &d_src, sp_src));
-  SG_TRY(upload(ctx, &d_inner, cl_inner));
-  SG_TRY(upload(ctx, &d_adj, adj_nbr));
-  SG_TRY(upload(ctx, &d_cloff, cl_off));
-  SG_TRY(upload(ctx, &d_adjoff, adj_off));
-  SG_TRY(upload(ctx, &d_outoff, out_off));
-  SG_TRY(upload(ctx, &d_div, div));
-  SG_TRY(dalloc(ctx, &d_val, std::max<uint64_t>(out_off.back(), 1)));
-  SG_TRY(dalloc(ctx, &d_del, std::max<uint64_t>(out_off.back(), 1)));
+  SG_TRY(stage_up(ctx, D, ST_WJOBS, warp_jobs, &d_wjobs));
+  SG_TRY(stage_up(ctx, D, ST_BJOBS, block_jobs, &d_bjobs));
+  SG_TRY(stage_up(ctx, D, ST_LINOFF, lin_off, &d_linoff));
+  SG_TRY(stage_up(ctx, D, ST_LINSRC, lin_src, &d_linsrc));
+  SG_TRY(stage_up(ctx, D, ST_SPC, sp_cluster, &d_spc));
+  SG_TRY(stage_up(ctx, D, ST_SRC, sp_src, &d_src));
+  SG_TRY(stage_up(ctx, D, ST_INNER, cl_inner, &d_inner));
+  SG_TRY(stage_up(ctx, D, ST_ADJ, adj_nbr, &d_adj));
+  SG_TRY(stage_up(ctx, D, ST_CLOFF, cl_off, &d_cloff));
+  SG_TRY(stage_up(ctx, D, ST_ADJOFF, adj_off, &d_adjoff));
+  SG_TRY(stage_up(ctx, D, ST_OUTOFF, out_off, &d_outoff));
+  SG_TRY(stage_up(ctx, D, ST_DIV, div, &d_div));
+  SG_TRY(stage_alloc(ctx, D, ST_VAL, out_off.back(), &d_val));
+  SG_TRY(stage_alloc(ctx, D, ST_DEL, out_off.back(), &d_del));
   ShortcutArgs A;
   A.n_sp = (uint32_t)spids.size();
   A.sp_cluster = d_spc;
@@ -560,9 +609,6 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
   SG_CUDA(ctx, cudaMemcpyAsync(val.data(), d_val, 8 * val.size(), cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaMemcpyAsync(del.data(), d_del, 8 * del.size(), cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  dfree(d_spc); dfree(d_src); dfree(d_inner); dfree(d_adj); dfree(d_cloff); dfree(d_adjoff);
-  dfree(d_outoff); dfree(d_div); dfree(d_val); dfree(d_del);
-  dfree(d_wjobs); dfree(d_bjobs); dfree(d_linoff); dfree(d_linsrc);
   // fianl_build_iter_index_for_mirror (iter_compressor.h:433-491); each
   // supernode writes only its own lists
 #pragma omp parallel for schedule(dynamic, 256)
@@ -1741,14 +1787,14 @@ static sg_status sssp_cluster_jobs(sg_ctx* ctx, SummaryDev& D,
   uint64_t *d_cloff = nullptr, *d_adjoff = nullptr, *d_outoff = nullptr;
   float* d_w = nullptr;
   double* d_out = nullptr;
-  SG_TRY(upload(ctx, &d_cl, job_cl));
-  SG_TRY(upload(ctx, &d_src, job_src));
-  SG_TRY(upload(ctx, &d_nbr, adj_nbr));
-  SG_TRY(upload(ctx, &d_w, adj_w));
-  SG_TRY(upload(ctx, &d_cloff, cl_off));
-  SG_TRY(upload(ctx, &d_adjoff, adj_off));
-  SG_TRY(upload(ctx, &d_outoff, out_off));
-  SG_TRY(dalloc(ctx, &d_out, std::max<uint64_t>(out_off.back(), 1)));
+  SG_TRY(stage_up(ctx, D, SS_CL, job_cl, &d_cl));
+  SG_TRY(stage_up(ctx, D, SS_SRC, job_src, &d_src));
+  SG_TRY(stage_up(ctx, D, SS_NBR, adj_nbr, &d_nbr));
+  SG_TRY(stage_up(ctx, D, SS_W, adj_w, &d_w));
+  SG_TRY(stage_up(ctx, D, SS_CLOFF, cl_off, &d_cloff));
+  SG_TRY(stage_up(ctx, D, SS_ADJOFF, adj_off, &d_adjoff));
+  SG_TRY(stage_up(ctx, D, SS_OUTOFF, out_off, &d_outoff));
+  SG_TRY(stage_alloc(ctx, D, SS_OUT, out_off.back(), &d_out));
   if (smem > 48 * 1024)
     SG_CUDA(ctx, cudaFuncSetAttribute(k_sssp_shortcuts, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
@@ -1757,11 +1803,9 @@ static sg_status sssp_cluster_jobs(sg_ctx* ctx, SummaryDev& D,
       d_cl, d_src, d_cloff, d_adjoff, d_nbr, d_w, d_outoff, d_out, (uint32_t)jobs.size());
   kprof_end(ctx, SG_K_SUMMARY);
   SG_CUDA(ctx, cudaGetLastError());
-  std::vector<double> all(out_off.back());
+  hvec<double> all(out_off.back());
   SG_CUDA(ctx, cudaMemcpyAsync(all.data(), d_out, 8 * all.size(), cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  dfree(d_cl); dfree(d_src); dfree(d_nbr); dfree(d_w); dfree(d_cloff); dfree(d_adjoff);
-  dfree(d_outoff); dfree(d_out);
 #pragma omp parallel for schedule(dynamic, 256)
   for (long long j = 0; j < (long long)jobs.size(); ++j)
     (*dist)[j].assign(all.begin() + out_off[j], all.begin() + out_off[j + 1]);
@@ -1888,14 +1932,14 @@ static sg_status sssp_sketch(sg_ctx* ctx, SummaryDev& D) {
     }
     coff.push_back(cv.size());
   }
-  SG_TRY(upload(ctx, &D.sk_off, off));
-  SG_TRY(upload(ctx, &D.sk_deg, deg));
-  SG_TRY(upload(ctx, &D.sk_col, col));
-  SG_TRY(upload(ctx, &D.sk_w, w));
-  SG_TRY(upload(ctx, &D.sk_coff, coff));
-  SG_TRY(upload(ctx, &D.sk_crow, crow));
-  SG_TRY(upload(ctx, &D.sk_cv, cv));
-  SG_TRY(upload(ctx, &D.sk_cd, cd));
+  SG_TRY(reupload(ctx, D, &D.sk_off, off));
+  SG_TRY(reupload(ctx, D, &D.sk_deg, deg));
+  SG_TRY(reupload(ctx, D, &D.sk_col, col));
+  SG_TRY(reupload(ctx, D, &D.sk_w, w));
+  SG_TRY(reupload(ctx, D, &D.sk_coff, coff));
+  SG_TRY(reupload(ctx, D, &D.sk_crow, crow));
+  SG_TRY(reupload(ctx, D, &D.sk_cv, cv));
+  SG_TRY(reupload(ctx, D, &D.sk_cd, cd));
   std::vector<uint32_t> spid, imir, imaster;
   for (uint32_t sp = 0; sp < S.supernodes.size(); ++sp)
     if (S.supernodes[sp].id != Summary::kIdDefault) spid.push_back(S.supernodes[sp].id);
@@ -1904,9 +1948,9 @@ static sg_status sssp_sketch(sg_ctx* ctx, SummaryDev& D) {
       imir.push_back(m);
       imaster.push_back(S.mirror_master(m));
     }
-  SG_TRY(upload(ctx, &D.sk_spid, spid));
-  SG_TRY(upload(ctx, &D.sk_imir, imir));
-  SG_TRY(upload(ctx, &D.sk_imaster, imaster));
+  SG_TRY(reupload(ctx, D, &D.sk_spid, spid));
+  SG_TRY(reupload(ctx, D, &D.sk_imir, imir));
+  SG_TRY(reupload(ctx, D, &D.sk_imaster, imaster));
   D.sk_nspid = (uint32_t)spid.size();
   D.sk_nimir = (uint32_t)imir.size();
   D.sk_m = pos;
@@ -2027,14 +2071,11 @@ sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
   }
   SG_TRY(sssp_prepare_external(ctx, source));
   unsigned long long* dist = nullptr;
-  SG_TRY(dalloc(ctx, &dist, S.all_n));
+  SG_TRY(stage_alloc(ctx, D, SP_DIST, S.all_n, &dist));
   SsspView G{S.all_n, D.sk_m, D.sk_off, D.sk_deg, D.sk_col, D.sk_w};
   unsigned long long h_cnt[4] = {0, 0, 0, 0};
   sg_status rs = sssp_run_view(ctx, G, seeds.data(), sdist.data(), (uint32_t)seeds.size(), dist, h_cnt);
-  if (rs != SG_OK) {
-    dfree(dist);
-    return rs;
-  }
+  if (rs != SG_OK) return rs;
   if (D.sk_ncorr)
     k_sssp_correct<<<grid_for((uint64_t)D.sk_ncorr * 32, 256), 256, 0, st>>>(
         D.sk_ncorr, D.sk_coff, D.sk_crow, D.sk_cv, D.sk_cd, dist);
@@ -2045,7 +2086,6 @@ sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   float ms = 0.f;
   SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->kev0, ctx->kev1));
-  dfree(dist);
   return sssp_finish_external(ctx, h_cnt, ms);
 }
 
@@ -2118,8 +2158,8 @@ sg_status sssp_summarized_inc(sg_ctx* ctx) {
   unsigned long long* dall = nullptr;
   uint32_t* seeds = nullptr;
   const uint64_t nseeds = (uint64_t)info.total + info.nadd + D.sk_nspid;
-  SG_TRY(dalloc(ctx, &dall, all));
-  SG_TRY(dalloc(ctx, &seeds, std::max<uint64_t>(nseeds, 1)));
+  SG_TRY(stage_alloc(ctx, D, SI_DALL, all, &dall));
+  SG_TRY(stage_alloc(ctx, D, SI_SEEDS, nseeds, &seeds));
   k_dist_all_init<<<grid_for(all, 256), 256, 0, st>>>(sp.dist, n, all, dall);
   if (D.sk_nimir)
     k_dist_mirrors<<<grid_for(D.sk_nimir, 256), 256, 0, st>>>(D.sk_imir, D.sk_imaster, D.sk_nimir,
@@ -2145,31 +2185,23 @@ sg_status sssp_summarized_inc(sg_ctx* ctx) {
   double* d_cd = nullptr;
   uint64_t nseeds_all = nseeds;
   if (!cs.empty()) {
-    SG_TRY(dalloc(ctx, &d_cs, cs.size()));
-    SG_TRY(dalloc(ctx, &d_cd, cd.size()));
+    SG_TRY(stage_alloc(ctx, D, SI_CS, cs.size(), &d_cs));
+    SG_TRY(stage_alloc(ctx, D, SI_CD, cd.size(), &d_cd));
     SG_CUDA(ctx, cudaMemcpyAsync(d_cs, cs.data(), 4ull * cs.size(), cudaMemcpyHostToDevice, st));
     SG_CUDA(ctx, cudaMemcpyAsync(d_cd, cd.data(), 8ull * cd.size(), cudaMemcpyHostToDevice, st));
     k_dist_min_list<<<grid_for(cs.size(), 256), 256, 0, st>>>(d_cs, d_cd, (uint32_t)cs.size(), dall);
     count_launch(ctx);
     uint32_t* s2 = nullptr;
-    SG_TRY(dalloc(ctx, &s2, nseeds + cs.size()));
+    SG_TRY(stage_alloc(ctx, D, SI_S2, nseeds + cs.size(), &s2));
     if (nseeds) SG_CUDA(ctx, cudaMemcpyAsync(s2, seeds, 4ull * nseeds, cudaMemcpyDeviceToDevice, st));
     SG_CUDA(ctx, cudaMemcpyAsync(s2 + nseeds, d_cs, 4ull * cs.size(), cudaMemcpyDeviceToDevice, st));
-    SG_CUDA(ctx, cudaStreamSynchronize(st));
-    dfree(seeds);
     seeds = s2;
     nseeds_all = nseeds + cs.size();
   }
   SsspView G{all, D.sk_m, D.sk_off, D.sk_deg, D.sk_col, D.sk_w};
   unsigned long long h_cnt[4] = {0, 0, 0, 0};
   sg_status rs = sssp_run_view_warm(ctx, G, seeds, (uint32_t)nseeds_all, dall, h_cnt);
-  dfree(d_cs);
-  dfree(d_cd);
-  if (rs != SG_OK) {
-    dfree(dall);
-    dfree(seeds);
-    return rs;
-  }
+  if (rs != SG_OK) return rs;
   if (D.sk_ncorr)
     k_sssp_correct<<<grid_for((uint64_t)D.sk_ncorr * 32, 256), 256, 0, st>>>(
         D.sk_ncorr, D.sk_coff, D.sk_crow, D.sk_cv, D.sk_cd, dall);
@@ -2180,8 +2212,6 @@ sg_status sssp_summarized_inc(sg_ctx* ctx) {
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   float ms = 0.f;
   SG_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->kev0, ctx->kev1));
-  dfree(dall);
-  dfree(seeds);
   ctx->stats.shortcut_edges = 0;
   return sssp_inc_finish_external(ctx, info, h_cnt, ms);
 }
