@@ -334,9 +334,20 @@ struct SsspView {
   const uint32_t* col;
   const float* w;
 };
+// Queues and tags of a delta-stepping run over a view, held by the caller
+// and grown on demand, so repeated runs allocate nothing.
+struct SsspViewScratch {
+  uint32_t *stamp = nullptr, *fstamp = nullptr, *reset = nullptr;
+  uint32_t* q[3] = {nullptr, nullptr, nullptr};
+  uint32_t *far = nullptr, *far2 = nullptr, *ctl = nullptr, *sv = nullptr;
+  unsigned long long* cnt = nullptr;
+  double* sd = nullptr;
+  uint64_t n_cap = 0, f_cap = 0, s_cap = 0;
+};
+void sssp_view_scratch_free(SsspViewScratch& v);
 sg_status sssp_run_view(sg_ctx* ctx, const SsspView& G, const uint32_t* h_seeds,
                         const double* h_seed_dist, uint32_t nseeds, unsigned long long* dist,
-                        unsigned long long* h_cnt);
+                        unsigned long long* h_cnt, SsspViewScratch& V);
 // prepares ctx->sp for a result written from outside (buffers, no run)
 sg_status sssp_prepare_external(sg_ctx* ctx, uint32_t source);
 sg_status sssp_finish_external(sg_ctx* ctx, const unsigned long long* h_cnt, float ms);
@@ -349,7 +360,8 @@ struct SsspIncInfo {
 };
 sg_status sssp_inc_prepare(sg_ctx* ctx, SsspIncInfo* info);
 sg_status sssp_run_view_warm(sg_ctx* ctx, const SsspView& G, const uint32_t* d_seeds,
-                             uint32_t nseeds, unsigned long long* dist, unsigned long long* h_cnt);
+                             uint32_t nseeds, unsigned long long* dist, unsigned long long* h_cnt,
+                             SsspViewScratch& V);
 sg_status sssp_inc_finish_external(sg_ctx* ctx, const SsspIncInfo& info,
                                    const unsigned long long* h_cnt, float ms);
 

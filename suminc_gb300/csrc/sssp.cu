@@ -972,28 +972,59 @@ __global__ void k_sssp_seed_list(const uint32_t* __restrict__ v, const double* _
 // Delta-stepping over a caller-given padded CSR view (segments 16-byte
 // aligned, readable in quads) from a list of seeds with start distances.
 // Temporary queues are allocated for the call.  dist: device [G.n].
+void sssp_view_scratch_free(SsspViewScratch& v) {
+  dfree(v.stamp); dfree(v.fstamp); dfree(v.reset);
+  dfree(v.q[0]); dfree(v.q[1]); dfree(v.q[2]);
+  dfree(v.far); dfree(v.far2); dfree(v.ctl); dfree(v.cnt); dfree(v.sv); dfree(v.sd);
+  v = SsspViewScratch();
+}
+
+// grows the scratch to n rows, a far capacity of fcap and nseeds seeds
+static sg_status view_scratch(sg_ctx* ctx, SsspViewScratch& V, uint64_t n, uint64_t fcap,
+                              uint64_t nseeds) {
+  if (V.n_cap < n) {
+    dfree(V.stamp); dfree(V.fstamp); dfree(V.reset);
+    dfree(V.q[0]); dfree(V.q[1]); dfree(V.q[2]);
+    V.n_cap = 0;
+    const uint64_t c = n + n / 8;
+    SG_TRY(dalloc(ctx, &V.stamp, c));
+    SG_TRY(dalloc(ctx, &V.fstamp, c));
+    SG_TRY(dalloc(ctx, &V.reset, c));
+    for (int i = 0; i < 3; ++i) SG_TRY(dalloc(ctx, &V.q[i], c));
+    V.n_cap = c;
+  }
+  if (V.f_cap < fcap) {
+    dfree(V.far); dfree(V.far2);
+    V.f_cap = 0;
+    const uint64_t c = fcap + fcap / 8;
+    SG_TRY(dalloc(ctx, &V.far, c));
+    SG_TRY(dalloc(ctx, &V.far2, c));
+    V.f_cap = c;
+  }
+  if (V.s_cap < std::max<uint64_t>(nseeds, 1)) {
+    dfree(V.sv); dfree(V.sd);
+    V.s_cap = 0;
+    const uint64_t c = std::max<uint64_t>(nseeds, 1) * 2;
+    SG_TRY(dalloc(ctx, &V.sv, c));
+    SG_TRY(dalloc(ctx, &V.sd, c));
+    V.s_cap = c;
+  }
+  if (!V.ctl) SG_TRY(dalloc(ctx, &V.ctl, S_WORDS));
+  if (!V.cnt) SG_TRY(dalloc(ctx, &V.cnt, SC_WORDS));
+  return SG_OK;
+}
+
 sg_status sssp_run_view(sg_ctx* ctx, const SsspView& G, const uint32_t* h_seeds,
                         const double* h_seed_dist, uint32_t nseeds, unsigned long long* dist,
-                        unsigned long long* h_cnt) {
+                        unsigned long long* h_cnt, SsspViewScratch& V) {
   cudaStream_t st = ctx->stream;
   const uint32_t n = G.n;
-  uint32_t *stamp = nullptr, *fstamp = nullptr, *reset = nullptr, *q0 = nullptr, *q1 = nullptr,
-           *q2 = nullptr, *far = nullptr, *far2 = nullptr, *ctl = nullptr, *sv = nullptr;
-  unsigned long long* cnt = nullptr;
-  double* sd = nullptr;
   const uint64_t fcap = G.m + (uint64_t)n + nseeds + 1024;
-  SG_TRY(dalloc(ctx, &stamp, n));
-  SG_TRY(dalloc(ctx, &fstamp, n));
-  SG_TRY(dalloc(ctx, &reset, n));
-  SG_TRY(dalloc(ctx, &q0, n));
-  SG_TRY(dalloc(ctx, &q1, n));
-  SG_TRY(dalloc(ctx, &q2, n));
-  SG_TRY(dalloc(ctx, &far, fcap));
-  SG_TRY(dalloc(ctx, &far2, fcap));
-  SG_TRY(dalloc(ctx, &ctl, S_WORDS));
-  SG_TRY(dalloc(ctx, &cnt, SC_WORDS));
-  SG_TRY(dalloc(ctx, &sv, std::max<uint32_t>(nseeds, 1)));
-  SG_TRY(dalloc(ctx, &sd, std::max<uint32_t>(nseeds, 1)));
+  SG_TRY(view_scratch(ctx, V, n, fcap, nseeds));
+  uint32_t *stamp = V.stamp, *fstamp = V.fstamp, *reset = V.reset, *q0 = V.q[0], *q1 = V.q[1],
+           *q2 = V.q[2], *far = V.far, *far2 = V.far2, *ctl = V.ctl, *sv = V.sv;
+  unsigned long long* cnt = V.cnt;
+  double* sd = V.sd;
   k_sssp_init<<<grid_for(n, 256), 256, 0, st>>>(n, dist, stamp, fstamp, reset);
   SG_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(uint32_t) * S_WORDS, st));
   SG_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * SC_WORDS, st));
@@ -1026,8 +1057,6 @@ sg_status sssp_run_view(sg_ctx* ctx, const SsspView& G, const uint32_t* h_seeds,
   sg_status rs = sssp_launch_args(ctx, A, h_ctl);
   if (rs == SG_OK && h_cnt)
     SG_CUDA(ctx, cudaMemcpy(h_cnt, cnt, sizeof(unsigned long long) * SC_WORDS, cudaMemcpyDeviceToHost));
-  dfree(stamp); dfree(fstamp); dfree(reset); dfree(q0); dfree(q1); dfree(q2);
-  dfree(far); dfree(far2); dfree(ctl); dfree(cnt); dfree(sv); dfree(sd);
   return rs;
 }
 
@@ -1331,22 +1360,15 @@ sg_status sssp_inc_finish_external(sg_ctx* ctx, const SsspIncInfo& info,
 // and the device list `d_seeds` holds the vertices whose out-rows must be
 // relaxed again.  Temporary queues are allocated for the call.
 sg_status sssp_run_view_warm(sg_ctx* ctx, const SsspView& G, const uint32_t* d_seeds,
-                             uint32_t nseeds, unsigned long long* dist, unsigned long long* h_cnt) {
+                             uint32_t nseeds, unsigned long long* dist, unsigned long long* h_cnt,
+                             SsspViewScratch& V) {
   cudaStream_t st = ctx->stream;
   const uint32_t n = G.n;
-  uint32_t *stamp = nullptr, *fstamp = nullptr, *q0 = nullptr, *q1 = nullptr, *q2 = nullptr,
-           *far = nullptr, *far2 = nullptr, *ctl = nullptr;
-  unsigned long long* cnt = nullptr;
   const uint64_t fcap = G.m + (uint64_t)n + nseeds + 1024;
-  SG_TRY(dalloc(ctx, &stamp, n));
-  SG_TRY(dalloc(ctx, &fstamp, n));
-  SG_TRY(dalloc(ctx, &q0, n));
-  SG_TRY(dalloc(ctx, &q1, n));
-  SG_TRY(dalloc(ctx, &q2, n));
-  SG_TRY(dalloc(ctx, &far, fcap));
-  SG_TRY(dalloc(ctx, &far2, fcap));
-  SG_TRY(dalloc(ctx, &ctl, S_WORDS));
-  SG_TRY(dalloc(ctx, &cnt, SC_WORDS));
+  SG_TRY(view_scratch(ctx, V, n, fcap, 0));
+  uint32_t *stamp = V.stamp, *fstamp = V.fstamp, *q0 = V.q[0], *q1 = V.q[1], *q2 = V.q[2],
+           *far = V.far, *far2 = V.far2, *ctl = V.ctl;
+  unsigned long long* cnt = V.cnt;
   SG_CUDA(ctx, cudaMemsetAsync(stamp, 0, 4ull * n, st));
   SG_CUDA(ctx, cudaMemsetAsync(fstamp, 0, 4ull * n, st));
   SG_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(uint32_t) * S_WORDS, st));
@@ -1377,8 +1399,6 @@ sg_status sssp_run_view_warm(sg_ctx* ctx, const SsspView& G, const uint32_t* d_s
   sg_status rs = sssp_launch_args(ctx, A, h_ctl);
   if (rs == SG_OK && h_cnt)
     SG_CUDA(ctx, cudaMemcpy(h_cnt, cnt, sizeof(unsigned long long) * SC_WORDS, cudaMemcpyDeviceToHost));
-  dfree(stamp); dfree(fstamp); dfree(q0); dfree(q1); dfree(q2);
-  dfree(far); dfree(far2); dfree(ctl); dfree(cnt);
   return rs;
 }
 

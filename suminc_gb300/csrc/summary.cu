@@ -113,6 +113,7 @@ struct SummaryDev {
     size_t cap = 0;
   };
   Stage stage[32];
+  SsspViewScratch view;  // queues of the delta-stepping runs over the summary
   // message_type = pull: per-vertex in-indexes (summary_pull_view)
   bool pull_stale = true;
   PullView pv;
@@ -171,6 +172,7 @@ static void sfree(SummaryDev& D) {
     dfree(st.p);
     st = SummaryDev::Stage();
   }
+  sssp_view_scratch_free(D.view);
   D.dcap.clear();
 }
 
@@ -2074,7 +2076,8 @@ sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
   SG_TRY(stage_alloc(ctx, D, SP_DIST, S.all_n, &dist));
   SsspView G{S.all_n, D.sk_m, D.sk_off, D.sk_deg, D.sk_col, D.sk_w};
   unsigned long long h_cnt[4] = {0, 0, 0, 0};
-  sg_status rs = sssp_run_view(ctx, G, seeds.data(), sdist.data(), (uint32_t)seeds.size(), dist, h_cnt);
+  sg_status rs = sssp_run_view(ctx, G, seeds.data(), sdist.data(), (uint32_t)seeds.size(), dist,
+                               h_cnt, D.view);
   if (rs != SG_OK) return rs;
   if (D.sk_ncorr)
     k_sssp_correct<<<grid_for((uint64_t)D.sk_ncorr * 32, 256), 256, 0, st>>>(
@@ -2200,7 +2203,7 @@ sg_status sssp_summarized_inc(sg_ctx* ctx) {
   }
   SsspView G{all, D.sk_m, D.sk_off, D.sk_deg, D.sk_col, D.sk_w};
   unsigned long long h_cnt[4] = {0, 0, 0, 0};
-  sg_status rs = sssp_run_view_warm(ctx, G, seeds, (uint32_t)nseeds_all, dall, h_cnt);
+  sg_status rs = sssp_run_view_warm(ctx, G, seeds, (uint32_t)nseeds_all, dall, h_cnt, D.view);
   if (rs != SG_OK) return rs;
   if (D.sk_ncorr)
     k_sssp_correct<<<grid_for((uint64_t)D.sk_ncorr * 32, 256), 256, 0, st>>>(
