@@ -1921,18 +1921,27 @@ static sg_status sssp_sketch(sg_ctx* ctx, SummaryDev& D) {
       w[k] = S.ib_w.empty() ? 1.f : S.ib_w[e];
     }
   }
+  // correction lists (entry -> inner member shortcuts), in supernode order:
+  // rows and offsets on one pass, the entries filled in parallel
+  const uint32_t nsp = (uint32_t)S.supernodes.size();
   std::vector<uint64_t> coff(1, 0);
-  std::vector<uint32_t> crow, cv;
-  std::vector<float> cd;
-  for (uint32_t sp = 0; sp < S.supernodes.size(); ++sp) {
+  std::vector<uint32_t> crow, csp;
+  for (uint32_t sp = 0; sp < nsp; ++sp) {
     const Supernode& nd = S.supernodes[sp];
     if (nd.id == Summary::kIdDefault || sp >= D.sp_inner_d.size() || D.sp_inner_d[sp].empty()) continue;
     crow.push_back(nd.id);
-    for (auto& e : D.sp_inner_d[sp]) {
-      cv.push_back(e.first);
-      cd.push_back((float)e.second);
+    csp.push_back(sp);
+    coff.push_back(coff.back() + D.sp_inner_d[sp].size());
+  }
+  hvec<uint32_t> cv(coff.back());
+  hvec<float> cd(coff.back());
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long long r = 0; r < (long long)csp.size(); ++r) {
+    uint64_t k = coff[r];
+    for (auto& e : D.sp_inner_d[csp[r]]) {
+      cv[k] = e.first;
+      cd[k++] = (float)e.second;
     }
-    coff.push_back(cv.size());
   }
   SG_TRY(reupload(ctx, D, &D.sk_off, off));
   SG_TRY(reupload(ctx, D, &D.sk_deg, deg));
