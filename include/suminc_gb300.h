@@ -72,8 +72,9 @@ typedef struct sg_options {
   double adjoint_rel_tol;     /* adjoint stop: residual < tol * sum|dL/dx|   */
   int32_t pull_hubs;          /* push values of the highest out-degree vertices
                                  each pull CTA keeps in shared memory: 0 =
-                                 automatic (up to 12,288), -1 = none, k > 0 =
-                                 at most min(k, 16,384)                     */
+                                 automatic (up to 12,288), -1 = none (and the
+                                 pull in vertex-id order instead of degree
+                                 rank order), k > 0 = at most min(k, 16,384) */
   int32_t message_type;       /* FLAGS_message_type for PageRank: 0 = push
                                  (SumSyncIterWorker / IngressSyncIterWorker),
                                  1 = pull (SumSyncIterWorkerPull: synchronous
@@ -264,7 +265,10 @@ sg_status sg_sssp_peval(sg_ctx* ctx, uint32_t source, double* out);
 
 /* Incremental SSSP after sg_apply_updates: re-seeds the reset vertices from
  * their in-neighbours and relaxes from every improved vertex
- * (sum_sync_traversal_worker.h:262-352, :1424-1690). */
+ * (sum_sync_traversal_worker.h:262-352, :1424-1690).  With compress = 1 and
+ * a summarized PEval before it, the relaxation runs over the summary
+ * (boundary edges and repaired shortcuts), followed by the correction of
+ * the inner members. */
 sg_status sg_sssp_inceval(sg_ctx* ctx, double* out);
 
 sg_status sg_sssp_distances(sg_ctx* ctx, double* out);
