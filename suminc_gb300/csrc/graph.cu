@@ -846,16 +846,21 @@ __global__ void k_inv_keys(const uint32_t* __restrict__ s, const uint32_t* __res
 // tail, a direction is repacked: fresh capacities with slack, live entries
 // copied in vertex order, a new pool with room for the batch.
 
-// slots a batch may need in one direction: every vertex with actions could
-// move, with its live entries plus the actions' inserts and slack
+// slots a batch may need in one direction: a vertex moves to the pool tail
+// only when its new length exceeds its capacity, and its new length is at
+// most its live entries plus its actions, so a vertex whose bound fits its
+// capacity needs nothing and any other at most the capacity the applier
+// gives a moved row for that bound
 __global__ void k_batch_need(const uint32_t* __restrict__ gv, const uint32_t* __restrict__ gb,
                              const uint32_t* __restrict__ ge, uint64_t n_grp,
-                             const uint32_t* __restrict__ deg, unsigned long long* need) {
+                             const uint32_t* __restrict__ deg, const uint32_t* __restrict__ cap,
+                             unsigned long long* need) {
   unsigned long long acc = 0;
   for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < n_grp;
        g += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t d1 = (uint64_t)deg[gv[g]] + (ge[g] - gb[g]);
-    acc += ((d1 + d1 / 8 + 4 + 3) & ~3ull);
+    const uint32_t v = gv[g];
+    const uint64_t d1 = (uint64_t)deg[v] + (ge[g] - gb[g]);
+    if (d1 > cap[v]) acc += ((d1 + d1 / 8 + 4 + 3) & ~3ull);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
@@ -922,7 +927,8 @@ static sg_status ensure_pool(sg_ctx* ctx, DevCSR& c, const uint32_t* gv, const u
                              const uint32_t* ge, uint64_t n_grp, unsigned long long* d_need) {
   SG_CUDA(ctx, cudaMemsetAsync(d_need, 0, 8, ctx->stream));
   if (n_grp)
-    k_batch_need<<<grid_for(n_grp, 256), 256, 0, ctx->stream>>>(gv, gb, ge, n_grp, c.deg, d_need);
+    k_batch_need<<<grid_for(n_grp, 256), 256, 0, ctx->stream>>>(gv, gb, ge, n_grp, c.deg, c.cap,
+                                                                  d_need);
   unsigned long long need = 0, tail = 0;
   SG_CUDA(ctx, cudaMemcpyAsync(&need, d_need, 8, cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaMemcpyAsync(&tail, c.pool_tail, 8, cudaMemcpyDeviceToHost, ctx->stream));

@@ -117,6 +117,7 @@ def test_pool_repacks_under_many_inserts():
             assert np.array_equal(drp, nrp) and np.array_equal(dcol, ncol)
             assert np.array_equal(dw, nw)
             assert np.array_equal(ctx.sssp_inceval(), oracle.dijkstra(nrp, ncol, nw, 0))
+        assert ctx.stats()["repacks"] > 0  # the repack path ran
 
 
 def test_graph_emptied_and_refilled_by_batches():
