@@ -270,3 +270,21 @@ def test_summary_without_supernodes_runs_the_plain_path():
         d2 = ctx.sssp_inceval()
         assert np.array_equal(d2, oracle.dijkstra(nrp, ncol, nw, 0))
         assert np.array_equal(d2, plain.sssp_inceval())
+
+
+def test_summarized_sssp_inceval_after_two_pending_batches():
+    """Two batches applied before one IncEval over the summary (the reset and
+    re-seed cover both, the shortcut repair covers the supernodes both
+    touched): bit-exact against Dijkstra."""
+    fx = load("planted2600")
+    rp, col, w = fx["row_ptr"], fx["col"], fx["w"]
+    cur = (rp, col, w)
+    with sg.Context(0, compress=1) as ctx:
+        ctx.load_csr(rp, col, w)
+        ctx.summary_build(fx["clusters"])
+        ctx.sssp_peval(5)
+        for seed in (71, 72):
+            upd = oracle.gen_updates(cur[0], cur[1], 80, 80, 40, seed=seed)
+            cur = oracle.apply_updates(*cur, upd)
+            ctx.apply_updates(upd)
+        assert np.array_equal(ctx.sssp_inceval(), oracle.dijkstra(*cur, 5))
