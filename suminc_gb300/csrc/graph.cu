@@ -850,7 +850,8 @@ __global__ void k_inv_keys(const uint32_t* __restrict__ s, const uint32_t* __res
 // only when its new length exceeds its capacity, and its new length is at
 // most its live entries plus its actions, so a vertex whose bound fits its
 // capacity needs nothing and any other at most the capacity the applier
-// gives a moved row for that bound
+// gives a moved row for that bound.  cap == nullptr counts every vertex with
+// actions (the need after a repack, which resets every capacity).
 __global__ void k_batch_need(const uint32_t* __restrict__ gv, const uint32_t* __restrict__ gb,
                              const uint32_t* __restrict__ ge, uint64_t n_grp,
                              const uint32_t* __restrict__ deg, const uint32_t* __restrict__ cap,
@@ -860,7 +861,7 @@ __global__ void k_batch_need(const uint32_t* __restrict__ gv, const uint32_t* __
        g += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t v = gv[g];
     const uint64_t d1 = (uint64_t)deg[v] + (ge[g] - gb[g]);
-    if (d1 > cap[v]) acc += ((d1 + d1 / 8 + 4 + 3) & ~3ull);
+    if (!cap || d1 > cap[v]) acc += ((d1 + d1 / 8 + 4 + 3) & ~3ull);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
@@ -922,20 +923,34 @@ static sg_status repack_direction(sg_ctx* ctx, DevCSR& c, uint64_t batch_need) {
   return SG_OK;
 }
 
-// Repacks each direction whose free tail cannot hold the batch's worst case.
+static sg_status batch_need(sg_ctx* ctx, const DevCSR& c, const uint32_t* gv, const uint32_t* gb,
+                            const uint32_t* ge, uint64_t n_grp, const uint32_t* cap,
+                            unsigned long long* d_need, unsigned long long* need) {
+  SG_CUDA(ctx, cudaMemsetAsync(d_need, 0, 8, ctx->stream));
+  if (n_grp) {
+    k_batch_need<<<grid_for(n_grp, 256), 256, 0, ctx->stream>>>(gv, gb, ge, n_grp, c.deg, cap,
+                                                                  d_need);
+    count_launch(ctx);
+  }
+  SG_CUDA(ctx, cudaMemcpyAsync(need, d_need, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  return SG_OK;
+}
+
+// Repacks each direction whose free tail cannot hold the batch's need.  The
+// need against the current capacities decides; a repack resets every
+// capacity to the live degree plus slack, so it reserves the worst case
+// (every vertex with actions moves).
 static sg_status ensure_pool(sg_ctx* ctx, DevCSR& c, const uint32_t* gv, const uint32_t* gb,
                              const uint32_t* ge, uint64_t n_grp, unsigned long long* d_need) {
-  SG_CUDA(ctx, cudaMemsetAsync(d_need, 0, 8, ctx->stream));
-  if (n_grp)
-    k_batch_need<<<grid_for(n_grp, 256), 256, 0, ctx->stream>>>(gv, gb, ge, n_grp, c.deg, c.cap,
-                                                                  d_need);
   unsigned long long need = 0, tail = 0;
-  SG_CUDA(ctx, cudaMemcpyAsync(&need, d_need, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  SG_TRY(batch_need(ctx, c, gv, gb, ge, n_grp, c.cap, d_need, &need));
   SG_CUDA(ctx, cudaMemcpyAsync(&tail, c.pool_tail, 8, cudaMemcpyDeviceToHost, ctx->stream));
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  count_launch(ctx);
   if (tail + need <= c.pool_cap) return SG_OK;
-  return repack_direction(ctx, c, need);
+  unsigned long long worst = 0;
+  SG_TRY(batch_need(ctx, c, gv, gb, ge, n_grp, nullptr, d_need, &worst));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return repack_direction(ctx, c, worst);
 }
 
 constexpr uint32_t kApplyChunk = 1024;  // segment entries per find / amend work item
