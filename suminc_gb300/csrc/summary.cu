@@ -297,6 +297,12 @@ struct ShortcutArgs {
   const uint8_t* lin_src;       // from members (local indices)
 };
 
+// Both kernels iterate like the reference's local sweep
+// (inc_run_to_convergence_mirror, iter_compressor.h:350-430): deltas and
+// the values pushed along edges in FP32 (the reference's value_t for
+// PageRank, outv = delta * d / out_degree), the accumulated shortcut value
+// of every node and the delta mass of a step in FP64.
+
 // One CTA per supernode job (clusters of any size).
 __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njobs) {
   extern __shared__ double sm[];
@@ -308,39 +314,40 @@ __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njob
   const uint32_t L = (uint32_t)(A.cl_off[c + 1] - l0);
   const uint32_t inner = A.cl_inner[c];
   const uint32_t src = A.sp_src[s];
+  const float d = A.damping;
   double* value = sm;
-  double* delta = sm + L;
-  double* next = sm + 2 * L;
+  float* delta = (float*)(sm + L);
+  float* next = delta + L;
   __shared__ double s_diff;
   for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) {
     value[i] = 0.0;
-    delta[i] = (i == src) ? 1.0 : 0.0;
+    delta[i] = (i == src) ? 1.f : 0.f;
   }
   __syncthreads();
   // an in-mirror entry first sends its unit along its edges into the cluster
   if (src >= inner) {
     const uint64_t e0 = A.adj_off[l0 + src], e1 = A.adj_off[l0 + src + 1];
-    const double outv = (double)A.damping / (double)A.div[l0 + src];
+    const float outv = d / A.div[l0 + src];
     for (uint64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) atomicAdd(&delta[A.adj_nbr[e]], outv);
     __syncthreads();
     if (threadIdx.x == 0) {
       value[src] += 1.0;
-      delta[src] = 0.0;
+      delta[src] = 0.f;
     }
     __syncthreads();
   }
   const double thr = A.thr_per_node * (double)inner;
   for (int step = 1;; ++step) {
     if (threadIdx.x == 0) s_diff = 0.0;
-    for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) next[i] = i < inner ? 0.0 : delta[i];
+    for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) next[i] = i < inner ? 0.f : delta[i];
     __syncthreads();
     double diff = 0.0;
     for (uint32_t i = threadIdx.x; i < inner; i += blockDim.x) {
-      const double ts = delta[i];
-      if (ts == 0.0) continue;
-      value[i] += ts;
-      diff += fabs(ts);
-      const double outv = ts * (double)A.damping / (double)A.div[l0 + i];
+      const float ts = delta[i];
+      if (ts == 0.f) continue;
+      value[i] += (double)ts;
+      diff += fabs((double)ts);
+      const float outv = ts * d / A.div[l0 + i];
       for (uint64_t e = A.adj_off[l0 + i]; e < A.adj_off[l0 + i + 1]; ++e)
         atomicAdd(&next[A.adj_nbr[e]], outv);
     }
@@ -355,24 +362,24 @@ __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njob
   const uint64_t o = A.out_off[s];
   for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) {
     A.out_value[o + i] = value[i];
-    A.out_delta[o + i] = delta[i];
+    A.out_delta[o + i] = (double)delta[i];
   }
 }
 
 // One warp per supernode job for clusters of at most kStageCap local nodes:
 // the same iteration as k_shortcuts (a unit of delta at the entry, Jacobi
-// steps in FP64 until the members' delta mass is at most thr x members or
-// 101 steps) in two phases per step without atomics: members take their
-// delta and publish d * delta / div, then every node sums the published
-// values of its in-edges from members (mirrors keep what they hold).
+// steps until the members' delta mass is at most thr x members or 101
+// steps) in two phases per step without atomics: members take their delta
+// and publish delta * d / div, then every node sums the published values
+// of its in-edges from members (mirrors keep what they hold).
 __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t njobs) {
   __shared__ double s_val[kStageWarps][kStageCap];
-  __shared__ double s_del[kStageWarps][kStageCap];
-  __shared__ double s_pv[kStageWarps][kStageCap];
-  __shared__ double s_f[kStageWarps][kStageCap];
+  __shared__ float s_del[kStageWarps][kStageCap];
+  __shared__ float s_pv[kStageWarps][kStageCap];
+  __shared__ float s_div[kStageWarps][kStageCap];
   const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  const double d = (double)A.damping;
+  const float d = A.damping;
   for (uint32_t jj = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; jj < njobs; jj += nwarps) {
     const uint32_t s = A.jobs[jj];
     const uint32_t c = A.sp_cluster[s];
@@ -381,23 +388,23 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
     const uint32_t inner = A.cl_inner[c];
     const uint32_t src = A.sp_src[s];
     double* val = s_val[w];
-    double* del = s_del[w];
-    double* pv = s_pv[w];
-    double* f = s_f[w];  // d / div per node: one FP64 division per node and job
+    float* del = s_del[w];
+    float* pv = s_pv[w];
+    float* dv = s_div[w];
     for (uint32_t i = lane; i < L; i += 32) {
       val[i] = 0.0;
-      del[i] = (i == src) ? 1.0 : 0.0;
-      f[i] = d / (double)A.div[l0 + i];
+      del[i] = (i == src) ? 1.f : 0.f;
+      dv[i] = A.div[l0 + i];
     }
     __syncwarp();
     // an in-mirror entry first sends its unit along its edges into the cluster
     if (src >= inner) {
       if (lane == 0) {
-        const double outv = d / (double)A.div[l0 + src];
+        const float outv = d / dv[src];
         for (uint64_t e = A.adj_off[l0 + src]; e < A.adj_off[l0 + src + 1]; ++e)
           del[A.adj_nbr[e]] += outv;
         val[src] += 1.0;
-        del[src] = 0.0;
+        del[src] = 0.f;
       }
       __syncwarp();
     }
@@ -405,20 +412,20 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
     for (int step = 1;; ++step) {
       double diff = 0.0;
       for (uint32_t i = lane; i < inner; i += 32) {
-        const double ts = del[i];
-        double out = 0.0;
-        if (ts != 0.0) {
-          val[i] += ts;
-          diff += fabs(ts);
-          out = ts * f[i];
+        const float ts = del[i];
+        float out = 0.f;
+        if (ts != 0.f) {
+          val[i] += (double)ts;
+          diff += fabs((double)ts);
+          out = ts * d / dv[i];
         }
         pv[i] = out;
       }
       __syncwarp();
       for (uint32_t j = lane; j < L; j += 32) {
-        double acc = 0.0;
+        float acc = 0.f;
         for (uint64_t f = A.lin_off[l0 + j]; f < A.lin_off[l0 + j + 1]; ++f) acc += pv[A.lin_src[f]];
-        del[j] = (j < inner ? 0.0 : del[j]) + acc;
+        del[j] = (j < inner ? 0.f : del[j]) + acc;
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) diff += __shfl_xor_sync(0xffffffffu, diff, o);
@@ -428,7 +435,7 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
     const uint64_t o = A.out_off[s];
     for (uint32_t i = lane; i < L; i += 32) {
       A.out_value[o + i] = val[i];
-      A.out_delta[o + i] = del[i];
+      A.out_delta[o + i] = (double)del[i];
     }
     __syncwarp();
   }
@@ -553,7 +560,7 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
     }
   }
   (void)maxL;
-  const size_t smem = 3 * maxL_block * sizeof(double);
+  const size_t smem = 2 * maxL_block * sizeof(double);
   if (smem > 200 * 1024) return fail(ctx, SG_ERR_UNSUPPORTED, "cluster too large for the shortcut kernel");
   uint32_t *d_spc = nullptr, *d_src = nullptr, *d_inner = nullptr, *d_adj = nullptr;
   uint64_t *d_cloff = nullptr, *d_adjoff = nullptr, *d_outoff = nullptr;
