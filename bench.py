@@ -1060,6 +1060,8 @@ def run_summarized(args, D: Dist):
     prof_batch = hg.gen_updates(bsz // 2, bsz - bsz // 2, 0, seed=799)
     out = {}
     for mode in (1, 0):
+        # PageRank on its own context: with compress = 1 the apply repairs the
+        # summary's PageRank tables on the device
         ctx = sg.Context(dev, compress=mode)
         ctx.load_csr(rp, col, w)
         t0 = time.perf_counter()
@@ -1069,11 +1071,7 @@ def run_summarized(args, D: Dist):
         build_s = time.perf_counter() - t0
         ctx.pr_peval(out=False)
         pe = ctx.stats()
-        d0 = ctx.sssp_peval(0)
-        sp_first = ctx.stats()
-        d0 = ctx.sssp_peval(0)  # shortcut distances and sketch now built
-        sp = ctx.stats()
-        inc_ms, rounds, apply_ms, sssp_inc_ms = [], [], [], []
+        inc_ms, rounds, apply_ms = [], [], []
         for b in batches:
             t1 = time.perf_counter()
             ctx.apply_updates(b)  # with compress=1 this includes the summary repair
@@ -1082,11 +1080,6 @@ def run_summarized(args, D: Dist):
             st = ctx.stats()
             inc_ms.append(st["elapsed_ms"])
             rounds.append(st["rounds"])
-            # SSSP from 0 re-evaluated after the same batch (with compress=1
-            # over the summary: reset, rounds over the summarized CSR and
-            # repaired shortcuts, inner correction)
-            d1 = ctx.sssp_inceval()
-            sssp_inc_ms.append(ctx.stats()["elapsed_ms"])
         # one more batch (the same one in both modes) with CUDA events around
         # every kernel class
         ctx.set_profile(0xFF)
@@ -1097,18 +1090,41 @@ def run_summarized(args, D: Dist):
         ctx.set_profile(0)
         kms = {k: round(v, 3) for k, v in stp["kernel_ms"].items() if v}
         x = ctx.pr_values()
+        check = ctx.summary_check() if mode else None
+        ctx.close()
+        # SSSP from 0 on a second context, re-evaluated after the same batches
+        # (with compress=1 over the summary: reset, rounds over the summarized
+        # CSR and repaired shortcuts, inner correction; its apply also brings
+        # the host restatement of the summary up to date)
+        ctx = sg.Context(dev, compress=mode)
+        ctx.load_csr(rp, col, w)
+        if mode:
+            ctx.summary_build(comms)
+        d0 = ctx.sssp_peval(0)
+        sp_first = ctx.stats()
+        d0 = ctx.sssp_peval(0)  # shortcut distances and sketch now built
+        sp = ctx.stats()
+        sssp_inc_ms, sssp_apply_ms = [], []
+        for b in batches:
+            t1 = time.perf_counter()
+            ctx.apply_updates(b)
+            sssp_apply_ms.append((time.perf_counter() - t1) * 1e3)
+            d1 = ctx.sssp_inceval()
+            sssp_inc_ms.append(ctx.stats()["elapsed_ms"])
+        ctx.close()
         out[mode] = {"peval_ms": round(pe["elapsed_ms"], 3), "peval_rounds": pe["rounds"],
                      "inceval_kernel_ms": kms, "inceval_profiled_ms": round(stp["elapsed_ms"], 3),
                      "sssp_peval_ms": round(sp["elapsed_ms"], 3),
                      "sssp_peval_first_ms": round(sp_first["elapsed_ms"], 3),
                      "inceval_ms": [round(v, 3) for v in inc_ms], "inceval_rounds": rounds,
                      "apply_ms": [round(v, 3) for v in apply_ms],
+                     "sssp_apply_ms": [round(v, 3) for v in sssp_apply_ms],
                      "sssp_inceval_ms": [round(v, 3) for v in sssp_inc_ms],
                      "build_s": round(build_s, 2), "x": x, "d0": d0, "d1": d1}
         if mode:
             out[mode]["summary"] = {k: info[k] for k in ("clusters", "supernodes", "shortcut_edges",
                                                          "boundary_edges", "all_rows")}
-        ctx.close()
+            out[mode]["repair_vs_host_restatement"] = check
     # the pull worker (message_type=pull) over a summary without mirrors
     ctx = sg.Context(dev, compress=1, message_type=sg.SG_MSG_PULL, mirror_k=1 << 30)
     ctx.load_csr(rp, col, w)
@@ -1146,7 +1162,7 @@ def run_summarized(args, D: Dist):
     s_inc = float(np.mean(out[1]["inceval_ms"]))
     p_inc = float(np.mean(out[0]["inceval_ms"]))
     # a batch's whole cost: the apply (with compress = 1 it repairs the
-    # summary on the host) plus the IncEval
+    # summary's PageRank tables on the device) plus the IncEval
     s_step = float(np.mean(np.add(out[1]["apply_ms"], out[1]["inceval_ms"])))
     p_step = float(np.mean(np.add(out[0]["apply_ms"], out[0]["inceval_ms"])))
     return {

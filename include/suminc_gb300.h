@@ -254,6 +254,24 @@ sg_status sg_summary_build(sg_ctx* ctx, uint32_t n_clusters, const uint32_t* clu
                            const uint32_t* members);
 sg_status sg_summary_info_get(sg_ctx* ctx, sg_summary_info* out);
 
+/* Diagnostic check of the incremental summary repair.  After each batch the
+ * device repairs the summary's PageRank tables itself (entry changes,
+ * exits, the touched supernodes' shortcuts, node types, the is / ib CSRs and
+ * the correction lists: the inc_run of iter_compressor.h:796-896 and
+ * compressor_base.h:5634-5924); the host restatement of the same repair runs
+ * on demand.  This brings the host copy up to date and compares the two:
+ * per row, as sets of targets, weights within a relative 1e-4. */
+typedef struct sg_summary_check {
+  uint64_t rows;       /* rows compared (vertices + mirror rows)                */
+  uint64_t type_diff;  /* vertices whose node type differs                      */
+  uint64_t list_diff;  /* entry / exit / single lists that differ (0..3)        */
+  uint64_t ib_diff;    /* boundary rows that differ                             */
+  uint64_t is_diff;    /* shortcut rows (bound_delta) that differ               */
+  uint64_t corr_diff;  /* supernode correction lists (inner_value / inner_delta) */
+  double max_rel;      /* largest relative weight difference of matched entries */
+} sg_summary_check;
+sg_status sg_summary_check_tables(sg_ctx* ctx, sg_summary_check* out);
+
 /* ----------------------------------------------------------------- SSSP */
 
 /* Batch SSSP from `source` with FP64 distances over the edge weights

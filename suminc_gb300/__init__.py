@@ -85,6 +85,16 @@ class SummaryInfo(C.Structure):
         return d
 
 
+class SummaryCheck(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in (
+        "rows", "type_diff", "list_diff", "ib_diff", "is_diff", "corr_diff")] + [
+        ("max_rel", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: (float(getattr(self, k)) if k == "max_rel" else int(getattr(self, k)))
+                for k, _ in self._fields_}
+
+
 class BatchSpec(C.Structure):
     _fields_ = [
         ("ppr_queries", C.c_uint32),
@@ -230,6 +240,7 @@ _SIGS = {
     "sg_batch_query_stats": ([_P, _P, _P], C.c_int),
     "sg_batch_outputs_device": ([_P, C.POINTER(_P), C.POINTER(_P)], C.c_int),
     "sg_summary_info_get": ([_P, C.POINTER(SummaryInfo)], C.c_int),
+    "sg_summary_check_tables": ([_P, C.POINTER(SummaryCheck)], C.c_int),
     "sg_util_summary_serialize": ([C.c_uint32, _P, _P, C.c_uint32, _P, _P, C.c_int, C.c_int,
                                    C.c_double, _P, C.POINTER(C.c_uint64)], C.c_int),
     "sg_util_greedy_clusters": ([C.c_uint32, _P, _P, C.c_int, C.c_int, C.c_uint64, _P, _P,
@@ -413,6 +424,13 @@ class Context:
         info = SummaryInfo()
         _check(self._lib.sg_summary_info_get(self._h, C.byref(info)), self, "sg_summary_info_get")
         return info.as_dict()
+
+    def summary_check(self) -> dict:
+        """Device-repaired summary tables against the host restatement."""
+        out = SummaryCheck()
+        _check(self._lib.sg_summary_check_tables(self._h, C.byref(out)), self,
+               "sg_summary_check_tables")
+        return out.as_dict()
 
     # -- the reference's text files ---------------------------------------
     def load_files(self, efile, vfile=None, weighted=False):

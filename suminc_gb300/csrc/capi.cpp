@@ -406,6 +406,16 @@ sg_status sg_summary_info_get(sg_ctx* ctx, sg_summary_info* out) {
   return summary_info(ctx, out);
 }
 
+sg_status sg_summary_check_tables(sg_ctx* ctx, sg_summary_check* out) {
+  SG_GUARD(ctx);
+  if (!out) return fail(ctx, SG_ERR_INVALID, "null output");
+  try {
+    return summary_check(ctx, out);
+  } catch (const std::bad_alloc&) {
+    return fail(ctx, SG_ERR_OOM, "host allocation failed");
+  }
+}
+
 sg_status sg_sssp_peval(sg_ctx* ctx, uint32_t source, double* out) {
   SG_GUARD(ctx);
   try {

@@ -390,6 +390,7 @@ sg_status batch_device_outputs(sg_ctx* ctx, const float** ppr, const double** ss
 sg_status summary_free(sg_ctx* ctx);
 sg_status summary_build(sg_ctx* ctx, const std::vector<std::vector<uint32_t>>& clusters);
 sg_status summary_after_apply(sg_ctx* ctx);
+sg_status summary_check(sg_ctx* ctx, sg_summary_check* out);
 // the reference's serialized cluster state (serialize_cluster layout)
 sg_status summary_build_serialized(sg_ctx* ctx, const std::vector<uint8_t>& blob);
 sg_status summary_serialized(sg_ctx* ctx, std::vector<uint8_t>* blob);

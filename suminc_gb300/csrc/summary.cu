@@ -33,95 +33,13 @@
 #include "ctx.h"
 #include "dev.cuh"
 #include "summary.h"
+#include "summary_dev.h"
 
 namespace sg {
 
 void host_transpose(const HostAdj& out, HostAdj& in);
 void host_adj_from_csr(uint32_t n, const uint64_t* rp, const uint32_t* col, const float* w,
                        HostAdj& out);
-
-// cluster precompute staged in shared memory: clusters of up to kStageCap
-// members (8-bit local indices) and kStageEdges local edges, one per warp
-constexpr int kStageCap = 160;
-constexpr int kStageEdges = 2048;
-constexpr int kStageWarps = 8;
-
-struct StageLists {
-  const uint64_t* lin_off;   // per cm_v position: local in-edges
-  const uint8_t* lin_src;    // their tails, as local indices
-  const uint64_t* lout_off;  // per cm_v position: edges to out-mirrors
-  const uint32_t* lout_dst;
-};
-
-struct SummaryDev {
-  bool valid = false;
-  uint32_t old_n = 0, all_n = 0;
-  Summary S;
-  HostAdj out, in;  // host copy of the graph the summary was built on
-  // device sketch
-  uint64_t *is_off = nullptr, *ib_off = nullptr, *sync_off = nullptr;
-  uint32_t *is_nbr = nullptr, *ib_nbr = nullptr, *sync_nbr = nullptr;
-  float* is_w = nullptr;
-  uint32_t* out_deg_all = nullptr;       // out-degree of each row (mirrors: master's)
-  uint32_t *l_entry = nullptr, *l_exit = nullptr, *l_single = nullptr, *l_omirror = nullptr;
-  uint32_t n_entry = 0, n_exit = 0, n_single = 0, n_omirror = 0;
-  uint32_t* omirror_master = nullptr;
-  uint8_t* ntype = nullptr;
-  // correction: per row -> supernode, cluster size; supernode CSRs
-  uint32_t *corr_sp = nullptr, *corr_c = nullptr;
-  uint64_t *id_off = nullptr, *iv_off = nullptr;
-  uint32_t *id_nbr = nullptr, *iv_nbr = nullptr;
-  float *id_w = nullptr, *iv_w = nullptr;
-  // cluster precompute: members (cm layout: clusters in order) and, per
-  // member position, the subgraph out-edges of clusters that are not staged
-  uint64_t *cm_off = nullptr, *sub_off = nullptr;
-  uint32_t *cm_v = nullptr, *sub_nbr = nullptr;
-  uint64_t *lin_off = nullptr, *lout_off = nullptr;  // per cm_v position (staged clusters)
-  uint8_t* lin_src = nullptr;
-  uint32_t* lout_dst = nullptr;
-  uint32_t *bound_list = nullptr;  // exit members per cluster (cm layout)
-  uint64_t* bl_off = nullptr;
-  // state
-  float *bound = nullptr, *spnode = nullptr, *old_x = nullptr;
-  double* d_res = nullptr;
-  uint32_t* sctl = nullptr;  // summarized rounds: done flag, blocks finished, rounds run
-  std::vector<uint32_t> pending_clusters;  // touched since the last IncEval
-  // SSSP over the summary: shortcut distances per supernode (entry -> exit /
-  // out-mirror, entry -> inner member), the summarized CSR and the
-  // correction lists; built on first use, repaired after each batch
-  bool sssp_ready = false;
-  std::vector<std::vector<std::pair<uint32_t, double>>> sp_bound_d, sp_inner_d;
-  std::vector<uint32_t> sssp_pending;  // supernodes touched since, repaired on the next SSSP use
-  uint64_t *sk_off = nullptr, *sk_coff = nullptr;
-  uint32_t *sk_deg = nullptr, *sk_col = nullptr, *sk_crow = nullptr, *sk_cv = nullptr;
-  float *sk_w = nullptr, *sk_cd = nullptr;
-  uint64_t sk_m = 0;
-  uint32_t sk_ncorr = 0;
-  bool sk_stale = true;
-  // IncEval over the summary: the rows whose shortcuts are relaxed again
-  // (every supernode's entry or in-mirror) and the in-mirrors with their
-  // masters (a mirror starts from its master's distance)
-  uint32_t *sk_spid = nullptr, *sk_imir = nullptr, *sk_imaster = nullptr;
-  uint32_t sk_nspid = 0, sk_nimir = 0;
-  // the construction's state between its two halves, serialized
-  std::vector<uint8_t> init_blob;
-  std::unordered_map<const void*, uint64_t> dcap;  // reupload capacities
-  // device staging of the shortcut and SSSP passes, kept between calls so a
-  // batch costs copies instead of frees and allocations (slot -> buffer)
-  struct Stage {
-    void* p = nullptr;
-    size_t cap = 0;
-  };
-  Stage stage[32];
-  SsspViewScratch view;  // queues of the delta-stepping runs over the summary
-  // message_type = pull: per-vertex in-indexes (summary_pull_view)
-  bool pull_stale = true;
-  PullView pv;
-  uint8_t* p_cls = nullptr;
-  uint64_t *p_ie_off = nullptr, *p_bd_off = nullptr;
-  uint32_t *p_ie_nbr = nullptr, *p_bd_src = nullptr, *p_act = nullptr, *p_ent = nullptr;
-  float* p_bd_w = nullptr;
-};
 
 static SummaryDev* sdev(sg_ctx* ctx) { return (SummaryDev*)ctx->summary; }
 
@@ -173,6 +91,7 @@ static void sfree(SummaryDev& D) {
     st = SummaryDev::Stage();
   }
   sssp_view_scratch_free(D.view);
+  repair_free(D);
   D.dcap.clear();
 }
 
@@ -278,24 +197,6 @@ static sg_status stage_up(sg_ctx* ctx, SummaryDev& D, int slot, const std::vecto
 
 // ------------------------------------------------------ shortcut kernel
 
-struct ShortcutArgs {
-  uint32_t n_sp;
-  const uint32_t* sp_cluster;   // cluster of each supernode job
-  const uint32_t* sp_src;       // local index of the entry
-  const uint64_t* cl_off;       // local node range of each cluster [cl_off[c], cl_off[c+1])
-  const uint32_t* cl_inner;     // number of members (iterated nodes) of each cluster
-  const uint64_t* adj_off;      // per local node (global local index) edge range
-  const uint32_t* adj_nbr;      // local target index (relative to the cluster)
-  const float* div;             // out-degree divisor per local node
-  const uint64_t* out_off;      // per job output offset
-  double* out_value;
-  double* out_delta;
-  float damping;
-  double thr_per_node;          // threshold / N
-  const uint32_t* jobs;         // the jobs this launch runs (null: all)
-  const uint64_t* lin_off;      // warp kernel: per local node, its in-edges
-  const uint8_t* lin_src;       // from members (local indices)
-};
 
 // Both kernels iterate like the reference's local sweep
 // (inc_run_to_convergence_mirror, iter_compressor.h:350-430): deltas and
@@ -877,6 +778,7 @@ static sg_status summary_build_with(sg_ctx* ctx, FIRST first_half) {
   D->old_n = S.old_n;
   D->all_n = S.all_n;
   SG_TRY(upload_sketch(ctx, *D));
+  SG_TRY(repair_init(ctx, *D));
   D->valid = true;
   return SG_OK;
 }
@@ -1248,24 +1150,35 @@ static SumArgs sum_args(sg_ctx* ctx, SummaryDev& D, unsigned long long* cnt) {
 
 // first_step: precompute the given clusters (all for PEval), push exits,
 // hand out-mirror deltas to their masters
+static sg_status first_step_dev(sg_ctx* ctx, SummaryDev& D, const uint32_t* d_cls, uint32_t ncls,
+                                unsigned long long* cnt);
+
 static sg_status first_step(sg_ctx* ctx, SummaryDev& D, const std::vector<uint32_t>& cls,
                             unsigned long long* cnt) {
+  uint32_t* d_cls = nullptr;
+  if (!cls.empty()) SG_TRY(upload(ctx, &d_cls, cls));
+  const sg_status st = first_step_dev(ctx, D, d_cls, (uint32_t)cls.size(), cnt);
+  dfree(d_cls);
+  return st;
+}
+
+// the same over a device list of clusters
+static sg_status first_step_dev(sg_ctx* ctx, SummaryDev& D, const uint32_t* d_cls, uint32_t ncls,
+                                unsigned long long* cnt) {
   cudaStream_t st = ctx->stream;
   SumArgs A = sum_args(ctx, D, cnt);
   SG_CUDA(ctx, cudaMemsetAsync(D.bound, 0, 4ull * D.all_n, st));
   SG_CUDA(ctx, cudaMemsetAsync(D.spnode, 0, 4ull * D.all_n, st));
-  if (cls.empty()) return SG_OK;
-  uint32_t* d_cls = nullptr;
-  SG_TRY(upload(ctx, &d_cls, cls));
+  if (ncls == 0) return SG_OK;
   k_stash_x<<<grid_for(D.old_n, 256), 256, 0, st>>>(D.old_n, ctx->pr.x, D.old_x, 0);
   kprof_begin(ctx);
-  k_sum_precompute<<<grid_for((uint64_t)cls.size() * 32, 32 * kStageWarps), 32 * kStageWarps, 0, st>>>(
-      A, d_cls, (uint32_t)cls.size(), D.cm_off, D.cm_v, D.sub_off, D.sub_nbr,
+  k_sum_precompute<<<grid_for((uint64_t)ncls * 32, 32 * kStageWarps), 32 * kStageWarps, 0, st>>>(
+      A, d_cls, ncls, D.cm_off, D.cm_v, D.sub_off, D.sub_nbr,
       StageLists{D.lin_off, D.lin_src, D.lout_off, D.lout_dst},
       ctx->opt.termcheck_threshold / (double)D.old_n);
   kprof_end(ctx, SG_K_SUM_LOCAL);
-  k_sum_bound_push<<<std::min<uint32_t>((uint32_t)cls.size(), ctx->num_sms * 8), 256, 0, st>>>(
-      A, d_cls, (uint32_t)cls.size(), D.bl_off, D.bound_list);
+  k_sum_bound_push<<<std::min<uint32_t>(ncls, ctx->num_sms * 8), 256, 0, st>>>(
+      A, d_cls, ncls, D.bl_off, D.bound_list);
   if (D.n_omirror)
     k_sum_mirror_to_master<<<grid_for(D.n_omirror, 256), 256, 0, st>>>(ctx->pr.delta, D.l_omirror,
                                                                       D.omirror_master, D.n_omirror);
@@ -1273,7 +1186,6 @@ static sg_status first_step(sg_ctx* ctx, SummaryDev& D, const std::vector<uint32
   count_launch(ctx, 5);
   SG_CUDA(ctx, cudaGetLastError());
   SG_CUDA(ctx, cudaStreamSynchronize(st));
-  dfree(d_cls);
   return SG_OK;
 }
 
@@ -1337,6 +1249,8 @@ sg_status pr_summarized(sg_ctx* ctx, bool inc) {
   SG_CUDA(ctx, cudaMemsetAsync(cnt, 0, 16, st));
   SG_CUDA(ctx, cudaEventRecord(ctx->ev0, st));
   std::vector<uint32_t> cls;
+  const uint32_t* d_pend = nullptr;
+  uint32_t n_pend = 0;
   if (!inc) {
     const float init_c = (float)((1.0 - ctx->opt.damping) / (double)ctx->g.n);
     std::vector<float> z(D->all_n, 0.f), dl(D->all_n, 0.f);
@@ -1345,11 +1259,14 @@ sg_status pr_summarized(sg_ctx* ctx, bool inc) {
     SG_CUDA(ctx, cudaMemcpyAsync(s.delta, dl.data(), 4ull * D->all_n, cudaMemcpyHostToDevice, st));
     SG_CUDA(ctx, cudaStreamSynchronize(st));
     for (uint32_t c = 0; c < D->S.supernode_ids.size(); ++c) cls.push_back(c);
+  } else if (D->rep) {
+    SG_TRY(repair_pending_clusters(ctx, *D, &d_pend, &n_pend));
   } else {
     cls = D->pending_clusters;
     D->pending_clusters.clear();
   }
-  SG_TRY(first_step(ctx, *D, cls, cnt));
+  if (d_pend) SG_TRY(first_step_dev(ctx, *D, d_pend, n_pend, cnt));
+  else SG_TRY(first_step(ctx, *D, cls, cnt));
   int srounds = 0;
   SG_TRY(summarized_rounds(ctx, *D, cnt, &srounds));
   SG_CUDA(ctx, cudaEventRecord(ctx->ev1, st));
@@ -1369,24 +1286,15 @@ sg_status pr_summarized(sg_ctx* ctx, bool inc) {
   return stt;
 }
 
-// After sg_apply_updates on a summarized graph: entry changes, exits,
-// subgraphs and shortcuts of the touched clusters, node types and sketch.
-sg_status summary_after_apply(sg_ctx* ctx) {
-  SummaryDev* D = sdev(ctx);
-  if (!D || !D->valid) return SG_OK;
-  if (summary_no_supernodes(ctx)) return SG_OK;  // nothing to repair, ever
-  PhaseTrace T("repair");
-  const DevBatch& B = ctx->batch;
-  // deleted / added pairs of the batch (actions are small; copy to host)
-  const uint64_t na = B.n_act;
-  std::vector<uint32_t> as(na), ad(na), ak(na), af(na);
-  std::vector<float> aw(na);
-  SG_CUDA(ctx, cudaMemcpyAsync(as.data(), B.a_src, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
-  SG_CUDA(ctx, cudaMemcpyAsync(ad.data(), B.a_dst, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
-  SG_CUDA(ctx, cudaMemcpyAsync(ak.data(), B.a_kind, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
-  SG_CUDA(ctx, cudaMemcpyAsync(af.data(), B.a_found, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
-  SG_CUDA(ctx, cudaMemcpyAsync(aw.data(), B.a_w, 4 * na, cudaMemcpyDeviceToHost, ctx->stream));
-  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+// The host restatement of one batch's repair (the summary.cpp passes with
+// the shortcut kernels on the device): entry changes, exits, subgraphs and
+// shortcuts of the touched clusters, node types and the sketch CSRs of S.
+// The device's PageRank tables are repaired by repair.cu; S serves the
+// SSSP and pull-mode paths, the counters and the checks.
+static sg_status host_repair_batch(sg_ctx* ctx, SummaryDev* D, const uint32_t* as,
+                                   const uint32_t* ad, const uint32_t* ak, const uint32_t* af,
+                                   const float* aw, uint64_t na, bool last) {
+  PhaseTrace T("host repair");
   std::vector<std::pair<uint32_t, uint32_t>> deleted, added;
   std::vector<AdjOp> ops_out, ops_in;
   for (uint64_t i = 0; i < na; ++i) {
@@ -1414,7 +1322,10 @@ sg_status summary_after_apply(sg_ctx* ctx) {
   T.mark("actions");
   const bool patched = D->out.n == n && D->in.n == n && host_adj_patch(D->out, ops_out) &&
                        host_adj_patch(D->in, ops_in);
-  if (!patched || D->out.rp[n] != ctx->g.m) {
+  // a batch before the last one of a replay has no device graph to fall
+  // back on (the device holds the graph after the last)
+  if (!patched && !last) return fail(ctx, SG_ERR_STATE, "host graph copy out of step with the batches");
+  if (!patched || (last && D->out.rp[n] != ctx->g.m)) {
     const uint64_t m = ctx->g.m;
     std::vector<uint64_t> rp(n + 1);
     std::vector<uint32_t> col(m);
@@ -1427,13 +1338,6 @@ sg_status summary_after_apply(sg_ctx* ctx) {
   T.mark("host graph patch");
   summary_inc_entries(S, D->out, D->in, deleted, added);
   T.mark("entries");
-  {
-    std::vector<uint32_t> u = D->pending_clusters;
-    u.insert(u.end(), S.update_cluster_ids.begin(), S.update_cluster_ids.end());
-    std::sort(u.begin(), u.end());
-    u.erase(std::unique(u.begin(), u.end()), u.end());
-    D->pending_clusters = u;
-  }
   summary_judge_out_bound(S, D->out, &S.update_cluster_ids);
   summary_build_subgraph(S, D->out, D->in, &S.update_cluster_ids);
   T.mark("exits and subgraphs");
@@ -1448,15 +1352,46 @@ sg_status summary_after_apply(sg_ctx* ctx) {
   T.mark("node types");
   summary_sketch_csr(S, D->out);
   T.mark("sketch CSRs");
-  SG_TRY(upload_sketch(ctx, *D));
-  T.mark("tables and uploads");
   if (D->sssp_ready && ctx->g.weighted) {
     // shortcut distances of the touched supernodes are repaired by the next
     // SSSP query over the summary (a PageRank-only caller never pays them)
     D->sssp_pending.insert(D->sssp_pending.end(), sps.begin(), sps.end());
   }
+  return SG_OK;
+}
+
+
+// Brings S up to date: replays the batches the device repair logged.
+static sg_status host_sync(sg_ctx* ctx, SummaryDev* D) {
+  if (!D->rep || repair_logged_batches(*D) == 0) return SG_OK;
+  std::vector<uint32_t> as, ad, ak, af;
+  std::vector<float> aw;
+  std::vector<uint64_t> ends;
+  SG_TRY(repair_take_log(ctx, *D, &as, &ad, &ak, &af, &aw, &ends));
+  uint64_t b = 0;
+  for (uint64_t e : ends) {
+    SG_TRY(host_repair_batch(ctx, D, as.data() + b, ad.data() + b, ak.data() + b, af.data() + b,
+                             aw.data() + b, e - b, e == ends.back()));
+    b = e;
+  }
+  return SG_OK;
+}
+
+// After sg_apply_updates on a summarized graph: the device repair of the
+// PageRank tables; the host restatement follows on demand (at once when SSSP
+// over the summary runs on this context, and before its action log grows
+// past 64 M actions).
+sg_status summary_after_apply(sg_ctx* ctx) {
+  SummaryDev* D = sdev(ctx);
+  if (!D || !D->valid) return SG_OK;
+  if (summary_no_supernodes(ctx) || !D->rep) return SG_OK;  // nothing to repair, ever
   D->sk_stale = true;
   D->pull_stale = true;
+  {
+    PhaseTrace T("device repair");
+    SG_TRY(repair_after_apply(ctx, *D));
+  }
+  if (D->sssp_ready || repair_logged_actions(*D) > (1ull << 26)) SG_TRY(host_sync(ctx, D));
   return SG_OK;
 }
 
@@ -1618,6 +1553,7 @@ static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
 sg_status summary_pull_view(sg_ctx* ctx, PullView* out) {
   SummaryDev* D = sdev(ctx);
   if (!D || !D->valid) return fail(ctx, SG_ERR_STATE, "compress=1 needs sg_summary_build first");
+  SG_TRY(host_sync(ctx, D));
   if (D->pull_stale) SG_TRY(pull_index_build(ctx, *D));
   *out = D->pv;
   return SG_OK;
@@ -1631,6 +1567,7 @@ uint32_t summary_rows(sg_ctx* ctx) {
 sg_status summary_info(sg_ctx* ctx, sg_summary_info* o) {
   SummaryDev* D = sdev(ctx);
   if (!D || !D->valid) return fail(ctx, SG_ERR_STATE, "no summary built");
+  SG_TRY(host_sync(ctx, D));
   const Summary& S = D->S;
   std::memset(o, 0, sizeof(*o));
   o->clusters = S.supernode_ids.size();
@@ -1653,6 +1590,110 @@ sg_status summary_info(sg_ctx* ctx, sg_summary_info* o) {
   o->shortcut_edges = S.is_off.empty() ? 0 : S.is_off.back();
   for (uint32_t v = 0; v < S.old_n; ++v)
     if (S.node_type[v] >= 0 && S.node_type[v] < 7) o->node_type_count[(int)S.node_type[v]]++;
+  return SG_OK;
+}
+
+// Device-repaired PageRank tables against the host restatement (S after
+// replaying the logged batches).
+template <typename T>
+static sg_status fetch(sg_ctx* ctx, const T* d, uint64_t count, std::vector<T>* h) {
+  h->resize(count);
+  if (count)
+    SG_CUDA(ctx, cudaMemcpyAsync(h->data(), d, sizeof(T) * count, cudaMemcpyDeviceToHost, ctx->stream));
+  return SG_OK;
+}
+
+sg_status summary_check(sg_ctx* ctx, sg_summary_check* o) {
+  SummaryDev* Dp = sdev(ctx);
+  if (!Dp || !Dp->valid) return fail(ctx, SG_ERR_STATE, "no summary built");
+  std::memset(o, 0, sizeof(*o));
+  if (summary_no_supernodes(ctx)) return SG_OK;
+  SG_TRY(host_sync(ctx, Dp));
+  SummaryDev& D = *Dp;
+  const Summary& S = D.S;
+  const uint32_t n = S.old_n, all = S.all_n;
+  std::vector<uint8_t> nt;
+  std::vector<uint64_t> ibo, iso, ivo, ido;
+  std::vector<uint32_t> le, lx, ls, csp;
+  SG_TRY(fetch(ctx, D.ntype, n, &nt));
+  SG_TRY(fetch(ctx, D.ib_off, (uint64_t)all + 1, &ibo));
+  SG_TRY(fetch(ctx, D.is_off, (uint64_t)all + 1, &iso));
+  SG_TRY(fetch(ctx, D.iv_off, (uint64_t)all + 1, &ivo));
+  SG_TRY(fetch(ctx, D.id_off, (uint64_t)all + 1, &ido));
+  SG_TRY(fetch(ctx, D.corr_sp, all, &csp));
+  SG_TRY(fetch(ctx, D.l_entry, D.n_entry, &le));
+  SG_TRY(fetch(ctx, D.l_exit, D.n_exit, &lx));
+  SG_TRY(fetch(ctx, D.l_single, D.n_single, &ls));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  std::vector<uint32_t> ibn, isn, ivn, idn;
+  std::vector<float> isw, ivw, idw;
+  SG_TRY(fetch(ctx, D.ib_nbr, ibo[all], &ibn));
+  SG_TRY(fetch(ctx, D.is_nbr, iso[all], &isn));
+  SG_TRY(fetch(ctx, D.is_w, iso[all], &isw));
+  SG_TRY(fetch(ctx, D.iv_nbr, ivo[all], &ivn));
+  SG_TRY(fetch(ctx, D.iv_w, ivo[all], &ivw));
+  SG_TRY(fetch(ctx, D.id_nbr, ido[all], &idn));
+  SG_TRY(fetch(ctx, D.id_w, ido[all], &idw));
+  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  o->rows = all;
+  std::vector<uint32_t> he, hx, hs;
+  for (uint32_t v = 0; v < n; ++v) {
+    const char t = S.node_type[v];
+    if ((uint8_t)t != nt[v]) o->type_diff++;
+    if (t == kOnlyIn || t == kBothOutIn || t == kBothOutInMaster) he.push_back(v);
+    if (t == kOnlyOut || t == kBothOutIn || t == kOutMaster || t == kBothOutInMaster) hx.push_back(v);
+    if (t == kSingle) hs.push_back(v);
+  }
+  o->list_diff = (he != le) + (hx != lx) + (hs != ls);
+  double max_rel = 0.0;
+  // (target, weight) lists compared as sets of targets, weights within 1e-4
+  auto same = [&](std::vector<std::pair<uint32_t, double>> a,
+                  std::vector<std::pair<uint32_t, double>> b) {
+    if (a.size() != b.size()) return false;
+    std::sort(a.begin(), a.end());
+    std::sort(b.begin(), b.end());
+    for (size_t i = 0; i < a.size(); ++i) {
+      if (a[i].first != b[i].first) return false;
+      const double den = std::max(std::fabs(a[i].second), std::fabs(b[i].second));
+      const double rel = den > 0 ? std::fabs(a[i].second - b[i].second) / den : 0.0;
+      max_rel = std::max(max_rel, rel);
+      if (rel > 1e-4) return false;
+    }
+    return true;
+  };
+  auto dev_row = [](const std::vector<uint64_t>& off, const std::vector<uint32_t>& nbr,
+                    const std::vector<float>* w, uint32_t r) {
+    std::vector<std::pair<uint32_t, double>> x;
+    for (uint64_t e = off[r]; e < off[r + 1]; ++e) x.push_back({nbr[e], w ? (double)(*w)[e] : 0.0});
+    return x;
+  };
+  for (uint32_t r = 0; r < all; ++r) {
+    {
+      std::vector<std::pair<uint32_t, double>> h;
+      for (uint64_t e = S.ib_off[r]; e < S.ib_off[r + 1]; ++e) h.push_back({S.ib_nbr[e], 0.0});
+      if (!same(dev_row(ibo, ibn, nullptr, r), h)) o->ib_diff++;
+    }
+    {
+      std::vector<std::pair<uint32_t, double>> h;
+      for (uint64_t e = S.is_off[r]; e < S.is_off[r + 1]; ++e) h.push_back({S.is_nbr[e], (double)S.is_w[e]});
+      if (!same(dev_row(iso, isn, &isw, r), h)) o->is_diff++;
+    }
+    const uint32_t sp = S.Fc_map[r];
+    const bool hsp = sp != Summary::kIdDefault && sp < S.supernodes.size() && S.supernodes[sp].id == r;
+    const bool dsp = csp[r] != 0xFFFFFFFFu;
+    if (hsp != dsp) {
+      o->corr_diff++;
+      continue;
+    }
+    if (!hsp) continue;
+    const Supernode& h = S.supernodes[sp];
+    std::vector<std::pair<uint32_t, double>> hv(h.inner_value.begin(), h.inner_value.end()),
+        hd(h.inner_delta.begin(), h.inner_delta.end());
+    for (auto& e : hv) e.second = (double)(float)e.second;
+    for (auto& e : hd) e.second = (double)(float)e.second;
+    if (!same(dev_row(ivo, ivn, &ivw, r), hv) || !same(dev_row(ido, idn, &idw, r), hd)) o->corr_diff++;
+  }
+  o->max_rel = max_rel;
   return SG_OK;
 }
 
@@ -2071,6 +2112,7 @@ sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
   SummaryDev* Dp = sdev(ctx);
   if (!Dp || !Dp->valid) return fail(ctx, SG_ERR_STATE, "compress=1 needs sg_summary_build first");
   SummaryDev& D = *Dp;
+  SG_TRY(host_sync(ctx, Dp));
   Summary& S = D.S;
   if (!ctx->g.weighted) return fail(ctx, SG_ERR_INVALID, "SSSP needs a weighted graph");
   if (source >= S.old_n) return fail(ctx, SG_ERR_INVALID, "source >= n");
@@ -2165,6 +2207,7 @@ sg_status sssp_summarized_inc(sg_ctx* ctx) {
   SummaryDev* Dp = sdev(ctx);
   if (!Dp || !Dp->valid) return fail(ctx, SG_ERR_STATE, "compress=1 needs sg_summary_build first");
   SummaryDev& D = *Dp;
+  SG_TRY(host_sync(ctx, Dp));
   Summary& S = D.S;
   if (!ctx->g.weighted) return fail(ctx, SG_ERR_INVALID, "SSSP needs a weighted graph");
   cudaStream_t st = ctx->stream;

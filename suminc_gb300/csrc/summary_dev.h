@@ -1,0 +1,141 @@
+// Device state of a summarized graph, shared by the summary's translation
+// units (summary.cu: construction, PageRank / SSSP over the summary and the
+// host restatement of the repair; repair.cu: the device repair).
+#pragma once
+
+#include <unordered_map>
+#include <vector>
+
+#include "ctx.h"
+#include "summary.h"
+
+namespace sg {
+
+struct RepairDev;  // repair.cu
+
+// cluster precompute staged in shared memory: clusters of up to kStageCap
+// members (8-bit local indices) and kStageEdges local edges, one per warp
+constexpr int kStageCap = 160;
+constexpr int kStageEdges = 2048;
+constexpr int kStageWarps = 8;
+
+struct StageLists {
+  const uint64_t* lin_off;   // per cm_v position: local in-edges
+  const uint8_t* lin_src;    // their tails, as local indices
+  const uint64_t* lout_off;  // per cm_v position: edges to out-mirrors
+  const uint32_t* lout_dst;
+};
+
+// Cluster-local shortcut solves (summary.cu): one job per supernode, the
+// cluster's nodes as local indices and its edges as a local CSR.
+struct ShortcutArgs {
+  uint32_t n_sp;
+  const uint32_t* sp_cluster;   // cluster of each supernode job
+  const uint32_t* sp_src;       // local index of the entry
+  const uint64_t* cl_off;       // local node range of each cluster [cl_off[c], cl_off[c+1])
+  const uint32_t* cl_inner;     // number of members (iterated nodes) of each cluster
+  const uint64_t* adj_off;      // per local node (global local index) edge range
+  const uint32_t* adj_nbr;      // local target index (relative to the cluster)
+  const float* div;             // out-degree divisor per local node
+  const uint64_t* out_off;      // per job output offset
+  double* out_value;
+  double* out_delta;
+  float damping;
+  double thr_per_node;          // threshold / N
+  const uint32_t* jobs;         // the jobs this launch runs (null: all)
+  const uint64_t* lin_off;      // warp kernel: per local node, its in-edges
+  const uint8_t* lin_src;       // from members (local indices)
+};
+
+__global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njobs);
+__global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t njobs);
+
+struct SummaryDev {
+  bool valid = false;
+  uint32_t old_n = 0, all_n = 0;
+  Summary S;
+  HostAdj out, in;  // host copy of the graph the summary was built on
+  // The PageRank tables below are repaired on the device after each batch
+  // (repair.cu).  The host restatement S (and the host graph copy) then
+  // lags behind by the batches in the repair's action log; host_sync
+  // replays them before anything reads S.
+  RepairDev* rep = nullptr;
+  // device sketch
+  uint64_t *is_off = nullptr, *ib_off = nullptr, *sync_off = nullptr;
+  uint32_t *is_nbr = nullptr, *ib_nbr = nullptr, *sync_nbr = nullptr;
+  float* is_w = nullptr;
+  uint32_t* out_deg_all = nullptr;       // out-degree of each row (mirrors: master's)
+  uint32_t *l_entry = nullptr, *l_exit = nullptr, *l_single = nullptr, *l_omirror = nullptr;
+  uint32_t n_entry = 0, n_exit = 0, n_single = 0, n_omirror = 0;
+  uint32_t* omirror_master = nullptr;
+  uint8_t* ntype = nullptr;
+  // correction: per row -> supernode, cluster size; supernode CSRs
+  uint32_t *corr_sp = nullptr, *corr_c = nullptr;
+  uint64_t *id_off = nullptr, *iv_off = nullptr;
+  uint32_t *id_nbr = nullptr, *iv_nbr = nullptr;
+  float *id_w = nullptr, *iv_w = nullptr;
+  // cluster precompute: members (cm layout: clusters in order) and, per
+  // member position, the subgraph out-edges of clusters that are not staged
+  uint64_t *cm_off = nullptr, *sub_off = nullptr;
+  uint32_t *cm_v = nullptr, *sub_nbr = nullptr;
+  uint64_t *lin_off = nullptr, *lout_off = nullptr;  // per cm_v position (staged clusters)
+  uint8_t* lin_src = nullptr;
+  uint32_t* lout_dst = nullptr;
+  uint32_t *bound_list = nullptr;  // exit members per cluster (cm layout)
+  uint64_t* bl_off = nullptr;
+  // state
+  float *bound = nullptr, *spnode = nullptr, *old_x = nullptr;
+  double* d_res = nullptr;
+  uint32_t* sctl = nullptr;  // summarized rounds: done flag, blocks finished, rounds run
+  std::vector<uint32_t> pending_clusters;  // touched since the last IncEval
+  // SSSP over the summary: shortcut distances per supernode (entry -> exit /
+  // out-mirror, entry -> inner member), the summarized CSR and the
+  // correction lists; built on first use, repaired after each batch
+  bool sssp_ready = false;
+  std::vector<std::vector<std::pair<uint32_t, double>>> sp_bound_d, sp_inner_d;
+  std::vector<uint32_t> sssp_pending;  // supernodes touched since, repaired on the next SSSP use
+  uint64_t *sk_off = nullptr, *sk_coff = nullptr;
+  uint32_t *sk_deg = nullptr, *sk_col = nullptr, *sk_crow = nullptr, *sk_cv = nullptr;
+  float *sk_w = nullptr, *sk_cd = nullptr;
+  uint64_t sk_m = 0;
+  uint32_t sk_ncorr = 0;
+  bool sk_stale = true;
+  // IncEval over the summary: the rows whose shortcuts are relaxed again
+  // (every supernode's entry or in-mirror) and the in-mirrors with their
+  // masters (a mirror starts from its master's distance)
+  uint32_t *sk_spid = nullptr, *sk_imir = nullptr, *sk_imaster = nullptr;
+  uint32_t sk_nspid = 0, sk_nimir = 0;
+  // the construction's state between its two halves, serialized
+  std::vector<uint8_t> init_blob;
+  std::unordered_map<const void*, uint64_t> dcap;  // reupload capacities
+  // device staging of the shortcut and SSSP passes, kept between calls so a
+  // batch costs copies instead of frees and allocations (slot -> buffer)
+  struct Stage {
+    void* p = nullptr;
+    size_t cap = 0;
+  };
+  Stage stage[32];
+  SsspViewScratch view;  // queues of the delta-stepping runs over the summary
+  // message_type = pull: per-vertex in-indexes (summary_pull_view)
+  bool pull_stale = true;
+  PullView pv;
+  uint8_t* p_cls = nullptr;
+  uint64_t *p_ie_off = nullptr, *p_bd_off = nullptr;
+  uint32_t *p_ie_nbr = nullptr, *p_bd_src = nullptr, *p_act = nullptr, *p_ent = nullptr;
+  float* p_bd_w = nullptr;
+};
+
+
+// repair.cu: the incremental repair of the PageRank tables on the device
+sg_status repair_init(sg_ctx* ctx, SummaryDev& D);
+sg_status repair_after_apply(sg_ctx* ctx, SummaryDev& D);
+sg_status repair_pending_clusters(sg_ctx* ctx, SummaryDev& D, const uint32_t** list, uint32_t* count);
+uint64_t repair_logged_actions(const SummaryDev& D);
+uint64_t repair_logged_batches(const SummaryDev& D);
+sg_status repair_take_log(sg_ctx* ctx, SummaryDev& D, std::vector<uint32_t>* src,
+                          std::vector<uint32_t>* dst, std::vector<uint32_t>* kind,
+                          std::vector<uint32_t>* found, std::vector<float>* w,
+                          std::vector<uint64_t>* batch_end);
+void repair_free(SummaryDev& D);
+
+}  // namespace sg
