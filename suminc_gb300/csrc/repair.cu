@@ -69,6 +69,9 @@ struct RepairDev {
   uint8_t *c_src = nullptr, *c_upd = nullptr, *c_job = nullptr;          // [ncl]
   uint8_t* c_pend = nullptr;                                             // [ncl]
   uint8_t* r_job = nullptr;                                              // [all_n]
+  uint8_t* f_sp = nullptr;                                               // [all_n]
+  uint32_t* sp_rows = nullptr;                                           // [all_n]
+  uint32_t n_sp = 0;
   uint8_t *f_entry = nullptr, *f_exit = nullptr, *f_single = nullptr;    // [n]
   uint64_t* r_size = nullptr;                                            // [all_n + 1]
   // shortcut blocks: row offsets [all_n + 1] and pools (current, next)
@@ -290,7 +293,7 @@ __global__ void k_rp_entries(RepArgs R) {
 
 // 3. per row: supernode rows and their block sizes, the solves to redo,
 //    exits of updated clusters, out-degrees of all rows
-__global__ void k_rp_rows(RepArgs R, uint64_t* r_size, uint32_t* out_deg_all) {
+__global__ void k_rp_rows(RepArgs R, uint64_t* r_size, uint8_t* f_sp, uint32_t* out_deg_all) {
   for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < R.all_n; r += gridDim.x * blockDim.x) {
     const uint32_t c = R.cl_of[r];
     const bool sp = is_sp_row(R, r, c);
@@ -319,6 +322,7 @@ __global__ void k_rp_rows(RepArgs R, uint64_t* r_size, uint32_t* out_deg_all) {
       }
     }
     r_size[r] = size;
+    f_sp[r] = sp;
     out_deg_all[r] = R.out_deg[r < R.n ? r : R.master[r - R.n]];
   }
 }
@@ -501,13 +505,15 @@ __global__ void k_rp_jobs(RepArgs R, const uint32_t* jobs, uint32_t nj, const ui
 
 // 12. per row (warp): blocks of supernodes whose solve stays move to the
 //     new layout
-__global__ void __launch_bounds__(256) k_rp_move(RepArgs R, const uint64_t* r_size,
+__global__ void __launch_bounds__(256) k_rp_move(RepArgs R, const uint32_t* sp_rows, uint32_t nsp,
+                                                 const uint64_t* r_size,
                                                  const uint64_t* blk, const uint64_t* blk2,
                                                  const double* val, const double* del, double* val2,
                                                  double* del2, uint32_t* err) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < R.all_n; r += nw) {
+  for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nsp; k += nw) {
+    const uint32_t r = sp_rows[k];
     const uint64_t L = r_size[r];
     if (L == 0 || R.r_job[r]) continue;
     const uint64_t s = blk[r], t = blk2[r];
@@ -537,20 +543,19 @@ struct TabArgs {
 // iter_compressor.h:433-491): members with a value go to bound_delta (exits)
 // or inner_value (the rest), members with a residual delta to inner_delta,
 // out-mirrors with value + delta to bound_delta.
+// over the supernode rows (the other rows' counts and correction entries are
+// cleared before)
 template <bool FILL>
-__global__ void __launch_bounds__(256) k_rp_tables(RepArgs R, TabArgs T) {
+__global__ void __launch_bounds__(256) k_rp_tables(RepArgs R, TabArgs T, const uint32_t* sp_rows,
+                                                   uint32_t nsp) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < R.all_n; r += nw) {
+  for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nsp; k += nw) {
+    const uint32_t r = sp_rows[k];
     const uint32_t c = R.cl_of[r];
-    const bool sp = is_sp_row(R, r, c);
     if (!FILL && lane == 0) {
-      T.corr_sp[r] = sp ? r : kNone;
-      T.corr_c[r] = sp ? R.inner[c] : 0u;
-    }
-    if (!sp) {
-      if (!FILL && lane == 0) T.is_cnt[r] = T.iv_cnt[r] = T.id_cnt[r] = 0;
-      continue;
+      T.corr_sp[r] = r;
+      T.corr_c[r] = R.inner[c];
     }
     const uint32_t L = cl_size(R, c), inner = R.inner[c], om0 = inner + R.n_im[c];
     const uint64_t b = T.blk[r], n0 = R.cn_off[c];
@@ -622,10 +627,13 @@ __device__ __forceinline__ int ib_mode(uint8_t t) {
 }
 
 // ib rows: exits keep their boundary edges, unclustered vertices all edges
+// over the rows of a list (exits, unclustered vertices); the other rows'
+// counts are cleared before
 template <bool FILL>
-__global__ void k_rp_ib(RepArgs R, const uint8_t* ntype, uint64_t* cnt, const uint64_t* off,
-                        uint32_t* nbr) {
-  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < R.all_n; r += gridDim.x * blockDim.x) {
+__global__ void k_rp_ib(RepArgs R, const uint8_t* ntype, const uint32_t* rows, uint32_t nrows,
+                        uint64_t* cnt, const uint64_t* off, uint32_t* nbr) {
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nrows; q += gridDim.x * blockDim.x) {
+    const uint32_t r = rows[q];
     const int mode = r < R.n ? ib_mode(ntype[r]) : 0;
     uint64_t k = FILL ? off[r] : 0;
     if (mode) {
@@ -867,7 +875,7 @@ RepArgs rep_args(sg_ctx* ctx, RepairDev& P) {
 
 // Solves again the supernode rows marked in r_job (r_size holds every row's
 // block size) into the next pool layout and moves the other blocks there.
-sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R) {
+sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, PhaseTrace& T) {
   cudaStream_t st = ctx->stream;
   const uint32_t all = P.all_n;
   SG_TRY(scan_u64(ctx, P.r_size, P.blk2, (uint64_t)all + 1));
@@ -875,9 +883,13 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
   SG_TRY(read_u64(ctx, P.blk2 + all, &total));
   SG_TRY(grow_pool(ctx, &P.pool2, total));
   SG_TRY(select_idx(ctx, P.r_job, P.jobs, P.d_num, all));
-  uint32_t nj = 0;
-  SG_CUDA(ctx, cudaMemcpyAsync(&nj, P.d_num, 4, cudaMemcpyDeviceToHost, st));
+  SG_TRY(select_idx(ctx, P.f_sp, P.sp_rows, P.d_num + 1, all));
+  uint32_t nj_sp[2] = {0, 0};
+  SG_CUDA(ctx, cudaMemcpyAsync(nj_sp, P.d_num, 8, cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
+  const uint32_t nj = nj_sp[0];
+  P.n_sp = nj_sp[1];
+  T.mark("layout and jobs");
   if (nj) {
     k_rp_job_clusters<<<grid_for(nj, 256), 256, 0, st>>>(R, P.jobs, nj);
     SG_TRY(select_idx(ctx, P.c_job, P.tcl, P.d_num, P.ncl));
@@ -914,6 +926,7 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
     uint32_t nwb[2] = {0, 0};
     SG_CUDA(ctx, cudaMemcpyAsync(nwb, P.d_num, 8, cudaMemcpyDeviceToHost, st));
     SG_CUDA(ctx, cudaStreamSynchronize(st));
+    T.mark("local problems");
     ShortcutArgs A;
     A.n_sp = nj;
     A.sp_cluster = P.sp_cl;
@@ -947,19 +960,22 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
     }
     kprof_end(ctx, SG_K_SUMMARY);
     count_launch(ctx, 12);
+    T.mark("shortcut kernels", st);
   }
-  k_rp_move<<<grid_for((uint64_t)all * 32, 256), 256, 0, st>>>(
-      R, P.r_size, P.blk, P.blk2, P.pool.val, P.pool.del, P.pool2.val, P.pool2.del, P.d_err);
+  k_rp_move<<<grid_for((uint64_t)P.n_sp * 32, 256), 256, 0, st>>>(
+      R, P.sp_rows, P.n_sp, P.r_size, P.blk, P.blk2, P.pool.val, P.pool.del, P.pool2.val,
+      P.pool2.del, P.d_err);
   count_launch(ctx);
   SG_CUDA(ctx, cudaGetLastError());
   std::swap(P.blk, P.blk2);
   std::swap(P.pool, P.pool2);
+  T.mark("blocks moved", st);
   (void)D;
   return SG_OK;
 }
 
 // Rebuilds the PageRank tables of the summary from the repaired state.
-sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R) {
+sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, PhaseTrace& PT) {
   cudaStream_t st = ctx->stream;
   const uint32_t n = P.n, all = P.all_n, ncl = P.ncl;
   SG_TRY(reserve(ctx, D, &D.ntype, n));
@@ -976,6 +992,19 @@ sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R) 
   SG_TRY(select_idx(ctx, P.f_entry, D.l_entry, P.d_num, n));
   SG_TRY(select_idx(ctx, P.f_exit, D.l_exit, P.d_num + 1, n));
   SG_TRY(select_idx(ctx, P.f_single, D.l_single, P.d_num + 2, n));
+  uint32_t nl[3] = {0, 0, 0};
+  SG_CUDA(ctx, cudaMemcpyAsync(nl, P.d_num, 12, cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaMemsetAsync(P.cnt_a, 0, 8ull * (all + 1), st));
+  SG_CUDA(ctx, cudaMemsetAsync(P.cnt_b, 0, 8ull * (all + 1), st));
+  SG_CUDA(ctx, cudaMemsetAsync(P.cnt_c, 0, 8ull * (all + 1), st));
+  SG_CUDA(ctx, cudaMemsetAsync(P.cnt_d, 0, 8ull * (all + 1), st));
+  SG_CUDA(ctx, cudaMemsetAsync(D.corr_sp, 0xFF, 4ull * all, st));
+  SG_CUDA(ctx, cudaMemsetAsync(D.corr_c, 0, 4ull * all, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  D.n_entry = nl[0];
+  D.n_exit = nl[1];
+  D.n_single = nl[2];
+  PT.mark("node types and lists", st);
   // supernode lists and the correction tables
   TabArgs T{};
   T.blk = P.blk;
@@ -986,24 +1015,24 @@ sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R) 
   T.id_cnt = P.cnt_c;
   T.corr_sp = D.corr_sp;
   T.corr_c = D.corr_c;
-  const unsigned rg = grid_for((uint64_t)all * 32, 256);
-  k_rp_tables<false><<<rg, 256, 0, st>>>(R, T);
+  const unsigned rg = grid_for((uint64_t)P.n_sp * 32, 256);
+  k_rp_tables<false><<<rg, 256, 0, st>>>(R, T, P.sp_rows, P.n_sp);
   SG_TRY(scan_u64(ctx, P.cnt_a, D.is_off, (uint64_t)all + 1));
   SG_TRY(scan_u64(ctx, P.cnt_b, D.iv_off, (uint64_t)all + 1));
   SG_TRY(scan_u64(ctx, P.cnt_c, D.id_off, (uint64_t)all + 1));
-  k_rp_ib<false><<<grid_for(all, 256), 256, 0, st>>>(R, D.ntype, P.cnt_a, nullptr, nullptr);
-  SG_TRY(scan_u64(ctx, P.cnt_a, D.ib_off, (uint64_t)all + 1));
+  if (D.n_exit)
+    k_rp_ib<false><<<grid_for(D.n_exit, 256), 256, 0, st>>>(R, D.ntype, D.l_exit, D.n_exit, P.cnt_d,
+                                                            nullptr, nullptr);
+  if (D.n_single)
+    k_rp_ib<false><<<grid_for(D.n_single, 256), 256, 0, st>>>(R, D.ntype, D.l_single, D.n_single,
+                                                              P.cnt_d, nullptr, nullptr);
+  SG_TRY(scan_u64(ctx, P.cnt_d, D.ib_off, (uint64_t)all + 1));
   uint64_t tot[4] = {0, 0, 0, 0};
-  uint32_t nl[3] = {0, 0, 0};
   SG_CUDA(ctx, cudaMemcpyAsync(&tot[0], D.is_off + all, 8, cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaMemcpyAsync(&tot[1], D.iv_off + all, 8, cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaMemcpyAsync(&tot[2], D.id_off + all, 8, cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaMemcpyAsync(&tot[3], D.ib_off + all, 8, cudaMemcpyDeviceToHost, st));
-  SG_CUDA(ctx, cudaMemcpyAsync(nl, P.d_num, 12, cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
-  D.n_entry = nl[0];
-  D.n_exit = nl[1];
-  D.n_single = nl[2];
   SG_TRY(reserve(ctx, D, &D.is_nbr, tot[0]));
   SG_TRY(reserve(ctx, D, &D.is_w, tot[0]));
   SG_TRY(reserve(ctx, D, &D.iv_nbr, tot[1]));
@@ -1020,8 +1049,14 @@ sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R) 
   T.iv_w = D.iv_w;
   T.id_nbr = D.id_nbr;
   T.id_w = D.id_w;
-  k_rp_tables<true><<<rg, 256, 0, st>>>(R, T);
-  k_rp_ib<true><<<grid_for(all, 256), 256, 0, st>>>(R, D.ntype, nullptr, D.ib_off, D.ib_nbr);
+  k_rp_tables<true><<<rg, 256, 0, st>>>(R, T, P.sp_rows, P.n_sp);
+  if (D.n_exit)
+    k_rp_ib<true><<<grid_for(D.n_exit, 256), 256, 0, st>>>(R, D.ntype, D.l_exit, D.n_exit, nullptr,
+                                                           D.ib_off, D.ib_nbr);
+  if (D.n_single)
+    k_rp_ib<true><<<grid_for(D.n_single, 256), 256, 0, st>>>(R, D.ntype, D.l_single, D.n_single,
+                                                             nullptr, D.ib_off, D.ib_nbr);
+  PT.mark("supernode lists and ib rows", st);
   // cluster precompute lists
   CmArgs C{};
   C.cm_off = D.cm_off;
@@ -1063,6 +1098,7 @@ sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R) 
   C.sub_nbr = D.sub_nbr;
   k_rp_cm<true><<<cg, 256, 0, st>>>(R, C);
   k_rp_cm_tail<<<1, 32, 0, st>>>(C, ncl, npos);
+  PT.mark("cluster lists", st);
   count_launch(ctx, 20);
   SG_CUDA(ctx, cudaGetLastError());
   return SG_OK;
@@ -1091,6 +1127,7 @@ void repair_free(SummaryDev& D) {
   dfree(P->m_src); dfree(P->m_ret); dfree(P->m_new);
   dfree(P->c_src); dfree(P->c_upd); dfree(P->c_job); dfree(P->c_pend); dfree(P->r_job);
   dfree(P->f_entry); dfree(P->f_exit); dfree(P->f_single); dfree(P->r_size);
+  dfree(P->f_sp); dfree(P->sp_rows);
   dfree(P->blk); dfree(P->blk2);
   dfree(P->pool.val); dfree(P->pool.del); dfree(P->pool2.val); dfree(P->pool2.del);
   dfree(P->jobs); dfree(P->tcl); dfree(P->tc_idx); dfree(P->tc_inner); dfree(P->sp_cl);
@@ -1191,6 +1228,8 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
   SG_TRY(dalloc(ctx, &P.c_job, ncl));
   SG_TRY(dalloc(ctx, &P.c_pend, ncl));
   SG_TRY(dalloc(ctx, &P.r_job, all));
+  SG_TRY(dalloc(ctx, &P.f_sp, all));
+  SG_TRY(dalloc(ctx, &P.sp_rows, all));
   SG_TRY(dalloc(ctx, &P.r_size, (uint64_t)all + 1));
   SG_TRY(dalloc(ctx, &P.blk, (uint64_t)all + 1));
   SG_TRY(dalloc(ctx, &P.blk2, (uint64_t)all + 1));
@@ -1237,10 +1276,11 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
   SG_CUDA(ctx, cudaMemsetAsync(P.c_src, 1, ncl, st));
   const RepArgs R = rep_args(ctx, P);
   SG_TRY(reserve(ctx, D, &D.out_deg_all, all));
-  k_rp_rows<<<grid_for(all, 256), 256, 0, st>>>(R, P.r_size, D.out_deg_all);
+  k_rp_rows<<<grid_for(all, 256), 256, 0, st>>>(R, P.r_size, P.f_sp, D.out_deg_all);
   count_launch(ctx);
-  SG_TRY(rp_shortcuts(ctx, D, P, R));
-  SG_TRY(rp_tables(ctx, D, P, R));
+  PhaseTrace T("device summary build");
+  SG_TRY(rp_shortcuts(ctx, D, P, R, T));
+  SG_TRY(rp_tables(ctx, D, P, R, T));
   return rp_finish(ctx, P, R);
 }
 
@@ -1251,6 +1291,7 @@ sg_status repair_after_apply(sg_ctx* ctx, SummaryDev& D) {
   cudaStream_t st = ctx->stream;
   const DevBatch& B = ctx->batch;
   const uint64_t na = B.n_act;
+  PhaseTrace T("device repair");
   // the actions, kept for the host restatement
   if (na) {
     const uint64_t need = P.log_n + na;
@@ -1269,16 +1310,20 @@ sg_status repair_after_apply(sg_ctx* ctx, SummaryDev& D) {
     P.log_n = need;
   }
   P.log_end.push_back(P.log_n);
+  T.mark("action log", st);
   const RepArgs R = rep_args(ctx, P);
   if (na)
     k_rp_actions<<<grid_for(na * 32, 256), 256, 0, st>>>(R, B.a_src, B.a_dst, B.a_kind, B.a_found, na);
   k_rp_entries<<<grid_for(P.n, 256), 256, 0, st>>>(R);
   SG_TRY(reserve(ctx, D, &D.out_deg_all, P.all_n));
-  k_rp_rows<<<grid_for(P.all_n, 256), 256, 0, st>>>(R, P.r_size, D.out_deg_all);
+  k_rp_rows<<<grid_for(P.all_n, 256), 256, 0, st>>>(R, P.r_size, P.f_sp, D.out_deg_all);
   count_launch(ctx, 3);
-  SG_TRY(rp_shortcuts(ctx, D, P, R));
-  SG_TRY(rp_tables(ctx, D, P, R));
-  return rp_finish(ctx, P, R);
+  T.mark("entries, exits, rows", st);
+  SG_TRY(rp_shortcuts(ctx, D, P, R, T));
+  SG_TRY(rp_tables(ctx, D, P, R, T));
+  const sg_status fs = rp_finish(ctx, P, R);
+  T.mark("finish");
+  return fs;
 }
 
 sg_status repair_pending_clusters(sg_ctx* ctx, SummaryDev& D, const uint32_t** list, uint32_t* count) {

@@ -43,32 +43,6 @@ void host_adj_from_csr(uint32_t n, const uint64_t* rp, const uint32_t* col, cons
 
 static SummaryDev* sdev(sg_ctx* ctx) { return (SummaryDev*)ctx->summary; }
 
-// Host phase times of the summary's maintenance, printed to stderr when the
-// environment sets SUMINC_GB300_TRACE (a diagnostic; off by default).
-struct PhaseTrace {
-  bool on;
-  const char* what;
-  std::chrono::steady_clock::time_point t0, t;
-  explicit PhaseTrace(const char* w) : what(w) {
-    static const bool env = std::getenv("SUMINC_GB300_TRACE") != nullptr;
-    on = env;
-    t0 = t = std::chrono::steady_clock::now();
-  }
-  void mark(const char* phase) {
-    if (!on) return;
-    const auto now = std::chrono::steady_clock::now();
-    std::fprintf(stderr, "[suminc_gb300] %s %s %.2f ms\n", what, phase,
-                 std::chrono::duration<double, std::milli>(now - t).count());
-    t = now;
-  }
-  ~PhaseTrace() {
-    if (on)
-      std::fprintf(stderr, "[suminc_gb300] %s total %.2f ms\n", what,
-                   std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
-                       .count());
-  }
-};
-
 static void sfree(SummaryDev& D) {
   dfree(D.is_off); dfree(D.ib_off); dfree(D.sync_off);
   dfree(D.is_nbr); dfree(D.ib_nbr); dfree(D.sync_nbr); dfree(D.is_w);
@@ -199,10 +173,25 @@ static sg_status stage_up(sg_ctx* ctx, SummaryDev& D, int slot, const std::vecto
 
 
 // Both kernels iterate like the reference's local sweep
-// (inc_run_to_convergence_mirror, iter_compressor.h:350-430): deltas and
-// the values pushed along edges in FP32 (the reference's value_t for
-// PageRank, outv = delta * d / out_degree), the accumulated shortcut value
-// of every node and the delta mass of a step in FP64.
+// (inc_run_to_convergence_mirror, iter_compressor.h:350-430): deltas, the
+// values pushed along edges (the reference's value_t for PageRank, outv =
+// delta * d / out_degree) and the delta mass of a step (its float Diff) in
+// FP32; the shortcut value of every node accumulates in FP64.
+
+// Exact FP32 -> FP64 widening of a normal float by its IEEE fields (sign,
+// exponent rebased from 127 to 1023, mantissa shifted into the top of the
+// 52-bit field); zero, subnormals and non-finite values take the
+// conversion instruction.  Keeps the widening off the FP64 pipe, which
+// GB300 runs at a small fraction of the FP32 rate.
+__device__ __forceinline__ double widen_f32(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xFFu;
+  if (e == 0u || e == 0xFFu) return (double)f;
+  const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) |
+                                  ((unsigned long long)(e + (1023u - 127u)) << 52) |
+                                  ((unsigned long long)(b & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)bits);
+}
 
 // One CTA per supernode job (clusters of any size).
 __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njobs) {
@@ -219,7 +208,7 @@ __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njob
   double* value = sm;
   float* delta = (float*)(sm + L);
   float* next = delta + L;
-  __shared__ double s_diff;
+  __shared__ float s_diff;
   for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) {
     value[i] = 0.0;
     delta[i] = (i == src) ? 1.f : 0.f;
@@ -239,20 +228,20 @@ __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njob
   }
   const double thr = A.thr_per_node * (double)inner;
   for (int step = 1;; ++step) {
-    if (threadIdx.x == 0) s_diff = 0.0;
+    if (threadIdx.x == 0) s_diff = 0.f;
     for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) next[i] = i < inner ? 0.f : delta[i];
     __syncthreads();
-    double diff = 0.0;
+    float diff = 0.f;
     for (uint32_t i = threadIdx.x; i < inner; i += blockDim.x) {
       const float ts = delta[i];
       if (ts == 0.f) continue;
-      value[i] += (double)ts;
-      diff += fabs((double)ts);
+      value[i] += widen_f32(ts);
+      diff += fabsf(ts);
       const float outv = ts * d / A.div[l0 + i];
       for (uint64_t e = A.adj_off[l0 + i]; e < A.adj_off[l0 + i + 1]; ++e)
         atomicAdd(&next[A.adj_nbr[e]], outv);
     }
-    if (diff != 0.0) atomicAdd(&s_diff, diff);
+    if (diff != 0.f) atomicAdd(&s_diff, diff);
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) delta[i] = next[i];
     __syncthreads();
@@ -311,13 +300,13 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
     }
     const double thr = A.thr_per_node * (double)inner;
     for (int step = 1;; ++step) {
-      double diff = 0.0;
+      float diff = 0.f;
       for (uint32_t i = lane; i < inner; i += 32) {
         const float ts = del[i];
         float out = 0.f;
         if (ts != 0.f) {
-          val[i] += (double)ts;
-          diff += fabs((double)ts);
+          val[i] += widen_f32(ts);
+          diff += fabsf(ts);
           out = ts * d / dv[i];
         }
         pv[i] = out;
@@ -331,7 +320,7 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) diff += __shfl_xor_sync(0xffffffffu, diff, o);
       __syncwarp();
-      if (diff <= thr || step > 100) break;
+      if ((double)diff <= thr || step > 100) break;
     }
     const uint64_t o = A.out_off[s];
     for (uint32_t i = lane; i < L; i += 32) {
@@ -1387,10 +1376,7 @@ sg_status summary_after_apply(sg_ctx* ctx) {
   if (summary_no_supernodes(ctx) || !D->rep) return SG_OK;  // nothing to repair, ever
   D->sk_stale = true;
   D->pull_stale = true;
-  {
-    PhaseTrace T("device repair");
-    SG_TRY(repair_after_apply(ctx, *D));
-  }
+  SG_TRY(repair_after_apply(ctx, *D));
   if (D->sssp_ready || repair_logged_actions(*D) > (1ull << 26)) SG_TRY(host_sync(ctx, D));
   return SG_OK;
 }

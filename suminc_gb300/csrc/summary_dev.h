@@ -3,6 +3,9 @@
 // host restatement of the repair; repair.cu: the device repair).
 #pragma once
 
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <unordered_map>
 #include <vector>
 
@@ -12,6 +15,35 @@
 namespace sg {
 
 struct RepairDev;  // repair.cu
+
+// Host phase times of the summary's maintenance, printed to stderr when the
+// environment sets SUMINC_GB300_TRACE (a diagnostic; off by default).
+struct PhaseTrace {
+  bool on;
+  const char* what;
+  std::chrono::steady_clock::time_point t0, t;
+  explicit PhaseTrace(const char* w) : what(w) {
+    static const bool env = std::getenv("SUMINC_GB300_TRACE") != nullptr;
+    on = env;
+    t0 = t = std::chrono::steady_clock::now();
+  }
+  // with a stream, the phase's device work is waited for first
+  void mark(const char* phase, cudaStream_t st = nullptr) {
+    if (!on) return;
+    if (st) cudaStreamSynchronize(st);
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "[suminc_gb300] %s %s %.2f ms\n", what, phase,
+                 std::chrono::duration<double, std::milli>(now - t).count());
+    t = now;
+  }
+  ~PhaseTrace() {
+    if (on)
+      std::fprintf(stderr, "[suminc_gb300] %s total %.2f ms\n", what,
+                   std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
+                       .count());
+  }
+};
+
 
 // cluster precompute staged in shared memory: clusters of up to kStageCap
 // members (8-bit local indices) and kStageEdges local edges, one per warp
