@@ -951,7 +951,7 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
           A, nwb[0]);
     }
     if (nwb[1]) {
-      const size_t smem = 2 * (size_t)P.max_L * sizeof(double);
+      const size_t smem = shortcut_smem(P.max_L);
       if (smem > 48 * 1024)
         SG_CUDA(ctx, cudaFuncSetAttribute(k_shortcuts, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem));
@@ -1179,7 +1179,7 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
     P.max_L = std::max<uint32_t>(P.max_L, (uint32_t)nodes.size());
     P.n_members += mem.size();
   }
-  if (2 * (size_t)P.max_L * sizeof(double) > 200 * 1024)
+  if (shortcut_smem(P.max_L) > 200 * 1024)
     return fail(ctx, SG_ERR_UNSUPPORTED, "cluster too large for the shortcut kernel");
   // in-mirrors and out-mirrors of each master, by cluster
   std::vector<std::vector<uint32_t>> byv_i(n), byv_o(n);

@@ -174,24 +174,13 @@ static sg_status stage_up(sg_ctx* ctx, SummaryDev& D, int slot, const std::vecto
 
 // Both kernels iterate like the reference's local sweep
 // (inc_run_to_convergence_mirror, iter_compressor.h:350-430): deltas, the
-// values pushed along edges (the reference's value_t for PageRank, outv =
-// delta * d / out_degree) and the delta mass of a step (its float Diff) in
-// FP32; the shortcut value of every node accumulates in FP64.
-
-// Exact FP32 -> FP64 widening of a normal float by its IEEE fields (sign,
-// exponent rebased from 127 to 1023, mantissa shifted into the top of the
-// 52-bit field); zero, subnormals and non-finite values take the
-// conversion instruction.  Keeps the widening off the FP64 pipe, which
-// GB300 runs at a small fraction of the FP32 rate.
-__device__ __forceinline__ double widen_f32(float f) {
-  const uint32_t b = __float_as_uint(f);
-  const uint32_t e = (b >> 23) & 0xFFu;
-  if (e == 0u || e == 0xFFu) return (double)f;
-  const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) |
-                                  ((unsigned long long)(e + (1023u - 127u)) << 52) |
-                                  ((unsigned long long)(b & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)bits);
-}
+// values pushed along edges (the reference's value_t for PageRank: delta
+// times d / out_degree) and the delta mass of a step (its float Diff) in
+// FP32.  The shortcut value of every node accumulates in FP64: each node
+// sums its deltas of eight steps in FP32 and adds that partial sum to its
+// FP64 value (GB300 issues a warp's FP64 add at a small fraction of the FP32
+// rate, and one per node and step held the kernel at the FP64 pipe's limit).
+constexpr int kShortcutFlush = 8;
 
 // One CTA per supernode job (clusters of any size).
 __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njobs) {
@@ -205,13 +194,15 @@ __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njob
   const uint32_t inner = A.cl_inner[c];
   const uint32_t src = A.sp_src[s];
   const float d = A.damping;
-  double* value = sm;
-  float* delta = (float*)(sm + L);
-  float* next = delta + L;
+  double* value = sm;                    // [L]
+  float* delta = (float*)(sm + L);       // [L]
+  float* next = delta + L;               // [L]
+  float* part = next + L;                // [L] partial sums of the current eight steps
   __shared__ float s_diff;
   for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) {
     value[i] = 0.0;
     delta[i] = (i == src) ? 1.f : 0.f;
+    part[i] = 0.f;
   }
   __syncthreads();
   // an in-mirror entry first sends its unit along its edges into the cluster
@@ -232,12 +223,19 @@ __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njob
     for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) next[i] = i < inner ? 0.f : delta[i];
     __syncthreads();
     float diff = 0.f;
+    const bool flush = step % kShortcutFlush == 0;
     for (uint32_t i = threadIdx.x; i < inner; i += blockDim.x) {
       const float ts = delta[i];
+      const float p = part[i] + ts;
+      if (flush) {
+        value[i] += widen_f32(p);
+        part[i] = 0.f;
+      } else {
+        part[i] = p;
+      }
       if (ts == 0.f) continue;
-      value[i] += widen_f32(ts);
       diff += fabsf(ts);
-      const float outv = ts * d / A.div[l0 + i];
+      const float outv = ts * (d / A.div[l0 + i]);
       for (uint64_t e = A.adj_off[l0 + i]; e < A.adj_off[l0 + i + 1]; ++e)
         atomicAdd(&next[A.adj_nbr[e]], outv);
     }
@@ -251,7 +249,7 @@ __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njob
   }
   const uint64_t o = A.out_off[s];
   for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) {
-    A.out_value[o + i] = value[i];
+    A.out_value[o + i] = i < inner ? value[i] + widen_f32(part[i]) : value[i];
     A.out_delta[o + i] = (double)delta[i];
   }
 }
@@ -264,9 +262,10 @@ __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njob
 // of its in-edges from members (mirrors keep what they hold).
 __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t njobs) {
   __shared__ double s_val[kStageWarps][kStageCap];
+  __shared__ float s_part[kStageWarps][kStageCap];
   __shared__ float s_del[kStageWarps][kStageCap];
   __shared__ float s_pv[kStageWarps][kStageCap];
-  __shared__ float s_div[kStageWarps][kStageCap];
+  __shared__ float s_f[kStageWarps][kStageCap];
   const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   const float d = A.damping;
@@ -278,19 +277,21 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
     const uint32_t inner = A.cl_inner[c];
     const uint32_t src = A.sp_src[s];
     double* val = s_val[w];
+    float* part = s_part[w];
     float* del = s_del[w];
     float* pv = s_pv[w];
-    float* dv = s_div[w];
+    float* f = s_f[w];  // d / out-degree of each node
     for (uint32_t i = lane; i < L; i += 32) {
       val[i] = 0.0;
+      part[i] = 0.f;
       del[i] = (i == src) ? 1.f : 0.f;
-      dv[i] = A.div[l0 + i];
+      f[i] = d / A.div[l0 + i];
     }
     __syncwarp();
     // an in-mirror entry first sends its unit along its edges into the cluster
     if (src >= inner) {
       if (lane == 0) {
-        const float outv = d / dv[src];
+        const float outv = f[src];
         for (uint64_t e = A.adj_off[l0 + src]; e < A.adj_off[l0 + src + 1]; ++e)
           del[A.adj_nbr[e]] += outv;
         val[src] += 1.0;
@@ -301,20 +302,24 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
     const double thr = A.thr_per_node * (double)inner;
     for (int step = 1;; ++step) {
       float diff = 0.f;
+      const bool flush = step % kShortcutFlush == 0;
       for (uint32_t i = lane; i < inner; i += 32) {
         const float ts = del[i];
-        float out = 0.f;
-        if (ts != 0.f) {
-          val[i] += widen_f32(ts);
-          diff += fabsf(ts);
-          out = ts * d / dv[i];
+        const float p = part[i] + ts;
+        if (flush) {
+          val[i] += widen_f32(p);
+          part[i] = 0.f;
+        } else {
+          part[i] = p;
         }
-        pv[i] = out;
+        diff += fabsf(ts);
+        pv[i] = ts * f[i];
       }
       __syncwarp();
       for (uint32_t j = lane; j < L; j += 32) {
         float acc = 0.f;
-        for (uint64_t f = A.lin_off[l0 + j]; f < A.lin_off[l0 + j + 1]; ++f) acc += pv[A.lin_src[f]];
+        const uint64_t f1 = A.lin_off[l0 + j + 1];
+        for (uint64_t q = A.lin_off[l0 + j]; q < f1; ++q) acc += pv[A.lin_src[q]];
         del[j] = (j < inner ? 0.f : del[j]) + acc;
       }
 #pragma unroll
@@ -324,7 +329,7 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
     }
     const uint64_t o = A.out_off[s];
     for (uint32_t i = lane; i < L; i += 32) {
-      A.out_value[o + i] = val[i];
+      A.out_value[o + i] = i < inner ? val[i] + widen_f32(part[i]) : val[i];
       A.out_delta[o + i] = (double)del[i];
     }
     __syncwarp();
@@ -450,7 +455,7 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
     }
   }
   (void)maxL;
-  const size_t smem = 2 * maxL_block * sizeof(double);
+  const size_t smem = shortcut_smem(maxL_block);
   if (smem > 200 * 1024) return fail(ctx, SG_ERR_UNSUPPORTED, "cluster too large for the shortcut kernel");
   uint32_t *d_spc = nullptr, *d_src = nullptr, *d_inner = nullptr, *d_adj = nullptr;
   uint64_t *d_cloff = nullptr, *d_adjoff = nullptr, *d_outoff = nullptr;

@@ -58,6 +58,21 @@ struct StageLists {
   const uint32_t* lout_dst;
 };
 
+// Exact FP32 -> FP64 widening of a normal float by its IEEE fields (sign,
+// exponent rebased from 127 to 1023, mantissa shifted into the top of the
+// 52-bit field); zero, subnormals and non-finite values take the
+// conversion instruction.  Keeps the widening off the FP64 pipe, which
+// GB300 runs at a small fraction of the FP32 rate.
+__device__ __forceinline__ double widen_f32(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xFFu;
+  if (e == 0u || e == 0xFFu) return (double)f;
+  const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) |
+                                  ((unsigned long long)(e + (1023u - 127u)) << 52) |
+                                  ((unsigned long long)(b & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
 // Cluster-local shortcut solves (summary.cu): one job per supernode, the
 // cluster's nodes as local indices and its edges as a local CSR.
 struct ShortcutArgs {
@@ -80,6 +95,8 @@ struct ShortcutArgs {
 };
 
 __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njobs);
+// dynamic shared memory of k_shortcuts for a cluster of L nodes
+inline size_t shortcut_smem(size_t L) { return L * (sizeof(double) + 3 * sizeof(float)); }
 __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t njobs);
 
 struct SummaryDev {
