@@ -164,13 +164,13 @@ struct Smem {
 
 // One query's delta update at vertex v (query column j of a float4).
 __device__ __forceinline__ void ppr_update(uint32_t st, float& d, float& x, float& pvn, float s,
-                                           float scale, float thr, double& res) {
+                                           float scale, float thr, float& res) {
   if (st == Q_DONE) {
     pvn = 0.f;
     return;
   }
   const float dl = d + s;
-  res += fabs((double)dl);
+  res += fabsf(dl);
   if (st == Q_PENDING) {  // drain round: collect, activate nothing
     d = dl;
     pvn = 0.f;
@@ -191,7 +191,7 @@ __device__ __forceinline__ void ppr_update(uint32_t st, float& d, float& x, floa
 template <int F>
 __device__ __forceinline__ bool ppr_finish(const BatchArgs& A, const Smem& S, uint32_t v,
                                            const float (&s)[F * 4], float* pv_next,
-                                           uint32_t li, uint32_t L, double (&res)[F * 4]) {
+                                           uint32_t li, uint32_t L, float (&res)[F * 4]) {
   const uint32_t od = A.out_deg[v];
   const float scale = od > 0 ? A.damping / (float)od : 0.f;
   bool any = false;
@@ -227,9 +227,9 @@ __device__ void ppr_activate_all(const BatchArgs& A, Smem& S) {
   const unsigned gmask = L == 32 ? 0xffffffffu : (((1u << L) - 1) << ((lane / L) * L));
   const float zero[F * 4] = {};
   for (uint64_t v = gid; v < A.n; v += ng) {
-    double r[F * 4];
+    float r[F * 4];
 #pragma unroll
-    for (int j = 0; j < F * 4; ++j) r[j] = 0.0;
+    for (int j = 0; j < F * 4; ++j) r[j] = 0.f;
     const bool any = ppr_finish<F>(A, S, (uint32_t)v, zero, A.PV0, li, L, r);
     const unsigned a = __reduce_or_sync(gmask, any ? 1u : 0u);
     if (li == 0) A.act0[v] = (uint8_t)a;
@@ -254,7 +254,7 @@ __device__ void ppr_activate_all(const BatchArgs& A, Smem& S) {
 
 // Pull number p: sums push values over the in-edges of every chunk.
 template <int F>
-__device__ void ppr_pull(const BatchArgs& A, Smem& S, uint32_t p, double (&res)[F * 4]) {
+__device__ void ppr_pull(const BatchArgs& A, Smem& S, uint32_t p, float (&res)[F * 4]) {
   const uint32_t L = min(32u, A.qw / 4);
   const uint32_t G = 32 / L;
   const uint32_t lane = threadIdx.x & 31;
@@ -331,7 +331,7 @@ __device__ void ppr_pull(const BatchArgs& A, Smem& S, uint32_t p, double (&res)[
 
 // Vertices spanning chunks: their sums arrived in ACC.
 template <int F>
-__device__ void ppr_fixup(const BatchArgs& A, Smem& S, uint32_t p, double (&res)[F * 4]) {
+__device__ void ppr_fixup(const BatchArgs& A, Smem& S, uint32_t p, float (&res)[F * 4]) {
   const uint32_t L = min(32u, A.qw / 4);
   const uint32_t G = 32 / L;
   const uint32_t lane = threadIdx.x & 31;
@@ -363,9 +363,10 @@ __device__ void ppr_fixup(const BatchArgs& A, Smem& S, uint32_t p, double (&res)
   }
 }
 
-// Lane-held residuals -> block sums -> one global atomic per query.
+// Lane-held residuals (FP32 sums of the lane's vertices) -> FP64 block sums
+// -> one global atomic per query.
 template <int F>
-__device__ void ppr_flush_res(const BatchArgs& A, Smem& S, double (&res)[F * 4]) {
+__device__ void ppr_flush_res(const BatchArgs& A, Smem& S, float (&res)[F * 4]) {
   const uint32_t L = min(32u, A.qw / 4);
   const uint32_t li = (threadIdx.x & 31) % L;
 #pragma unroll
@@ -374,8 +375,8 @@ __device__ void ppr_flush_res(const BatchArgs& A, Smem& S, double (&res)[F * 4])
     if (qb >= A.qw) continue;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      if (res[f * 4 + j] != 0.0) atomicAdd(&S.qres[qb + j], res[f * 4 + j]);
-      res[f * 4 + j] = 0.0;
+      if (res[f * 4 + j] != 0.f) atomicAdd(&S.qres[qb + j], (double)res[f * 4 + j]);
+      res[f * 4 + j] = 0.f;
     }
   }
   __syncthreads();
@@ -626,9 +627,9 @@ __global__ void __launch_bounds__(BT) k_batch(BatchArgs A) {
     S.qstate[q] = q < A.nq ? A.qstate[q] : Q_DONE;
   }
   __syncthreads();
-  double res[F * 4];
+  float res[F * 4];
 #pragma unroll
-  for (int j = 0; j < F * 4; ++j) res[j] = 0.0;
+  for (int j = 0; j < F * 4; ++j) res[j] = 0.f;
   unsigned long long relax = 0, improve = 0;
   if (A.qw > 0 && __ldcg(A.ctl + B_PULL) == 0 && __ldcg(A.ctl + B_ITER) == 0) {
     // the first activation's residual is not tested (the first pull's is)

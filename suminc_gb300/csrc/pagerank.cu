@@ -69,10 +69,14 @@ struct PrArgs {
   unsigned long long* cnt;
 };
 
-// activation of one vertex with its new delta; returns 1 when active
+// activation of one vertex with its new delta; returns 1 when active.  Each
+// thread sums its vertices' |delta| in FP32; the block, grid and the
+// termination test take those partial sums in FP64 (per-vertex FP64 adds
+// would load GB300's FP64 pipe, which issues at a small fraction of the
+// FP32 rate, once per vertex and round).
 __device__ __forceinline__ uint32_t activate(const PrArgs& A, uint32_t v, float dl, float* pv_next,
-                                             double& res) {
-  res += fabs((double)dl);
+                                             float& res) {
+  res += fabsf(dl);
   const uint32_t r = A.rank ? A.rank[v] : v;
   if (fabsf(dl) > A.thr_v) {
     A.x[v] += dl;
@@ -93,20 +97,18 @@ __device__ __forceinline__ uint32_t activate(const PrArgs& A, uint32_t v, float 
 __global__ void __launch_bounds__(VT) k_pr_vertex(PrArgs A) {
   __shared__ double s_red[VT / 32];
   __shared__ double s_red2[VT / 32];
-  double res = 0.0, res0 = 0.0;
+  float res = 0.f, res0 = 0.f;
   unsigned long long visits = 0;
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < A.n; v += gridDim.x * blockDim.x) {
-    double r = 0.0;
-    visits += activate(A, v, A.delta[v], A.pv0, r);
-    res += r;
+    visits += activate(A, v, A.delta[v], A.pv0, res);
     // vertices without in-edges never change again: their leftover delta is
     // a constant part of every later residual
-    if (A.pull_deg[v] == 0) res0 += fabs((double)A.delta[v]);
+    if (A.pull_deg[v] == 0) res0 += fabsf(A.delta[v]);
     A.pvb[0][v] = 0.f;
     A.pvb[1][v] = 0.f;
   }
-  const double b = block_sum<VT>(res, s_red);
-  const double b0 = block_sum<VT>(res0, s_red2);
+  const double b = block_sum<VT>((double)res, s_red);
+  const double b0 = block_sum<VT>((double)res0, s_red2);
   if (threadIdx.x == 0) {
     atomicAdd(&A.res[R_LAST], b);
     atomicAdd(&A.res[R_ZERO_IN], b0);
@@ -191,7 +193,7 @@ __global__ void __launch_bounds__(HUB ? kHubThreads : PT_THREADS, HUB ? 2 : 8)
   // tiles are 32 quads, so tile indices fit 32 bits for any graph in HBM
   const uint32_t nwarps = (gridDim.x * NT) >> 5;
   const uint32_t ntiles = (uint32_t)P.ntiles;
-  double res = 0.0;
+  float res = 0.f;
   uint32_t visits = 0;
   uint32_t t = (blockIdx.x * NT + threadIdx.x) >> 5;
   uint32_t i0 = t < ntiles ? P.wtile_v0[t] : 0u;
@@ -260,7 +262,7 @@ __global__ void __launch_bounds__(HUB ? kHubThreads : PT_THREADS, HUB ? 2 : 8)
         const float dl = dl_c + tot;
         if (drain) {
           A.delta[v_c] = dl;
-          res += fabs((double)dl);
+          res += fabsf(dl);
         } else {
           visits += activate(A, v_c, dl, pv_next, res);
         }
@@ -270,7 +272,7 @@ __global__ void __launch_bounds__(HUB ? kHubThreads : PT_THREADS, HUB ? 2 : 8)
     }
     i0 = i0_next;
   }
-  const double b = block_sum<NT>(res, s_red);
+  const double b = block_sum<NT>((double)res, s_red);
   if (threadIdx.x == 0 && b != 0.0) atomicAdd(&A.res[R_ACC], b);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) visits += __shfl_down_sync(0xffffffffu, visits, o);
@@ -454,15 +456,15 @@ __global__ void __launch_bounds__(VT) k_pr_fixup(PrArgs A, const uint32_t* __res
   if (A.misc[M_DONE]) return;
   const bool drain = A.misc[M_PENDING] != 0;
   float* pv_next = (p & 1) ? A.pvb[0] : A.pvb[1];
-  double res = 0.0;
+  float res = 0.f;
   unsigned long long visits = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += gridDim.x * blockDim.x) {
     const uint32_t v = bnd[i];
     const float dl = A.delta[v];
-    if (drain) res += fabs((double)dl);
+    if (drain) res += fabsf(dl);
     else visits += activate(A, v, dl, pv_next, res);
   }
-  const double b = block_sum<VT>(res, s_red);
+  const double b = block_sum<VT>((double)res, s_red);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) visits += __shfl_down_sync(0xffffffffu, visits, o);
   if ((threadIdx.x & 31) == 0 && visits) atomicAdd(&A.cnt[C_VISITS], visits);

@@ -86,8 +86,8 @@ struct RepairDev {
   // scratch of the passes (grown on demand)
   uint32_t *jobs = nullptr, *tcl = nullptr, *tc_idx = nullptr, *tc_inner = nullptr;
   uint32_t *sp_cl = nullptr, *sp_src = nullptr;
-  uint32_t *wjobs = nullptr, *bjobs = nullptr;
-  uint8_t *j_warp = nullptr, *j_block = nullptr;
+  uint32_t *wjobs = nullptr, *wjobs5 = nullptr, *bjobs = nullptr;
+  uint8_t *j_warp = nullptr, *j_warp5 = nullptr, *j_block = nullptr;
   uint64_t *lp_off = nullptr, *adj_off = nullptr, *out_off = nullptr, *lin_off = nullptr;
   uint64_t* cl_lin = nullptr;
   uint32_t* adj_nbr = nullptr;
@@ -490,16 +490,17 @@ __global__ void __launch_bounds__(256) k_rp_lin_fill(RepArgs R, const uint32_t* 
 // 11. per job: cluster index, local source, output offset, kernel choice
 __global__ void k_rp_jobs(RepArgs R, const uint32_t* jobs, uint32_t nj, const uint32_t* tc_idx,
                           const uint64_t* blk, uint32_t* sp_cl, uint32_t* sp_src, uint64_t* out_off,
-                          uint8_t* j_warp, uint8_t* j_block) {
+                          uint8_t* j_warp, uint8_t* j_warp5, uint8_t* j_block) {
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nj; j += gridDim.x * blockDim.x) {
     const uint32_t r = jobs[j];
     const uint32_t c = R.cl_of[r];
     sp_cl[j] = tc_idx[c];
     sp_src[j] = R.loc[r];
     out_off[j] = blk[r];
-    const bool small = cl_size(R, c) <= (uint32_t)kStageCap;
-    j_warp[j] = small;
-    j_block[j] = !small;
+    const uint32_t L = cl_size(R, c);
+    j_warp[j] = L <= kShortcutSmallL;
+    j_warp5[j] = L > kShortcutSmallL && L <= (uint32_t)kStageCap;
+    j_block[j] = L > (uint32_t)kStageCap;
   }
 }
 
@@ -920,11 +921,12 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
                                       P.lin_off, P.lin_src);
     SG_CUDA(ctx, cudaMemcpyAsync(P.lin_off + npos, P.cl_lin + ntc, 8, cudaMemcpyDeviceToDevice, st));
     k_rp_jobs<<<grid_for(nj, 256), 256, 0, st>>>(R, P.jobs, nj, P.tc_idx, P.blk2, P.sp_cl, P.sp_src,
-                                                 P.out_off, P.j_warp, P.j_block);
+                                                 P.out_off, P.j_warp, P.j_warp5, P.j_block);
     SG_TRY(select_idx(ctx, P.j_warp, P.wjobs, P.d_num, nj));
     SG_TRY(select_idx(ctx, P.j_block, P.bjobs, P.d_num + 1, nj));
-    uint32_t nwb[2] = {0, 0};
-    SG_CUDA(ctx, cudaMemcpyAsync(nwb, P.d_num, 8, cudaMemcpyDeviceToHost, st));
+    SG_TRY(select_idx(ctx, P.j_warp5, P.wjobs5, P.d_num + 2, nj));
+    uint32_t nwb[3] = {0, 0, 0};
+    SG_CUDA(ctx, cudaMemcpyAsync(nwb, P.d_num, 12, cudaMemcpyDeviceToHost, st));
     SG_CUDA(ctx, cudaStreamSynchronize(st));
     T.mark("local problems");
     ShortcutArgs A;
@@ -947,8 +949,11 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
     kprof_begin(ctx);
     if (nwb[0]) {
       A.jobs = P.wjobs;
-      k_shortcuts_warp<<<grid_for((uint64_t)nwb[0] * 32, 32 * kStageWarps), 32 * kStageWarps, 0, st>>>(
-          A, nwb[0]);
+      launch_shortcuts_warp(2, A, nwb[0], st);
+    }
+    if (nwb[2]) {
+      A.jobs = P.wjobs5;
+      launch_shortcuts_warp(5, A, nwb[2], st);
     }
     if (nwb[1]) {
       const size_t smem = shortcut_smem(P.max_L);
@@ -1132,6 +1137,7 @@ void repair_free(SummaryDev& D) {
   dfree(P->pool.val); dfree(P->pool.del); dfree(P->pool2.val); dfree(P->pool2.del);
   dfree(P->jobs); dfree(P->tcl); dfree(P->tc_idx); dfree(P->tc_inner); dfree(P->sp_cl);
   dfree(P->sp_src); dfree(P->wjobs); dfree(P->bjobs); dfree(P->j_warp); dfree(P->j_block);
+  dfree(P->wjobs5); dfree(P->j_warp5);
   dfree(P->lp_off); dfree(P->adj_off); dfree(P->out_off); dfree(P->lin_off); dfree(P->cl_lin);
   dfree(P->adj_nbr); dfree(P->lin_src); dfree(P->div);
   dfree(P->cnt_a); dfree(P->cnt_b); dfree(P->cnt_c); dfree(P->cnt_d);
@@ -1240,6 +1246,8 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
   SG_TRY(dalloc(ctx, &P.wjobs, all));
   SG_TRY(dalloc(ctx, &P.bjobs, all));
   SG_TRY(dalloc(ctx, &P.j_warp, all));
+  SG_TRY(dalloc(ctx, &P.j_warp5, all));
+  SG_TRY(dalloc(ctx, &P.wjobs5, all));
   SG_TRY(dalloc(ctx, &P.j_block, all));
   SG_TRY(dalloc(ctx, &P.tcl, ncl));
   SG_TRY(dalloc(ctx, &P.tc_idx, ncl));

@@ -135,7 +135,7 @@ static sg_status reupload(sg_ctx* ctx, SummaryDev& D, T** d, const std::vector<T
 // across calls.  Callers synchronise before returning, so a slot is free
 // again at the next call.
 enum StageSlot {
-  ST_WJOBS, ST_BJOBS, ST_LINOFF, ST_LINSRC, ST_SPC, ST_SRC, ST_INNER, ST_ADJ, ST_CLOFF,
+  ST_WJOBS, ST_WJOBS5, ST_BJOBS, ST_LINOFF, ST_LINSRC, ST_SPC, ST_SRC, ST_INNER, ST_ADJ, ST_CLOFF,
   ST_ADJOFF, ST_OUTOFF, ST_DIV, ST_VAL, ST_DEL,
   SS_CL, SS_SRC, SS_NBR, SS_W, SS_CLOFF, SS_ADJOFF, SS_OUTOFF, SS_OUT,
   SI_DALL, SI_SEEDS, SI_CS, SI_CD, SI_S2, SP_DIST, ST_SLOTS
@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njob
     }
     __syncthreads();
   }
-  const double thr = A.thr_per_node * (double)inner;
+  const float thr = f32_at_most(A.thr_per_node * (double)inner);
   for (int step = 1;; ++step) {
     if (threadIdx.x == 0) s_diff = 0.f;
     for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) next[i] = i < inner ? 0.f : delta[i];
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njob
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) delta[i] = next[i];
     __syncthreads();
-    const double d_all = s_diff;
+    const float d_all = s_diff;
     __syncthreads();
     if (d_all <= thr || step > 100) break;
   }
@@ -254,21 +254,22 @@ __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njob
   }
 }
 
-// One warp per supernode job for clusters of at most kStageCap local nodes:
+// One warp per supernode job for clusters of at most 32 x NPL local nodes:
 // the same iteration as k_shortcuts (a unit of delta at the entry, Jacobi
 // steps until the members' delta mass is at most thr x members or 101
 // steps) in two phases per step without atomics: members take their delta
 // and publish delta * d / div, then every node sums the published values
-// of its in-edges from members (mirrors keep what they hold).
+// of its in-edges from members (mirrors keep what they hold).  Lane l owns
+// nodes l, l + 32, ..., and keeps their delta, partial sum, FP64 value,
+// d / div and in-edge range in registers; only the published values go
+// through shared memory.
+template <int NPL>
 __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t njobs) {
-  __shared__ double s_val[kStageWarps][kStageCap];
-  __shared__ float s_part[kStageWarps][kStageCap];
-  __shared__ float s_del[kStageWarps][kStageCap];
-  __shared__ float s_pv[kStageWarps][kStageCap];
-  __shared__ float s_f[kStageWarps][kStageCap];
+  __shared__ float s_pv[kStageWarps][32 * NPL];
   const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   const float d = A.damping;
+  float* pv = s_pv[w];
   for (uint32_t jj = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; jj < njobs; jj += nwarps) {
     const uint32_t s = A.jobs[jj];
     const uint32_t c = A.sp_cluster[s];
@@ -276,64 +277,104 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
     const uint32_t L = (uint32_t)(A.cl_off[c + 1] - l0);
     const uint32_t inner = A.cl_inner[c];
     const uint32_t src = A.sp_src[s];
-    double* val = s_val[w];
-    float* part = s_part[w];
-    float* del = s_del[w];
-    float* pv = s_pv[w];
-    float* f = s_f[w];  // d / out-degree of each node
-    for (uint32_t i = lane; i < L; i += 32) {
-      val[i] = 0.0;
-      part[i] = 0.f;
-      del[i] = (i == src) ? 1.f : 0.f;
-      f[i] = d / A.div[l0 + i];
+    const uint64_t e_base = A.lin_off[l0];
+    float del[NPL], part[NPL], f[NPL];
+    double val[NPL];
+    uint32_t e0[NPL], e1[NPL];
+#pragma unroll
+    for (int t = 0; t < NPL; ++t) {
+      const uint32_t j = lane + 32 * t;
+      val[t] = 0.0;
+      part[t] = 0.f;
+      del[t] = 0.f;
+      f[t] = 0.f;
+      e0[t] = e1[t] = 0;
+      if (j < L) {
+        f[t] = d / A.div[l0 + j];
+        e0[t] = (uint32_t)(A.lin_off[l0 + j] - e_base);
+        e1[t] = (uint32_t)(A.lin_off[l0 + j + 1] - e_base);
+        del[t] = j == src ? 1.f : 0.f;
+      }
     }
-    __syncwarp();
-    // an in-mirror entry first sends its unit along its edges into the cluster
+    // an in-mirror entry first sends its unit along its edges into the
+    // cluster (through shared memory: its targets belong to other lanes)
     if (src >= inner) {
+#pragma unroll
+      for (int t = 0; t < NPL; ++t)
+        if (lane + 32 * t < L) pv[lane + 32 * t] = 0.f;
+      __syncwarp();
       if (lane == 0) {
-        const float outv = f[src];
+        const float outv = d / A.div[l0 + src];
         for (uint64_t e = A.adj_off[l0 + src]; e < A.adj_off[l0 + src + 1]; ++e)
-          del[A.adj_nbr[e]] += outv;
-        val[src] += 1.0;
-        del[src] = 0.f;
+          pv[A.adj_nbr[e]] += outv;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int t = 0; t < NPL; ++t) {
+        const uint32_t j = lane + 32 * t;
+        if (j < L) {
+          if (j == src) {
+            val[t] = 1.0;
+            del[t] = 0.f;
+          } else {
+            del[t] = pv[j];
+          }
+        }
       }
       __syncwarp();
     }
-    const double thr = A.thr_per_node * (double)inner;
+    const float thr = f32_at_most(A.thr_per_node * (double)inner);
+    const uint8_t* ls = A.lin_src + e_base;
     for (int step = 1;; ++step) {
       float diff = 0.f;
       const bool flush = step % kShortcutFlush == 0;
-      for (uint32_t i = lane; i < inner; i += 32) {
-        const float ts = del[i];
-        const float p = part[i] + ts;
-        if (flush) {
-          val[i] += widen_f32(p);
-          part[i] = 0.f;
-        } else {
-          part[i] = p;
+#pragma unroll
+      for (int t = 0; t < NPL; ++t) {
+        const uint32_t j = lane + 32 * t;
+        if (j < inner) {
+          const float ts = del[t];
+          const float p = part[t] + ts;
+          if (flush) {
+            val[t] += widen_f32(p);
+            part[t] = 0.f;
+          } else {
+            part[t] = p;
+          }
+          diff += fabsf(ts);
+          pv[j] = ts * f[t];
         }
-        diff += fabsf(ts);
-        pv[i] = ts * f[i];
       }
       __syncwarp();
-      for (uint32_t j = lane; j < L; j += 32) {
-        float acc = 0.f;
-        const uint64_t f1 = A.lin_off[l0 + j + 1];
-        for (uint64_t q = A.lin_off[l0 + j]; q < f1; ++q) acc += pv[A.lin_src[q]];
-        del[j] = (j < inner ? 0.f : del[j]) + acc;
+#pragma unroll
+      for (int t = 0; t < NPL; ++t) {
+        const uint32_t j = lane + 32 * t;
+        if (j < L) {
+          float acc = 0.f;
+          for (uint32_t e = e0[t]; e < e1[t]; ++e) acc += pv[ls[e]];
+          del[t] = (j < inner ? 0.f : del[t]) + acc;
+        }
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) diff += __shfl_xor_sync(0xffffffffu, diff, o);
       __syncwarp();
-      if ((double)diff <= thr || step > 100) break;
+      if (diff <= thr || step > 100) break;
     }
     const uint64_t o = A.out_off[s];
-    for (uint32_t i = lane; i < L; i += 32) {
-      A.out_value[o + i] = i < inner ? val[i] + widen_f32(part[i]) : val[i];
-      A.out_delta[o + i] = (double)del[i];
+#pragma unroll
+    for (int t = 0; t < NPL; ++t) {
+      const uint32_t j = lane + 32 * t;
+      if (j < L) {
+        A.out_value[o + j] = j < inner ? val[t] + widen_f32(part[t]) : val[t];
+        A.out_delta[o + j] = (double)del[t];
+      }
     }
     __syncwarp();
   }
+}
+void launch_shortcuts_warp(int npl, ShortcutArgs A, uint32_t njobs, cudaStream_t st) {
+  const unsigned grid = grid_for((uint64_t)njobs * 32, 32 * kStageWarps);
+  if (npl == 2) k_shortcuts_warp<2><<<grid, 32 * kStageWarps, 0, st>>>(A, njobs);
+  else k_shortcuts_warp<5><<<grid, 32 * kStageWarps, 0, st>>>(A, njobs);
 }
 
 // Builds the local problems of the given supernodes, runs the kernel and
@@ -442,13 +483,15 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
         lin_src[cl_lin[k] + cnt[adj_nbr[e]]++] = (uint8_t)i;
   }
   lin_off[cl_off[ncl]] = cl_lin[ncl];
-  std::vector<uint32_t> warp_jobs, block_jobs;
+  std::vector<uint32_t> warp_jobs, warp_jobs5, block_jobs;
   size_t maxL_block = 1;
   for (size_t j = 0; j < spids.size(); ++j) {
     const uint32_t k = sp_cluster[j];
     const uint64_t L = cl_off[k + 1] - cl_off[k];
-    if (L <= (uint64_t)kStageCap) {
+    if (L <= (uint64_t)kShortcutSmallL) {
       warp_jobs.push_back((uint32_t)j);
+    } else if (L <= (uint64_t)kStageCap) {
+      warp_jobs5.push_back((uint32_t)j);
     } else {
       block_jobs.push_back((uint32_t)j);
       maxL_block = std::max<size_t>(maxL_block, L);
@@ -464,7 +507,9 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
   uint32_t *d_wjobs = nullptr, *d_bjobs = nullptr;
   uint64_t* d_linoff = nullptr;
   uint8_t* d_linsrc = nullptr;
+  uint32_t* d_wjobs5 = nullptr;
   SG_TRY(stage_up(ctx, D, ST_WJOBS, warp_jobs, &d_wjobs));
+  SG_TRY(stage_up(ctx, D, ST_WJOBS5, warp_jobs5, &d_wjobs5));
   SG_TRY(stage_up(ctx, D, ST_BJOBS, block_jobs, &d_bjobs));
   SG_TRY(stage_up(ctx, D, ST_LINOFF, lin_off, &d_linoff));
   SG_TRY(stage_up(ctx, D, ST_LINSRC, lin_src, &d_linsrc));
@@ -500,8 +545,11 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
   kprof_begin(ctx);
   if (!warp_jobs.empty()) {
     A.jobs = d_wjobs;
-    k_shortcuts_warp<<<grid_for((uint64_t)warp_jobs.size() * 32, 32 * kStageWarps), 32 * kStageWarps,
-                       0, ctx->stream>>>(A, (uint32_t)warp_jobs.size());
+    launch_shortcuts_warp(2, A, (uint32_t)warp_jobs.size(), ctx->stream);
+  }
+  if (!warp_jobs5.empty()) {
+    A.jobs = d_wjobs5;
+    launch_shortcuts_warp(5, A, (uint32_t)warp_jobs5.size(), ctx->stream);
   }
   if (!block_jobs.empty()) {
     A.jobs = d_bjobs;
@@ -936,10 +984,10 @@ __global__ void __launch_bounds__(256) k_sum_residual_decide(SumArgs A, uint32_t
   __shared__ double s_red[8];
   __shared__ bool s_last;
   if (rounds_done(A)) return;
-  double r = 0.0;
+  float r = 0.f;  // the thread's vertices in FP32, the block and grid sums in FP64
   for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
-    r += fabs((double)A.delta[v]);
-  const double b = block_sum<256>(r, s_red);
+    r += fabsf(A.delta[v]);
+  const double b = block_sum<256>((double)r, s_red);
   if (threadIdx.x == 0) {
     if (b != 0.0) atomicAdd(A.sres, b);
     __threadfence();
@@ -981,7 +1029,8 @@ __global__ void __launch_bounds__(256) k_sum_correct(SumArgs A, uint32_t all_n, 
 
 // Cluster-local convergence of the current deltas (the precompute of
 // iter_compressor.h:534-785: local iteration of each supernode until its delta
-// mass falls under the per-vertex threshold times its size, at most 100 steps).
+// mass, a float sum as the reference's Diff, falls under the per-vertex
+// threshold times its size, at most 100 steps).
 // One warp per cluster.  A cluster of up to kStageCap members and
 // kStageEdges local edges is staged in shared memory and iterated in two
 // phases per step with no atomics inside the cluster: each member takes its
@@ -1008,7 +1057,7 @@ __global__ void __launch_bounds__(256) k_sum_precompute(SumArgs A, const uint32_
     const uint32_t c = clusters[k];
     const uint64_t b = cm_off[c], e = cm_off[c + 1];
     const uint32_t m = (uint32_t)(e - b);
-    const double thr = thr_v * (double)m;
+    const float thr = f32_at_most(thr_v * (double)m);  // the reference's float Diff
     const uint64_t l0 = L.lin_off[b], nl = L.lin_off[e] - l0;
     if (m <= (uint32_t)kStageCap && nl <= (uint64_t)kStageEdges) {
       for (uint32_t i = lane; i < m; i += 32) {
@@ -1022,14 +1071,14 @@ __global__ void __launch_bounds__(256) k_sum_precompute(SumArgs A, const uint32_
       for (uint32_t j = lane; j < (uint32_t)nl; j += 32) s_ls[w][j] = L.lin_src[l0 + j];
       __syncwarp();
       for (int step = 1;; ++step) {
-        double diff = 0.0;
+        float diff = 0.f;
         for (uint32_t i = lane; i < m; i += 32) {
           const float ts = s_d[w][i];
           float pv = 0.f;
           if (ts != 0.f) {
             s_d[w][i] = 0.f;
             s_x[w][i] += ts;
-            diff += fabs((double)ts);
+            diff += fabsf(ts);
             pv = ts * A.damping / s_deg[w][i];
             for (uint64_t f = L.lout_off[b + i]; f < L.lout_off[b + i + 1]; ++f)
               atomicAdd(&A.delta[L.lout_dst[f]], pv);
@@ -1056,13 +1105,13 @@ __global__ void __launch_bounds__(256) k_sum_precompute(SumArgs A, const uint32_
       continue;
     }
     for (int step = 1;; ++step) {
-      double diff = 0.0;
+      float diff = 0.f;
       for (uint64_t i = b + lane; i < e; i += 32) {
         const uint32_t v = cm_v[i];
         const float ts = atomicExch(&A.delta[v], 0.f);
         if (ts == 0.f) continue;
         A.x[v] += ts;
-        diff += fabs((double)ts);
+        diff += fabsf(ts);
         const float outv = ts * A.damping / (float)A.out_deg_all[v];
         for (uint64_t f = sub_off[i]; f < sub_off[i + 1]; ++f) atomicAdd(&A.delta[sub_nbr[f]], outv);
       }

@@ -73,6 +73,17 @@ __device__ __forceinline__ double widen_f32(float f) {
   return __longlong_as_double((long long)bits);
 }
 
+// The largest float not above a non-negative double threshold t: for any
+// float x, x <= f32_at_most(t) exactly when (double)x <= t.  Lets a loop
+// test its FP32 step mass against an FP64 threshold with one FP32 compare
+// (positive floats are ordered like their bit patterns, so the next float
+// below is the pattern minus one).
+__device__ __forceinline__ float f32_at_most(double t) {
+  float f = __double2float_rn(t);
+  if ((double)f > t) f = __uint_as_float(__float_as_uint(f) - 1u);
+  return f;
+}
+
 // Cluster-local shortcut solves (summary.cu): one job per supernode, the
 // cluster's nodes as local indices and its edges as a local CSR.
 struct ShortcutArgs {
@@ -97,7 +108,9 @@ struct ShortcutArgs {
 __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njobs);
 // dynamic shared memory of k_shortcuts for a cluster of L nodes
 inline size_t shortcut_smem(size_t L) { return L * (sizeof(double) + 3 * sizeof(float)); }
-__global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t njobs);
+// a warp per job for clusters of at most 32 x npl nodes (npl = 2 or 5)
+void launch_shortcuts_warp(int npl, ShortcutArgs A, uint32_t njobs, cudaStream_t st);
+constexpr uint32_t kShortcutSmallL = 64;  // clusters the npl = 2 variant takes
 
 struct SummaryDev {
   bool valid = false;
