@@ -83,6 +83,20 @@ struct RepairDev {
   uint64_t *blk = nullptr, *blk2 = nullptr;
   Pool pool, pool2;
   uint64_t n_members = 0;       // members over all clusters (cm layout positions)
+  // SSSP over the summary (after its first query): distance blocks in the
+  // layout of the PageRank blocks, the weights of the ib rows, and whether
+  // the summarized CSR needs a rebuild
+  bool sssp_on = false, sk_stale = true;
+  double *sd = nullptr, *sd2 = nullptr;
+  uint64_t sd_cap = 0, sd2_cap = 0;
+  float* ib_w = nullptr;
+  uint64_t ib_w_cap = 0;
+  uint8_t* f_corr = nullptr;       // [all_n] rows with correction entries
+  uint32_t *im_list = nullptr, *im_master = nullptr;  // every in-mirror and its master
+  uint32_t n_im_total = 0;
+  double* src_dist = nullptr;      // the source cluster's local distances
+  uint32_t *seed_v = nullptr, *seed_n = nullptr;
+  double* seed_d = nullptr;
   // scratch of the passes (grown on demand)
   uint32_t *jobs = nullptr, *tcl = nullptr, *tc_idx = nullptr, *tc_inner = nullptr;
   uint32_t *sp_cl = nullptr, *sp_src = nullptr;
@@ -91,6 +105,8 @@ struct RepairDev {
   uint64_t *lp_off = nullptr, *adj_off = nullptr, *out_off = nullptr, *lin_off = nullptr;
   uint64_t* cl_lin = nullptr;
   uint32_t* adj_nbr = nullptr;
+  float* adj_w = nullptr;
+  uint64_t cap_adjw = 0;
   uint8_t* lin_src = nullptr;
   float* div = nullptr;
   uint64_t *cnt_a = nullptr, *cnt_b = nullptr, *cnt_c = nullptr, *cnt_d = nullptr;
@@ -188,6 +204,7 @@ struct RepArgs {
   uint8_t *m_src, *m_ret, *m_new, *c_src, *c_upd, *c_job, *c_pend, *r_job;
   const uint64_t *out_off, *in_off;  // the graph's two directions (live prefix of each row)
   const uint32_t *out_deg, *in_deg, *out_col, *in_col;
+  const float* out_w;                // edge weights (null: unweighted)
 };
 
 __device__ __forceinline__ uint32_t cl_size(const RepArgs& R, uint32_t c) {
@@ -372,7 +389,7 @@ __global__ void k_rp_tcl(RepArgs R, const uint32_t* tcl, uint32_t ntc, uint32_t*
 // into the cluster; none for out-mirrors (build_subgraph_mirror)
 template <bool FILL>
 __device__ __forceinline__ uint32_t local_edges(const RepArgs& R, uint32_t c, uint32_t i,
-                                                uint32_t* out) {
+                                                uint32_t* out, float* wout = nullptr) {
   const uint32_t inner = R.inner[c];
   const uint32_t node = R.cn[R.cn_off[c] + i];
   uint32_t k = 0;
@@ -390,7 +407,10 @@ __device__ __forceinline__ uint32_t local_edges(const RepArgs& R, uint32_t c, ui
         if (m != kNone && !im_of(R, ct, node)) l = R.loc[m];
       }
       if (l != kNone) {
-        if (FILL) out[k] = l;
+        if (FILL) {
+          out[k] = l;
+          if (wout) wout[k] = R.out_w[b + e];
+        }
         ++k;
       }
     }
@@ -401,7 +421,10 @@ __device__ __forceinline__ uint32_t local_edges(const RepArgs& R, uint32_t c, ui
     for (uint32_t e = 0; e < d; ++e) {
       const uint32_t t = R.out_col[b + e];
       if (R.cl_of[t] == c) {
-        if (FILL) out[k] = R.loc[t];
+        if (FILL) {
+          out[k] = R.loc[t];
+          if (wout) wout[k] = R.out_w[b + e];
+        }
         ++k;
       }
     }
@@ -424,7 +447,7 @@ __global__ void __launch_bounds__(256) k_rp_lp_count(RepArgs R, const uint32_t* 
 // 8. per touched cluster (warp): local edges and divisors
 __global__ void __launch_bounds__(256) k_rp_lp_fill(RepArgs R, const uint32_t* tcl, uint32_t ntc,
                                                     const uint64_t* lp_off, const uint64_t* adj_off,
-                                                    uint32_t* adj_nbr, float* div) {
+                                                    uint32_t* adj_nbr, float* adj_w, float* div) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < ntc; k += nw) {
@@ -432,7 +455,7 @@ __global__ void __launch_bounds__(256) k_rp_lp_fill(RepArgs R, const uint32_t* t
     const uint32_t L = cl_size(R, c);
     for (uint32_t i = lane; i < L; i += 32) {
       const uint64_t p = lp_off[k] + i;
-      local_edges<true>(R, c, i, adj_nbr + adj_off[p]);
+      local_edges<true>(R, c, i, adj_nbr + adj_off[p], adj_w ? adj_w + adj_off[p] : nullptr);
       const uint32_t node = R.cn[R.cn_off[c] + i];
       const uint32_t mst = node < R.n ? node : R.master[node - R.n];
       div[p] = (float)max(R.out_deg[mst], 1u);
@@ -526,6 +549,100 @@ __global__ void __launch_bounds__(256) k_rp_move(RepArgs R, const uint32_t* sp_r
       val2[t + i] = val[s + i];
       del2[t + i] = del[s + i];
     }
+  }
+}
+
+// SSSP over the summary.  Rows of the summarized CSR (sketch2csr's traversal
+// form): a master's 0-weight edges to its in-mirrors (clusters in order),
+// then a supernode row's bound shortcuts (exits, and out-mirrors as their
+// masters, at their local distance), then a row's boundary edges; rows are
+// padded to quads.  Correction entries: a supernode's inner members at a
+// finite distance.
+struct SkArgs {
+  const uint64_t* blk;
+  const double* sd;
+  const uint64_t* ib_off;
+  const uint32_t* ib_nbr;
+  const float* ib_w;
+  uint32_t* deg;      // count pass
+  uint64_t* pad;
+  uint64_t* ccnt;
+  uint8_t* fcorr;
+  const uint64_t* off;  // fill pass
+  uint32_t* col;
+  float* w;
+  const uint64_t* coff;
+  uint32_t* cv;
+  float* cd;
+};
+
+template <bool FILL>
+__global__ void k_rp_sketch(RepArgs R, SkArgs K) {
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < R.all_n; r += gridDim.x * blockDim.x) {
+    uint64_t k = FILL ? K.off[r] : 0, kc = FILL ? K.coff[r] : 0;
+    uint32_t ne = 0, nc = 0;
+    if (r < R.n)
+      for (uint64_t q = R.vim_off[r]; q < R.vim_off[r + 1]; ++q, ++ne)
+        if (FILL) {
+          K.col[k] = R.vim[q];
+          K.w[k++] = 0.f;
+        }
+    const uint32_t c = R.cl_of[r];
+    if (is_sp_row(R, r, c)) {
+      const uint32_t L = cl_size(R, c), inner = R.inner[c], om0 = inner + R.n_im[c];
+      const uint64_t b = K.blk[r], n0 = R.cn_off[c];
+      for (uint32_t i = 0; i < L; ++i) {
+        const double d = K.sd[b + i];
+        if (!isfinite(d)) continue;  // unreached inside the cluster
+        const uint32_t node = R.cn[n0 + i];
+        if (i < inner && !R.ob[node]) {
+          if (FILL) {
+            K.cv[kc] = node;
+            K.cd[kc++] = (float)d;
+          }
+          ++nc;
+        } else if (i < inner || i >= om0) {
+          if (FILL) {
+            K.col[k] = i < inner ? node : R.master[node - R.n];
+            K.w[k++] = (float)d;
+          }
+          ++ne;
+        }
+      }
+    }
+    if (r < R.n)
+      for (uint64_t e = K.ib_off[r]; e < K.ib_off[r + 1]; ++e, ++ne)
+        if (FILL) {
+          K.col[k] = K.ib_nbr[e];
+          K.w[k++] = K.ib_w ? K.ib_w[e] : 1.f;
+        }
+    if (!FILL) {
+      K.deg[r] = ne;
+      K.pad[r] = (ne + 3u) & ~3u;
+      K.ccnt[r] = nc;
+      K.fcorr[r] = nc != 0;
+    }
+  }
+}
+
+__global__ void k_rp_gather_off(const uint32_t* rows, uint32_t nrows, const uint64_t* off_row,
+                                uint64_t total, uint64_t* out) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k <= nrows; k += gridDim.x * blockDim.x)
+    out[k] = k < nrows ? off_row[rows[k]] : total;
+}
+
+// seeds of the source's cluster from its local distances
+__global__ void k_rp_seeds(RepArgs R, uint32_t c, const double* dist, uint32_t* sv, double* sdist,
+                           uint32_t* count) {
+  const uint32_t L = cl_size(R, c), inner = R.inner[c], om0 = inner + R.n_im[c];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < L; i += gridDim.x * blockDim.x) {
+    const double d = dist[i];
+    if (!isfinite(d)) continue;
+    if (i >= inner && i < om0) continue;  // in-mirrors do not seed
+    const uint32_t node = R.cn[R.cn_off[c] + i];
+    const uint32_t p = atomicAdd(count, 1u);
+    sv[p] = i < inner ? node : R.master[node - R.n];
+    sdist[p] = d;
   }
 }
 
@@ -632,7 +749,7 @@ __device__ __forceinline__ int ib_mode(uint8_t t) {
 // counts are cleared before
 template <bool FILL>
 __global__ void k_rp_ib(RepArgs R, const uint8_t* ntype, const uint32_t* rows, uint32_t nrows,
-                        uint64_t* cnt, const uint64_t* off, uint32_t* nbr) {
+                        uint64_t* cnt, const uint64_t* off, uint32_t* nbr, float* wout) {
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nrows; q += gridDim.x * blockDim.x) {
     const uint32_t r = rows[q];
     const int mode = r < R.n ? ib_mode(ntype[r]) : 0;
@@ -643,7 +760,10 @@ __global__ void k_rp_ib(RepArgs R, const uint8_t* ntype, const uint32_t* rows, u
       for (uint32_t e = 0; e < d; ++e) {
         const uint32_t x = R.out_col[b + e];
         if (mode == 2 || ib_take(R, r, x)) {
-          if (FILL) nbr[k] = x;
+          if (FILL) {
+            nbr[k] = x;
+            if (wout) wout[k] = R.out_w[b + e];
+          }
           ++k;
         }
       }
@@ -871,11 +991,66 @@ RepArgs rep_args(sg_ctx* ctx, RepairDev& P) {
   const DevGraph& g = ctx->g;
   R.out_off = g.out.off; R.out_deg = g.out.deg; R.out_col = g.out.col;
   R.in_off = g.in.off; R.in_deg = g.in.deg; R.in_col = g.in.col;
+  R.out_w = g.out.w;
   return R;
 }
 
 // Solves again the supernode rows marked in r_job (r_size holds every row's
 // block size) into the next pool layout and moves the other blocks there.
+// Local problems of the ntc clusters listed in P.tcl: their node ranges
+// (lp_off), local edges (adj_off / adj_nbr, with weights when the graph has
+// them), divisors, and for the clusters of at most kStageCap nodes the
+// in-edges from members (lin_off / lin_src).
+sg_status rp_local_problems(sg_ctx* ctx, RepairDev& P, const RepArgs& R, uint32_t ntc,
+                            uint64_t* npos_out) {
+  cudaStream_t st = ctx->stream;
+  k_rp_tcl<<<grid_for(ntc, 256), 256, 0, st>>>(R, P.tcl, ntc, P.tc_idx, P.tc_inner, P.cnt_a);
+  SG_TRY(scan_u64(ctx, P.cnt_a, P.lp_off, (uint64_t)ntc + 1));
+  uint64_t npos = 0;
+  SG_TRY(read_u64(ctx, P.lp_off + ntc, &npos));
+  SG_TRY(grow(ctx, &P.adj_off, &P.cap_lp, npos + 1));
+  SG_TRY(grow(ctx, &P.div, &P.cap_div, npos + 1));
+  SG_TRY(grow(ctx, &P.lin_off, &P.cap_linoff, npos + 1));
+  SG_TRY(grow(ctx, &P.cnt_d, &P.cap_cntd, npos + 1));
+  const unsigned wg = grid_for((uint64_t)ntc * 32, 256);
+  k_rp_lp_count<<<wg, 256, 0, st>>>(R, P.tcl, ntc, P.lp_off, P.cnt_d);
+  SG_TRY(scan_u64(ctx, P.cnt_d, P.adj_off, npos + 1));
+  uint64_t nadj = 0;
+  SG_TRY(read_u64(ctx, P.adj_off + npos, &nadj));
+  SG_TRY(grow(ctx, &P.adj_nbr, &P.cap_adj, nadj));
+  if (R.out_w) SG_TRY(grow(ctx, &P.adj_w, &P.cap_adjw, nadj));
+  k_rp_lp_fill<<<wg, 256, 0, st>>>(R, P.tcl, ntc, P.lp_off, P.adj_off, P.adj_nbr,
+                                   R.out_w ? P.adj_w : nullptr, P.div);
+  k_rp_lin_count<<<grid_for(ntc, 256), 256, 0, st>>>(R, P.tcl, ntc, P.lp_off, P.adj_off, P.cnt_a);
+  SG_TRY(scan_u64(ctx, P.cnt_a, P.cl_lin, (uint64_t)ntc + 1));
+  uint64_t nlin = 0;
+  SG_TRY(read_u64(ctx, P.cl_lin + ntc, &nlin));
+  SG_TRY(grow(ctx, &P.lin_src, &P.cap_lin, nlin));
+  k_rp_lin_fill<<<wg, 256, 0, st>>>(R, P.tcl, ntc, P.lp_off, P.adj_off, P.adj_nbr, P.cl_lin,
+                                    P.lin_off, P.lin_src);
+  SG_CUDA(ctx, cudaMemcpyAsync(P.lin_off + npos, P.cl_lin + ntc, 8, cudaMemcpyDeviceToDevice, st));
+  count_launch(ctx, 9);
+  *npos_out = npos;
+  return SG_OK;
+}
+
+// SSSP distances inside the listed jobs' clusters (Bellman-Ford in shared
+// memory, a CTA per job) into out at the jobs' offsets
+sg_status rp_sssp_solve(sg_ctx* ctx, RepairDev& P, uint32_t nj, const uint64_t* out_off, double* out) {
+  const size_t smem = (size_t)P.max_L * sizeof(unsigned long long);
+  if (smem > 48 * 1024)
+    SG_CUDA(ctx, cudaFuncSetAttribute(k_sssp_shortcuts, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  k_sssp_shortcuts<<<nj, 128, smem, ctx->stream>>>(P.sp_cl, P.sp_src, P.lp_off, P.adj_off, P.adj_nbr,
+                                                   P.adj_w, out_off, out, nj);
+  count_launch(ctx);
+  SG_CUDA(ctx, cudaGetLastError());
+  return SG_OK;
+}
+
+// Solves again the supernode rows marked in r_job (r_size holds every row's
+// block size) into the next pool layout and moves the other blocks there
+// (the SSSP distance blocks too, once SSSP over the summary has run).
 sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, PhaseTrace& T) {
   cudaStream_t st = ctx->stream;
   const uint32_t all = P.all_n;
@@ -883,6 +1058,7 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
   uint64_t total = 0;
   SG_TRY(read_u64(ctx, P.blk2 + all, &total));
   SG_TRY(grow_pool(ctx, &P.pool2, total));
+  if (P.sssp_on) SG_TRY(grow(ctx, &P.sd2, &P.sd2_cap, total));
   SG_TRY(select_idx(ctx, P.r_job, P.jobs, P.d_num, all));
   SG_TRY(select_idx(ctx, P.f_sp, P.sp_rows, P.d_num + 1, all));
   uint32_t nj_sp[2] = {0, 0};
@@ -897,29 +1073,8 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
     uint32_t ntc = 0;
     SG_CUDA(ctx, cudaMemcpyAsync(&ntc, P.d_num, 4, cudaMemcpyDeviceToHost, st));
     SG_CUDA(ctx, cudaStreamSynchronize(st));
-    k_rp_tcl<<<grid_for(ntc, 256), 256, 0, st>>>(R, P.tcl, ntc, P.tc_idx, P.tc_inner, P.cnt_a);
-    SG_TRY(scan_u64(ctx, P.cnt_a, P.lp_off, (uint64_t)ntc + 1));
     uint64_t npos = 0;
-    SG_TRY(read_u64(ctx, P.lp_off + ntc, &npos));
-    SG_TRY(grow(ctx, &P.adj_off, &P.cap_lp, npos + 1));
-    SG_TRY(grow(ctx, &P.div, &P.cap_div, npos + 1));
-    SG_TRY(grow(ctx, &P.lin_off, &P.cap_linoff, npos + 1));
-    SG_TRY(grow(ctx, &P.cnt_d, &P.cap_cntd, npos + 1));
-    const unsigned wg = grid_for((uint64_t)ntc * 32, 256);
-    k_rp_lp_count<<<wg, 256, 0, st>>>(R, P.tcl, ntc, P.lp_off, P.cnt_d);
-    SG_TRY(scan_u64(ctx, P.cnt_d, P.adj_off, npos + 1));
-    uint64_t nadj = 0;
-    SG_TRY(read_u64(ctx, P.adj_off + npos, &nadj));
-    SG_TRY(grow(ctx, &P.adj_nbr, &P.cap_adj, nadj));
-    k_rp_lp_fill<<<wg, 256, 0, st>>>(R, P.tcl, ntc, P.lp_off, P.adj_off, P.adj_nbr, P.div);
-    k_rp_lin_count<<<grid_for(ntc, 256), 256, 0, st>>>(R, P.tcl, ntc, P.lp_off, P.adj_off, P.cnt_a);
-    SG_TRY(scan_u64(ctx, P.cnt_a, P.cl_lin, (uint64_t)ntc + 1));
-    uint64_t nlin = 0;
-    SG_TRY(read_u64(ctx, P.cl_lin + ntc, &nlin));
-    SG_TRY(grow(ctx, &P.lin_src, &P.cap_lin, nlin));
-    k_rp_lin_fill<<<wg, 256, 0, st>>>(R, P.tcl, ntc, P.lp_off, P.adj_off, P.adj_nbr, P.cl_lin,
-                                      P.lin_off, P.lin_src);
-    SG_CUDA(ctx, cudaMemcpyAsync(P.lin_off + npos, P.cl_lin + ntc, 8, cudaMemcpyDeviceToDevice, st));
+    SG_TRY(rp_local_problems(ctx, P, R, ntc, &npos));
     k_rp_jobs<<<grid_for(nj, 256), 256, 0, st>>>(R, P.jobs, nj, P.tc_idx, P.blk2, P.sp_cl, P.sp_src,
                                                  P.out_off, P.j_warp, P.j_warp5, P.j_block);
     SG_TRY(select_idx(ctx, P.j_warp, P.wjobs, P.d_num, nj));
@@ -934,7 +1089,7 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
     A.sp_cluster = P.sp_cl;
     A.sp_src = P.sp_src;
     A.cl_off = P.lp_off;
-    A.cl_inner = nullptr;
+    A.cl_inner = P.tc_inner;  // members per touched cluster, by its index
     A.adj_off = P.adj_off;
     A.adj_nbr = P.adj_nbr;
     A.div = P.div;
@@ -945,7 +1100,6 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
     A.thr_per_node = ctx->opt.termcheck_threshold / (double)P.n;
     A.lin_off = P.lin_off;
     A.lin_src = P.lin_src;
-    A.cl_inner = P.tc_inner;  // members per touched cluster, by its index
     kprof_begin(ctx);
     if (nwb[0]) {
       A.jobs = P.wjobs;
@@ -964,16 +1118,26 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
       k_shortcuts<<<nwb[1], 128, smem, st>>>(A, nwb[1]);
     }
     kprof_end(ctx, SG_K_SUMMARY);
-    count_launch(ctx, 12);
+    count_launch(ctx, 4);
     T.mark("shortcut kernels", st);
+    if (P.sssp_on) {
+      SG_TRY(rp_sssp_solve(ctx, P, nj, P.out_off, P.sd2));
+      T.mark("SSSP shortcut distances", st);
+    }
   }
   k_rp_move<<<grid_for((uint64_t)P.n_sp * 32, 256), 256, 0, st>>>(
       R, P.sp_rows, P.n_sp, P.r_size, P.blk, P.blk2, P.pool.val, P.pool.del, P.pool2.val,
       P.pool2.del, P.d_err);
-  count_launch(ctx);
+  if (P.sssp_on)
+    k_rp_move<<<grid_for((uint64_t)P.n_sp * 32, 256), 256, 0, st>>>(
+        R, P.sp_rows, P.n_sp, P.r_size, P.blk, P.blk2, P.sd, P.sd, P.sd2, P.sd2, P.d_err);
+  count_launch(ctx, 1 + P.sssp_on);
   SG_CUDA(ctx, cudaGetLastError());
   std::swap(P.blk, P.blk2);
   std::swap(P.pool, P.pool2);
+  std::swap(P.sd, P.sd2);
+  std::swap(P.sd_cap, P.sd2_cap);
+  P.sk_stale = true;
   T.mark("blocks moved", st);
   (void)D;
   return SG_OK;
@@ -1027,10 +1191,10 @@ sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, 
   SG_TRY(scan_u64(ctx, P.cnt_c, D.id_off, (uint64_t)all + 1));
   if (D.n_exit)
     k_rp_ib<false><<<grid_for(D.n_exit, 256), 256, 0, st>>>(R, D.ntype, D.l_exit, D.n_exit, P.cnt_d,
-                                                            nullptr, nullptr);
+                                                            nullptr, nullptr, nullptr);
   if (D.n_single)
     k_rp_ib<false><<<grid_for(D.n_single, 256), 256, 0, st>>>(R, D.ntype, D.l_single, D.n_single,
-                                                              P.cnt_d, nullptr, nullptr);
+                                                              P.cnt_d, nullptr, nullptr, nullptr);
   SG_TRY(scan_u64(ctx, P.cnt_d, D.ib_off, (uint64_t)all + 1));
   uint64_t tot[4] = {0, 0, 0, 0};
   SG_CUDA(ctx, cudaMemcpyAsync(&tot[0], D.is_off + all, 8, cudaMemcpyDeviceToHost, st));
@@ -1055,12 +1219,17 @@ sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, 
   T.id_nbr = D.id_nbr;
   T.id_w = D.id_w;
   k_rp_tables<true><<<rg, 256, 0, st>>>(R, T, P.sp_rows, P.n_sp);
+  float* ibw = nullptr;
+  if (R.out_w) {
+    SG_TRY(grow(ctx, &P.ib_w, &P.ib_w_cap, tot[3]));
+    ibw = P.ib_w;
+  }
   if (D.n_exit)
     k_rp_ib<true><<<grid_for(D.n_exit, 256), 256, 0, st>>>(R, D.ntype, D.l_exit, D.n_exit, nullptr,
-                                                           D.ib_off, D.ib_nbr);
+                                                           D.ib_off, D.ib_nbr, ibw);
   if (D.n_single)
     k_rp_ib<true><<<grid_for(D.n_single, 256), 256, 0, st>>>(R, D.ntype, D.l_single, D.n_single,
-                                                             nullptr, D.ib_off, D.ib_nbr);
+                                                             nullptr, D.ib_off, D.ib_nbr, ibw);
   PT.mark("supernode lists and ib rows", st);
   // cluster precompute lists
   CmArgs C{};
@@ -1133,7 +1302,9 @@ void repair_free(SummaryDev& D) {
   dfree(P->c_src); dfree(P->c_upd); dfree(P->c_job); dfree(P->c_pend); dfree(P->r_job);
   dfree(P->f_entry); dfree(P->f_exit); dfree(P->f_single); dfree(P->r_size);
   dfree(P->f_sp); dfree(P->sp_rows);
-  dfree(P->blk); dfree(P->blk2);
+  dfree(P->blk); dfree(P->blk2); dfree(P->sd); dfree(P->sd2); dfree(P->ib_w); dfree(P->adj_w);
+  dfree(P->f_corr); dfree(P->im_list); dfree(P->im_master); dfree(P->src_dist);
+  dfree(P->seed_v); dfree(P->seed_n); dfree(P->seed_d);
   dfree(P->pool.val); dfree(P->pool.del); dfree(P->pool2.val); dfree(P->pool2.del);
   dfree(P->jobs); dfree(P->tcl); dfree(P->tc_idx); dfree(P->tc_inner); dfree(P->sp_cl);
   dfree(P->sp_src); dfree(P->wjobs); dfree(P->bjobs); dfree(P->j_warp); dfree(P->j_block);
@@ -1221,6 +1392,17 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
   SG_TRY(put(ctx, &P.vom, vom));
   SG_TRY(put(ctx, &P.fc, fc));
   SG_TRY(put(ctx, &P.ob, ob));
+  {
+    std::vector<uint32_t> iml, imm;
+    for (uint32_t c = 0; c < ncl; ++c)
+      for (uint32_t m : S.cluster_in_mirror_ids[c]) {
+        iml.push_back(m);
+        imm.push_back(S.mirror_master(m));
+      }
+    P.n_im_total = (uint32_t)iml.size();
+    SG_TRY(put(ctx, &P.im_list, iml));
+    SG_TRY(put(ctx, &P.im_master, imm));
+  }
   P.n_nodes = cn.size();
   // marks and fixed-size scratch
   SG_TRY(dalloc(ctx, &P.m_src, n));
@@ -1235,6 +1417,11 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
   SG_TRY(dalloc(ctx, &P.c_pend, ncl));
   SG_TRY(dalloc(ctx, &P.r_job, all));
   SG_TRY(dalloc(ctx, &P.f_sp, all));
+  SG_TRY(dalloc(ctx, &P.f_corr, all));
+  SG_TRY(dalloc(ctx, &P.src_dist, std::max<uint32_t>(P.max_L, 1)));
+  SG_TRY(dalloc(ctx, &P.seed_v, std::max<uint32_t>(P.max_L, 1)));
+  SG_TRY(dalloc(ctx, &P.seed_d, std::max<uint32_t>(P.max_L, 1)));
+  SG_TRY(dalloc(ctx, &P.seed_n, 1));
   SG_TRY(dalloc(ctx, &P.sp_rows, all));
   SG_TRY(dalloc(ctx, &P.r_size, (uint64_t)all + 1));
   SG_TRY(dalloc(ctx, &P.blk, (uint64_t)all + 1));
@@ -1344,6 +1531,140 @@ sg_status repair_pending_clusters(sg_ctx* ctx, SummaryDev& D, const uint32_t** l
   SG_CUDA(ctx, cudaMemsetAsync(P->c_pend, 0, P->ncl, ctx->stream));
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   *list = P->tcl;
+  return SG_OK;
+}
+
+
+bool repair_active(const SummaryDev& D) { return D.rep != nullptr; }
+
+namespace {
+
+// the summarized CSR and correction lists from the SSSP distance blocks
+sg_status rp_sketch(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R) {
+  cudaStream_t st = ctx->stream;
+  const uint32_t all = P.all_n;
+  SG_TRY(reserve(ctx, D, &D.sk_deg, all));
+  SG_TRY(reserve(ctx, D, &D.sk_off, (uint64_t)all + 1));
+  SkArgs K{};
+  K.blk = P.blk;
+  K.sd = P.sd;
+  K.ib_off = D.ib_off;
+  K.ib_nbr = D.ib_nbr;
+  K.ib_w = P.ib_w;
+  K.deg = D.sk_deg;
+  K.pad = P.cnt_a;
+  K.ccnt = P.cnt_b;
+  K.fcorr = P.f_corr;
+  k_rp_sketch<false><<<grid_for(all, 256), 256, 0, st>>>(R, K);
+  SG_TRY(scan_u64(ctx, P.cnt_a, D.sk_off, (uint64_t)all + 1));
+  SG_TRY(scan_u64(ctx, P.cnt_b, P.cnt_c, (uint64_t)all + 1));
+  SG_TRY(reserve(ctx, D, &D.sk_crow, all));
+  SG_TRY(select_idx(ctx, P.f_corr, D.sk_crow, P.d_num, all));
+  uint64_t tot[2] = {0, 0};
+  uint32_t ncorr = 0;
+  SG_CUDA(ctx, cudaMemcpyAsync(&tot[0], D.sk_off + all, 8, cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaMemcpyAsync(&tot[1], P.cnt_c + all, 8, cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaMemcpyAsync(&ncorr, P.d_num, 4, cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  SG_TRY(reserve(ctx, D, &D.sk_col, tot[0] + 4));
+  SG_TRY(reserve(ctx, D, &D.sk_w, tot[0] + 4));
+  SG_TRY(reserve(ctx, D, &D.sk_cv, tot[1]));
+  SG_TRY(reserve(ctx, D, &D.sk_cd, tot[1]));
+  SG_TRY(reserve(ctx, D, &D.sk_coff, (uint64_t)ncorr + 1));
+  SG_CUDA(ctx, cudaMemsetAsync(D.sk_col, 0, 4 * (tot[0] + 4), st));
+  SG_CUDA(ctx, cudaMemsetAsync(D.sk_w, 0, 4 * (tot[0] + 4), st));
+  K.off = D.sk_off;
+  K.col = D.sk_col;
+  K.w = D.sk_w;
+  K.coff = P.cnt_c;
+  K.cv = D.sk_cv;
+  K.cd = D.sk_cd;
+  k_rp_sketch<true><<<grid_for(all, 256), 256, 0, st>>>(R, K);
+  k_rp_gather_off<<<grid_for((uint64_t)ncorr + 1, 256), 256, 0, st>>>(D.sk_crow, ncorr, P.cnt_c, tot[1],
+                                                                     D.sk_coff);
+  SG_TRY(reserve(ctx, D, &D.sk_spid, std::max<uint32_t>(P.n_sp, 1)));
+  if (P.n_sp)
+    SG_CUDA(ctx, cudaMemcpyAsync(D.sk_spid, P.sp_rows, 4ull * P.n_sp, cudaMemcpyDeviceToDevice, st));
+  SG_TRY(reserve(ctx, D, &D.sk_imir, std::max<uint32_t>(P.n_im_total, 1)));
+  SG_TRY(reserve(ctx, D, &D.sk_imaster, std::max<uint32_t>(P.n_im_total, 1)));
+  if (P.n_im_total) {
+    SG_CUDA(ctx, cudaMemcpyAsync(D.sk_imir, P.im_list, 4ull * P.n_im_total, cudaMemcpyDeviceToDevice,
+                                 st));
+    SG_CUDA(ctx, cudaMemcpyAsync(D.sk_imaster, P.im_master, 4ull * P.n_im_total,
+                                 cudaMemcpyDeviceToDevice, st));
+  }
+  count_launch(ctx, 6);
+  SG_CUDA(ctx, cudaGetLastError());
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  D.sk_m = tot[0];
+  D.sk_ncorr = ncorr;
+  D.sk_nspid = P.n_sp;
+  D.sk_nimir = P.n_im_total;
+  P.sk_stale = false;
+  return SG_OK;
+}
+
+}  // namespace
+
+sg_status repair_sssp_refresh(sg_ctx* ctx, SummaryDev& D) {
+  RepairDev* Pp = D.rep;
+  if (!Pp) return fail(ctx, SG_ERR_STATE, "no device summary");
+  RepairDev& P = *Pp;
+  cudaStream_t st = ctx->stream;
+  PhaseTrace T("device SSSP summary");
+  const RepArgs R = rep_args(ctx, P);
+  if (!P.sssp_on) {
+    // every supernode's distances (and its PageRank solve again) once
+    P.sssp_on = true;
+    SG_CUDA(ctx, cudaMemsetAsync(P.c_src, 1, P.ncl, st));
+    SG_TRY(reserve(ctx, D, &D.out_deg_all, P.all_n));
+    k_rp_rows<<<grid_for(P.all_n, 256), 256, 0, st>>>(R, P.r_size, P.f_sp, D.out_deg_all);
+    count_launch(ctx);
+    SG_TRY(rp_shortcuts(ctx, D, P, R, T));
+    SG_TRY(rp_tables(ctx, D, P, R, T));
+    SG_TRY(rp_finish(ctx, P, R));
+  }
+  if (P.sk_stale) SG_TRY(rp_sketch(ctx, D, P, R));
+  T.mark("summarized CSR", st);
+  D.sssp_ready = true;
+  return SG_OK;
+}
+
+sg_status repair_source_seeds(sg_ctx* ctx, SummaryDev& D, uint32_t source, const uint32_t** v,
+                              const double** d, uint32_t* count) {
+  RepairDev* Pp = D.rep;
+  *count = 0;
+  *v = nullptr;
+  *d = nullptr;
+  if (!Pp) return SG_OK;
+  RepairDev& P = *Pp;
+  const Summary& S = D.S;  // membership and local indices are fixed after the build
+  if (source >= S.old_n) return SG_OK;
+  const uint32_t c = S.id2spids[source];
+  if (c == Summary::kIdDefault || c >= P.ncl) return SG_OK;
+  const auto& nodes = S.cluster_ids[c];
+  uint32_t loc = 0;
+  while (loc < nodes.size() && nodes[loc] != source) ++loc;
+  if (loc == nodes.size()) return fail(ctx, SG_ERR_STATE, "source missing from its cluster");
+  cudaStream_t st = ctx->stream;
+  const RepArgs R = rep_args(ctx, P);
+  SG_CUDA(ctx, cudaMemcpyAsync(P.tcl, &c, 4, cudaMemcpyHostToDevice, st));
+  uint64_t npos = 0;
+  SG_TRY(rp_local_problems(ctx, P, R, 1, &npos));
+  const uint32_t zero = 0;
+  const uint64_t zero64 = 0;
+  SG_CUDA(ctx, cudaMemcpyAsync(P.sp_cl, &zero, 4, cudaMemcpyHostToDevice, st));
+  SG_CUDA(ctx, cudaMemcpyAsync(P.sp_src, &loc, 4, cudaMemcpyHostToDevice, st));
+  SG_CUDA(ctx, cudaMemcpyAsync(P.out_off, &zero64, 8, cudaMemcpyHostToDevice, st));
+  SG_TRY(rp_sssp_solve(ctx, P, 1, P.out_off, P.src_dist));
+  SG_CUDA(ctx, cudaMemsetAsync(P.seed_n, 0, 4, st));
+  k_rp_seeds<<<1, 256, 0, st>>>(R, c, P.src_dist, P.seed_v, P.seed_d, P.seed_n);
+  count_launch(ctx);
+  SG_CUDA(ctx, cudaMemcpyAsync(count, P.seed_n, 4, cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  SG_CUDA(ctx, cudaGetLastError());
+  *v = P.seed_v;
+  *d = P.seed_d;
   return SG_OK;
 }
 

@@ -137,8 +137,7 @@ static sg_status reupload(sg_ctx* ctx, SummaryDev& D, T** d, const std::vector<T
 enum StageSlot {
   ST_WJOBS, ST_WJOBS5, ST_BJOBS, ST_LINOFF, ST_LINSRC, ST_SPC, ST_SRC, ST_INNER, ST_ADJ, ST_CLOFF,
   ST_ADJOFF, ST_OUTOFF, ST_DIV, ST_VAL, ST_DEL,
-  SS_CL, SS_SRC, SS_NBR, SS_W, SS_CLOFF, SS_ADJOFF, SS_OUTOFF, SS_OUT,
-  SI_DALL, SI_SEEDS, SI_CS, SI_CD, SI_S2, SP_DIST, ST_SLOTS
+  SI_DALL, SI_SEEDS, SI_S2, SP_DIST, ST_SLOTS
 };
 static_assert(ST_SLOTS <= 32, "staging slots");
 
@@ -784,7 +783,6 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
   return SG_OK;
 }
 
-static sg_status sssp_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector<uint32_t>& spids);
 
 // ------------------------------------------------------ build entry point
 
@@ -1395,11 +1393,6 @@ static sg_status host_repair_batch(sg_ctx* ctx, SummaryDev* D, const uint32_t* a
   T.mark("node types");
   summary_sketch_csr(S, D->out);
   T.mark("sketch CSRs");
-  if (D->sssp_ready && ctx->g.weighted) {
-    // shortcut distances of the touched supernodes are repaired by the next
-    // SSSP query over the summary (a PageRank-only caller never pays them)
-    D->sssp_pending.insert(D->sssp_pending.end(), sps.begin(), sps.end());
-  }
   return SG_OK;
 }
 
@@ -1421,17 +1414,16 @@ static sg_status host_sync(sg_ctx* ctx, SummaryDev* D) {
 }
 
 // After sg_apply_updates on a summarized graph: the device repair of the
-// PageRank tables; the host restatement follows on demand (at once when SSSP
-// over the summary runs on this context, and before its action log grows
-// past 64 M actions).
+// PageRank tables (and of the SSSP distance blocks once SSSP over the
+// summary has run); the host restatement follows on demand (and before its
+// action log grows past 64 M actions).
 sg_status summary_after_apply(sg_ctx* ctx) {
   SummaryDev* D = sdev(ctx);
   if (!D || !D->valid) return SG_OK;
   if (summary_no_supernodes(ctx) || !D->rep) return SG_OK;  // nothing to repair, ever
-  D->sk_stale = true;
   D->pull_stale = true;
   SG_TRY(repair_after_apply(ctx, *D));
-  if (D->sssp_ready || repair_logged_actions(*D) > (1ull << 26)) SG_TRY(host_sync(ctx, D));
+  if (repair_logged_actions(*D) > (1ull << 26)) SG_TRY(host_sync(ctx, D));
   return SG_OK;
 }
 
@@ -1799,265 +1791,6 @@ __global__ void __launch_bounds__(128) k_sssp_shortcuts(const uint32_t* __restri
   for (uint32_t i = threadIdx.x; i < L; i += blockDim.x) out[o + i] = bitsd(sd[i]);
 }
 
-// Runs one shortcut job per (cluster, local source) pair; dist[j] gets the
-// local distances of job j in the order of cluster_ids.
-static sg_status sssp_cluster_jobs(sg_ctx* ctx, SummaryDev& D,
-                                   const std::vector<std::pair<uint32_t, uint32_t>>& jobs,
-                                   std::vector<std::vector<double>>* dist) {
-  Summary& S = D.S;
-  dist->assign(jobs.size(), {});
-  if (jobs.empty()) return SG_OK;
-  if (S.subgraph_w.empty() && !S.subgraph.empty())
-    return fail(ctx, SG_ERR_INVALID, "SSSP over the summary needs edge weights");
-  std::unordered_map<uint32_t, uint32_t> cl_index;
-  std::vector<uint32_t> cls;
-  for (auto& jb : jobs)
-    if (cl_index.emplace(jb.first, (uint32_t)cls.size()).second) cls.push_back(jb.first);
-  // local problems per cluster (nodes, weighted subgraph edges as local
-  // indices; edges to nodes outside the cluster's list are dropped), built in
-  // two parallel passes; nodes of different clusters are distinct
-  const size_t ncl = cls.size();
-  std::vector<uint64_t> cl_off(ncl + 1, 0), cl_adj(ncl + 1, 0);
-  std::vector<uint32_t> local_of(S.all_n, 0xFFFFFFFFu);
-  size_t maxL = 1;
-  for (size_t k = 0; k < ncl; ++k) {
-    const auto& nodes = S.cluster_ids[cls[k]];
-    cl_off[k + 1] = cl_off[k] + nodes.size();
-    maxL = std::max(maxL, nodes.size());
-  }
-  auto local = [&](const std::vector<uint32_t>& nodes, uint32_t t) {
-    const uint32_t l = local_of[t];
-    return (l < nodes.size() && nodes[l] == t) ? l : 0xFFFFFFFFu;
-  };
-#pragma omp parallel for schedule(dynamic, 256)
-  for (long long k = 0; k < (long long)ncl; ++k) {
-    const auto& nodes = S.cluster_ids[cls[k]];
-    for (uint32_t i = 0; i < nodes.size(); ++i) local_of[nodes[i]] = i;
-  }
-#pragma omp parallel for schedule(dynamic, 256)
-  for (long long k = 0; k < (long long)ncl; ++k) {
-    const auto& nodes = S.cluster_ids[cls[k]];
-    uint64_t ne = 0;
-    for (uint32_t v : nodes)
-      for (uint32_t t : S.subgraph[v]) ne += local(nodes, t) != 0xFFFFFFFFu;
-    cl_adj[k + 1] = ne;
-  }
-  for (size_t k = 0; k < ncl; ++k) cl_adj[k + 1] += cl_adj[k];
-  std::vector<uint64_t> adj_off(cl_off[ncl] + 1);
-  std::vector<uint32_t> adj_nbr(cl_adj[ncl]);
-  std::vector<float> adj_w(cl_adj[ncl]);
-#pragma omp parallel for schedule(dynamic, 256)
-  for (long long k = 0; k < (long long)ncl; ++k) {
-    const auto& nodes = S.cluster_ids[cls[k]];
-    uint64_t o = cl_adj[k];
-    for (uint32_t i = 0; i < nodes.size(); ++i) {
-      adj_off[cl_off[k] + i] = o;
-      const auto& nb = S.subgraph[nodes[i]];
-      const auto& wt = S.subgraph_w[nodes[i]];
-      for (size_t e = 0; e < nb.size(); ++e) {
-        const uint32_t l = local(nodes, nb[e]);
-        if (l == 0xFFFFFFFFu) continue;
-        adj_nbr[o] = l;
-        adj_w[o++] = wt[e];
-      }
-    }
-  }
-  adj_off[cl_off[ncl]] = cl_adj[ncl];
-  std::vector<uint32_t> job_cl(jobs.size()), job_src(jobs.size());
-  std::vector<uint64_t> out_off(jobs.size() + 1, 0);
-  for (size_t j = 0; j < jobs.size(); ++j) {
-    const uint32_t k = cl_index[jobs[j].first];
-    job_cl[j] = k;
-    job_src[j] = jobs[j].second;
-    out_off[j + 1] = out_off[j] + (cl_off[k + 1] - cl_off[k]);
-  }
-  const size_t smem = maxL * sizeof(unsigned long long);
-  if (smem > 200 * 1024) return fail(ctx, SG_ERR_UNSUPPORTED, "cluster too large for the shortcut kernel");
-  uint32_t *d_cl = nullptr, *d_src = nullptr, *d_nbr = nullptr;
-  uint64_t *d_cloff = nullptr, *d_adjoff = nullptr, *d_outoff = nullptr;
-  float* d_w = nullptr;
-  double* d_out = nullptr;
-  SG_TRY(stage_up(ctx, D, SS_CL, job_cl, &d_cl));
-  SG_TRY(stage_up(ctx, D, SS_SRC, job_src, &d_src));
-  SG_TRY(stage_up(ctx, D, SS_NBR, adj_nbr, &d_nbr));
-  SG_TRY(stage_up(ctx, D, SS_W, adj_w, &d_w));
-  SG_TRY(stage_up(ctx, D, SS_CLOFF, cl_off, &d_cloff));
-  SG_TRY(stage_up(ctx, D, SS_ADJOFF, adj_off, &d_adjoff));
-  SG_TRY(stage_up(ctx, D, SS_OUTOFF, out_off, &d_outoff));
-  SG_TRY(stage_alloc(ctx, D, SS_OUT, out_off.back(), &d_out));
-  if (smem > 48 * 1024)
-    SG_CUDA(ctx, cudaFuncSetAttribute(k_sssp_shortcuts, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-  kprof_begin(ctx);
-  k_sssp_shortcuts<<<(unsigned)jobs.size(), 128, smem, ctx->stream>>>(
-      d_cl, d_src, d_cloff, d_adjoff, d_nbr, d_w, d_outoff, d_out, (uint32_t)jobs.size());
-  kprof_end(ctx, SG_K_SUMMARY);
-  SG_CUDA(ctx, cudaGetLastError());
-  hvec<double> all(out_off.back());
-  SG_CUDA(ctx, cudaMemcpyAsync(all.data(), d_out, 8 * all.size(), cudaMemcpyDeviceToHost, ctx->stream));
-  SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-#pragma omp parallel for schedule(dynamic, 256)
-  for (long long j = 0; j < (long long)jobs.size(); ++j)
-    (*dist)[j].assign(all.begin() + out_off[j], all.begin() + out_off[j + 1]);
-  return SG_OK;
-}
-
-static bool is_out_mirror(const Summary& S, uint32_t c, uint32_t v) {
-  const auto& om = S.cluster_out_mirror_ids[c];
-  return v >= S.old_n && std::find(om.begin(), om.end(), v) != om.end();
-}
-
-static uint32_t local_index(const std::vector<uint32_t>& nodes, uint32_t v) {
-  for (uint32_t i = 0; i < nodes.size(); ++i)
-    if (nodes[i] == v) return i;
-  return 0;
-}
-
-// Bound and inner shortcut distances of the given supernodes
-// (fianl_build_trav_index_mirror, trav_compressor.h:366-430).
-static sg_status sssp_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector<uint32_t>& spids) {
-  Summary& S = D.S;
-  D.sp_bound_d.resize(S.supernodes.size());
-  D.sp_inner_d.resize(S.supernodes.size());
-  std::vector<std::pair<uint32_t, uint32_t>> jobs;
-  std::vector<uint32_t> jsp;
-  for (uint32_t sp : spids) {
-    const Supernode& n = S.supernodes[sp];
-    D.sp_bound_d[sp].clear();
-    D.sp_inner_d[sp].clear();
-    if (n.id == Summary::kIdDefault) continue;
-    jobs.push_back({n.ids, local_index(S.cluster_ids[n.ids], n.id)});
-    jsp.push_back(sp);
-  }
-  std::vector<std::vector<double>> dist;
-  SG_TRY(sssp_cluster_jobs(ctx, D, jobs, &dist));
-  const double inf = std::numeric_limits<double>::infinity();
-  // each job writes its own supernode's lists
-#pragma omp parallel for schedule(dynamic, 256)
-  for (long long j = 0; j < (long long)jobs.size(); ++j) {
-    const uint32_t sp = jsp[j];
-    const uint32_t c = S.supernodes[sp].ids;
-    const auto& nodes = S.cluster_ids[c];
-    const uint32_t inner = (uint32_t)S.supernode_ids[c].size();
-    for (uint32_t i = 0; i < nodes.size(); ++i) {
-      const double d = dist[j][i];
-      if (!(d < inf)) continue;
-      const uint32_t v = nodes[i];
-      if (i >= inner) {
-        if (is_out_mirror(S, c, v))
-          D.sp_bound_d[sp].push_back({S.mirror_master(v), d});  // out-mirror: its master
-      } else if (S.out_bound[v]) {
-        D.sp_bound_d[sp].push_back({v, d});
-      } else {
-        D.sp_inner_d[sp].push_back({v, d});
-      }
-    }
-  }
-  D.sk_stale = true;
-  return SG_OK;
-}
-
-// The summarized CSR (padded to quads) and the correction lists.
-static sg_status sssp_sketch(sg_ctx* ctx, SummaryDev& D) {
-  Summary& S = D.S;
-  const uint32_t all = S.all_n, n = S.old_n;
-  // rows in two passes: per row, master -> in-mirror edges first, then the
-  // supernode's shortcuts, then the boundary edges; rows padded to quads
-  std::vector<uint32_t> head(all, 0);  // mirror + shortcut entries per row
-  for (size_t i = 0; i < S.cluster_in_mirror_ids.size(); ++i)
-    for (uint32_t m : S.cluster_in_mirror_ids[i]) head[S.mirror_master(m)]++;
-  for (uint32_t sp = 0; sp < S.supernodes.size(); ++sp) {
-    const Supernode& nd = S.supernodes[sp];
-    if (nd.id == Summary::kIdDefault || sp >= D.sp_bound_d.size()) continue;
-    head[nd.id] += (uint32_t)D.sp_bound_d[sp].size();
-  }
-  std::vector<uint64_t> off(all);
-  std::vector<uint32_t> deg(all);
-#pragma omp parallel for schedule(static)
-  for (long long uu = 0; uu < (long long)all; ++uu) {
-    const uint32_t u = (uint32_t)uu;
-    deg[u] = head[u] + (u < n ? (uint32_t)(S.ib_off[u + 1] - S.ib_off[u]) : 0u);
-  }
-  uint64_t pos = 0;
-  for (uint32_t u = 0; u < all; ++u) {
-    off[u] = pos;
-    pos += (deg[u] + 3u) & ~3u;
-  }
-  std::vector<uint32_t> col(pos + 4, 0);
-  std::vector<float> w(pos + 4, 0.f);
-  std::vector<uint32_t> fill(all, 0);
-  for (size_t i = 0; i < S.cluster_in_mirror_ids.size(); ++i)
-    for (uint32_t m : S.cluster_in_mirror_ids[i]) {
-      const uint32_t u = S.mirror_master(m);
-      col[off[u] + fill[u]++] = m;  // weight 0
-    }
-  for (uint32_t sp = 0; sp < S.supernodes.size(); ++sp) {
-    const Supernode& nd = S.supernodes[sp];
-    if (nd.id == Summary::kIdDefault || sp >= D.sp_bound_d.size()) continue;
-    for (auto& e : D.sp_bound_d[sp]) {
-      const uint64_t k = off[nd.id] + fill[nd.id]++;
-      col[k] = e.first;
-      w[k] = (float)e.second;
-    }
-  }
-#pragma omp parallel for schedule(dynamic, 4096)
-  for (long long uu = 0; uu < (long long)n; ++uu) {
-    const uint32_t u = (uint32_t)uu;
-    uint64_t k = off[u] + head[u];
-    for (uint64_t e = S.ib_off[u]; e < S.ib_off[u + 1]; ++e, ++k) {
-      col[k] = S.ib_nbr[e];
-      w[k] = S.ib_w.empty() ? 1.f : S.ib_w[e];
-    }
-  }
-  // correction lists (entry -> inner member shortcuts), in supernode order:
-  // rows and offsets on one pass, the entries filled in parallel
-  const uint32_t nsp = (uint32_t)S.supernodes.size();
-  std::vector<uint64_t> coff(1, 0);
-  std::vector<uint32_t> crow, csp;
-  for (uint32_t sp = 0; sp < nsp; ++sp) {
-    const Supernode& nd = S.supernodes[sp];
-    if (nd.id == Summary::kIdDefault || sp >= D.sp_inner_d.size() || D.sp_inner_d[sp].empty()) continue;
-    crow.push_back(nd.id);
-    csp.push_back(sp);
-    coff.push_back(coff.back() + D.sp_inner_d[sp].size());
-  }
-  hvec<uint32_t> cv(coff.back());
-  hvec<float> cd(coff.back());
-#pragma omp parallel for schedule(dynamic, 256)
-  for (long long r = 0; r < (long long)csp.size(); ++r) {
-    uint64_t k = coff[r];
-    for (auto& e : D.sp_inner_d[csp[r]]) {
-      cv[k] = e.first;
-      cd[k++] = (float)e.second;
-    }
-  }
-  SG_TRY(reupload(ctx, D, &D.sk_off, off));
-  SG_TRY(reupload(ctx, D, &D.sk_deg, deg));
-  SG_TRY(reupload(ctx, D, &D.sk_col, col));
-  SG_TRY(reupload(ctx, D, &D.sk_w, w));
-  SG_TRY(reupload(ctx, D, &D.sk_coff, coff));
-  SG_TRY(reupload(ctx, D, &D.sk_crow, crow));
-  SG_TRY(reupload(ctx, D, &D.sk_cv, cv));
-  SG_TRY(reupload(ctx, D, &D.sk_cd, cd));
-  std::vector<uint32_t> spid, imir, imaster;
-  for (uint32_t sp = 0; sp < S.supernodes.size(); ++sp)
-    if (S.supernodes[sp].id != Summary::kIdDefault) spid.push_back(S.supernodes[sp].id);
-  for (size_t i = 0; i < S.cluster_in_mirror_ids.size(); ++i)
-    for (uint32_t m : S.cluster_in_mirror_ids[i]) {
-      imir.push_back(m);
-      imaster.push_back(S.mirror_master(m));
-    }
-  SG_TRY(reupload(ctx, D, &D.sk_spid, spid));
-  SG_TRY(reupload(ctx, D, &D.sk_imir, imir));
-  SG_TRY(reupload(ctx, D, &D.sk_imaster, imaster));
-  D.sk_nspid = (uint32_t)spid.size();
-  D.sk_nimir = (uint32_t)imir.size();
-  D.sk_m = pos;
-  D.sk_ncorr = (uint32_t)crow.size();
-  D.sk_stale = false;
-  return SG_OK;
-}
-
 // inner member <- min over its cluster's entries of entry distance + shortcut
 __global__ void k_sssp_correct(uint32_t nrows, const uint64_t* __restrict__ coff,
                                const uint32_t* __restrict__ crow, const uint32_t* __restrict__ cv,
@@ -2079,92 +1812,35 @@ __global__ void k_copy_u64(const unsigned long long* a, uint64_t n, unsigned lon
     b[i] = a[i];
 }
 
-// Shortcut distances built on first use, repaired for the supernodes the
-// batches since the last query touched, and the summarized CSR rebuilt when
-// stale.
-static sg_status sssp_summary_refresh(sg_ctx* ctx, SummaryDev& D) {
-  Summary& S = D.S;
-  PhaseTrace T("sssp summary");
-  if (!D.sssp_ready) {
-    std::vector<uint32_t> all_sp(S.supernodes.size());
-    for (uint32_t i = 0; i < all_sp.size(); ++i) all_sp[i] = i;
-    SG_TRY(sssp_shortcuts(ctx, D, all_sp));
-    D.sssp_ready = true;
-    D.sssp_pending.clear();
-  }
-  if (!D.sssp_pending.empty()) {
-    // supernodes touched by the batches since the last query; new
-    // supernodes get their lists
-    std::vector<uint32_t>& P = D.sssp_pending;
-    std::sort(P.begin(), P.end());
-    P.erase(std::unique(P.begin(), P.end()), P.end());
-    P.erase(std::remove_if(P.begin(), P.end(),
-                           [&](uint32_t sp) { return sp >= S.supernodes.size(); }),
-            P.end());
-    if (D.sp_bound_d.size() < S.supernodes.size()) {
-      D.sp_bound_d.resize(S.supernodes.size());
-      D.sp_inner_d.resize(S.supernodes.size());
-    }
-    SG_TRY(sssp_shortcuts(ctx, D, P));
-    T.mark("shortcut distances");
-    P.clear();
-    D.sk_stale = true;
-  }
-  if (D.sk_stale) SG_TRY(sssp_sketch(ctx, D));
-  T.mark("summarized CSR");
-  return SG_OK;
-}
-
-// A source inside a cluster reaches the cluster's other members by paths
-// that pass through no entry, which no shortcut holds: its cluster is solved
-// locally from it (as the PEval of SumSyncTraversalWorker does for the
-// source's supernode), and every member (an out-mirror as its master) seeds
-// the traversal with its local distance.  *member is false for a source
-// outside the clusters (nothing added).
-static sg_status source_cluster_seeds(sg_ctx* ctx, SummaryDev& D, uint32_t source,
-                                      std::vector<uint32_t>* seeds, std::vector<double>* sdist,
-                                      bool* member) {
-  Summary& S = D.S;
-  *member = false;
-  const uint32_t c = S.id2spids[source];
-  if (c == Summary::kIdDefault || c >= S.cluster_ids.size()) return SG_OK;
-  *member = true;
-  std::vector<std::vector<double>> dist;
-  const auto& nodes = S.cluster_ids[c];
-  SG_TRY(sssp_cluster_jobs(ctx, D, {{c, local_index(nodes, source)}}, &dist));
-  const double inf = std::numeric_limits<double>::infinity();
-  for (uint32_t i = 0; i < nodes.size(); ++i) {
-    if (!(dist[0][i] < inf)) continue;
-    const uint32_t v = nodes[i];
-    if (v < S.old_n) {
-      seeds->push_back(v);
-    } else if (is_out_mirror(S, c, v)) {
-      seeds->push_back(S.mirror_master(v));
-    } else {
-      continue;
-    }
-    sdist->push_back(dist[0][i]);
-  }
-  return SG_OK;
-}
-
 sg_status sssp_summarized(sg_ctx* ctx, uint32_t source) {
   SummaryDev* Dp = sdev(ctx);
   if (!Dp || !Dp->valid) return fail(ctx, SG_ERR_STATE, "compress=1 needs sg_summary_build first");
   SummaryDev& D = *Dp;
-  SG_TRY(host_sync(ctx, Dp));
-  Summary& S = D.S;
+  Summary& S = D.S;  // (its membership part, fixed after the build)
   if (!ctx->g.weighted) return fail(ctx, SG_ERR_INVALID, "SSSP needs a weighted graph");
   if (source >= S.old_n) return fail(ctx, SG_ERR_INVALID, "source >= n");
-  if (summary_no_supernodes(ctx)) return sssp_run_peval(ctx, source);
+  if (summary_no_supernodes(ctx) || !repair_active(D)) return sssp_run_peval(ctx, source);
   cudaStream_t st = ctx->stream;
   SG_CUDA(ctx, cudaEventRecord(ctx->kev0, st));
-  SG_TRY(sssp_summary_refresh(ctx, D));
-  // seeds: the source, expanded inside its cluster when it is a member
+  SG_TRY(repair_sssp_refresh(ctx, D));
+  // seeds: the source, expanded inside its cluster when it is a member (a
+  // path from the source to its own cluster's members needs no entry)
   std::vector<uint32_t> seeds;
   std::vector<double> sdist;
-  bool member = false;
-  SG_TRY(source_cluster_seeds(ctx, D, source, &seeds, &sdist, &member));
+  const bool member = S.id2spids[source] != Summary::kIdDefault;
+  {
+    const uint32_t* dv = nullptr;
+    const double* dd = nullptr;
+    uint32_t cnt = 0;
+    SG_TRY(repair_source_seeds(ctx, D, source, &dv, &dd, &cnt));
+    seeds.resize(cnt);
+    sdist.resize(cnt);
+    if (cnt) {
+      SG_CUDA(ctx, cudaMemcpyAsync(seeds.data(), dv, 4ull * cnt, cudaMemcpyDeviceToHost, st));
+      SG_CUDA(ctx, cudaMemcpyAsync(sdist.data(), dd, 8ull * cnt, cudaMemcpyDeviceToHost, st));
+      SG_CUDA(ctx, cudaStreamSynchronize(st));
+    }
+  }
   if (!member) {
     seeds.push_back(source);
     sdist.push_back(0.0);
@@ -2247,14 +1923,14 @@ sg_status sssp_summarized_inc(sg_ctx* ctx) {
   SummaryDev* Dp = sdev(ctx);
   if (!Dp || !Dp->valid) return fail(ctx, SG_ERR_STATE, "compress=1 needs sg_summary_build first");
   SummaryDev& D = *Dp;
-  SG_TRY(host_sync(ctx, Dp));
-  Summary& S = D.S;
+  Summary& S = D.S;  // (its membership part, fixed after the build)
   if (!ctx->g.weighted) return fail(ctx, SG_ERR_INVALID, "SSSP needs a weighted graph");
+  if (!repair_active(D)) return fail(ctx, SG_ERR_STATE, "no device summary");
   cudaStream_t st = ctx->stream;
   SG_CUDA(ctx, cudaEventRecord(ctx->kev0, st));
   SsspIncInfo info;
   SG_TRY(sssp_inc_prepare(ctx, &info));
-  SG_TRY(sssp_summary_refresh(ctx, D));
+  SG_TRY(repair_sssp_refresh(ctx, D));
   const uint32_t n = S.old_n, all = S.all_n;
   SsspState& sp = ctx->sp;
   unsigned long long* dall = nullptr;
@@ -2279,26 +1955,20 @@ sg_status sssp_summarized_inc(sg_ctx* ctx) {
     SG_CUDA(ctx, cudaMemcpyAsync(seeds + o, D.sk_spid, 4ull * D.sk_nspid, cudaMemcpyDeviceToDevice,
                                  st));
   // the source's own cluster, solved locally on the repaired subgraph
-  std::vector<uint32_t> cs;
-  std::vector<double> cd;
-  bool member = false;
-  SG_TRY(source_cluster_seeds(ctx, D, sp.source, &cs, &cd, &member));
-  uint32_t* d_cs = nullptr;
-  double* d_cd = nullptr;
+  const uint32_t* d_cs = nullptr;
+  const double* d_cd = nullptr;
+  uint32_t ncs = 0;
+  SG_TRY(repair_source_seeds(ctx, D, sp.source, &d_cs, &d_cd, &ncs));
   uint64_t nseeds_all = nseeds;
-  if (!cs.empty()) {
-    SG_TRY(stage_alloc(ctx, D, SI_CS, cs.size(), &d_cs));
-    SG_TRY(stage_alloc(ctx, D, SI_CD, cd.size(), &d_cd));
-    SG_CUDA(ctx, cudaMemcpyAsync(d_cs, cs.data(), 4ull * cs.size(), cudaMemcpyHostToDevice, st));
-    SG_CUDA(ctx, cudaMemcpyAsync(d_cd, cd.data(), 8ull * cd.size(), cudaMemcpyHostToDevice, st));
-    k_dist_min_list<<<grid_for(cs.size(), 256), 256, 0, st>>>(d_cs, d_cd, (uint32_t)cs.size(), dall);
+  if (ncs) {
+    k_dist_min_list<<<grid_for(ncs, 256), 256, 0, st>>>(d_cs, d_cd, ncs, dall);
     count_launch(ctx);
     uint32_t* s2 = nullptr;
-    SG_TRY(stage_alloc(ctx, D, SI_S2, nseeds + cs.size(), &s2));
+    SG_TRY(stage_alloc(ctx, D, SI_S2, nseeds + ncs, &s2));
     if (nseeds) SG_CUDA(ctx, cudaMemcpyAsync(s2, seeds, 4ull * nseeds, cudaMemcpyDeviceToDevice, st));
-    SG_CUDA(ctx, cudaMemcpyAsync(s2 + nseeds, d_cs, 4ull * cs.size(), cudaMemcpyDeviceToDevice, st));
+    SG_CUDA(ctx, cudaMemcpyAsync(s2 + nseeds, d_cs, 4ull * ncs, cudaMemcpyDeviceToDevice, st));
     seeds = s2;
-    nseeds_all = nseeds + cs.size();
+    nseeds_all = nseeds + ncs;
   }
   SsspView G{all, D.sk_m, D.sk_off, D.sk_deg, D.sk_col, D.sk_w};
   unsigned long long h_cnt[4] = {0, 0, 0, 0};

@@ -108,6 +108,15 @@ struct ShortcutArgs {
 __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njobs);
 // dynamic shared memory of k_shortcuts for a cluster of L nodes
 inline size_t shortcut_smem(size_t L) { return L * (sizeof(double) + 3 * sizeof(float)); }
+// SSSP distances inside a cluster from each job's local source (summary.cu)
+__global__ void __launch_bounds__(128) k_sssp_shortcuts(const uint32_t* __restrict__ job_cl,
+                                                        const uint32_t* __restrict__ job_src,
+                                                        const uint64_t* __restrict__ cl_off,
+                                                        const uint64_t* __restrict__ adj_off,
+                                                        const uint32_t* __restrict__ adj_nbr,
+                                                        const float* __restrict__ adj_w,
+                                                        const uint64_t* __restrict__ out_off,
+                                                        double* __restrict__ out, uint32_t njobs);
 // a warp per job for clusters of at most 32 x npl nodes (npl = 2 or 5)
 void launch_shortcuts_warp(int npl, ShortcutArgs A, uint32_t njobs, cudaStream_t st);
 constexpr uint32_t kShortcutSmallL = 64;  // clusters the npl = 2 variant takes
@@ -150,18 +159,14 @@ struct SummaryDev {
   double* d_res = nullptr;
   uint32_t* sctl = nullptr;  // summarized rounds: done flag, blocks finished, rounds run
   std::vector<uint32_t> pending_clusters;  // touched since the last IncEval
-  // SSSP over the summary: shortcut distances per supernode (entry -> exit /
-  // out-mirror, entry -> inner member), the summarized CSR and the
-  // correction lists; built on first use, repaired after each batch
+  // SSSP over the summary (built by repair.cu on the first query): the
+  // summarized CSR and the correction lists
   bool sssp_ready = false;
-  std::vector<std::vector<std::pair<uint32_t, double>>> sp_bound_d, sp_inner_d;
-  std::vector<uint32_t> sssp_pending;  // supernodes touched since, repaired on the next SSSP use
   uint64_t *sk_off = nullptr, *sk_coff = nullptr;
   uint32_t *sk_deg = nullptr, *sk_col = nullptr, *sk_crow = nullptr, *sk_cv = nullptr;
   float *sk_w = nullptr, *sk_cd = nullptr;
   uint64_t sk_m = 0;
   uint32_t sk_ncorr = 0;
-  bool sk_stale = true;
   // IncEval over the summary: the rows whose shortcuts are relaxed again
   // (every supernode's entry or in-mirror) and the in-mirrors with their
   // masters (a mirror starts from its master's distance)
@@ -199,5 +204,15 @@ sg_status repair_take_log(sg_ctx* ctx, SummaryDev& D, std::vector<uint32_t>* src
                           std::vector<uint32_t>* found, std::vector<float>* w,
                           std::vector<uint64_t>* batch_end);
 void repair_free(SummaryDev& D);
+// SSSP over the summary from the device repair's state: distance blocks of
+// every supernode (built on the first call, repaired with each batch), the
+// summarized CSR and the correction lists in SummaryDev's sk_* tables.
+bool repair_active(const SummaryDev& D);
+sg_status repair_sssp_refresh(sg_ctx* ctx, SummaryDev& D);
+// Seeds of a source inside a cluster: every member (an out-mirror as its
+// master) with its distance from a local solve of the source's cluster, in
+// device arrays valid until the next repair call.
+sg_status repair_source_seeds(sg_ctx* ctx, SummaryDev& D, uint32_t source, const uint32_t** v,
+                              const double** d, uint32_t* count);
 
 }  // namespace sg
