@@ -100,8 +100,8 @@ struct RepairDev {
   // scratch of the passes (grown on demand)
   uint32_t *jobs = nullptr, *tcl = nullptr, *tc_idx = nullptr, *tc_inner = nullptr;
   uint32_t *sp_cl = nullptr, *sp_src = nullptr;
-  uint32_t *wjobs = nullptr, *wjobs5 = nullptr, *bjobs = nullptr;
-  uint8_t *j_warp = nullptr, *j_warp5 = nullptr, *j_block = nullptr;
+  uint32_t *wjobs = nullptr, *wjobs5 = nullptr, *bjobs = nullptr, *hjobs = nullptr;
+  uint8_t *j_warp = nullptr, *j_warp5 = nullptr, *j_block = nullptr, *j_half = nullptr;
   uint64_t *lp_off = nullptr, *adj_off = nullptr, *out_off = nullptr, *lin_off = nullptr;
   uint64_t* cl_lin = nullptr;
   uint32_t* adj_nbr = nullptr;
@@ -513,7 +513,7 @@ __global__ void __launch_bounds__(256) k_rp_lin_fill(RepArgs R, const uint32_t* 
 // 11. per job: cluster index, local source, output offset, kernel choice
 __global__ void k_rp_jobs(RepArgs R, const uint32_t* jobs, uint32_t nj, const uint32_t* tc_idx,
                           const uint64_t* blk, uint32_t* sp_cl, uint32_t* sp_src, uint64_t* out_off,
-                          uint8_t* j_warp, uint8_t* j_warp5, uint8_t* j_block) {
+                          uint8_t* j_half, uint8_t* j_warp, uint8_t* j_warp5, uint8_t* j_block) {
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nj; j += gridDim.x * blockDim.x) {
     const uint32_t r = jobs[j];
     const uint32_t c = R.cl_of[r];
@@ -521,7 +521,8 @@ __global__ void k_rp_jobs(RepArgs R, const uint32_t* jobs, uint32_t nj, const ui
     sp_src[j] = R.loc[r];
     out_off[j] = blk[r];
     const uint32_t L = cl_size(R, c);
-    j_warp[j] = L <= kShortcutSmallL;
+    j_half[j] = L <= kShortcutHalfL;
+    j_warp[j] = L > kShortcutHalfL && L <= kShortcutSmallL;
     j_warp5[j] = L > kShortcutSmallL && L <= (uint32_t)kStageCap;
     j_block[j] = L > (uint32_t)kStageCap;
   }
@@ -1076,12 +1077,13 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
     uint64_t npos = 0;
     SG_TRY(rp_local_problems(ctx, P, R, ntc, &npos));
     k_rp_jobs<<<grid_for(nj, 256), 256, 0, st>>>(R, P.jobs, nj, P.tc_idx, P.blk2, P.sp_cl, P.sp_src,
-                                                 P.out_off, P.j_warp, P.j_warp5, P.j_block);
+                                                 P.out_off, P.j_half, P.j_warp, P.j_warp5, P.j_block);
     SG_TRY(select_idx(ctx, P.j_warp, P.wjobs, P.d_num, nj));
     SG_TRY(select_idx(ctx, P.j_block, P.bjobs, P.d_num + 1, nj));
     SG_TRY(select_idx(ctx, P.j_warp5, P.wjobs5, P.d_num + 2, nj));
-    uint32_t nwb[3] = {0, 0, 0};
-    SG_CUDA(ctx, cudaMemcpyAsync(nwb, P.d_num, 12, cudaMemcpyDeviceToHost, st));
+    SG_TRY(select_idx(ctx, P.j_half, P.hjobs, P.d_num + 3, nj));
+    uint32_t nwb[4] = {0, 0, 0, 0};
+    SG_CUDA(ctx, cudaMemcpyAsync(nwb, P.d_num, 16, cudaMemcpyDeviceToHost, st));
     SG_CUDA(ctx, cudaStreamSynchronize(st));
     T.mark("local problems");
     ShortcutArgs A;
@@ -1101,6 +1103,10 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
     A.lin_off = P.lin_off;
     A.lin_src = P.lin_src;
     kprof_begin(ctx);
+    if (nwb[3]) {
+      A.jobs = P.hjobs;
+      launch_shortcuts_warp(3, A, nwb[3], st);
+    }
     if (nwb[0]) {
       A.jobs = P.wjobs;
       launch_shortcuts_warp(2, A, nwb[0], st);
@@ -1308,7 +1314,7 @@ void repair_free(SummaryDev& D) {
   dfree(P->pool.val); dfree(P->pool.del); dfree(P->pool2.val); dfree(P->pool2.del);
   dfree(P->jobs); dfree(P->tcl); dfree(P->tc_idx); dfree(P->tc_inner); dfree(P->sp_cl);
   dfree(P->sp_src); dfree(P->wjobs); dfree(P->bjobs); dfree(P->j_warp); dfree(P->j_block);
-  dfree(P->wjobs5); dfree(P->j_warp5);
+  dfree(P->wjobs5); dfree(P->j_warp5); dfree(P->hjobs); dfree(P->j_half);
   dfree(P->lp_off); dfree(P->adj_off); dfree(P->out_off); dfree(P->lin_off); dfree(P->cl_lin);
   dfree(P->adj_nbr); dfree(P->lin_src); dfree(P->div);
   dfree(P->cnt_a); dfree(P->cnt_b); dfree(P->cnt_c); dfree(P->cnt_d);
@@ -1434,6 +1440,8 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
   SG_TRY(dalloc(ctx, &P.bjobs, all));
   SG_TRY(dalloc(ctx, &P.j_warp, all));
   SG_TRY(dalloc(ctx, &P.j_warp5, all));
+  SG_TRY(dalloc(ctx, &P.j_half, all));
+  SG_TRY(dalloc(ctx, &P.hjobs, all));
   SG_TRY(dalloc(ctx, &P.wjobs5, all));
   SG_TRY(dalloc(ctx, &P.j_block, all));
   SG_TRY(dalloc(ctx, &P.tcl, ncl));

@@ -135,7 +135,7 @@ static sg_status reupload(sg_ctx* ctx, SummaryDev& D, T** d, const std::vector<T
 // across calls.  Callers synchronise before returning, so a slot is free
 // again at the next call.
 enum StageSlot {
-  ST_WJOBS, ST_WJOBS5, ST_BJOBS, ST_LINOFF, ST_LINSRC, ST_SPC, ST_SRC, ST_INNER, ST_ADJ, ST_CLOFF,
+  ST_HJOBS, ST_WJOBS, ST_WJOBS5, ST_BJOBS, ST_LINOFF, ST_LINSRC, ST_SPC, ST_SRC, ST_INNER, ST_ADJ, ST_CLOFF,
   ST_ADJOFF, ST_OUTOFF, ST_DIV, ST_VAL, ST_DEL,
   SI_DALL, SI_SEEDS, SI_S2, SP_DIST, ST_SLOTS
 };
@@ -253,36 +253,47 @@ __global__ void __launch_bounds__(128) k_shortcuts(ShortcutArgs A, uint32_t njob
   }
 }
 
-// One warp per supernode job for clusters of at most 32 x NPL local nodes:
-// the same iteration as k_shortcuts (a unit of delta at the entry, Jacobi
-// steps until the members' delta mass is at most thr x members or 101
-// steps) in two phases per step without atomics: members take their delta
-// and publish delta * d / div, then every node sums the published values
-// of its in-edges from members (mirrors keep what they hold).  Lane l owns
-// nodes l, l + 32, ..., and keeps their delta, partial sum, FP64 value,
+// G lanes per supernode job (a warp, or half a warp for two jobs) for
+// clusters of at most G x NPL local nodes: the same iteration as
+// k_shortcuts (a unit of delta at the entry, Jacobi steps until the
+// members' delta mass is at most thr x members or 101 steps) in two phases
+// per step without atomics: members take their delta and publish
+// delta * d / div, then every node sums the published values of its
+// in-edges from members (mirrors keep what they hold).  Lane l of a group
+// owns nodes l, l + G, ..., and keeps their delta, partial sum, FP64 value,
 // d / div and in-edge range in registers; only the published values go
-// through shared memory.
-template <int NPL>
+// through shared memory.  The two jobs of a warp step together until both
+// have stopped; a stopped job's state no longer changes.
+template <int NPL, int G>
 __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t njobs) {
+  constexpr uint32_t JPW = 32 / G;  // jobs per warp
   __shared__ float s_pv[kStageWarps][32 * NPL];
   const uint32_t lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t h = lane / G, sl = lane % G;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   const float d = A.damping;
-  float* pv = s_pv[w];
-  for (uint32_t jj = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; jj < njobs; jj += nwarps) {
-    const uint32_t s = A.jobs[jj];
-    const uint32_t c = A.sp_cluster[s];
-    const uint64_t l0 = A.cl_off[c];
-    const uint32_t L = (uint32_t)(A.cl_off[c + 1] - l0);
-    const uint32_t inner = A.cl_inner[c];
-    const uint32_t src = A.sp_src[s];
-    const uint64_t e_base = A.lin_off[l0];
+  float* pv = s_pv[w] + h * G * NPL;
+  for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * JPW; base < njobs;
+       base += nwarps * JPW) {
+    const uint32_t jj = base + h;
+    const bool valid = jj < njobs;
+    uint32_t s = 0, L = 0, inner = 0, src = 0;
+    uint64_t l0 = 0, e_base = 0;
+    if (valid) {
+      s = A.jobs[jj];
+      const uint32_t c = A.sp_cluster[s];
+      l0 = A.cl_off[c];
+      L = (uint32_t)(A.cl_off[c + 1] - l0);
+      inner = A.cl_inner[c];
+      src = A.sp_src[s];
+      e_base = A.lin_off[l0];
+    }
     float del[NPL], part[NPL], f[NPL];
     double val[NPL];
     uint32_t e0[NPL], e1[NPL];
 #pragma unroll
     for (int t = 0; t < NPL; ++t) {
-      const uint32_t j = lane + 32 * t;
+      const uint32_t j = sl + G * t;
       val[t] = 0.0;
       part[t] = 0.f;
       del[t] = 0.f;
@@ -297,83 +308,99 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
     }
     // an in-mirror entry first sends its unit along its edges into the
     // cluster (through shared memory: its targets belong to other lanes)
-    if (src >= inner) {
+    const bool mirror_src = valid && src >= inner;
+    if (__any_sync(0xffffffffu, mirror_src)) {
 #pragma unroll
       for (int t = 0; t < NPL; ++t)
-        if (lane + 32 * t < L) pv[lane + 32 * t] = 0.f;
+        if (sl + G * t < L) pv[sl + G * t] = 0.f;
       __syncwarp();
-      if (lane == 0) {
+      if (sl == 0 && mirror_src) {
         const float outv = d / A.div[l0 + src];
         for (uint64_t e = A.adj_off[l0 + src]; e < A.adj_off[l0 + src + 1]; ++e)
           pv[A.adj_nbr[e]] += outv;
       }
       __syncwarp();
+      if (mirror_src) {
 #pragma unroll
-      for (int t = 0; t < NPL; ++t) {
-        const uint32_t j = lane + 32 * t;
-        if (j < L) {
-          if (j == src) {
-            val[t] = 1.0;
-            del[t] = 0.f;
-          } else {
-            del[t] = pv[j];
+        for (int t = 0; t < NPL; ++t) {
+          const uint32_t j = sl + G * t;
+          if (j < L) {
+            if (j == src) {
+              val[t] = 1.0;
+              del[t] = 0.f;
+            } else {
+              del[t] = pv[j];
+            }
           }
         }
       }
       __syncwarp();
     }
-    const float thr = f32_at_most(A.thr_per_node * (double)inner);
+    const float thr = valid ? f32_at_most(A.thr_per_node * (double)inner) : 0.f;
     const uint8_t* ls = A.lin_src + e_base;
+    bool active = valid;
     for (int step = 1;; ++step) {
       float diff = 0.f;
       const bool flush = step % kShortcutFlush == 0;
+      if (active) {
 #pragma unroll
-      for (int t = 0; t < NPL; ++t) {
-        const uint32_t j = lane + 32 * t;
-        if (j < inner) {
-          const float ts = del[t];
-          const float p = part[t] + ts;
-          if (flush) {
-            val[t] += widen_f32(p);
-            part[t] = 0.f;
-          } else {
-            part[t] = p;
+        for (int t = 0; t < NPL; ++t) {
+          const uint32_t j = sl + G * t;
+          if (j < inner) {
+            const float ts = del[t];
+            const float p = part[t] + ts;
+            if (flush) {
+              val[t] += widen_f32(p);
+              part[t] = 0.f;
+            } else {
+              part[t] = p;
+            }
+            diff += fabsf(ts);
+            pv[j] = ts * f[t];
           }
-          diff += fabsf(ts);
-          pv[j] = ts * f[t];
         }
       }
       __syncwarp();
+      if (active) {
+#pragma unroll
+        for (int t = 0; t < NPL; ++t) {
+          const uint32_t j = sl + G * t;
+          if (j < L) {
+            float acc = 0.f;
+            for (uint32_t e = e0[t]; e < e1[t]; ++e) acc += pv[ls[e]];
+            del[t] = (j < inner ? 0.f : del[t]) + acc;
+          }
+        }
+      }
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) diff += __shfl_xor_sync(0xffffffffu, diff, o);
+      __syncwarp();
+      if (active && (diff <= thr || step > 100)) active = false;
+      if (!__any_sync(0xffffffffu, active)) break;
+    }
+    if (valid) {
+      const uint64_t o = A.out_off[s];
 #pragma unroll
       for (int t = 0; t < NPL; ++t) {
-        const uint32_t j = lane + 32 * t;
+        const uint32_t j = sl + G * t;
         if (j < L) {
-          float acc = 0.f;
-          for (uint32_t e = e0[t]; e < e1[t]; ++e) acc += pv[ls[e]];
-          del[t] = (j < inner ? 0.f : del[t]) + acc;
+          A.out_value[o + j] = j < inner ? val[t] + widen_f32(part[t]) : val[t];
+          A.out_delta[o + j] = (double)del[t];
         }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) diff += __shfl_xor_sync(0xffffffffu, diff, o);
-      __syncwarp();
-      if (diff <= thr || step > 100) break;
-    }
-    const uint64_t o = A.out_off[s];
-#pragma unroll
-    for (int t = 0; t < NPL; ++t) {
-      const uint32_t j = lane + 32 * t;
-      if (j < L) {
-        A.out_value[o + j] = j < inner ? val[t] + widen_f32(part[t]) : val[t];
-        A.out_delta[o + j] = (double)del[t];
       }
     }
     __syncwarp();
   }
 }
 void launch_shortcuts_warp(int npl, ShortcutArgs A, uint32_t njobs, cudaStream_t st) {
+  if (npl == 3) {
+    k_shortcuts_warp<3, 16><<<grid_for((uint64_t)njobs * 16, 32 * kStageWarps), 32 * kStageWarps, 0,
+                              st>>>(A, njobs);
+    return;
+  }
   const unsigned grid = grid_for((uint64_t)njobs * 32, 32 * kStageWarps);
-  if (npl == 2) k_shortcuts_warp<2><<<grid, 32 * kStageWarps, 0, st>>>(A, njobs);
-  else k_shortcuts_warp<5><<<grid, 32 * kStageWarps, 0, st>>>(A, njobs);
+  if (npl == 2) k_shortcuts_warp<2, 32><<<grid, 32 * kStageWarps, 0, st>>>(A, njobs);
+  else k_shortcuts_warp<5, 32><<<grid, 32 * kStageWarps, 0, st>>>(A, njobs);
 }
 
 // Builds the local problems of the given supernodes, runs the kernel and
@@ -482,12 +509,14 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
         lin_src[cl_lin[k] + cnt[adj_nbr[e]]++] = (uint8_t)i;
   }
   lin_off[cl_off[ncl]] = cl_lin[ncl];
-  std::vector<uint32_t> warp_jobs, warp_jobs5, block_jobs;
+  std::vector<uint32_t> half_jobs, warp_jobs, warp_jobs5, block_jobs;
   size_t maxL_block = 1;
   for (size_t j = 0; j < spids.size(); ++j) {
     const uint32_t k = sp_cluster[j];
     const uint64_t L = cl_off[k + 1] - cl_off[k];
-    if (L <= (uint64_t)kShortcutSmallL) {
+    if (L <= (uint64_t)kShortcutHalfL) {
+      half_jobs.push_back((uint32_t)j);
+    } else if (L <= (uint64_t)kShortcutSmallL) {
       warp_jobs.push_back((uint32_t)j);
     } else if (L <= (uint64_t)kStageCap) {
       warp_jobs5.push_back((uint32_t)j);
@@ -506,7 +535,8 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
   uint32_t *d_wjobs = nullptr, *d_bjobs = nullptr;
   uint64_t* d_linoff = nullptr;
   uint8_t* d_linsrc = nullptr;
-  uint32_t* d_wjobs5 = nullptr;
+  uint32_t *d_wjobs5 = nullptr, *d_hjobs = nullptr;
+  SG_TRY(stage_up(ctx, D, ST_HJOBS, half_jobs, &d_hjobs));
   SG_TRY(stage_up(ctx, D, ST_WJOBS, warp_jobs, &d_wjobs));
   SG_TRY(stage_up(ctx, D, ST_WJOBS5, warp_jobs5, &d_wjobs5));
   SG_TRY(stage_up(ctx, D, ST_BJOBS, block_jobs, &d_bjobs));
@@ -542,6 +572,10 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
     SG_CUDA(ctx, cudaFuncSetAttribute(k_shortcuts, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   kprof_begin(ctx);
+  if (!half_jobs.empty()) {
+    A.jobs = d_hjobs;
+    launch_shortcuts_warp(3, A, (uint32_t)half_jobs.size(), ctx->stream);
+  }
   if (!warp_jobs.empty()) {
     A.jobs = d_wjobs;
     launch_shortcuts_warp(2, A, (uint32_t)warp_jobs.size(), ctx->stream);

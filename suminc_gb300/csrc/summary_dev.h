@@ -117,8 +117,10 @@ __global__ void __launch_bounds__(128) k_sssp_shortcuts(const uint32_t* __restri
                                                         const float* __restrict__ adj_w,
                                                         const uint64_t* __restrict__ out_off,
                                                         double* __restrict__ out, uint32_t njobs);
-// a warp per job for clusters of at most 32 x npl nodes (npl = 2 or 5)
+// a warp per job for clusters of at most 32 x npl nodes (npl = 2 or 5), or
+// half a warp per job for clusters of at most 48 nodes (npl = 3)
 void launch_shortcuts_warp(int npl, ShortcutArgs A, uint32_t njobs, cudaStream_t st);
+constexpr uint32_t kShortcutHalfL = 48;   // clusters the half-warp variant takes
 constexpr uint32_t kShortcutSmallL = 64;  // clusters the npl = 2 variant takes
 
 struct SummaryDev {
