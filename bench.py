@@ -63,6 +63,9 @@ def parse():
     p.add_argument("--batch-frac", type=float, default=0.001)
     p.add_argument("--seed", type=int, default=1)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-community", action="store_true",
+                   help="skip the summarized planted-community sub-record")
+    p.add_argument("--community-batches", type=int, default=3)
     p.add_argument("--summary-batches", type=int, default=2,
                    help="headline workload: batches of the summarized sub-record (0: none)")
     p.add_argument("--ref-budget-s", type=float, default=150.0,
@@ -430,6 +433,9 @@ def run_ours(args, D: Dist):
     summarized = None
     if clusters is not None:
         summarized = summarized_subrecord(args, D, batches, clusters, cl_s)
+    community = None
+    if not args.no_community and D.rank == 0:
+        community = community_subrecord(args, D)
 
     result = {
         "metric": "GTEPS for PR incremental re-eval (IncEval)",
@@ -464,6 +470,8 @@ def run_ours(args, D: Dist):
         result["clocks"] = clk
     if summarized:
         result["summarized"] = summarized
+    if community:
+        result["summarized_community"] = community
     return result, hg, batches, None
 
 
@@ -546,6 +554,67 @@ def summarized_subrecord(args, D, batches, clusters, cl_s):
         "peval_ms": round(pe["elapsed_ms"], 2), "peval_rounds": pe["rounds"],
         "steps": steps,
         "accuracy": {"l1_bound_vs_fixed_point": res / 0.15, "within_tolerance": bool(res / 0.15 <= 1e-5)},
+    }
+
+
+def community_subrecord(args, D):
+    """The summarized path on a graph whose clusters are profitable
+    supernodes: planted communities (batch scale 22: 131,072 communities of
+    40, 5.24 M vertices, 39 M edges) with the communities as the cluster
+    file.  PageRank IncEval after 0.1 % batches, each step the batch's apply
+    (which repairs the summary on the device) on the host clock plus the
+    IncEval on the device, against the plain path on the same batches; then
+    the device-repaired tables against the host restatement."""
+    import oracle
+    import suminc_gb300 as sg
+    n_comm = 1 << max(args.batch_scale - 5, 4)
+    rp, col, _, comms = community_graph(n_comm, 40, args.seed)
+    hg = sg.HostGraph(rp, col)
+    E = len(col)
+    bsz = max(1000, E // 1000)
+    batches = [hg.gen_updates(bsz // 2, bsz - bsz // 2, 0, seed=700 + i)
+               for i in range(args.community_batches)]
+    nrp, ncol, _ = hg.csr()
+    out = {}
+    for mode in (1, 0):
+        ctx = sg.Context(D.local, compress=mode)
+        ctx.load_csr(rp, col)
+        rec = {}
+        if mode:
+            t0 = time.perf_counter()
+            ctx.summary_build(comms)
+            rec["summary_build_s"] = round(time.perf_counter() - t0, 2)
+            info = ctx.summary_info()
+            rec["summary"] = {k: info[k] for k in ("clusters", "supernodes", "shortcut_edges",
+                                                   "boundary_edges", "all_rows")}
+        ctx.pr_peval(out=False)
+        rec["peval_ms"] = round(ctx.stats()["elapsed_ms"], 3)
+        apply_ms, inc_ms = [], []
+        for b in batches:
+            ctx.synchronize()
+            t1 = time.perf_counter()
+            ctx.apply_updates(b)
+            ctx.synchronize()
+            apply_ms.append(round((time.perf_counter() - t1) * 1e3, 3))
+            ctx.pr_inceval_into(None)
+            inc_ms.append(round(ctx.stats()["elapsed_ms"], 3))
+        x = ctx.pr_values()
+        if mode:
+            rec["repair_vs_host_restatement"] = ctx.summary_check()
+        ctx.close()
+        rec["apply_ms"] = apply_ms
+        rec["inceval_ms"] = inc_ms
+        rec["step_ms"] = [round(a + i, 3) for a, i in zip(apply_ms, inc_ms)]
+        rec["l1_bound_vs_fixed_point"] = float(oracle.pr_residual_l1(nrp, ncol, x) / 0.15)
+        out["summarized" if mode else "plain"] = rec
+    s_step = statistics.median(out["summarized"]["step_ms"])
+    p_step = statistics.median(out["plain"]["step_ms"])
+    return {
+        "graph": {"communities": n_comm, "size": 40, "vertices": len(rp) - 1, "edges": E,
+                  "batch_changes": bsz, "clusters": "the planted communities"},
+        "summarized": out["summarized"], "plain": out["plain"],
+        "step_ms_median": {"summarized": round(s_step, 3), "plain": round(p_step, 3),
+                           "summarized_over_plain": round(s_step / p_step, 3)},
     }
 
 
