@@ -145,12 +145,13 @@ def test_summary_save_and_load_reference_file(name, tmp_path):
 
 
 def _mixed_communities(seed=3):
-    """Planted communities of three kinds: 40 members with ~8 inner out-edges
-    each, 200 members (more than a warp-staged cluster holds), and 120
-    members with ~24 inner out-edges each (more local edges than staging
-    holds); three exits per community link to four other communities."""
+    """Planted communities of four kinds: 40 members with ~8 inner out-edges
+    each, 56 members (more than half a warp's solve holds), 200 members (more
+    than a warp-staged cluster holds), and 120 members with ~24 inner
+    out-edges each (more local edges than staging holds); three exits per
+    community link to four other communities."""
     rng = np.random.default_rng(seed)
-    spec = [(40, 8)] * 60 + [(200, 8)] * 6 + [(120, 24)] * 4
+    spec = [(40, 8)] * 60 + [(56, 8)] * 4 + [(200, 8)] * 6 + [(120, 24)] * 4
     rng.shuffle(spec)
     starts = np.cumsum([0] + [s for s, _ in spec])
     n = int(starts[-1])
@@ -196,6 +197,11 @@ def test_summarized_pagerank_staged_and_global_clusters():
             x2 = ctx.pr_inceval()
             assert np.abs(x2 - oracle.pr_fixed_point(nrp, ncol)).sum() <= TOL_FIXED
             assert np.abs(x2 - plain.pr_inceval()).sum() <= TOL_REF
+            # the device repair over every solver variant (cluster sizes up
+            # to 48, 64, 160 nodes and beyond) equals the host restatement
+            chk = ctx.summary_check()
+            for k in ("type_diff", "list_diff", "ib_diff", "is_diff", "corr_diff"):
+                assert chk[k] == 0, chk
 
 
 @pytest.mark.parametrize("name,source", [("planted2600", 0), ("planted2600", 5), ("rmat12", 0)])
