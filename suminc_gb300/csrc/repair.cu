@@ -48,7 +48,6 @@ constexpr uint32_t kNone = 0xFFFFFFFFu;
 struct RepairDev {
   uint32_t n = 0, all_n = 0, ncl = 0;
   uint32_t max_L = 0;           // largest cluster node list
-  uint64_t n_nodes = 0;         // cluster nodes over all clusters
   // fixed after the construction
   uint32_t* cl_of = nullptr;    // [all_n] cluster of each vertex / mirror
   uint32_t* loc = nullptr;      // [all_n] index in its cluster's node list
@@ -1409,7 +1408,6 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
     SG_TRY(put(ctx, &P.im_list, iml));
     SG_TRY(put(ctx, &P.im_master, imm));
   }
-  P.n_nodes = cn.size();
   // marks and fixed-size scratch
   SG_TRY(dalloc(ctx, &P.m_src, n));
   SG_TRY(dalloc(ctx, &P.m_ret, n));

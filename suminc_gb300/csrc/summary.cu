@@ -1334,13 +1334,11 @@ sg_status pr_summarized(sg_ctx* ctx, bool inc) {
     SG_CUDA(ctx, cudaMemcpyAsync(s.delta, dl.data(), 4ull * D->all_n, cudaMemcpyHostToDevice, st));
     SG_CUDA(ctx, cudaStreamSynchronize(st));
     for (uint32_t c = 0; c < D->S.supernode_ids.size(); ++c) cls.push_back(c);
-  } else if (D->rep) {
-    SG_TRY(repair_pending_clusters(ctx, *D, &d_pend, &n_pend));
   } else {
-    cls = D->pending_clusters;
-    D->pending_clusters.clear();
+    // clusters the batches since the last IncEval updated (device marks)
+    SG_TRY(repair_pending_clusters(ctx, *D, &d_pend, &n_pend));
   }
-  if (d_pend) SG_TRY(first_step_dev(ctx, *D, d_pend, n_pend, cnt));
+  if (inc) SG_TRY(first_step_dev(ctx, *D, d_pend, n_pend, cnt));
   else SG_TRY(first_step(ctx, *D, cls, cnt));
   int srounds = 0;
   SG_TRY(summarized_rounds(ctx, *D, cnt, &srounds));

@@ -160,7 +160,6 @@ struct SummaryDev {
   float *bound = nullptr, *spnode = nullptr, *old_x = nullptr;
   double* d_res = nullptr;
   uint32_t* sctl = nullptr;  // summarized rounds: done flag, blocks finished, rounds run
-  std::vector<uint32_t> pending_clusters;  // touched since the last IncEval
   // SSSP over the summary (built by repair.cu on the first query): the
   // summarized CSR and the correction lists
   bool sssp_ready = false;
