@@ -399,6 +399,21 @@ sg_status pr_summarized(sg_ctx* ctx, bool inc);
 // SumSyncIterWorkerPull's in-indexes over the summary, on the device (built
 // on first use after each summary change).  Vertex classes: 0 out node, 1
 // exit only, 2 entry only, 3 entry and exit, 4 inner member.
+// A summary's supernode lists on the device (the repair's slot layout):
+// supernode row r keeps its shortcuts to exits (is), to inner members'
+// values (inner_value) and deltas (inner_delta) at slot[r], with a count per
+// row; row_sp marks supernode rows and row_inner holds their clusters'
+// member counts.
+struct SpLists {
+  const uint64_t* slot = nullptr;
+  const uint8_t* row_sp = nullptr;
+  const uint32_t* row_inner = nullptr;
+  const uint32_t *is_cnt = nullptr, *iv_cnt = nullptr, *id_cnt = nullptr;
+  const uint32_t *is_nbr = nullptr, *iv_nbr = nullptr, *id_nbr = nullptr;
+  const float *is_w = nullptr, *iv_w = nullptr, *id_w = nullptr;
+  uint64_t pool = 0;  // entries of the slot arrays in use
+};
+
 struct PullView {
   uint32_t n = 0;
   const uint8_t* cls = nullptr;
@@ -413,10 +428,7 @@ struct PullView {
   const uint32_t* bd_src = nullptr;  // (the supernode's entry)
   const float* bd_w = nullptr;
   // the correction scatters each entry's supernode lists
-  const uint32_t* corr_sp = nullptr;  // row -> supernode
-  const uint64_t *id_off = nullptr, *iv_off = nullptr;  // per supernode
-  const uint32_t *id_nbr = nullptr, *iv_nbr = nullptr;
-  const float *id_w = nullptr, *iv_w = nullptr;
+  SpLists L;
   uint64_t round_edges = 0;      // entries one summarized round reads
   uint64_t round_shortcuts = 0;  // of which shortcut entries
   uint64_t corr_entries = 0;

@@ -293,13 +293,13 @@ __global__ void __launch_bounds__(kPT) k_pull_spread(PullArgs A) {
   for (uint32_t i = (blockIdx.x * kPT + threadIdx.x) >> 5; i < A.V.n_ent;
        i += (gridDim.x * kPT) >> 5) {
     const uint32_t u = A.V.ent[i];
-    const uint32_t sp = A.V.corr_sp[u];
     const float m = A.spd[u];
-    if (sp == 0xFFFFFFFFu || m == 0.f) continue;
-    for (uint64_t e = A.V.iv_off[sp] + lane; e < A.V.iv_off[sp + 1]; e += 32)
-      atomicAdd(&A.x[A.V.iv_nbr[e]], m * A.V.iv_w[e]);
-    for (uint64_t e = A.V.id_off[sp] + lane; e < A.V.id_off[sp + 1]; e += 32)
-      atomicAdd(&A.delta[A.V.id_nbr[e]], m * A.V.id_w[e]);
+    if (!A.V.L.row_sp[u] || m == 0.f) continue;
+    const uint64_t b = A.V.L.slot[u];
+    for (uint64_t e = b + lane; e < b + A.V.L.iv_cnt[u]; e += 32)
+      atomicAdd(&A.x[A.V.L.iv_nbr[e]], m * A.V.L.iv_w[e]);
+    for (uint64_t e = b + lane; e < b + A.V.L.id_cnt[u]; e += 32)
+      atomicAdd(&A.delta[A.V.L.id_nbr[e]], m * A.V.L.id_w[e]);
   }
 }
 

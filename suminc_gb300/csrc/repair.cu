@@ -77,10 +77,17 @@ struct RepairDev {
   struct Pool {
     double* val = nullptr;  // value of each node of the cluster
     double* del = nullptr;  // residual delta of each node
+    // the row's lists (at most a cluster's node count each): shortcuts to
+    // exits and out-mirrors, inner values, inner deltas
+    uint32_t *is_nbr = nullptr, *iv_nbr = nullptr, *id_nbr = nullptr;
+    float *is_w = nullptr, *iv_w = nullptr, *id_w = nullptr;
     uint64_t cap = 0;
   };
   uint64_t *blk = nullptr, *blk2 = nullptr;
   Pool pool, pool2;
+  uint64_t pool_used = 0;       // entries of the current layout
+  uint32_t *is_cnt = nullptr, *iv_cnt = nullptr, *id_cnt = nullptr;  // [all_n] list lengths
+  uint32_t* row_inner = nullptr;  // [all_n] members of the row's cluster
   uint64_t n_members = 0;       // members over all clusters (cm layout positions)
   // SSSP over the summary (after its first query): distance blocks in the
   // layout of the PageRank blocks, the weights of the ib rows, and whether
@@ -201,6 +208,7 @@ struct RepArgs {
   int32_t* fc;
   uint8_t* ob;
   uint8_t *m_src, *m_ret, *m_new, *c_src, *c_upd, *c_job, *c_pend, *r_job;
+  uint32_t *is_cnt, *iv_cnt, *id_cnt;
   const uint64_t *out_off, *in_off;  // the graph's two directions (live prefix of each row)
   const uint32_t *out_deg, *in_deg, *out_col, *in_col;
   const float* out_w;                // edge weights (null: unweighted)
@@ -319,6 +327,7 @@ __global__ void k_rp_rows(RepArgs R, uint64_t* r_size, uint8_t* f_sp, uint32_t* 
       if (R.c_src[c]) R.r_job[r] = 1;
     } else {
       R.r_job[r] = 0;
+      R.is_cnt[r] = R.iv_cnt[r] = R.id_cnt[r] = 0;
     }
     if (c != kNone && R.c_upd[c]) {
       if (r < R.n) {
@@ -527,27 +536,47 @@ __global__ void k_rp_jobs(RepArgs R, const uint32_t* jobs, uint32_t nj, const ui
   }
 }
 
-// 12. per row (warp): blocks of supernodes whose solve stays move to the
-//     new layout
+// 12. per supernode row (warp): blocks (and lists) of rows whose solve stays
+//     move to the new layout
+struct MoveArgs {
+  const uint64_t *blk, *blk2;
+  const double *val, *del;
+  double *val2, *del2;
+  const uint32_t *is_nbr, *iv_nbr, *id_nbr;  // null: blocks only
+  const float *is_w, *iv_w, *id_w;
+  uint32_t *is_nbr2, *iv_nbr2, *id_nbr2;
+  float *is_w2, *iv_w2, *id_w2;
+};
+
 __global__ void __launch_bounds__(256) k_rp_move(RepArgs R, const uint32_t* sp_rows, uint32_t nsp,
-                                                 const uint64_t* r_size,
-                                                 const uint64_t* blk, const uint64_t* blk2,
-                                                 const double* val, const double* del, double* val2,
-                                                 double* del2, uint32_t* err) {
+                                                 const uint64_t* r_size, MoveArgs M, uint32_t* err) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nsp; k += nw) {
     const uint32_t r = sp_rows[k];
     const uint64_t L = r_size[r];
     if (L == 0 || R.r_job[r]) continue;
-    const uint64_t s = blk[r], t = blk2[r];
-    if (blk[r + 1] - s != L) {  // a kept supernode without a block of its cluster's size
+    const uint64_t s = M.blk[r], t = M.blk2[r];
+    if (M.blk[r + 1] - s != L) {  // a kept supernode without a block of its cluster's size
       if (lane == 0) atomicExch(err, 1u);
       continue;
     }
     for (uint64_t i = lane; i < L; i += 32) {
-      val2[t + i] = val[s + i];
-      del2[t + i] = del[s + i];
+      M.val2[t + i] = M.val[s + i];
+      M.del2[t + i] = M.del[s + i];
+    }
+    if (!M.is_nbr) continue;
+    for (uint32_t i = lane; i < R.is_cnt[r]; i += 32) {
+      M.is_nbr2[t + i] = M.is_nbr[s + i];
+      M.is_w2[t + i] = M.is_w[s + i];
+    }
+    for (uint32_t i = lane; i < R.iv_cnt[r]; i += 32) {
+      M.iv_nbr2[t + i] = M.iv_nbr[s + i];
+      M.iv_w2[t + i] = M.iv_w[s + i];
+    }
+    for (uint32_t i = lane; i < R.id_cnt[r]; i += 32) {
+      M.id_nbr2[t + i] = M.id_nbr[s + i];
+      M.id_w2[t + i] = M.id_w[s + i];
     }
   }
 }
@@ -646,38 +675,21 @@ __global__ void k_rp_seeds(RepArgs R, uint32_t c, const double* dist, uint32_t* 
   }
 }
 
-struct TabArgs {
-  const uint64_t* blk;
-  const double* val;
-  const double* del;
-  uint64_t *is_cnt, *iv_cnt, *id_cnt;
-  const uint64_t *is_off, *iv_off, *id_off;
-  uint32_t *is_nbr, *iv_nbr, *id_nbr;
-  float *is_w, *iv_w, *id_w;
-  uint32_t *corr_sp, *corr_c;
-};
-
 // A supernode's lists (fianl_build_iter_index_for_mirror,
-// iter_compressor.h:433-491): members with a value go to bound_delta (exits)
-// or inner_value (the rest), members with a residual delta to inner_delta,
-// out-mirrors with value + delta to bound_delta.
-// over the supernode rows (the other rows' counts and correction entries are
-// cleared before)
-template <bool FILL>
-__global__ void __launch_bounds__(256) k_rp_tables(RepArgs R, TabArgs T, const uint32_t* sp_rows,
-                                                   uint32_t nsp) {
+// iter_compressor.h:433-491), written into its slot: members with a value go
+// to bound_delta (exits) or inner_value (the rest), members with a residual
+// delta to inner_delta, out-mirrors with value + delta to bound_delta.  A
+// warp per row solved again (the other rows' lists moved with their blocks).
+__global__ void __launch_bounds__(256) k_rp_lists(RepArgs R, const uint32_t* rows, uint32_t nrows,
+                                                  const uint64_t* blk, RepairDev::Pool Q) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nsp; k += nw) {
-    const uint32_t r = sp_rows[k];
+  for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nrows; k += nw) {
+    const uint32_t r = rows[k];
     const uint32_t c = R.cl_of[r];
-    if (!FILL && lane == 0) {
-      T.corr_sp[r] = r;
-      T.corr_c[r] = R.inner[c];
-    }
     const uint32_t L = cl_size(R, c), inner = R.inner[c], om0 = inner + R.n_im[c];
-    const uint64_t b = T.blk[r], n0 = R.cn_off[c];
-    uint64_t nis = 0, niv = 0, nid = 0;
+    const uint64_t b = blk[r], n0 = R.cn_off[c];
+    uint32_t nis = 0, niv = 0, nid = 0;
     for (uint32_t i0 = 0; i0 < L; i0 += 32) {
       const uint32_t i = i0 + lane;
       bool bis = false, biv = false, bid = false;
@@ -685,7 +697,7 @@ __global__ void __launch_bounds__(256) k_rp_tables(RepArgs R, TabArgs T, const u
       uint32_t node = 0;
       if (i < L) {
         node = R.cn[n0 + i];
-        const double v = T.val[b + i], d = T.del[b + i];
+        const double v = Q.val[b + i], d = Q.del[b + i];
         if (i < inner) {
           if (v != 0.0) {
             if (R.ob[node]) { bis = true; wis = (float)v; }
@@ -693,38 +705,36 @@ __global__ void __launch_bounds__(256) k_rp_tables(RepArgs R, TabArgs T, const u
           }
           if (d != 0.0) { bid = true; wid = (float)d; }
         } else if (i >= om0) {
-          const double s = v + d;
-          if (s != 0.0) { bis = true; wis = (float)s; }
+          const double sum = v + d;
+          if (sum != 0.0) { bis = true; wis = (float)sum; }
         }
       }
+      const uint32_t lt = lanemask_lt();
       const uint32_t mis = __ballot_sync(0xffffffffu, bis), miv = __ballot_sync(0xffffffffu, biv),
                      mid = __ballot_sync(0xffffffffu, bid);
-      if (FILL) {
-        const uint32_t lt = lanemask_lt();
-        if (bis) {
-          const uint64_t p = T.is_off[r] + nis + __popc(mis & lt);
-          T.is_nbr[p] = node;
-          T.is_w[p] = wis;
-        }
-        if (biv) {
-          const uint64_t p = T.iv_off[r] + niv + __popc(miv & lt);
-          T.iv_nbr[p] = node;
-          T.iv_w[p] = wiv;
-        }
-        if (bid) {
-          const uint64_t p = T.id_off[r] + nid + __popc(mid & lt);
-          T.id_nbr[p] = node;
-          T.id_w[p] = wid;
-        }
+      if (bis) {
+        const uint64_t p = b + nis + __popc(mis & lt);
+        Q.is_nbr[p] = node;
+        Q.is_w[p] = wis;
+      }
+      if (biv) {
+        const uint64_t p = b + niv + __popc(miv & lt);
+        Q.iv_nbr[p] = node;
+        Q.iv_w[p] = wiv;
+      }
+      if (bid) {
+        const uint64_t p = b + nid + __popc(mid & lt);
+        Q.id_nbr[p] = node;
+        Q.id_w[p] = wid;
       }
       nis += __popc(mis);
       niv += __popc(miv);
       nid += __popc(mid);
     }
-    if (!FILL && lane == 0) {
-      T.is_cnt[r] = nis;
-      T.iv_cnt[r] = niv;
-      T.id_cnt[r] = nid;
+    if (lane == 0) {
+      R.is_cnt[r] = nis;
+      R.iv_cnt[r] = niv;
+      R.id_cnt[r] = nid;
     }
   }
 }
@@ -964,14 +974,26 @@ sg_status grow_keep(sg_ctx* ctx, T** p, uint64_t used, uint64_t* cap, uint64_t n
   return SG_OK;
 }
 
+void free_pool(RepairDev::Pool* p) {
+  dfree(p->val); dfree(p->del);
+  dfree(p->is_nbr); dfree(p->iv_nbr); dfree(p->id_nbr);
+  dfree(p->is_w); dfree(p->iv_w); dfree(p->id_w);
+  p->cap = 0;
+}
+
 sg_status grow_pool(sg_ctx* ctx, RepairDev::Pool* p, uint64_t need) {
   if (need <= p->cap && p->val) return SG_OK;
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  dfree(p->val);
-  dfree(p->del);
+  free_pool(p);
   const uint64_t c = std::max<uint64_t>(need + need / 8, 64);
   SG_TRY(dalloc(ctx, &p->val, c));
   SG_TRY(dalloc(ctx, &p->del, c));
+  SG_TRY(dalloc(ctx, &p->is_nbr, c));
+  SG_TRY(dalloc(ctx, &p->iv_nbr, c));
+  SG_TRY(dalloc(ctx, &p->id_nbr, c));
+  SG_TRY(dalloc(ctx, &p->is_w, c));
+  SG_TRY(dalloc(ctx, &p->iv_w, c));
+  SG_TRY(dalloc(ctx, &p->id_w, c));
   p->cap = c;
   return SG_OK;
 }
@@ -988,6 +1010,7 @@ RepArgs rep_args(sg_ctx* ctx, RepairDev& P) {
   R.fc = P.fc; R.ob = P.ob;
   R.m_src = P.m_src; R.m_ret = P.m_ret; R.m_new = P.m_new;
   R.c_src = P.c_src; R.c_upd = P.c_upd; R.c_job = P.c_job; R.c_pend = P.c_pend; R.r_job = P.r_job;
+  R.is_cnt = P.is_cnt; R.iv_cnt = P.iv_cnt; R.id_cnt = P.id_cnt;
   const DevGraph& g = ctx->g;
   R.out_off = g.out.off; R.out_deg = g.out.deg; R.out_col = g.out.col;
   R.in_off = g.in.off; R.in_deg = g.in.deg; R.in_col = g.in.col;
@@ -1130,19 +1153,39 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
       T.mark("SSSP shortcut distances", st);
     }
   }
-  k_rp_move<<<grid_for((uint64_t)P.n_sp * 32, 256), 256, 0, st>>>(
-      R, P.sp_rows, P.n_sp, P.r_size, P.blk, P.blk2, P.pool.val, P.pool.del, P.pool2.val,
-      P.pool2.del, P.d_err);
-  if (P.sssp_on)
-    k_rp_move<<<grid_for((uint64_t)P.n_sp * 32, 256), 256, 0, st>>>(
-        R, P.sp_rows, P.n_sp, P.r_size, P.blk, P.blk2, P.sd, P.sd, P.sd2, P.sd2, P.d_err);
+  MoveArgs M{};
+  M.blk = P.blk;
+  M.blk2 = P.blk2;
+  M.val = P.pool.val; M.del = P.pool.del; M.val2 = P.pool2.val; M.del2 = P.pool2.del;
+  M.is_nbr = P.pool.is_nbr; M.iv_nbr = P.pool.iv_nbr; M.id_nbr = P.pool.id_nbr;
+  M.is_w = P.pool.is_w; M.iv_w = P.pool.iv_w; M.id_w = P.pool.id_w;
+  M.is_nbr2 = P.pool2.is_nbr; M.iv_nbr2 = P.pool2.iv_nbr; M.id_nbr2 = P.pool2.id_nbr;
+  M.is_w2 = P.pool2.is_w; M.iv_w2 = P.pool2.iv_w; M.id_w2 = P.pool2.id_w;
+  k_rp_move<<<grid_for((uint64_t)P.n_sp * 32, 256), 256, 0, st>>>(R, P.sp_rows, P.n_sp, P.r_size, M,
+                                                                  P.d_err);
+  if (P.sssp_on) {
+    MoveArgs Ms{};
+    Ms.blk = P.blk;
+    Ms.blk2 = P.blk2;
+    Ms.val = Ms.del = P.sd;
+    Ms.val2 = Ms.del2 = P.sd2;
+    k_rp_move<<<grid_for((uint64_t)P.n_sp * 32, 256), 256, 0, st>>>(R, P.sp_rows, P.n_sp, P.r_size,
+                                                                    Ms, P.d_err);
+  }
   count_launch(ctx, 1 + P.sssp_on);
   SG_CUDA(ctx, cudaGetLastError());
   std::swap(P.blk, P.blk2);
   std::swap(P.pool, P.pool2);
   std::swap(P.sd, P.sd2);
   std::swap(P.sd_cap, P.sd2_cap);
+  P.pool_used = total;
   P.sk_stale = true;
+  // the lists of the rows solved again, in their new slots
+  if (nj) {
+    k_rp_lists<<<grid_for((uint64_t)nj * 32, 256), 256, 0, st>>>(R, P.jobs, nj, P.blk, P.pool);
+    count_launch(ctx);
+    SG_CUDA(ctx, cudaGetLastError());
+  }
   T.mark("blocks moved", st);
   (void)D;
   return SG_OK;
@@ -1156,11 +1199,6 @@ sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, 
   SG_TRY(reserve(ctx, D, &D.l_entry, n));
   SG_TRY(reserve(ctx, D, &D.l_exit, n));
   SG_TRY(reserve(ctx, D, &D.l_single, n));
-  SG_TRY(reserve(ctx, D, &D.corr_sp, all));
-  SG_TRY(reserve(ctx, D, &D.corr_c, all));
-  SG_TRY(reserve(ctx, D, &D.is_off, (uint64_t)all + 1));
-  SG_TRY(reserve(ctx, D, &D.iv_off, (uint64_t)all + 1));
-  SG_TRY(reserve(ctx, D, &D.id_off, (uint64_t)all + 1));
   SG_TRY(reserve(ctx, D, &D.ib_off, (uint64_t)all + 1));
   k_rp_types<<<grid_for(n, 256), 256, 0, st>>>(R, D.ntype, P.f_entry, P.f_exit, P.f_single);
   SG_TRY(select_idx(ctx, P.f_entry, D.l_entry, P.d_num, n));
@@ -1168,32 +1206,13 @@ sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, 
   SG_TRY(select_idx(ctx, P.f_single, D.l_single, P.d_num + 2, n));
   uint32_t nl[3] = {0, 0, 0};
   SG_CUDA(ctx, cudaMemcpyAsync(nl, P.d_num, 12, cudaMemcpyDeviceToHost, st));
-  SG_CUDA(ctx, cudaMemsetAsync(P.cnt_a, 0, 8ull * (all + 1), st));
-  SG_CUDA(ctx, cudaMemsetAsync(P.cnt_b, 0, 8ull * (all + 1), st));
-  SG_CUDA(ctx, cudaMemsetAsync(P.cnt_c, 0, 8ull * (all + 1), st));
   SG_CUDA(ctx, cudaMemsetAsync(P.cnt_d, 0, 8ull * (all + 1), st));
-  SG_CUDA(ctx, cudaMemsetAsync(D.corr_sp, 0xFF, 4ull * all, st));
-  SG_CUDA(ctx, cudaMemsetAsync(D.corr_c, 0, 4ull * all, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   D.n_entry = nl[0];
   D.n_exit = nl[1];
   D.n_single = nl[2];
   PT.mark("node types and lists", st);
-  // supernode lists and the correction tables
-  TabArgs T{};
-  T.blk = P.blk;
-  T.val = P.pool.val;
-  T.del = P.pool.del;
-  T.is_cnt = P.cnt_a;
-  T.iv_cnt = P.cnt_b;
-  T.id_cnt = P.cnt_c;
-  T.corr_sp = D.corr_sp;
-  T.corr_c = D.corr_c;
-  const unsigned rg = grid_for((uint64_t)P.n_sp * 32, 256);
-  k_rp_tables<false><<<rg, 256, 0, st>>>(R, T, P.sp_rows, P.n_sp);
-  SG_TRY(scan_u64(ctx, P.cnt_a, D.is_off, (uint64_t)all + 1));
-  SG_TRY(scan_u64(ctx, P.cnt_b, D.iv_off, (uint64_t)all + 1));
-  SG_TRY(scan_u64(ctx, P.cnt_c, D.id_off, (uint64_t)all + 1));
+  // boundary rows of exits and unclustered vertices
   if (D.n_exit)
     k_rp_ib<false><<<grid_for(D.n_exit, 256), 256, 0, st>>>(R, D.ntype, D.l_exit, D.n_exit, P.cnt_d,
                                                             nullptr, nullptr, nullptr);
@@ -1201,32 +1220,12 @@ sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, 
     k_rp_ib<false><<<grid_for(D.n_single, 256), 256, 0, st>>>(R, D.ntype, D.l_single, D.n_single,
                                                               P.cnt_d, nullptr, nullptr, nullptr);
   SG_TRY(scan_u64(ctx, P.cnt_d, D.ib_off, (uint64_t)all + 1));
-  uint64_t tot[4] = {0, 0, 0, 0};
-  SG_CUDA(ctx, cudaMemcpyAsync(&tot[0], D.is_off + all, 8, cudaMemcpyDeviceToHost, st));
-  SG_CUDA(ctx, cudaMemcpyAsync(&tot[1], D.iv_off + all, 8, cudaMemcpyDeviceToHost, st));
-  SG_CUDA(ctx, cudaMemcpyAsync(&tot[2], D.id_off + all, 8, cudaMemcpyDeviceToHost, st));
-  SG_CUDA(ctx, cudaMemcpyAsync(&tot[3], D.ib_off + all, 8, cudaMemcpyDeviceToHost, st));
-  SG_CUDA(ctx, cudaStreamSynchronize(st));
-  SG_TRY(reserve(ctx, D, &D.is_nbr, tot[0]));
-  SG_TRY(reserve(ctx, D, &D.is_w, tot[0]));
-  SG_TRY(reserve(ctx, D, &D.iv_nbr, tot[1]));
-  SG_TRY(reserve(ctx, D, &D.iv_w, tot[1]));
-  SG_TRY(reserve(ctx, D, &D.id_nbr, tot[2]));
-  SG_TRY(reserve(ctx, D, &D.id_w, tot[2]));
-  SG_TRY(reserve(ctx, D, &D.ib_nbr, tot[3]));
-  T.is_off = D.is_off;
-  T.iv_off = D.iv_off;
-  T.id_off = D.id_off;
-  T.is_nbr = D.is_nbr;
-  T.is_w = D.is_w;
-  T.iv_nbr = D.iv_nbr;
-  T.iv_w = D.iv_w;
-  T.id_nbr = D.id_nbr;
-  T.id_w = D.id_w;
-  k_rp_tables<true><<<rg, 256, 0, st>>>(R, T, P.sp_rows, P.n_sp);
+  uint64_t nib = 0;
+  SG_TRY(read_u64(ctx, D.ib_off + all, &nib));
+  SG_TRY(reserve(ctx, D, &D.ib_nbr, nib));
   float* ibw = nullptr;
   if (R.out_w) {
-    SG_TRY(grow(ctx, &P.ib_w, &P.ib_w_cap, tot[3]));
+    SG_TRY(grow(ctx, &P.ib_w, &P.ib_w_cap, nib));
     ibw = P.ib_w;
   }
   if (D.n_exit)
@@ -1235,7 +1234,7 @@ sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, 
   if (D.n_single)
     k_rp_ib<true><<<grid_for(D.n_single, 256), 256, 0, st>>>(R, D.ntype, D.l_single, D.n_single,
                                                              nullptr, D.ib_off, D.ib_nbr, ibw);
-  PT.mark("supernode lists and ib rows", st);
+  PT.mark("ib rows", st);
   // cluster precompute lists
   CmArgs C{};
   C.cm_off = D.cm_off;
@@ -1421,6 +1420,15 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
   SG_TRY(dalloc(ctx, &P.c_pend, ncl));
   SG_TRY(dalloc(ctx, &P.r_job, all));
   SG_TRY(dalloc(ctx, &P.f_sp, all));
+  SG_TRY(dalloc(ctx, &P.is_cnt, all));
+  SG_TRY(dalloc(ctx, &P.iv_cnt, all));
+  SG_TRY(dalloc(ctx, &P.id_cnt, all));
+  {
+    std::vector<uint32_t> ri(all, 0);
+    for (uint32_t r = 0; r < all; ++r)
+      if (cl_of[r] != kNone) ri[r] = inner[cl_of[r]];
+    SG_TRY(put(ctx, &P.row_inner, ri));
+  }
   SG_TRY(dalloc(ctx, &P.f_corr, all));
   SG_TRY(dalloc(ctx, &P.src_dist, std::max<uint32_t>(P.max_L, 1)));
   SG_TRY(dalloc(ctx, &P.seed_v, std::max<uint32_t>(P.max_L, 1)));
@@ -1466,6 +1474,9 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
   SG_CUDA(ctx, cudaMemsetAsync(P.c_job, 0, ncl, st));
   SG_CUDA(ctx, cudaMemsetAsync(P.c_pend, 0, ncl, st));
   SG_CUDA(ctx, cudaMemsetAsync(P.r_job, 0, all, st));
+  SG_CUDA(ctx, cudaMemsetAsync(P.is_cnt, 0, 4ull * all, st));
+  SG_CUDA(ctx, cudaMemsetAsync(P.iv_cnt, 0, 4ull * all, st));
+  SG_CUDA(ctx, cudaMemsetAsync(P.id_cnt, 0, 4ull * all, st));
   SG_CUDA(ctx, cudaMemsetAsync(P.blk, 0, 8ull * (all + 1), st));
   SG_CUDA(ctx, cudaMemsetAsync(P.cnt_a, 0, 8ull * nc, st));
   SG_CUDA(ctx, cudaMemsetAsync(P.cnt_b, 0, 8ull * nc, st));
@@ -1542,6 +1553,26 @@ sg_status repair_pending_clusters(sg_ctx* ctx, SummaryDev& D, const uint32_t** l
 
 
 bool repair_active(const SummaryDev& D) { return D.rep != nullptr; }
+
+SpLists repair_lists(const SummaryDev& D) {
+  SpLists L;
+  const RepairDev* P = D.rep;
+  if (!P) return L;
+  L.slot = P->blk;
+  L.row_sp = P->f_sp;
+  L.row_inner = P->row_inner;
+  L.is_cnt = P->is_cnt;
+  L.iv_cnt = P->iv_cnt;
+  L.id_cnt = P->id_cnt;
+  L.is_nbr = P->pool.is_nbr;
+  L.iv_nbr = P->pool.iv_nbr;
+  L.id_nbr = P->pool.id_nbr;
+  L.is_w = P->pool.is_w;
+  L.iv_w = P->pool.iv_w;
+  L.id_w = P->pool.id_w;
+  L.pool = P->pool_used;
+  return L;
+}
 
 namespace {
 

@@ -44,13 +44,11 @@ void host_adj_from_csr(uint32_t n, const uint64_t* rp, const uint32_t* col, cons
 static SummaryDev* sdev(sg_ctx* ctx) { return (SummaryDev*)ctx->summary; }
 
 static void sfree(SummaryDev& D) {
-  dfree(D.is_off); dfree(D.ib_off); dfree(D.sync_off);
-  dfree(D.is_nbr); dfree(D.ib_nbr); dfree(D.sync_nbr); dfree(D.is_w);
+  dfree(D.ib_off); dfree(D.sync_off);
+  dfree(D.ib_nbr); dfree(D.sync_nbr);
   dfree(D.out_deg_all);
   dfree(D.l_entry); dfree(D.l_exit); dfree(D.l_single); dfree(D.l_omirror);
   dfree(D.omirror_master); dfree(D.ntype);
-  dfree(D.corr_sp); dfree(D.corr_c);
-  dfree(D.id_off); dfree(D.iv_off); dfree(D.id_nbr); dfree(D.iv_nbr); dfree(D.id_w); dfree(D.iv_w);
   dfree(D.cm_off); dfree(D.sub_off); dfree(D.cm_v); dfree(D.sub_nbr);
   dfree(D.lin_off); dfree(D.lin_src); dfree(D.lout_off); dfree(D.lout_dst);
   dfree(D.bound_list); dfree(D.bl_off);
@@ -631,9 +629,6 @@ static sg_status compute_shortcuts(sg_ctx* ctx, SummaryDev& D, const std::vector
 static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
   Summary& S = D.S;
   const uint32_t all = S.all_n, n = S.old_n;
-  SG_TRY(reupload(ctx, D, &D.is_off, S.is_off));
-  SG_TRY(reupload(ctx, D, &D.is_nbr, S.is_nbr));
-  SG_TRY(reupload(ctx, D, &D.is_w, S.is_w));
   SG_TRY(reupload(ctx, D, &D.ib_off, S.ib_off));
   SG_TRY(reupload(ctx, D, &D.ib_nbr, S.ib_nbr));
   SG_TRY(reupload(ctx, D, &D.sync_off, S.sync_off));
@@ -667,47 +662,8 @@ static sg_status upload_sketch(sg_ctx* ctx, SummaryDev& D) {
   SG_TRY(reupload(ctx, D, &D.l_omirror, om));
   SG_TRY(reupload(ctx, D, &D.omirror_master, omm));
   D.n_omirror = (uint32_t)om.size();
-  // correction tables
-  std::vector<uint32_t> csp(all, 0xFFFFFFFFu), cc(all, 0);
-  const size_t nsp = S.supernodes.size();
-  std::vector<uint64_t> ido(nsp + 1, 0), ivo(nsp + 1, 0);
-  for (size_t sp = 0; sp < nsp; ++sp) {
-    ido[sp + 1] = ido[sp] + S.supernodes[sp].inner_delta.size();
-    ivo[sp + 1] = ivo[sp] + S.supernodes[sp].inner_value.size();
-  }
-  hvec<uint32_t> idn(ido[nsp]), ivn(ivo[nsp]);
-  hvec<float> idw(ido[nsp]), ivw(ivo[nsp]);
-#pragma omp parallel for schedule(dynamic, 1024)
-  for (long long sp = 0; sp < (long long)nsp; ++sp) {
-    const Supernode& s = S.supernodes[sp];
-    uint64_t k = ido[sp];
-    for (auto& e : s.inner_delta) {
-      idn[k] = e.first;
-      idw[k++] = (float)e.second;
-    }
-    k = ivo[sp];
-    for (auto& e : s.inner_value) {
-      ivn[k] = e.first;
-      ivw[k++] = (float)e.second;
-    }
-  }
-#pragma omp parallel for schedule(static)
-  for (long long uu = 0; uu < (long long)all; ++uu) {
-    const uint32_t u = (uint32_t)uu;
-    const uint32_t sp = S.Fc_map[u];
-    if (sp == Summary::kIdDefault || sp >= nsp) continue;
-    if (S.supernodes[sp].id != u) continue;
-    csp[u] = sp;
-    cc[u] = (uint32_t)S.supernode_ids[S.id2spids[u]].size();
-  }
-  SG_TRY(reupload(ctx, D, &D.corr_sp, csp));
-  SG_TRY(reupload(ctx, D, &D.corr_c, cc));
-  SG_TRY(reupload(ctx, D, &D.id_off, ido));
-  SG_TRY(reupload(ctx, D, &D.iv_off, ivo));
-  SG_TRY(reupload(ctx, D, &D.id_nbr, idn));
-  SG_TRY(reupload(ctx, D, &D.iv_nbr, ivn));
-  SG_TRY(reupload(ctx, D, &D.id_w, idw));
-  SG_TRY(reupload(ctx, D, &D.iv_w, ivw));
+  // the supernode lists (shortcuts and correction) live in the device
+  // repair's slots (repair_init)
   // Cluster members, exits and the precompute lists, all per member
   // position of the cm layout, built in two parallel passes (counts, then
   // fills at prefix offsets).  Clusters of at most kStageCap members get
@@ -890,9 +846,9 @@ struct SumArgs {
   float* delta;
   float* bound;
   float* spnode;
-  const uint64_t *is_off, *ib_off, *sync_off;
-  const uint32_t *is_nbr, *ib_nbr, *sync_nbr;
-  const float* is_w;
+  const uint64_t *ib_off, *sync_off;
+  const uint32_t *ib_nbr, *sync_nbr;
+  SpLists L;  // supernode lists (slot layout)
   const uint32_t* out_deg_all;
   const uint8_t* ntype;
   unsigned long long* cnt;  // [0] edges, [1] shortcut edges
@@ -911,11 +867,11 @@ __device__ __forceinline__ bool rounds_done(const SumArgs& A) {
 // mass a (mirror) entry receives goes along its shortcuts into exit buffers
 __device__ __forceinline__ void entry_push(const SumArgs& A, uint32_t u, float d, uint32_t lane,
                                            unsigned long long& sc) {
-  for (uint64_t e = A.is_off[u] + lane; e < A.is_off[u + 1]; e += 32)
-    atomicAdd(&A.bound[A.is_nbr[e]], A.is_w[e] * d);
+  const uint64_t b = A.L.slot[u], e1 = b + A.L.is_cnt[u];
+  for (uint64_t e = b + lane; e < e1; e += 32) atomicAdd(&A.bound[A.L.is_nbr[e]], A.L.is_w[e] * d);
   if (lane == 0) {
     atomicAdd(&A.spnode[u], d);
-    sc += A.is_off[u + 1] - A.is_off[u];
+    sc += e1 - b;
   }
 }
 
@@ -1038,22 +994,18 @@ __global__ void __launch_bounds__(256) k_sum_residual_decide(SumArgs A, uint32_t
 }
 
 // correction through inner_delta / inner_value (warp per row)
-__global__ void __launch_bounds__(256) k_sum_correct(SumArgs A, uint32_t all_n, const uint32_t* corr_sp,
-                                                     const uint32_t* corr_c, const uint64_t* id_off,
-                                                     const uint32_t* id_nbr, const float* id_w,
-                                                     const uint64_t* iv_off, const uint32_t* iv_nbr,
-                                                     const float* iv_w) {
+__global__ void __launch_bounds__(256) k_sum_correct(SumArgs A, uint32_t all_n) {
   const uint32_t lane = threadIdx.x & 31;
   for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < all_n;
        u += (gridDim.x * blockDim.x) >> 5) {
-    const uint32_t sp = corr_sp[u];
-    if (sp == 0xFFFFFFFFu) continue;
+    if (!A.L.row_sp[u]) continue;
     const float d = A.spnode[u];
-    if (!(fabsf(d) * (float)corr_c[u] > A.thr_v)) continue;
-    for (uint64_t e = id_off[sp] + lane; e < id_off[sp + 1]; e += 32)
-      atomicAdd(&A.delta[id_nbr[e]], d * id_w[e]);
-    for (uint64_t e = iv_off[sp] + lane; e < iv_off[sp + 1]; e += 32)
-      atomicAdd(&A.x[iv_nbr[e]], d * iv_w[e]);
+    if (!(fabsf(d) * (float)A.L.row_inner[u] > A.thr_v)) continue;
+    const uint64_t b = A.L.slot[u];
+    for (uint64_t e = b + lane; e < b + A.L.id_cnt[u]; e += 32)
+      atomicAdd(&A.delta[A.L.id_nbr[e]], d * A.L.id_w[e]);
+    for (uint64_t e = b + lane; e < b + A.L.iv_cnt[u]; e += 32)
+      atomicAdd(&A.x[A.L.iv_nbr[e]], d * A.L.iv_w[e]);
     __syncwarp();
     if (lane == 0) A.spnode[u] = 0.f;
   }
@@ -1211,9 +1163,9 @@ static SumArgs sum_args(sg_ctx* ctx, SummaryDev& D, unsigned long long* cnt) {
   A.delta = ctx->pr.delta;
   A.bound = D.bound;
   A.spnode = D.spnode;
-  A.is_off = D.is_off; A.ib_off = D.ib_off; A.sync_off = D.sync_off;
-  A.is_nbr = D.is_nbr; A.ib_nbr = D.ib_nbr; A.sync_nbr = D.sync_nbr;
-  A.is_w = D.is_w;
+  A.ib_off = D.ib_off; A.sync_off = D.sync_off;
+  A.ib_nbr = D.ib_nbr; A.sync_nbr = D.sync_nbr;
+  A.L = repair_lists(D);
   A.out_deg_all = D.out_deg_all;
   A.ntype = D.ntype;
   A.cnt = cnt;
@@ -1294,8 +1246,7 @@ static sg_status summarized_rounds(sg_ctx* ctx, SummaryDev& D, unsigned long lon
     if (h_ctl[0]) break;
   }
   const int r = (int)h_ctl[2];
-  k_sum_correct<<<grid_for((uint64_t)D.all_n * 32, 256), 256, 0, st>>>(
-      A, D.all_n, D.corr_sp, D.corr_c, D.id_off, D.id_nbr, D.id_w, D.iv_off, D.iv_nbr, D.iv_w);
+  k_sum_correct<<<grid_for((uint64_t)D.all_n * 32, 256), 256, 0, st>>>(A, D.all_n);
   count_launch(ctx);
   SG_CUDA(ctx, cudaGetLastError());
   SG_CUDA(ctx, cudaStreamSynchronize(st));
@@ -1604,9 +1555,7 @@ static sg_status pull_index_build(sg_ctx* ctx, SummaryDev& D) {
   V.n_ent = (uint32_t)ent.size();
   V.ie_off = D.p_ie_off; V.ie_nbr = D.p_ie_nbr;
   V.bd_off = D.p_bd_off; V.bd_src = D.p_bd_src; V.bd_w = D.p_bd_w;
-  V.corr_sp = D.corr_sp;
-  V.id_off = D.id_off; V.id_nbr = D.id_nbr; V.id_w = D.id_w;
-  V.iv_off = D.iv_off; V.iv_nbr = D.iv_nbr; V.iv_w = D.iv_w;
+  V.L = repair_lists(D);
   V.round_edges = round_edges;
   V.round_shortcuts = bd_off[n];
   V.corr_entries = corr;
@@ -1676,15 +1625,17 @@ sg_status summary_check(sg_ctx* ctx, sg_summary_check* o) {
   SummaryDev& D = *Dp;
   const Summary& S = D.S;
   const uint32_t n = S.old_n, all = S.all_n;
-  std::vector<uint8_t> nt;
-  std::vector<uint64_t> ibo, iso, ivo, ido;
-  std::vector<uint32_t> le, lx, ls, csp;
+  const SpLists L = repair_lists(D);
+  std::vector<uint8_t> nt, rsp;
+  std::vector<uint64_t> ibo, slot;
+  std::vector<uint32_t> le, lx, ls, isc, ivc, idc;
   SG_TRY(fetch(ctx, D.ntype, n, &nt));
   SG_TRY(fetch(ctx, D.ib_off, (uint64_t)all + 1, &ibo));
-  SG_TRY(fetch(ctx, D.is_off, (uint64_t)all + 1, &iso));
-  SG_TRY(fetch(ctx, D.iv_off, (uint64_t)all + 1, &ivo));
-  SG_TRY(fetch(ctx, D.id_off, (uint64_t)all + 1, &ido));
-  SG_TRY(fetch(ctx, D.corr_sp, all, &csp));
+  SG_TRY(fetch(ctx, L.slot, all, &slot));
+  SG_TRY(fetch(ctx, L.row_sp, all, &rsp));
+  SG_TRY(fetch(ctx, L.is_cnt, all, &isc));
+  SG_TRY(fetch(ctx, L.iv_cnt, all, &ivc));
+  SG_TRY(fetch(ctx, L.id_cnt, all, &idc));
   SG_TRY(fetch(ctx, D.l_entry, D.n_entry, &le));
   SG_TRY(fetch(ctx, D.l_exit, D.n_exit, &lx));
   SG_TRY(fetch(ctx, D.l_single, D.n_single, &ls));
@@ -1692,12 +1643,12 @@ sg_status summary_check(sg_ctx* ctx, sg_summary_check* o) {
   std::vector<uint32_t> ibn, isn, ivn, idn;
   std::vector<float> isw, ivw, idw;
   SG_TRY(fetch(ctx, D.ib_nbr, ibo[all], &ibn));
-  SG_TRY(fetch(ctx, D.is_nbr, iso[all], &isn));
-  SG_TRY(fetch(ctx, D.is_w, iso[all], &isw));
-  SG_TRY(fetch(ctx, D.iv_nbr, ivo[all], &ivn));
-  SG_TRY(fetch(ctx, D.iv_w, ivo[all], &ivw));
-  SG_TRY(fetch(ctx, D.id_nbr, ido[all], &idn));
-  SG_TRY(fetch(ctx, D.id_w, ido[all], &idw));
+  SG_TRY(fetch(ctx, L.is_nbr, L.pool, &isn));
+  SG_TRY(fetch(ctx, L.is_w, L.pool, &isw));
+  SG_TRY(fetch(ctx, L.iv_nbr, L.pool, &ivn));
+  SG_TRY(fetch(ctx, L.iv_w, L.pool, &ivw));
+  SG_TRY(fetch(ctx, L.id_nbr, L.pool, &idn));
+  SG_TRY(fetch(ctx, L.id_w, L.pool, &idw));
   SG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   o->rows = all;
   std::vector<uint32_t> he, hx, hs;
@@ -1725,27 +1676,30 @@ sg_status summary_check(sg_ctx* ctx, sg_summary_check* o) {
     }
     return true;
   };
-  auto dev_row = [](const std::vector<uint64_t>& off, const std::vector<uint32_t>& nbr,
-                    const std::vector<float>* w, uint32_t r) {
+  // a device row: cnt entries at the row's slot (none for other rows)
+  auto dev_row = [&](const std::vector<uint32_t>& nbr, const std::vector<float>* w,
+                     const std::vector<uint32_t>& cnt, uint32_t r) {
     std::vector<std::pair<uint32_t, double>> x;
-    for (uint64_t e = off[r]; e < off[r + 1]; ++e) x.push_back({nbr[e], w ? (double)(*w)[e] : 0.0});
+    if (!rsp[r]) return x;
+    for (uint64_t e = slot[r]; e < slot[r] + cnt[r]; ++e)
+      x.push_back({nbr[e], w ? (double)(*w)[e] : 0.0});
     return x;
   };
   for (uint32_t r = 0; r < all; ++r) {
     {
-      std::vector<std::pair<uint32_t, double>> h;
+      std::vector<std::pair<uint32_t, double>> h, d;
       for (uint64_t e = S.ib_off[r]; e < S.ib_off[r + 1]; ++e) h.push_back({S.ib_nbr[e], 0.0});
-      if (!same(dev_row(ibo, ibn, nullptr, r), h)) o->ib_diff++;
+      for (uint64_t e = ibo[r]; e < ibo[r + 1]; ++e) d.push_back({ibn[e], 0.0});
+      if (!same(d, h)) o->ib_diff++;
     }
     {
       std::vector<std::pair<uint32_t, double>> h;
       for (uint64_t e = S.is_off[r]; e < S.is_off[r + 1]; ++e) h.push_back({S.is_nbr[e], (double)S.is_w[e]});
-      if (!same(dev_row(iso, isn, &isw, r), h)) o->is_diff++;
+      if (!same(dev_row(isn, &isw, isc, r), h)) o->is_diff++;
     }
     const uint32_t sp = S.Fc_map[r];
     const bool hsp = sp != Summary::kIdDefault && sp < S.supernodes.size() && S.supernodes[sp].id == r;
-    const bool dsp = csp[r] != 0xFFFFFFFFu;
-    if (hsp != dsp) {
+    if (hsp != (rsp[r] != 0)) {
       o->corr_diff++;
       continue;
     }
@@ -1755,7 +1709,8 @@ sg_status summary_check(sg_ctx* ctx, sg_summary_check* o) {
         hd(h.inner_delta.begin(), h.inner_delta.end());
     for (auto& e : hv) e.second = (double)(float)e.second;
     for (auto& e : hd) e.second = (double)(float)e.second;
-    if (!same(dev_row(ivo, ivn, &ivw, r), hv) || !same(dev_row(ido, idn, &idw, r), hd)) o->corr_diff++;
+    if (!same(dev_row(ivn, &ivw, ivc, r), hv) || !same(dev_row(idn, &idw, idc, r), hd))
+      o->corr_diff++;
   }
   o->max_rel = max_rel;
   return SG_OK;

@@ -133,20 +133,14 @@ struct SummaryDev {
   // lags behind by the batches in the repair's action log; host_sync
   // replays them before anything reads S.
   RepairDev* rep = nullptr;
-  // device sketch
-  uint64_t *is_off = nullptr, *ib_off = nullptr, *sync_off = nullptr;
-  uint32_t *is_nbr = nullptr, *ib_nbr = nullptr, *sync_nbr = nullptr;
-  float* is_w = nullptr;
+  // device sketch (the supernode lists live in the repair's slots)
+  uint64_t *ib_off = nullptr, *sync_off = nullptr;
+  uint32_t *ib_nbr = nullptr, *sync_nbr = nullptr;
   uint32_t* out_deg_all = nullptr;       // out-degree of each row (mirrors: master's)
   uint32_t *l_entry = nullptr, *l_exit = nullptr, *l_single = nullptr, *l_omirror = nullptr;
   uint32_t n_entry = 0, n_exit = 0, n_single = 0, n_omirror = 0;
   uint32_t* omirror_master = nullptr;
   uint8_t* ntype = nullptr;
-  // correction: per row -> supernode, cluster size; supernode CSRs
-  uint32_t *corr_sp = nullptr, *corr_c = nullptr;
-  uint64_t *id_off = nullptr, *iv_off = nullptr;
-  uint32_t *id_nbr = nullptr, *iv_nbr = nullptr;
-  float *id_w = nullptr, *iv_w = nullptr;
   // cluster precompute: members (cm layout: clusters in order) and, per
   // member position, the subgraph out-edges of clusters that are not staged
   uint64_t *cm_off = nullptr, *sub_off = nullptr;
@@ -198,6 +192,7 @@ struct SummaryDev {
 sg_status repair_init(sg_ctx* ctx, SummaryDev& D);
 sg_status repair_after_apply(sg_ctx* ctx, SummaryDev& D);
 sg_status repair_pending_clusters(sg_ctx* ctx, SummaryDev& D, const uint32_t** list, uint32_t* count);
+SpLists repair_lists(const SummaryDev& D);
 uint64_t repair_logged_actions(const SummaryDev& D);
 uint64_t repair_logged_batches(const SummaryDev& D);
 sg_status repair_take_log(sg_ctx* ctx, SummaryDev& D, std::vector<uint32_t>* src,
