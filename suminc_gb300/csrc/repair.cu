@@ -43,6 +43,7 @@ namespace sg {
 
 namespace {
 constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr uint64_t kNoSlot = ~0ull;  // a row without a block
 }
 
 struct RepairDev {
@@ -85,7 +86,10 @@ struct RepairDev {
   };
   uint64_t *blk = nullptr, *blk2 = nullptr;
   Pool pool, pool2;
-  uint64_t pool_used = 0;       // entries of the current layout
+  uint64_t pool_used = 0;       // slots handed out (the pool tail)
+  uint64_t live_at_layout = 0;  // live entries at the last new layout
+  uint64_t relayouts = 0;
+  unsigned long long* d_tail = nullptr;  // device copy of the pool tail
   uint32_t *is_cnt = nullptr, *iv_cnt = nullptr, *id_cnt = nullptr;  // [all_n] list lengths
   uint32_t* row_inner = nullptr;  // [all_n] members of the row's cluster
   uint64_t n_members = 0;       // members over all clusters (cm layout positions)
@@ -209,6 +213,7 @@ struct RepArgs {
   uint8_t* ob;
   uint8_t *m_src, *m_ret, *m_new, *c_src, *c_upd, *c_job, *c_pend, *r_job;
   uint32_t *is_cnt, *iv_cnt, *id_cnt;
+  uint64_t* slot;  // block of each row (kNoSlot: none)
   const uint64_t *out_off, *in_off;  // the graph's two directions (live prefix of each row)
   const uint32_t *out_deg, *in_deg, *out_col, *in_col;
   const float* out_w;                // edge weights (null: unweighted)
@@ -328,6 +333,7 @@ __global__ void k_rp_rows(RepArgs R, uint64_t* r_size, uint8_t* f_sp, uint32_t* 
     } else {
       R.r_job[r] = 0;
       R.is_cnt[r] = R.iv_cnt[r] = R.id_cnt[r] = 0;
+      R.slot[r] = kNoSlot;  // a retired supernode's block becomes a hole
     }
     if (c != kNone && R.c_upd[c]) {
       if (r < R.n) {
@@ -557,7 +563,7 @@ __global__ void __launch_bounds__(256) k_rp_move(RepArgs R, const uint32_t* sp_r
     const uint64_t L = r_size[r];
     if (L == 0 || R.r_job[r]) continue;
     const uint64_t s = M.blk[r], t = M.blk2[r];
-    if (M.blk[r + 1] - s != L) {  // a kept supernode without a block of its cluster's size
+    if (s == kNoSlot) {  // a kept supernode without a block
       if (lane == 0) atomicExch(err, 1u);
       continue;
     }
@@ -673,6 +679,21 @@ __global__ void k_rp_seeds(RepArgs R, uint32_t c, const double* dist, uint32_t* 
     sv[p] = i < inner ? node : R.master[node - R.n];
     sdist[p] = d;
   }
+}
+
+// slots for supernode rows that have none (new entries): at the pool tail
+__global__ void k_rp_alloc(const uint32_t* jobs, uint32_t nj, const uint64_t* r_size, uint64_t* blk,
+                           unsigned long long* tail) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < nj; j += gridDim.x * blockDim.x) {
+    const uint32_t r = jobs[j];
+    if (blk[r] == kNoSlot) blk[r] = atomicAdd(tail, (unsigned long long)r_size[r]);
+  }
+}
+
+// after a re-layout: rows without a block have no slot
+__global__ void k_rp_unslot(const uint8_t* f_sp, uint32_t all_n, uint64_t* blk) {
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < all_n; r += gridDim.x * blockDim.x)
+    if (!f_sp[r]) blk[r] = kNoSlot;
 }
 
 // A supernode's lists (fianl_build_iter_index_for_mirror,
@@ -1011,11 +1032,58 @@ RepArgs rep_args(sg_ctx* ctx, RepairDev& P) {
   R.m_src = P.m_src; R.m_ret = P.m_ret; R.m_new = P.m_new;
   R.c_src = P.c_src; R.c_upd = P.c_upd; R.c_job = P.c_job; R.c_pend = P.c_pend; R.r_job = P.r_job;
   R.is_cnt = P.is_cnt; R.iv_cnt = P.iv_cnt; R.id_cnt = P.id_cnt;
+  R.slot = P.blk;
   const DevGraph& g = ctx->g;
   R.out_off = g.out.off; R.out_deg = g.out.deg; R.out_col = g.out.col;
   R.in_off = g.in.off; R.in_deg = g.in.deg; R.in_col = g.in.col;
   R.out_w = g.out.w;
   return R;
+}
+
+// A new layout: every supernode row packed in row order (an exclusive scan
+// of the block sizes), with room for new rows; rows that keep their solve
+// move there with their lists, rows solved again only get their slot.
+sg_status rp_relayout(sg_ctx* ctx, RepairDev& P, const RepArgs& R) {
+  cudaStream_t st = ctx->stream;
+  const uint32_t all = P.all_n;
+  SG_TRY(scan_u64(ctx, P.r_size, P.blk2, (uint64_t)all + 1));
+  uint64_t total = 0;
+  SG_TRY(read_u64(ctx, P.blk2 + all, &total));
+  const uint64_t cap = total + total / 2 + 1024;
+  SG_TRY(grow_pool(ctx, &P.pool2, cap));
+  if (P.sssp_on) SG_TRY(grow(ctx, &P.sd2, &P.sd2_cap, P.pool2.cap));
+  MoveArgs M{};
+  M.blk = P.blk;
+  M.blk2 = P.blk2;
+  M.val = P.pool.val; M.del = P.pool.del; M.val2 = P.pool2.val; M.del2 = P.pool2.del;
+  M.is_nbr = P.pool.is_nbr; M.iv_nbr = P.pool.iv_nbr; M.id_nbr = P.pool.id_nbr;
+  M.is_w = P.pool.is_w; M.iv_w = P.pool.iv_w; M.id_w = P.pool.id_w;
+  M.is_nbr2 = P.pool2.is_nbr; M.iv_nbr2 = P.pool2.iv_nbr; M.id_nbr2 = P.pool2.id_nbr;
+  M.is_w2 = P.pool2.is_w; M.iv_w2 = P.pool2.iv_w; M.id_w2 = P.pool2.id_w;
+  k_rp_move<<<grid_for((uint64_t)P.n_sp * 32, 256), 256, 0, st>>>(R, P.sp_rows, P.n_sp, P.r_size, M,
+                                                                  P.d_err);
+  if (P.sssp_on && P.sd) {
+    MoveArgs Ms{};
+    Ms.blk = P.blk;
+    Ms.blk2 = P.blk2;
+    Ms.val = Ms.del = P.sd;
+    Ms.val2 = Ms.del2 = P.sd2;
+    k_rp_move<<<grid_for((uint64_t)P.n_sp * 32, 256), 256, 0, st>>>(R, P.sp_rows, P.n_sp, P.r_size,
+                                                                    Ms, P.d_err);
+  }
+  std::swap(P.blk, P.blk2);
+  std::swap(P.pool, P.pool2);
+  std::swap(P.sd, P.sd2);
+  std::swap(P.sd_cap, P.sd2_cap);
+  k_rp_unslot<<<grid_for(all, 256), 256, 0, st>>>(P.f_sp, all, P.blk);
+  SG_CUDA(ctx, cudaMemcpyAsync(P.d_tail, &total, 8, cudaMemcpyHostToDevice, st));
+  SG_CUDA(ctx, cudaStreamSynchronize(st));
+  count_launch(ctx, 3 + (P.sssp_on ? 1 : 0));
+  SG_CUDA(ctx, cudaGetLastError());
+  P.pool_used = total;
+  P.live_at_layout = total;
+  P.relayouts++;
+  return SG_OK;
 }
 
 // Solves again the supernode rows marked in r_job (r_size holds every row's
@@ -1072,16 +1140,14 @@ sg_status rp_sssp_solve(sg_ctx* ctx, RepairDev& P, uint32_t nj, const uint64_t* 
 }
 
 // Solves again the supernode rows marked in r_job (r_size holds every row's
-// block size) into the next pool layout and moves the other blocks there
-// (the SSSP distance blocks too, once SSSP over the summary has run).
+// block size) into their slots (the SSSP distance blocks too, once SSSP over
+// the summary has run), and writes their lists.
 sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, PhaseTrace& T) {
   cudaStream_t st = ctx->stream;
   const uint32_t all = P.all_n;
-  SG_TRY(scan_u64(ctx, P.r_size, P.blk2, (uint64_t)all + 1));
-  uint64_t total = 0;
-  SG_TRY(read_u64(ctx, P.blk2 + all, &total));
-  SG_TRY(grow_pool(ctx, &P.pool2, total));
-  if (P.sssp_on) SG_TRY(grow(ctx, &P.sd2, &P.sd2_cap, total));
+  // distance blocks once SSSP over the summary starts (every row is solved
+  // again then, so nothing to keep)
+  if (P.sssp_on && P.sd_cap < P.pool.cap) SG_TRY(grow(ctx, &P.sd, &P.sd_cap, P.pool.cap));
   SG_TRY(select_idx(ctx, P.r_job, P.jobs, P.d_num, all));
   SG_TRY(select_idx(ctx, P.f_sp, P.sp_rows, P.d_num + 1, all));
   uint32_t nj_sp[2] = {0, 0};
@@ -1089,6 +1155,16 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   const uint32_t nj = nj_sp[0];
   P.n_sp = nj_sp[1];
+  // Rows keep their blocks; new rows take slots at the pool tail.  A new
+  // layout (every row packed in row order, blocks moved) when the tail could
+  // outgrow the pool or the holes of retired rows reach the live size.
+  if (P.pool_used + (uint64_t)nj * P.max_L > P.pool.cap || P.pool_used > 2 * P.live_at_layout + 1024) {
+    SG_TRY(rp_relayout(ctx, P, R));
+  } else if (nj) {
+    k_rp_alloc<<<grid_for(nj, 256), 256, 0, st>>>(P.jobs, nj, P.r_size, P.blk, P.d_tail);
+    SG_TRY(read_u64(ctx, (const uint64_t*)P.d_tail, &P.pool_used));
+    count_launch(ctx);
+  }
   T.mark("layout and jobs");
   if (nj) {
     k_rp_job_clusters<<<grid_for(nj, 256), 256, 0, st>>>(R, P.jobs, nj);
@@ -1098,7 +1174,7 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
     SG_CUDA(ctx, cudaStreamSynchronize(st));
     uint64_t npos = 0;
     SG_TRY(rp_local_problems(ctx, P, R, ntc, &npos));
-    k_rp_jobs<<<grid_for(nj, 256), 256, 0, st>>>(R, P.jobs, nj, P.tc_idx, P.blk2, P.sp_cl, P.sp_src,
+    k_rp_jobs<<<grid_for(nj, 256), 256, 0, st>>>(R, P.jobs, nj, P.tc_idx, P.blk, P.sp_cl, P.sp_src,
                                                  P.out_off, P.j_half, P.j_warp, P.j_warp5, P.j_block);
     SG_TRY(select_idx(ctx, P.j_warp, P.wjobs, P.d_num, nj));
     SG_TRY(select_idx(ctx, P.j_block, P.bjobs, P.d_num + 1, nj));
@@ -1118,8 +1194,8 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
     A.adj_nbr = P.adj_nbr;
     A.div = P.div;
     A.out_off = P.out_off;
-    A.out_value = P.pool2.val;
-    A.out_delta = P.pool2.del;
+    A.out_value = P.pool.val;
+    A.out_delta = P.pool.del;
     A.damping = (float)ctx->opt.damping;
     A.thr_per_node = ctx->opt.termcheck_threshold / (double)P.n;
     A.lin_off = P.lin_off;
@@ -1149,44 +1225,18 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
     count_launch(ctx, 4);
     T.mark("shortcut kernels", st);
     if (P.sssp_on) {
-      SG_TRY(rp_sssp_solve(ctx, P, nj, P.out_off, P.sd2));
+      SG_TRY(rp_sssp_solve(ctx, P, nj, P.out_off, P.sd));
       T.mark("SSSP shortcut distances", st);
     }
   }
-  MoveArgs M{};
-  M.blk = P.blk;
-  M.blk2 = P.blk2;
-  M.val = P.pool.val; M.del = P.pool.del; M.val2 = P.pool2.val; M.del2 = P.pool2.del;
-  M.is_nbr = P.pool.is_nbr; M.iv_nbr = P.pool.iv_nbr; M.id_nbr = P.pool.id_nbr;
-  M.is_w = P.pool.is_w; M.iv_w = P.pool.iv_w; M.id_w = P.pool.id_w;
-  M.is_nbr2 = P.pool2.is_nbr; M.iv_nbr2 = P.pool2.iv_nbr; M.id_nbr2 = P.pool2.id_nbr;
-  M.is_w2 = P.pool2.is_w; M.iv_w2 = P.pool2.iv_w; M.id_w2 = P.pool2.id_w;
-  k_rp_move<<<grid_for((uint64_t)P.n_sp * 32, 256), 256, 0, st>>>(R, P.sp_rows, P.n_sp, P.r_size, M,
-                                                                  P.d_err);
-  if (P.sssp_on) {
-    MoveArgs Ms{};
-    Ms.blk = P.blk;
-    Ms.blk2 = P.blk2;
-    Ms.val = Ms.del = P.sd;
-    Ms.val2 = Ms.del2 = P.sd2;
-    k_rp_move<<<grid_for((uint64_t)P.n_sp * 32, 256), 256, 0, st>>>(R, P.sp_rows, P.n_sp, P.r_size,
-                                                                    Ms, P.d_err);
-  }
-  count_launch(ctx, 1 + P.sssp_on);
-  SG_CUDA(ctx, cudaGetLastError());
-  std::swap(P.blk, P.blk2);
-  std::swap(P.pool, P.pool2);
-  std::swap(P.sd, P.sd2);
-  std::swap(P.sd_cap, P.sd2_cap);
-  P.pool_used = total;
   P.sk_stale = true;
-  // the lists of the rows solved again, in their new slots
+  // the lists of the rows solved again, in their slots
   if (nj) {
     k_rp_lists<<<grid_for((uint64_t)nj * 32, 256), 256, 0, st>>>(R, P.jobs, nj, P.blk, P.pool);
     count_launch(ctx);
     SG_CUDA(ctx, cudaGetLastError());
   }
-  T.mark("blocks moved", st);
+  T.mark("lists", st);
   (void)D;
   return SG_OK;
 }
@@ -1467,6 +1517,7 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
   P.cap_cntd = nc;
   SG_TRY(dalloc(ctx, &P.d_num, 4));
   SG_TRY(dalloc(ctx, &P.d_err, 1));
+  SG_TRY(dalloc(ctx, &P.d_tail, 1));
   SG_CUDA(ctx, cudaMemsetAsync(P.m_src, 0, n, st));
   SG_CUDA(ctx, cudaMemsetAsync(P.m_ret, 0, n, st));
   SG_CUDA(ctx, cudaMemsetAsync(P.m_new, 0, n, st));
@@ -1477,7 +1528,7 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
   SG_CUDA(ctx, cudaMemsetAsync(P.is_cnt, 0, 4ull * all, st));
   SG_CUDA(ctx, cudaMemsetAsync(P.iv_cnt, 0, 4ull * all, st));
   SG_CUDA(ctx, cudaMemsetAsync(P.id_cnt, 0, 4ull * all, st));
-  SG_CUDA(ctx, cudaMemsetAsync(P.blk, 0, 8ull * (all + 1), st));
+  SG_CUDA(ctx, cudaMemsetAsync(P.blk, 0xFF, 8ull * (all + 1), st));  // no row has a slot yet
   SG_CUDA(ctx, cudaMemsetAsync(P.cnt_a, 0, 8ull * nc, st));
   SG_CUDA(ctx, cudaMemsetAsync(P.cnt_b, 0, 8ull * nc, st));
   SG_CUDA(ctx, cudaMemsetAsync(P.cnt_c, 0, 8ull * nc, st));

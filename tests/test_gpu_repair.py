@@ -132,3 +132,22 @@ def test_device_repair_retires_and_creates_entries():
         ctx.apply_updates(upd)
         assert fixed_point_l1(ctx.pr_inceval(), cur[0], cur[1]) <= TOL_FIXED
         assert_tables_equal(ctx)
+
+
+def test_device_repair_over_many_batches():
+    """Ten batches on one summary: new entries take slots at the pool tail,
+    retired ones leave holes, and the slots are packed again when the tail
+    outgrows the pool; tables equal the host's and PageRank stays within the
+    bound after every batch."""
+    fx = load("planted2600")
+    cur = (fx["row_ptr"], fx["col"], fx["w"])
+    with sg.Context(0, compress=1) as ctx:
+        ctx.load_csr(cur[0], cur[1])
+        ctx.summary_build(fx["clusters"])
+        ctx.pr_peval(out=False)
+        for seed in range(80, 90):
+            upd = oracle.gen_updates(cur[0], cur[1], 150, 150, 0, seed=seed)
+            cur = oracle.apply_updates(*cur, upd)
+            ctx.apply_updates(upd)
+            assert fixed_point_l1(ctx.pr_inceval(), cur[0], cur[1]) <= TOL_FIXED, f"seed {seed}"
+            assert_tables_equal(ctx)
