@@ -121,6 +121,20 @@ struct RepairDev {
   float* div = nullptr;
   uint64_t *cnt_a = nullptr, *cnt_b = nullptr, *cnt_c = nullptr, *cnt_d = nullptr;
   uint64_t *o_lin = nullptr, *o_lout = nullptr, *o_sub = nullptr;  // [ncl + 1]
+  // the cluster-precompute lists' next build (the summary holds the current)
+  struct CmCaps {
+    uint64_t bl_off = 0, bound_list = 0, lin_off = 0, lin_src = 0, lout_off = 0, lout_dst = 0,
+             sub_off = 0, sub_nbr = 0;
+  };
+  struct CmBuf {
+    uint64_t *bl_off = nullptr, *lin_off = nullptr, *lout_off = nullptr, *sub_off = nullptr;
+    uint32_t *bound_list = nullptr, *lout_dst = nullptr, *sub_nbr = nullptr;
+    uint8_t* lin_src = nullptr;
+    CmCaps cap;
+  };
+  CmBuf nx;
+  CmCaps cur;          // capacities of the summary's current arrays (0: unknown)
+  bool cm_built = false;
   uint32_t* d_num = nullptr;    // selected counts
   uint32_t* d_err = nullptr;
   uint64_t cap_lp = 0, cap_div = 0, cap_linoff = 0, cap_cntd = 0, cap_adj = 0, cap_lin = 0;
@@ -816,6 +830,12 @@ struct CmArgs {
   uint64_t *lin_off, *lout_off, *sub_off;         // per member position (+ total)
   uint8_t* lin_src;
   uint32_t *lout_dst, *sub_nbr;
+  // clusters a batch left alone copy their lists from the previous build
+  // (changed == null: every cluster is built)
+  const uint8_t* changed;
+  const uint64_t *old_bl_off, *old_lin_off, *old_lout_off, *old_sub_off;
+  const uint32_t *old_bound_list, *old_lout_dst, *old_sub_nbr;
+  const uint8_t* old_lin_src;
 };
 
 // the subgraph target of member edge v -> t in cluster c (kNone: not in the
@@ -838,6 +858,33 @@ __global__ void __launch_bounds__(256) k_rp_cm(RepArgs R, CmArgs A) {
     const uint32_t m = R.inner[c];
     const uint64_t n0 = R.cn_off[c], p0 = A.cm_off[c];
     const bool small = m <= (uint32_t)kStageCap;
+    if (A.changed && !A.changed[c]) {
+      const uint64_t p1 = p0 + m;
+      if (!FILL) {
+        if (lane == 0) {
+          A.c_bl[c] = A.old_bl_off[c + 1] - A.old_bl_off[c];
+          A.c_lin[c] = A.old_lin_off[p1] - A.old_lin_off[p0];
+          A.c_lout[c] = A.old_lout_off[p1] - A.old_lout_off[p0];
+          A.c_sub[c] = A.old_sub_off[p1] - A.old_sub_off[p0];
+        }
+        continue;
+      }
+      // the previous lists at their new offsets
+      const uint64_t ob = A.old_bl_off[c], nb = A.o_bl[c];
+      for (uint64_t i = lane; i < A.old_bl_off[c + 1] - ob; i += 32) A.bound_list[nb + i] = A.old_bound_list[ob + i];
+      const uint64_t oli = A.old_lin_off[p0], nli = A.o_lin[c];
+      const uint64_t olo = A.old_lout_off[p0], nlo = A.o_lout[c];
+      const uint64_t osu = A.old_sub_off[p0], nsu = A.o_sub[c];
+      for (uint64_t i = lane; i < A.old_lin_off[p1] - oli; i += 32) A.lin_src[nli + i] = A.old_lin_src[oli + i];
+      for (uint64_t i = lane; i < A.old_lout_off[p1] - olo; i += 32) A.lout_dst[nlo + i] = A.old_lout_dst[olo + i];
+      for (uint64_t i = lane; i < A.old_sub_off[p1] - osu; i += 32) A.sub_nbr[nsu + i] = A.old_sub_nbr[osu + i];
+      for (uint32_t i = lane; i < m; i += 32) {
+        A.lin_off[p0 + i] = A.old_lin_off[p0 + i] - oli + nli;
+        A.lout_off[p0 + i] = A.old_lout_off[p0 + i] - olo + nlo;
+        A.sub_off[p0 + i] = A.old_sub_off[p0 + i] - osu + nsu;
+      }
+      continue;
+    }
     if (!FILL) {
       uint64_t nb = 0, nin = 0, nout = 0;
       for (uint32_t i = lane; i < m; i += 32) {
@@ -1285,49 +1332,72 @@ sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, 
     k_rp_ib<true><<<grid_for(D.n_single, 256), 256, 0, st>>>(R, D.ntype, D.l_single, D.n_single,
                                                              nullptr, D.ib_off, D.ib_nbr, ibw);
   PT.mark("ib rows", st);
-  // cluster precompute lists
+  // cluster precompute lists: clusters the batch updated are built again,
+  // the others copy theirs into the new layout (double-buffered: the
+  // summary's arrays are the current build, P.nx the next)
   CmArgs C{};
   C.cm_off = D.cm_off;
   C.c_bl = P.cnt_a;
   C.c_lin = P.cnt_b;
   C.c_lout = P.cnt_c;
   C.c_sub = P.cnt_d;
+  C.changed = P.cm_built ? P.c_upd : nullptr;
+  C.old_bl_off = D.bl_off;
+  C.old_lin_off = D.lin_off;
+  C.old_lout_off = D.lout_off;
+  C.old_sub_off = D.sub_off;
+  C.old_bound_list = D.bound_list;
+  C.old_lin_src = D.lin_src;
+  C.old_lout_dst = D.lout_dst;
+  C.old_sub_nbr = D.sub_nbr;
   const unsigned cg = grid_for((uint64_t)ncl * 32, 256);
   k_rp_cm<false><<<cg, 256, 0, st>>>(R, C);
-  SG_TRY(reserve(ctx, D, &D.bl_off, (uint64_t)ncl + 1));
-  SG_TRY(scan_u64(ctx, P.cnt_a, D.bl_off, (uint64_t)ncl + 1));
+  RepairDev::CmBuf& X = P.nx;
+  SG_TRY(grow(ctx, &X.bl_off, &X.cap.bl_off, (uint64_t)ncl + 1));
+  SG_TRY(scan_u64(ctx, P.cnt_a, X.bl_off, (uint64_t)ncl + 1));
   SG_TRY(scan_u64(ctx, P.cnt_b, P.o_lin, (uint64_t)ncl + 1));
   SG_TRY(scan_u64(ctx, P.cnt_c, P.o_lout, (uint64_t)ncl + 1));
   SG_TRY(scan_u64(ctx, P.cnt_d, P.o_sub, (uint64_t)ncl + 1));
   uint64_t ct[4] = {0, 0, 0, 0};
-  SG_CUDA(ctx, cudaMemcpyAsync(&ct[0], D.bl_off + ncl, 8, cudaMemcpyDeviceToHost, st));
+  SG_CUDA(ctx, cudaMemcpyAsync(&ct[0], X.bl_off + ncl, 8, cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaMemcpyAsync(&ct[1], P.o_lin + ncl, 8, cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaMemcpyAsync(&ct[2], P.o_lout + ncl, 8, cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaMemcpyAsync(&ct[3], P.o_sub + ncl, 8, cudaMemcpyDeviceToHost, st));
   SG_CUDA(ctx, cudaStreamSynchronize(st));
   const uint64_t npos = P.n_members;
-  SG_TRY(reserve(ctx, D, &D.bound_list, ct[0]));
-  SG_TRY(reserve(ctx, D, &D.lin_src, ct[1]));
-  SG_TRY(reserve(ctx, D, &D.lout_dst, ct[2]));
-  SG_TRY(reserve(ctx, D, &D.sub_nbr, ct[3]));
-  SG_TRY(reserve(ctx, D, &D.lin_off, npos + 1));
-  SG_TRY(reserve(ctx, D, &D.lout_off, npos + 1));
-  SG_TRY(reserve(ctx, D, &D.sub_off, npos + 1));
-  C.o_bl = D.bl_off;
+  SG_TRY(grow(ctx, &X.bound_list, &X.cap.bound_list, ct[0]));
+  SG_TRY(grow(ctx, &X.lin_src, &X.cap.lin_src, ct[1]));
+  SG_TRY(grow(ctx, &X.lout_dst, &X.cap.lout_dst, ct[2]));
+  SG_TRY(grow(ctx, &X.sub_nbr, &X.cap.sub_nbr, ct[3]));
+  SG_TRY(grow(ctx, &X.lin_off, &X.cap.lin_off, npos + 1));
+  SG_TRY(grow(ctx, &X.lout_off, &X.cap.lout_off, npos + 1));
+  SG_TRY(grow(ctx, &X.sub_off, &X.cap.sub_off, npos + 1));
+  C.o_bl = X.bl_off;
   C.o_lin = P.o_lin;
   C.o_lout = P.o_lout;
   C.o_sub = P.o_sub;
-  C.bound_list = D.bound_list;
-  C.lin_off = D.lin_off;
-  C.lout_off = D.lout_off;
-  C.sub_off = D.sub_off;
-  C.lin_src = D.lin_src;
-  C.lout_dst = D.lout_dst;
-  C.sub_nbr = D.sub_nbr;
+  C.bound_list = X.bound_list;
+  C.lin_off = X.lin_off;
+  C.lout_off = X.lout_off;
+  C.sub_off = X.sub_off;
+  C.lin_src = X.lin_src;
+  C.lout_dst = X.lout_dst;
+  C.sub_nbr = X.sub_nbr;
   k_rp_cm<true><<<cg, 256, 0, st>>>(R, C);
   k_rp_cm_tail<<<1, 32, 0, st>>>(C, ncl, npos);
+  // the new build becomes the summary's (and the old one the next buffer)
+  std::swap(D.bl_off, X.bl_off);
+  std::swap(D.bound_list, X.bound_list);
+  std::swap(D.lin_off, X.lin_off);
+  std::swap(D.lin_src, X.lin_src);
+  std::swap(D.lout_off, X.lout_off);
+  std::swap(D.lout_dst, X.lout_dst);
+  std::swap(D.sub_off, X.sub_off);
+  std::swap(D.sub_nbr, X.sub_nbr);
+  std::swap(P.cur, X.cap);
+  P.cm_built = true;
   PT.mark("cluster lists", st);
-  count_launch(ctx, 20);
+  count_launch(ctx, 8);
   SG_CUDA(ctx, cudaGetLastError());
   return SG_OK;
 }
@@ -1367,6 +1437,8 @@ void repair_free(SummaryDev& D) {
   dfree(P->adj_nbr); dfree(P->lin_src); dfree(P->div);
   dfree(P->cnt_a); dfree(P->cnt_b); dfree(P->cnt_c); dfree(P->cnt_d);
   dfree(P->o_lin); dfree(P->o_lout); dfree(P->o_sub);
+  dfree(P->nx.bl_off); dfree(P->nx.lin_off); dfree(P->nx.lout_off); dfree(P->nx.sub_off);
+  dfree(P->nx.bound_list); dfree(P->nx.lout_dst); dfree(P->nx.sub_nbr); dfree(P->nx.lin_src);
   dfree(P->d_num); dfree(P->d_err);
   dfree(P->log_src); dfree(P->log_dst); dfree(P->log_kind); dfree(P->log_found); dfree(P->log_w);
   delete P;
