@@ -127,7 +127,12 @@ sg_status sg_ctx_create(int device, const sg_options* opt, sg_ctx** out) {
   }
   ctx->device = device;
   cudaError_t e = cudaSetDevice(device);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  // The context's stream takes the highest priority: the summary repair
+  // runs its shortcut solves on a stream of the lowest priority beside it,
+  // and the table rebuilds queued here are dispatched ahead of them.
+  int least = 0, greatest = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, greatest);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->kev0);

@@ -135,6 +135,12 @@ struct RepairDev {
   CmBuf nx;
   CmCaps cur;          // capacities of the summary's current arrays (0: unknown)
   bool cm_built = false;
+  // the shortcut solves run on a stream of their own, below the context
+  // stream's priority, while the tables are rebuilt on the context stream
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_ready = nullptr, ev_solved = nullptr;
+  uint32_t n_jobs = 0;      // rows solved again by the batch
+  bool solving = false;     // solves launched and not joined yet
   uint32_t* d_num = nullptr;    // selected counts
   uint32_t* d_err = nullptr;
   uint64_t cap_lp = 0, cap_div = 0, cap_linoff = 0, cap_cntd = 0, cap_adj = 0, cap_lin = 0;
@@ -1174,21 +1180,23 @@ sg_status rp_local_problems(sg_ctx* ctx, RepairDev& P, const RepArgs& R, uint32_
 
 // SSSP distances inside the listed jobs' clusters (Bellman-Ford in shared
 // memory, a CTA per job) into out at the jobs' offsets
-sg_status rp_sssp_solve(sg_ctx* ctx, RepairDev& P, uint32_t nj, const uint64_t* out_off, double* out) {
+sg_status rp_sssp_solve(sg_ctx* ctx, RepairDev& P, uint32_t nj, const uint64_t* out_off, double* out,
+                        cudaStream_t st) {
   const size_t smem = (size_t)P.max_L * sizeof(unsigned long long);
   if (smem > 48 * 1024)
     SG_CUDA(ctx, cudaFuncSetAttribute(k_sssp_shortcuts, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-  k_sssp_shortcuts<<<nj, 128, smem, ctx->stream>>>(P.sp_cl, P.sp_src, P.lp_off, P.adj_off, P.adj_nbr,
-                                                   P.adj_w, out_off, out, nj);
+  k_sssp_shortcuts<<<nj, 128, smem, st>>>(P.sp_cl, P.sp_src, P.lp_off, P.adj_off, P.adj_nbr, P.adj_w,
+                                          out_off, out, nj);
   count_launch(ctx);
   SG_CUDA(ctx, cudaGetLastError());
   return SG_OK;
 }
 
-// Solves again the supernode rows marked in r_job (r_size holds every row's
-// block size) into their slots (the SSSP distance blocks too, once SSSP over
-// the summary has run), and writes their lists.
+// Launches the solves of the supernode rows marked in r_job (r_size holds
+// every row's block size) into their slots (the SSSP distance blocks too,
+// once SSSP over the summary has run) on the side stream; rp_join waits for
+// them and writes the rows' lists.
 sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, PhaseTrace& T) {
   cudaStream_t st = ctx->stream;
   const uint32_t all = P.all_n;
@@ -1247,18 +1255,26 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
     A.thr_per_node = ctx->opt.termcheck_threshold / (double)P.n;
     A.lin_off = P.lin_off;
     A.lin_src = P.lin_src;
+    // The side stream starts after the work queued so far; the kernel-class
+    // profiler brackets kernels on the context stream, so the solves stay
+    // there while it is on.
+    cudaStream_t ss = ctx->opt.profile ? st : P.side;
+    if (ss != st) {
+      SG_CUDA(ctx, cudaEventRecord(P.ev_ready, st));
+      SG_CUDA(ctx, cudaStreamWaitEvent(ss, P.ev_ready, 0));
+    }
     kprof_begin(ctx);
     if (nwb[3]) {
       A.jobs = P.hjobs;
-      launch_shortcuts_warp(3, A, nwb[3], st);
+      launch_shortcuts_warp(3, A, nwb[3], ss);
     }
     if (nwb[0]) {
       A.jobs = P.wjobs;
-      launch_shortcuts_warp(2, A, nwb[0], st);
+      launch_shortcuts_warp(2, A, nwb[0], ss);
     }
     if (nwb[2]) {
       A.jobs = P.wjobs5;
-      launch_shortcuts_warp(5, A, nwb[2], st);
+      launch_shortcuts_warp(5, A, nwb[2], ss);
     }
     if (nwb[1]) {
       const size_t smem = shortcut_smem(P.max_L);
@@ -1266,25 +1282,39 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
         SG_CUDA(ctx, cudaFuncSetAttribute(k_shortcuts, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem));
       A.jobs = P.bjobs;
-      k_shortcuts<<<nwb[1], 128, smem, st>>>(A, nwb[1]);
+      k_shortcuts<<<nwb[1], 128, smem, ss>>>(A, nwb[1]);
     }
     kprof_end(ctx, SG_K_SUMMARY);
     count_launch(ctx, 4);
-    T.mark("shortcut kernels", st);
-    if (P.sssp_on) {
-      SG_TRY(rp_sssp_solve(ctx, P, nj, P.out_off, P.sd));
-      T.mark("SSSP shortcut distances", st);
+    SG_CUDA(ctx, cudaGetLastError());
+    if (P.sssp_on) SG_TRY(rp_sssp_solve(ctx, P, nj, P.out_off, P.sd, ss));
+    if (ss != st) {
+      SG_CUDA(ctx, cudaEventRecord(P.ev_solved, ss));
+      P.solving = true;
     }
   }
+  P.n_jobs = nj;
   P.sk_stale = true;
-  // the lists of the rows solved again, in their slots
-  if (nj) {
-    k_rp_lists<<<grid_for((uint64_t)nj * 32, 256), 256, 0, st>>>(R, P.jobs, nj, P.blk, P.pool);
-    count_launch(ctx);
-    SG_CUDA(ctx, cudaGetLastError());
-  }
-  T.mark("lists", st);
   (void)D;
+  (void)R;
+  return SG_OK;
+}
+
+// The context stream waits for the solves launched by rp_shortcuts, then
+// the lists of the rows solved again are written into their slots.
+sg_status rp_join(sg_ctx* ctx, RepairDev& P, const RepArgs& R, PhaseTrace& T) {
+  cudaStream_t st = ctx->stream;
+  if (P.solving) {
+    P.solving = false;
+    SG_CUDA(ctx, cudaStreamWaitEvent(st, P.ev_solved, 0));
+  }
+  const uint32_t nj = P.n_jobs;
+  if (!nj) return SG_OK;
+  T.mark("shortcut solves (the rest after the tables)", st);
+  k_rp_lists<<<grid_for((uint64_t)nj * 32, 256), 256, 0, st>>>(R, P.jobs, nj, P.blk, P.pool);
+  count_launch(ctx);
+  SG_CUDA(ctx, cudaGetLastError());
+  T.mark("lists", st);
   return SG_OK;
 }
 
@@ -1414,11 +1444,29 @@ sg_status rp_finish(sg_ctx* ctx, RepairDev& P, const RepArgs& R) {
   return SG_OK;
 }
 
+// The shortcut solves (side stream) beside the table rebuild (context
+// stream), then the solved rows' lists and the end of the batch; the solves
+// are waited for on every path, so no work of this batch outlives the call.
+sg_status rp_rebuild(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, PhaseTrace& T) {
+  sg_status s = rp_shortcuts(ctx, D, P, R, T);
+  if (s == SG_OK) s = rp_tables(ctx, D, P, R, T);
+  const sg_status j = rp_join(ctx, P, R, T);
+  if (s != SG_OK) return s;
+  if (j != SG_OK) return j;
+  return rp_finish(ctx, P, R);
+}
+
 }  // namespace
 
 void repair_free(SummaryDev& D) {
   RepairDev* P = D.rep;
   if (!P) return;
+  if (P->side) {
+    cudaStreamSynchronize(P->side);
+    cudaStreamDestroy(P->side);
+  }
+  if (P->ev_ready) cudaEventDestroy(P->ev_ready);
+  if (P->ev_solved) cudaEventDestroy(P->ev_solved);
   dfree(P->cl_of); dfree(P->loc); dfree(P->cn_off); dfree(P->cn); dfree(P->inner); dfree(P->n_im);
   dfree(P->master); dfree(P->vim_off); dfree(P->vim); dfree(P->vom_off); dfree(P->vom);
   dfree(P->fc); dfree(P->ob);
@@ -1429,7 +1477,8 @@ void repair_free(SummaryDev& D) {
   dfree(P->blk); dfree(P->blk2); dfree(P->sd); dfree(P->sd2); dfree(P->ib_w); dfree(P->adj_w);
   dfree(P->f_corr); dfree(P->im_list); dfree(P->im_master); dfree(P->src_dist);
   dfree(P->seed_v); dfree(P->seed_n); dfree(P->seed_d);
-  dfree(P->pool.val); dfree(P->pool.del); dfree(P->pool2.val); dfree(P->pool2.del);
+  free_pool(&P->pool); free_pool(&P->pool2);
+  dfree(P->is_cnt); dfree(P->iv_cnt); dfree(P->id_cnt); dfree(P->row_inner); dfree(P->d_tail);
   dfree(P->jobs); dfree(P->tcl); dfree(P->tc_idx); dfree(P->tc_inner); dfree(P->sp_cl);
   dfree(P->sp_src); dfree(P->wjobs); dfree(P->bjobs); dfree(P->j_warp); dfree(P->j_block);
   dfree(P->wjobs5); dfree(P->j_warp5); dfree(P->hjobs); dfree(P->j_half);
@@ -1453,6 +1502,13 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
   D.rep = Pp;
   RepairDev& P = *Pp;
   cudaStream_t st = ctx->stream;
+  {
+    int least = 0, greatest = 0;
+    SG_CUDA(ctx, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    SG_CUDA(ctx, cudaStreamCreateWithPriority(&P.side, cudaStreamNonBlocking, least));
+    SG_CUDA(ctx, cudaEventCreateWithFlags(&P.ev_ready, cudaEventDisableTiming));
+    SG_CUDA(ctx, cudaEventCreateWithFlags(&P.ev_solved, cudaEventDisableTiming));
+  }
   const uint32_t n = S.old_n, all = S.all_n, ncl = (uint32_t)S.supernode_ids.size();
   P.n = n;
   P.all_n = all;
@@ -1614,9 +1670,7 @@ sg_status repair_init(sg_ctx* ctx, SummaryDev& D) {
   k_rp_rows<<<grid_for(all, 256), 256, 0, st>>>(R, P.r_size, P.f_sp, D.out_deg_all);
   count_launch(ctx);
   PhaseTrace T("device summary build");
-  SG_TRY(rp_shortcuts(ctx, D, P, R, T));
-  SG_TRY(rp_tables(ctx, D, P, R, T));
-  return rp_finish(ctx, P, R);
+  return rp_rebuild(ctx, D, P, R, T);
 }
 
 sg_status repair_after_apply(sg_ctx* ctx, SummaryDev& D) {
@@ -1654,9 +1708,7 @@ sg_status repair_after_apply(sg_ctx* ctx, SummaryDev& D) {
   k_rp_rows<<<grid_for(P.all_n, 256), 256, 0, st>>>(R, P.r_size, P.f_sp, D.out_deg_all);
   count_launch(ctx, 3);
   T.mark("entries, exits, rows", st);
-  SG_TRY(rp_shortcuts(ctx, D, P, R, T));
-  SG_TRY(rp_tables(ctx, D, P, R, T));
-  const sg_status fs = rp_finish(ctx, P, R);
+  const sg_status fs = rp_rebuild(ctx, D, P, R, T);
   T.mark("finish");
   return fs;
 }
@@ -1780,9 +1832,7 @@ sg_status repair_sssp_refresh(sg_ctx* ctx, SummaryDev& D) {
     SG_TRY(reserve(ctx, D, &D.out_deg_all, P.all_n));
     k_rp_rows<<<grid_for(P.all_n, 256), 256, 0, st>>>(R, P.r_size, P.f_sp, D.out_deg_all);
     count_launch(ctx);
-    SG_TRY(rp_shortcuts(ctx, D, P, R, T));
-    SG_TRY(rp_tables(ctx, D, P, R, T));
-    SG_TRY(rp_finish(ctx, P, R));
+    SG_TRY(rp_rebuild(ctx, D, P, R, T));
   }
   if (P.sk_stale) SG_TRY(rp_sketch(ctx, D, P, R));
   T.mark("summarized CSR", st);
@@ -1816,7 +1866,7 @@ sg_status repair_source_seeds(sg_ctx* ctx, SummaryDev& D, uint32_t source, const
   SG_CUDA(ctx, cudaMemcpyAsync(P.sp_cl, &zero, 4, cudaMemcpyHostToDevice, st));
   SG_CUDA(ctx, cudaMemcpyAsync(P.sp_src, &loc, 4, cudaMemcpyHostToDevice, st));
   SG_CUDA(ctx, cudaMemcpyAsync(P.out_off, &zero64, 8, cudaMemcpyHostToDevice, st));
-  SG_TRY(rp_sssp_solve(ctx, P, 1, P.out_off, P.src_dist));
+  SG_TRY(rp_sssp_solve(ctx, P, 1, P.out_off, P.src_dist, ctx->stream));
   SG_CUDA(ctx, cudaMemsetAsync(P.seed_n, 0, 4, st));
   k_rp_seeds<<<1, 256, 0, st>>>(R, c, P.src_dist, P.seed_v, P.seed_d, P.seed_n);
   count_launch(ctx);
