@@ -1349,6 +1349,7 @@ sg_status rp_tables(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& R, 
   SG_TRY(scan_u64(ctx, P.cnt_d, D.ib_off, (uint64_t)all + 1));
   uint64_t nib = 0;
   SG_TRY(read_u64(ctx, D.ib_off + all, &nib));
+  D.n_ib = nib;
   SG_TRY(reserve(ctx, D, &D.ib_nbr, nib));
   float* ibw = nullptr;
   if (R.out_w) {

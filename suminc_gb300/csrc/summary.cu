@@ -865,97 +865,119 @@ __device__ __forceinline__ bool rounds_done(const SumArgs& A) {
 }
 
 // mass a (mirror) entry receives goes along its shortcuts into exit buffers
-__device__ __forceinline__ void entry_push(const SumArgs& A, uint32_t u, float d, uint32_t lane,
+// The round kernels give each listed row a group of G lanes (G divides 32):
+// a supernode's shortcut list and an exit's boundary edges hold a few
+// entries each, so several rows per warp keep more of their dependent
+// loads and atomics in flight than one row per warp.
+template <uint32_t G>
+__device__ __forceinline__ unsigned group_mask() {
+  if (G == 32) return 0xffffffffu;
+  return ((1u << (G & 31)) - 1u) << ((threadIdx.x & 31) & ~(G - 1));
+}
+
+template <uint32_t G>
+__device__ __forceinline__ void entry_push(const SumArgs& A, uint32_t u, float d, uint32_t gl,
                                            unsigned long long& sc) {
   const uint64_t b = A.L.slot[u], e1 = b + A.L.is_cnt[u];
-  for (uint64_t e = b + lane; e < e1; e += 32) atomicAdd(&A.bound[A.L.is_nbr[e]], A.L.is_w[e] * d);
-  if (lane == 0) {
+  for (uint64_t e = b + gl; e < e1; e += G) atomicAdd(&A.bound[A.L.is_nbr[e]], A.L.is_w[e] * d);
+  if (gl == 0) {
     atomicAdd(&A.spnode[u], d);
     sc += e1 - b;
   }
 }
 
+// the warp's sum of v into *dst (every lane of the warp calls it)
+__device__ __forceinline__ void warp_add_to(unsigned long long* dst, unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
+}
+
+template <uint32_t G>
 __global__ void __launch_bounds__(256) k_sum_entries(SumArgs A, const uint32_t* list, uint32_t cnt) {
   if (rounds_done(A)) return;
-  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t gl = threadIdx.x & (G - 1);
+  const unsigned gm = group_mask<G>();
   unsigned long long sc = 0;
-  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt;
-       i += (gridDim.x * blockDim.x) >> 5) {
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / G; i < cnt;
+       i += (gridDim.x * blockDim.x) / G) {
     const uint32_t u = list[i];
     float d = 0.f;
-    if (lane == 0) {
+    if (gl == 0) {
       d = A.delta[u];
       d = fabsf(d) > A.thr_v ? atomicExch(&A.delta[u], 0.f) : 0.f;
     }
-    d = __shfl_sync(0xffffffffu, d, 0);
-    if (d != 0.f) entry_push(A, u, d, lane, sc);
+    d = __shfl_sync(gm, d, 0, G);
+    if (d != 0.f) entry_push<G>(A, u, d, gl, sc);
   }
-  if (lane == 0 && sc) atomicAdd(&A.cnt[1], sc);
+  warp_add_to(&A.cnt[1], sc);
 }
 
+template <uint32_t G>
 __global__ void __launch_bounds__(256) k_sum_exits(SumArgs A, const uint32_t* list, uint32_t cnt) {
   if (rounds_done(A)) return;
-  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t gl = threadIdx.x & (G - 1);
+  const unsigned gm = group_mask<G>();
   unsigned long long ed = 0, sc = 0;
-  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt;
-       i += (gridDim.x * blockDim.x) >> 5) {
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / G; i < cnt;
+       i += (gridDim.x * blockDim.x) / G) {
     const uint32_t u = list[i];
     float b = 0.f;
-    if (lane == 0) {
+    if (gl == 0) {
       b = A.bound[u];
       b = fabsf(b) > A.thr_v ? atomicExch(&A.bound[u], 0.f) : 0.f;
       if (b != 0.f) A.x[u] += b;
     }
-    b = __shfl_sync(0xffffffffu, b, 0);
+    b = __shfl_sync(gm, b, 0, G);
     if (b == 0.f) continue;
     // boundary edges with the original out-degree (g_function, pagerank_ingress.h:75-99)
     const float outv = b * A.damping / (float)A.out_deg_all[u];
-    for (uint64_t e = A.ib_off[u] + lane; e < A.ib_off[u + 1]; e += 32)
+    for (uint64_t e = A.ib_off[u] + gl; e < A.ib_off[u + 1]; e += G)
       atomicAdd(&A.delta[A.ib_nbr[e]], outv);
-    if (lane == 0) ed += A.ib_off[u + 1] - A.ib_off[u];
+    if (gl == 0) ed += A.ib_off[u + 1] - A.ib_off[u];
     // a master forwards to its in-mirrors, which push at once
     const uint8_t t = A.ntype[u];
     if (t == kOutMaster || t == kBothOutInMaster) {
       for (uint64_t s = A.sync_off[u]; s < A.sync_off[u + 1]; ++s) {
         const uint32_t mm = A.sync_nbr[s];
         float dm = 0.f;
-        if (lane == 0) {
+        if (gl == 0) {
           atomicAdd(&A.delta[mm], b);
           dm = atomicExch(&A.delta[mm], 0.f);
         }
-        dm = __shfl_sync(0xffffffffu, dm, 0);
-        if (dm != 0.f) entry_push(A, mm, dm, lane, sc);
+        dm = __shfl_sync(gm, dm, 0, G);
+        if (dm != 0.f) entry_push<G>(A, mm, dm, gl, sc);
       }
     }
   }
-  if (lane == 0) {
-    if (ed) atomicAdd(&A.cnt[0], ed);
-    if (sc) atomicAdd(&A.cnt[1], sc);
-  }
+  warp_add_to(&A.cnt[0], ed);
+  warp_add_to(&A.cnt[1], sc);
 }
 
+template <uint32_t G>
 __global__ void __launch_bounds__(256) k_sum_singles(SumArgs A, const uint32_t* list, uint32_t cnt) {
   if (rounds_done(A)) return;
-  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t gl = threadIdx.x & (G - 1);
+  const unsigned gm = group_mask<G>();
   unsigned long long ed = 0;
-  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < cnt;
-       i += (gridDim.x * blockDim.x) >> 5) {
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) / G; i < cnt;
+       i += (gridDim.x * blockDim.x) / G) {
     const uint32_t u = list[i];
     float d = 0.f;
-    if (lane == 0) {
+    if (gl == 0) {
       d = A.delta[u];
       d = fabsf(d) > A.thr_v ? atomicExch(&A.delta[u], 0.f) : 0.f;
       if (d != 0.f) A.x[u] += d;
     }
-    d = __shfl_sync(0xffffffffu, d, 0);
+    d = __shfl_sync(gm, d, 0, G);
     if (d == 0.f) continue;
     const uint64_t e0 = A.ib_off[u], e1 = A.ib_off[u + 1];
     if (e1 == e0) continue;
     const float outv = d * A.damping / (float)(e1 - e0);
-    for (uint64_t e = e0 + lane; e < e1; e += 32) atomicAdd(&A.delta[A.ib_nbr[e]], outv);
-    if (lane == 0) ed += e1 - e0;
+    for (uint64_t e = e0 + gl; e < e1; e += G) atomicAdd(&A.delta[A.ib_nbr[e]], outv);
+    if (gl == 0) ed += e1 - e0;
   }
-  if (lane == 0 && ed) atomicAdd(&A.cnt[0], ed);
+  warp_add_to(&A.cnt[0], ed);
 }
 
 __global__ void k_sum_omirror(SumArgs A, const uint32_t* list, const uint32_t* master, uint32_t cnt) {
@@ -1129,7 +1151,7 @@ __global__ void __launch_bounds__(256) k_sum_bound_push(SumArgs A, const uint32_
           dm = atomicExch(&A.delta[mm], 0.f);
         }
         dm = __shfl_sync(0xffffffffu, dm, 0);
-        if (dm != 0.f) entry_push(A, mm, dm, lane, sc);
+        if (dm != 0.f) entry_push<32>(A, mm, dm, lane, sc);
       }
     }
   }
@@ -1227,14 +1249,33 @@ static sg_status summarized_rounds(sg_ctx* ctx, SummaryDev& D, unsigned long lon
   SG_CUDA(ctx, cudaMemsetAsync(D.sctl, 0, 4 * sizeof(uint32_t), st));
   SG_CUDA(ctx, cudaMemsetAsync(D.d_res, 0, 2 * sizeof(double), st));
   const unsigned rblocks = grid_for(D.old_n, 256, ctx->num_sms * 4);
+  // lanes per row: shortcut lists hold at most a cluster's nodes (a few on
+  // average); boundary rows get a short group while they average a few edges
+  constexpr uint32_t kEntryLanes = 8, kShortLanes = 8;
+  const bool short_ib = D.n_ib <= (uint64_t)kShortLanes * ((uint64_t)D.n_exit + D.n_single);
   uint32_t h_ctl[4] = {0, 0, 0, 0};
   int launched = 0;
   while (launched < cap) {
     for (int c = 0; c < 4 && launched < cap; ++c, ++launched) {
       kprof_begin(ctx);
-      if (D.n_entry) k_sum_entries<<<grid_for((uint64_t)D.n_entry * 32, 256), 256, 0, st>>>(A, D.l_entry, D.n_entry);
-      if (D.n_exit) k_sum_exits<<<grid_for((uint64_t)D.n_exit * 32, 256), 256, 0, st>>>(A, D.l_exit, D.n_exit);
-      if (D.n_single) k_sum_singles<<<grid_for((uint64_t)D.n_single * 32, 256), 256, 0, st>>>(A, D.l_single, D.n_single);
+      if (D.n_entry)
+        k_sum_entries<kEntryLanes><<<grid_for((uint64_t)D.n_entry * kEntryLanes, 256), 256, 0, st>>>(
+            A, D.l_entry, D.n_entry);
+      if (D.n_exit) {
+        if (short_ib)
+          k_sum_exits<kShortLanes><<<grid_for((uint64_t)D.n_exit * kShortLanes, 256), 256, 0, st>>>(
+              A, D.l_exit, D.n_exit);
+        else
+          k_sum_exits<32><<<grid_for((uint64_t)D.n_exit * 32, 256), 256, 0, st>>>(A, D.l_exit, D.n_exit);
+      }
+      if (D.n_single) {
+        if (short_ib)
+          k_sum_singles<kShortLanes><<<grid_for((uint64_t)D.n_single * kShortLanes, 256), 256, 0, st>>>(
+              A, D.l_single, D.n_single);
+        else
+          k_sum_singles<32><<<grid_for((uint64_t)D.n_single * 32, 256), 256, 0, st>>>(A, D.l_single,
+                                                                                    D.n_single);
+      }
       if (D.n_omirror) k_sum_omirror<<<grid_for(D.n_omirror, 256), 256, 0, st>>>(A, D.l_omirror, D.omirror_master, D.n_omirror);
       k_sum_residual_decide<<<rblocks, 256, 0, st>>>(A, D.old_n);
       kprof_end(ctx, SG_K_SUMMARY);

@@ -139,6 +139,7 @@ struct SummaryDev {
   uint32_t* out_deg_all = nullptr;       // out-degree of each row (mirrors: master's)
   uint32_t *l_entry = nullptr, *l_exit = nullptr, *l_single = nullptr, *l_omirror = nullptr;
   uint32_t n_entry = 0, n_exit = 0, n_single = 0, n_omirror = 0;
+  uint64_t n_ib = 0;                     // boundary edges of the exit and single rows
   uint32_t* omirror_master = nullptr;
   uint8_t* ntype = nullptr;
   // cluster precompute: members (cm layout: clusters in order) and, per
