@@ -390,13 +390,16 @@ __global__ void __launch_bounds__(256) k_shortcuts_warp(ShortcutArgs A, uint32_t
     __syncwarp();
   }
 }
+// One block per batch of jobs (no grid cap): blocks live for one solve, so
+// SM slots free up all along the launch for kernels queued beside it.
 void launch_shortcuts_warp(int npl, ShortcutArgs A, uint32_t njobs, cudaStream_t st) {
+  constexpr int kNoCap = 1 << 30;
   if (npl == 3) {
-    k_shortcuts_warp<3, 16><<<grid_for((uint64_t)njobs * 16, 32 * kStageWarps), 32 * kStageWarps, 0,
-                              st>>>(A, njobs);
+    k_shortcuts_warp<3, 16><<<grid_for((uint64_t)njobs * 16, 32 * kStageWarps, kNoCap), 32 * kStageWarps,
+                              0, st>>>(A, njobs);
     return;
   }
-  const unsigned grid = grid_for((uint64_t)njobs * 32, 32 * kStageWarps);
+  const unsigned grid = grid_for((uint64_t)njobs * 32, 32 * kStageWarps, kNoCap);
   if (npl == 2) k_shortcuts_warp<2, 32><<<grid, 32 * kStageWarps, 0, st>>>(A, njobs);
   else k_shortcuts_warp<5, 32><<<grid, 32 * kStageWarps, 0, st>>>(A, njobs);
 }
@@ -1251,7 +1254,7 @@ static sg_status summarized_rounds(sg_ctx* ctx, SummaryDev& D, unsigned long lon
   const unsigned rblocks = grid_for(D.old_n, 256, ctx->num_sms * 4);
   // lanes per row: shortcut lists hold at most a cluster's nodes (a few on
   // average); boundary rows get a short group while they average a few edges
-  constexpr uint32_t kEntryLanes = 8, kShortLanes = 8;
+  constexpr uint32_t kEntryLanes = 4, kShortLanes = 4;
   const bool short_ib = D.n_ib <= (uint64_t)kShortLanes * ((uint64_t)D.n_exit + D.n_single);
   uint32_t h_ctl[4] = {0, 0, 0, 0};
   int launched = 0;
