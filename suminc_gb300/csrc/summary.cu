@@ -1302,7 +1302,7 @@ static sg_status summarized_rounds(sg_ctx* ctx, SummaryDev& D, unsigned long lon
 // mirror and every vertex of type 0 (single), and no batch can add one (the
 // incremental repair works on the kept clusters): its summarized rounds are
 // the plain Ingress rounds over the whole graph.  Such a summary runs the
-// plain path (the dense pull), and its batches skip the host repair.
+// plain path (the dense pull), and its batches skip the repair.
 bool summary_no_supernodes(sg_ctx* ctx) {
   SummaryDev* D = sdev(ctx);
   return D && D->valid && D->S.supernode_ids.empty();
