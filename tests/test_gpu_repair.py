@@ -151,3 +151,22 @@ def test_device_repair_over_many_batches():
             ctx.apply_updates(upd)
             assert fixed_point_l1(ctx.pr_inceval(), cur[0], cur[1]) <= TOL_FIXED, f"seed {seed}"
             assert_tables_equal(ctx)
+
+
+def test_device_repair_under_kernel_profiler():
+    """With the kernel-class profiler on, the shortcut solves stay on the
+    context's stream (no side stream); the repaired tables are the same."""
+    fx = load("planted2600")
+    cur = (fx["row_ptr"], fx["col"], fx["w"])
+    with sg.Context(0, compress=1) as ctx:
+        ctx.load_csr(cur[0], cur[1])
+        ctx.summary_build(fx["clusters"])
+        ctx.pr_peval(out=False)
+        for seed, prof in ((61, 0xFF), (62, 0), (63, 0xFF)):
+            ctx.set_profile(prof)
+            upd = oracle.gen_updates(cur[0], cur[1], 150, 150, 0, seed=seed)
+            cur = oracle.apply_updates(*cur, upd)
+            ctx.apply_updates(upd)
+            assert fixed_point_l1(ctx.pr_inceval(), cur[0], cur[1]) <= TOL_FIXED, f"seed {seed}"
+            assert_tables_equal(ctx)
+        ctx.set_profile(0)
