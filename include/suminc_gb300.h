@@ -418,11 +418,12 @@ sg_status sg_adjoint_values(sg_ctx* ctx, float* x, float* lambda);
  * fixed file-scope device array of SG_PR_NOALLOC_MAX_VERTICES entries that
  * every GPU loading the library keeps until the process exits; n above that
  * returns SG_ERR_TOO_LARGE.  The first call on each device looks up the
- * array's device address (cudaGetSymbolAddress) with that device current,
- * so make that first call before any stream capture.  Every call shares the
- * array: calls whose work overlaps on the GPU race and must be serialised
- * by the caller.  Each round ends by reading two control words back to the
- * host, which synchronises `stream`.  A CUDA error still pending from the
+ * array's device address (cudaGetSymbolAddress) with that device current.
+ * Every call shares the array: calls whose work overlaps on the GPU race
+ * and must be serialised by the caller.  Each round ends by reading two
+ * control words back to the host, which synchronises `stream` once per
+ * round, so no call can run under stream capture or inside a CUDA graph.
+ * A CUDA error still pending from the
  * caller's own work makes the call return SG_ERR_CUDA before it launches
  * anything, and that error is left for the caller to collect.  Returns
  * SG_ERR_NOT_CONVERGED when max_rounds is reached. */
