@@ -412,6 +412,8 @@ struct SpLists {
   const uint32_t *is_nbr = nullptr, *iv_nbr = nullptr, *id_nbr = nullptr;
   const float *is_w = nullptr, *iv_w = nullptr, *id_w = nullptr;
   uint64_t pool = 0;  // entries of the slot arrays in use
+  const uint32_t* sp_rows = nullptr;  // the supernode rows, in row order
+  uint32_t n_sp = 0;
 };
 
 struct PullView {

@@ -1747,6 +1747,8 @@ SpLists repair_lists(const SummaryDev& D) {
   L.iv_w = P->pool.iv_w;
   L.id_w = P->pool.id_w;
   L.pool = P->pool_used;
+  L.sp_rows = P->sp_rows;
+  L.n_sp = P->n_sp;
   return L;
 }
 

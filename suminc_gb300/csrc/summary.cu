@@ -1018,12 +1018,13 @@ __global__ void __launch_bounds__(256) k_sum_residual_decide(SumArgs A, uint32_t
   }
 }
 
-// correction through inner_delta / inner_value (warp per row)
-__global__ void __launch_bounds__(256) k_sum_correct(SumArgs A, uint32_t all_n) {
+// correction through inner_delta / inner_value, a warp per supernode row
+// (the other rows hold no correction lists)
+__global__ void __launch_bounds__(256) k_sum_correct(SumArgs A) {
   const uint32_t lane = threadIdx.x & 31;
-  for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < all_n;
-       u += (gridDim.x * blockDim.x) >> 5) {
-    if (!A.L.row_sp[u]) continue;
+  for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < A.L.n_sp;
+       i += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t u = A.L.sp_rows[i];
     const float d = A.spnode[u];
     if (!(fabsf(d) * (float)A.L.row_inner[u] > A.thr_v)) continue;
     const uint64_t b = A.L.slot[u];
@@ -1290,7 +1291,7 @@ static sg_status summarized_rounds(sg_ctx* ctx, SummaryDev& D, unsigned long lon
     if (h_ctl[0]) break;
   }
   const int r = (int)h_ctl[2];
-  k_sum_correct<<<grid_for((uint64_t)D.all_n * 32, 256), 256, 0, st>>>(A, D.all_n);
+  if (A.L.n_sp) k_sum_correct<<<grid_for((uint64_t)A.L.n_sp * 32, 256), 256, 0, st>>>(A);
   count_launch(ctx);
   SG_CUDA(ctx, cudaGetLastError());
   SG_CUDA(ctx, cudaStreamSynchronize(st));
