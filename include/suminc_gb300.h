@@ -5,7 +5,11 @@
  * Conventions
  *   - Every entry point returns an sg_status; no C++ exception crosses it.
  *   - Host pointers are caller-owned and copied (or written) before return.
- *   - Device memory is owned by the context; one CUDA stream per context.
+ *   - Device memory is owned by the context; one CUDA stream per context,
+ *     created at the device's highest stream priority.  The summary repair
+ *     after a batch also runs its shortcut solves on a second stream of the
+ *     lowest priority, ordered against the context's stream by events; both
+ *     have finished when the call returns.
  *   - A context must not be used by two host threads at once; distinct
  *     contexts are independent.
  *   - Vertex ids are dense 0..n-1 ("vid = rank of oid" as in the reference's
@@ -135,7 +139,9 @@ sg_status sg_ctx_destroy(sg_ctx* ctx);
 /* Message of the last failing call on this context (never NULL). */
 const char* sg_last_error(const sg_ctx* ctx);
 
-/* Runs subsequent work of this context on `stream` (a cudaStream_t). */
+/* Runs subsequent work of this context on `stream` (a cudaStream_t); its
+ * priority is the caller's.  The summary repair's solve stream still waits
+ * for the work queued on it and is waited for by it, through events. */
 sg_status sg_ctx_set_stream(sg_ctx* ctx, void* stream);
 sg_status sg_get_stats(const sg_ctx* ctx, sg_stats* out);
 

@@ -1296,7 +1296,6 @@ sg_status rp_shortcuts(sg_ctx* ctx, SummaryDev& D, RepairDev& P, const RepArgs& 
   P.n_jobs = nj;
   P.sk_stale = true;
   (void)D;
-  (void)R;
   return SG_OK;
 }
 
